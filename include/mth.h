@@ -1,0 +1,181 @@
+/*
+ * mth.h -- C-ABI of the GB300 EVPFFT / sparse phase-field solve.
+ *
+ * The reference (M-THEMES, `forge`) has no plugin layer: `main` calls
+ * `SetupJob()`, `Evolution()` and `DestroyJob()` over global state
+ * (src/evp.c:18-25, src/evp.h:595-615).  This header replaces that trio with
+ * a context object; every entry point returns an `mth_status` instead of
+ * aborting (the reference calls `PError` -> `MPI_Abort`, src/evp.h:62-63).
+ *
+ * Plain C types only: no CUDA or torch types cross this boundary.  All host
+ * buffers belong to the caller and are never retained after a call returns.
+ * One context per host thread; contexts are independent.
+ */
+#ifndef MTH_H
+#define MTH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MTH_NSYS_MAX 12   /* NSYSMX, src/evpFlags.h:5 */
+#define MTH_NPH_MAX 2     /* NPHMAX, src/evpFlags.h:4 */
+
+typedef enum {
+  MTH_OK = 0,
+  MTH_ERR_ARG = 1,          /* bad argument or inconsistent input */
+  MTH_ERR_CUDA = 2,         /* CUDA runtime error (message in mth_last_error) */
+  MTH_ERR_NOMEM = 3,        /* device or host allocation failed */
+  MTH_ERR_SINGULAR = 4,     /* singular matrix (reference: exit(35), src/kinematics.c:306-313) */
+  MTH_ERR_NOT_CONVERGED = 5,/* local Newton hit its iteration cap in some voxel */
+  MTH_ERR_IO = 6,           /* input file missing or malformed */
+  MTH_ERR_STATE = 7,        /* call out of order (e.g. step before upload) */
+  MTH_ERR_TIMEOUT = 8,      /* a bounded device wait gave up */
+  MTH_ERR_NAN = 9,          /* non-finite value in a field or a report */
+  MTH_ERR_UNSUPPORTED = 10  /* grid size / option not supported by this build */
+} mth_status;
+
+typedef enum {
+  MTH_FP64 = 0,   /* all fields, FFTs and the local Newton in FP64 */
+  MTH_MIXED = 1   /* FP32 fields/FFT/Green operator, FP64 local Newton solve and reductions */
+} mth_precision;
+
+/* One phase: elastic constants plus the active slip mode of its .sx file
+ * (src/init.c:52-231).  Slip normals/directions are given as read (not
+ * normalised); the library normalises them as PlasticInit does. */
+typedef struct {
+  int    type;               /* Type_phases: 0 crystal, 1 gas */
+  double c11, c12, c44;      /* MPa (ElastConst_Phase*, src/io.c:42-43) */
+  int    nsys;               /* nsmx */
+  double bn[MTH_NSYS_MAX][3];/* slip-plane normals */
+  double bb[MTH_NSYS_MAX][3];/* slip directions */
+  double nrs;                /* rate-sensitivity exponent n */
+  double gamd0;              /* reference shear rate, 1/s */
+  double tau0f, tau0b;       /* initial CRSS, forward/backward, MPa */
+  double tau1, thet0, thet1; /* Voce parameters, MPa */
+  double hself, hlat;        /* self/latent hardening ratios */
+} mth_phase;
+
+/* Run parameters: the subset of the reference namelist (src/io.c:25-94) that
+ * drives the EVPFFT solve, plus the phase-field/DRX block. */
+typedef struct {
+  int    cell_dim[3];        /* CellDim */
+  int    n_phases;           /* N_phases */
+  mth_phase phase[MTH_NPH_MAX];
+  double time_step;          /* TimeStep [s] */
+  int    n_steps;            /* N_steps */
+  double err;                /* Err: Green-iteration tolerance */
+  int    iter_max;           /* IterMax */
+  int    velgrad_bc_flag[6]; /* VelGrad_BC_Flag (Voigt 11,22,33,23,13,12) */
+  double velgrad_bc[6];      /* VelGrad_BC */
+  int    stress_bc_flag[6];  /* Stress_BC_Flag */
+  double stress_bc[6];       /* Stress_BC */
+  int    elast_bc;           /* ElastBC: 0 -> Gamma(k=0) = -S0, 1 -> 0 */
+  int    update_flag;        /* Update_Flag: texture update */
+  int    hard_flag;          /* Hard_Flag: Voce hardening */
+  int    precision;          /* mth_precision */
+  double newton_tol;         /* local Newton tolerance; <=0 selects the default
+                                (1e-10 FP64 as in src/evolution.c:104, 1e-7 mixed) */
+  int    newton_itmax;       /* <=0 selects 500 (src/evolution.c:105) */
+  /* Phase-field / DRX block (src/io.c:71-90) */
+  double pf_length_scale;    /* dx [m] */
+  double pf_time_step;       /* dt of one PF substep [s] */
+  double e_gb;               /* GB energy [J/m^2] */
+  double m_gb;               /* GB mobility [m^4/(J s)] */
+  double pf_width_cells;     /* L_gb / dx; the reference hard-codes 3 (src/pf_xrx.c:1493) */
+  double stored_energy_scale;/* Scale_Fdeform (alpha in PF_XRX) */
+  double shear_modulus;      /* mu in the stored energy alpha*mu*b^2 [GPa] */
+  double burgers;            /* b [nm] */
+  int    nucleus_radius;     /* cells */
+  double rho_nucleation;     /* nucleation threshold on rho_tot [1e12/m^2] */
+  double rho0;               /* initial dislocation density [1e12/m^2] */
+  double rho_k;              /* rho = rho0 + rho_k * accumulated slip [1e12/m^2] */
+  int    pf_substeps;        /* PF substeps per mechanical step */
+  uint64_t seed;             /* counter-based RNG seed */
+} mth_params;
+
+/* Per-step record; the reference prints the scalars to vm.out
+ * (src/evolution.c:1621-1625) and keeps the tensors in globals. */
+typedef struct {
+  int    step;
+  int    iterations;         /* Green iterations taken */
+  double time;               /* TimeTot */
+  double sig_avg[3][3];      /* <sigma> (SigAvg) */
+  double sig_avg_ph1[3][3];  /* <sigma> over phase 1 (SigAvg1) */
+  double disgrad_avg[3][3];  /* <grad u> actual (DisGradAvg_actual) */
+  double eps_avg[3][3];      /* <eps^p> (EpsAvg) */
+  double edot_avg[3][3];     /* <edot^p> (EdotAvg) */
+  double e_vm, evmp, d_vm, dvmp, s_vm, s_vm1;
+  double err_s, err_e;       /* final normalised errors */
+  long long newton_iters;    /* local Newton iterations summed over voxels and Green iterations */
+  long long newton_failed;   /* voxel solves that hit the iteration cap */
+  int    n_new_grains;       /* DRX nuclei seeded this step */
+} mth_step_report;
+
+typedef enum {
+  MTH_FIELD_SIG = 0,      /* 9 doubles/voxel, Cauchy stress (3x3 row-major) */
+  MTH_FIELD_EPS = 1,      /* 9: plastic strain */
+  MTH_FIELD_EDOT = 2,     /* 9: plastic strain rate */
+  MTH_FIELD_STRAIN = 3,   /* 9: sym(grad u) */
+  MTH_FIELD_ROT = 4,      /* 9: crystal->sample transformation (TranMat_xt2sa) */
+  MTH_FIELD_CRSS = 5,     /* 12: forward CRSS per slip system */
+  MTH_FIELD_GAMACUM = 6,  /* 1: accumulated shear */
+  MTH_FIELD_GRAIN = 7,    /* 1: grain id (as double) */
+  MTH_FIELD_RHO = 8       /* 1: total dislocation density */
+} mth_field;
+
+/* Library */
+const char* mth_version(void);
+const char* mth_last_error(void);   /* thread-local message of the last failure */
+
+/* Context lifecycle: replaces SetupJob/Evolution/DestroyJob (src/evp.c:23-26). */
+typedef struct mth_ctx mth_ctx;
+mth_status mth_create(const mth_params* params, mth_ctx** out);
+/* Voxel microstructure in the reference's text order: z fastest, then y, then
+ * x (pIDX, src/evp.h:53).  Euler angles are Bunge degrees as in the file
+ * (src/init.c:255-273); phase is 1-based.  Replaces InitMicroStruct
+ * (src/init.c:233-396) and InitFields (src/init.c:444-515). */
+mth_status mth_upload_microstructure(mth_ctx* ctx, const int* grain, const int* phase,
+                                     const double* euler_deg, size_t n_voxels);
+/* One mechanical step: Green iteration + end-of-step updates, the body of
+ * the loop in Evolution (src/evolution.c:1319-1693). */
+mth_status mth_step(mth_ctx* ctx, mth_step_report* report);
+/* Copy a field to host memory as doubles (count = voxels * components). */
+mth_status mth_download_field(mth_ctx* ctx, int field, double* host, size_t count);
+mth_status mth_destroy(mth_ctx* ctx);
+
+/* Batch local solve: the per-voxel Newton of UpdateStress
+ * (src/evolution.c:44-310) over n independent voxels, all inputs on the host
+ * in the 6-component Lebensohn-Tome basis (chg_basis, src/kinematics.c:14-93).
+ *   sig [n*6]   in: initial guess = lambda; out: converged stress
+ *   eps_p [n*6] plastic strain at t
+ *   strain [n*6] total strain sym(grad u)
+ *   rot [n*9]   crystal->sample rotation, row-major
+ *   crss [n*12] forward CRSS per system (backward = forward + (tau0b-tau0f))
+ *   edot [n*6]  out: plastic strain rate
+ *   err [n*2]   out: |sig-lambda|, |eps_tot-strain| (src/evolution.c:291-299)
+ * c066 is the 6x6 reference stiffness.  Phase 1 parameters come from params. */
+mth_status mth_local_solve(const mth_params* params, const double c066[36], size_t n,
+                           double* sig, const double* eps_p, const double* strain,
+                           const double* rot, const double* crss, double* edot,
+                           double* err, long long* newton_iters);
+
+/* Host-side readers for the reference's input files. */
+/* input.in namelist (src/io.c:96-164); fills params and copies the file
+ * names of the .sx files and the microstructure. */
+mth_status mth_read_namelist(const char* path, mth_params* params,
+                             char* slip_path_1, char* slip_path_2, char* ms_path,
+                             size_t path_cap);
+/* single-crystal .sx file (src/init.c:52-231) into params->phase[iphase]. */
+mth_status mth_read_sx(const char* path, mth_params* params, int iphase);
+/* voxel microstructure text (src/init.c:255-270): n voxels, z fastest. */
+mth_status mth_read_microstructure(const char* path, size_t n, int* grain, int* phase,
+                                   double* euler_deg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MTH_H */

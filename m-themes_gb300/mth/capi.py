@@ -1,0 +1,160 @@
+"""ctypes mirror of include/mth.h and loader of the in-tree libmth.so.
+
+The C-ABI is the product boundary; this module only marshals Python values
+into the structs it declares.  Loading fails loudly when the shared library
+has not been built: there is no Python fallback for any compute entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+NSYS = 12
+NPH = 2
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(HERE)
+REPO_ROOT = os.path.dirname(PKG_ROOT)
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libmth.so")
+
+MTH_FP64 = 0
+MTH_MIXED = 1
+
+FIELD = {"sig": 0, "eps": 1, "edot": 2, "strain": 3, "rot": 4, "crss": 5, "gamacum": 6, "grain": 7, "rho": 8}
+FIELD_NCOMP = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 1, 7: 1, 8: 1}
+
+STATUS = {0: "MTH_OK", 1: "MTH_ERR_ARG", 2: "MTH_ERR_CUDA", 3: "MTH_ERR_NOMEM", 4: "MTH_ERR_SINGULAR",
+          5: "MTH_ERR_NOT_CONVERGED", 6: "MTH_ERR_IO", 7: "MTH_ERR_STATE", 8: "MTH_ERR_TIMEOUT",
+          9: "MTH_ERR_NAN", 10: "MTH_ERR_UNSUPPORTED"}
+
+
+class MthPhase(C.Structure):
+    _fields_ = [("type", C.c_int), ("c11", C.c_double), ("c12", C.c_double), ("c44", C.c_double),
+                ("nsys", C.c_int), ("bn", (C.c_double * 3) * NSYS), ("bb", (C.c_double * 3) * NSYS),
+                ("nrs", C.c_double), ("gamd0", C.c_double), ("tau0f", C.c_double), ("tau0b", C.c_double),
+                ("tau1", C.c_double), ("thet0", C.c_double), ("thet1", C.c_double),
+                ("hself", C.c_double), ("hlat", C.c_double)]
+
+
+class MthParams(C.Structure):
+    _fields_ = [("cell_dim", C.c_int * 3), ("n_phases", C.c_int), ("phase", MthPhase * NPH),
+                ("time_step", C.c_double), ("n_steps", C.c_int), ("err", C.c_double), ("iter_max", C.c_int),
+                ("velgrad_bc_flag", C.c_int * 6), ("velgrad_bc", C.c_double * 6),
+                ("stress_bc_flag", C.c_int * 6), ("stress_bc", C.c_double * 6),
+                ("elast_bc", C.c_int), ("update_flag", C.c_int), ("hard_flag", C.c_int),
+                ("precision", C.c_int), ("newton_tol", C.c_double), ("newton_itmax", C.c_int),
+                ("pf_length_scale", C.c_double), ("pf_time_step", C.c_double), ("e_gb", C.c_double),
+                ("m_gb", C.c_double), ("pf_width_cells", C.c_double), ("stored_energy_scale", C.c_double),
+                ("shear_modulus", C.c_double), ("burgers", C.c_double), ("nucleus_radius", C.c_int),
+                ("rho_nucleation", C.c_double), ("rho0", C.c_double), ("rho_k", C.c_double),
+                ("pf_substeps", C.c_int), ("seed", C.c_uint64)]
+
+
+T33 = (C.c_double * 3) * 3
+
+
+class MthStepReport(C.Structure):
+    _fields_ = [("step", C.c_int), ("iterations", C.c_int), ("time", C.c_double),
+                ("sig_avg", T33), ("sig_avg_ph1", T33), ("disgrad_avg", T33), ("eps_avg", T33),
+                ("edot_avg", T33), ("e_vm", C.c_double), ("evmp", C.c_double), ("d_vm", C.c_double),
+                ("dvmp", C.c_double), ("s_vm", C.c_double), ("s_vm1", C.c_double),
+                ("err_s", C.c_double), ("err_e", C.c_double), ("newton_iters", C.c_longlong),
+                ("newton_failed", C.c_longlong), ("n_new_grains", C.c_int)]
+
+    def to_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            if isinstance(v, C.Array):
+                v = np.array([[v[i][j] for j in range(3)] for i in range(3)])
+            d[name] = v
+        return d
+
+
+def params_from_config(cfg, precision=MTH_FP64, newton_tol=0.0, newton_itmax=0) -> MthParams:
+    """Fill MthParams from a synth.Config (power-law/Voce FCC, optional gas phase)."""
+    from . import synth
+    p = MthParams()
+    p.cell_dim[:] = list(cfg.cell_dim)
+    p.n_phases = 2 if cfg.n_pores else 1
+    m = cfg.material
+    for k in range(NPH):
+        ph = p.phase[k]
+        ph.type = 0 if k == 0 else 1
+        if k == 0:
+            ph.c11, ph.c12, ph.c44 = m.c11, m.c12, m.c44
+            ph.nsys = len(synth.FCC_SLIP)
+            for i, (n, b) in enumerate(synth.FCC_SLIP):
+                ph.bn[i][:] = [float(x) for x in n]
+                ph.bb[i][:] = [float(x) for x in b]
+            ph.nrs, ph.gamd0 = m.nrs, m.gamd0
+            ph.tau0f, ph.tau0b, ph.tau1, ph.thet0, ph.thet1 = m.tau0f, m.tau0b, m.tau1, m.thet0, m.thet1
+            ph.hself, ph.hlat = m.hself, m.hlat
+    p.time_step = cfg.time_step
+    p.n_steps = cfg.n_steps
+    p.err = cfg.err
+    p.iter_max = cfg.iter_max
+    p.velgrad_bc_flag[:] = list(cfg.velgrad_bc_flag)
+    p.velgrad_bc[:] = [float(x) for x in cfg.velgrad_bc]
+    p.stress_bc_flag[:] = list(cfg.stress_bc_flag)
+    p.stress_bc[:] = [float(x) for x in cfg.stress_bc]
+    p.elast_bc = cfg.elast_bc
+    p.update_flag = cfg.update_flag
+    p.hard_flag = cfg.hard_flag
+    p.precision = precision
+    p.newton_tol = newton_tol
+    p.newton_itmax = newton_itmax
+    return p
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class MthError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libmth.so (built by build.py).  Raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise MthError(f"{p} not found: build the CUDA library first (python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(p)
+    lib.mth_version.restype = C.c_char_p
+    lib.mth_last_error.restype = C.c_char_p
+    lib.mth_create.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_void_p)]
+    lib.mth_upload_microstructure.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_double), C.c_size_t]
+    lib.mth_step.argtypes = [C.c_void_p, C.POINTER(MthStepReport)]
+    lib.mth_download_field.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t]
+    lib.mth_destroy.argtypes = [C.c_void_p]
+    lib.mth_local_solve.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_double), C.c_size_t,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    lib.mth_read_namelist.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_char_p, C.c_char_p, C.c_char_p,
+                                      C.c_size_t]
+    lib.mth_read_sx.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_int]
+    lib.mth_read_microstructure.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double)]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(lib, st):
+    if st != 0:
+        msg = lib.mth_last_error().decode(errors="replace")
+        raise MthError(f"{STATUS.get(st, st)}: {msg}")

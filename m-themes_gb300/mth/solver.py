@@ -1,0 +1,73 @@
+"""High-level wrapper over the C-ABI (include/mth.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+
+
+class Solver:
+    """One RVE on the GPU: mth_create + mth_upload_microstructure, then
+    `step()` per mechanical step (the loop body of Evolution,
+    src/evolution.c:1319-1693)."""
+
+    def __init__(self, params: capi.MthParams, grain, phase, euler):
+        self.lib = capi.load()
+        self.params = params
+        self.nv = int(np.prod(list(params.cell_dim)))
+        ctx = C.c_void_p()
+        capi.check(self.lib, self.lib.mth_create(C.byref(params), C.byref(ctx)))
+        self.ctx = ctx
+        g = np.ascontiguousarray(grain, dtype=np.int32)
+        p = np.ascontiguousarray(phase, dtype=np.int32)
+        e = np.ascontiguousarray(euler, dtype=np.float64)
+        if g.size != self.nv or p.size != self.nv or e.size != 3 * self.nv:
+            self.close()
+            raise ValueError("microstructure arrays do not match cell_dim")
+        capi.check(self.lib, self.lib.mth_upload_microstructure(self.ctx, capi._iptr(g), capi._iptr(p),
+                                                                capi._dptr(e), self.nv))
+
+    def step(self) -> dict:
+        rep = capi.MthStepReport()
+        capi.check(self.lib, self.lib.mth_step(self.ctx, C.byref(rep)))
+        return rep.to_dict()
+
+    def field(self, name: str) -> np.ndarray:
+        f = capi.FIELD[name]
+        out = np.zeros(self.nv * capi.FIELD_NCOMP[f])
+        capi.check(self.lib, self.lib.mth_download_field(self.ctx, f, capi._dptr(out), out.size))
+        return out.reshape(self.nv, -1)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.mth_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def local_solve(params, c066, sig, eps_p, strain, rot, crss):
+    """Batch local Newton (mth_local_solve); arrays as in include/mth.h."""
+    lib = capi.load()
+    n = sig.shape[0]
+    sig = np.ascontiguousarray(sig, dtype=np.float64).copy()
+    edot = np.zeros((n, 6))
+    err = np.zeros((n, 2))
+    it = C.c_longlong(0)
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (c066, eps_p, strain, rot, crss)]
+    capi.check(lib, lib.mth_local_solve(C.byref(params), capi._dptr(a[0]), n, capi._dptr(sig), capi._dptr(a[1]),
+                                        capi._dptr(a[2]), capi._dptr(a[3]), capi._dptr(a[4]), capi._dptr(edot),
+                                        capi._dptr(err), C.byref(it)))
+    return sig, edot, err, it.value

@@ -1,0 +1,264 @@
+"""Seeded synthetic inputs in the reference's own file formats.
+
+The reference reads three files: the ``input.in`` namelist (src/io.c:25-164),
+a single-crystal ``.sx`` slip file (src/init.c:52-231) and a voxel
+microstructure text with one line ``phi1 Phi phi2 i j k grain phase`` per voxel,
+Bunge angles in degrees, 1-based indices, x slowest and z fastest
+(src/init.c:255-270).  This module generates periodic Voronoi polycrystals with
+orientations uniform on SO(3), optional spherical pores (phase 2 = gas), and the
+FCC copper parameter sets of the benchmark workloads, and writes all three
+files.  Values are rounded to what the text holds, so a run that reads the
+files and a run that takes the arrays directly see identical doubles.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+
+import numpy as np
+
+# FCC {111}<110>: the 12 systems of test_run/Cu_p.sx mode 1 (plane normal, direction)
+FCC_SLIP = [
+    ((1, 1, -1), (0, 1, 1)), ((1, 1, -1), (1, 0, 1)), ((1, 1, -1), (1, -1, 0)),
+    ((1, -1, -1), (0, 1, -1)), ((1, -1, -1), (1, 0, 1)), ((1, -1, -1), (1, 1, 0)),
+    ((1, -1, 1), (0, 1, 1)), ((1, -1, 1), (1, 0, -1)), ((1, -1, 1), (1, 1, 0)),
+    ((1, 1, 1), (0, 1, -1)), ((1, 1, 1), (1, 0, -1)), ((1, 1, 1), (1, -1, 0)),
+]
+
+
+@dataclasses.dataclass
+class Material:
+    """Cubic elastic constants (MPa) and one power-law/Voce slip mode."""
+    c11: float = 168400.0
+    c12: float = 121400.0
+    c44: float = 75400.0
+    nrs: float = 10.0
+    gamd0: float = 1.0
+    tau0f: float = 16.0
+    tau0b: float = 16.0
+    tau1: float = 148.0
+    thet0: float = 250.0
+    thet1: float = 2.0
+    hself: float = 1.0
+    hlat: float = 1.0
+
+
+@dataclasses.dataclass
+class Config:
+    """One run: grid, loading and control parameters (namelist keys)."""
+    cell_dim: tuple = (32, 32, 32)
+    n_grains: int = 64
+    n_pores: int = 0
+    pore_radius: int = 3
+    seed: int = 1234
+    material: Material = dataclasses.field(default_factory=Material)
+    time_step: float = 1e-3
+    n_steps: int = 10
+    err: float = 1e-5
+    iter_max: int = 100
+    velgrad_bc_flag: tuple = (0, 0, 1, 1, 1, 1)
+    velgrad_bc: tuple = (-0.5, -0.5, 1.0, 0.0, 0.0, 0.0)
+    stress_bc_flag: tuple = (1, 1, 0, 0, 0, 0)
+    stress_bc: tuple = (0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    elast_bc: int = 1
+    update_flag: int = 1
+    hard_flag: int = 1
+
+
+def voronoi(cell_dim, n_grains, rng):
+    """Periodic Voronoi tessellation: 1-based grain id of every voxel centre,
+    flattened with z fastest."""
+    from scipy.spatial import cKDTree
+    dims = np.asarray(cell_dim, dtype=np.float64)
+    seeds = rng.random((n_grains, 3)) * dims
+    tree = cKDTree(seeds, boxsize=dims)
+    ax = [np.arange(n, dtype=np.float64) + 0.5 for n in cell_dim]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    _, idx = tree.query(pts, k=1)
+    return idx.astype(np.int32) + 1
+
+
+def uniform_orientations(n, rng):
+    """Bunge angles (degrees) uniform on SO(3): phi1, phi2 ~ U[0, 360),
+    cos(Phi) ~ U[-1, 1]."""
+    phi1 = rng.random(n) * 360.0
+    phi2 = rng.random(n) * 360.0
+    Phi = np.degrees(np.arccos(rng.random(n) * 2.0 - 1.0))
+    eul = np.stack([phi1, Phi, phi2], axis=1)
+    return np.round(eul, 6)
+
+
+def spherical_pores(cell_dim, n_pores, radius, rng, max_tries=100000):
+    """Boolean gas mask of non-overlapping periodic spheres of the given radius
+    (cells) at seeded random centres."""
+    dims = np.asarray(cell_dim)
+    centres = []
+    tries = 0
+    while len(centres) < n_pores:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place non-overlapping pores")
+        c = rng.random(3) * dims
+        ok = True
+        for o in centres:
+            d = np.abs(c - o)
+            d = np.minimum(d, dims - d)
+            if np.sqrt((d * d).sum()) < 2 * radius + 1:
+                ok = False
+                break
+        if ok:
+            centres.append(c)
+    mask = np.zeros(tuple(cell_dim), dtype=bool)
+    ax = [np.arange(n, dtype=np.float64) + 0.5 for n in cell_dim]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    for c in centres:
+        d = [np.abs(A - ci) for A, ci in zip((X, Y, Z), c)]
+        d = [np.minimum(di, n - di) for di, n in zip(d, cell_dim)]
+        mask |= (d[0] ** 2 + d[1] ** 2 + d[2] ** 2) <= radius * radius
+    return mask.ravel()
+
+
+def microstructure(cfg: Config):
+    """(grain, phase, euler_deg) arrays of one configuration, z fastest."""
+    rng = np.random.default_rng(cfg.seed)
+    grain = voronoi(cfg.cell_dim, cfg.n_grains, rng)
+    eul_g = uniform_orientations(cfg.n_grains, rng)
+    euler = eul_g[grain - 1].copy()
+    phase = np.ones(grain.shape, dtype=np.int32)
+    if cfg.n_pores:
+        gas = spherical_pores(cfg.cell_dim, cfg.n_pores, cfg.pore_radius, rng)
+        phase[gas] = 2
+        grain[gas] = cfg.n_grains + 1
+        euler[gas] = 0.0
+    return grain.astype(np.int32), phase, np.ascontiguousarray(euler)
+
+
+# ---------------------------------------------------------------- writers
+def write_microstructure(path, cfg: Config, grain, phase, euler):
+    nx, ny, nz = cfg.cell_dim
+    ii, jj, kk = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1), np.arange(1, nz + 1), indexing="ij")
+    with open(path, "w") as f:
+        for v, (i, j, k) in enumerate(zip(ii.ravel(), jj.ravel(), kk.ravel())):
+            e = euler[v]
+            f.write("%.6f %.6f %.6f %d %d %d %d %d\n" % (e[0], e[1], e[2], i, j, k, grain[v], phase[v]))
+
+
+def write_sx(path, m: Material):
+    """One-mode FCC file in the line layout PlasticInit reads (src/init.c:66-176)."""
+    lines = ["# Crystal system (XtalSys):", "CUBIC", "",
+             "# Crystal axes (XtalAxis):", "1.0 1.0 1.0", "",
+             "# Total number of modes listed in the file (N_modes_max):", "1", "",
+             "# Number of modes to be used in the calculation (N_modes):", "1", "",
+             "# Labels of the modes to be used (iMode):", "1", "",
+             "# Mode# 1 -- <110>(111) SLIP",
+             "\tnsmx\tnrsx\tgamd0x\ttwshx\tisectwx",
+             "\t12\t\t%r\t\t%r\t\t0.0\t\t0" % (float(m.nrs), float(m.gamd0)),
+             "\ttau0xf\ttau0xb\ttau1x\tthet0\tthet1",
+             "\t%r\t\t%r\t\t%r\t\t%r\t\t%r" % (float(m.tau0f), float(m.tau0b), float(m.tau1),
+                                                float(m.thet0), float(m.thet1)),
+             "\thselfx\thlatex",
+             "\t%r\t\t%r" % (float(m.hself), float(m.hlat)),
+             "\tSlip (n-b)"]
+    for n, b in FCC_SLIP:
+        lines.append("\t%d %d %d\t\t%d %d %d" % (n + b))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_input(path, cfg: Config, ms_name="ms.txt", sx_name="cu.sx"):
+    m = cfg.material
+    n_phases = 2 if cfg.n_pores else 1
+
+    def vec(v):
+        return " ".join(repr(float(x)) if isinstance(x, float) else str(x) for x in v)
+
+    txt = f"""# generated input (reference namelist layout)
+N_phases\t{n_phases}
+CellDim {cfg.cell_dim[0]} {cfg.cell_dim[1]} {cfg.cell_dim[2]}
+initial_ms {ms_name}
+Type_phases 0 1
+ElastConst_PhaseI {m.c11!r} {m.c12!r} {m.c44!r} 0.35
+Slip_PhaseI {sx_name}
+ElastConst_PhaseII 0.0 0.0 0.0 0.0
+Slip_PhaseII {sx_name}
+VelGrad_BC_Flag {vec(cfg.velgrad_bc_flag)}
+VelGrad_BC {vec(cfg.velgrad_bc)}
+Stress_BC_Flag {vec(cfg.stress_bc_flag)}
+Stress_BC {vec(cfg.stress_bc)}
+ElastBC {cfg.elast_bc}
+TimeStep {cfg.time_step!r}
+N_steps {cfg.n_steps}
+Err {cfg.err!r}
+IterMax {cfg.iter_max}
+PrintControl 0 2000
+Update_Flag {cfg.update_flag}
+Hard_Flag {cfg.hard_flag}
+Tex_Flag 0
+a0 0.362 0.0
+L0 0.003
+GND_ScaleRatio 6000.0
+Q_slip 20000000000.0 0.0
+Q_bulk 300000000000.51 0.0
+rho_SSD_initial 0.05
+T__K 30
+C_1 0.48 0.0
+C_2 3.0 0.0
+C_3 3.0 0.0
+C_4 800.0 0.0
+C_5 16.0 0.0
+C_6 1100E0 0.0
+C_7 1.25E-8 0.0
+C_8 0.24 0.0
+Selfinter 0.125 0.0
+Coplanar 0.125 0.0
+CrossSlip 0.725 0.0
+GlissileJunction 0.125 0.0
+HirthLock 0.05 0.0
+LomerCottrellLock 0.18 0.0
+D_0 4E-05
+nucleus_radius 2
+CellDim_pf {cfg.cell_dim[0]} {cfg.cell_dim[1]} {cfg.cell_dim[2]}
+RandSeed 123
+E_gb 0.625
+M_gb 7.4E-11
+Scale_Fdeform 0.5
+k_c 320000.0
+alpha 8.5
+zeta_kc 1.0
+age_drx 1E0
+ssdScaler_DRX 0.74
+gndScaler_DRX 0.66
+sigScaler_DRX 0.66
+Nucl_Static_Flag 1
+tau_DRX 1000.0
+DeltaQ_DRX 0.0
+DeltaTau_DRX 0.0
+pf_length_scale 2.5E-06
+pf_time_step 0.004
+"""
+    with open(path, "w") as f:
+        f.write(txt)
+
+
+def write_case(directory, cfg: Config):
+    """Write input.in, cu.sx and ms.txt of one configuration; returns the
+    microstructure arrays."""
+    os.makedirs(directory, exist_ok=True)
+    grain, phase, euler = microstructure(cfg)
+    write_microstructure(os.path.join(directory, "ms.txt"), cfg, grain, phase, euler)
+    write_sx(os.path.join(directory, "cu.sx"), cfg.material)
+    write_input(os.path.join(directory, "input.in"), cfg)
+    return grain, phase, euler
+
+
+# ------------------------------------------------------ named workloads
+def workload(name: str) -> Config:
+    """Benchmark workloads: 'c0' = 32^3 / 64 grains FP64 plain EVPFFT, 10 steps;
+    'c1' = 128^3 / 512 grains + 40 radius-3 pores, 100 steps."""
+    if name == "c0":
+        return Config(cell_dim=(32, 32, 32), n_grains=64, n_steps=10, seed=20240101)
+    if name == "c1":
+        return Config(cell_dim=(128, 128, 128), n_grains=512, n_pores=40, pore_radius=3,
+                      n_steps=100, seed=20240102)
+    raise KeyError(name)

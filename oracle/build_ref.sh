@@ -1,0 +1,37 @@
+#!/bin/bash
+# Builds the reference M-THEMES `forge` from its sources where they lie
+# (MTH_REFERENCE, default /root/reference) into oracle/_ref/ only, for
+# pinning the oracle.  It compiles the reference's own 8 translation units
+# (src/Makefile:11) with single-rank MPI/FFTW-MPI/GSL stand-ins
+# (oracle/refshim) and serial FFTW 2.1.5 built from the vendored tarball.
+# The reference's build system and MPICH are not used.  x86 or Arm host; no
+# GPU needed.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${MTH_REFERENCE:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -d "$REF/src" ]; then echo "reference sources not found at $REF" >&2; exit 2; fi
+mkdir -p "$OUT/obj"
+if [ ! -f "$OUT/fftw/lib/libfftw.a" ]; then
+  rm -rf "$OUT/fftw-src"; mkdir -p "$OUT/fftw-src"
+  tar xzf "$REF/fftw/src/fftw-2.1.5.tar.gz" -C "$OUT/fftw-src"
+  ( cd "$OUT/fftw-src/fftw-2.1.5" && \
+    ./configure --prefix="$OUT/fftw" --disable-shared CFLAGS="-O2 -fPIC" > ../configure.log 2>&1 && \
+    make -j8 > ../make.log 2>&1 && make install > ../install.log 2>&1 )
+fi
+CXX="${CXX:-g++}"
+COMMON=(-O3 -w -fPIC -include "$HERE/refshim/mth_ref_prelude.h" -I"$HERE/refshim" -I"$OUT/fftw/include" -I"$REF/src")
+declare -A EXTRA
+EXTRA[evp.c]="-DSetupJob=mth_ref_SetupJob -DDestroyJob=mth_ref_DestroyJob"
+EXTRA[evolution.c]="-DStrainRate_Orowan=StrainRate_eval -DDislocationEvolution=mth_ref_after_step -DAvgDislocation=mth_ref_noop -DGradient_ShearRate=mth_ref_noop -DGradient_Shear=mth_ref_noop -DVonMises=mth_ref_VonMises"
+OBJS=()
+for s in evp.c io.c init.c kinematics.c evolution.c constitutive.c integrated.c pf_xrx.c; do
+  o="$OUT/obj/${s%.c}.o"
+  # shellcheck disable=SC2086
+  $CXX -x c++ "${COMMON[@]}" ${EXTRA[$s]:-} -c "$REF/src/$s" -o "$o" &
+  OBJS+=("$o")
+done
+$CXX "${COMMON[@]}" -c "$HERE/refshim/refshim.cc" -o "$OUT/obj/refshim.o" &
+wait
+$CXX -o "$OUT/forge_ref" "${OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
+echo "built $OUT/forge_ref"

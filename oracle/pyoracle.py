@@ -1,0 +1,134 @@
+"""ctypes binding of the oracle library (oracle/_build/liborc.so).
+
+ORACLE - test infrastructure only.  tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py load it as the checker; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(REPO, "m-themes_gb300"))
+from mth import capi  # noqa: E402  (struct layouts shared with include/mth.h)
+
+LIB = os.path.join(HERE, "_build", "liborc.so")
+SVM_OOB_ZERO, SVM_OOB_EPSAVG10, SVM_OOB_SIGAVG1_00 = 0, 1, 2
+
+
+def build(force=False):
+    """Compile oracle/evpfft_oracle.c into oracle/_build/liborc.so."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    src = os.path.join(HERE, "evpfft_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", LIB, src, "-lm"]
+    subprocess.check_call(cmd)
+    return LIB
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(LIB)
+        lib.orc_create.restype = C.c_void_p
+        lib.orc_create.argtypes = [C.POINTER(capi.MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int)]
+        lib.orc_step.argtypes = [C.c_void_p, C.POINTER(capi.MthStepReport)]
+        lib.orc_get_field.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        lib.orc_get_c066.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        lib.orc_second_backtracks.argtypes = [C.c_void_p]
+        lib.orc_second_backtracks.restype = C.c_longlong
+        lib.orc_destroy.argtypes = [C.c_void_p]
+        lib.orc_local_solve.argtypes = [C.POINTER(capi.MthParams), C.POINTER(C.c_double), C.c_size_t,
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+        lib.orc_fft3d.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int, C.c_int]
+        _lib = lib
+    return _lib
+
+
+class Oracle:
+    """FP64 CPU restatement of the reference EVPFFT step."""
+
+    def __init__(self, params, grain, phase, euler, nthreads=None, svm_oob=SVM_OOB_SIGAVG1_00):
+        lib = load()
+        self.lib = lib
+        self.nv = int(np.prod(list(params.cell_dim)))
+        g = np.ascontiguousarray(grain, dtype=np.int32)
+        p = np.ascontiguousarray(phase, dtype=np.int32)
+        e = np.ascontiguousarray(euler, dtype=np.float64)
+        st = C.c_int(0)
+        nt = nthreads or os.cpu_count() or 1
+        self.ctx = lib.orc_create(C.byref(params), capi._iptr(g), capi._iptr(p), capi._dptr(e), nt, svm_oob,
+                                  C.byref(st))
+        if not self.ctx:
+            raise RuntimeError(f"orc_create failed: {capi.STATUS.get(st.value, st.value)}")
+
+    def step(self):
+        rep = capi.MthStepReport()
+        st = self.lib.orc_step(self.ctx, C.byref(rep))
+        if st != 0:
+            raise RuntimeError(f"orc_step failed: {capi.STATUS.get(st, st)}")
+        return rep.to_dict()
+
+    def field(self, name):
+        f = capi.FIELD[name]
+        out = np.zeros(self.nv * capi.FIELD_NCOMP[f])
+        if self.lib.orc_get_field(self.ctx, f, capi._dptr(out)) != 0:
+            raise RuntimeError("orc_get_field")
+        return out.reshape(self.nv, -1)
+
+    def c066(self):
+        out = np.zeros(36)
+        self.lib.orc_get_c066(self.ctx, capi._dptr(out))
+        return out.reshape(6, 6)
+
+    def second_backtracks(self):
+        return self.lib.orc_second_backtracks(self.ctx)
+
+    def close(self):
+        if self.ctx:
+            self.lib.orc_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def local_solve(params, c066, sig, eps_p, strain, rot, crss):
+    lib = load()
+    n = sig.shape[0]
+    sig = np.ascontiguousarray(sig, dtype=np.float64).copy()
+    edot = np.zeros((n, 6))
+    err = np.zeros((n, 2))
+    it = C.c_longlong(0)
+    args = [np.ascontiguousarray(a, dtype=np.float64) for a in (c066, eps_p, strain, rot, crss)]
+    st = lib.orc_local_solve(C.byref(params), capi._dptr(args[0]), n, capi._dptr(sig), capi._dptr(args[1]),
+                             capi._dptr(args[2]), capi._dptr(args[3]), capi._dptr(args[4]), capi._dptr(edot),
+                             capi._dptr(err), C.byref(it))
+    if st != 0:
+        raise RuntimeError(f"orc_local_solve: {capi.STATUS.get(st, st)}")
+    return sig, edot, err, it.value
+
+
+def fft3d(data, sign):
+    """In-place complex 3-D FFT of a (n0,n1,n2) complex128 array (copy returned)."""
+    lib = load()
+    a = np.ascontiguousarray(data, dtype=np.complex128).copy()
+    n0, n1, n2 = a.shape
+    lib.orc_fft3d(a.ctypes.data_as(C.POINTER(C.c_double)), n0, n1, n2, sign)
+    return a
