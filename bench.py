@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark of the EVPFFT Green iteration on GB300.
+
+Metric: voxel-iterations/s = voxels x Green iterations / time, on the
+128^3 workload (512 periodic Voronoi grains, uniform SO(3) orientations, 40
+non-overlapping radius-3 pores as gas, FCC Cu power law n=10 with Voce
+hardening, uniaxial tension eps33_dot = 1/s with stress-free lateral mixed
+boundary conditions, dt = 1e-3, IterMax 100 Green iterations per step).  A
+"step" is one mechanical step.  Inputs are seeded synthetic data of those
+shapes (the reference ships no dataset).  The fields (~0.5 GB in mixed
+precision) are larger than L2, so no L2 flush is done between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+--impl reference times the CPU implementation of the same path: the oracle
+(a C restatement of the reference's algorithm, oracle/evpfft_oracle.c) on
+all host cores, one Green iteration of the same workload per step.  The
+reference's own build needs its sources, which do not travel with the repo.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "m-themes_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "voxel-iterations/s at 128³: mixed vs FP64 GPU at ≤1e-4 rel stress error"
+UNIT = "voxel-iterations/s"
+THROTTLE_BAD = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--iter-max", type=int, default=0, help="override IterMax (default: the workload's 100)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- helpers
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summary,
+    scaled to the 128^3 workload (profiles/traffic.json), or None."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    v = d.get(kernel)
+    return None if v is None else float(v)
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+def workload_cfg(args):
+    from mth import synth
+    cfg = synth.workload(args.workload)
+    if args.iter_max:
+        cfg.iter_max = args.iter_max
+    return cfg
+
+
+# ------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    import torch
+    from mth import Solver, capi, synth
+    ws, rank, lrank = dist_init()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(lrank)
+        dist.init_process_group("nccl")
+    dev_index = lrank if ws > 1 else 0
+    cfg = workload_cfg(args)
+    cfg.seed += rank     # replicas: each rank its own RVE of the same size
+    grain, phase, euler = synth.microstructure(cfg)
+    nv = int(np.prod(cfg.cell_dim))
+    prec = capi.MTH_MIXED if args.precision == "mixed" else capi.MTH_FP64
+
+    def barrier_sync():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def reduce_max(x):
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def reduce_sum(x):
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t)
+        return float(t.item())
+
+    def timed_run(precision, steps, warmup, profile=False, clocks=False):
+        par = capi.params_from_config(cfg, precision=precision)
+        par.device = dev_index
+        s = Solver(par, grain, phase, euler)
+        for _ in range(warmup):
+            s.step()
+        s.profile(enable=profile, reset=True)
+        barrier_sync()
+        cs = ClockSampler(dev_index) if clocks else None
+        if cs:
+            cs.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        reps = [s.step() for _ in range(steps)]
+        e1.record()
+        barrier_sync()
+        ms = e0.elapsed_time(e1)
+        clk = cs.stop() if cs else None
+        prof, launches = s.profile(reset=True)
+        iters = sum(r["iterations"] for r in reps)
+        s.close()
+        return ms, iters, reps, prof, launches, clk
+
+    # main (device-resident) measurement
+    ms, iters, reps, prof, launches, clk = timed_run(prec, args.steps, args.warmup, profile=True, clocks=True)
+    ms_max = reduce_max(ms)
+    vox_it = reduce_sum(float(nv) * iters)
+    value = vox_it / (ms_max / 1e3)
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 fields + f64 Newton" if prec == capi.MTH_MIXED else "f64",
+           "data": "synthetic: seeded periodic Voronoi, 512 grains, uniform SO(3) orientations, 40 radius-3 pores",
+           "config": {"workload": "128^3 RVE, 512 grains, 40 pores, FCC Cu power law n=10 + Voce, uniaxial "
+                                  "tension eps33_dot=1/s, dt=1e-3, IterMax=%d" % cfg.iter_max,
+                      "grid": list(cfg.cell_dim), "voxels": nv, "green_iterations": iters,
+                      "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single GPU",
+                      "l2": "fields (~0.5 GB) larger than the 129 MB L2; no flush"}}
+
+    # roofline of the dominant kernel (device time from CUDA events on the library stream)
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    dname, d = dom
+    peak, peak_kind = measured_peaks()
+    per_launch_s = (d["ms"] / 1e3) / max(d["launches"], 1)
+    per_launch_bytes = d["bytes"] / max(d["launches"], 1)
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    tr = traffic_per_launch(dname)
+    out["roofline"] = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "peak_source": peak_kind, "traffic": tr,
+                       "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_s * 1e3,
+                       "note": "the local Newton is ALU-bound (FP64 solve, FP32 flow rule); its HBM fraction is low "
+                               "by construction"}
+    tot_ms = sum(v["ms"] for v in prof.values())
+    out["kernels"] = {k: {"ms": round(v["ms"], 3), "share": round(v["ms"] / tot_ms, 4) if tot_ms else None,
+                          "launches": v["launches"],
+                          "gbs": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None}
+                      for k, v in prof.items() if v["launches"]}
+    out["gpu_launches"] = launches
+    out["clocks"] = clk
+
+    # FP64 comparison: same warm-up and steps, last-step macroscopic stress
+    if not args.no_fp64 and prec == capi.MTH_MIXED:
+        ms64, it64, reps64, _, _, _ = timed_run(capi.MTH_FP64, args.steps, args.warmup)
+        ms64 = reduce_max(ms64)
+        v64 = reduce_sum(float(nv) * it64) / (ms64 / 1e3)
+        a, b = reps[-1]["sig_avg"], reps64[-1]["sig_avg"]
+        err = float(np.abs(a - b).max() / np.abs(b).max())
+        out["fp64"] = {"value": v64, "ms_per_step": ms64 / args.steps, "green_iterations": it64}
+        out["mixed_over_fp64"] = value / v64
+        out["rel_stress_err_vs_fp64"] = err
+
+    # end to end through the C-ABI with host buffers: create + upload (H2D of
+    # the microstructure from pinned memory), K steps each returning the
+    # report and the full stress field to the host
+    if not args.no_e2e:
+        import ctypes as C
+        lib = capi.load()
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        g_h, p_h, e_h = pin(grain), pin(phase), pin(euler)
+        sig_h = torch.empty(9 * nv, dtype=torch.float64).pin_memory().numpy()
+        par = capi.params_from_config(cfg, precision=prec)
+        par.device = dev_index
+        barrier_sync()
+        t0 = time.perf_counter()
+        ctx = C.c_void_p()
+        capi.check(lib, lib.mth_create(C.byref(par), C.byref(ctx)))
+        capi.check(lib, lib.mth_upload_microstructure(ctx, capi._iptr(g_h), capi._iptr(p_h), capi._dptr(e_h), nv))
+        rep = capi.MthStepReport()
+        it_e2e = 0
+        for _ in range(args.steps):
+            capi.check(lib, lib.mth_step(ctx, C.byref(rep)))
+            it_e2e += rep.iterations
+            capi.check(lib, lib.mth_download_field(ctx, 0, capi._dptr(sig_h), sig_h.size))
+        barrier_sync()
+        dt = time.perf_counter() - t0
+        lib.mth_destroy(ctx)
+        dt = reduce_max(dt)
+        h2d = (g_h.nbytes + p_h.nbytes + e_h.nbytes) / args.steps
+        out["e2e"] = {"value": reduce_sum(float(nv) * it_e2e) / dt, "unit": UNIT,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(sig_h.nbytes + C.sizeof(rep)),
+                      "note": "create + microstructure upload amortised over the steps; the stress field is "
+                              "returned to the host after every step"}
+
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_sample(cfg)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------------------ CPU (oracle)
+def cpu_sample(cfg, iterations=1):
+    """Oracle (C port of the reference algorithm, OpenMP over all host cores)
+    on one mechanical step limited to `iterations` Green iterations of the
+    full 128^3 workload."""
+    import pyoracle
+    from mth import capi, synth
+    c = synth.Config(**{**cfg.__dict__})
+    c.iter_max = iterations
+    grain, phase, euler = synth.microstructure(c)
+    cores = os.cpu_count() or 1
+    o = pyoracle.Oracle(capi.params_from_config(c), grain, phase, euler, nthreads=cores)
+    t0 = time.perf_counter()
+    r = o.step()
+    dt = time.perf_counter() - t0
+    o.close()
+    nv = int(np.prod(c.cell_dim))
+    return {"value": nv * r["iterations"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d Green iteration(s) of mechanical step 0 of the 128^3 workload (%d voxel-iterations), "
+                      "%.1f s" % (r["iterations"], nv * r["iterations"], dt)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return
+    import pyoracle
+    from mth import capi, synth
+    cfg = workload_cfg(args)
+    c = synth.Config(**{**cfg.__dict__})
+    c.iter_max = 1
+    grain, phase, euler = synth.microstructure(c)
+    cores = os.cpu_count() or 1
+    o = pyoracle.Oracle(capi.params_from_config(c), grain, phase, euler, nthreads=cores)
+    for _ in range(args.warmup):
+        o.step()
+    nv = int(np.prod(c.cell_dim))
+    t0 = time.perf_counter()
+    its = 0
+    for _ in range(args.steps):
+        its += o.step()["iterations"]
+    dt = time.perf_counter() - t0
+    o.close()
+    value = nv * its / dt
+    sample = "one Green iteration per step of the 128^3 workload (%d voxel-iterations per step)" % nv
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+           "data": "synthetic: seeded periodic Voronoi, 512 grains, uniform SO(3) orientations, 40 radius-3 pores",
+           "config": {"workload": "128^3 RVE, 512 grains, 40 pores, FCC Cu power law n=10 + Voce, uniaxial "
+                                  "tension eps33_dot=1/s, dt=1e-3", "grid": list(c.cell_dim),
+                      "parallelism": "OpenMP %d threads" % cores},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

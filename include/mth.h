@@ -78,7 +78,7 @@ typedef struct {
   int    hard_flag;          /* Hard_Flag: Voce hardening */
   int    precision;          /* mth_precision */
   double newton_tol;         /* local Newton tolerance; <=0 selects the default
-                                (1e-10 FP64 as in src/evolution.c:104, 1e-7 mixed) */
+                                (1e-10 FP64 as in src/evolution.c:104, 1e-6 mixed) */
   int    newton_itmax;       /* <=0 selects 500 (src/evolution.c:105) */
   /* Phase-field / DRX block (src/io.c:71-90) */
   double pf_length_scale;    /* dx [m] */
@@ -95,6 +95,7 @@ typedef struct {
   double rho_k;              /* rho = rho0 + rho_k * accumulated slip [1e12/m^2] */
   int    pf_substeps;        /* PF substeps per mechanical step */
   uint64_t seed;             /* counter-based RNG seed */
+  int    device;             /* CUDA device ordinal the context runs on */
 } mth_params;
 
 /* Per-step record; the reference prints the scalars to vm.out
@@ -163,6 +164,23 @@ mth_status mth_local_solve(const mth_params* params, const double c066[36], size
                            const double* rot, const double* crss, double* edot,
                            double* err, long long* newton_iters);
 
+/* Per-kernel device timing.  When enabled, every kernel launch of the context
+ * is bracketed by CUDA events on the context's stream; times are summed per
+ * kernel class.  Launch counts are kept whether or not timing is enabled.
+ * The reference has no timers (no MPI_Wtime in src/); this replaces ad hoc
+ * printf timing for the benchmark. */
+#define MTH_PROF_MAX 16
+typedef struct {
+  int       n_kernels;
+  char      name[MTH_PROF_MAX][32];
+  double    ms[MTH_PROF_MAX];           /* summed device time per class */
+  long long launches[MTH_PROF_MAX];     /* launches per class */
+  double    bytes[MTH_PROF_MAX];        /* algorithmic HBM bytes moved, summed */
+  long long total_launches;
+} mth_profile;
+mth_status mth_profile_enable(mth_ctx* ctx, int on);
+mth_status mth_profile_read(mth_ctx* ctx, mth_profile* out, int reset);
+
 /* Host-side readers for the reference's input files. */
 /* input.in namelist (src/io.c:96-164); fills params and copies the file
  * names of the .sx files and the microstructure. */
@@ -171,8 +189,10 @@ mth_status mth_read_namelist(const char* path, mth_params* params,
                              size_t path_cap);
 /* single-crystal .sx file (src/init.c:52-231) into params->phase[iphase]. */
 mth_status mth_read_sx(const char* path, mth_params* params, int iphase);
-/* voxel microstructure text (src/init.c:255-270): n voxels, z fastest. */
-mth_status mth_read_microstructure(const char* path, size_t n, int* grain, int* phase,
+/* voxel microstructure text (src/init.c:255-270): cell_dim[0]*cell_dim[1]*
+ * cell_dim[2] lines, z fastest; the i,j,k columns are checked against the
+ * line order as the reference does (src/init.c:262-266). */
+mth_status mth_read_microstructure(const char* path, const int cell_dim[3], int* grain, int* phase,
                                    double* euler_deg);
 
 #ifdef __cplusplus

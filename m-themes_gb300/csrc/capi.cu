@@ -1,0 +1,957 @@
+// capi.cu -- host orchestration and the extern "C" entry points of
+// include/mth.h: context creation (SetupJob, src/init.c:727-1205), one
+// mechanical step (the istep loop body of Evolution, src/evolution.c:
+// 1319-1693, power-law path), field download and the batch local solve.
+//
+// The macroscopic bookkeeping of get_smacro (src/evolution.c:473-547), the
+// error normalisation (src/evolution.c:1430-1455) and the end-of-step macro
+// updates (src/evolution.c:1471-1535,1691-1693) run on the host in FP64 on
+// the reduced sums that the kernels produce; everything per voxel or per
+// wave vector runs on the GPU.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+#include "../../include/mth.h"
+#include "mth_common.cuh"
+#include "mth_internal.h"
+
+using namespace mth;
+
+static thread_local char g_err[512] = "";
+
+static mth_status set_err(mth_status s, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return s;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return set_err(MTH_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                     __FILE__, __LINE__);                                                     \
+  } while (0)
+
+extern "C" const char* mth_version(void) { return "mth-gb300 0.1 (sm_103a)"; }
+extern "C" const char* mth_last_error(void) { return g_err; }
+
+// ------------------------------------------------------------ host math
+namespace {
+typedef double t33[3][3];
+
+const double Bh[6][3][3] = {
+    {{-RSQ2, 0, 0}, {0, RSQ2, 0}, {0, 0, 0}},
+    {{-RSQ6, 0, 0}, {0, -RSQ6, 0}, {0, 0, 2. * RSQ6}},
+    {{0, 0, 0}, {0, 0, RSQ2}, {0, RSQ2, 0}},
+    {{0, 0, RSQ2}, {0, 0, 0}, {RSQ2, 0, 0}},
+    {{0, RSQ2, 0}, {RSQ2, 0, 0}, {0, 0, 0}},
+    {{RSQ3, 0, 0}, {0, RSQ3, 0}, {0, 0, RSQ3}}};
+
+void t2v(const t33 t, double* v, int nv) {
+  for (int i = 0; i < nv; i++) {
+    double s = 0;
+    for (int m = 0; m < 3; m++)
+      for (int n = 0; n < 3; n++) s += t[m][n] * Bh[i][m][n];
+    v[i] = s;
+  }
+}
+void v2t(const double* v, t33 t, int nv) {
+  for (int m = 0; m < 3; m++)
+    for (int n = 0; n < 3; n++) {
+      double s = 0;
+      for (int i = 0; i < nv; i++) s += v[i] * Bh[i][m][n];
+      t[m][n] = s;
+    }
+}
+void m2t4(const double c[6][6], double* t /*81*/) {
+  for (int m = 0; m < 3; m++)
+    for (int n = 0; n < 3; n++)
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++) {
+          double s = 0;
+          for (int i = 0; i < 6; i++)
+            for (int j = 0; j < 6; j++) s += c[i][j] * Bh[i][m][n] * Bh[j][k][l];
+          t[((m * 3 + n) * 3 + k) * 3 + l] = s;
+        }
+}
+// Gauss-Jordan inverse with partial pivoting; false if singular.
+bool inv6(const double a[6][6], double out[6][6]) {
+  double m[6][12];
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 12; j++) m[i][j] = j < 6 ? a[i][j] : (double)(j - 6 == i);
+  for (int c = 0; c < 6; c++) {
+    int p = c;
+    for (int r = c + 1; r < 6; r++)
+      if (fabs(m[r][c]) > fabs(m[p][c])) p = r;
+    if (fabs(m[p][c]) < 1e-300) return false;
+    if (p != c)
+      for (int j = 0; j < 12; j++) { double t = m[p][j]; m[p][j] = m[c][j]; m[c][j] = t; }
+    double id = 1.0 / m[c][c];
+    for (int j = 0; j < 12; j++) m[c][j] *= id;
+    for (int r = 0; r < 6; r++)
+      if (r != c) {
+        double f = m[r][c];
+        if (f != 0.0)
+          for (int j = 0; j < 12; j++) m[r][j] -= f * m[c][j];
+      }
+  }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) out[i][j] = m[i][j + 6];
+  return true;
+}
+double von_mises(const t33 t) {
+  double tr = t[0][0] + t[1][1] + t[2][2], vm = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double d = (t[i][j] + t[j][i]) / 2. - (double)(i == j) * tr / 3.0;
+      vm += d * d;
+    }
+  return sqrt(2. / 3. * vm);
+}
+void voigt_to_full(const double* v, t33 m) {
+  m[0][0] = v[0]; m[0][1] = v[5]; m[0][2] = v[4];
+  m[1][0] = v[5]; m[1][1] = v[1]; m[1][2] = v[3];
+  m[2][0] = v[4]; m[2][1] = v[3]; m[2][2] = v[2];
+}
+bool radix_ok(int n) {
+  if (n < 2 || (n & 1)) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+// Phase constants: PlasticInit (src/init.c:52-231) normalisation of the slip
+// vectors, Schmid tensors in crystal axes, hardening matrix and the
+// tau1/thet checks; crystal-axes stiffness/compliance, diagonal in the LT
+// basis for cubic symmetry.
+mth_status fill_phase(const mth_phase& in, PhaseConst& ph) {
+  memset(&ph, 0, sizeof(ph));
+  ph.type = in.type;
+  const double ev[6] = {in.c11 - in.c12, in.c11 - in.c12, 2 * in.c44, 2 * in.c44, 2 * in.c44, in.c11 + 2 * in.c12};
+  for (int i = 0; i < 6; i++) {
+    ph.c_xt[i] = ev[i];
+    ph.s_xt[i] = ev[i] != 0.0 ? 1.0 / ev[i] : 0.0;
+  }
+  if (in.type != 0) return MTH_OK;
+  if (in.nsys <= 0 || in.nsys > NSYS) return set_err(MTH_ERR_ARG, "nsys=%d out of range", in.nsys);
+  for (int i = 0; i < 5; i++)
+    if (!(ev[i] > 0)) return set_err(MTH_ERR_SINGULAR, "elastic constants not positive definite");
+  double tau1 = in.tau1, thet0 = in.thet0, thet1 = in.thet1;
+  if (thet0 < thet1) return set_err(MTH_ERR_ARG, "Initial hardening rate is lower than final hardening rate");
+  if (tau1 < 1.e-6) { tau1 = 1.e-6; thet0 = thet1; }
+  ph.nsys = in.nsys;
+  ph.nrs = in.nrs;
+  ph.gamd0 = in.gamd0;
+  ph.tau0f = in.tau0f;
+  ph.tau_back_minus_fwd = in.tau0b - in.tau0f;
+  ph.tau1 = tau1;
+  ph.thet0 = thet0;
+  ph.thet1 = thet1;
+  ph.nrs_int = (in.nrs == floor(in.nrs) && in.nrs >= 1 && in.nrs <= 64) ? (int)in.nrs : 0;
+  if (!(in.tau0f > 0) || !(in.tau0b > 0)) return set_err(MTH_ERR_ARG, "CRSS must be positive");
+  for (int j = 0; j < ph.nsys; j++) {
+    double nn = sqrt(in.bn[j][0] * in.bn[j][0] + in.bn[j][1] * in.bn[j][1] + in.bn[j][2] * in.bn[j][2]);
+    double nb = sqrt(in.bb[j][0] * in.bb[j][0] + in.bb[j][1] * in.bb[j][1] + in.bb[j][2] * in.bb[j][2]);
+    if (!(nn > 0) || !(nb > 0)) return set_err(MTH_ERR_ARG, "zero slip vector in system %d", j);
+    double dot = 0;
+    for (int m = 0; m < 3; m++) {
+      ph.bn[j][m] = in.bn[j][m] / nn;
+      ph.bb[j][m] = in.bb[j][m] / nb;
+      dot += ph.bn[j][m] * ph.bb[j][m];
+    }
+    if (dot > 1e-3) return set_err(MTH_ERR_ARG, "Slip systems is NOT orthogonal (system %d)", j);
+    t33 a;
+    for (int m = 0; m < 3; m++)
+      for (int n = 0; n < 3; n++) a[m][n] = (ph.bn[j][m] * ph.bb[j][n] + ph.bn[j][n] * ph.bb[j][m]) / 2.0;
+    t2v(a, ph.m_xt[j], 5);
+  }
+  for (int i = 0; i < ph.nsys; i++)
+    for (int j = 0; j < ph.nsys; j++) ph.hard[i][j] = (i == j) ? in.hself : in.hlat;
+  return MTH_OK;
+}
+}  // namespace
+
+
+namespace {
+int pkh(int i, int j) {
+  if (i > j) { int t = i; i = j; j = t; }
+  return i * 5 - (i * (i - 1)) / 2 + (j - i);
+}
+// Crystal->sample matrix of Bunge angles in degrees: the transpose of
+// EulerToTransMatrix opt 2 (src/kinematics.c:221-232, src/init.c:273-278).
+void euler_to_rot(const double* e, double R[9]) {
+  const double d2r = 3.14159265359 / 180.;
+  const double t1 = e[0] * d2r, p = e[1] * d2r, t2 = e[2] * d2r;
+  const double ct1 = cos(t1), st1 = sin(t1), cph = cos(p), sph = sin(p), ct2 = cos(t2), st2 = sin(t2);
+  double a[3][3];
+  a[0][0] = ct1 * ct2 - st1 * st2 * cph;
+  a[0][1] = st1 * ct2 + ct1 * st2 * cph;
+  a[0][2] = st2 * sph;
+  a[1][0] = -1.0 * ct1 * st2 - st1 * ct2 * cph;
+  a[1][1] = -1.0 * st1 * st2 + ct1 * ct2 * cph;
+  a[1][2] = ct2 * sph;
+  a[2][0] = st1 * sph;
+  a[2][1] = -1.0 * ct1 * sph;
+  a[2][2] = cph;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[i * 3 + j] = a[j][i];
+}
+// Elastic-class row without the S066 part: C_gr and S_gr = C_gr^-1 of a
+// cubic crystal at rotation R, Q^T diag(.) Q in the LT basis.
+void class_row(const PhaseConst& ph, const double R[9], double* row) {
+  double Q[25];
+  rot_to_q<double>(R, Q);
+  for (int i = 0; i < ETAB_W; i++) row[i] = 0.0;
+  for (int i = 0; i < 5; i++)
+    for (int j = i; j < 5; j++) {
+      double c = 0, s = 0;
+      for (int k = 0; k < 5; k++) {
+        c += Q[k * 5 + i] * ph.c_xt[k] * Q[k * 5 + j];
+        s += Q[k * 5 + i] * ph.s_xt[k] * Q[k * 5 + j];
+      }
+      row[ET_CGR + pkh(i, j)] = c;
+      row[ET_SEL + pkh(i, j)] = s;
+    }
+  row[ET_CGR_HH] = ph.c_xt[5];
+  row[ET_SEL_HH] = ph.s_xt[5];
+}
+void class_row_add_s0(double* row, const double s066[6][6]) {
+  for (int i = 0; i < 5; i++)
+    for (int j = i; j < 5; j++) row[ET_STOT + pkh(i, j)] = s066[i][j] + row[ET_SEL + pkh(i, j)];
+}
+}  // namespace
+
+bool mth::make_plan(int n, FftPlan* p) {
+  p->n = n;
+  p->nst = 0;
+  int m = n;
+  while (m % 4 == 0) { p->radix[p->nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { p->radix[p->nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { p->radix[p->nst++] = 3; m /= 3; }
+  return m == 1 && p->nst <= 8;
+}
+
+// ---------------------------------------------------------------- context
+struct mth_ctx {
+  mth_params p;
+  int mixed;
+  int n[3];
+  long long nv;
+  FftGeom geom;
+  NewtonConst nc;
+  GreenConst gc;
+  cudaStream_t st;
+  int nblocks;
+  // device memory
+  void* fieldmem;
+  Fields<float> ff;
+  Fields<double> fd;
+  void* spec;
+  void* anti;
+  uint8_t* phase_d;
+  int* grain_d;
+  int* eclass_d;
+  double* etab_d;
+  int nclass;
+  double* partials;
+  double* red;
+  double* red_h;  // pinned
+  void* tw[3][2]; // per axis, forward/inverse
+  // profiling
+  int prof_on;
+  double prof_ms[MTH_PROF_MAX];
+  double prof_bytes[MTH_PROF_MAX];
+  long long prof_launch[MTH_PROF_MAX];
+  std::vector<cudaEvent_t>* ev_pool;
+  std::vector<int>* ev_pending;   // class of each pending pair (events 2i, 2i+1)
+  // macro state (FP64, host)
+  t33 udot, udot_s, udot_a, scauchy;
+  int vbc[6], sbc[6], creep;
+  t33 disgrad_avg, disgrad_avg_t, ddg, ddg_acum, ddg_applied, sig_avg, sig_avg1;
+  double c066[6][6], s066[6][6], s0_4[81];
+  double wgt, wgt_ph1, e_vm, d_vm, s_vm, s_vm1, err_e, err_s, time_tot;
+  int istep;
+  int uploaded;
+};
+
+static void ctx_free(mth_ctx* c) {
+  if (!c) return;
+  cudaFree(c->fieldmem);
+  cudaFree(c->spec);
+  cudaFree(c->anti);
+  cudaFree(c->phase_d);
+  cudaFree(c->grain_d);
+  cudaFree(c->eclass_d);
+  cudaFree(c->etab_d);
+  cudaFree(c->partials);
+  cudaFree(c->red);
+  if (c->red_h) cudaFreeHost(c->red_h);
+  for (int a = 0; a < 3; a++)
+    for (int d = 0; d < 2; d++) cudaFree(c->tw[a][d]);
+  if (c->st) cudaStreamDestroy(c->st);
+  if (c->ev_pool) {
+    for (cudaEvent_t e : *c->ev_pool) cudaEventDestroy(e);
+    delete c->ev_pool;
+  }
+  delete c->ev_pending;
+  delete c;
+}
+
+// ------------------------------------------------------------- profiling
+enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_NCLASS };
+static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain",
+                                        "newton", "reduce", "end_step", "spin_fft", "setup"};
+
+static void prof_begin(mth_ctx* c) {
+  if (!c->prof_on) return;
+  size_t i = c->ev_pending->size();
+  if (c->ev_pool->size() < 2 * (i + 1)) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    c->ev_pool->push_back(a);
+    c->ev_pool->push_back(b);
+  }
+  cudaEventRecord((*c->ev_pool)[2 * i], c->st);
+}
+static void prof_end(mth_ctx* c, int cls, double bytes) {
+  c->prof_launch[cls]++;
+  c->prof_bytes[cls] += bytes;
+  if (!c->prof_on) return;
+  size_t i = c->ev_pending->size();
+  cudaEventRecord((*c->ev_pool)[2 * i + 1], c->st);
+  c->ev_pending->push_back(cls);
+}
+// after the stream has been synchronised
+static void prof_resolve(mth_ctx* c) {
+  if (!c->ev_pending) return;
+  for (size_t i = 0; i < c->ev_pending->size(); i++) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, (*c->ev_pool)[2 * i], (*c->ev_pool)[2 * i + 1]) == cudaSuccess)
+      c->prof_ms[(*c->ev_pending)[i]] += ms;
+  }
+  c->ev_pending->clear();
+}
+#define LAUNCH(cls, bytes, call)          \
+  do {                                    \
+    prof_begin(c);                        \
+    cudaError_t e__ = (call);             \
+    prof_end(c, cls, (double)(bytes));    \
+    if (e__ != cudaSuccess) CK(e__);      \
+  } while (0)
+
+template <typename T>
+static mth_status make_twiddles(int n, int sign, void** out) {
+  std::vector<c2<T>> h(n);
+  for (int k = 0; k < n; k++) {
+    long double a = (long double)sign * 2.0L * 3.14159265358979323846264338327950288L * (long double)k / (long double)n;
+    h[k].x = (T)cosl(a);
+    h[k].y = (T)sinl(a);
+  }
+  CK(cudaMalloc(out, sizeof(c2<T>) * n));
+  CK(cudaMemcpy(*out, h.data(), sizeof(c2<T>) * n, cudaMemcpyHostToDevice));
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
+  if (!p || !out) return set_err(MTH_ERR_ARG, "null argument");
+  *out = nullptr;
+  for (int i = 0; i < 3; i++)
+    if (!radix_ok(p->cell_dim[i]) || p->cell_dim[i] > 512)
+      return set_err(MTH_ERR_UNSUPPORTED, "CellDim[%d]=%d: each edge must be even, of the form 2^a 3^b, <= 512", i,
+                     p->cell_dim[i]);
+  if (p->n_phases < 1 || p->n_phases > MTH_NPH_MAX) return set_err(MTH_ERR_ARG, "N_phases=%d", p->n_phases);
+  if (p->iter_max < 1) return set_err(MTH_ERR_ARG, "IterMax must be >= 1");
+  if (!(p->time_step > 0)) return set_err(MTH_ERR_ARG, "TimeStep must be > 0");
+  if (p->precision != MTH_FP64 && p->precision != MTH_MIXED) return set_err(MTH_ERR_ARG, "precision");
+  mth_ctx* c = new mth_ctx();
+  memset(c, 0, sizeof(*c));
+  c->p = *p;
+  c->mixed = p->precision == MTH_MIXED;
+  for (int i = 0; i < 3; i++) c->n[i] = p->cell_dim[i];
+  c->nv = (long long)c->n[0] * c->n[1] * c->n[2];
+  c->wgt = 1.0 / (double)c->nv;
+  for (int k = 0; k < p->n_phases; k++) {
+    mth_status s = fill_phase(p->phase[k], c->nc.ph[k]);
+    if (s) { delete c; return s; }
+  }
+  c->nc.dt = p->time_step;
+  c->nc.tol = p->newton_tol > 0 ? p->newton_tol : (c->mixed ? 1e-6 : 1e-10);
+  c->nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
+  // boundary conditions (src/init.c:861-900)
+  double vb[6];
+  for (int i = 0; i < 6; i++) {
+    c->vbc[i] = p->velgrad_bc_flag[i];
+    c->sbc[i] = p->stress_bc_flag[i];
+    vb[i] = p->velgrad_bc[i] * c->vbc[i];
+  }
+  if (c->vbc[0] + c->vbc[1] + c->vbc[2] == 2) {
+    delete c;
+    return set_err(MTH_ERR_ARG, "Cannot enforce only two deviatoric components (Check input VelGrad_BC_Flag)");
+  }
+  for (int i = 0; i < 6; i++)
+    if ((c->sbc[i] * c->vbc[i] != 0) || (c->sbc[i] + c->vbc[i] != 1)) {
+      delete c;
+      return set_err(MTH_ERR_ARG, "Check boundary conditions on strain rate and stress");
+    }
+  voigt_to_full(vb, c->udot);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      c->udot_s[i][j] = (c->udot[i][j] + c->udot[j][i]) / 2.;
+      c->udot_a[i][j] = (c->udot[i][j] - c->udot[j][i]) / 2.;
+    }
+  {
+    double d6[6];
+    t33 dev;
+    t2v(c->udot_s, d6, 6);
+    v2t(d6, dev, 5);
+    double s = 0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) s += dev[i][j] * dev[i][j];
+    c->d_vm = sqrt(2. / 3. * s);
+  }
+  c->creep = 0;
+  for (int i = 0; i < 6; i++) c->creep += c->sbc[i];
+  c->creep /= 6;
+  if (c->creep) { delete c; return set_err(MTH_ERR_UNSUPPORTED, "all-stress (creep) boundary conditions"); }
+  voigt_to_full(p->stress_bc, c->scauchy);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) c->disgrad_avg[i][j] = c->udot[i][j] * p->time_step;
+  c->e_vm = c->d_vm * p->time_step;
+
+  // geometry and plans
+  FftGeom& g = c->geom;
+  g.n0 = c->n[0]; g.n1 = c->n[1]; g.n2 = c->n[2];
+  g.kz = g.n2 / 2 + 1;
+  g.plane = c->nv;
+  g.kplane = (long long)g.n0 * g.n1 * g.kz;
+  make_plan(g.n0, &g.px);
+  make_plan(g.n1, &g.py);
+  make_plan(g.n2, &g.pz);
+  g.smem_budget = 100 * 1024;
+  c->nblocks = (int)((c->nv + 255) / 256);
+  c->ev_pool = new std::vector<cudaEvent_t>();
+  c->ev_pending = new std::vector<int>();
+
+  {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) { delete c; return set_err(MTH_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e)); }
+    if (p->device < 0 || p->device >= ndev) { delete c; return set_err(MTH_ERR_ARG, "device %d of %d", p->device, ndev); }
+    e = cudaSetDevice(p->device);
+    if (e != cudaSuccess) { delete c; return set_err(MTH_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e)); }
+  }
+  mth_status s = MTH_OK;
+#define CKC(call)                                                                                  \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) {                                                                       \
+      s = set_err(e_ == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "%s: %s", #call, \
+                  cudaGetErrorString(e_));                                                         \
+      ctx_free(c);                                                                                 \
+      return s;                                                                                    \
+    }                                                                                              \
+  } while (0)
+  CKC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
+  const long long P = c->nv;
+  const int nplanes = 6 + 6 + 6 + 6 + 9 + 12 + 1 + 3;
+  CKC(cudaMalloc(&c->fieldmem, esz * P * nplanes));
+  CKC(cudaMalloc(&c->spec, 2 * esz * g.kplane * 6));
+  CKC(cudaMalloc(&c->anti, 2 * esz * g.kplane * 3));
+  CKC(cudaMalloc(&c->phase_d, P));
+  CKC(cudaMalloc(&c->grain_d, sizeof(int) * P));
+  CKC(cudaMalloc(&c->eclass_d, sizeof(int) * P));
+  CKC(cudaMalloc(&c->partials, sizeof(double) * 21 * c->nblocks));
+  CKC(cudaMalloc(&c->red, sizeof(double) * 32));
+  CKC(cudaMallocHost(&c->red_h, sizeof(double) * 32));
+  auto carve = [&](auto* base, auto& f) {
+    long long o = 0;
+    f.sig = base + o; o += 6 * P;
+    f.strain = base + o; o += 6 * P;
+    f.epsp = base + o; o += 6 * P;
+    f.edot = base + o; o += 6 * P;
+    f.rot = base + o; o += 9 * P;
+    f.crss = base + o; o += 12 * P;
+    f.gamacum = base + o; o += P;
+    f.wspin = base + o; o += 3 * P;
+    f.phase = c->phase_d;
+    f.eclass = c->eclass_d;
+    f.etab = nullptr;
+    f.nv = P;
+  };
+  if (c->mixed) carve(static_cast<float*>(c->fieldmem), c->ff);
+  else carve(static_cast<double*>(c->fieldmem), c->fd);
+  for (int a = 0; a < 3; a++)
+    for (int d = 0; d < 2; d++) {
+      mth_status t = c->mixed ? make_twiddles<float>(c->n[a], d == 0 ? -1 : 1, &c->tw[a][d])
+                              : make_twiddles<double>(c->n[a], d == 0 ? -1 : 1, &c->tw[a][d]);
+      if (t) { ctx_free(c); return t; }
+    }
+#undef CKC
+  *out = c;
+  return MTH_OK;
+}
+
+#define SETDEV(c) CK(cudaSetDevice((c)->p.device))
+
+extern "C" mth_status mth_destroy(mth_ctx* c) {
+  if (!c) return set_err(MTH_ERR_ARG, "null context");
+  SETDEV(c);
+  cudaStreamSynchronize(c->st);
+  ctx_free(c);
+  return MTH_OK;
+}
+
+static mth_status reduce_to_host(mth_ctx* c, int width, double* out) {
+  LAUNCH(K_REDUCE, 8.0 * width * (c->nblocks + 1), launch_reduce_partials(c->partials, c->nblocks, width, c->red, c->st));
+  CK(cudaMemcpyAsync(c->red_h, c->red, sizeof(double) * width, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  prof_resolve(c);
+  memcpy(out, c->red_h, sizeof(double) * width);
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, const int* phase,
+                                                const double* euler_deg, size_t n) {
+  if (!c || !grain || !phase || !euler_deg) return set_err(MTH_ERR_ARG, "null argument");
+  if ((long long)n != c->nv) return set_err(MTH_ERR_ARG, "n_voxels=%zu but CellDim gives %lld", n, c->nv);
+  SETDEV(c);
+  std::vector<uint8_t> ph(n);
+  std::vector<int> ecl(n, 0);
+  // elastic classes: voxels of equal phase and initial Euler angles share
+  // C_gr (src/init.c:272-283); C066 is their voxel-weighted average
+  std::map<std::tuple<int, double, double, double>, int> key2class;
+  std::vector<double> rows;
+  std::vector<long long> counts;
+  long long nph1 = 0;
+  for (size_t v = 0; v < n; v++) {
+    if (phase[v] < 1 || phase[v] > c->p.n_phases)
+      return set_err(MTH_ERR_ARG, "voxel %zu has phase %d (N_phases=%d)", v, phase[v], c->p.n_phases);
+    ph[v] = (uint8_t)(phase[v] - 1);
+    if (phase[v] == 1) nph1++;
+    const PhaseConst& pc = c->nc.ph[phase[v] - 1];
+    if (pc.type != 0) continue;
+    const double* e = euler_deg + 3 * v;
+    auto key = std::make_tuple(phase[v], e[0], e[1], e[2]);
+    auto it = key2class.find(key);
+    int k;
+    if (it == key2class.end()) {
+      k = (int)counts.size();
+      key2class.emplace(key, k);
+      counts.push_back(0);
+      rows.resize(rows.size() + ETAB_W);
+      double R[9];
+      euler_to_rot(e, R);
+      class_row(pc, R, &rows[(size_t)k * ETAB_W]);
+    } else {
+      k = it->second;
+    }
+    counts[k]++;
+    ecl[v] = k;
+  }
+  if (counts.empty()) return set_err(MTH_ERR_ARG, "no crystal voxel in the microstructure");
+  memset(c->c066, 0, sizeof(c->c066));
+  for (size_t k = 0; k < counts.size(); k++) {
+    const double* r = &rows[k * ETAB_W];
+    for (int i = 0; i < 5; i++)
+      for (int j = 0; j < 5; j++) c->c066[i][j] += (double)counts[k] * r[ET_CGR + pkh(i, j)];
+    c->c066[5][5] += (double)counts[k] * r[ET_CGR_HH];
+  }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) c->c066[i][j] *= c->wgt;
+  c->wgt_ph1 = (double)nph1 * c->wgt;
+  if (!inv6(c->c066, c->s066)) return set_err(MTH_ERR_SINGULAR, "reference stiffness C066 is singular");
+  for (size_t k = 0; k < counts.size(); k++) class_row_add_s0(&rows[k * ETAB_W], c->s066);
+  m2t4(c->c066, c->gc.c0);
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) c->gc.s066[i * 6 + j] = c->s066[i][j];
+  c->gc.elast_bc = c->p.elast_bc;
+  m2t4(c->s066, c->s0_4);
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 5; j++) c->nc.s0dev[i * 5 + j] = c->s066[i][j];
+  c->nc.s0hh = c->s066[5][5];
+  cudaFree(c->etab_d);
+  c->etab_d = nullptr;
+  c->nclass = (int)counts.size();
+  CK(cudaMalloc(&c->etab_d, sizeof(double) * rows.size()));
+  c->ff.etab = c->etab_d;
+  c->fd.etab = c->etab_d;
+  double* eul_d = nullptr;
+  CK(cudaMalloc(&eul_d, sizeof(double) * 3 * n));
+  CK(cudaMemcpyAsync(c->etab_d, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(eul_d, euler_deg, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->phase_d, ph.data(), n, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->grain_d, grain, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->eclass_d, ecl.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+  double d6[6];
+  t2v(c->disgrad_avg, d6, 6);
+  const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+  LAUNCH(K_SETUP, 0.0, launch_setup(c->mixed, c->nc, f, eul_d, d6, c->nblocks, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  prof_resolve(c);
+  cudaFree(eul_d);
+  c->uploaded = 1;
+  c->istep = 0;
+  return MTH_OK;
+}
+
+// get_smacro (src/evolution.c:473-547) on the reduced sums.  The von Mises
+// stress keeps the reference's formula, whose out-of-bounds word
+// SigDevAvg[3][3] (src/evolution.c:531) holds SigAvg1[0][0] in the reference
+// as built with g++ (SigAvg1 is laid out right after SigDevAvg's padding).
+static void get_smacro(mth_ctx* c, const double* red) {
+  static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
+  double s6[6], s16[6];
+  for (int i = 0; i < 6; i++) {
+    s6[i] = red[2 + i] * c->wgt;
+    s16[i] = red[8 + i] * (c->wgt / c->wgt_ph1);
+  }
+  v2t(s6, c->sig_avg, 6);
+  v2t(s16, c->sig_avg1, 6);
+  for (int a = 0; a < 6; a++) {
+    int ii = IJV[0][a], jj = IJV[1][a];
+    c->ddg[ii][jj] = 0.0;
+    if (c->vbc[a] == 0)
+      for (int b = 0; b < 6; b++) {
+        int kk = IJV[0][b], ll = IJV[1][b];
+        c->ddg[ii][jj] += c->s0_4[((ii * 3 + jj) * 3 + kk) * 3 + ll] * c->sbc[b] * (c->scauchy[kk][ll] - c->sig_avg[kk][ll]);
+      }
+  }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) c->ddg_acum[i][j] += c->ddg[i][j];
+  t33 dev;
+  double v6[6];
+  t2v(c->sig_avg, v6, 6);
+  v2t(v6, dev, 5);
+  const double oob = c->sig_avg1[0][0];
+  double svm = 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      if (i != j) svm += dev[i][j] * dev[i][j];
+      else {
+        double d = dev[i][j] - (dev[1][1] + dev[2][2] + oob) / 3.0;
+        svm += d * d;
+      }
+    }
+  c->s_vm = sqrt(3. / 2. * svm);
+  t2v(c->sig_avg1, v6, 6);
+  v2t(v6, dev, 5);
+  double svm1 = 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) svm1 += dev[i][j] * dev[i][j];
+  c->s_vm1 = sqrt(3. / 2. * svm1);
+}
+
+template <typename T>
+static mth_status green_iteration(mth_ctx* c, const AddVec& add) {
+  const FftGeom& g = c->geom;
+  Fields<T>& f = *reinterpret_cast<Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
+  c2<T>* spec = static_cast<c2<T>*>(c->spec);
+  c2<T>* anti = static_cast<c2<T>*>(c->anti);
+  auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
+  // algorithmic bytes: real plane = w*nv, complex spectrum plane = 2w*kplane
+  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.kplane;
+  LAUNCH(K_FFT_Z_R2C, 6 * rp + 6 * kp, launch_fft_z_r2c<T>(g, f.sig, spec, 6, tw(2, 0), c->st));
+  LAUNCH(K_FFT_Y, 12 * kp, launch_fft_strided<T>(g, spec, 6, 1, -1, tw(1, 0), c->st));
+  LAUNCH(K_FFT_X_GREEN, 12 * kp + 6 * kp, launch_fft_x_green<T>(g, c->gc, spec, anti, tw(0, 0), tw(0, 1), c->st));
+  LAUNCH(K_FFT_Y, 12 * kp, launch_fft_strided<T>(g, spec, 6, 1, +1, tw(1, 1), c->st));
+  LAUNCH(K_FFT_Z_C2R, 6 * kp + 12 * rp,
+         launch_fft_z_c2r<T>(g, spec, f.strain, 6, tw(2, 1), (T)(1.0 / (double)c->nv), add, 1, c->st));
+  // Newton: read sigma, strain, eps_p (18), rot (9), CRSS (12); write sigma, edot (12);
+  // phase (1 B) and elastic class (4 B) per voxel
+  LAUNCH(K_NEWTON, (18 + 9 + 12 + 12) * rp + 5.0 * (double)c->nv,
+         launch_newton(c->mixed, c->nc, &f, c->partials, c->nblocks, c->st));
+  return MTH_OK;
+}
+
+template <typename T>
+static mth_status spin_field(mth_ctx* c) {
+  const FftGeom& g = c->geom;
+  Fields<T>& f = *reinterpret_cast<Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
+  c2<T>* anti = static_cast<c2<T>*>(c->anti);
+  auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
+  AddVec zero;
+  memset(&zero, 0, sizeof(zero));
+  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.kplane;
+  LAUNCH(K_SPIN, 6 * kp, launch_fft_strided<T>(g, anti, 3, 0, +1, tw(0, 1), c->st));
+  LAUNCH(K_SPIN, 6 * kp, launch_fft_strided<T>(g, anti, 3, 1, +1, tw(1, 1), c->st));
+  LAUNCH(K_SPIN, 3 * kp + 3 * rp, launch_fft_z_c2r<T>(g, anti, f.wspin, 3, tw(2, 1), (T)(1.0 / (double)c->nv), zero, 0, c->st));
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
+  if (!c) return set_err(MTH_ERR_ARG, "null context");
+  if (!c->uploaded) return set_err(MTH_ERR_STATE, "mth_step before mth_upload_microstructure");
+  SETDEV(c);
+  const int istep = c->istep;
+  const double dt = c->p.time_step;
+  c->nc.flow_off = (istep == 0 && c->p.update_flag != 1) ? 1 : 0;
+  memset(c->ddg, 0, sizeof(c->ddg));
+  memset(c->ddg_acum, 0, sizeof(c->ddg_acum));
+  memset(c->ddg_applied, 0, sizeof(c->ddg_applied));
+  const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
+  CK(cudaMemsetAsync(c->anti, 0, 2 * esz * c->geom.kplane * 3, c->st));
+  int iter = 0;
+  c->err_e = 2. * c->p.err;
+  c->err_s = 2. * c->p.err;
+  long long nit = 0, nbad = 0;
+  while (iter < c->p.iter_max && fmax(fabs(c->err_s), fabs(c->err_e)) > c->p.err) {
+    iter++;
+    // uniform strain added this iteration: dDisGradAvg of the previous
+    // get_smacro, plus Udot dt on the first one (src/evolution.c:1319-1332)
+    t33 u;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        u[i][j] = c->ddg[i][j] + (iter == 1 ? c->udot[i][j] * dt : 0.0);
+        c->ddg_applied[i][j] += c->ddg[i][j];
+      }
+    AddVec add;
+    t2v(u, add.v, 6);
+    mth_status s = c->mixed ? green_iteration<float>(c, add) : green_iteration<double>(c, add);
+    if (s) return s;
+    double red[NPART];
+    s = reduce_to_host(c, NPART, red);
+    if (s) return s;
+    for (int i = 0; i < NPART; i++)
+      if (!std::isfinite(red[i])) return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", istep, iter);
+    nit += (long long)red[14];
+    nbad += (long long)red[15];
+    c->err_s = red[0] * c->wgt;
+    c->err_e = red[1] * c->wgt;
+    get_smacro(c, red);
+    if (fabs(c->e_vm) < 1E-5) c->err_e = 0.0;
+    else c->err_e /= c->e_vm;
+    c->err_s /= c->s_vm;
+  }
+  // end of step (src/evolution.c:1471-1546)
+  t33 actual, vg;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      actual[i][j] = c->disgrad_avg[i][j] + c->ddg_acum[i][j];
+      vg[i][j] = (actual[i][j] - c->disgrad_avg_t[i][j]) / dt;
+    }
+  c->e_vm = von_mises(actual);
+  c->d_vm = von_mises(vg);
+  c->time_tot += dt;
+  memcpy(c->disgrad_avg_t, actual, sizeof(t33));
+  const int do_orient = (c->p.update_flag == 1 && istep > 1);
+  const int do_harden = (c->p.hard_flag == 1);
+  if (do_orient) {
+    mth_status s = c->mixed ? spin_field<float>(c) : spin_field<double>(c);
+    if (s) return s;
+  }
+  // uniform part of the spin increment: Udot_a dt (applied rotation) plus the
+  // antisymmetric part of the uniform grad-u added to the field this step,
+  // Udot dt + the dDisGradAvg corrections applied before each iteration (the
+  // correction of the last get_smacro enters DisGradAvg_actual only)
+  double au[3];
+  {
+    t33 a;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        a[i][j] = 2.0 * c->udot_a[i][j] * dt + 0.5 * (c->ddg_applied[i][j] - c->ddg_applied[j][i]);
+    au[0] = a[2][1];
+    au[1] = a[0][2];
+    au[2] = a[1][0];
+  }
+  const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+  {
+    // end-of-step bytes: eps_p RMW + edot (18), sigma (6), rot RMW (18), CRSS RMW (24), gamacum RMW (2), spin (3)
+    const double rp = (double)(c->mixed ? sizeof(float) : sizeof(double)) * (double)c->nv;
+    LAUNCH(K_END_STEP, (18 + 6 + 18 + 24 + 2 + 3) * rp + (double)c->nv,
+           launch_end_step(c->mixed, c->nc, f, au, do_orient, do_harden, c->partials, c->nblocks, c->st));
+  }
+  double red[NPART_END];
+  mth_status s = reduce_to_host(c, NPART_END, red);
+  if (s) return s;
+  double e6[6], d6[6];
+  t33 ea, da;
+  for (int i = 0; i < 6; i++) { e6[i] = red[i] * c->wgt; d6[i] = red[6 + i] * c->wgt; }
+  v2t(e6, ea, 6);
+  v2t(d6, da, 6);
+  double evmp = 0, dvmp = 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) { evmp += ea[i][j] * ea[i][j]; dvmp += da[i][j] * da[i][j]; }
+  evmp = sqrt(2. / 3. * evmp);
+  dvmp = sqrt(2. / 3. * dvmp);
+  if (rep) {
+    memset(rep, 0, sizeof(*rep));
+    rep->step = istep;
+    rep->iterations = iter;
+    rep->time = c->time_tot;
+    memcpy(rep->sig_avg, c->sig_avg, sizeof(t33));
+    memcpy(rep->sig_avg_ph1, c->sig_avg1, sizeof(t33));
+    memcpy(rep->disgrad_avg, actual, sizeof(t33));
+    memcpy(rep->eps_avg, ea, sizeof(t33));
+    memcpy(rep->edot_avg, da, sizeof(t33));
+    rep->e_vm = c->e_vm; rep->evmp = evmp; rep->d_vm = c->d_vm; rep->dvmp = dvmp;
+    rep->s_vm = c->s_vm; rep->s_vm1 = c->s_vm1;
+    rep->err_s = c->err_s; rep->err_e = c->err_e;
+    rep->newton_iters = nit;
+    rep->newton_failed = nbad;
+  }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) c->disgrad_avg[i][j] = c->disgrad_avg_t[i][j] + c->udot[i][j] * dt;
+  c->istep++;
+  return MTH_OK;
+}
+
+// ------------------------------------------------------------- downloads
+template <typename T>
+static mth_status download(mth_ctx* c, int field, double* host) {
+  const Fields<T>& f = *reinterpret_cast<const Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
+  const long long P = c->nv;
+  int nc;
+  const T* src;
+  switch (field) {
+    case MTH_FIELD_SIG: src = f.sig; nc = 6; break;
+    case MTH_FIELD_EPS: src = f.epsp; nc = 6; break;
+    case MTH_FIELD_EDOT: src = f.edot; nc = 6; break;
+    case MTH_FIELD_STRAIN: src = f.strain; nc = 6; break;
+    case MTH_FIELD_ROT: src = f.rot; nc = 9; break;
+    case MTH_FIELD_CRSS: src = f.crss; nc = 12; break;
+    case MTH_FIELD_GAMACUM: src = f.gamacum; nc = 1; break;
+    default: return set_err(MTH_ERR_ARG, "field %d", field);
+  }
+  std::vector<T> h((size_t)nc * P);
+  CK(cudaMemcpyAsync(h.data(), src, sizeof(T) * nc * P, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (nc == 6) {
+    for (long long v = 0; v < P; v++) {
+      double s6[6];
+      t33 t;
+      for (int i = 0; i < 6; i++) s6[i] = (double)h[i * P + v];
+      v2t(s6, t, 6);
+      memcpy(host + 9 * v, t, sizeof(t33));
+    }
+  } else {
+    for (long long v = 0; v < P; v++)
+      for (int i = 0; i < nc; i++) host[nc * v + i] = (double)h[i * P + v];
+  }
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, size_t count) {
+  if (!c || !host) return set_err(MTH_ERR_ARG, "null argument");
+  if (!c->uploaded) return set_err(MTH_ERR_STATE, "no microstructure uploaded");
+  SETDEV(c);
+  if (field == MTH_FIELD_GRAIN) {
+    if (count != (size_t)c->nv) return set_err(MTH_ERR_ARG, "count");
+    std::vector<int> h(c->nv);
+    CK(cudaMemcpyAsync(h.data(), c->grain_d, sizeof(int) * c->nv, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (long long v = 0; v < c->nv; v++) host[v] = h[v];
+    return MTH_OK;
+  }
+  const int ncomp = (field == MTH_FIELD_CRSS) ? 12 : (field == MTH_FIELD_GAMACUM || field == MTH_FIELD_RHO) ? 1 : 9;
+  if (count != (size_t)ncomp * c->nv) return set_err(MTH_ERR_ARG, "count=%zu, expected %lld", count, ncomp * c->nv);
+  return c->mixed ? download<float>(c, field, host) : download<double>(c, field, host);
+}
+
+// ------------------------------------------------------------- profiling
+extern "C" mth_status mth_profile_enable(mth_ctx* c, int on) {
+  if (!c) return set_err(MTH_ERR_ARG, "null context");
+  SETDEV(c);
+  CK(cudaStreamSynchronize(c->st));
+  prof_resolve(c);
+  c->prof_on = on ? 1 : 0;
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_profile_read(mth_ctx* c, mth_profile* out, int reset) {
+  if (!c || !out) return set_err(MTH_ERR_ARG, "null argument");
+  SETDEV(c);
+  CK(cudaStreamSynchronize(c->st));
+  prof_resolve(c);
+  memset(out, 0, sizeof(*out));
+  out->n_kernels = K_NCLASS;
+  for (int k = 0; k < K_NCLASS; k++) {
+    strncpy(out->name[k], k_names[k], 31);
+    out->ms[k] = c->prof_ms[k];
+    out->launches[k] = c->prof_launch[k];
+    out->bytes[k] = c->prof_bytes[k];
+    out->total_launches += c->prof_launch[k];
+  }
+  if (reset) {
+    memset(c->prof_ms, 0, sizeof(c->prof_ms));
+    memset(c->prof_launch, 0, sizeof(c->prof_launch));
+    memset(c->prof_bytes, 0, sizeof(c->prof_bytes));
+  }
+  return MTH_OK;
+}
+
+// ------------------------------------------------------------ local solve
+extern "C" mth_status mth_local_solve(const mth_params* p, const double c066[36], size_t n, double* sig,
+                                      const double* eps_p, const double* strain, const double* rot,
+                                      const double* crss, double* edot, double* err, long long* newton_iters) {
+  if (!p || !c066 || !sig || !eps_p || !strain || !rot || !crss || !edot || !err)
+    return set_err(MTH_ERR_ARG, "null argument");
+  if (n == 0) {
+    if (newton_iters) *newton_iters = 0;
+    return MTH_OK;
+  }
+  NewtonConst nc;
+  memset(&nc, 0, sizeof(nc));
+  mth_status s = fill_phase(p->phase[0], nc.ph[0]);
+  if (s) return s;
+  if (p->phase[0].type != 0) return set_err(MTH_ERR_ARG, "phase 1 must be a crystal");
+  double cm[6][6], sm[6][6];
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) cm[i][j] = c066[i * 6 + j];
+  if (!inv6(cm, sm)) return set_err(MTH_ERR_SINGULAR, "C066 singular");
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 5; j++) nc.s0dev[i * 5 + j] = sm[i][j];
+  nc.s0hh = sm[5][5];
+  nc.dt = p->time_step;
+  nc.tol = p->newton_tol > 0 ? p->newton_tol : 1e-10;
+  nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
+  CK(cudaSetDevice(p->device));
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  double *ds, *de, *dst, *dr, *dc, *ded, *der;
+  long long* dit;
+  CK(cudaMalloc(&ds, sizeof(double) * 6 * n));
+  CK(cudaMalloc(&de, sizeof(double) * 6 * n));
+  CK(cudaMalloc(&dst, sizeof(double) * 6 * n));
+  CK(cudaMalloc(&dr, sizeof(double) * 9 * n));
+  CK(cudaMalloc(&dc, sizeof(double) * 12 * n));
+  CK(cudaMalloc(&ded, sizeof(double) * 6 * n));
+  CK(cudaMalloc(&der, sizeof(double) * 2 * n));
+  CK(cudaMalloc(&dit, sizeof(long long) * n));
+  CK(cudaMemcpyAsync(ds, sig, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(de, eps_p, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dst, strain, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dr, rot, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dc, crss, sizeof(double) * 12 * n, cudaMemcpyHostToDevice, st));
+  std::vector<double> rows(n * ETAB_W);
+  for (size_t v = 0; v < n; v++) {
+    class_row(nc.ph[0], rot + 9 * v, &rows[v * ETAB_W]);
+    class_row_add_s0(&rows[v * ETAB_W], sm);
+  }
+  double* det;
+  CK(cudaMalloc(&det, sizeof(double) * rows.size()));
+  CK(cudaMemcpyAsync(det, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, st));
+  CK(launch_local_solve(nc, (long long)n, ds, de, dst, dr, dc, det, ded, der, dit, st));
+  std::vector<long long> it(n);
+  CK(cudaMemcpyAsync(sig, ds, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(edot, ded, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(err, der, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(it.data(), dit, sizeof(long long) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  long long tot = 0;
+  for (size_t v = 0; v < n; v++) tot += it[v];
+  if (newton_iters) *newton_iters = tot;
+  cudaFree(ds); cudaFree(de); cudaFree(dst); cudaFree(dr); cudaFree(dc); cudaFree(ded); cudaFree(der); cudaFree(dit);
+  cudaFree(det);
+  cudaStreamDestroy(st);
+  return MTH_OK;
+}

@@ -1,0 +1,486 @@
+// fft_green.cu -- 3-D real FFT passes and the fused Green-operator pass.
+//
+// Replaces the 9+9 FFTW-MPI transforms and the GAMMA contraction of one
+// Green iteration (src/evolution.c:1361-1405, GAMMA from src/init.c:541-591).
+// Every pass is a batch of 1-D transforms done in shared memory with a
+// mixed-radix (4/2/3) Stockham autosort, so each line is read from and
+// written to HBM exactly once per pass:
+//   fft_z_r2c   : 6 real stress planes -> 6 half spectra along z (two real
+//                 lines packed per complex transform)
+//   fft_strided : complex lines along y or x, in place (forward/inverse)
+//   fft_x_green : forward x transform, Gamma0 applied at every k, antisymmetric
+//                 part accumulated for the lattice spin, inverse x transform
+//   fft_z_c2r   : half spectra -> real planes, fused with the strain update
+//                 DisGrad += dDisGradAvg + Re(.)/Nxyz of src/evolution.c:1402
+#include <cstdio>
+#include "mth_common.cuh"
+#include "mth_internal.h"
+
+namespace mth {
+
+// ---------------------------------------------------------------- smem FFT
+// Stockham autosort over nl lines of length n stored at d0 + l*ls.  Stage s
+// with radix R takes element j + r*n/R, multiplies by W^(k*r) (k = j mod Ns,
+// W = exp(sign*2*pi*i/(Ns*R))), does an R-point DFT and writes element
+// (j/Ns)*Ns*R + k + r*Ns.  The result is in d0 or d1 (returned).
+template <typename T>
+__device__ c2<T>* smem_fft(c2<T>* d0, c2<T>* d1, int n, int ls, int nl, const FftPlan& pl, const c2<T>* tw,
+                           int sign) {
+  int Ns = 1;
+  for (int s = 0; s < pl.nst; s++) {
+    const int R = pl.radix[s];
+    const int nb = n / R;
+    const int total = nl * nb;
+    const int twstep = n / (Ns * R);
+    for (int w = threadIdx.x; w < total; w += blockDim.x) {
+      const int l = w / nb, j = w - l * nb;
+      const c2<T>* in = d0 + l * ls;
+      c2<T>* out = d1 + l * ls;
+      const int k = j % Ns;
+      c2<T> v[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        if (r < R) {
+          v[r] = in[j + r * nb];
+          if (r) v[r] = cmul<T>(v[r], tw[k * r * twstep]);
+        }
+      }
+      if (R == 2) {
+        c2<T> a = v[0], b = v[1];
+        v[0] = cadd<T>(a, b);
+        v[1] = csub<T>(a, b);
+      } else if (R == 4) {
+        c2<T> s02 = cadd<T>(v[0], v[2]), d02 = csub<T>(v[0], v[2]);
+        c2<T> s13 = cadd<T>(v[1], v[3]), d13 = csub<T>(v[1], v[3]);
+        // W = sign*i ; W*d13
+        c2<T> wd = mk<T>(-(T)sign * d13.y, (T)sign * d13.x);
+        v[0] = cadd<T>(s02, s13);
+        v[2] = csub<T>(s02, s13);
+        v[1] = cadd<T>(d02, wd);
+        v[3] = csub<T>(d02, wd);
+      } else {  // R == 3
+        const T h = (T)0.86602540378443864676 * (T)sign;
+        c2<T> t = cadd<T>(v[1], v[2]), u = csub<T>(v[1], v[2]);
+        c2<T> m = mk<T>(v[0].x - (T)0.5 * t.x, v[0].y - (T)0.5 * t.y);
+        c2<T> iu = mk<T>(-h * u.y, h * u.x);
+        v[0] = cadd<T>(v[0], t);
+        v[1] = cadd<T>(m, iu);
+        v[2] = csub<T>(m, iu);
+      }
+      const int idxD = (j / Ns) * Ns * R + k;
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+        if (r < R) out[idxD + r * Ns] = v[r];
+    }
+    __syncthreads();
+    c2<T>* t = d0;
+    d0 = d1;
+    d1 = t;
+    Ns *= R;
+  }
+  return d0;
+}
+
+template <typename T>
+__device__ void load_twiddles(c2<T>* s, const c2<T>* g, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
+}
+
+// ------------------------------------------------------------- z passes
+// One block: lb consecutive (x,y) lines, npair = ceil(ncomp/2) packed
+// transforms per line.
+template <typename T>
+__global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in, c2<T>* __restrict__ out, int ncomp,
+                                                        long long plane, long long kplane, int nlines, int n2,
+                                                        int lb, FftPlan pl, const c2<T>* __restrict__ twg) {
+  extern __shared__ unsigned char smraw[];
+  c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
+  const int npair = (ncomp + 1) / 2;
+  const int ls = n2 + 1;
+  c2<T>* d0 = tw + n2;
+  c2<T>* d1 = d0 + npair * lb * ls;
+  const int line0 = blockIdx.x * lb;
+  const int nl_here = min(lb, nlines - line0);
+  load_twiddles<T>(tw, twg, n2);
+  for (int idx = threadIdx.x; idx < npair * lb * n2; idx += blockDim.x) {
+    const int z = idx % n2;
+    const int l = (idx / n2) % lb;
+    const int p = idx / (n2 * lb);
+    T a = 0, b = 0;
+    if (l < nl_here) {
+      const long long o = (long long)(line0 + l) * n2 + z;
+      a = in[(2 * p) * plane + o];
+      if (2 * p + 1 < ncomp) b = in[(2 * p + 1) * plane + o];
+    }
+    d0[(p * lb + l) * ls + z] = mk<T>(a, b);
+  }
+  __syncthreads();
+  c2<T>* r = smem_fft<T>(d0, d1, n2, ls, npair * lb, pl, tw, -1);
+  const int kz = n2 / 2 + 1;
+  for (int idx = threadIdx.x; idx < npair * lb * kz; idx += blockDim.x) {
+    const int k = idx % kz;
+    const int l = (idx / kz) % lb;
+    const int p = idx / (kz * lb);
+    if (l >= nl_here) continue;
+    const c2<T>* X = r + (p * lb + l) * ls;
+    c2<T> xk = X[k], xm = X[(n2 - k) % n2];
+    // A = (X[k] + conj(X[-k]))/2 ; B = -i (X[k] - conj(X[-k]))/2
+    c2<T> A = mk<T>((T)0.5 * (xk.x + xm.x), (T)0.5 * (xk.y - xm.y));
+    c2<T> B = mk<T>((T)0.5 * (xk.y + xm.y), (T)-0.5 * (xk.x - xm.x));
+    const long long o = (long long)(line0 + l) * kz + k;
+    out[(2 * p) * kplane + o] = A;
+    if (2 * p + 1 < ncomp) out[(2 * p + 1) * kplane + o] = B;
+  }
+}
+
+// mode 0: field = val*scale + add ; mode 1: field += val*scale + add
+template <typename T>
+__global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict__ spec, T* __restrict__ field, int ncomp,
+                                                        long long plane, long long kplane, int nlines, int n2,
+                                                        int lb, FftPlan pl, const c2<T>* __restrict__ twg, T scale,
+                                                        AddVec add, int mode) {
+  extern __shared__ unsigned char smraw[];
+  c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
+  const int npair = (ncomp + 1) / 2;
+  const int ls = n2 + 1;
+  c2<T>* d0 = tw + n2;
+  c2<T>* d1 = d0 + npair * lb * ls;
+  const int line0 = blockIdx.x * lb;
+  const int nl_here = min(lb, nlines - line0);
+  const int kz = n2 / 2 + 1;
+  load_twiddles<T>(tw, twg, n2);
+  for (int idx = threadIdx.x; idx < npair * lb * kz; idx += blockDim.x) {
+    const int k = idx % kz;
+    const int l = (idx / kz) % lb;
+    const int p = idx / (kz * lb);
+    c2<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
+    if (l < nl_here) {
+      const long long o = (long long)(line0 + l) * kz + k;
+      A = spec[(2 * p) * kplane + o];
+      if (2 * p + 1 < ncomp) B = spec[(2 * p + 1) * kplane + o];
+    }
+    if (k == 0 || 2 * k == n2) { A.y = 0; B.y = 0; }
+    c2<T>* X = d0 + (p * lb + l) * ls;
+    X[k] = mk<T>(A.x - B.y, A.y + B.x);                       // A + iB
+    if (k > 0 && 2 * k < n2) X[n2 - k] = mk<T>(A.x + B.y, -A.y + B.x);  // conj(A) + i conj(B)
+  }
+  __syncthreads();
+  c2<T>* r = smem_fft<T>(d0, d1, n2, ls, npair * lb, pl, tw, +1);
+  for (int idx = threadIdx.x; idx < ncomp * lb * n2; idx += blockDim.x) {
+    const int z = idx % n2;
+    const int l = (idx / n2) % lb;
+    const int c = idx / (n2 * lb);
+    if (l >= nl_here) continue;
+    const c2<T> X = r[((c >> 1) * lb + l) * ls + z];
+    const T val = (c & 1) ? X.y : X.x;
+    const long long o = (long long)c * plane + (long long)(line0 + l) * n2 + z;
+    const T v = val * scale + (T)add.v[c];
+    if (mode == 0) field[o] = v;
+    else field[o] += v;
+  }
+}
+
+// ------------------------------------------------------- strided passes
+// Lines along a dimension of length L with element stride S (in complex
+// elements); the block covers kb consecutive kz and one outer index.
+// base(outer) = outer * ostride.
+template <typename T>
+__global__ void __launch_bounds__(256) fft_strided_kernel(c2<T>* __restrict__ spec, int ncomp, long long kplane,
+                                                          int L, long long S, long long ostride, int kzn, int kb,
+                                                          FftPlan pl, const c2<T>* __restrict__ twg, int sign) {
+  extern __shared__ unsigned char smraw[];
+  c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
+  const int ls = L + 1;
+  const int nl = ncomp * kb;
+  c2<T>* d0 = tw + L;
+  c2<T>* d1 = d0 + nl * ls;
+  const int k0 = blockIdx.x * kb;
+  const long long base = (long long)blockIdx.y * ostride + k0;
+  load_twiddles<T>(tw, twg, L);
+  for (int idx = threadIdx.x; idx < ncomp * L * kb; idx += blockDim.x) {
+    const int kk = idx % kb;
+    const int e = (idx / kb) % L;
+    const int c = idx / (kb * L);
+    c2<T> v = mk<T>(0, 0);
+    if (k0 + kk < kzn) v = spec[c * kplane + base + e * S + kk];
+    d0[(c * kb + kk) * ls + e] = v;
+  }
+  __syncthreads();
+  c2<T>* r = smem_fft<T>(d0, d1, L, ls, nl, pl, tw, sign);
+  for (int idx = threadIdx.x; idx < ncomp * L * kb; idx += blockDim.x) {
+    const int kk = idx % kb;
+    const int e = (idx / kb) % L;
+    const int c = idx / (kb * L);
+    if (k0 + kk < kzn) spec[c * kplane + base + e * S + kk] = r[(c * kb + kk) * ls + e];
+  }
+}
+
+// ------------------------------------------------------- Green operator
+// Unit wave vector of index idx on an axis of n points: the frequency of
+// src/init.c:778-786 (idx/n - round(idx/n), Nyquist -> -1/2).
+template <typename T> __device__ __forceinline__ T freq(int idx, int n) {
+  double t = (double)idx * (1.0 / (double)n);
+  t -= round(t);
+  return (T)t;
+}
+
+// Delta = -Omega(n) (sig n) (x) n for one n; accumulates into dsym (LT, 6
+// complex) and danti (3 complex: [2][1], [0][2], [1][0]) with weight wgt.
+template <typename T>
+__device__ __forceinline__ void green_apply_n(const GreenConst& gc, const T n[3], const c2<T> s[3][3], T wgt, c2<T> dsym[6],
+                                              c2<T> danti[3]) {
+  T A[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = i; k < 3; k++) {
+      T a = 0;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int l = 0; l < 3; l++) a += (T)gc.c0[((i * 3 + j) * 3 + k) * 3 + l] * n[j] * n[l];
+      A[i][k] = a;
+      A[k][i] = a;
+    }
+  T det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+          A[0][2] * (A[1][0] * A[2][1] - A[2][0] * A[1][1]);
+  T id = (T)1 / det;
+  T O[3][3];
+  O[0][0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) * id;
+  O[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id;
+  O[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
+  O[1][0] = O[0][1];
+  O[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id;
+  O[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
+  O[2][0] = O[0][2];
+  O[2][1] = O[1][2];
+  O[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
+  c2<T> t[3], v[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    t[k] = mk<T>(s[k][0].x * n[0] + s[k][1].x * n[1] + s[k][2].x * n[2],
+                 s[k][0].y * n[0] + s[k][1].y * n[1] + s[k][2].y * n[2]);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    v[i] = mk<T>(-(O[i][0] * t[0].x + O[i][1] * t[1].x + O[i][2] * t[2].x) * wgt,
+                 -(O[i][0] * t[0].y + O[i][1] * t[1].y + O[i][2] * t[2].y) * wgt);
+  // Delta_ij = v_i n_j
+  T r2 = (T)RSQ2, r3 = (T)RSQ3, r6 = (T)RSQ6;
+  c2<T> d00 = cscale<T>(v[0], n[0]), d11 = cscale<T>(v[1], n[1]), d22 = cscale<T>(v[2], n[2]);
+  c2<T> d12 = cscale<T>(v[1], n[2]), d21 = cscale<T>(v[2], n[1]);
+  c2<T> d02 = cscale<T>(v[0], n[2]), d20 = cscale<T>(v[2], n[0]);
+  c2<T> d01 = cscale<T>(v[0], n[1]), d10 = cscale<T>(v[1], n[0]);
+  dsym[0] = cadd<T>(dsym[0], cscale<T>(csub<T>(d11, d00), r2));
+  dsym[1] = cadd<T>(dsym[1], cscale<T>(csub<T>(cscale<T>(d22, (T)2), cadd<T>(d00, d11)), r6));
+  dsym[2] = cadd<T>(dsym[2], cscale<T>(cadd<T>(d12, d21), r2));
+  dsym[3] = cadd<T>(dsym[3], cscale<T>(cadd<T>(d02, d20), r2));
+  dsym[4] = cadd<T>(dsym[4], cscale<T>(cadd<T>(d01, d10), r2));
+  dsym[5] = cadd<T>(dsym[5], cscale<T>(cadd<T>(cadd<T>(d00, d11), d22), r3));
+  danti[0] = cadd<T>(danti[0], cscale<T>(csub<T>(d21, d12), (T)0.5));
+  danti[1] = cadd<T>(danti[1], cscale<T>(csub<T>(d02, d20), (T)0.5));
+  danti[2] = cadd<T>(danti[2], cscale<T>(csub<T>(d10, d01), (T)0.5));
+}
+
+// sig: LT components of sigma-hat at k (in), replaced by LT of sym(Delta);
+// anti: antisymmetric part of Delta.  When k has Nyquist components the
+// operator is the mean of Gamma at n(k) and n(-k): the reference keeps only
+// the real part of its complex inverse transform (src/evolution.c:1402),
+// which equals the transform of the Hermitian part of Delta-hat.
+template <typename T>
+__device__ __forceinline__ void green_point(const GreenConst& gc, int kx, int ky, int kz, int n0, int n1, int n2,
+                                            c2<T> sig[6], c2<T> anti[3]) {
+  c2<T> dsym[6], danti[3];
+#pragma unroll
+  for (int i = 0; i < 6; i++) dsym[i] = mk<T>(0, 0);
+#pragma unroll
+  for (int i = 0; i < 3; i++) danti[i] = mk<T>(0, 0);
+  if (kx == 0 && ky == 0 && kz == 0) {
+    if (gc.elast_bc == 0) {
+      for (int i = 0; i < 6; i++) {
+        T re = 0, im = 0;
+        for (int j = 0; j < 6; j++) {
+          re -= (T)gc.s066[i * 6 + j] * sig[j].x;
+          im -= (T)gc.s066[i * 6 + j] * sig[j].y;
+        }
+        dsym[i] = mk<T>(re, im);
+      }
+    }
+  } else {
+    c2<T> s[3][3];
+    {
+      T re[6], im[6], tr[3][3], ti[3][3];
+#pragma unroll
+      for (int i = 0; i < 6; i++) { re[i] = sig[i].x; im[i] = sig[i].y; }
+      lt_to_cart<T>(re, tr);
+      lt_to_cart<T>(im, ti);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) s[i][j] = mk<T>(tr[i][j], ti[i][j]);
+    }
+    T f[3] = {freq<T>(kx, n0), freq<T>(ky, n1), freq<T>(kz, n2)};
+    const bool q0 = (2 * kx == n0), q1 = (2 * ky == n1), q2 = (2 * kz == n2);
+    T nrm = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    T n[3] = {f[0] / nrm, f[1] / nrm, f[2] / nrm};
+    const bool anyq = q0 || q1 || q2;
+    const bool anyv = (!q0 && kx != 0) || (!q1 && ky != 0) || (!q2 && kz != 0);
+    if (anyq && anyv) {
+      green_apply_n<T>(gc, n, s, (T)0.5, dsym, danti);
+      T m[3] = {q0 ? n[0] : -n[0], q1 ? n[1] : -n[1], q2 ? n[2] : -n[2]};
+      green_apply_n<T>(gc, m, s, (T)0.5, dsym, danti);
+    } else {
+      green_apply_n<T>(gc, n, s, (T)1, dsym, danti);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 6; i++) sig[i] = dsym[i];
+#pragma unroll
+  for (int i = 0; i < 3; i++) anti[i] = danti[i];
+}
+
+// x pass fused with Gamma0: forward transform along x of the 6 stress
+// spectra, Delta = Gamma0 : sigma-hat per k, antisymmetric part added to
+// the spin accumulator, inverse transform along x.  One block: fixed y,
+// kb consecutive kz.
+template <typename T>
+__global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c2<T>* __restrict__ spec, c2<T>* __restrict__ anti_acc,
+                                                          long long kplane, int n0, int n1, int n2, int kzn, int kb,
+                                                          FftPlan pl, const c2<T>* __restrict__ twf,
+                                                          const c2<T>* __restrict__ twi) {
+  extern __shared__ unsigned char smraw[];
+  c2<T>* tw_f = reinterpret_cast<c2<T>*>(smraw);
+  c2<T>* tw_i = tw_f + n0;
+  const int ls = n0 + 1;
+  const int nl = 6 * kb;
+  c2<T>* d0 = tw_i + n0;
+  c2<T>* d1 = d0 + nl * ls;
+  const int k0 = blockIdx.x * kb;
+  const int y = blockIdx.y;
+  const long long S = (long long)n1 * kzn;
+  const long long base = (long long)y * kzn + k0;
+  load_twiddles<T>(tw_f, twf, n0);
+  load_twiddles<T>(tw_i, twi, n0);
+  for (int idx = threadIdx.x; idx < 6 * n0 * kb; idx += blockDim.x) {
+    const int kk = idx % kb;
+    const int e = (idx / kb) % n0;
+    const int c = idx / (kb * n0);
+    c2<T> v = mk<T>(0, 0);
+    if (k0 + kk < kzn) v = spec[c * kplane + base + e * S + kk];
+    d0[(c * kb + kk) * ls + e] = v;
+  }
+  __syncthreads();
+  c2<T>* r = smem_fft<T>(d0, d1, n0, ls, nl, pl, tw_f, -1);
+  c2<T>* other = (r == d0) ? d1 : d0;
+  for (int idx = threadIdx.x; idx < n0 * kb; idx += blockDim.x) {
+    const int kk = idx % kb;
+    const int kx = idx / kb;
+    if (k0 + kk >= kzn) continue;
+    c2<T> s[6], a[3];
+#pragma unroll
+    for (int c = 0; c < 6; c++) s[c] = r[(c * kb + kk) * ls + kx];
+    green_point<T>(gc, kx, y, k0 + kk, n0, n1, n2, s, a);
+#pragma unroll
+    for (int c = 0; c < 6; c++) r[(c * kb + kk) * ls + kx] = s[c];
+    const long long o = base + kx * S + kk;
+#pragma unroll
+    for (int c = 0; c < 3; c++) anti_acc[c * kplane + o] = cadd<T>(anti_acc[c * kplane + o], a[c]);
+  }
+  __syncthreads();
+  c2<T>* r2 = smem_fft<T>(r, other, n0, ls, nl, pl, tw_i, +1);
+  for (int idx = threadIdx.x; idx < 6 * n0 * kb; idx += blockDim.x) {
+    const int kk = idx % kb;
+    const int e = (idx / kb) % n0;
+    const int c = idx / (kb * n0);
+    if (k0 + kk < kzn) spec[c * kplane + base + e * S + kk] = r2[(c * kb + kk) * ls + e];
+  }
+}
+
+// ------------------------------------------------------------ launchers
+static size_t z_smem(int n2, int npair, int lb, size_t esz) { return (size_t)esz * (n2 + 2 * npair * lb * (n2 + 1)); }
+
+template <typename T>
+static int pick_lb(int n2, int npair, int nlines, size_t budget) {
+  int lb = 16;
+  while (lb > 1 && z_smem(n2, npair, lb, sizeof(c2<T>)) > budget) lb >>= 1;
+  if (lb > nlines) lb = nlines;
+  return lb;
+}
+
+template <typename T>
+cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, cudaStream_t st) {
+  const int npair = (ncomp + 1) / 2;
+  const int nlines = g.n0 * g.n1;
+  const int lb = pick_lb<T>(g.n2, npair, nlines, g.smem_budget);
+  const size_t sm = z_smem(g.n2, npair, lb, sizeof(c2<T>));
+  auto k = fft_z_r2c_kernel<T>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(in, out, ncomp, g.plane, g.kplane, nlines, g.n2, lb, g.pz, tw);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int ncomp, const c2<T>* tw, T scale,
+                             const AddVec& add, int mode, cudaStream_t st) {
+  const int npair = (ncomp + 1) / 2;
+  const int nlines = g.n0 * g.n1;
+  const int lb = pick_lb<T>(g.n2, npair, nlines, g.smem_budget);
+  const size_t sm = z_smem(g.n2, npair, lb, sizeof(c2<T>));
+  auto k = fft_z_c2r_kernel<T>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(spec, field, ncomp, g.plane, g.kplane, nlines, g.n2, lb, g.pz, tw,
+                                             scale, add, mode);
+  return cudaGetLastError();
+}
+
+static size_t s_smem(int L, int nl, size_t esz, int ntw) { return esz * ((size_t)ntw * L + 2 * (size_t)nl * (L + 1)); }
+
+template <typename T>
+static int pick_kb(int L, int ncomp, size_t budget, int ntw) {
+  int kb = 16;
+  while (kb > 1 && s_smem(L, ncomp * kb, sizeof(c2<T>), ntw) > budget) kb >>= 1;
+  return kb;
+}
+
+// axis 1 (y) or 0 (x)
+template <typename T>
+cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axis, int sign, const c2<T>* tw,
+                               cudaStream_t st) {
+  const int L = axis == 1 ? g.n1 : g.n0;
+  const long long S = axis == 1 ? g.kz : (long long)g.n1 * g.kz;
+  const long long ostride = axis == 1 ? (long long)g.n1 * g.kz : g.kz;
+  const int nouter = axis == 1 ? g.n0 : g.n1;
+  const FftPlan& pl = axis == 1 ? g.py : g.px;
+  const int kb = pick_kb<T>(L, ncomp, g.smem_budget, 1);
+  const size_t sm = s_smem(L, ncomp * kb, sizeof(c2<T>), 1);
+  auto k = fft_strided_kernel<T>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((g.kz + kb - 1) / kb, nouter);
+  k<<<grid, 256, sm, st>>>(spec, ncomp, g.kplane, L, S, ostride, g.kz, kb, pl, tw, sign);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* spec, c2<T>* anti, const c2<T>* twf,
+                               const c2<T>* twi, cudaStream_t st) {
+  const int kb = pick_kb<T>(g.n0, 6, g.smem_budget, 2);
+  const size_t sm = s_smem(g.n0, 6 * kb, sizeof(c2<T>), 2);
+  auto k = fft_x_green_kernel<T>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((g.kz + kb - 1) / kb, g.n1);
+  k<<<grid, 256, sm, st>>>(gc, spec, anti, g.kplane, g.n0, g.n1, g.n2, g.kz, kb, g.px, twf, twi);
+  return cudaGetLastError();
+}
+
+#define INST(T)                                                                                                      \
+  template cudaError_t launch_fft_z_r2c<T>(const FftGeom&, const T*, c2<T>*, int, const c2<T>*, cudaStream_t);        \
+  template cudaError_t launch_fft_z_c2r<T>(const FftGeom&, const c2<T>*, T*, int, const c2<T>*, T, const AddVec&, int, \
+                                           cudaStream_t);                                                            \
+  template cudaError_t launch_fft_strided<T>(const FftGeom&, c2<T>*, int, int, int, const c2<T>*, cudaStream_t);      \
+  template cudaError_t launch_fft_x_green<T>(const FftGeom&, const GreenConst&, c2<T>*, c2<T>*, const c2<T>*, const c2<T>*, \
+                                            cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace mth

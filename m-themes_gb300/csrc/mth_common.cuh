@@ -1,0 +1,97 @@
+// mth_common.cuh -- shared types and helpers of the sm_103a EVPFFT kernels.
+//
+// Field layout in HBM: structure of arrays, one plane of N0*N1*N2 values per
+// component, voxel index (x*N1+y)*N2+z with z fastest (the reference's pIDX,
+// src/evp.h:53).  Symmetric tensors are stored as 6 components in the
+// Lebensohn-Tome basis of chg_basis (src/kinematics.c:27-53): components 0..4
+// deviatoric, 5 hydrostatic.  Spectra are half spectra along z
+// (N2/2+1 points), one plane per component, index (x*N1+y)*Kz+kz.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mth {
+
+constexpr int NSYS = 12;
+constexpr double RSQ2 = 0.70710678118654744;
+constexpr double RSQ3 = 0.57735026918962584;
+constexpr double RSQ6 = 0.40824829046386304;
+
+template <typename T> struct cplx;
+template <> struct cplx<float> { using type = float2; };
+template <> struct cplx<double> { using type = double2; };
+template <typename T> using c2 = typename cplx<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ c2<T> mk(T a, T b) { c2<T> r; r.x = a; r.y = b; return r; }
+template <typename T> __device__ __forceinline__ c2<T> cadd(c2<T> a, c2<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ c2<T> csub(c2<T> a, c2<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ c2<T> cmul(c2<T> a, c2<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ c2<T> cscale(c2<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+template <typename T> __device__ __forceinline__ c2<T> conjg(c2<T> a) { return mk<T>(a.x, -a.y); }
+
+// Symmetric 3x3 tensor (Cartesian) <-> 6-vector in the LT basis.
+// v2t: t = sum_i v_i B_i ; t2v: v_i = t : B_i  (chg_basis opt 1 / opt 2).
+template <typename T> __host__ __device__ __forceinline__ void lt_to_cart(const T* v, T t[3][3]) {
+  const T r2 = (T)RSQ2, r3 = (T)RSQ3, r6 = (T)RSQ6;
+  t[0][0] = -r2 * v[0] - r6 * v[1] + r3 * v[5];
+  t[1][1] = r2 * v[0] - r6 * v[1] + r3 * v[5];
+  t[2][2] = (T)2 * r6 * v[1] + r3 * v[5];
+  t[1][2] = t[2][1] = r2 * v[2];
+  t[0][2] = t[2][0] = r2 * v[3];
+  t[0][1] = t[1][0] = r2 * v[4];
+}
+template <typename T> __host__ __device__ __forceinline__ void cart_to_lt(const T t[3][3], T* v) {
+  const T r2 = (T)RSQ2, r3 = (T)RSQ3, r6 = (T)RSQ6;
+  v[0] = r2 * (t[1][1] - t[0][0]);
+  v[1] = r6 * ((T)2 * t[2][2] - t[0][0] - t[1][1]);
+  v[2] = r2 * (t[1][2] + t[2][1]);
+  v[3] = r2 * (t[0][2] + t[2][0]);
+  v[4] = r2 * (t[0][1] + t[1][0]);
+  v[5] = r3 * (t[0][0] + t[1][1] + t[2][2]);
+}
+
+// Q (5x5, row-major) maps deviatoric LT components from sample to crystal
+// axes: a_c = Q a_s, with A_c = T^T A_s T and T the crystal->sample matrix
+// (TranMat_xt2sa).  Q_ij = B_i : (T^T B_j T).
+template <typename T> __host__ __device__ __forceinline__ void rot_to_q(const T R[9], T Q[25]) {
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    T bj[6] = {0, 0, 0, 0, 0, 0};
+    bj[j] = (T)1;
+    T b[3][3], m[3][3], c[3][3];
+    lt_to_cart<T>(bj, b);
+    // m = b T
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) m[p][q] = b[p][0] * R[0 * 3 + q] + b[p][1] * R[1 * 3 + q] + b[p][2] * R[2 * 3 + q];
+    // c = T^T m
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) c[p][q] = R[0 * 3 + p] * m[0][q] + R[1 * 3 + p] * m[1][q] + R[2 * 3 + p] * m[2][q];
+    T v[6];
+    cart_to_lt<T>(c, v);
+#pragma unroll
+    for (int i = 0; i < 5; i++) Q[i * 5 + j] = v[i];
+  }
+}
+
+// Per-phase constants of the flow rule in crystal axes.
+struct PhaseConst {
+  int type;          // 0 crystal, 1 gas
+  int nsys;
+  double nrs, gamd0;
+  double tau_back_minus_fwd;   // tau0b - tau0f (harden shifts both alike)
+  double s_xt[6];    // crystal-axes compliance, diagonal in the LT basis
+  double c_xt[6];    // crystal-axes stiffness, diagonal in the LT basis
+  double m_xt[NSYS][5];  // Schmid tensors in crystal axes (Schm_xt)
+  double bn[NSYS][3], bb[NSYS][3];
+  double hard[NSYS][NSYS];
+  double tau0f, tau1, thet0, thet1;
+  int nrs_int;       // >0 when nrs is an integer: exponent fast path
+};
+
+}  // namespace mth

@@ -1,0 +1,102 @@
+// mth_internal.h -- declarations shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "mth_common.cuh"
+
+namespace mth {
+
+// Radix plan of one axis: n = prod(radix[0..nst)).
+struct FftPlan {
+  int n;
+  int nst;
+  int radix[8];
+};
+
+struct FftGeom {
+  int n0, n1, n2, kz;      // grid and half-spectrum length along z
+  long long plane, kplane; // elements per real plane / per spectrum plane
+  FftPlan px, py, pz;
+  size_t smem_budget;      // dynamic shared memory per block (bytes)
+};
+
+struct AddVec { double v[6]; };
+
+// Green-operator constants, passed by value (kernel parameter space).
+struct GreenConst {
+  double c0[81];      // C0_ijkl (chg_basis of C066, src/init.c:376)
+  double s066[36];    // S066 = C066^-1 (used at k=0 when ElastBC=0)
+  int elast_bc;
+};
+
+// Flow-rule, hardening and reference-medium constants, passed by value.
+struct NewtonConst {
+  PhaseConst ph[2];
+  double s0dev[25];     // 5x5 deviatoric block of S066
+  double s0hh;          // hydrostatic entry of S066
+  double dt;
+  double tol;
+  int itmax;
+  int flow_off;         // 1: Schmid tensors zero (Update_Flag=0 at istep 0)
+};
+
+bool make_plan(int n, FftPlan* p);
+
+template <typename T>
+cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, cudaStream_t st);
+template <typename T>
+cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int ncomp, const c2<T>* tw, T scale,
+                             const AddVec& add, int mode, cudaStream_t st);
+template <typename T>
+cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axis, int sign, const c2<T>* tw,
+                               cudaStream_t st);
+template <typename T>
+cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* spec, c2<T>* anti, const c2<T>* twf,
+                               const c2<T>* twi, cudaStream_t st);
+
+// Per-voxel field pointers of one RVE; TSt is the storage type.
+template <typename TSt>
+struct Fields {
+  TSt* sig;      // 6 planes, LT basis, sample axes
+  TSt* strain;   // 6 planes: sym(grad u)
+  TSt* epsp;     // 6 planes: plastic strain
+  TSt* edot;     // 6 planes: plastic strain rate
+  TSt* rot;      // 9 planes: crystal->sample matrix, row-major
+  TSt* crss;     // 12 planes: forward CRSS
+  TSt* gamacum;  // 1 plane
+  TSt* wspin;    // 3 planes: antisymmetric part of the accumulated grad-u increment
+  const uint8_t* phase;  // 0-based phase index
+  const int* eclass;     // elastic class of the voxel (row of etab)
+  const double* etab;    // ETAB_W doubles per class
+  long long nv;
+};
+
+// Elastic-class table row.  The reference builds the stiffness C_gr of each
+// voxel once, from its initial orientation (src/init.c:272-283), and never
+// rotates it with the lattice; only the Schmid tensors follow the texture
+// (update_schmid).  Voxels with equal phase and initial Euler angles share a
+// row.  Packed symmetric 5x5 blocks in the LT basis, sample axes:
+constexpr int ETAB_W = 48;
+constexpr int ET_STOT = 0;    // S066_dev + S_gr (15): Hessian base of the local solve
+constexpr int ET_SEL = 15;    // S_gr dev (15)
+constexpr int ET_SEL_HH = 30; // S_gr hydrostatic
+constexpr int ET_CGR = 31;    // C_gr dev (15)
+constexpr int ET_CGR_HH = 46; // C_gr hydrostatic
+
+// Partial sums written per block by the Newton kernel.
+constexpr int NPART = 16;   // err_s, err_e, sig[6], sig_ph1[6], newton_iters, newton_failed
+// Partial sums written per block by the end-of-step kernel.
+constexpr int NPART_END = 12;  // epsp[6], edot[6]
+
+cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
+                          cudaStream_t st);
+cudaError_t launch_end_step(int mixed, const NewtonConst& nc, const void* fields, const double anti_uniform[3],
+                            int do_orient, int do_harden, double* partials, int nblocks, cudaStream_t st);
+cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, const double* euler,
+                         const double d6[6], int nblocks, cudaStream_t st);
+cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, const double* epsp,
+                               const double* strain, const double* rot, const double* crss, const double* etab,
+                               double* edot, double* err, long long* iters, cudaStream_t st);
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, cudaStream_t st);
+
+}  // namespace mth

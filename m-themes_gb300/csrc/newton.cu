@@ -1,0 +1,719 @@
+// newton.cu -- per-voxel kernels: the local stress solve of UpdateStress
+// (src/evolution.c:44-310) with the power-law flow rule of StrainRate_eval
+// (src/constitutive.c:5-67), the end-of-step updates (plastic strain,
+// update_orient src/constitutive.c:196-273, harden src/constitutive.c:275-326)
+// and the set-up of InitMicroStruct/InitFields (src/init.c:233-515).
+//
+// One thread per voxel, structure-of-arrays fields, coalesced loads.
+//
+// Local problem.  The reference solves, per voxel and in the 6-component
+// Lebensohn-Tome basis, R(s) = s - lambda + C066 (S s + e_p + edot_p(s) dt - e)
+// = 0 by Newton with a line search on |R|^2 (src/evolution.c:129-253).  Here
+// the same root is found from the equivalent system S0 R = 0 (S0 = C066^-1),
+// which is the gradient of the strictly convex potential
+//   Phi(s) = 1/2 (s-lambda).S0.(s-lambda) + 1/2 s.S.s + (e_p - e).s + dt psi(s),
+//   psi(s) = sum_a gamd0 tau_a |r_a|^(n+1) / (n+1),  r_a = m_a.s / tau_a,
+// so Newton's direction is always a descent direction and the Hessian
+// S0 + S + dt sum_a w_a m_a m_a^T is symmetric positive definite (Cholesky).
+// The solve runs in crystal axes: there the cubic compliance S is diagonal and
+// the Schmid tensors m_a are the constants of the .sx file, so no per-voxel
+// Schmid field is stored (update_schmid, src/kinematics.c:430-463, becomes a
+// 5x5 rotation of the stress).  The hydrostatic component decouples exactly
+// for cubic crystals (edot_p has no trace, src/constitutive.c:50) and is
+// solved in closed form.  Convergence: |step| <= tol |lambda|, as the
+// reference's erral (src/evolution.c:264-270).
+#include <cstdio>
+#include <cmath>
+#include "mth_common.cuh"
+#include "mth_internal.h"
+
+namespace mth {
+
+// |r|^e for the flow rule; integer exponents by repeated squaring.
+template <typename T>
+__device__ __forceinline__ T pow_abs(T a, int ei, T ef) {
+  if (ei > 0) {
+    T r = (T)1, b = a;
+    int e = ei;
+    while (e) {
+      if (e & 1) r *= b;
+      b *= b;
+      e >>= 1;
+    }
+    return r;
+  }
+  return a > (T)0 ? (T)pow(a, ef) : (T)0;
+}
+
+// Flow rule in crystal axes at deviatoric stress x (5).  Returns edot (5),
+// optional Hessian contribution D (15, packed upper triangle) and psi.
+// gam (optional) receives the shear rates.
+template <typename TF, bool WANT_D>
+__device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], const TF* tauf, TF tau_off, TF ed[5],
+                                          TF D[15], TF& psi, TF* gam) {
+#pragma unroll
+  for (int i = 0; i < 5; i++) ed[i] = 0;
+  if (WANT_D) {
+#pragma unroll
+    for (int i = 0; i < 15; i++) D[i] = 0;
+  }
+  psi = 0;
+  const int ns = ph.nsys;
+  const TF n = (TF)ph.nrs;
+  const TF g0 = (TF)ph.gamd0;
+  const int nm1 = ph.nrs_int > 0 ? ph.nrs_int - 1 : 0;
+  for (int s = 0; s < ns; s++) {
+    TF m[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) m[i] = (TF)ph.m_xt[s][i];
+    const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
+    const TF tau = rss < (TF)0 ? tauf[s] + tau_off : tauf[s];
+    const TF r = rss / tau;
+    const TF ar = fabs(r);
+    const TF pnm1 = pow_abs<TF>(ar, nm1, n - (TF)1);   // |r|^(n-1)
+    const TF pn = pnm1 * ar;                             // |r|^n
+    const TF g = g0 * (r > (TF)0 ? pn : -pn);
+    if (gam) gam[s] = g;
+#pragma unroll
+    for (int i = 0; i < 5; i++) ed[i] += m[i] * g;
+    if (WANT_D) {
+      const TF w = g0 * n * pnm1 / tau;
+      int q = 0;
+#pragma unroll
+      for (int i = 0; i < 5; i++)
+#pragma unroll
+        for (int j = i; j < 5; j++) D[q++] += w * m[i] * m[j];
+    }
+    psi += g0 * tau * pn * ar / (n + (TF)1);
+  }
+}
+
+__device__ __forceinline__ int pk(int i, int j) {  // packed upper-triangle index of 5x5
+  if (i > j) { int t = i; i = j; j = t; }
+  return i * 5 - (i * (i - 1)) / 2 + (j - i);
+}
+
+template <typename T>
+__device__ __forceinline__ void symv5(const T* K, const T* x, T* y) {
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) s += K[pk(i, j)] * x[j];
+    y[i] = s;
+  }
+}
+
+// Cholesky solve of the packed SPD matrix A (5x5): x = A^-1 b.  Returns
+// false when a pivot is not positive.
+template <typename T>
+__device__ __forceinline__ bool chol_solve5(const T* A, const T* b, T* x) {
+  T L[15];
+#pragma unroll
+  for (int i = 0; i < 15; i++) L[i] = A[i];
+  // L stored packed by rows of the upper triangle: L^T (upper) in place
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    T d = L[pk(k, k)];
+#pragma unroll
+    for (int p = 0; p < 5; p++)
+      if (p < k) d -= L[pk(p, k)] * L[pk(p, k)];
+    if (!(d > (T)0)) return false;
+    d = sqrt(d);
+    L[pk(k, k)] = d;
+    const T id = (T)1 / d;
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+      if (j > k) {
+        T s = L[pk(k, j)];
+#pragma unroll
+        for (int p = 0; p < 5; p++)
+          if (p < k) s -= L[pk(p, k)] * L[pk(p, j)];
+        L[pk(k, j)] = s * id;
+      }
+    }
+  }
+  T y[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    T s = b[i];
+#pragma unroll
+    for (int p = 0; p < 5; p++)
+      if (p < i) s -= L[pk(p, i)] * y[p];
+    y[i] = s / L[pk(i, i)];
+  }
+#pragma unroll
+  for (int i = 4; i >= 0; i--) {
+    T s = y[i];
+#pragma unroll
+    for (int p = 0; p < 5; p++)
+      if (p > i) s -= L[pk(i, p)] * x[p];
+    x[i] = s / L[pk(i, i)];
+  }
+  return true;
+}
+
+// Result of one voxel solve.
+struct VoxelOut {
+  double conv_s, conv_e;
+  int iters;
+  int failed;
+};
+
+// Local solve of one crystal voxel.  lam6/eps6/ep6: LT sample-frame inputs
+// (lambda = current stress, total strain, plastic strain); Q: sample->crystal
+// 5x5 of the current lattice orientation; et: elastic-class row (initial
+// orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
+// (plastic strain rate, sample frame).  TF: flow-rule and frame-transform
+// type; TS: Newton solve type.
+template <typename TF, typename TS>
+__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const double* __restrict__ et,
+                                const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* tauf, TF* sig6,
+                                TF* ed6) {
+  VoxelOut o = {0.0, 0.0, 0, 0};
+  const TS dt = (TS)nc.dt;
+  // crystal-frame inputs
+  TF lamx[5], epsx[5], epx[5], s0s[5], s0l[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    TF a = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) a += (TF)nc.s0dev[i * 5 + j] * lam6[j];
+    s0s[i] = a;   // S0 lambda, sample axes
+  }
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    TF a = 0, b = 0, c = 0, d = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+      a += Q[i * 5 + j] * lam6[j];
+      b += Q[i * 5 + j] * eps6[j];
+      c += Q[i * 5 + j] * ep6[j];
+      d += Q[i * 5 + j] * s0s[j];
+    }
+    lamx[i] = a; epsx[i] = b; epx[i] = c; s0l[i] = d;   // crystal axes
+  }
+  // Hessian base K = Q (S0 + S_gr) Q^T in crystal axes of the current lattice
+  TS K[15];
+  {
+    TF St[25], t[25];
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = 0; j < 5; j++) St[i * 5 + j] = (TF)et[ET_STOT + pk(i, j)];
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = 0; j < 5; j++) {
+        TF s = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) s += Q[i * 5 + k] * St[k * 5 + j];
+        t[i * 5 + j] = s;
+      }
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = i; j < 5; j++) {
+        TF s = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) s += t[i * 5 + k] * Q[j * 5 + k];
+        K[pk(i, j)] = (TS)s;
+      }
+  }
+  // c = -S0x lam + e_p - e  (gradient of Phi = K x + c + dt edot)
+  TS c[5], lamxs[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    lamxs[i] = (TS)lamx[i];
+    c[i] = -(TS)s0l[i] + (TS)epx[i] - (TS)epsx[i];
+  }
+  // hydrostatic part in closed form
+  const TS s0hh = (TS)nc.s0hh, shh = (TS)et[ET_SEL_HH];
+  const TS h = (s0hh * (TS)lam6[5] + (TS)eps6[5] - (TS)ep6[5]) / (s0hh + shh);
+  TS signorm = 0;
+#pragma unroll
+  for (int i = 0; i < 6; i++) signorm += (TS)lam6[i] * (TS)lam6[i];
+  signorm = sqrt(signorm);
+  const TS dh = h - (TS)lam6[5];
+
+  TS x[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) x[i] = lamxs[i];
+  const TF tau_off = (TF)ph.tau_back_minus_fwd;
+  TF edf[5], Df[15], psif;
+  TS step_norm = 0;
+  int it = 0;
+  bool done = false;
+  // first step includes the hydrostatic correction in the step norm
+  TS hstep2 = dh * dh;
+  const TS ref = signorm > (TS)0 ? signorm : (TS)0;
+  for (; it < nc.itmax && !done; it++) {
+    TF xf[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) xf[i] = (TF)x[i];
+    if (nc.flow_off) {
+#pragma unroll
+      for (int i = 0; i < 5; i++) edf[i] = 0;
+#pragma unroll
+      for (int i = 0; i < 15; i++) Df[i] = 0;
+      psif = 0;
+    } else {
+      flow_rule<TF, true>(ph, xf, tauf, tau_off, edf, Df, psif, nullptr);
+    }
+    TS g[5], Kx[5], H[15];
+    symv5<TS>(K, x, Kx);
+#pragma unroll
+    for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * (TS)edf[i];
+#pragma unroll
+    for (int i = 0; i < 15; i++) H[i] = K[i] + dt * (TS)Df[i];
+    TS p[5], mg[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) mg[i] = -g[i];
+    if (!chol_solve5<TS>(H, mg, p)) { o.failed = 1; break; }
+    TS pn2 = 0, slope = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) { pn2 += p[i] * p[i]; slope += g[i] * p[i]; }
+    const TS pn = sqrt(pn2);
+    TS alpha = 1;
+    // Line search on Phi only for large steps; near the root Newton's full
+    // step is taken (quadratic convergence region).
+    if (pn > (TS)1e-3 * ref && !nc.flow_off) {
+      TS phi0 = 0;
+#pragma unroll
+      for (int i = 0; i < 5; i++) phi0 += x[i] * ((TS)0.5 * Kx[i] + c[i]);
+      phi0 += dt * (TS)psif;
+      for (int ls = 0; ls < 40; ls++) {
+        TS xt[5];
+        TF xtf[5];
+#pragma unroll
+        for (int i = 0; i < 5; i++) { xt[i] = x[i] + alpha * p[i]; xtf[i] = (TF)xt[i]; }
+        TF edt[5], psit;
+        flow_rule<TF, false>(ph, xtf, tauf, tau_off, edt, nullptr, psit, nullptr);
+        TS Kxt[5];
+        symv5<TS>(K, xt, Kxt);
+        TS phi = 0;
+#pragma unroll
+        for (int i = 0; i < 5; i++) phi += xt[i] * ((TS)0.5 * Kxt[i] + c[i]);
+        phi += dt * (TS)psit;
+        if (phi <= phi0 + (TS)1e-4 * alpha * slope) break;
+        TS den = (TS)2 * (phi - phi0 - slope * alpha);
+        TS an = den > (TS)0 ? -slope * alpha * alpha / den : (TS)0.5 * alpha;
+        an = fmin(an, (TS)0.5 * alpha);
+        alpha = fmax(an, (TS)0.1 * alpha);
+        if (alpha * pn <= (TS)1e-14 * (ref + (TS)1)) break;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) x[i] += alpha * p[i];
+    step_norm = sqrt(alpha * alpha * pn2 + hstep2);
+    hstep2 = 0;
+    const TS den = ref > (TS)0 ? ref : sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h);
+    if (!(den > (TS)0) || step_norm <= (TS)nc.tol * den) done = true;
+  }
+  o.iters = it;
+  if (!done) o.failed = 1;
+  // final rates at the solution
+  TF xf[5], edx[5], psid;
+#pragma unroll
+  for (int i = 0; i < 5; i++) xf[i] = (TF)x[i];
+  if (nc.flow_off) {
+#pragma unroll
+    for (int i = 0; i < 5; i++) edx[i] = 0;
+  } else {
+    flow_rule<TF, false>(ph, xf, tauf, tau_off, edx, nullptr, psid, nullptr);
+  }
+  // back to sample axes: s = Q^T x, edot = Q^T edot_x
+  TS ss[5], es[5];
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    TS a = 0, b = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      a += (TS)Q[i * 5 + j] * x[i];
+      b += (TS)Q[i * 5 + j] * (TS)edx[i];
+    }
+    ss[j] = a;
+    es[j] = b;
+  }
+  // error contributions (src/evolution.c:264-299): |sig - lambda| and
+  // |S_gr sig + e_p + edot dt - e|, in sample axes
+  TS cs = dh * dh, ce = 0;
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    const TS ds = ss[i] - (TS)lam6[i];
+    cs += ds * ds;
+    TS de = (TS)ep6[i] + dt * es[i] - (TS)eps6[i];
+#pragma unroll
+    for (int j = 0; j < 5; j++) de += (TS)et[ET_SEL + pk(i, j)] * ss[j];
+    ce += de * de;
+  }
+  {
+    const TS de = (TS)ep6[5] + shh * h - (TS)eps6[5];
+    ce += de * de;
+  }
+  o.conv_s = (double)sqrt(cs);
+  o.conv_e = (double)sqrt(ce);
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    sig6[j] = (TF)ss[j];
+    ed6[j] = (TF)es[j];
+  }
+  sig6[5] = (TF)h;
+  ed6[5] = 0;
+  return o;
+}
+
+// ------------------------------------------------------------ reductions
+template <int W>
+__device__ __forceinline__ void block_reduce_store(double (&v)[W], double* out) {
+  __shared__ double sm[W][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < W; i++) {
+    double a = v[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) sm[i][wid] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < W) {
+    double a = 0;
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; w++) a += sm[threadIdx.x][w];
+    out[(size_t)blockIdx.x * W + threadIdx.x] = a;
+  }
+}
+
+// ------------------------------------------------------------ Newton kernel
+template <typename TSt, typename TF, typename TS>
+__global__ void __launch_bounds__(256) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long P = f.nv;
+  double acc[NPART];
+#pragma unroll
+  for (int i = 0; i < NPART; i++) acc[i] = 0.0;
+  if (v < P) {
+    const int jph = f.phase[v];
+    const PhaseConst& ph = nc.ph[jph];
+    if (ph.type == 0) {
+      TF lam6[6], eps6[6], ep6[6], R[9], Q[25], tauf[NSYS];
+#pragma unroll
+      for (int i = 0; i < 6; i++) {
+        lam6[i] = (TF)f.sig[i * P + v];
+        eps6[i] = (TF)f.strain[i * P + v];
+        ep6[i] = (TF)f.epsp[i * P + v];
+      }
+#pragma unroll
+      for (int i = 0; i < 9; i++) R[i] = (TF)f.rot[i * P + v];
+#pragma unroll
+      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+      rot_to_q<TF>(R, Q);
+      TF s6[6], e6[6];
+      const double* et = f.etab + (size_t)f.eclass[v] * ETAB_W;
+      VoxelOut o = solve_voxel<TF, TS>(nc, ph, Q, et, lam6, eps6, ep6, tauf, s6, e6);
+#pragma unroll
+      for (int i = 0; i < 6; i++) {
+        f.sig[i * P + v] = (TSt)s6[i];
+        f.edot[i * P + v] = (TSt)e6[i];
+      }
+      acc[0] = o.conv_s;
+      acc[1] = o.conv_e;
+#pragma unroll
+      for (int i = 0; i < 6; i++) {
+        acc[2 + i] = (double)s6[i];
+        acc[8 + i] = jph == 0 ? (double)s6[i] : 0.0;
+      }
+      acc[14] = (double)o.iters;
+      acc[15] = (double)o.failed;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 6; i++) {
+        f.sig[i * P + v] = (TSt)0;
+        f.edot[i * P + v] = (TSt)0;
+      }
+    }
+  }
+  block_reduce_store<NPART>(acc, partials);
+}
+
+cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
+                          cudaStream_t st) {
+  if (mixed) {
+    const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+    newton_kernel<float, float, double><<<nblocks, 256, 0, st>>>(nc, f, partials);
+  } else {
+    const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
+    newton_kernel<double, double, double><<<nblocks, 256, 0, st>>>(nc, f, partials);
+  }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- end-of-step kernel
+// Eps += Edot dt (src/evolution.c:1500-1504), update_orient + Orientation
+// (src/constitutive.c:142-273) and harden (src/constitutive.c:275-326).
+// anti_u: uniform part of the lattice spin increment, (2,1),(0,2),(1,0)
+// components of 2 Udot_a dt + antisym(sum dDisGradAvg).
+template <typename TSt, typename TF>
+__global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fields<TSt> f, double au0, double au1,
+                                                       double au2, int do_orient, int do_harden,
+                                                       double* __restrict__ partials) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long P = f.nv;
+  double acc[NPART_END];
+#pragma unroll
+  for (int i = 0; i < NPART_END; i++) acc[i] = 0.0;
+  if (v < P) {
+    const int jph = f.phase[v];
+    const PhaseConst& ph = nc.ph[jph];
+    const TF dt = (TF)nc.dt;
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      const TF ed = (TF)f.edot[i * P + v];
+      const TF ep = (TF)f.epsp[i * P + v] + ed * dt;
+      f.epsp[i * P + v] = (TSt)ep;
+      acc[i] = (double)ep;
+      acc[6 + i] = (double)ed;
+    }
+    if (ph.type == 0 && (do_orient || do_harden)) {
+      TF R[9], Q[25], s6[6], x[5], tauf[NSYS], gam[NSYS], ed[5], psi;
+#pragma unroll
+      for (int i = 0; i < 9; i++) R[i] = (TF)f.rot[i * P + v];
+#pragma unroll
+      for (int i = 0; i < 6; i++) s6[i] = (TF)f.sig[i * P + v];
+#pragma unroll
+      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+      rot_to_q<TF>(R, Q);
+#pragma unroll
+      for (int i = 0; i < 5; i++) {
+        TF a = 0;
+#pragma unroll
+        for (int j = 0; j < 5; j++) a += Q[i * 5 + j] * s6[j];
+        x[i] = a;
+      }
+#pragma unroll
+      for (int s = 0; s < NSYS; s++) gam[s] = 0;
+      if (!nc.flow_off) flow_rule<TF, false>(ph, x, tauf, (TF)ph.tau_back_minus_fwd, ed, nullptr, psi, gam);
+      if (do_orient) {
+        // plastic spin: RotSlip = -1/2 T sum_a gam_a (b_a x n_a)
+        TF cx = 0, cy = 0, cz = 0;
+        for (int s = 0; s < ph.nsys; s++) {
+          const TF b0 = (TF)ph.bb[s][0], b1 = (TF)ph.bb[s][1], b2 = (TF)ph.bb[s][2];
+          const TF n0 = (TF)ph.bn[s][0], n1 = (TF)ph.bn[s][1], n2 = (TF)ph.bn[s][2];
+          cx += gam[s] * (b1 * n2 - b2 * n1);
+          cy += gam[s] * (b2 * n0 - b0 * n2);
+          cz += gam[s] * (b0 * n1 - b1 * n0);
+        }
+        TF ws[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) ws[i] = (TF)-0.5 * (R[i * 3 + 0] * cx + R[i * 3 + 1] * cy + R[i * 3 + 2] * cz);
+        // Rot = (Udot_a + RotLoc - RotSlip) dt, as the vector (Rot21, Rot02, Rot10)
+        TF w[3];
+        w[0] = (TF)au0 + (TF)f.wspin[0 * P + v] - ws[0] * dt;
+        w[1] = (TF)au1 + (TF)f.wspin[1 * P + v] - ws[1] * dt;
+        w[2] = (TF)au2 + (TF)f.wspin[2 * P + v] - ws[2] * dt;
+        // Orientation (src/constitutive.c:142-194)
+        TF wn = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        TF wt = tan(wn / (TF)2);
+        if (fabs(wn) < (TF)1e-6) wn = (TF)1;
+#pragma unroll
+        for (int i = 0; i < 3; i++) w[i] *= wt / wn;
+        TF om[3][3] = {{0, -w[2], w[1]}, {w[2], 0, -w[0]}, {-w[1], w[0], 0}};
+        TF rot[3][3];
+        wt = wt * wt;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            TF o2 = om[i][0] * om[0][j] + om[i][1] * om[1][j] + om[i][2] * om[2][j];
+            rot[i][j] = (TF)(i == j) + (TF)2 * (om[i][j] + o2) / ((TF)1 + wt);
+          }
+        TF Rn[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) Rn[i * 3 + j] = rot[i][0] * R[0 * 3 + j] + rot[i][1] * R[1 * 3 + j] + rot[i][2] * R[2 * 3 + j];
+#pragma unroll
+        for (int i = 0; i < 9; i++) f.rot[i * P + v] = (TSt)Rn[i];
+      }
+      if (do_harden) {
+        const TF gamtot = (TF)f.gamacum[v];
+        TF deltgam = 0;
+        for (int s = 0; s < ph.nsys; s++) deltgam += fabs(gam[s]) * dt;
+        if (deltgam > (TF)0) {
+          const TF tau0 = (TF)ph.tau0f, tau1 = (TF)ph.tau1, th0 = (TF)ph.thet0, th1 = (TF)ph.thet1;
+          const TF tiny = (TF)1e-4 * tau0;
+          TF voce = 0;
+          if (fabs(th0) > tiny) {
+            voce = th1 * deltgam;
+            if (fabs(tau1) > tiny) {
+              const TF fact = fabs(th0 / tau1);
+              const TF exp_ini = exp((TF)-1 * gamtot * fact);
+              const TF exp_del = exp((TF)-1 * deltgam * fact);
+              voce += (TF)-1 * (fact * tau1 - th1) / fact * exp_ini * (exp_del - (TF)1) -
+                      th1 / fact * exp_ini * (exp_del * ((gamtot + deltgam) * fact + (TF)1) - (gamtot * fact + (TF)1));
+            }
+          }
+          for (int s = 0; s < ph.nsys; s++) {
+            TF dtau = 0;
+            for (int j = 0; j < ph.nsys; j++) dtau += (TF)ph.hard[s][j] * fabs(gam[j]) * dt;
+            f.crss[s * P + v] = (TSt)((TF)f.crss[s * P + v] + dtau * voce / deltgam);
+          }
+          f.gamacum[v] = (TSt)(gamtot + deltgam);
+        }
+      }
+    }
+  }
+  block_reduce_store<NPART_END>(acc, partials);
+}
+
+cudaError_t launch_end_step(int mixed, const NewtonConst& nc, const void* fields, const double au[3], int do_orient,
+                            int do_harden, double* partials, int nblocks, cudaStream_t st) {
+  if (mixed) {
+    const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+    end_step_kernel<float, double><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);
+  } else {
+    const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
+    end_step_kernel<double, double><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);
+  }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ set-up kernel
+// Per voxel: crystal->sample matrix from Bunge angles (EulerToTransMatrix,
+// src/kinematics.c:187-240, transposed as at src/init.c:276-278), the
+// elastic initial stress C_gr : <grad u> (src/init.c:470-480) and the
+// initial CRSS (src/init.c:1164-1170).  C066 is summed on the host from the
+// elastic classes.
+template <typename TSt>
+__global__ void __launch_bounds__(256) setup_kernel(const NewtonConst nc, Fields<TSt> f, const double* __restrict__ euler,
+                                                    AddVec d6) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long P = f.nv;
+  if (v >= P) return;
+  const int jph = f.phase[v];
+  const PhaseConst& ph = nc.ph[jph];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    f.strain[i * P + v] = (TSt)0;
+    f.epsp[i * P + v] = (TSt)0;
+    f.edot[i * P + v] = (TSt)0;
+    f.sig[i * P + v] = (TSt)0;
+  }
+  for (int i = 0; i < 3; i++) f.wspin[i * P + v] = (TSt)0;
+  f.gamacum[v] = (TSt)0;
+  double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (ph.type == 0) {
+    const double d2r = 3.14159265359 / 180.;
+    const double t1 = euler[3 * v] * d2r, p = euler[3 * v + 1] * d2r, t2 = euler[3 * v + 2] * d2r;
+    const double ct1 = cos(t1), st1 = sin(t1), cph = cos(p), sph = sin(p), ct2 = cos(t2), st2 = sin(t2);
+    double a[3][3];
+    a[0][0] = ct1 * ct2 - st1 * st2 * cph;
+    a[0][1] = st1 * ct2 + ct1 * st2 * cph;
+    a[0][2] = st2 * sph;
+    a[1][0] = -1.0 * ct1 * st2 - st1 * ct2 * cph;
+    a[1][1] = -1.0 * st1 * st2 + ct1 * ct2 * cph;
+    a[1][2] = ct2 * sph;
+    a[2][0] = st1 * sph;
+    a[2][1] = -1.0 * ct1 * sph;
+    a[2][2] = cph;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) R[i * 3 + j] = a[j][i];
+    const double* et = f.etab + (size_t)f.eclass[v] * ETAB_W;
+    double s6[6];
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      double s = 0;
+#pragma unroll
+      for (int j = 0; j < 5; j++) s += et[ET_CGR + pk(i, j)] * d6.v[j];
+      s6[i] = s;
+    }
+    s6[5] = et[ET_CGR_HH] * d6.v[5];
+#pragma unroll
+    for (int i = 0; i < 6; i++) f.sig[i * P + v] = (TSt)s6[i];
+    for (int s = 0; s < NSYS; s++) f.crss[s * P + v] = (TSt)(s < ph.nsys ? ph.tau0f : 0.0);
+  } else {
+    for (int s = 0; s < NSYS; s++) f.crss[s * P + v] = (TSt)0;
+  }
+#pragma unroll
+  for (int i = 0; i < 9; i++) f.rot[i * P + v] = (TSt)R[i];
+}
+
+cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, const double* euler, const double d6[6],
+                         int nblocks, cudaStream_t st) {
+  AddVec d;
+  for (int i = 0; i < 6; i++) d.v[i] = d6[i];
+  if (mixed) {
+    const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+    setup_kernel<float><<<nblocks, 256, 0, st>>>(nc, f, euler, d);
+  } else {
+    const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
+    setup_kernel<double><<<nblocks, 256, 0, st>>>(nc, f, euler, d);
+  }
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------- batch local solve
+__global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, long long n, double* __restrict__ sig,
+                                                          const double* __restrict__ epsp,
+                                                          const double* __restrict__ strain,
+                                                          const double* __restrict__ rot,
+                                                          const double* __restrict__ crss,
+                                                          const double* __restrict__ etab, double* __restrict__ edot,
+                                                          double* __restrict__ err, long long* __restrict__ iters) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const PhaseConst& ph = nc.ph[0];
+  double lam6[6], eps6[6], ep6[6], R[9], Q[25], tauf[NSYS], s6[6], e6[6];
+  for (int i = 0; i < 6; i++) {
+    lam6[i] = sig[6 * v + i];
+    eps6[i] = strain[6 * v + i];
+    ep6[i] = epsp[6 * v + i];
+  }
+  for (int i = 0; i < 9; i++) R[i] = rot[9 * v + i];
+  for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? crss[NSYS * v + s] : 1.0;
+  rot_to_q<double>(R, Q);
+  VoxelOut o = solve_voxel<double, double>(nc, ph, Q, etab + (size_t)v * ETAB_W, lam6, eps6, ep6, tauf, s6, e6);
+  for (int i = 0; i < 6; i++) {
+    sig[6 * v + i] = s6[i];
+    edot[6 * v + i] = e6[i];
+  }
+  err[2 * v] = o.conv_s;
+  err[2 * v + 1] = o.conv_e;
+  iters[v] = o.iters;
+}
+
+cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, const double* epsp,
+                               const double* strain, const double* rot, const double* crss, const double* etab,
+                               double* edot, double* err, long long* iters, cudaStream_t st) {
+  const int nb = (int)((n + 255) / 256);
+  local_solve_kernel<<<nb, 256, 0, st>>>(nc, n, sig, epsp, strain, rot, crss, etab, edot, err, iters);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------- deterministic reduction
+// out[w] = sum over blocks (fixed order) of partials[b*width + w].
+__global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, int width,
+                                       double* __restrict__ out) {
+  __shared__ double sm[256];
+  for (int w = blockIdx.x; w < width; w += gridDim.x) {
+    double a = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a += partials[(size_t)b * width + w];
+    sm[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[w] = sm[0];
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, cudaStream_t st) {
+  reduce_partials_kernel<<<width, 256, 0, st>>>(partials, nblocks, width, out);
+  return cudaGetLastError();
+}
+
+}  // namespace mth

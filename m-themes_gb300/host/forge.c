@@ -1,0 +1,79 @@
+/*
+ * forge.c -- C driver with the shape of the reference's main (src/evp.c:7-32):
+ * read the namelist given on the command line, set up, evolve N_steps
+ * mechanical steps, tear down.  The solve goes through the C-ABI of
+ * include/mth.h; the per-step scalars go to vm.out in the reference's columns
+ * (TIME EVM EVMP DVM DVMP SVM SVM_1, src/init.c:497 and
+ * src/evolution.c:1621-1625), and the macroscopic stress-strain curve (which
+ * the reference keeps only in globals) to ss.out.
+ *
+ * Usage: forge input.in [--mixed]
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../../include/mth.h"
+
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    fprintf(stderr, "usage: %s input.in [--mixed]\n", argv[0]);
+    return 2;
+  }
+  mth_params p;
+  memset(&p, 0, sizeof(p));
+  char sx1[256], sx2[256], ms[256];
+  if (mth_read_namelist(argv[1], &p, sx1, sx2, ms, sizeof(sx1)) != MTH_OK) {
+    fprintf(stderr, "Input file not found!\n");
+    return 1;
+  }
+  for (int i = 2; i < argc; i++)
+    if (!strcmp(argv[i], "--mixed")) p.precision = MTH_MIXED;
+  if (p.n_phases >= 1 && p.phase[0].type == 0 && mth_read_sx(sx1, &p, 0) != MTH_OK) {
+    fprintf(stderr, "cannot read %s\n", sx1);
+    return 1;
+  }
+  if (p.n_phases == 2 && p.phase[1].type == 0 && mth_read_sx(sx2, &p, 1) != MTH_OK) {
+    fprintf(stderr, "cannot read %s\n", sx2);
+    return 1;
+  }
+  size_t nv = (size_t)p.cell_dim[0] * p.cell_dim[1] * p.cell_dim[2];
+  int* grain = (int*)malloc(sizeof(int) * nv);
+  int* phase = (int*)malloc(sizeof(int) * nv);
+  double* euler = (double*)malloc(sizeof(double) * 3 * nv);
+  if (!grain || !phase || !euler || mth_read_microstructure(ms, p.cell_dim, grain, phase, euler) != MTH_OK) {
+    fprintf(stderr, "Error in reading microstructure data file %s\n", ms);
+    return 1;
+  }
+  mth_ctx* ctx = NULL;
+  mth_status s = mth_create(&p, &ctx);
+  if (s == MTH_OK) s = mth_upload_microstructure(ctx, grain, phase, euler, nv);
+  if (s != MTH_OK) {
+    fprintf(stderr, "set-up failed (%d): %s\n", (int)s, mth_last_error());
+    return 1;
+  }
+  FILE* vm = fopen("vm.out", "w");
+  FILE* ss = fopen("ss.out", "w");
+  fprintf(vm, "TIME\tEVM\tEVMP\tDVM\tDVMP\tSVM\tSVMSVM_1\n");
+  fprintf(ss, "STEP\tITER\tTIME\tE11\tE22\tE33\tS11\tS22\tS33\tERRS\tERRE\n");
+  for (int istep = 0; istep < p.n_steps; istep++) {
+    mth_step_report r;
+    s = mth_step(ctx, &r);
+    if (s != MTH_OK) {
+      fprintf(stderr, "step %d failed (%d): %s\n", istep, (int)s, mth_last_error());
+      break;
+    }
+    fprintf(vm, "%e\t%e\t%e\t%e\t%e\t%e\t%e\n", r.time, r.e_vm, r.evmp, r.d_vm, r.dvmp, r.s_vm, r.s_vm1);
+    fprintf(ss, "%d\t%d\t%e\t%.9e\t%.9e\t%.9e\t%.9e\t%.9e\t%.9e\t%e\t%e\n", istep, r.iterations, r.time,
+            r.disgrad_avg[0][0], r.disgrad_avg[1][1], r.disgrad_avg[2][2], r.sig_avg[0][0], r.sig_avg[1][1],
+            r.sig_avg[2][2], r.err_s, r.err_e);
+    fflush(vm);
+    fflush(ss);
+  }
+  fclose(vm);
+  fclose(ss);
+  mth_destroy(ctx);
+  free(grain);
+  free(phase);
+  free(euler);
+  return s == MTH_OK ? 0 : 1;
+}

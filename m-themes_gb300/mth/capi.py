@@ -48,7 +48,7 @@ class MthParams(C.Structure):
                 ("m_gb", C.c_double), ("pf_width_cells", C.c_double), ("stored_energy_scale", C.c_double),
                 ("shear_modulus", C.c_double), ("burgers", C.c_double), ("nucleus_radius", C.c_int),
                 ("rho_nucleation", C.c_double), ("rho0", C.c_double), ("rho_k", C.c_double),
-                ("pf_substeps", C.c_int), ("seed", C.c_uint64)]
+                ("pf_substeps", C.c_int), ("seed", C.c_uint64), ("device", C.c_int)]
 
 
 T33 = (C.c_double * 3) * 3
@@ -70,6 +70,18 @@ class MthStepReport(C.Structure):
                 v = np.array([[v[i][j] for j in range(3)] for i in range(3)])
             d[name] = v
         return d
+
+
+class MthProfile(C.Structure):
+    _fields_ = [("n_kernels", C.c_int), ("name", (C.c_char * 32) * 16), ("ms", C.c_double * 16),
+                ("launches", C.c_longlong * 16), ("bytes", C.c_double * 16), ("total_launches", C.c_longlong)]
+
+    def to_dict(self):
+        out = {}
+        for k in range(self.n_kernels):
+            out[bytes(self.name[k]).split(b"\0")[0].decode()] = {
+                "ms": self.ms[k], "launches": self.launches[k], "bytes": self.bytes[k]}
+        return out
 
 
 def params_from_config(cfg, precision=MTH_FP64, newton_tol=0.0, newton_itmax=0) -> MthParams:
@@ -144,10 +156,12 @@ def load(path: str | None = None):
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    lib.mth_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    lib.mth_profile_read.argtypes = [C.c_void_p, C.POINTER(MthProfile), C.c_int]
     lib.mth_read_namelist.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_char_p, C.c_char_p, C.c_char_p,
                                       C.c_size_t]
     lib.mth_read_sx.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_int]
-    lib.mth_read_microstructure.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
+    lib.mth_read_microstructure.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
     if path is None:
         _lib = lib

@@ -40,6 +40,15 @@ class Solver:
         capi.check(self.lib, self.lib.mth_download_field(self.ctx, f, capi._dptr(out), out.size))
         return out.reshape(self.nv, -1)
 
+    def profile(self, enable=None, reset=False):
+        """Per-kernel device times (CUDA events on the context's stream),
+        launch counts and algorithmic bytes; optionally switch timing on/off."""
+        if enable is not None:
+            capi.check(self.lib, self.lib.mth_profile_enable(self.ctx, 1 if enable else 0))
+        pr = capi.MthProfile()
+        capi.check(self.lib, self.lib.mth_profile_read(self.ctx, C.byref(pr), 1 if reset else 0))
+        return pr.to_dict(), pr.total_launches
+
     def close(self):
         if getattr(self, "ctx", None):
             self.lib.mth_destroy(self.ctx)

@@ -1,0 +1,149 @@
+"""GPU parity: the CUDA path, called through the C-ABI, against the
+reference's golden traces and the oracle.
+
+Tolerances: FP64 mode must match the reference's macroscopic stress and
+strain to 1e-6 relative (and the fields to 1e-6 relative L2); mixed
+precision (FP32 fields/FFT/Green operator, FP64 local Newton solve) must stay
+within 1e-4 relative on the macroscopic stress.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import (GOLDEN_CASES, T_DG, T_EPS, T_ITER, T_SIG, T_SVM, load_golden, rel, rel_l2, run_gpu,
+                     run_oracle)
+from mth import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+FP64_MACRO = 1e-6
+FP64_FIELD = 1e-6
+MIXED_MACRO = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    import os
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call([sys.executable, os.path.join(repo, "m-themes_gb300", "build.py")])
+    return capi.load()
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_fp64_matches_reference(name):
+    cfg, trace, fields = load_golden(name)
+    s, reps = run_gpu(cfg, capi.MTH_FP64)
+    for k, r in enumerate(reps):
+        row = trace[k]
+        assert r["iterations"] == int(row[T_ITER]), (k, r["iterations"], row[T_ITER])
+        assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < FP64_MACRO, k
+        assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < FP64_MACRO, k
+        assert rel(r["eps_avg"], row[T_EPS].reshape(3, 3)) < 1e-5, k
+        assert abs(r["s_vm"] - row[T_SVM]) < FP64_MACRO * row[T_SVM], k
+        assert r["newton_failed"] == 0
+    if fields:
+        assert rel_l2(s.field("sig"), fields["sig"]) < FP64_FIELD
+        dg = fields["disgrad"].reshape(-1, 3, 3)
+        strain = 0.5 * (dg + dg.transpose(0, 2, 1)).reshape(-1, 9)
+        assert rel_l2(s.field("strain"), strain) < FP64_FIELD
+        assert rel_l2(s.field("eps"), fields["eps"]) < 1e-5
+        assert rel(s.field("rot"), fields["rot"]) < 1e-8
+        assert rel(s.field("crss"), fields["crss"]) < 1e-7
+    s.close()
+
+
+@pytest.mark.parametrize("name", ["g8_poly", "g12_radix3", "g16_pores", "g8_shear"])
+def test_mixed_within_tolerance(name):
+    cfg, trace, _ = load_golden(name)
+    s, reps = run_gpu(cfg, capi.MTH_MIXED)
+    for k, r in enumerate(reps):
+        assert rel(r["sig_avg"], trace[k][T_SIG].reshape(3, 3)) < MIXED_MACRO, k
+        assert rel(r["disgrad_avg"], trace[k][T_DG].reshape(3, 3)) < MIXED_MACRO, k
+    s.close()
+
+
+@pytest.mark.parametrize("dims", [(48, 8, 16), (8, 24, 6), (32, 32, 32)])
+def test_fp64_matches_oracle_shapes(dims):
+    cfg = synth.Config(cell_dim=dims, n_grains=12, n_steps=3, seed=31, iter_max=12)
+    o, ro = run_oracle(cfg)
+    s, rg = run_gpu(cfg, capi.MTH_FP64)
+    for a, b in zip(rg, ro):
+        assert a["iterations"] == b["iterations"]
+        assert rel(a["sig_avg"], b["sig_avg"]) < FP64_MACRO
+        assert rel(a["disgrad_avg"], b["disgrad_avg"]) < FP64_MACRO
+    assert rel_l2(s.field("sig"), o.field("sig")) < FP64_FIELD
+    assert rel(s.field("rot"), o.field("rot")) < 1e-8
+    s.close()
+
+
+def test_local_solve_matches_oracle():
+    import pyoracle
+    from test_oracle_cpu import random_states
+    cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=4)
+    p = capi.params_from_config(cfg)
+    o = pyoracle.Oracle(p, *synth.microstructure(cfg), nthreads=2)
+    c066 = o.c066()
+    rng = np.random.default_rng(11)
+    st = random_states(512, rng, cfg)
+    so, eo, erro, _ = pyoracle.local_solve(p, c066, *st)
+    from mth import local_solve
+    sg, eg, errg, it = local_solve(p, c066, *st)
+    assert it > 0
+    assert rel(sg, so) < 1e-8
+    assert rel(eg, eo) < 1e-6
+    assert rel(errg[:, 0], erro[:, 0]) < 1e-6
+
+
+def test_deterministic_fp64():
+    cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=6, n_steps=2, seed=9, iter_max=8)
+    s1, r1 = run_gpu(cfg, capi.MTH_FP64)
+    s2, r2 = run_gpu(cfg, capi.MTH_FP64)
+    assert np.array_equal(s1.field("sig"), s2.field("sig"))
+    assert all(np.array_equal(a["sig_avg"], b["sig_avg"]) for a, b in zip(r1, r2))
+
+
+def test_fullsize_mixed_properties():
+    """128^3, 512 grains, 40 pores: the benchmark workload for 2 steps of 6
+    Green iterations; size-independent checks."""
+    cfg = synth.workload("c1")
+    cfg.n_steps = 2
+    cfg.iter_max = 6
+    g, p, e = synth.microstructure(cfg)
+    from mth import Solver
+    s = Solver(capi.params_from_config(cfg, precision=capi.MTH_MIXED), g, p, e)
+    reps = [s.step() for _ in range(2)]
+    sig = s.field("sig").reshape(-1, 3, 3)
+    assert np.all(np.isfinite(sig))
+    assert np.array_equal(sig, sig.transpose(0, 2, 1))
+    assert np.all(sig[p == 2] == 0.0)
+    for k, r in enumerate(reps):
+        # the imposed strain rate: <grad u>_33 grows by dt per step
+        assert abs(r["disgrad_avg"][2, 2] - (k + 1) * cfg.time_step) < 1e-12
+        assert r["iterations"] == cfg.iter_max
+    rot = s.field("rot").reshape(-1, 3, 3)
+    ortho = np.einsum("vij,vkj->vik", rot[p == 1], rot[p == 1]) - np.eye(3)
+    assert np.abs(ortho).max() < 1e-5
+    s.close()
+
+
+def test_status_codes():
+    lib = capi.load()
+    cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=2)
+    p = capi.params_from_config(cfg)
+    ctx = C.c_void_p()
+    capi.check(lib, lib.mth_create(C.byref(p), C.byref(ctx)))
+    rep = capi.MthStepReport()
+    assert lib.mth_step(ctx, C.byref(rep)) == 7              # before upload
+    g, ph, e = synth.microstructure(cfg)
+    bad = ph.copy()
+    bad[3] = 5
+    assert lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(bad), capi._dptr(e), g.size) == 1
+    assert lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(ph), capi._dptr(e), g.size - 1) == 1
+    capi.check(lib, lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(ph), capi._dptr(e), g.size))
+    out = np.zeros(10)
+    assert lib.mth_download_field(ctx, 0, capi._dptr(out), 10) == 1
+    assert lib.mth_step(ctx, C.byref(rep)) == 0
+    assert lib.mth_destroy(ctx) == 0

@@ -1,0 +1,38 @@
+"""The oracle against the reference's own outputs.
+
+The golden fixtures come from the reference M-THEMES sources compiled here
+with single-rank stand-ins (tests/golden/make_golden.py); the oracle must
+reproduce their per-step trace and final fields to round-off.
+"""
+import numpy as np
+import pytest
+
+from helpers import (GOLDEN_CASES, T_DG, T_EDOT, T_EPS, T_ERRE, T_ERRS, T_ITER, T_SIG, T_SVM, T_SVM1, load_golden,
+                     rel, run_oracle)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_oracle_matches_reference_trace(name):
+    cfg, trace, fields = load_golden(name)
+    o, reps = run_oracle(cfg, nthreads=4)
+    for s, r in enumerate(reps):
+        row = trace[s]
+        assert r["iterations"] == int(row[T_ITER]), (s, r["iterations"], row[T_ITER])
+        assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-11
+        assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-11
+        assert rel(r["eps_avg"], row[T_EPS].reshape(3, 3)) < 1e-9
+        assert rel(r["edot_avg"], row[T_EDOT].reshape(3, 3)) < 1e-9
+        assert abs(r["s_vm"] - row[T_SVM]) <= 1e-11 * abs(row[T_SVM])
+        assert abs(r["s_vm1"] - row[T_SVM1]) <= 1e-11 * abs(row[T_SVM1])
+        assert abs(r["err_s"] - row[T_ERRS]) <= 1e-7 * abs(row[T_ERRS])
+        assert abs(r["err_e"] - row[T_ERRE]) <= 1e-7 * abs(row[T_ERRE]) + 1e-18
+    if fields:
+        assert rel(o.field("sig"), fields["sig"]) < 1e-10
+        assert rel(o.field("eps"), fields["eps"]) < 1e-9
+        assert rel(o.field("rot"), fields["rot"]) < 1e-12
+        assert rel(o.field("crss"), fields["crss"]) < 1e-12
+        assert rel(o.field("gamacum")[:, 0], fields["gamacum"][:, 0]) < 1e-9
+        dg = fields["disgrad"].reshape(-1, 3, 3)
+        strain = 0.5 * (dg + dg.transpose(0, 2, 1))
+        assert rel(o.field("strain"), strain.reshape(-1, 9)) < 1e-10
+    assert o.second_backtracks() == 0
