@@ -164,6 +164,30 @@ mth_status mth_local_solve(const mth_params* params, const double c066[36], size
                            const double* rot, const double* crss, double* edot,
                            double* err, long long* newton_iters);
 
+/* Allocation-free batch local solve.  No counterpart in the reference.
+ * Same computation and argument meaning as mth_local_solve, but every array
+ * is a DEVICE pointer owned by the caller, and the call allocates nothing:
+ * no cudaMalloc/cudaFree and no allocating library routine.  It is meant for
+ * callers that cannot allocate device memory during a solve: a host
+ * application that hands out all device memory from its own preallocated pool
+ * (an allocation behind its back would bypass the pool's accounting and could
+ * fail on a GPU that the pool has filled), and code that must not trigger the
+ * implicit device synchronisation a cudaMalloc/cudaFree can cause.
+ * Its only scratch (per-block partial sums) is a fixed array in the library's
+ * device image, held by every GPU that loads the library until the process
+ * exits; n may not exceed MTH_NOALLOC_MAX_VOXELS (MTH_ERR_ARG otherwise).
+ * The first call on each device looks up that array's device address, so
+ * make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (different streams or threads) race, so serialise them.
+ * stream: a cudaStream_t passed as void* (NULL = the default stream); the
+ * call returns after the stream has finished the solve.  The device is
+ * params->device. */
+#define MTH_NOALLOC_MAX_VOXELS (1LL << 20)
+mth_status mth_local_solve_noalloc(const mth_params* params, const double c066[36], size_t n,
+                                   double* d_sig, const double* d_eps_p, const double* d_strain,
+                                   const double* d_rot, const double* d_crss, double* d_edot,
+                                   double* d_err, long long* newton_iters, void* stream);
+
 /* Per-kernel device timing.  When enabled, every kernel launch of the context
  * is bracketed by CUDA events on the context's stream; times are summed per
  * kernel class.  Launch counts are kept whether or not timing is enabled.

@@ -857,6 +857,40 @@ extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, si
   return c->mixed ? download<float>(c, field, host) : download<double>(c, field, host);
 }
 
+// ------------------------------------------------- allocation-free local solve
+extern "C" mth_status mth_local_solve_noalloc(const mth_params* p, const double c066[36], size_t n, double* d_sig,
+                                              const double* d_eps_p, const double* d_strain, const double* d_rot,
+                                              const double* d_crss, double* d_edot, double* d_err,
+                                              long long* newton_iters, void* stream) {
+  if (!p || !c066 || !d_sig || !d_eps_p || !d_strain || !d_rot || !d_crss || !d_edot || !d_err)
+    return set_err(MTH_ERR_ARG, "null argument");
+  if ((long long)n > noalloc_max_voxels())
+    return set_err(MTH_ERR_ARG, "n=%zu exceeds the allocation-free limit of %lld voxels", n, noalloc_max_voxels());
+  if (n == 0) {
+    if (newton_iters) *newton_iters = 0;
+    return MTH_OK;
+  }
+  NewtonConst nc;
+  memset(&nc, 0, sizeof(nc));
+  mth_status s = fill_phase(p->phase[0], nc.ph[0]);
+  if (s) return s;
+  if (p->phase[0].type != 0) return set_err(MTH_ERR_ARG, "phase 1 must be a crystal");
+  double cm[6][6], sm[6][6];
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) cm[i][j] = c066[i * 6 + j];
+  if (!inv6(cm, sm)) return set_err(MTH_ERR_SINGULAR, "C066 singular");
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 5; j++) nc.s0dev[i * 5 + j] = sm[i][j];
+  nc.s0hh = sm[5][5];
+  nc.dt = p->time_step;
+  nc.tol = p->newton_tol > 0 ? p->newton_tol : 1e-10;
+  nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
+  CK(cudaSetDevice(p->device));
+  CK(launch_local_solve_noalloc(nc, (long long)n, d_sig, d_eps_p, d_strain, d_rot, d_crss, d_edot, d_err,
+                                newton_iters, static_cast<cudaStream_t>(stream)));
+  return MTH_OK;
+}
+
 // ------------------------------------------------------------- profiling
 extern "C" mth_status mth_profile_enable(mth_ctx* c, int on) {
   if (!c) return set_err(MTH_ERR_ARG, "null context");

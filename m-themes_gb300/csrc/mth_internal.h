@@ -97,6 +97,10 @@ cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, c
 cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, const double* epsp,
                                const double* strain, const double* rot, const double* crss, const double* etab,
                                double* edot, double* err, long long* iters, cudaStream_t st);
+long long noalloc_max_voxels();
+cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,
+                                       const double* strain, const double* rot, const double* crss, double* edot,
+                                       double* err, long long* iters_host, cudaStream_t st);
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, cudaStream_t st);
 
 }  // namespace mth

@@ -716,4 +716,113 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, int widt
   return cudaGetLastError();
 }
 
+
+// ------------------------------------------------ allocation-free local solve
+// Variant of local_solve_kernel for callers that cannot allocate device
+// memory: the caller passes device pointers for every input and output, the
+// elastic rows are built in the kernel from each voxel's rotation, and the
+// only scratch (per-block Newton-iteration partial sums and their total)
+// lives in the fixed array below, which every GPU that loads the library holds
+// until the process exits.  Calls that overlap on the GPU share it and race.
+namespace {
+constexpr long long NOALLOC_MAX_VOXELS = 1LL << 20;
+constexpr int NOALLOC_MAX_BLOCKS = (int)(NOALLOC_MAX_VOXELS / 256);
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_MAX_BLOCKS + 1];
+
+__global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonConst nc, long long n, double* sig,
+                                                                  const double* __restrict__ epsp,
+                                                                  const double* __restrict__ strain,
+                                                                  const double* __restrict__ rot,
+                                                                  const double* __restrict__ crss,
+                                                                  double* __restrict__ edot, double* __restrict__ err,
+                                                                  double* __restrict__ scratch) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[1] = {0.0};
+  if (v < n) {
+    const PhaseConst& ph = nc.ph[0];
+    double lam6[6], eps6[6], ep6[6], R[9], Q[25], tauf[NSYS], s6[6], e6[6], et[ETAB_W];
+    for (int i = 0; i < 6; i++) {
+      lam6[i] = sig[6 * v + i];
+      eps6[i] = strain[6 * v + i];
+      ep6[i] = epsp[6 * v + i];
+    }
+    for (int i = 0; i < 9; i++) R[i] = rot[9 * v + i];
+    for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? crss[NSYS * v + s] : 1.0;
+    rot_to_q<double>(R, Q);
+    // elastic row of this voxel: S_gr = Q^T diag(s_xt) Q, S_tot = S0 + S_gr
+    for (int i = 0; i < 5; i++)
+      for (int j = i; j < 5; j++) {
+        double sg = 0;
+        for (int k = 0; k < 5; k++) sg += Q[k * 5 + i] * ph.s_xt[k] * Q[k * 5 + j];
+        et[ET_SEL + pk(i, j)] = sg;
+        et[ET_STOT + pk(i, j)] = nc.s0dev[i * 5 + j] + sg;
+      }
+    et[ET_SEL_HH] = ph.s_xt[5];
+    VoxelOut o = solve_voxel<double, double>(nc, ph, Q, et, lam6, eps6, ep6, tauf, s6, e6);
+    for (int i = 0; i < 6; i++) {
+      sig[6 * v + i] = s6[i];
+      edot[6 * v + i] = e6[i];
+    }
+    err[2 * v] = o.conv_s;
+    err[2 * v + 1] = o.conv_e;
+    acc[0] = (double)o.iters;
+  }
+  block_reduce_store<1>(acc, scratch);
+}
+
+__global__ void noalloc_total_kernel(double* scratch, int nblocks) {
+  __shared__ double sm[256];
+  double a = 0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a += scratch[b];
+  sm[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) scratch[NOALLOC_MAX_BLOCKS] = sm[0];
+}
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current (the host-side name is only a stand-in, not a device
+// address).
+constexpr int NOALLOC_MAX_DEVICES = 64;
+double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+}  // namespace
+
+long long noalloc_max_voxels() { return NOALLOC_MAX_VOXELS; }
+
+cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,
+                                       const double* strain, const double* rot, const double* crss, double* edot,
+                                       double* err, long long* iters_host, cudaStream_t st) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  if (!g_noalloc_ptr[dev]) {
+    double* p = nullptr;
+    e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = p;
+  }
+  double* scratch = g_noalloc_ptr[dev];
+  const int nb = (int)((n + 255) / 256);
+  // the total slot is the only one read without being written first
+  e = cudaMemsetAsync(scratch + NOALLOC_MAX_BLOCKS, 0, sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  local_solve_noalloc_kernel<<<nb, 256, 0, st>>>(nc, n, sig, epsp, strain, rot, crss, edot, err, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  noalloc_total_kernel<<<1, 256, 0, st>>>(scratch, nb);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  double tot = 0;
+  e = cudaMemcpyAsync(&tot, scratch + NOALLOC_MAX_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (iters_host) *iters_host = (long long)tot;
+  return cudaSuccess;
+}
+
 }  // namespace mth

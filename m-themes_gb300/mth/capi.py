@@ -156,6 +156,9 @@ def load(path: str | None = None):
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    lib.mth_local_solve_noalloc.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_double), C.c_size_t,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong), C.c_void_p]
     lib.mth_profile_enable.argtypes = [C.c_void_p, C.c_int]
     lib.mth_profile_read.argtypes = [C.c_void_p, C.POINTER(MthProfile), C.c_int]
     lib.mth_read_namelist.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_char_p, C.c_char_p, C.c_char_p,
