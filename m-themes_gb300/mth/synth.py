@@ -255,10 +255,14 @@ def write_case(directory, cfg: Config):
 # ------------------------------------------------------ named workloads
 def workload(name: str) -> Config:
     """Benchmark workloads: 'c0' = 32^3 / 64 grains FP64 plain EVPFFT, 10 steps;
-    'c1' = 128^3 / 512 grains + 40 radius-3 pores, 100 steps."""
+    'c1' = 128^3 / 512 grains + 40 radius-3 pores, 100 steps; 'c1m' = the same at 96^3
+    (216 grains, 17 pores) for profiler captures."""
     if name == "c0":
         return Config(cell_dim=(32, 32, 32), n_grains=64, n_steps=10, seed=20240101)
     if name == "c1":
         return Config(cell_dim=(128, 128, 128), n_grains=512, n_pores=40, pore_radius=3,
                       n_steps=100, seed=20240102)
+    if name == "c1m":   # 96^3 profiling case of c1: fields still larger than L2
+        return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
+                      n_steps=100, seed=20240103)
     raise KeyError(name)
