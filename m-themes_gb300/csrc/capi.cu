@@ -574,6 +574,8 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   m2t4(c->c066, c->gc.c0);
   for (int i = 0; i < 6; i++)
     for (int j = 0; j < 6; j++) c->gc.s066[i * 6 + j] = c->s066[i][j];
+  for (int i = 0; i < 81; i++) c->gc.c0f[i] = (float)c->gc.c0[i];
+  for (int i = 0; i < 36; i++) c->gc.s066f[i] = (float)c->gc.s066[i];
   c->gc.elast_bc = c->p.elast_bc;
   m2t4(c->s066, c->s0_4);
   for (int i = 0; i < 5; i++)

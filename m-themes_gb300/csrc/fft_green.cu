@@ -216,13 +216,18 @@ __global__ void __launch_bounds__(256) fft_strided_kernel(c2<T>* __restrict__ sp
 }
 
 // ------------------------------------------------------- Green operator
-// Unit wave vector of index idx on an axis of n points: the frequency of
-// src/init.c:778-786 (idx/n - round(idx/n), Nyquist -> -1/2).
+// Frequency of index idx on an axis of n points: idx/n - round(idx/n) of
+// src/init.c:778-786 (the Nyquist index maps to -1/2), from integers.
 template <typename T> __device__ __forceinline__ T freq(int idx, int n) {
-  double t = (double)idx * (1.0 / (double)n);
-  t -= round(t);
-  return (T)t;
+  const int k = (2 * idx >= n) ? idx - n : idx;
+  return (T)k / (T)n;
 }
+template <typename T> __device__ __forceinline__ T c0_at(const GreenConst& gc, int i);
+template <> __device__ __forceinline__ float c0_at<float>(const GreenConst& gc, int i) { return gc.c0f[i]; }
+template <> __device__ __forceinline__ double c0_at<double>(const GreenConst& gc, int i) { return gc.c0[i]; }
+template <typename T> __device__ __forceinline__ T s066_at(const GreenConst& gc, int i);
+template <> __device__ __forceinline__ float s066_at<float>(const GreenConst& gc, int i) { return gc.s066f[i]; }
+template <> __device__ __forceinline__ double s066_at<double>(const GreenConst& gc, int i) { return gc.s066[i]; }
 
 // Delta = -Omega(n) (sig n) (x) n for one n; accumulates into dsym (LT, 6
 // complex) and danti (3 complex: [2][1], [0][2], [1][0]) with weight wgt.
@@ -238,7 +243,7 @@ __device__ __forceinline__ void green_apply_n(const GreenConst& gc, const T n[3]
 #pragma unroll
       for (int j = 0; j < 3; j++)
 #pragma unroll
-        for (int l = 0; l < 3; l++) a += (T)gc.c0[((i * 3 + j) * 3 + k) * 3 + l] * n[j] * n[l];
+        for (int l = 0; l < 3; l++) a += c0_at<T>(gc, ((i * 3 + j) * 3 + k) * 3 + l) * n[j] * n[l];
       A[i][k] = a;
       A[k][i] = a;
     }
@@ -300,8 +305,8 @@ __device__ __forceinline__ void green_point(const GreenConst& gc, int kx, int ky
       for (int i = 0; i < 6; i++) {
         T re = 0, im = 0;
         for (int j = 0; j < 6; j++) {
-          re -= (T)gc.s066[i * 6 + j] * sig[j].x;
-          im -= (T)gc.s066[i * 6 + j] * sig[j].y;
+          re -= s066_at<T>(gc, i * 6 + j) * sig[j].x;
+          im -= s066_at<T>(gc, i * 6 + j) * sig[j].y;
         }
         dsym[i] = mk<T>(re, im);
       }

@@ -26,6 +26,8 @@ struct AddVec { double v[6]; };
 struct GreenConst {
   double c0[81];      // C0_ijkl (chg_basis of C066, src/init.c:376)
   double s066[36];    // S066 = C066^-1 (used at k=0 when ElastBC=0)
+  float c0f[81];      // single-precision copies for the FP32 pass
+  float s066f[36];
   int elast_bc;
 };
 

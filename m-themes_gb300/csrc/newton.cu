@@ -61,30 +61,38 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
   const int ns = ph.nsys;
   const TF n = (TF)ph.nrs;
   const TF g0 = (TF)ph.gamd0;
+  const TF inv_np1 = (TF)1 / (n + (TF)1);
   const int nm1 = ph.nrs_int > 0 ? ph.nrs_int - 1 : 0;
-  for (int s = 0; s < ns; s++) {
-    TF m[5];
+  // fully unrolled over the NSYS slots so the per-voxel CRSS stay in registers
 #pragma unroll
-    for (int i = 0; i < 5; i++) m[i] = (TF)ph.m_xt[s][i];
-    const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
-    const TF tau = rss < (TF)0 ? tauf[s] + tau_off : tauf[s];
-    const TF r = rss / tau;
-    const TF ar = fabs(r);
-    const TF pnm1 = pow_abs<TF>(ar, nm1, n - (TF)1);   // |r|^(n-1)
-    const TF pn = pnm1 * ar;                             // |r|^n
-    const TF g = g0 * (r > (TF)0 ? pn : -pn);
-    if (gam) gam[s] = g;
+  for (int s = 0; s < NSYS; s++) {
+    if (s < ns) {
+      TF m[5];
 #pragma unroll
-    for (int i = 0; i < 5; i++) ed[i] += m[i] * g;
-    if (WANT_D) {
-      const TF w = g0 * n * pnm1 / tau;
-      int q = 0;
+      for (int i = 0; i < 5; i++) m[i] = (TF)ph.m_xt[s][i];
+      const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
+      const TF tau = rss < (TF)0 ? tauf[s] + tau_off : tauf[s];
+      const TF itau = (TF)1 / tau;
+      const TF r = rss * itau;
+      const TF ar = fabs(r);
+      const TF pnm1 = pow_abs<TF>(ar, nm1, n - (TF)1);   // |r|^(n-1)
+      const TF pn = pnm1 * ar;                             // |r|^n
+      const TF g = g0 * (r > (TF)0 ? pn : -pn);
+      if (gam) gam[s] = g;
 #pragma unroll
-      for (int i = 0; i < 5; i++)
+      for (int i = 0; i < 5; i++) ed[i] += m[i] * g;
+      if (WANT_D) {
+        const TF w = g0 * n * pnm1 * itau;
+        int q = 0;
 #pragma unroll
-        for (int j = i; j < 5; j++) D[q++] += w * m[i] * m[j];
+        for (int i = 0; i < 5; i++)
+#pragma unroll
+          for (int j = i; j < 5; j++) D[q++] += w * m[i] * m[j];
+      }
+      psi += g0 * tau * pn * ar * inv_np1;
+    } else if (gam) {
+      gam[s] = 0;
     }
-    psi += g0 * tau * pn * ar / (n + (TF)1);
   }
 }
 
@@ -104,51 +112,50 @@ __device__ __forceinline__ void symv5(const T* K, const T* x, T* y) {
   }
 }
 
-// Cholesky solve of the packed SPD matrix A (5x5): x = A^-1 b.  Returns
-// false when a pivot is not positive.
+// LDL^T solve of the packed symmetric positive definite 5x5 matrix A:
+// x = A^-1 b.  Returns false when a pivot is not positive.
 template <typename T>
-__device__ __forceinline__ bool chol_solve5(const T* A, const T* b, T* x) {
-  T L[15];
+__device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
+  T L[5][5], d[5], id[5];
 #pragma unroll
-  for (int i = 0; i < 15; i++) L[i] = A[i];
-  // L stored packed by rows of the upper triangle: L^T (upper) in place
+  for (int j = 0; j < 5; j++) {
+    T v[5];
+    T dj = A[pk(j, j)];
 #pragma unroll
-  for (int k = 0; k < 5; k++) {
-    T d = L[pk(k, k)];
-#pragma unroll
-    for (int p = 0; p < 5; p++)
-      if (p < k) d -= L[pk(p, k)] * L[pk(p, k)];
-    if (!(d > (T)0)) return false;
-    d = sqrt(d);
-    L[pk(k, k)] = d;
-    const T id = (T)1 / d;
-#pragma unroll
-    for (int j = 0; j < 5; j++) {
-      if (j > k) {
-        T s = L[pk(k, j)];
-#pragma unroll
-        for (int p = 0; p < 5; p++)
-          if (p < k) s -= L[pk(p, k)] * L[pk(p, j)];
-        L[pk(k, j)] = s * id;
+    for (int k = 0; k < 5; k++)
+      if (k < j) {
+        v[k] = L[j][k] * d[k];
+        dj -= L[j][k] * v[k];
       }
-    }
+    if (!(dj > (T)0)) return false;
+    d[j] = dj;
+    id[j] = (T)1 / dj;
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+      if (i > j) {
+        T a = A[pk(i, j)];
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+          if (k < j) a -= L[i][k] * v[k];
+        L[i][j] = a * id[j];
+      }
   }
   T y[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) {
-    T s = b[i];
+    T a = b[i];
 #pragma unroll
-    for (int p = 0; p < 5; p++)
-      if (p < i) s -= L[pk(p, i)] * y[p];
-    y[i] = s / L[pk(i, i)];
+    for (int k = 0; k < 5; k++)
+      if (k < i) a -= L[i][k] * y[k];
+    y[i] = a;
   }
 #pragma unroll
   for (int i = 4; i >= 0; i--) {
-    T s = y[i];
+    T a = y[i] * id[i];
 #pragma unroll
-    for (int p = 0; p < 5; p++)
-      if (p > i) s -= L[pk(i, p)] * x[p];
-    x[i] = s / L[pk(i, i)];
+    for (int k = 0; k < 5; k++)
+      if (k > i) a -= L[k][i] * x[k];
+    x[i] = a;
   }
   return true;
 }
@@ -164,16 +171,19 @@ struct VoxelOut {
 // (lambda = current stress, total strain, plastic strain); Q: sample->crystal
 // 5x5 of the current lattice orientation; et: elastic-class row (initial
 // orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
-// (plastic strain rate, sample frame).  TF: flow-rule and frame-transform
-// type; TS: Newton solve type.
-template <typename TF, typename TS>
+// (plastic strain rate, sample frame).
+// TF: flow rule, residual, Hessian assembly, line search and frame
+// transforms; TL: the Jacobian (Hessian) solve.  FP64 mode: both double.
+// Mixed mode: TF = float, TL = double (GB300 issues FP64 at 1/64 of the FP32
+// rate, so only the 5x5 solve stays in FP64).
+template <typename TF, typename TL>
 __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const double* __restrict__ et,
                                 const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* tauf, TF* sig6,
                                 TF* ed6) {
   VoxelOut o = {0.0, 0.0, 0, 0};
-  const TS dt = (TS)nc.dt;
+  const TF dt = (TF)nc.dt;
   // crystal-frame inputs
-  TF lamx[5], epsx[5], epx[5], s0s[5], s0l[5];
+  TF lamx[5], epsx[5], epx[5], s0s[5], c[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) {
     TF a = 0;
@@ -183,18 +193,19 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
   }
 #pragma unroll
   for (int i = 0; i < 5; i++) {
-    TF a = 0, b = 0, c = 0, d = 0;
+    TF a = 0, b = 0, e = 0, d = 0;
 #pragma unroll
     for (int j = 0; j < 5; j++) {
       a += Q[i * 5 + j] * lam6[j];
       b += Q[i * 5 + j] * eps6[j];
-      c += Q[i * 5 + j] * ep6[j];
+      e += Q[i * 5 + j] * ep6[j];
       d += Q[i * 5 + j] * s0s[j];
     }
-    lamx[i] = a; epsx[i] = b; epx[i] = c; s0l[i] = d;   // crystal axes
+    lamx[i] = a; epsx[i] = b; epx[i] = e;
+    c[i] = -d + e - b;   // gradient of Phi = K x + c + dt edot
   }
   // Hessian base K = Q (S0 + S_gr) Q^T in crystal axes of the current lattice
-  TS K[15];
+  TF K[15];
   {
     TF St[25], t[25];
 #pragma unroll
@@ -205,52 +216,40 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
     for (int i = 0; i < 5; i++)
 #pragma unroll
       for (int j = 0; j < 5; j++) {
-        TF s = 0;
+        TF a = 0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) s += Q[i * 5 + k] * St[k * 5 + j];
-        t[i * 5 + j] = s;
+        for (int k = 0; k < 5; k++) a += Q[i * 5 + k] * St[k * 5 + j];
+        t[i * 5 + j] = a;
       }
 #pragma unroll
     for (int i = 0; i < 5; i++)
 #pragma unroll
       for (int j = i; j < 5; j++) {
-        TF s = 0;
+        TF a = 0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) s += t[i * 5 + k] * Q[j * 5 + k];
-        K[pk(i, j)] = (TS)s;
+        for (int k = 0; k < 5; k++) a += t[i * 5 + k] * Q[j * 5 + k];
+        K[pk(i, j)] = a;
       }
   }
-  // c = -S0x lam + e_p - e  (gradient of Phi = K x + c + dt edot)
-  TS c[5], lamxs[5];
-#pragma unroll
-  for (int i = 0; i < 5; i++) {
-    lamxs[i] = (TS)lamx[i];
-    c[i] = -(TS)s0l[i] + (TS)epx[i] - (TS)epsx[i];
-  }
   // hydrostatic part in closed form
-  const TS s0hh = (TS)nc.s0hh, shh = (TS)et[ET_SEL_HH];
-  const TS h = (s0hh * (TS)lam6[5] + (TS)eps6[5] - (TS)ep6[5]) / (s0hh + shh);
-  TS signorm = 0;
+  const TF s0hh = (TF)nc.s0hh, shh = (TF)et[ET_SEL_HH];
+  const TF h = (s0hh * lam6[5] + eps6[5] - ep6[5]) / (s0hh + shh);
+  TF ref2 = 0;
 #pragma unroll
-  for (int i = 0; i < 6; i++) signorm += (TS)lam6[i] * (TS)lam6[i];
-  signorm = sqrt(signorm);
-  const TS dh = h - (TS)lam6[5];
+  for (int i = 0; i < 6; i++) ref2 += lam6[i] * lam6[i];
+  const TF dh = h - lam6[5];
+  const TF tol2 = (TF)nc.tol * (TF)nc.tol;
+  const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
 
-  TS x[5];
+  TF x[5];
 #pragma unroll
-  for (int i = 0; i < 5; i++) x[i] = lamxs[i];
+  for (int i = 0; i < 5; i++) x[i] = lamx[i];
   const TF tau_off = (TF)ph.tau_back_minus_fwd;
-  TF edf[5], Df[15], psif;
-  TS step_norm = 0;
   int it = 0;
   bool done = false;
-  // first step includes the hydrostatic correction in the step norm
-  TS hstep2 = dh * dh;
-  const TS ref = signorm > (TS)0 ? signorm : (TS)0;
+  TF hstep2 = dh * dh;   // the first step includes the hydrostatic correction
   for (; it < nc.itmax && !done; it++) {
-    TF xf[5];
-#pragma unroll
-    for (int i = 0; i < 5; i++) xf[i] = (TF)x[i];
+    TF edf[5], Df[15], psif;
     if (nc.flow_off) {
 #pragma unroll
       for (int i = 0; i < 5; i++) edf[i] = 0;
@@ -258,107 +257,109 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       for (int i = 0; i < 15; i++) Df[i] = 0;
       psif = 0;
     } else {
-      flow_rule<TF, true>(ph, xf, tauf, tau_off, edf, Df, psif, nullptr);
+      flow_rule<TF, true>(ph, x, tauf, tau_off, edf, Df, psif, nullptr);
     }
-    TS g[5], Kx[5], H[15];
-    symv5<TS>(K, x, Kx);
+    TF g[5], Kx[5];
+    symv5<TF>(K, x, Kx);
 #pragma unroll
-    for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * (TS)edf[i];
+    for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * edf[i];
+    TF p[5];
+    {
+      TL H[15], mg[5], pl[5];
 #pragma unroll
-    for (int i = 0; i < 15; i++) H[i] = K[i] + dt * (TS)Df[i];
-    TS p[5], mg[5];
+      for (int i = 0; i < 15; i++) H[i] = (TL)K[i] + (TL)dt * (TL)Df[i];
 #pragma unroll
-    for (int i = 0; i < 5; i++) mg[i] = -g[i];
-    if (!chol_solve5<TS>(H, mg, p)) { o.failed = 1; break; }
-    TS pn2 = 0, slope = 0;
+      for (int i = 0; i < 5; i++) mg[i] = -(TL)g[i];
+      if (!ldl_solve5<TL>(H, mg, pl)) { o.failed = 1; break; }
+#pragma unroll
+      for (int i = 0; i < 5; i++) p[i] = (TF)pl[i];
+    }
+    TF pn2 = 0, slope = 0;
 #pragma unroll
     for (int i = 0; i < 5; i++) { pn2 += p[i] * p[i]; slope += g[i] * p[i]; }
-    const TS pn = sqrt(pn2);
-    TS alpha = 1;
+    TF alpha = 1;
     // Line search on Phi only for large steps; near the root Newton's full
     // step is taken (quadratic convergence region).
-    if (pn > (TS)1e-3 * ref && !nc.flow_off) {
-      TS phi0 = 0;
+    if (pn2 > ls_thr2 && !nc.flow_off) {
+      TF phi0 = 0;
 #pragma unroll
-      for (int i = 0; i < 5; i++) phi0 += x[i] * ((TS)0.5 * Kx[i] + c[i]);
-      phi0 += dt * (TS)psif;
+      for (int i = 0; i < 5; i++) phi0 += x[i] * ((TF)0.5 * Kx[i] + c[i]);
+      phi0 += dt * psif;
       for (int ls = 0; ls < 40; ls++) {
-        TS xt[5];
-        TF xtf[5];
+        TF xt[5];
 #pragma unroll
-        for (int i = 0; i < 5; i++) { xt[i] = x[i] + alpha * p[i]; xtf[i] = (TF)xt[i]; }
+        for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
         TF edt[5], psit;
-        flow_rule<TF, false>(ph, xtf, tauf, tau_off, edt, nullptr, psit, nullptr);
-        TS Kxt[5];
-        symv5<TS>(K, xt, Kxt);
-        TS phi = 0;
+        flow_rule<TF, false>(ph, xt, tauf, tau_off, edt, nullptr, psit, nullptr);
+        TF Kxt[5];
+        symv5<TF>(K, xt, Kxt);
+        TF phi = 0;
 #pragma unroll
-        for (int i = 0; i < 5; i++) phi += xt[i] * ((TS)0.5 * Kxt[i] + c[i]);
-        phi += dt * (TS)psit;
-        if (phi <= phi0 + (TS)1e-4 * alpha * slope) break;
-        TS den = (TS)2 * (phi - phi0 - slope * alpha);
-        TS an = den > (TS)0 ? -slope * alpha * alpha / den : (TS)0.5 * alpha;
-        an = fmin(an, (TS)0.5 * alpha);
-        alpha = fmax(an, (TS)0.1 * alpha);
-        if (alpha * pn <= (TS)1e-14 * (ref + (TS)1)) break;
+        for (int i = 0; i < 5; i++) phi += xt[i] * ((TF)0.5 * Kxt[i] + c[i]);
+        phi += dt * psit;
+        if (phi <= phi0 + (TF)1e-4 * alpha * slope) break;
+        TF den = (TF)2 * (phi - phi0 - slope * alpha);
+        TF an = den > (TF)0 ? -slope * alpha * alpha / den : (TF)0.5 * alpha;
+        an = fmin(an, (TF)0.5 * alpha);
+        alpha = fmax(an, (TF)0.1 * alpha);
+        if (alpha * alpha * pn2 <= (TF)1e-28 * (ref2 + (TF)1)) break;
       }
     }
 #pragma unroll
     for (int i = 0; i < 5; i++) x[i] += alpha * p[i];
-    step_norm = sqrt(alpha * alpha * pn2 + hstep2);
+    const TF step2 = alpha * alpha * pn2 + hstep2;
     hstep2 = 0;
-    const TS den = ref > (TS)0 ? ref : sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h);
-    if (!(den > (TS)0) || step_norm <= (TS)nc.tol * den) done = true;
+    TF den2 = ref2;
+    if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
+    if (!(den2 > (TF)0) || step2 <= tol2 * den2) done = true;
   }
   o.iters = it;
   if (!done) o.failed = 1;
   // final rates at the solution
-  TF xf[5], edx[5], psid;
-#pragma unroll
-  for (int i = 0; i < 5; i++) xf[i] = (TF)x[i];
+  TF edx[5], psid;
   if (nc.flow_off) {
 #pragma unroll
     for (int i = 0; i < 5; i++) edx[i] = 0;
   } else {
-    flow_rule<TF, false>(ph, xf, tauf, tau_off, edx, nullptr, psid, nullptr);
+    flow_rule<TF, false>(ph, x, tauf, tau_off, edx, nullptr, psid, nullptr);
   }
   // back to sample axes: s = Q^T x, edot = Q^T edot_x
-  TS ss[5], es[5];
+  TF ss[5], es[5];
 #pragma unroll
   for (int j = 0; j < 5; j++) {
-    TS a = 0, b = 0;
+    TF a = 0, b = 0;
 #pragma unroll
     for (int i = 0; i < 5; i++) {
-      a += (TS)Q[i * 5 + j] * x[i];
-      b += (TS)Q[i * 5 + j] * (TS)edx[i];
+      a += Q[i * 5 + j] * x[i];
+      b += Q[i * 5 + j] * edx[i];
     }
     ss[j] = a;
     es[j] = b;
   }
   // error contributions (src/evolution.c:264-299): |sig - lambda| and
-  // |S_gr sig + e_p + edot dt - e|, in sample axes
-  TS cs = dh * dh, ce = 0;
+  // |S_gr sig + e_p + edot dt - e|, in sample axes; summed over voxels in FP64
+  TF cs = dh * dh, ce = 0;
 #pragma unroll
   for (int i = 0; i < 5; i++) {
-    const TS ds = ss[i] - (TS)lam6[i];
+    const TF ds = ss[i] - lam6[i];
     cs += ds * ds;
-    TS de = (TS)ep6[i] + dt * es[i] - (TS)eps6[i];
+    TF de = ep6[i] + dt * es[i] - eps6[i];
 #pragma unroll
-    for (int j = 0; j < 5; j++) de += (TS)et[ET_SEL + pk(i, j)] * ss[j];
+    for (int j = 0; j < 5; j++) de += (TF)et[ET_SEL + pk(i, j)] * ss[j];
     ce += de * de;
   }
   {
-    const TS de = (TS)ep6[5] + shh * h - (TS)eps6[5];
+    const TF de = ep6[5] + shh * h - eps6[5];
     ce += de * de;
   }
   o.conv_s = (double)sqrt(cs);
   o.conv_e = (double)sqrt(ce);
 #pragma unroll
   for (int j = 0; j < 5; j++) {
-    sig6[j] = (TF)ss[j];
-    ed6[j] = (TF)es[j];
+    sig6[j] = ss[j];
+    ed6[j] = es[j];
   }
-  sig6[5] = (TF)h;
+  sig6[5] = h;
   ed6[5] = 0;
   return o;
 }
