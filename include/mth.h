@@ -39,8 +39,10 @@ typedef enum {
 } mth_status;
 
 typedef enum {
-  MTH_FP64 = 0,   /* all fields, FFTs and the local Newton in FP64 */
-  MTH_MIXED = 1   /* FP32 fields/FFT/Green operator, FP64 local Newton solve and reductions */
+  MTH_FP64 = 0,       /* all fields, FFTs and the local Newton in FP64 */
+  MTH_MIXED = 1,      /* FP32 fields/FFT/Green operator/flow rule; FP64 Jacobian solve of the
+                         local Newton, FP64 error norms and volume averages */
+  MTH_MIXED_FAST = 2  /* as MTH_MIXED but the 5x5 Jacobian solve in FP32 too */
 } mth_precision;
 
 /* One phase: elastic constants plus the active slip mode of its .sx file

@@ -86,13 +86,95 @@ __device__ void load_twiddles(c2<T>* s, const c2<T>* g, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
 }
 
+// Compile-time variant for the line lengths the workloads use: the radix
+// plan (4s, then 2s, then 3s, as make_plan) and every index computation fold
+// into constants.
+__host__ __device__ constexpr int ct_nst(int n) {
+  int s = 0;
+  while (n % 4 == 0) { n /= 4; s++; }
+  while (n % 2 == 0) { n /= 2; s++; }
+  while (n % 3 == 0) { n /= 3; s++; }
+  return s;
+}
+__host__ __device__ constexpr int ct_radix(int n, int idx) {
+  int s = 0;
+  while (n % 4 == 0) { if (s == idx) return 4; n /= 4; s++; }
+  while (n % 2 == 0) { if (s == idx) return 2; n /= 2; s++; }
+  while (n % 3 == 0) { if (s == idx) return 3; n /= 3; s++; }
+  return 1;
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void butterfly(c2<T> v[4], int sign) {
+  if constexpr (R == 2) {
+    c2<T> a = v[0], b = v[1];
+    v[0] = cadd<T>(a, b);
+    v[1] = csub<T>(a, b);
+  } else if constexpr (R == 4) {
+    c2<T> s02 = cadd<T>(v[0], v[2]), d02 = csub<T>(v[0], v[2]);
+    c2<T> s13 = cadd<T>(v[1], v[3]), d13 = csub<T>(v[1], v[3]);
+    c2<T> wd = mk<T>(-(T)sign * d13.y, (T)sign * d13.x);
+    v[0] = cadd<T>(s02, s13);
+    v[2] = csub<T>(s02, s13);
+    v[1] = cadd<T>(d02, wd);
+    v[3] = csub<T>(d02, wd);
+  } else {
+    const T h = (T)0.86602540378443864676 * (T)sign;
+    c2<T> t = cadd<T>(v[1], v[2]), u = csub<T>(v[1], v[2]);
+    c2<T> m = mk<T>(v[0].x - (T)0.5 * t.x, v[0].y - (T)0.5 * t.y);
+    c2<T> iu = mk<T>(-h * u.y, h * u.x);
+    v[0] = cadd<T>(v[0], t);
+    v[1] = cadd<T>(m, iu);
+    v[2] = csub<T>(m, iu);
+  }
+}
+
+template <typename T, int N, int S = 0, int NS = 1>
+__device__ __forceinline__ c2<T>* smem_fft_ct(c2<T>* d0, c2<T>* d1, int ls, int nl, const c2<T>* tw, int sign) {
+  if constexpr (S < ct_nst(N)) {
+    constexpr int R = ct_radix(N, S);
+    constexpr int NB = N / R;
+    constexpr int TWS = N / (NS * R);
+    const int total = nl * NB;
+    for (int w = threadIdx.x; w < total; w += blockDim.x) {
+      const int l = w / NB, j = w - l * NB;
+      const int k = j % NS;
+      const c2<T>* in = d0 + l * ls;
+      c2<T>* out = d1 + l * ls;
+      c2<T> v[4];
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        v[r] = in[j + r * NB];
+        if (r && NS > 1) v[r] = cmul<T>(v[r], tw[k * r * TWS]);
+      }
+      butterfly<T, R>(v, sign);
+      const int idxD = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) out[idxD + r * NS] = v[r];
+    }
+    __syncthreads();
+    return smem_fft_ct<T, N, S + 1, NS * R>(d1, d0, ls, nl, tw, sign);
+  } else {
+    return d0;
+  }
+}
+
+// NC > 0: compile-time line length; NC == 0: runtime plan.
+template <typename T, int NC>
+__device__ __forceinline__ c2<T>* do_fft(c2<T>* d0, c2<T>* d1, int n, int ls, int nl, const FftPlan& pl,
+                                         const c2<T>* tw, int sign) {
+  if constexpr (NC > 0) return smem_fft_ct<T, NC>(d0, d1, ls, nl, tw, sign);
+  else return smem_fft<T>(d0, d1, n, ls, nl, pl, tw, sign);
+}
+
 // ------------------------------------------------------------- z passes
 // One block: lb consecutive (x,y) lines, npair = ceil(ncomp/2) packed
 // transforms per line.
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in, c2<T>* __restrict__ out, int ncomp,
-                                                        long long plane, long long kplane, int nlines, int n2,
+                                                        long long plane, long long kplane, int nlines, int n2_,
                                                         int lb, FftPlan pl, const c2<T>* __restrict__ twg) {
+  const int n2 = NC > 0 ? NC : n2_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
   const int npair = (ncomp + 1) / 2;
@@ -115,7 +197,7 @@ __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in
     d0[(p * lb + l) * ls + z] = mk<T>(a, b);
   }
   __syncthreads();
-  c2<T>* r = smem_fft<T>(d0, d1, n2, ls, npair * lb, pl, tw, -1);
+  c2<T>* r = do_fft<T, NC>(d0, d1, n2, ls, npair * lb, pl, tw, -1);
   const int kz = n2 / 2 + 1;
   for (int idx = threadIdx.x; idx < npair * lb * kz; idx += blockDim.x) {
     const int k = idx % kz;
@@ -134,11 +216,12 @@ __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in
 }
 
 // mode 0: field = val*scale + add ; mode 1: field += val*scale + add
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict__ spec, T* __restrict__ field, int ncomp,
-                                                        long long plane, long long kplane, int nlines, int n2,
+                                                        long long plane, long long kplane, int nlines, int n2_,
                                                         int lb, FftPlan pl, const c2<T>* __restrict__ twg, T scale,
                                                         AddVec add, int mode) {
+  const int n2 = NC > 0 ? NC : n2_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
   const int npair = (ncomp + 1) / 2;
@@ -165,7 +248,10 @@ __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict_
     if (k > 0 && 2 * k < n2) X[n2 - k] = mk<T>(A.x + B.y, -A.y + B.x);  // conj(A) + i conj(B)
   }
   __syncthreads();
-  c2<T>* r = smem_fft<T>(d0, d1, n2, ls, npair * lb, pl, tw, +1);
+  c2<T>* r = do_fft<T, NC>(d0, d1, n2, ls, npair * lb, pl, tw, +1);
+  __shared__ T addv[6];
+  if (threadIdx.x < 6) addv[threadIdx.x] = (T)add.v[threadIdx.x];
+  __syncthreads();
   for (int idx = threadIdx.x; idx < ncomp * lb * n2; idx += blockDim.x) {
     const int z = idx % n2;
     const int l = (idx / n2) % lb;
@@ -174,7 +260,7 @@ __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict_
     const c2<T> X = r[((c >> 1) * lb + l) * ls + z];
     const T val = (c & 1) ? X.y : X.x;
     const long long o = (long long)c * plane + (long long)(line0 + l) * n2 + z;
-    const T v = val * scale + (T)add.v[c];
+    const T v = val * scale + addv[c];
     if (mode == 0) field[o] = v;
     else field[o] += v;
   }
@@ -184,10 +270,11 @@ __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict_
 // Lines along a dimension of length L with element stride S (in complex
 // elements); the block covers kb consecutive kz and one outer index.
 // base(outer) = outer * ostride.
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_strided_kernel(c2<T>* __restrict__ spec, int ncomp, long long kplane,
-                                                          int L, long long S, long long ostride, int kzn, int kb,
+                                                          int L_, long long S, long long ostride, int kzn, int kb,
                                                           FftPlan pl, const c2<T>* __restrict__ twg, int sign) {
+  const int L = NC > 0 ? NC : L_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
   const int ls = L + 1;
@@ -206,7 +293,7 @@ __global__ void __launch_bounds__(256) fft_strided_kernel(c2<T>* __restrict__ sp
     d0[(c * kb + kk) * ls + e] = v;
   }
   __syncthreads();
-  c2<T>* r = smem_fft<T>(d0, d1, L, ls, nl, pl, tw, sign);
+  c2<T>* r = do_fft<T, NC>(d0, d1, L, ls, nl, pl, tw, sign);
   for (int idx = threadIdx.x; idx < ncomp * L * kb; idx += blockDim.x) {
     const int kk = idx % kb;
     const int e = (idx / kb) % L;
@@ -348,11 +435,12 @@ __device__ __forceinline__ void green_point(const GreenConst& gc, int kx, int ky
 // spectra, Delta = Gamma0 : sigma-hat per k, antisymmetric part added to
 // the spin accumulator, inverse transform along x.  One block: fixed y,
 // kb consecutive kz.
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c2<T>* __restrict__ spec, c2<T>* __restrict__ anti_acc,
-                                                          long long kplane, int n0, int n1, int n2, int kzn, int kb,
+                                                          long long kplane, int n0_, int n1, int n2, int kzn, int kb,
                                                           FftPlan pl, const c2<T>* __restrict__ twf,
                                                           const c2<T>* __restrict__ twi) {
+  const int n0 = NC > 0 ? NC : n0_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw_f = reinterpret_cast<c2<T>*>(smraw);
   c2<T>* tw_i = tw_f + n0;
@@ -375,7 +463,7 @@ __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c
     d0[(c * kb + kk) * ls + e] = v;
   }
   __syncthreads();
-  c2<T>* r = smem_fft<T>(d0, d1, n0, ls, nl, pl, tw_f, -1);
+  c2<T>* r = do_fft<T, NC>(d0, d1, n0, ls, nl, pl, tw_f, -1);
   c2<T>* other = (r == d0) ? d1 : d0;
   for (int idx = threadIdx.x; idx < n0 * kb; idx += blockDim.x) {
     const int kk = idx % kb;
@@ -392,7 +480,7 @@ __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c
     for (int c = 0; c < 3; c++) anti_acc[c * kplane + o] = cadd<T>(anti_acc[c * kplane + o], a[c]);
   }
   __syncthreads();
-  c2<T>* r2 = smem_fft<T>(r, other, n0, ls, nl, pl, tw_i, +1);
+  c2<T>* r2 = do_fft<T, NC>(r, other, n0, ls, nl, pl, tw_i, +1);
   for (int idx = threadIdx.x; idx < 6 * n0 * kb; idx += blockDim.x) {
     const int kk = idx % kb;
     const int e = (idx / kb) % n0;
@@ -402,6 +490,10 @@ __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c
 }
 
 // ------------------------------------------------------------ launchers
+// line lengths with compile-time kernels; other even 2^a 3^b lengths use the
+// runtime-plan kernels
+#define MTH_CT_SIZES(X) X(16) X(32) X(48) X(64) X(96) X(128) X(256)
+
 static size_t z_smem(int n2, int npair, int lb, size_t esz) { return (size_t)esz * (n2 + 2 * npair * lb * (n2 + 1)); }
 
 template <typename T>
@@ -418,7 +510,13 @@ cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncom
   const int nlines = g.n0 * g.n1;
   const int lb = pick_lb<T>(g.n2, npair, nlines, g.smem_budget);
   const size_t sm = z_smem(g.n2, npair, lb, sizeof(c2<T>));
-  auto k = fft_z_r2c_kernel<T>;
+  auto k = fft_z_r2c_kernel<T, 0>;
+  switch (g.n2) {
+#define MTH_CASE(N) case N: k = fft_z_r2c_kernel<T, N>; break;
+    MTH_CT_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: break;
+  }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(in, out, ncomp, g.plane, g.kplane, nlines, g.n2, lb, g.pz, tw);
   return cudaGetLastError();
@@ -431,7 +529,13 @@ cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int 
   const int nlines = g.n0 * g.n1;
   const int lb = pick_lb<T>(g.n2, npair, nlines, g.smem_budget);
   const size_t sm = z_smem(g.n2, npair, lb, sizeof(c2<T>));
-  auto k = fft_z_c2r_kernel<T>;
+  auto k = fft_z_c2r_kernel<T, 0>;
+  switch (g.n2) {
+#define MTH_CASE(N) case N: k = fft_z_c2r_kernel<T, N>; break;
+    MTH_CT_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: break;
+  }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(spec, field, ncomp, g.plane, g.kplane, nlines, g.n2, lb, g.pz, tw,
                                              scale, add, mode);
@@ -458,7 +562,13 @@ cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axi
   const FftPlan& pl = axis == 1 ? g.py : g.px;
   const int kb = pick_kb<T>(L, ncomp, g.smem_budget, 1);
   const size_t sm = s_smem(L, ncomp * kb, sizeof(c2<T>), 1);
-  auto k = fft_strided_kernel<T>;
+  auto k = fft_strided_kernel<T, 0>;
+  switch (L) {
+#define MTH_CASE(N) case N: k = fft_strided_kernel<T, N>; break;
+    MTH_CT_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: break;
+  }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kz + kb - 1) / kb, nouter);
   k<<<grid, 256, sm, st>>>(spec, ncomp, g.kplane, L, S, ostride, g.kz, kb, pl, tw, sign);
@@ -470,7 +580,13 @@ cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* sp
                                const c2<T>* twi, cudaStream_t st) {
   const int kb = pick_kb<T>(g.n0, 6, g.smem_budget, 2);
   const size_t sm = s_smem(g.n0, 6 * kb, sizeof(c2<T>), 2);
-  auto k = fft_x_green_kernel<T>;
+  auto k = fft_x_green_kernel<T, 0>;
+  switch (g.n0) {
+#define MTH_CASE(N) case N: k = fft_x_green_kernel<T, N>; break;
+    MTH_CT_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: break;
+  }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kz + kb - 1) / kb, g.n1);
   k<<<grid, 256, sm, st>>>(gc, spec, anti, g.kplane, g.n0, g.n1, g.n2, g.kz, kb, g.px, twf, twi);

@@ -173,9 +173,10 @@ struct VoxelOut {
 // orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
 // (plastic strain rate, sample frame).
 // TF: flow rule, residual, Hessian assembly, line search and frame
-// transforms; TL: the Jacobian (Hessian) solve.  FP64 mode: both double.
-// Mixed mode: TF = float, TL = double (GB300 issues FP64 at 1/64 of the FP32
-// rate, so only the 5x5 solve stays in FP64).
+// transforms; TL: accuracy of the Jacobian (Hessian) solve.  FP64 mode: both
+// double.  Mixed mode: TF = float, TL = double: the FP32-assembled 5x5
+// system is factored and solved in FP64 (GB300 issues FP64 at 1/64 of the
+// FP32 rate, so everything else stays FP32).  Fast mode: both float.
 template <typename TF, typename TL>
 __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const double* __restrict__ et,
                                 const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* tauf, TF* sig6,
@@ -265,14 +266,26 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
     for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * edf[i];
     TF p[5];
     {
-      TL H[15], mg[5], pl[5];
+      TF H[15], mg[5];
 #pragma unroll
-      for (int i = 0; i < 15; i++) H[i] = (TL)K[i] + (TL)dt * (TL)Df[i];
+      for (int i = 0; i < 15; i++) H[i] = K[i] + dt * Df[i];
 #pragma unroll
-      for (int i = 0; i < 5; i++) mg[i] = -(TL)g[i];
-      if (!ldl_solve5<TL>(H, mg, pl)) { o.failed = 1; break; }
+      for (int i = 0; i < 5; i++) mg[i] = -g[i];
+      bool ok;
+      if constexpr (sizeof(TL) > sizeof(TF)) {
+        // FP64 Jacobian solve of the FP32-assembled system
+        TL Hl[15], bl[5], pl[5];
 #pragma unroll
-      for (int i = 0; i < 5; i++) p[i] = (TF)pl[i];
+        for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
+#pragma unroll
+        for (int i = 0; i < 5; i++) bl[i] = (TL)mg[i];
+        ok = ldl_solve5<TL>(Hl, bl, pl);
+#pragma unroll
+        for (int i = 0; i < 5; i++) p[i] = (TF)pl[i];
+      } else {
+        ok = ldl_solve5<TF>(H, mg, p);
+      }
+      if (!ok) { o.failed = 1; break; }
     }
     TF pn2 = 0, slope = 0;
 #pragma unroll
@@ -386,8 +399,8 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[W], double* out) 
 }
 
 // ------------------------------------------------------------ Newton kernel
-template <typename TSt, typename TF, typename TS>
-__global__ void __launch_bounds__(256) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials) {
+template <typename TSt, typename TF, typename TS, int MINB>
+__global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   double acc[NPART];
@@ -439,12 +452,15 @@ __global__ void __launch_bounds__(256) newton_kernel(const NewtonConst nc, Field
 
 cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
                           cudaStream_t st) {
-  if (mixed) {
+  if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double><<<nblocks, 256, 0, st>>>(nc, f, partials);
+    newton_kernel<float, float, float, 2><<<nblocks, 256, 0, st>>>(nc, f, partials);
+  } else if (mixed) {
+    const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+    newton_kernel<float, float, double, 2><<<nblocks, 256, 0, st>>>(nc, f, partials);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    newton_kernel<double, double, double><<<nblocks, 256, 0, st>>>(nc, f, partials);
+    newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials);
   }
   return cudaGetLastError();
 }
