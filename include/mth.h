@@ -95,8 +95,9 @@ typedef struct {
   double rho_nucleation;     /* nucleation threshold on rho_tot [1e12/m^2] */
   double rho0;               /* initial dislocation density [1e12/m^2] */
   double rho_k;              /* rho = rho0 + rho_k * accumulated slip [1e12/m^2] */
-  int    pf_substeps;        /* PF substeps per mechanical step */
+  int    pf_substeps;        /* PF substeps per mechanical step; 0 disables DRX */
   uint64_t seed;             /* counter-based RNG seed */
+  double nucleation_prob;    /* per-step nucleation probability of a candidate voxel */
   int    device;             /* CUDA device ordinal the context runs on */
 } mth_params;
 
@@ -165,6 +166,31 @@ mth_status mth_local_solve(const mth_params* params, const double c066[36], size
                            double* sig, const double* eps_p, const double* strain,
                            const double* rot, const double* crss, double* edot,
                            double* err, long long* newton_iters);
+
+/* Sparse phase-field relaxation on arrays: PF_XRX (src/pf_xrx.c:1469-1698)
+ * for `substeps` explicit substeps from sharp interfaces (one order
+ * parameter per voxel), with rho the stored-energy density [1e12/m^2] of
+ * each voxel.  Outputs the relaxed grain ids (argmax) and, when the pointers
+ * are not NULL, the MTH_PF_K order parameters of every voxel (ids sorted
+ * ascending, values, count).  FP64 when params->precision is MTH_FP64,
+ * FP32 otherwise.  Coefficients from params (pf_length_scale,
+ * pf_time_step, e_gb, m_gb, pf_width_cells, stored_energy_scale,
+ * shear_modulus, burgers). */
+#define MTH_PF_K 8
+mth_status mth_pf_relax(const mth_params* params, const int cell_dim[3], const int* grain, const double* rho,
+                        int substeps, int* grain_out, int* ids_out, double* phi_out, int* cnt_out);
+
+/* DRX nucleation on arrays: NucleationCheckDRX (src/integrated.c:161-494)
+ * with a counter-based generator.  A voxel nucleates when it has a face
+ * neighbour in another grain, its phase (1-based) is a crystal phase of
+ * params, rho > params->rho_nucleation and u(params->seed, step*N + voxel) <
+ * params->nucleation_prob.  Nuclei are numbered first_id, first_id+1, ... in
+ * voxel order and paint grain ids on a periodic disc |d|^2 <= r^2
+ * (r = params->nucleus_radius), later nuclei over earlier ones.  sites
+ * receives up to cap nucleus voxels; *n_new the number of nuclei. */
+mth_status mth_nucleate(const mth_params* params, const int cell_dim[3], int* grain, const int* phase,
+                        const double* rho, long long step, int first_id, long long* sites, long long cap,
+                        int* n_new);
 
 /* Allocation-free batch local solve.  No counterpart in the reference.
  * Same computation and argument meaning as mth_local_solve, but every array

@@ -23,7 +23,9 @@ LIB = os.path.join(HERE, "lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + os.path.join(REPO, "include")]
-CU_SOURCES = ["fft_green.cu", "newton.cu", "capi.cu"]
+CU_SOURCES = ["fft_green.cu", "newton.cu", "drx.cu", "capi.cu"]
+# sources compiled without FMA contraction (bit-exact FP64 restatement)
+NO_FMAD = {"drx.cu"}
 C_SOURCES = ["mth_io.c"]
 
 
@@ -60,7 +62,8 @@ def build(force=False, verbose=False):
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            extra = ["-fmad=false"] if s in NO_FMAD else []
+            jobs.append([nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
     for s in C_SOURCES:
         src = os.path.join(HOST, s)
         obj = os.path.join(BUILD, s + ".o")

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -240,6 +241,9 @@ bool mth::make_plan(int n, FftPlan* p) {
 }
 
 // ---------------------------------------------------------------- context
+constexpr long long MAX_CANDIDATES = 1LL << 20;   // nucleation candidates collected per step
+constexpr int MAX_NUCLEI = 65536;                 // nuclei kept per step (first in voxel order)
+
 struct mth_ctx {
   mth_params p;
   int mixed;
@@ -280,6 +284,30 @@ struct mth_ctx {
   double wgt, wgt_ph1, e_vm, d_vm, s_vm, s_vm1, err_e, err_s, time_tot;
   int istep;
   int uploaded;
+  // dynamic recrystallisation
+  int drx;
+  int first_drx_id, next_grain_id;
+  std::vector<double>* etab_h;       // host copy of the elastic-class table
+  std::vector<double>* drx_rot_h;    // 9 per recrystallised grain
+  std::vector<int>* drx_class_h;
+  double* drx_rot_d;
+  int* drx_class_d;
+  size_t drx_cap;
+  PfBuffers<float> pff;
+  PfBuffers<double> pfd;
+  PfCoef pfc;
+  double* rho_d;
+  void* rho_t;
+  int* grain_prev_d;
+  int* winner_d;
+  long long* sites_d;
+  unsigned long long* count_d;
+  uint8_t* crystal_d;
+  unsigned long long* hist_d;
+  double* gather_d;
+  size_t hist_cap;
+  double tau0f;
+  int nsys;
 };
 
 static void ctx_free(mth_ctx* c) {
@@ -302,13 +330,34 @@ static void ctx_free(mth_ctx* c) {
     delete c->ev_pool;
   }
   delete c->ev_pending;
+  delete c->etab_h;
+  delete c->drx_rot_h;
+  delete c->drx_class_h;
+  cudaFree(c->drx_rot_d);
+  cudaFree(c->drx_class_d);
+  for (int i = 0; i < 2; i++) {
+    cudaFree(c->pff.ids[i]); cudaFree(c->pff.phi[i]); cudaFree(c->pff.cnt[i]);
+    cudaFree(c->pfd.ids[i]); cudaFree(c->pfd.phi[i]); cudaFree(c->pfd.cnt[i]);
+  }
+  cudaFree(c->pff.gid);
+  cudaFree(c->pfd.gid);
+  cudaFree(c->rho_d);
+  cudaFree(c->rho_t);
+  cudaFree(c->grain_prev_d);
+  cudaFree(c->winner_d);
+  cudaFree(c->sites_d);
+  cudaFree(c->count_d);
+  cudaFree(c->crystal_d);
+  cudaFree(c->hist_d);
+  cudaFree(c->gather_d);
   delete c;
 }
 
 // ------------------------------------------------------------- profiling
-enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_NCLASS };
-static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain",
-                                        "newton", "reduce", "end_step", "spin_fft", "setup"};
+enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_DRX,
+       K_NCLASS };
+static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain", "newton",
+                                        "reduce", "end_step", "spin_fft", "setup", "drx_pf"};
 
 static void prof_begin(mth_ctx* c) {
   if (!c->prof_on) return;
@@ -491,6 +540,38 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   };
   if (c->mixed) carve(static_cast<float*>(c->fieldmem), c->ff);
   else carve(static_cast<double*>(c->fieldmem), c->fd);
+  CKC(cudaMalloc(&c->crystal_d, P));
+  c->etab_h = new std::vector<double>();
+  c->drx_rot_h = new std::vector<double>();
+  c->drx_class_h = new std::vector<int>();
+  c->drx = p->pf_substeps > 0;
+  if (c->drx) {
+    if (!(p->pf_length_scale > 0) || !(p->pf_time_step > 0) || !(p->pf_width_cells > 0) || !(p->m_gb >= 0) ||
+        p->nucleus_radius < 0 || p->nucleus_radius > 16) {
+      ctx_free(c);
+      return set_err(MTH_ERR_ARG, "phase-field parameters");
+    }
+    c->pfc.mcoef = p->pf_time_step * 4.0 / 3.0 * p->m_gb / (p->pf_width_cells * p->pf_length_scale);
+    c->pfc.kappa = 3.0 / 4.0 * p->e_gb * (p->pf_width_cells * p->pf_length_scale) / p->pf_length_scale / p->pf_length_scale;
+    c->pfc.mwell = 6 * p->e_gb / (p->pf_width_cells * p->pf_length_scale);
+    c->pfc.edisl = p->stored_energy_scale * p->shear_modulus * p->burgers * p->burgers;
+    for (int i = 0; i < 2; i++) {
+      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.ids[i] : (void*&)c->pfd.ids[i]), sizeof(int) * PF_K * P));
+      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.phi[i] : (void*&)c->pfd.phi[i]), esz * PF_K * P));
+      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.cnt[i] : (void*&)c->pfd.cnt[i]), P));
+    }
+    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.gid : (void*&)c->pfd.gid), sizeof(int) * P));
+    CKC(cudaMalloc(&c->rho_d, sizeof(double) * P));
+    CKC(cudaMalloc(&c->rho_t, esz * P));
+    CKC(cudaMalloc(&c->grain_prev_d, sizeof(int) * P));
+    CKC(cudaMalloc(&c->winner_d, sizeof(int) * P));
+    CKC(cudaMemset(c->winner_d, 0xff, sizeof(int) * P));
+    CKC(cudaMalloc(&c->sites_d, sizeof(long long) * MAX_CANDIDATES));
+    CKC(cudaMalloc(&c->count_d, sizeof(unsigned long long)));
+    CKC(cudaMalloc(&c->gather_d, sizeof(double) * 9 * MAX_NUCLEI));
+    c->hist_cap = (size_t)(P + MAX_NUCLEI);
+    CKC(cudaMalloc(&c->hist_d, sizeof(unsigned long long) * c->hist_cap));
+  }
   for (int a = 0; a < 3; a++)
     for (int d = 0; d < 2; d++) {
       mth_status t = c->mixed ? make_twiddles<float>(c->n[a], d == 0 ? -1 : 1, &c->tw[a][d])
@@ -585,6 +666,21 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   cudaFree(c->etab_d);
   c->etab_d = nullptr;
   c->nclass = (int)counts.size();
+  *c->etab_h = rows;
+  {
+    std::vector<uint8_t> cry(n);
+    int gmax = 0;
+    for (size_t v = 0; v < n; v++) {
+      cry[v] = c->nc.ph[phase[v] - 1].type == 0 ? 1 : 0;
+      if (grain[v] > gmax) gmax = grain[v];
+    }
+    CK(cudaMemcpy(c->crystal_d, cry.data(), n, cudaMemcpyHostToDevice));
+    c->first_drx_id = c->next_grain_id = gmax + 1;
+    c->drx_rot_h->clear();
+    c->drx_class_h->clear();
+    c->tau0f = c->nc.ph[0].tau0f;
+    c->nsys = c->nc.ph[0].nsys;
+  }
   CK(cudaMalloc(&c->etab_d, sizeof(double) * rows.size()));
   c->ff.etab = c->etab_d;
   c->fd.etab = c->etab_d;
@@ -691,12 +787,144 @@ static mth_status spin_field(mth_ctx* c) {
   return MTH_OK;
 }
 
+// Reference stiffness after a change of the elastic classes: C066 as the
+// voxel average of C_gr, S066, S0 (src/evolution.c:1200-1216); the Green
+// operator keeps the initial C0 (src/init.c:1195).
+static mth_status refresh_reference_medium(mth_ctx* c) {
+  const int ncl = (int)(c->etab_h->size() / ETAB_W);
+  if ((size_t)ncl > c->hist_cap) {
+    CK(cudaStreamSynchronize(c->st));
+    cudaFree(c->hist_d);
+    c->hist_cap = (size_t)ncl * 2;
+    CK(cudaMalloc(&c->hist_d, sizeof(unsigned long long) * c->hist_cap));
+  }
+  CK(cudaMemsetAsync(c->hist_d, 0, sizeof(unsigned long long) * ncl, c->st));
+  LAUNCH(K_DRX, 0.0, launch_class_histogram(c->nv, c->crystal_d, c->eclass_d, c->hist_d, c->st));
+  std::vector<unsigned long long> hist(ncl);
+  CK(cudaMemcpyAsync(hist.data(), c->hist_d, sizeof(unsigned long long) * ncl, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  prof_resolve(c);
+  std::vector<double>& rows = *c->etab_h;
+  memset(c->c066, 0, sizeof(c->c066));
+  for (int k = 0; k < ncl; k++) {
+    const double* r = &rows[(size_t)k * ETAB_W];
+    for (int i = 0; i < 5; i++)
+      for (int j = 0; j < 5; j++) c->c066[i][j] += (double)hist[k] * r[ET_CGR + pkh(i, j)];
+    c->c066[5][5] += (double)hist[k] * r[ET_CGR_HH];
+  }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) c->c066[i][j] *= c->wgt;
+  if (!inv6(c->c066, c->s066)) return set_err(MTH_ERR_SINGULAR, "reference stiffness C066 is singular after DRX");
+  for (int k = 0; k < ncl; k++) class_row_add_s0(&rows[(size_t)k * ETAB_W], c->s066);
+  m2t4(c->s066, c->s0_4);
+  for (int i = 0; i < 5; i++)
+    for (int j = 0; j < 5; j++) c->nc.s0dev[i * 5 + j] = c->s066[i][j];
+  c->nc.s0hh = c->s066[5][5];
+  cudaFree(c->etab_d);
+  CK(cudaMalloc(&c->etab_d, sizeof(double) * rows.size()));
+  CK(cudaMemcpyAsync(c->etab_d, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, c->st));
+  c->ff.etab = c->etab_d;
+  c->fd.etab = c->etab_d;
+  c->nclass = ncl;
+  return MTH_OK;
+}
+
+// Dynamic recrystallisation at the start of a mechanical step, the order of
+// Evolution (src/evolution.c:850-1253): nucleation, phase-field relaxation,
+// microstructure update, reset of recrystallised voxels, new reference
+// medium.  Returns the number of nuclei.
+static mth_status drx_step(mth_ctx* c, int* n_new) {
+  *n_new = 0;
+  const mth_params& p = c->p;
+  const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+  LAUNCH(K_DRX, 0.0, launch_drx_rho(c->mixed, f, p.rho0, p.rho_k, c->rho_d, c->rho_t, c->st));
+  CK(cudaMemcpyAsync(c->grain_prev_d, c->grain_d, sizeof(int) * c->nv, cudaMemcpyDeviceToDevice, c->st));
+  // nucleation
+  CK(cudaMemsetAsync(c->count_d, 0, sizeof(unsigned long long), c->st));
+  LAUNCH(K_DRX, 0.0, launch_nucleation_candidates(c->n, c->grain_d, c->crystal_d, c->rho_d, p.rho_nucleation,
+                                                  p.nucleation_prob, p.seed, (uint64_t)c->istep * (uint64_t)c->nv,
+                                                  c->sites_d, c->count_d, MAX_CANDIDATES, c->st));
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, c->count_d, sizeof(cnt), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  prof_resolve(c);
+  if ((long long)cnt > MAX_CANDIDATES)
+    return set_err(MTH_ERR_UNSUPPORTED, "%llu nucleation candidates in one step (limit %lld)", cnt, MAX_CANDIDATES);
+  int nn = 0;
+  if (cnt > 0) {
+    std::vector<long long> sites(cnt);
+    CK(cudaMemcpy(sites.data(), c->sites_d, sizeof(long long) * cnt, cudaMemcpyDeviceToHost));
+    std::sort(sites.begin(), sites.end());
+    nn = (int)std::min<unsigned long long>(cnt, (unsigned long long)MAX_NUCLEI);
+    CK(cudaMemcpy(c->sites_d, sites.data(), sizeof(long long) * nn, cudaMemcpyHostToDevice));
+    // each nucleus takes the current orientation of its parent voxel
+    // (src/integrated.c:271-283): gather the rotations
+    const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
+    std::vector<unsigned char> rb(esz);
+    std::vector<double> R((size_t)nn * 9);
+    const char* rot = c->mixed ? (const char*)c->ff.rot : (const char*)c->fd.rot;
+    for (int k = 0; k < nn; k++)
+      for (int i = 0; i < 9; i++) {
+        CK(cudaMemcpy(rb.data(), rot + esz * ((size_t)i * c->nv + sites[k]), esz, cudaMemcpyDeviceToHost));
+        R[(size_t)k * 9 + i] = c->mixed ? (double)*(float*)rb.data() : *(double*)rb.data();
+      }
+    for (int k = 0; k < nn; k++) {
+      const int cls = (int)(c->etab_h->size() / ETAB_W);
+      c->etab_h->resize(c->etab_h->size() + ETAB_W);
+      class_row(c->nc.ph[0], &R[(size_t)k * 9], &(*c->etab_h)[(size_t)cls * ETAB_W]);
+      c->drx_rot_h->insert(c->drx_rot_h->end(), &R[(size_t)k * 9], &R[(size_t)k * 9] + 9);
+      c->drx_class_h->push_back(cls);
+    }
+    LAUNCH(K_DRX, 0.0, launch_paint_nuclei(c->n, c->sites_d, nn, p.nucleus_radius, c->next_grain_id, c->winner_d,
+                                           c->grain_d, c->st));
+    c->next_grain_id += nn;
+  }
+  *n_new = nn;
+  const int n_drx = c->next_grain_id - c->first_drx_id;
+  if (n_drx == 0) return MTH_OK;
+  // class table with the new rows (S066 part refreshed below)
+  for (size_t k = 0; k < c->etab_h->size() / ETAB_W; k++) class_row_add_s0(&(*c->etab_h)[k * ETAB_W], c->s066);
+  cudaFree(c->etab_d);
+  CK(cudaMalloc(&c->etab_d, sizeof(double) * c->etab_h->size()));
+  CK(cudaMemcpyAsync(c->etab_d, c->etab_h->data(), sizeof(double) * c->etab_h->size(), cudaMemcpyHostToDevice, c->st));
+  c->ff.etab = c->etab_d;
+  c->fd.etab = c->etab_d;
+  if ((size_t)n_drx > c->drx_cap) {
+    cudaFree(c->drx_rot_d);
+    cudaFree(c->drx_class_d);
+    c->drx_cap = (size_t)n_drx * 2 + 64;
+    CK(cudaMalloc(&c->drx_rot_d, sizeof(double) * 9 * c->drx_cap));
+    CK(cudaMalloc(&c->drx_class_d, sizeof(int) * c->drx_cap));
+  }
+  CK(cudaMemcpyAsync(c->drx_rot_d, c->drx_rot_h->data(), sizeof(double) * 9 * n_drx, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->drx_class_d, c->drx_class_h->data(), sizeof(int) * n_drx, cudaMemcpyHostToDevice, c->st));
+  // phase-field relaxation from the painted grain map
+  int* gid_new;
+  if (c->mixed) {
+    LAUNCH(K_DRX, 0.0, launch_pf_relax<float>(c->n, c->grain_d, (const float*)c->rho_t, p.pf_substeps, c->pfc, c->pff,
+                                              c->st));
+    gid_new = c->pff.gid;
+  } else {
+    LAUNCH(K_DRX, 0.0, launch_pf_relax<double>(c->n, c->grain_d, (const double*)c->rho_t, p.pf_substeps, c->pfc,
+                                               c->pfd, c->st));
+    gid_new = c->pfd.gid;
+  }
+  LAUNCH(K_DRX, 0.0, launch_drx_update(c->mixed, f, c->grain_d, c->grain_prev_d, gid_new, c->first_drx_id, n_drx,
+                                       c->drx_rot_d, c->drx_class_d, c->tau0f, c->nsys, c->st));
+  return refresh_reference_medium(c);
+}
+
 extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
   if (!c) return set_err(MTH_ERR_ARG, "null context");
   if (!c->uploaded) return set_err(MTH_ERR_STATE, "mth_step before mth_upload_microstructure");
   SETDEV(c);
   const int istep = c->istep;
   const double dt = c->p.time_step;
+  int n_new = 0;
+  if (c->drx && istep > 0) {
+    mth_status s = drx_step(c, &n_new);
+    if (s) return s;
+  }
   c->nc.flow_off = (istep == 0 && c->p.update_flag != 1) ? 1 : 0;
   memset(c->ddg, 0, sizeof(c->ddg));
   memset(c->ddg_acum, 0, sizeof(c->ddg_acum));
@@ -801,6 +1029,7 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
     rep->err_s = c->err_s; rep->err_e = c->err_e;
     rep->newton_iters = nit;
     rep->newton_failed = nbad;
+    rep->n_new_grains = n_new;
   }
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) c->disgrad_avg[i][j] = c->disgrad_avg_t[i][j] + c->udot[i][j] * dt;
@@ -847,6 +1076,15 @@ extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, si
   if (!c || !host) return set_err(MTH_ERR_ARG, "null argument");
   if (!c->uploaded) return set_err(MTH_ERR_STATE, "no microstructure uploaded");
   SETDEV(c);
+  if (field == MTH_FIELD_RHO) {
+    if (count != (size_t)c->nv) return set_err(MTH_ERR_ARG, "count");
+    if (!c->drx) return set_err(MTH_ERR_STATE, "rho is only kept when DRX is enabled (pf_substeps > 0)");
+    const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+    CK(launch_drx_rho(c->mixed, f, c->p.rho0, c->p.rho_k, c->rho_d, c->rho_t, c->st));
+    CK(cudaMemcpyAsync(host, c->rho_d, sizeof(double) * c->nv, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return MTH_OK;
+  }
   if (field == MTH_FIELD_GRAIN) {
     if (count != (size_t)c->nv) return set_err(MTH_ERR_ARG, "count");
     std::vector<int> h(c->nv);
@@ -858,6 +1096,132 @@ extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, si
   const int ncomp = (field == MTH_FIELD_CRSS) ? 12 : (field == MTH_FIELD_GAMACUM || field == MTH_FIELD_RHO) ? 1 : 9;
   if (count != (size_t)ncomp * c->nv) return set_err(MTH_ERR_ARG, "count=%zu, expected %lld", count, ncomp * c->nv);
   return c->mixed ? download<float>(c, field, host) : download<double>(c, field, host);
+}
+
+// ------------------------------------------------------ array-level DRX
+template <typename T>
+static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps,
+                                  int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
+  const long long nv = (long long)n[0] * n[1] * n[2];
+  PfCoef co;
+  const double lgb = p->pf_width_cells * p->pf_length_scale;
+  co.mcoef = p->pf_time_step * 4.0 / 3.0 * p->m_gb / lgb;
+  co.kappa = 3.0 / 4.0 * p->e_gb * lgb / p->pf_length_scale / p->pf_length_scale;
+  co.mwell = 6 * p->e_gb / lgb;
+  co.edisl = p->stored_energy_scale * p->shear_modulus * p->burgers * p->burgers;
+  PfBuffers<T> b;
+  memset(&b, 0, sizeof(b));
+  int* g_d = nullptr;
+  T* r_d = nullptr;
+  std::vector<T> rt(nv);
+  for (long long v = 0; v < nv; v++) rt[v] = (T)rho[v];
+  mth_status st = MTH_OK;
+  cudaStream_t s = nullptr;
+  auto fail = [&](cudaError_t e, const char* what) {
+    st = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    e = cudaMalloc(&b.ids[i], sizeof(int) * PF_K * nv);
+    if (e == cudaSuccess) e = cudaMalloc(&b.phi[i], sizeof(T) * PF_K * nv);
+    if (e == cudaSuccess) e = cudaMalloc(&b.cnt[i], nv);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&b.gid, sizeof(int) * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&g_d, sizeof(int) * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&r_d, sizeof(T) * nv);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g_d, grain, sizeof(int) * nv, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(r_d, rt.data(), sizeof(T) * nv, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = launch_pf_relax<T>(n, g_d, r_d, substeps, co, b, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(grain_out, b.gid, sizeof(int) * nv, cudaMemcpyDeviceToHost, s);
+  std::vector<T> ph;
+  std::vector<uint8_t> cn;
+  if (e == cudaSuccess && ids_out) e = cudaMemcpyAsync(ids_out, b.ids[b.cur], sizeof(int) * PF_K * nv, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && phi_out) {
+    ph.resize((size_t)PF_K * nv);
+    e = cudaMemcpyAsync(ph.data(), b.phi[b.cur], sizeof(T) * PF_K * nv, cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess && cnt_out) {
+    cn.resize(nv);
+    e = cudaMemcpyAsync(cn.data(), b.cnt[b.cur], nv, cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) fail(e, "phase-field relaxation");
+  else {
+    if (phi_out)
+      for (size_t i = 0; i < ph.size(); i++) phi_out[i] = (double)ph[i];
+    if (cnt_out)
+      for (long long v = 0; v < nv; v++) cnt_out[v] = cn[v];
+  }
+  for (int i = 0; i < 2; i++) { cudaFree(b.ids[i]); cudaFree(b.phi[i]); cudaFree(b.cnt[i]); }
+  cudaFree(b.gid);
+  cudaFree(g_d);
+  cudaFree(r_d);
+  if (s) cudaStreamDestroy(s);
+  return st;
+}
+
+extern "C" mth_status mth_pf_relax(const mth_params* p, const int cell_dim[3], const int* grain, const double* rho,
+                                   int substeps, int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
+  if (!p || !cell_dim || !grain || !rho || !grain_out) return set_err(MTH_ERR_ARG, "null argument");
+  for (int i = 0; i < 3; i++)
+    if (cell_dim[i] < 1) return set_err(MTH_ERR_ARG, "cell_dim");
+  if (substeps < 0) return set_err(MTH_ERR_ARG, "substeps");
+  if (!(p->pf_length_scale > 0) || !(p->pf_width_cells > 0)) return set_err(MTH_ERR_ARG, "phase-field parameters");
+  CK(cudaSetDevice(p->device));
+  return p->precision == MTH_FP64 ? pf_relax_arrays<double>(p, cell_dim, grain, rho, substeps, grain_out, ids_out, phi_out, cnt_out)
+                                  : pf_relax_arrays<float>(p, cell_dim, grain, rho, substeps, grain_out, ids_out, phi_out, cnt_out);
+}
+
+extern "C" mth_status mth_nucleate(const mth_params* p, const int cell_dim[3], int* grain, const int* phase,
+                                   const double* rho, long long step, int first_id, long long* sites, long long cap,
+                                   int* n_new) {
+  if (!p || !cell_dim || !grain || !phase || !rho || !n_new) return set_err(MTH_ERR_ARG, "null argument");
+  const long long nv = (long long)cell_dim[0] * cell_dim[1] * cell_dim[2];
+  if (nv <= 0) return set_err(MTH_ERR_ARG, "cell_dim");
+  std::vector<uint8_t> cry(nv);
+  for (long long v = 0; v < nv; v++) {
+    if (phase[v] < 1 || phase[v] > p->n_phases) return set_err(MTH_ERR_ARG, "phase of voxel %lld", v);
+    cry[v] = p->phase[phase[v] - 1].type == 0;
+  }
+  CK(cudaSetDevice(p->device));
+  int *g_d = nullptr, *w_d = nullptr;
+  uint8_t* c_d = nullptr;
+  double* r_d = nullptr;
+  long long* s_d = nullptr;
+  unsigned long long* n_d = nullptr;
+  CK(cudaMalloc(&g_d, sizeof(int) * nv));
+  CK(cudaMalloc(&w_d, sizeof(int) * nv));
+  CK(cudaMalloc(&c_d, nv));
+  CK(cudaMalloc(&r_d, sizeof(double) * nv));
+  CK(cudaMalloc(&s_d, sizeof(long long) * MAX_CANDIDATES));
+  CK(cudaMalloc(&n_d, sizeof(unsigned long long)));
+  CK(cudaMemcpy(g_d, grain, sizeof(int) * nv, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c_d, cry.data(), nv, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(r_d, rho, sizeof(double) * nv, cudaMemcpyHostToDevice));
+  CK(cudaMemset(w_d, 0xff, sizeof(int) * nv));
+  CK(cudaMemset(n_d, 0, sizeof(unsigned long long)));
+  CK(launch_nucleation_candidates(cell_dim, g_d, c_d, r_d, p->rho_nucleation, p->nucleation_prob, p->seed,
+                                  (uint64_t)step * (uint64_t)nv, s_d, n_d, MAX_CANDIDATES, nullptr));
+  unsigned long long cnt = 0;
+  CK(cudaMemcpy(&cnt, n_d, sizeof(cnt), cudaMemcpyDeviceToHost));
+  mth_status st = MTH_OK;
+  if ((long long)cnt > MAX_CANDIDATES) {
+    st = set_err(MTH_ERR_UNSUPPORTED, "%llu nucleation candidates (limit %lld)", cnt, MAX_CANDIDATES);
+  } else {
+    std::vector<long long> sv(cnt);
+    if (cnt) CK(cudaMemcpy(sv.data(), s_d, sizeof(long long) * cnt, cudaMemcpyDeviceToHost));
+    std::sort(sv.begin(), sv.end());
+    const int nn = (int)std::min<unsigned long long>(cnt, (unsigned long long)MAX_NUCLEI);
+    if (nn) {
+      CK(cudaMemcpy(s_d, sv.data(), sizeof(long long) * nn, cudaMemcpyHostToDevice));
+      CK(launch_paint_nuclei(cell_dim, s_d, nn, p->nucleus_radius, first_id, w_d, g_d, nullptr));
+      CK(cudaMemcpy(grain, g_d, sizeof(int) * nv, cudaMemcpyDeviceToHost));
+    }
+    for (long long k = 0; k < nn && k < cap && sites; k++) sites[k] = sv[k];
+    *n_new = nn;
+  }
+  cudaFree(g_d); cudaFree(w_d); cudaFree(c_d); cudaFree(r_d); cudaFree(s_d); cudaFree(n_d);
+  return st;
 }
 
 // ------------------------------------------------- allocation-free local solve

@@ -99,6 +99,38 @@ cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, c
 cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, const double* epsp,
                                const double* strain, const double* rot, const double* crss, const double* etab,
                                double* edot, double* err, long long* iters, cudaStream_t st);
+// ------------------------------------------------------------ DRX / phase field
+constexpr int PF_K = 8;   // order parameters kept per voxel
+
+struct PfCoef { double mcoef, kappa, mwell, edisl; };
+
+template <typename T>
+struct PfBuffers {
+  int* ids[2];        // PF_K per voxel, voxel-major, sorted by id
+  T* phi[2];
+  uint8_t* cnt[2];
+  int* gid;           // current argmax grain id
+  int cur;            // buffer holding the result
+};
+
+cudaError_t launch_nucleation_candidates(const int dims[3], const int* grain, const uint8_t* crystal, const double* rho,
+                                         double rho_nuc, double prob, uint64_t seed, uint64_t counter0,
+                                         long long* out, unsigned long long* count, long long cap, cudaStream_t st);
+cudaError_t launch_paint_nuclei(const int dims[3], const long long* sites, int nn, int radius, int first_id,
+                                int* winner, int* grain, cudaStream_t st);
+template <typename T>
+cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, int substeps, const PfCoef& co,
+                            PfBuffers<T>& b, cudaStream_t st);
+// DRX microstructure update on the fields: rho from accumulated slip,
+// adoption of the relaxed grain ids and the reset of recrystallised voxels.
+cudaError_t launch_drx_rho(int mixed, const void* fields, double rho0, double rho_k, double* rho_d, void* rho_t,
+                           cudaStream_t st);
+cudaError_t launch_drx_update(int mixed, const void* fields, int* grain, const int* grain_prev, const int* gid_new,
+                              int first_drx_id, int n_drx, const double* drx_rot, const int* drx_class,
+                              double tau0f, int nsys, cudaStream_t st);
+cudaError_t launch_class_histogram(long long nv, const uint8_t* crystal, const int* eclass, unsigned long long* hist,
+                                   cudaStream_t st);
+
 long long noalloc_max_voxels();
 cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,
                                        const double* strain, const double* rot, const double* crss, double* edot,

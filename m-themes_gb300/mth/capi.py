@@ -49,7 +49,8 @@ class MthParams(C.Structure):
                 ("m_gb", C.c_double), ("pf_width_cells", C.c_double), ("stored_energy_scale", C.c_double),
                 ("shear_modulus", C.c_double), ("burgers", C.c_double), ("nucleus_radius", C.c_int),
                 ("rho_nucleation", C.c_double), ("rho0", C.c_double), ("rho_k", C.c_double),
-                ("pf_substeps", C.c_int), ("seed", C.c_uint64), ("device", C.c_int)]
+                ("pf_substeps", C.c_int), ("seed", C.c_uint64), ("nucleation_prob", C.c_double),
+                ("device", C.c_int)]
 
 
 T33 = (C.c_double * 3) * 3
@@ -118,6 +119,23 @@ def params_from_config(cfg, precision=MTH_FP64, newton_tol=0.0, newton_itmax=0) 
     p.precision = precision
     p.newton_tol = newton_tol
     p.newton_itmax = newton_itmax
+    d = getattr(cfg, "drx", None)
+    if d is not None:
+        p.pf_substeps = d.pf_substeps
+        p.pf_time_step = d.pf_time_step
+        p.pf_length_scale = d.pf_length_scale
+        p.e_gb = d.e_gb
+        p.m_gb = d.m_gb
+        p.pf_width_cells = d.pf_width_cells
+        p.stored_energy_scale = d.stored_energy_scale
+        p.shear_modulus = synth.shear_modulus(m)
+        p.burgers = d.burgers
+        p.rho0 = d.rho0
+        p.rho_k = d.rho_k
+        p.rho_nucleation = d.rho_nucleation
+        p.nucleation_prob = d.nucleation_prob
+        p.nucleus_radius = d.nucleus_radius
+        p.seed = d.seed
     return p
 
 
@@ -160,6 +178,12 @@ def load(path: str | None = None):
     lib.mth_local_solve_noalloc.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_double), C.c_size_t,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong), C.c_void_p]
+    lib.mth_pf_relax.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                 C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int)]
+    lib.mth_nucleate.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double), C.c_longlong, C.c_int, C.POINTER(C.c_longlong), C.c_longlong,
+                                 C.POINTER(C.c_int)]
     lib.mth_profile_enable.argtypes = [C.c_void_p, C.c_int]
     lib.mth_profile_read.argtypes = [C.c_void_p, C.POINTER(MthProfile), C.c_int]
     lib.mth_read_namelist.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_char_p, C.c_char_p, C.c_char_p,

@@ -44,6 +44,35 @@ class Material:
 
 
 @dataclasses.dataclass
+class Drx:
+    """Dynamic-recrystallisation parameters.  Defaults follow the reference's
+    test_run/input.in (pf_length_scale, pf_time_step, E_gb, Scale_Fdeform)
+    and the coupled DRX workload (mobility 1e-10 m^4/(J s), interface width 4
+    cells, 10 substeps, nucleus radius 2, nucleation at 5e14 m^-2).  rho is
+    rho0 + rho_k * accumulated slip in units of 1e12 m^-2."""
+    pf_substeps: int = 10
+    pf_time_step: float = 0.004
+    pf_length_scale: float = 2.5e-6
+    e_gb: float = 0.625
+    m_gb: float = 1e-10
+    pf_width_cells: float = 4.0
+    stored_energy_scale: float = 0.5
+    burgers: float = 0.362 / 2 ** 0.5      # nm, a0/sqrt(2) (src/init.c:172)
+    rho0: float = 1.0
+    rho_k: float = 600.0
+    rho_nucleation: float = 500.0
+    nucleation_prob: float = 2e-5
+    nucleus_radius: int = 2
+    seed: int = 12345
+
+
+def shear_modulus(m: "Material") -> float:
+    """Shear_G of src/init.c:826 from the cubic constants (MPa)."""
+    c11, c12, c44 = m.c11, m.c12, m.c44
+    return 0.1 * (c11 - c12 + 3 * c44) + 0.5 * (5 * (c11 - c12) * c44) / (4 * c44 + 3 * (c11 - c12))
+
+
+@dataclasses.dataclass
 class Config:
     """One run: grid, loading and control parameters (namelist keys)."""
     cell_dim: tuple = (32, 32, 32)
@@ -63,6 +92,7 @@ class Config:
     elast_bc: int = 1
     update_flag: int = 1
     hard_flag: int = 1
+    drx: Drx = None
 
 
 def voronoi(cell_dim, n_grains, rng):
@@ -262,6 +292,9 @@ def workload(name: str) -> Config:
     if name == "c1":
         return Config(cell_dim=(128, 128, 128), n_grains=512, n_pores=40, pore_radius=3,
                       n_steps=100, seed=20240102)
+    if name == "c2":    # coupled EVPFFT + sparse phase-field DRX, compression to true strain 0.5
+        return Config(cell_dim=(128, 128, 128), n_grains=1000, n_steps=500, seed=20240104,
+                      velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0), drx=Drx())
     if name == "c1m":   # 96^3 profiling case of c1: fields still larger than L2
         return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
                       n_steps=100, seed=20240103)

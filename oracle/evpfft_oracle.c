@@ -542,7 +542,8 @@ struct orc_ctx {
   int *grain, *phase;
   /* fields */
   t33 *sig, *eps, *edot, *disgrad, *velgrad, *tranmat;
-  m66* sg66;                 /* inverse of C_gr, constant per voxel */
+  m66* sg66;                 /* inverse of C_gr */
+  m66* cgr;                  /* C_gr (changes only by DRX) */
   double (*schm)[NS][5];
   double (*crss)[NS][2];
   double (*gamdot)[NS];
@@ -555,6 +556,10 @@ struct orc_ctx {
   /* macro state */
   m66 c066, s066;
   t3333 c0, s0;
+  t3333 gc0, gs0;            /* C0 and S0 of the Green operator, frozen at set-up (src/init.c:1195) */
+  mth_params par;
+  int first_drx_id, next_grain_id, n_drx;
+  double* drx_rot;           /* 9 per recrystallised grain */
   t33 udot, udot_s, udot_a, scauchy;
   int vbc[6], sbc[6], creep, elast_bc, update_flag, hard_flag;
   double dt, err_tol, time_tot, e_vm, d_vm, s_vm, s_vm1, err_e, err_s;
@@ -597,6 +602,7 @@ orc_ctx* orc_create(const mth_params* p, const int* grain, const int* phase, con
   c->velgrad = (t33*)xcalloc(nv, sizeof(t33));
   c->tranmat = (t33*)xcalloc(nv, sizeof(t33));
   c->sg66 = (m66*)xcalloc(nv, sizeof(m66));
+  c->cgr = (m66*)xcalloc(nv, sizeof(m66));
   c->schm = (double(*)[NS][5])xcalloc(nv, sizeof(double[NS][5]));
   c->crss = (double(*)[NS][2])xcalloc(nv, sizeof(double[NS][2]));
   c->gamdot = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
@@ -707,6 +713,7 @@ orc_ctx* orc_create(const mth_params* p, const int* grain, const int* phase, con
         }
         memcpy(c->tranmat[v], cache_tm, sizeof(t33));
         memcpy(c->sg66[v], cache_s, sizeof(m66));
+        memcpy(c->cgr[v], cache_c, sizeof(m66));
         memcpy(c->sig[v], cache_sig, sizeof(t33));
         for (int i = 0; i < 6; i++) for (int j = 0; j < 6; j++) csum[i][j] += cache_c[i][j];
         for (int i = 0; i < ph->nsys; i++) {
@@ -721,6 +728,12 @@ orc_ctx* orc_create(const mth_params* p, const int* grain, const int* phase, con
     if (lu_inv66(c->s066)) { st = MTH_ERR_SINGULAR; goto fail; }
     m2t4((const double(*)[6])c->c066, c->c0);
     m2t4((const double(*)[6])c->s066, c->s0);
+    memcpy(c->gc0, c->c0, sizeof(t3333));
+    memcpy(c->gs0, c->s0, sizeof(t3333));
+    c->par = *p;
+    int gmax = 0;
+    for (size_t v = 0; v < nv; v++) if (grain[v] > gmax) gmax = grain[v];
+    c->first_drx_id = c->next_grain_id = gmax + 1;
   }
   c->e_vm = c->d_vm * c->dt;
   c->istep = 0;
@@ -738,6 +751,7 @@ void orc_destroy(orc_ctx* c) {
   free(c->velgrad); free(c->tranmat); free(c->sg66); free(c->schm); free(c->crss); free(c->gamdot);
   free(c->gamacum); free(c->kbuf); free(c->nvec); free(c->conv_s); free(c->conv_e);
   free(c->newton_it); free(c->newton_bad);
+  free(c->cgr); free(c->drx_rot);
   free(c);
 }
 
@@ -757,12 +771,12 @@ static void gamma_apply(const orc_ctx* c, size_t v, const double* nv, double* ks
   if (v == 0) {
     for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++)
       for (int k = 0; k < 3; k++) for (int l = 0; l < 3; l++)
-        G[i][j][k][l] = (c->elast_bc == 0) ? -1.0 * c->s0[i][j][k][l] : 0.0;
+        G[i][j][k][l] = (c->elast_bc == 0) ? -1.0 * c->gs0[i][j][k][l] : 0.0;
   } else {
     double io[3][3], om[3][3];
     for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) {
       double s = 0.0;
-      for (int j = 0; j < 3; j++) for (int l = 0; l < 3; l++) s += c->c0[i][j][k][l] * nv[j] * nv[l];
+      for (int j = 0; j < 3; j++) for (int l = 0; l < 3; l++) s += c->gc0[i][j][k][l] * nv[j] * nv[l];
       io[i][k] = s;
     }
     /* M3Inverse (src/init.c:517-539) */
@@ -922,6 +936,74 @@ static void harden(orc_ctx* c) {
   }
 }
 
+/* Dynamic recrystallisation at the start of a mechanical step, in the order
+ * of Evolution (src/evolution.c:850-1253), restated as in drx_oracle.c:
+ * rho from accumulated slip, nucleation, phase-field relaxation, adoption
+ * of the relaxed grain ids, reset of voxels that joined a recrystallised
+ * grain (src/evolution.c:1120-1200) and the new reference medium C066/S0
+ * (src/evolution.c:1200-1216; the Green operator keeps the initial C0). */
+static int orc_drx_step(orc_ctx* c, int* n_new) {
+  const size_t nv = c->nv;
+  const mth_params* p = &c->par;
+  const phase_t* ph0 = &c->ph[0];
+  double* rho = (double*)malloc(sizeof(double) * nv);
+  int* cry = (int*)malloc(sizeof(int) * nv);
+  int* prev = (int*)malloc(sizeof(int) * nv);
+  int* gnew = (int*)malloc(sizeof(int) * nv);
+  long long* sites = (long long*)malloc(sizeof(long long) * 65536);
+  for (size_t v = 0; v < nv; v++) {
+    const int crystal = c->ph[c->phase[v] - 1].type == 0;
+    cry[v] = crystal;
+    rho[v] = crystal ? p->rho0 + p->rho_k * c->gamacum[v] : 0.0;
+    prev[v] = c->grain[v];
+  }
+  long long ns = orc_nucleation_sites(c->n, c->grain, cry, rho, p->rho_nucleation, p->nucleation_prob, p->seed,
+                                      c->istep, sites, 65536);
+  int nn = (int)(ns < 65536 ? ns : 65536);
+  if (nn > 0) {
+    c->drx_rot = (double*)realloc(c->drx_rot, sizeof(double) * 9 * (size_t)(c->n_drx + nn));
+    for (int k = 0; k < nn; k++) memcpy(c->drx_rot + 9 * (size_t)(c->n_drx + k), c->tranmat[sites[k]], sizeof(t33));
+    orc_paint_nuclei(c->n, c->grain, sites, nn, c->next_grain_id, p->nucleus_radius);
+    c->next_grain_id += nn;
+    c->n_drx += nn;
+  }
+  *n_new = nn;
+  int st = MTH_OK;
+  if (c->n_drx > 0) {
+    st = orc_pf_relax(p, c->n, c->grain, rho, p->pf_substeps, 8, gnew, NULL, NULL, NULL);
+    for (size_t v = 0; v < nv && st == MTH_OK; v++) {
+      const int g = gnew[v];
+      c->grain[v] = g;
+      const int k = g - c->first_drx_id;
+      if (g == prev[v] || !cry[v] || k < 0 || k >= c->n_drx) continue;
+      memset(c->sig[v], 0, sizeof(t33));
+      c->gamacum[v] = 0.0;
+      for (int i = 0; i < ph0->nsys; i++) { c->crss[v][i][0] = ph0->tau[0]; c->crss[v][i][1] = ph0->tau[1]; }
+      memcpy(c->tranmat[v], c->drx_rot + 9 * (size_t)k, sizeof(t33));
+      t33 sa2xt;
+      t3333 caux;
+      for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) sa2xt[i][j] = c->tranmat[v][j][i];
+      ten4_inverse_transform(caux, (const double(*)[3])sa2xt, (const double(*)[3][3][3])ph0->cijkl);
+      t42m((const double(*)[3][3][3])caux, c->cgr[v]);
+      memcpy(c->sg66[v], c->cgr[v], sizeof(m66));
+      if (lu_inv66(c->sg66[v])) st = MTH_ERR_SINGULAR;
+    }
+    if (st == MTH_OK) {
+      m66 csum;
+      memset(csum, 0, sizeof(csum));
+      for (size_t v = 0; v < nv; v++)
+        if (cry[v]) for (int i = 0; i < 6; i++) for (int j = 0; j < 6; j++) csum[i][j] += c->cgr[v][i][j];
+      for (int i = 0; i < 6; i++) for (int j = 0; j < 6; j++) c->c066[i][j] = csum[i][j] * c->wgt;
+      memcpy(c->s066, c->c066, sizeof(m66));
+      if (lu_inv66(c->s066)) st = MTH_ERR_SINGULAR;
+      m2t4((const double(*)[6])c->c066, c->c0);
+      m2t4((const double(*)[6])c->s066, c->s0);
+    }
+  }
+  free(rho); free(cry); free(prev); free(gnew); free(sites);
+  return st;
+}
+
 /* One mechanical step: body of the istep loop in Evolution
  * (src/evolution.c:1319-1693) on the power-law path. */
 int orc_step(orc_ctx* c, mth_step_report* rep) {
@@ -929,6 +1011,11 @@ int orc_step(orc_ctx* c, mth_step_report* rep) {
   const int istep = c->istep;
   int st = MTH_OK;
   if (c->creep == 1 && c->e_vm > 0.3) return MTH_ERR_STATE;   /* src/evolution.c:606 */
+  int n_new = 0;
+  if (c->par.pf_substeps > 0 && istep > 0) {
+    st = orc_drx_step(c, &n_new);
+    if (st) return st;
+  }
   /* src/evolution.c:1319-1332 */
 #pragma omp parallel for schedule(static)
   for (long long v = 0; v < (long long)nv; v++)
@@ -1076,6 +1163,7 @@ int orc_step(orc_ctx* c, mth_step_report* rep) {
     rep->err_s = c->err_s; rep->err_e = c->err_e;
     rep->newton_iters = nit_total;
     rep->newton_failed = nbad_total;
+    rep->n_new_grains = n_new;
   }
   /* next macro guess (src/evolution.c:1691-1693) */
   for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++)
@@ -1101,6 +1189,9 @@ int orc_get_field(orc_ctx* c, int field, double* out) {
         break;
       case MTH_FIELD_GAMACUM: out[v] = c->gamacum[v]; break;
       case MTH_FIELD_GRAIN: out[v] = (double)c->grain[v]; break;
+      case MTH_FIELD_RHO:
+        out[v] = c->ph[c->phase[v] - 1].type == 0 ? c->par.rho0 + c->par.rho_k * c->gamacum[v] : 0.0;
+        break;
       default: return MTH_ERR_ARG;
     }
   }

@@ -42,6 +42,17 @@ int orc_local_solve(const mth_params* p, const double c066[36], size_t n,
                     const double* rot, const double* crss, double* edot,
                     double* err, long long* newton_iters);
 
+/* DRX restatement (oracle/drx_oracle.c). */
+double orc_uniform(uint64_t seed, uint64_t counter);
+void orc_pf_coefficients(const mth_params* p, double* mcoef, double* kappa, double* mwell, double* edisl);
+void orc_gb_indicator(const int* n, const int* grain, unsigned char* gb);
+long long orc_nucleation_sites(const int* n, const int* grain, const int* phase_crystal, const double* rho,
+                               double rho_nuc, double prob, uint64_t seed, long long step, long long* sites,
+                               long long cap);
+void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, int first_id, int radius);
+int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps, int K,
+                 int* grain_out, int* ids_out, double* phi_out, int* cnt_out);
+
 /* Complex FFT used by the oracle: in-place 3-D transform of an n0*n1*n2
  * array of interleaved (re,im) doubles, un-normalised, sign -1 forward,
  * +1 backward (FFTW 2.1.5 convention used at src/evolution.c:1367,1399). */

@@ -24,10 +24,12 @@ SVM_OOB_ZERO, SVM_OOB_EPSAVG10, SVM_OOB_SIGAVG1_00 = 0, 1, 2
 def build(force=False):
     """Compile oracle/evpfft_oracle.c into oracle/_build/liborc.so."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    src = os.path.join(HERE, "evpfft_oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("evpfft_oracle.c", "drx_oracle.c")]
+    deps = srcs + [os.path.join(HERE, "oracle.h"), os.path.join(REPO, "include", "mth.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
-    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", LIB, src, "-lm"]
+    # no FMA contraction: every operation separately rounded, on x86 and Arm alike
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", LIB] + srcs + ["-lm"]
     subprocess.check_call(cmd)
     return LIB
 
@@ -54,6 +56,17 @@ def load():
                                         C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
         lib.orc_fft3d.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int, C.c_int]
+        lib.orc_uniform.restype = C.c_double
+        lib.orc_uniform.argtypes = [C.c_uint64, C.c_uint64]
+        lib.orc_nucleation_sites.restype = C.c_longlong
+        lib.orc_nucleation_sites.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                             C.POINTER(C.c_double), C.c_double, C.c_double, C.c_uint64,
+                                             C.c_longlong, C.POINTER(C.c_longlong), C.c_longlong]
+        lib.orc_paint_nuclei.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.c_int,
+                                         C.c_int, C.c_int]
+        lib.orc_pf_relax.argtypes = [C.POINTER(capi.MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_int)]
         _lib = lib
     return _lib
 
@@ -132,3 +145,38 @@ def fft3d(data, sign):
     n0, n1, n2 = a.shape
     lib.orc_fft3d(a.ctypes.data_as(C.POINTER(C.c_double)), n0, n1, n2, sign)
     return a
+
+
+def pf_relax(params, dims, grain, rho, substeps, K=8):
+    """Oracle phase-field relaxation: (grain_out, ids[N,K], phi[N,K], cnt[N])."""
+    lib = load()
+    nv = int(np.prod(dims))
+    d = (C.c_int * 3)(*dims)
+    g = np.ascontiguousarray(grain, dtype=np.int32)
+    r = np.ascontiguousarray(rho, dtype=np.float64)
+    go = np.zeros(nv, np.int32)
+    ids = np.zeros(nv * K, np.int32)
+    phi = np.zeros(nv * K)
+    cnt = np.zeros(nv, np.int32)
+    st = lib.orc_pf_relax(C.byref(params), d, capi._iptr(g), capi._dptr(r), substeps, K, capi._iptr(go),
+                          capi._iptr(ids), capi._dptr(phi), capi._iptr(cnt))
+    if st != 0:
+        raise RuntimeError("orc_pf_relax failed")
+    return go, ids.reshape(nv, K), phi.reshape(nv, K), cnt
+
+
+def nucleate(params, dims, grain, crystal, rho, step, first_id, cap=65536):
+    """Oracle nucleation: (painted grain, sites)."""
+    lib = load()
+    d = (C.c_int * 3)(*dims)
+    g = np.ascontiguousarray(grain, dtype=np.int32).copy()
+    cr = np.ascontiguousarray(crystal, dtype=np.int32)
+    r = np.ascontiguousarray(rho, dtype=np.float64)
+    sites = np.zeros(cap, np.int64)
+    n = lib.orc_nucleation_sites(d, capi._iptr(g), capi._iptr(cr), capi._dptr(r), params.rho_nucleation,
+                                 params.nucleation_prob, params.seed, step,
+                                 sites.ctypes.data_as(C.POINTER(C.c_longlong)), cap)
+    nn = int(min(n, cap))
+    lib.orc_paint_nuclei(d, capi._iptr(g), sites.ctypes.data_as(C.POINTER(C.c_longlong)), nn, first_id,
+                         params.nucleus_radius)
+    return g, sites[:nn]

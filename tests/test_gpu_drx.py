@@ -1,0 +1,114 @@
+"""GPU dynamic recrystallisation against the DRX restatement in the oracle.
+
+FP64: the phase-field relaxation and the nucleation are the same separately
+rounded IEEE operations in the same order (oracle built with
+-ffp-contract=off, kernels with -fmad=false), so order parameters, grain maps
+and nucleation sites must be bit-identical.  Mixed precision (FP32 order
+parameters) must agree on at least 99% of the grain map."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pyoracle
+from helpers import rel
+from mth import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    import os
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call([sys.executable, os.path.join(repo, "m-themes_gb300", "build.py")])
+    return capi.load()
+
+
+def pf_case(dims=(24, 24, 24), seed=3):
+    cfg = synth.Config(cell_dim=dims, n_grains=8, seed=seed, drx=synth.Drx())
+    g, _, _ = synth.microstructure(cfg)
+    rng = np.random.default_rng(seed)
+    base = 100.0 + 400.0 * rng.random(9)
+    rho = base[g] + 20.0 * rng.random(g.size)
+    # three dislocation-free nuclei on grain boundaries
+    ax = [np.arange(n) for n in dims]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    for k, c in enumerate(((4, 5, 6), (15, 10, 18), (20, 20, 3))):
+        m = ((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2 <= 4).ravel()
+        g[m] = 9 + k
+        rho[m] = 1.0
+    return cfg, g.astype(np.int32), rho
+
+
+def gpu_pf(lib, par, dims, g, rho, substeps):
+    nv = g.size
+    d = (C.c_int * 3)(*dims)
+    go = np.zeros(nv, np.int32)
+    ids = np.zeros(nv * 8, np.int32)
+    phi = np.zeros(nv * 8)
+    cnt = np.zeros(nv, np.int32)
+    capi.check(lib, lib.mth_pf_relax(C.byref(par), d, capi._iptr(g), capi._dptr(rho), substeps, capi._iptr(go),
+                                     capi._iptr(ids), capi._dptr(phi), capi._iptr(cnt)))
+    return go, ids.reshape(nv, 8), phi.reshape(nv, 8), cnt
+
+
+def test_pf_relax_fp64_bit_exact(lib):
+    cfg, g, rho = pf_case()
+    par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
+    o = pyoracle.pf_relax(par, cfg.cell_dim, g, rho, 8)
+    r = gpu_pf(lib, par, cfg.cell_dim, g, rho, 8)
+    assert np.array_equal(r[0], o[0])                 # grain map
+    assert np.array_equal(r[3], o[3])                 # counts
+    assert np.array_equal(r[1], o[1])                 # ids
+    assert np.array_equal(r[2].view(np.int64), o[2].view(np.int64))   # values, bit for bit
+    assert (r[0] >= 9).sum() > 0
+
+
+def test_pf_relax_mixed_close(lib):
+    cfg, g, rho = pf_case(seed=5)
+    par64 = capi.params_from_config(cfg, precision=capi.MTH_FP64)
+    par32 = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
+    o = pyoracle.pf_relax(par64, cfg.cell_dim, g, rho, 8)
+    r = gpu_pf(lib, par32, cfg.cell_dim, g, rho, 8)
+    assert (r[0] == o[0]).mean() >= 0.99
+
+
+def test_nucleation_bit_exact(lib):
+    dims = (20, 20, 20)
+    cfg = synth.Config(cell_dim=dims, n_grains=9, seed=8,
+                       drx=synth.Drx(rho_nucleation=50.0, nucleation_prob=0.03, seed=777))
+    g, ph, _ = synth.microstructure(cfg)
+    rho = 100.0 * np.random.default_rng(1).random(g.size)
+    par = capi.params_from_config(cfg)
+    og, osites = pyoracle.nucleate(par, dims, g, np.ones(g.size, np.int32), rho, step=7, first_id=10)
+    gg = g.astype(np.int32).copy()
+    sites = np.zeros(65536, np.int64)
+    n = C.c_int(0)
+    capi.check(lib, lib.mth_nucleate(C.byref(par), (C.c_int * 3)(*dims), capi._iptr(gg), capi._iptr(ph),
+                                     capi._dptr(rho), 7, 10, sites.ctypes.data_as(C.POINTER(C.c_longlong)), 65536,
+                                     C.byref(n)))
+    assert n.value == osites.size > 0
+    assert np.array_equal(sites[:n.value], osites)
+    assert np.array_equal(gg, og)
+
+
+def test_coupled_drx_matches_oracle():
+    cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=6, n_steps=6, seed=5, iter_max=8,
+                       drx=synth.Drx(rho_k=4000.0, rho_nucleation=30.0, nucleation_prob=0.02))
+    g, p, e = synth.microstructure(cfg)
+    par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
+    from mth import Solver
+    s = Solver(par, g, p, e)
+    o = pyoracle.Oracle(par, g, p, e, nthreads=4)
+    total_new = 0
+    for k in range(cfg.n_steps):
+        a, b = s.step(), o.step()
+        assert a["n_new_grains"] == b["n_new_grains"], k
+        total_new += a["n_new_grains"]
+        assert np.array_equal(s.field("grain"), o.field("grain")), k
+        assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
+    assert total_new > 0
+    assert rel(s.field("sig"), o.field("sig")) < 1e-5
