@@ -154,8 +154,8 @@ def run_gpu(args):
         torch.cuda.set_device(lrank)
         dist.init_process_group("nccl")
     dev_index = lrank if ws > 1 else 0
-    cfg = workload_cfg(args)
-    cfg.seed += rank     # replicas: each rank its own RVE of the same size
+    from mth import replicas
+    cfg = replicas.replica_config(workload_cfg(args), rank)   # replicas: each rank its own RVE
     grain, phase, euler = synth.microstructure(cfg)
     nv = int(np.prod(cfg.cell_dim))
     prec = capi.MTH_MIXED if args.precision == "mixed" else capi.MTH_FP64
