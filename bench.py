@@ -221,7 +221,7 @@ def run_gpu(args):
                       "l2": "fields (~0.5 GB) larger than the 129 MB L2; no flush"}}
 
     # roofline of the dominant kernel (device time from CUDA events on the library stream)
-    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    dom = max(((k, v) for k, v in prof.items() if v["bytes"] > 0), key=lambda kv: kv[1]["ms"])
     dname, d = dom
     peak, peak_kind = measured_peaks()
     per_launch_s = (d["ms"] / 1e3) / max(d["launches"], 1)

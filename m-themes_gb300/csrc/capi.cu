@@ -355,9 +355,10 @@ static void ctx_free(mth_ctx* c) {
 
 // ------------------------------------------------------------- profiling
 enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_DRX,
-       K_NCLASS };
+       K_PF, K_NCLASS };
 static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain", "newton",
-                                        "reduce", "end_step", "spin_fft", "setup", "drx_pf"};
+                                        "reduce", "end_step", "spin_fft", "setup", "drx",
+                                        "pf_relax"};
 
 static void prof_begin(mth_ctx* c) {
   if (!c->prof_on) return;
@@ -371,8 +372,8 @@ static void prof_begin(mth_ctx* c) {
   }
   cudaEventRecord((*c->ev_pool)[2 * i], c->st);
 }
-static void prof_end(mth_ctx* c, int cls, double bytes) {
-  c->prof_launch[cls]++;
+static void prof_end(mth_ctx* c, int cls, int kernels, double bytes) {
+  c->prof_launch[cls] += kernels;
   c->prof_bytes[cls] += bytes;
   if (!c->prof_on) return;
   size_t i = c->ev_pending->size();
@@ -389,13 +390,16 @@ static void prof_resolve(mth_ctx* c) {
   }
   c->ev_pending->clear();
 }
-#define LAUNCH(cls, bytes, call)          \
-  do {                                    \
-    prof_begin(c);                        \
-    cudaError_t e__ = (call);             \
-    prof_end(c, cls, (double)(bytes));    \
-    if (e__ != cudaSuccess) CK(e__);      \
+// one launcher call of class cls issuing `kernels` kernels that move
+// `bytes` algorithmic bytes
+#define LAUNCHN(cls, kernels, bytes, call)         \
+  do {                                             \
+    prof_begin(c);                                 \
+    cudaError_t e__ = (call);                      \
+    prof_end(c, cls, (kernels), (double)(bytes));  \
+    if (e__ != cudaSuccess) CK(e__);               \
   } while (0)
+#define LAUNCH(cls, bytes, call) LAUNCHN(cls, 1, bytes, call)
 
 template <typename T>
 static mth_status make_twiddles(int n, int sign, void** out) {
@@ -799,7 +803,7 @@ static mth_status refresh_reference_medium(mth_ctx* c) {
     CK(cudaMalloc(&c->hist_d, sizeof(unsigned long long) * c->hist_cap));
   }
   CK(cudaMemsetAsync(c->hist_d, 0, sizeof(unsigned long long) * ncl, c->st));
-  LAUNCH(K_DRX, 0.0, launch_class_histogram(c->nv, c->crystal_d, c->eclass_d, c->hist_d, c->st));
+  LAUNCH(K_DRX, 5.0 * c->nv, launch_class_histogram(c->nv, c->crystal_d, c->eclass_d, c->hist_d, c->st));
   std::vector<unsigned long long> hist(ncl);
   CK(cudaMemcpyAsync(hist.data(), c->hist_d, sizeof(unsigned long long) * ncl, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -829,6 +833,18 @@ static mth_status refresh_reference_medium(mth_ctx* c) {
   return MTH_OK;
 }
 
+// Algorithmic HBM bytes of one phase-field relaxation of nv voxels with
+// field element size ts: each pass reads and/or writes the sparse state
+// (PF_K ids and order parameters and a count per voxel) once; neighbour
+// reads are served from cache.
+static double pf_relax_bytes(long long nv, size_t ts, int substeps) {
+  const double state = PF_K * (4.0 + (double)ts) + 1.0;
+  const double init = 4.0 + state + 4.0;                   // grain in; state, grain id out
+  const double sub = 2.0 * state + (double)ts + 4.0;       // state in and out, rho, grain id
+  const double amax = state + 4.0;                         // state in, grain id out
+  return (double)nv * (init + substeps * (sub + amax));
+}
+
 // Dynamic recrystallisation at the start of a mechanical step, the order of
 // Evolution (src/evolution.c:850-1253): nucleation, phase-field relaxation,
 // microstructure update, reset of recrystallised voxels, new reference
@@ -837,11 +853,13 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   *n_new = 0;
   const mth_params& p = c->p;
   const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
-  LAUNCH(K_DRX, 0.0, launch_drx_rho(c->mixed, f, p.rho0, p.rho_k, c->rho_d, c->rho_t, c->st));
+  const double es = c->mixed ? 4.0 : 8.0;   // bytes of a field element
+  LAUNCH(K_DRX, (double)c->nv * (4 + 2 * es + 8),
+         launch_drx_rho(c->mixed, f, p.rho0, p.rho_k, c->rho_d, c->rho_t, c->st));
   CK(cudaMemcpyAsync(c->grain_prev_d, c->grain_d, sizeof(int) * c->nv, cudaMemcpyDeviceToDevice, c->st));
   // nucleation
   CK(cudaMemsetAsync(c->count_d, 0, sizeof(unsigned long long), c->st));
-  LAUNCH(K_DRX, 0.0, launch_nucleation_candidates(c->n, c->grain_d, c->crystal_d, c->rho_d, p.rho_nucleation,
+  LAUNCH(K_DRX, (double)c->nv * (4 + 1 + 8), launch_nucleation_candidates(c->n, c->grain_d, c->crystal_d, c->rho_d, p.rho_nucleation,
                                                   p.nucleation_prob, p.seed, (uint64_t)c->istep * (uint64_t)c->nv,
                                                   c->sites_d, c->count_d, MAX_CANDIDATES, c->st));
   unsigned long long cnt = 0;
@@ -859,15 +877,12 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
     CK(cudaMemcpy(c->sites_d, sites.data(), sizeof(long long) * nn, cudaMemcpyHostToDevice));
     // each nucleus takes the current orientation of its parent voxel
     // (src/integrated.c:271-283): gather the rotations
-    const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
-    std::vector<unsigned char> rb(esz);
     std::vector<double> R((size_t)nn * 9);
-    const char* rot = c->mixed ? (const char*)c->ff.rot : (const char*)c->fd.rot;
-    for (int k = 0; k < nn; k++)
-      for (int i = 0; i < 9; i++) {
-        CK(cudaMemcpy(rb.data(), rot + esz * ((size_t)i * c->nv + sites[k]), esz, cudaMemcpyDeviceToHost));
-        R[(size_t)k * 9 + i] = c->mixed ? (double)*(float*)rb.data() : *(double*)rb.data();
-      }
+    const void* rot = c->mixed ? (const void*)c->ff.rot : (const void*)c->fd.rot;
+    LAUNCH(K_DRX, 9.0 * nn * (8 + (c->mixed ? 4 : 8)),
+           launch_gather_rot(c->mixed, rot, c->nv, c->sites_d, nn, c->gather_d, c->st));
+    CK(cudaMemcpyAsync(R.data(), c->gather_d, sizeof(double) * 9 * nn, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     for (int k = 0; k < nn; k++) {
       const int cls = (int)(c->etab_h->size() / ETAB_W);
       c->etab_h->resize(c->etab_h->size() + ETAB_W);
@@ -875,7 +890,7 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
       c->drx_rot_h->insert(c->drx_rot_h->end(), &R[(size_t)k * 9], &R[(size_t)k * 9] + 9);
       c->drx_class_h->push_back(cls);
     }
-    LAUNCH(K_DRX, 0.0, launch_paint_nuclei(c->n, c->sites_d, nn, p.nucleus_radius, c->next_grain_id, c->winner_d,
+    LAUNCHN(K_DRX, 2, (double)c->nv * 8, launch_paint_nuclei(c->n, c->sites_d, nn, p.nucleus_radius, c->next_grain_id, c->winner_d,
                                            c->grain_d, c->st));
     c->next_grain_id += nn;
   }
@@ -901,15 +916,15 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   // phase-field relaxation from the painted grain map
   int* gid_new;
   if (c->mixed) {
-    LAUNCH(K_DRX, 0.0, launch_pf_relax<float>(c->n, c->grain_d, (const float*)c->rho_t, p.pf_substeps, c->pfc, c->pff,
-                                              c->st));
+    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nv, sizeof(float), p.pf_substeps),
+            launch_pf_relax<float>(c->n, c->grain_d, (const float*)c->rho_t, p.pf_substeps, c->pfc, c->pff, c->st));
     gid_new = c->pff.gid;
   } else {
-    LAUNCH(K_DRX, 0.0, launch_pf_relax<double>(c->n, c->grain_d, (const double*)c->rho_t, p.pf_substeps, c->pfc,
-                                               c->pfd, c->st));
+    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nv, sizeof(double), p.pf_substeps),
+            launch_pf_relax<double>(c->n, c->grain_d, (const double*)c->rho_t, p.pf_substeps, c->pfc, c->pfd, c->st));
     gid_new = c->pfd.gid;
   }
-  LAUNCH(K_DRX, 0.0, launch_drx_update(c->mixed, f, c->grain_d, c->grain_prev_d, gid_new, c->first_drx_id, n_drx,
+  LAUNCH(K_DRX, (double)c->nv * 12, launch_drx_update(c->mixed, f, c->grain_d, c->grain_prev_d, gid_new, c->first_drx_id, n_drx,
                                        c->drx_rot_d, c->drx_class_d, c->tau0f, c->nsys, c->st));
   return refresh_reference_medium(c);
 }

@@ -403,4 +403,26 @@ cudaError_t launch_class_histogram(long long nv, const uint8_t* crystal, const i
   return cudaGetLastError();
 }
 
+// rotation matrices (9 components, component-major fields) of the parent
+// voxels of the nn nuclei, as double, nucleus-major: out[k*9 + i]
+template <typename TSt>
+__global__ void gather_rot_kernel(const TSt* __restrict__ rot, long long nv, const long long* __restrict__ sites, int nn,
+                                  double* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 9LL * nn) return;
+  const long long k = t / 9;
+  const int i = (int)(t - 9 * k);
+  out[t] = (double)rot[(size_t)i * nv + sites[k]];
+}
+
+cudaError_t launch_gather_rot(int mixed, const void* rot, long long nv, const long long* sites, int nn, double* out,
+                              cudaStream_t st) {
+  if (nn <= 0) return cudaSuccess;
+  if (mixed)
+    gather_rot_kernel<float><<<nb(9LL * nn, 256), 256, 0, st>>>(static_cast<const float*>(rot), nv, sites, nn, out);
+  else
+    gather_rot_kernel<double><<<nb(9LL * nn, 256), 256, 0, st>>>(static_cast<const double*>(rot), nv, sites, nn, out);
+  return cudaGetLastError();
+}
+
 }  // namespace mth

@@ -130,6 +130,8 @@ cudaError_t launch_drx_update(int mixed, const void* fields, int* grain, const i
                               double tau0f, int nsys, cudaStream_t st);
 cudaError_t launch_class_histogram(long long nv, const uint8_t* crystal, const int* eclass, unsigned long long* hist,
                                    cudaStream_t st);
+cudaError_t launch_gather_rot(int mixed, const void* rot, long long nv, const long long* sites, int nn, double* out,
+                              cudaStream_t st);
 
 long long noalloc_max_voxels();
 cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,

@@ -174,9 +174,12 @@ struct VoxelOut {
 // (plastic strain rate, sample frame).
 // TF: flow rule, residual, Hessian assembly, line search and frame
 // transforms; TL: accuracy of the Jacobian (Hessian) solve.  FP64 mode: both
-// double.  Mixed mode: TF = float, TL = double: the FP32-assembled 5x5
-// system is factored and solved in FP64 (GB300 issues FP64 at 1/64 of the
-// FP32 rate, so everything else stays FP32).  Fast mode: both float.
+// double.  Mixed mode: TF = float, TL = double: once the Newton is within
+// 1e-3 |lambda| of the root (the iterations that fix the converged answer)
+// the FP32-assembled 5x5 system is factored and solved in FP64; the large
+// early steps, whose direction only has to be a descent direction, use the
+// FP32 factorisation (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
+// mode: all float.
 template <typename TF, typename TL>
 __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const double* __restrict__ et,
                                 const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* tauf, TF* sig6,
@@ -248,6 +251,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
   const TF tau_off = (TF)ph.tau_back_minus_fwd;
   int it = 0;
   bool done = false;
+  bool near_root = false;   // previous step within 1e-3 |lambda|
   TF hstep2 = dh * dh;   // the first step includes the hydrostatic correction
   for (; it < nc.itmax && !done; it++) {
     TF edf[5], Df[15], psif;
@@ -272,8 +276,9 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
       for (int i = 0; i < 5; i++) mg[i] = -g[i];
       bool ok;
-      if constexpr (sizeof(TL) > sizeof(TF)) {
-        // FP64 Jacobian solve of the FP32-assembled system
+      if (sizeof(TL) > sizeof(TF) && near_root) {
+        // FP64 Jacobian solve of the FP32-assembled system for the steps
+        // that set the converged answer
         TL Hl[15], bl[5], pl[5];
 #pragma unroll
         for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
@@ -322,6 +327,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
     for (int i = 0; i < 5; i++) x[i] += alpha * p[i];
     const TF step2 = alpha * alpha * pn2 + hstep2;
     hstep2 = 0;
+    near_root = step2 <= ls_thr2;
     TF den2 = ref2;
     if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
     if (!(den2 > (TF)0) || step2 <= tol2 * den2) done = true;

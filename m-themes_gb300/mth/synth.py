@@ -295,6 +295,10 @@ def workload(name: str) -> Config:
     if name == "c2":    # coupled EVPFFT + sparse phase-field DRX, compression to true strain 0.5
         return Config(cell_dim=(128, 128, 128), n_grains=1000, n_steps=500, seed=20240104,
                       velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0), drx=Drx())
+    if name == "c2s":   # 64^3 profiling case of c2: nucleation from the second step on
+        return Config(cell_dim=(64, 64, 64), n_grains=125, n_steps=10, seed=20240105, iter_max=10,
+                      velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0),
+                      drx=Drx(rho_k=40000.0, nucleation_prob=2e-3))
     if name == "c1m":   # 96^3 profiling case of c1: fields still larger than L2
         return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
                       n_steps=100, seed=20240103)
