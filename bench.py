@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--precision", choices=["mixed", "fp64", "mixed_fast"], default="mixed")
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--iter-max", type=int, default=0, help="override IterMax (default: the workload's 100)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
@@ -158,7 +158,7 @@ def run_gpu(args):
     cfg = replicas.replica_config(workload_cfg(args), rank)   # replicas: each rank its own RVE
     grain, phase, euler = synth.microstructure(cfg)
     nv = int(np.prod(cfg.cell_dim))
-    prec = capi.MTH_MIXED if args.precision == "mixed" else capi.MTH_FP64
+    prec = {"mixed": capi.MTH_MIXED, "fp64": capi.MTH_FP64, "mixed_fast": capi.MTH_MIXED_FAST}[args.precision]
 
     def barrier_sync():
         torch.cuda.synchronize()
@@ -212,7 +212,8 @@ def run_gpu(args):
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f32 fields + f64 Newton" if prec == capi.MTH_MIXED else "f64",
+           "dtype": {capi.MTH_MIXED: "f32 fields + f64 Newton solve", capi.MTH_FP64: "f64",
+                     capi.MTH_MIXED_FAST: "f32"}[prec],
            "data": "synthetic: seeded periodic Voronoi, 512 grains, uniform SO(3) orientations, 40 radius-3 pores",
            "config": {"workload": "128^3 RVE, 512 grains, 40 pores, FCC Cu power law n=10 + Voce, uniaxial "
                                   "tension eps33_dot=1/s, dt=1e-3, IterMax=%d" % cfg.iter_max,

@@ -264,6 +264,7 @@ struct mth_ctx {
   int* grain_d;
   int* eclass_d;
   double* etab_d;
+  float* etabf_d;      // float copy of the class table for the FP32 paths
   int nclass;
   double* partials;
   double* red;
@@ -319,6 +320,7 @@ static void ctx_free(mth_ctx* c) {
   cudaFree(c->grain_d);
   cudaFree(c->eclass_d);
   cudaFree(c->etab_d);
+  cudaFree(c->etabf_d);
   cudaFree(c->partials);
   cudaFree(c->red);
   if (c->red_h) cudaFreeHost(c->red_h);
@@ -540,6 +542,7 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     f.phase = c->phase_d;
     f.eclass = c->eclass_d;
     f.etab = nullptr;
+    f.etabf = nullptr;
     f.nv = P;
   };
   if (c->mixed) carve(static_cast<float*>(c->fieldmem), c->ff);
@@ -606,6 +609,27 @@ static mth_status reduce_to_host(mth_ctx* c, int width, double* out) {
   return MTH_OK;
 }
 
+// (Re)upload the elastic class table in double and as a float copy; the
+// stream is synchronised first so no kernel still reads the old tables.
+static mth_status upload_class_table(mth_ctx* c, const std::vector<double>& rows) {
+  CK(cudaStreamSynchronize(c->st));
+  cudaFree(c->etab_d);
+  cudaFree(c->etabf_d);
+  c->etab_d = nullptr;
+  c->etabf_d = nullptr;
+  std::vector<float> rf(rows.size());
+  for (size_t i = 0; i < rows.size(); i++) rf[i] = (float)rows[i];
+  CK(cudaMalloc(&c->etab_d, sizeof(double) * rows.size()));
+  CK(cudaMalloc(&c->etabf_d, sizeof(float) * rows.size()));
+  CK(cudaMemcpy(c->etab_d, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->etabf_d, rf.data(), sizeof(float) * rows.size(), cudaMemcpyHostToDevice));
+  c->ff.etab = c->etab_d;
+  c->fd.etab = c->etab_d;
+  c->ff.etabf = c->etabf_d;
+  c->fd.etabf = c->etabf_d;
+  return MTH_OK;
+}
+
 extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, const int* phase,
                                                 const double* euler_deg, size_t n) {
   if (!c || !grain || !phase || !euler_deg) return set_err(MTH_ERR_ARG, "null argument");
@@ -667,8 +691,6 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   for (int i = 0; i < 5; i++)
     for (int j = 0; j < 5; j++) c->nc.s0dev[i * 5 + j] = c->s066[i][j];
   c->nc.s0hh = c->s066[5][5];
-  cudaFree(c->etab_d);
-  c->etab_d = nullptr;
   c->nclass = (int)counts.size();
   *c->etab_h = rows;
   {
@@ -685,12 +707,12 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
     c->tau0f = c->nc.ph[0].tau0f;
     c->nsys = c->nc.ph[0].nsys;
   }
-  CK(cudaMalloc(&c->etab_d, sizeof(double) * rows.size()));
-  c->ff.etab = c->etab_d;
-  c->fd.etab = c->etab_d;
+  {
+    mth_status s = upload_class_table(c, rows);
+    if (s != MTH_OK) return s;
+  }
   double* eul_d = nullptr;
   CK(cudaMalloc(&eul_d, sizeof(double) * 3 * n));
-  CK(cudaMemcpyAsync(c->etab_d, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(eul_d, euler_deg, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->phase_d, ph.data(), n, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->grain_d, grain, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
@@ -824,11 +846,10 @@ static mth_status refresh_reference_medium(mth_ctx* c) {
   for (int i = 0; i < 5; i++)
     for (int j = 0; j < 5; j++) c->nc.s0dev[i * 5 + j] = c->s066[i][j];
   c->nc.s0hh = c->s066[5][5];
-  cudaFree(c->etab_d);
-  CK(cudaMalloc(&c->etab_d, sizeof(double) * rows.size()));
-  CK(cudaMemcpyAsync(c->etab_d, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, c->st));
-  c->ff.etab = c->etab_d;
-  c->fd.etab = c->etab_d;
+  {
+    mth_status s = upload_class_table(c, rows);
+    if (s != MTH_OK) return s;
+  }
   c->nclass = ncl;
   return MTH_OK;
 }
@@ -899,11 +920,10 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   if (n_drx == 0) return MTH_OK;
   // class table with the new rows (S066 part refreshed below)
   for (size_t k = 0; k < c->etab_h->size() / ETAB_W; k++) class_row_add_s0(&(*c->etab_h)[k * ETAB_W], c->s066);
-  cudaFree(c->etab_d);
-  CK(cudaMalloc(&c->etab_d, sizeof(double) * c->etab_h->size()));
-  CK(cudaMemcpyAsync(c->etab_d, c->etab_h->data(), sizeof(double) * c->etab_h->size(), cudaMemcpyHostToDevice, c->st));
-  c->ff.etab = c->etab_d;
-  c->fd.etab = c->etab_d;
+  {
+    mth_status s = upload_class_table(c, *c->etab_h);
+    if (s != MTH_OK) return s;
+  }
   if ((size_t)n_drx > c->drx_cap) {
     cudaFree(c->drx_rot_d);
     cudaFree(c->drx_class_d);

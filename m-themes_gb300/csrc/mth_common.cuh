@@ -92,6 +92,18 @@ struct PhaseConst {
   double hard[NSYS][NSYS];
   double tau0f, tau1, thet0, thet1;
   int nrs_int;       // >0 when nrs is an integer: exponent fast path
+  // float copies for the FP32 flow rule (filled by fill_float_consts)
+  float nrsf, gamd0f, tau_offf;
+  float m_xtf[NSYS][5];
 };
+
+// Constant of precision T from its double and float copies: the FP32 paths
+// read float constants instead of converting doubles on the FP64 pipe.
+template <typename T>
+__host__ __device__ __forceinline__ T cpick(double d, float f);
+template <>
+__host__ __device__ __forceinline__ float cpick<float>(double, float f) { return f; }
+template <>
+__host__ __device__ __forceinline__ double cpick<double>(double d, float) { return d; }
 
 }  // namespace mth

@@ -40,7 +40,13 @@ struct NewtonConst {
   double tol;
   int itmax;
   int flow_off;         // 1: Schmid tensors zero (Update_Flag=0 at istep 0)
+  // float copies (fill_float_consts)
+  float s0devf[25];
+  float s0hhf, dtf, tolf;
 };
+
+// Fill the float copies of the double constants of nc and its phases.
+void fill_float_consts(NewtonConst& nc);
 
 bool make_plan(int n, FftPlan* p);
 
@@ -70,6 +76,7 @@ struct Fields {
   const uint8_t* phase;  // 0-based phase index
   const int* eclass;     // elastic class of the voxel (row of etab)
   const double* etab;    // ETAB_W doubles per class
+  const float* etabf;    // float copy of etab
   long long nv;
 };
 

@@ -45,6 +45,14 @@ __device__ __forceinline__ T pow_abs(T a, int ei, T ef) {
   return a > (T)0 ? (T)pow(a, ef) : (T)0;
 }
 
+// class-table row pointer of precision T
+template <typename T>
+__device__ __forceinline__ const T* cpick_ptr(const double* d, const float* f);
+template <>
+__device__ __forceinline__ const float* cpick_ptr<float>(const double*, const float* f) { return f; }
+template <>
+__device__ __forceinline__ const double* cpick_ptr<double>(const double* d, const float*) { return d; }
+
 // Flow rule in crystal axes at deviatoric stress x (5).  Returns edot (5),
 // optional Hessian contribution D (15, packed upper triangle) and psi.
 // gam (optional) receives the shear rates.
@@ -59,8 +67,8 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
   }
   psi = 0;
   const int ns = ph.nsys;
-  const TF n = (TF)ph.nrs;
-  const TF g0 = (TF)ph.gamd0;
+  const TF n = cpick<TF>(ph.nrs, ph.nrsf);
+  const TF g0 = cpick<TF>(ph.gamd0, ph.gamd0f);
   const TF inv_np1 = (TF)1 / (n + (TF)1);
   const int nm1 = ph.nrs_int > 0 ? ph.nrs_int - 1 : 0;
   // fully unrolled over the NSYS slots so the per-voxel CRSS stay in registers
@@ -69,7 +77,7 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
     if (s < ns) {
       TF m[5];
 #pragma unroll
-      for (int i = 0; i < 5; i++) m[i] = (TF)ph.m_xt[s][i];
+      for (int i = 0; i < 5; i++) m[i] = cpick<TF>(ph.m_xt[s][i], ph.m_xtf[s][i]);
       const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
       const TF tau = rss < (TF)0 ? tauf[s] + tau_off : tauf[s];
       const TF itau = (TF)1 / tau;
@@ -160,6 +168,20 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
   return true;
 }
 
+// LDL^T solve of a TF system in precision TL.
+template <typename TF, typename TL>
+__device__ __forceinline__ bool ldl_solve5_wide(const TF* H, const TF* b, TF* x) {
+  TL Hl[15], bl[5], pl[5];
+#pragma unroll
+  for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
+#pragma unroll
+  for (int i = 0; i < 5; i++) bl[i] = (TL)b[i];
+  const bool ok = ldl_solve5<TL>(Hl, bl, pl);
+#pragma unroll
+  for (int i = 0; i < 5; i++) x[i] = (TF)pl[i];
+  return ok;
+}
+
 // Result of one voxel solve.
 struct VoxelOut {
   double conv_s, conv_e;
@@ -181,18 +203,18 @@ struct VoxelOut {
 // FP32 factorisation (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
 // mode: all float.
 template <typename TF, typename TL>
-__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const double* __restrict__ et,
+__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const TF* __restrict__ et,
                                 const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* tauf, TF* sig6,
                                 TF* ed6) {
   VoxelOut o = {0.0, 0.0, 0, 0};
-  const TF dt = (TF)nc.dt;
+  const TF dt = cpick<TF>(nc.dt, nc.dtf);
   // crystal-frame inputs
   TF lamx[5], epsx[5], epx[5], s0s[5], c[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) {
     TF a = 0;
 #pragma unroll
-    for (int j = 0; j < 5; j++) a += (TF)nc.s0dev[i * 5 + j] * lam6[j];
+    for (int j = 0; j < 5; j++) a += cpick<TF>(nc.s0dev[i * 5 + j], nc.s0devf[i * 5 + j]) * lam6[j];
     s0s[i] = a;   // S0 lambda, sample axes
   }
 #pragma unroll
@@ -215,7 +237,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
     for (int i = 0; i < 5; i++)
 #pragma unroll
-      for (int j = 0; j < 5; j++) St[i * 5 + j] = (TF)et[ET_STOT + pk(i, j)];
+      for (int j = 0; j < 5; j++) St[i * 5 + j] = et[ET_STOT + pk(i, j)];
 #pragma unroll
     for (int i = 0; i < 5; i++)
 #pragma unroll
@@ -236,19 +258,19 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       }
   }
   // hydrostatic part in closed form
-  const TF s0hh = (TF)nc.s0hh, shh = (TF)et[ET_SEL_HH];
+  const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf), shh = et[ET_SEL_HH];
   const TF h = (s0hh * lam6[5] + eps6[5] - ep6[5]) / (s0hh + shh);
   TF ref2 = 0;
 #pragma unroll
   for (int i = 0; i < 6; i++) ref2 += lam6[i] * lam6[i];
   const TF dh = h - lam6[5];
-  const TF tol2 = (TF)nc.tol * (TF)nc.tol;
+  const TF tol2 = cpick<TF>(nc.tol, nc.tolf) * cpick<TF>(nc.tol, nc.tolf);
   const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
 
   TF x[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) x[i] = lamx[i];
-  const TF tau_off = (TF)ph.tau_back_minus_fwd;
+  const TF tau_off = cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf);
   int it = 0;
   bool done = false;
   bool near_root = false;   // previous step within 1e-3 |lambda|
@@ -279,14 +301,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       if (sizeof(TL) > sizeof(TF) && near_root) {
         // FP64 Jacobian solve of the FP32-assembled system for the steps
         // that set the converged answer
-        TL Hl[15], bl[5], pl[5];
-#pragma unroll
-        for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
-#pragma unroll
-        for (int i = 0; i < 5; i++) bl[i] = (TL)mg[i];
-        ok = ldl_solve5<TL>(Hl, bl, pl);
-#pragma unroll
-        for (int i = 0; i < 5; i++) p[i] = (TF)pl[i];
+        ok = ldl_solve5_wide<TF, TL>(H, mg, p);
       } else {
         ok = ldl_solve5<TF>(H, mg, p);
       }
@@ -364,7 +379,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
     cs += ds * ds;
     TF de = ep6[i] + dt * es[i] - eps6[i];
 #pragma unroll
-    for (int j = 0; j < 5; j++) de += (TF)et[ET_SEL + pk(i, j)] * ss[j];
+    for (int j = 0; j < 5; j++) de += et[ET_SEL + pk(i, j)] * ss[j];
     ce += de * de;
   }
   {
@@ -404,14 +419,47 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[W], double* out) 
   }
 }
 
+// Block sum of W per-thread values for 256-thread blocks, in FP64 in a fixed
+// order: the values are staged in shared memory (in their own precision);
+// 16 threads per component each sum 16 of them (stride 16), one thread per
+// component sums the 16 partials.  The row stride 256 + 16 keeps the
+// two components read by one warp on opposite bank halves.
+template <typename TV, int W>
+__device__ __forceinline__ void block_reduce_smem(const TV (&v)[W], double* out) {
+  constexpr int NT = 256, LD = NT + 16;
+  static_assert(W <= 16, "at most 16 components");
+  __shared__ TV sv[W][LD];
+  __shared__ double sp[W][16];
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < W; i++) sv[i][t] = v[i];
+  __syncthreads();
+  {
+    const int comp = t >> 4, chunk = t & 15;
+    if (comp < W) {
+      double a = 0.0;
+#pragma unroll
+      for (int k = 0; k < NT / 16; k++) a += (double)sv[comp][k * 16 + chunk];
+      sp[comp][chunk] = a;
+    }
+  }
+  __syncthreads();
+  if (t < W) {
+    double a = 0.0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) a += sp[t][k];
+    out[(size_t)blockIdx.x * W + t] = a;
+  }
+}
+
 // ------------------------------------------------------------ Newton kernel
 template <typename TSt, typename TF, typename TS, int MINB>
 __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
-  double acc[NPART];
+  TF acc[NPART];
 #pragma unroll
-  for (int i = 0; i < NPART; i++) acc[i] = 0.0;
+  for (int i = 0; i < NPART; i++) acc[i] = (TF)0;
   if (v < P) {
     const int jph = f.phase[v];
     const PhaseConst& ph = nc.ph[jph];
@@ -429,22 +477,22 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
       for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
       rot_to_q<TF>(R, Q);
       TF s6[6], e6[6];
-      const double* et = f.etab + (size_t)f.eclass[v] * ETAB_W;
+      const TF* et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
       VoxelOut o = solve_voxel<TF, TS>(nc, ph, Q, et, lam6, eps6, ep6, tauf, s6, e6);
 #pragma unroll
       for (int i = 0; i < 6; i++) {
         f.sig[i * P + v] = (TSt)s6[i];
         f.edot[i * P + v] = (TSt)e6[i];
       }
-      acc[0] = o.conv_s;
-      acc[1] = o.conv_e;
+      acc[0] = (TF)o.conv_s;   // exact: computed in TF
+      acc[1] = (TF)o.conv_e;
 #pragma unroll
       for (int i = 0; i < 6; i++) {
-        acc[2 + i] = (double)s6[i];
-        acc[8 + i] = jph == 0 ? (double)s6[i] : 0.0;
+        acc[2 + i] = s6[i];
+        acc[8 + i] = jph == 0 ? s6[i] : (TF)0;
       }
-      acc[14] = (double)o.iters;
-      acc[15] = (double)o.failed;
+      acc[14] = (TF)o.iters;    // small integers: exact in float
+      acc[15] = (TF)o.failed;
     } else {
 #pragma unroll
       for (int i = 0; i < 6; i++) {
@@ -453,11 +501,28 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
       }
     }
   }
-  block_reduce_store<NPART>(acc, partials);
+  block_reduce_smem<TF, NPART>(acc, partials);
 }
 
-cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
+void fill_float_consts(NewtonConst& nc) {
+  for (int k = 0; k < 2; k++) {
+    PhaseConst& ph = nc.ph[k];
+    ph.nrsf = (float)ph.nrs;
+    ph.gamd0f = (float)ph.gamd0;
+    ph.tau_offf = (float)ph.tau_back_minus_fwd;
+    for (int s = 0; s < NSYS; s++)
+      for (int i = 0; i < 5; i++) ph.m_xtf[s][i] = (float)ph.m_xt[s][i];
+  }
+  for (int i = 0; i < 25; i++) nc.s0devf[i] = (float)nc.s0dev[i];
+  nc.s0hhf = (float)nc.s0hh;
+  nc.dtf = (float)nc.dt;
+  nc.tolf = (float)nc.tol;
+}
+
+cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* fields, double* partials, int nblocks,
                           cudaStream_t st) {
+  NewtonConst nc = nc_in;
+  fill_float_consts(nc);
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     newton_kernel<float, float, float, 2><<<nblocks, 256, 0, st>>>(nc, f, partials);
@@ -589,8 +654,10 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
   block_reduce_store<NPART_END>(acc, partials);
 }
 
-cudaError_t launch_end_step(int mixed, const NewtonConst& nc, const void* fields, const double au[3], int do_orient,
+cudaError_t launch_end_step(int mixed, const NewtonConst& nc_in, const void* fields, const double au[3], int do_orient,
                             int do_harden, double* partials, int nblocks, cudaStream_t st) {
+  NewtonConst nc = nc_in;
+  fill_float_consts(nc);
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     end_step_kernel<float, double><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);
