@@ -260,6 +260,9 @@ struct mth_ctx {
   Fields<double> fd;
   void* spec;
   void* anti;
+  TmaMaps* tma;       // tensor maps of the TMA passes (null members: shared-memory passes)
+  int* err_d;         // raised by a timed-out wait in a kernel
+  int* err_h;         // pinned copy
   uint8_t* phase_d;
   int* grain_d;
   int* eclass_d;
@@ -316,6 +319,9 @@ static void ctx_free(mth_ctx* c) {
   cudaFree(c->fieldmem);
   cudaFree(c->spec);
   cudaFree(c->anti);
+  tma_destroy(c->tma);
+  cudaFree(c->err_d);
+  if (c->err_h) cudaFreeHost(c->err_h);
   cudaFree(c->phase_d);
   cudaFree(c->grain_d);
   cudaFree(c->eclass_d);
@@ -487,8 +493,9 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   FftGeom& g = c->geom;
   g.n0 = c->n[0]; g.n1 = c->n[1]; g.n2 = c->n[2];
   g.kz = g.n2 / 2 + 1;
+  g.kzs = (g.kz + 1) & ~1;
   g.plane = c->nv;
-  g.kplane = (long long)g.n0 * g.n1 * g.kz;
+  g.kplane = (long long)g.n0 * g.n1 * g.kzs;
   make_plan(g.n0, &g.px);
   make_plan(g.n1, &g.py);
   make_plan(g.n2, &g.pz);
@@ -523,12 +530,19 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   CKC(cudaMalloc(&c->fieldmem, esz * P * nplanes));
   CKC(cudaMalloc(&c->spec, 2 * esz * g.kplane * 6));
   CKC(cudaMalloc(&c->anti, 2 * esz * g.kplane * 3));
+  // the padding column of the half spectra stays zero
+  CKC(cudaMemset(c->spec, 0, 2 * esz * g.kplane * 6));
+  CKC(cudaMemset(c->anti, 0, 2 * esz * g.kplane * 3));
   CKC(cudaMalloc(&c->phase_d, P));
   CKC(cudaMalloc(&c->grain_d, sizeof(int) * P));
   CKC(cudaMalloc(&c->eclass_d, sizeof(int) * P));
   CKC(cudaMalloc(&c->partials, sizeof(double) * 21 * c->nblocks));
   CKC(cudaMalloc(&c->red, sizeof(double) * 32));
   CKC(cudaMallocHost(&c->red_h, sizeof(double) * 32));
+  CKC(cudaMalloc(&c->err_d, sizeof(int)));
+  CKC(cudaMemset(c->err_d, 0, sizeof(int)));
+  CKC(cudaMallocHost(&c->err_h, sizeof(int)));
+  *c->err_h = 0;
   auto carve = [&](auto* base, auto& f) {
     long long o = 0;
     f.sig = base + o; o += 6 * P;
@@ -547,6 +561,10 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   };
   if (c->mixed) carve(static_cast<float*>(c->fieldmem), c->ff);
   else carve(static_cast<double*>(c->fieldmem), c->fd);
+  c->tma = c->mixed ? tma_create<float>(g, c->ff.sig, c->ff.strain, c->ff.wspin, static_cast<c2<float>*>(c->spec),
+                                        static_cast<c2<float>*>(c->anti))
+                    : tma_create<double>(g, c->fd.sig, c->fd.strain, c->fd.wspin, static_cast<c2<double>*>(c->spec),
+                                         static_cast<c2<double>*>(c->anti));
   CKC(cudaMalloc(&c->crystal_d, P));
   c->etab_h = new std::vector<double>();
   c->drx_rot_h = new std::vector<double>();
@@ -603,8 +621,10 @@ extern "C" mth_status mth_destroy(mth_ctx* c) {
 static mth_status reduce_to_host(mth_ctx* c, int width, double* out) {
   LAUNCH(K_REDUCE, 8.0 * width * (c->nblocks + 1), launch_reduce_partials(c->partials, c->nblocks, width, c->red, c->st));
   CK(cudaMemcpyAsync(c->red_h, c->red, sizeof(double) * width, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->err_h, c->err_d, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   prof_resolve(c);
+  if (*c->err_h) return set_err(MTH_ERR_TIMEOUT, "a kernel timed out waiting for its tile copies");
   memcpy(out, c->red_h, sizeof(double) * width);
   return MTH_OK;
 }
@@ -784,13 +804,24 @@ static mth_status green_iteration(mth_ctx* c, const AddVec& add) {
   c2<T>* anti = static_cast<c2<T>*>(c->anti);
   auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
   // algorithmic bytes: real plane = w*nv, complex spectrum plane = 2w*kplane
-  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.kplane;
-  LAUNCH(K_FFT_Z_R2C, 6 * rp + 6 * kp, launch_fft_z_r2c<T>(g, f.sig, spec, 6, tw(2, 0), c->st));
-  LAUNCH(K_FFT_Y, 12 * kp, launch_fft_strided<T>(g, spec, 6, 1, -1, tw(1, 0), c->st));
-  LAUNCH(K_FFT_X_GREEN, 12 * kp + 6 * kp, launch_fft_x_green<T>(g, c->gc, spec, anti, tw(0, 0), tw(0, 1), c->st));
-  LAUNCH(K_FFT_Y, 12 * kp, launch_fft_strided<T>(g, spec, 6, 1, +1, tw(1, 1), c->st));
+  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.n0 * g.n1 * g.kz;
+  const bool tz = tma_has(c->tma, 0), ts = tma_has(c->tma, 1), tg = tma_has(c->tma, 2);
+  const T scale = (T)(1.0 / (double)c->nv);
+  LAUNCH(K_FFT_Z_R2C, 6 * rp + 6 * kp,
+         tz ? tma_fft_z_r2c<T>(c->tma, g, tw(2, 0), c->err_d, c->st)
+            : launch_fft_z_r2c<T>(g, f.sig, spec, 6, tw(2, 0), c->st));
+  LAUNCH(K_FFT_Y, 12 * kp,
+         ts ? tma_fft_strided<T>(c->tma, g, 0, -1, tw(1, 0), c->err_d, c->st)
+            : launch_fft_strided<T>(g, spec, 6, 1, -1, tw(1, 0), c->st));
+  LAUNCH(K_FFT_X_GREEN, 12 * kp + 6 * kp,
+         tg ? tma_fft_x_green<T>(c->tma, g, c->gc, tw(0, 0), tw(0, 1), c->err_d, c->st)
+            : launch_fft_x_green<T>(g, c->gc, spec, anti, tw(0, 0), tw(0, 1), c->st));
+  LAUNCH(K_FFT_Y, 12 * kp,
+         ts ? tma_fft_strided<T>(c->tma, g, 0, +1, tw(1, 1), c->err_d, c->st)
+            : launch_fft_strided<T>(g, spec, 6, 1, +1, tw(1, 1), c->st));
   LAUNCH(K_FFT_Z_C2R, 6 * kp + 12 * rp,
-         launch_fft_z_c2r<T>(g, spec, f.strain, 6, tw(2, 1), (T)(1.0 / (double)c->nv), add, 1, c->st));
+         tz ? tma_fft_z_c2r<T>(c->tma, g, 0, tw(2, 1), scale, add, c->err_d, c->st)
+            : launch_fft_z_c2r<T>(g, spec, f.strain, 6, tw(2, 1), scale, add, 1, c->st));
   // Newton: read sigma, strain, eps_p (18), rot (9), CRSS (12); write sigma, edot (12);
   // phase (1 B) and elastic class (4 B) per voxel
   LAUNCH(K_NEWTON, (18 + 9 + 12 + 12) * rp + 5.0 * (double)c->nv,
@@ -806,10 +837,18 @@ static mth_status spin_field(mth_ctx* c) {
   auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
   AddVec zero;
   memset(&zero, 0, sizeof(zero));
-  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.kplane;
-  LAUNCH(K_SPIN, 6 * kp, launch_fft_strided<T>(g, anti, 3, 0, +1, tw(0, 1), c->st));
-  LAUNCH(K_SPIN, 6 * kp, launch_fft_strided<T>(g, anti, 3, 1, +1, tw(1, 1), c->st));
-  LAUNCH(K_SPIN, 3 * kp + 3 * rp, launch_fft_z_c2r<T>(g, anti, f.wspin, 3, tw(2, 1), (T)(1.0 / (double)c->nv), zero, 0, c->st));
+  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.n0 * g.n1 * g.kz;
+  const bool tz = tma_has(c->tma, 0), ts = tma_has(c->tma, 1);
+  const T scale = (T)(1.0 / (double)c->nv);
+  LAUNCH(K_SPIN, 6 * kp,
+         ts ? tma_fft_strided<T>(c->tma, g, 2, +1, tw(0, 1), c->err_d, c->st)
+            : launch_fft_strided<T>(g, anti, 3, 0, +1, tw(0, 1), c->st));
+  LAUNCH(K_SPIN, 6 * kp,
+         ts ? tma_fft_strided<T>(c->tma, g, 1, +1, tw(1, 1), c->err_d, c->st)
+            : launch_fft_strided<T>(g, anti, 3, 1, +1, tw(1, 1), c->st));
+  LAUNCH(K_SPIN, 3 * kp + 3 * rp,
+         tz ? tma_fft_z_c2r<T>(c->tma, g, 1, tw(2, 1), scale, zero, c->err_d, c->st)
+            : launch_fft_z_c2r<T>(g, anti, f.wspin, 3, tw(2, 1), scale, zero, 0, c->st));
   return MTH_OK;
 }
 

@@ -15,6 +15,8 @@
 #include <cstdio>
 #include "mth_common.cuh"
 #include "mth_internal.h"
+#include "green_op.cuh"
+#include "fft_core.cuh"
 
 namespace mth {
 
@@ -86,49 +88,6 @@ __device__ void load_twiddles(c2<T>* s, const c2<T>* g, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
 }
 
-// Compile-time variant for the line lengths the workloads use: the radix
-// plan (4s, then 2s, then 3s, as make_plan) and every index computation fold
-// into constants.
-__host__ __device__ constexpr int ct_nst(int n) {
-  int s = 0;
-  while (n % 4 == 0) { n /= 4; s++; }
-  while (n % 2 == 0) { n /= 2; s++; }
-  while (n % 3 == 0) { n /= 3; s++; }
-  return s;
-}
-__host__ __device__ constexpr int ct_radix(int n, int idx) {
-  int s = 0;
-  while (n % 4 == 0) { if (s == idx) return 4; n /= 4; s++; }
-  while (n % 2 == 0) { if (s == idx) return 2; n /= 2; s++; }
-  while (n % 3 == 0) { if (s == idx) return 3; n /= 3; s++; }
-  return 1;
-}
-
-template <typename T, int R>
-__device__ __forceinline__ void butterfly(c2<T> v[4], int sign) {
-  if constexpr (R == 2) {
-    c2<T> a = v[0], b = v[1];
-    v[0] = cadd<T>(a, b);
-    v[1] = csub<T>(a, b);
-  } else if constexpr (R == 4) {
-    c2<T> s02 = cadd<T>(v[0], v[2]), d02 = csub<T>(v[0], v[2]);
-    c2<T> s13 = cadd<T>(v[1], v[3]), d13 = csub<T>(v[1], v[3]);
-    c2<T> wd = mk<T>(-(T)sign * d13.y, (T)sign * d13.x);
-    v[0] = cadd<T>(s02, s13);
-    v[2] = csub<T>(s02, s13);
-    v[1] = cadd<T>(d02, wd);
-    v[3] = csub<T>(d02, wd);
-  } else {
-    const T h = (T)0.86602540378443864676 * (T)sign;
-    c2<T> t = cadd<T>(v[1], v[2]), u = csub<T>(v[1], v[2]);
-    c2<T> m = mk<T>(v[0].x - (T)0.5 * t.x, v[0].y - (T)0.5 * t.y);
-    c2<T> iu = mk<T>(-h * u.y, h * u.x);
-    v[0] = cadd<T>(v[0], t);
-    v[1] = cadd<T>(m, iu);
-    v[2] = csub<T>(m, iu);
-  }
-}
-
 template <typename T, int N, int S = 0, int NS = 1>
 __device__ __forceinline__ c2<T>* smem_fft_ct(c2<T>* d0, c2<T>* d1, int ls, int nl, const c2<T>* tw, int sign) {
   if constexpr (S < ct_nst(N)) {
@@ -173,7 +132,7 @@ __device__ __forceinline__ c2<T>* do_fft(c2<T>* d0, c2<T>* d1, int n, int ls, in
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in, c2<T>* __restrict__ out, int ncomp,
                                                         long long plane, long long kplane, int nlines, int n2_,
-                                                        int lb, FftPlan pl, const c2<T>* __restrict__ twg) {
+                                                        int kzs, int lb, FftPlan pl, const c2<T>* __restrict__ twg) {
   const int n2 = NC > 0 ? NC : n2_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
@@ -209,7 +168,7 @@ __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in
     // A = (X[k] + conj(X[-k]))/2 ; B = -i (X[k] - conj(X[-k]))/2
     c2<T> A = mk<T>((T)0.5 * (xk.x + xm.x), (T)0.5 * (xk.y - xm.y));
     c2<T> B = mk<T>((T)0.5 * (xk.y + xm.y), (T)-0.5 * (xk.x - xm.x));
-    const long long o = (long long)(line0 + l) * kz + k;
+    const long long o = (long long)(line0 + l) * kzs + k;
     out[(2 * p) * kplane + o] = A;
     if (2 * p + 1 < ncomp) out[(2 * p + 1) * kplane + o] = B;
   }
@@ -219,7 +178,7 @@ __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict__ spec, T* __restrict__ field, int ncomp,
                                                         long long plane, long long kplane, int nlines, int n2_,
-                                                        int lb, FftPlan pl, const c2<T>* __restrict__ twg, T scale,
+                                                        int kzs, int lb, FftPlan pl, const c2<T>* __restrict__ twg, T scale,
                                                         AddVec add, int mode) {
   const int n2 = NC > 0 ? NC : n2_;
   extern __shared__ unsigned char smraw[];
@@ -238,7 +197,7 @@ __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict_
     const int p = idx / (kz * lb);
     c2<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
     if (l < nl_here) {
-      const long long o = (long long)(line0 + l) * kz + k;
+      const long long o = (long long)(line0 + l) * kzs + k;
       A = spec[(2 * p) * kplane + o];
       if (2 * p + 1 < ncomp) B = spec[(2 * p + 1) * kplane + o];
     }
@@ -302,142 +261,13 @@ __global__ void __launch_bounds__(256) fft_strided_kernel(c2<T>* __restrict__ sp
   }
 }
 
-// ------------------------------------------------------- Green operator
-// Frequency of index idx on an axis of n points: idx/n - round(idx/n) of
-// src/init.c:778-786 (the Nyquist index maps to -1/2), from integers.
-template <typename T> __device__ __forceinline__ T freq(int idx, int n) {
-  const int k = (2 * idx >= n) ? idx - n : idx;
-  return (T)k / (T)n;
-}
-template <typename T> __device__ __forceinline__ T c0_at(const GreenConst& gc, int i);
-template <> __device__ __forceinline__ float c0_at<float>(const GreenConst& gc, int i) { return gc.c0f[i]; }
-template <> __device__ __forceinline__ double c0_at<double>(const GreenConst& gc, int i) { return gc.c0[i]; }
-template <typename T> __device__ __forceinline__ T s066_at(const GreenConst& gc, int i);
-template <> __device__ __forceinline__ float s066_at<float>(const GreenConst& gc, int i) { return gc.s066f[i]; }
-template <> __device__ __forceinline__ double s066_at<double>(const GreenConst& gc, int i) { return gc.s066[i]; }
-
-// Delta = -Omega(n) (sig n) (x) n for one n; accumulates into dsym (LT, 6
-// complex) and danti (3 complex: [2][1], [0][2], [1][0]) with weight wgt.
-template <typename T>
-__device__ __forceinline__ void green_apply_n(const GreenConst& gc, const T n[3], const c2<T> s[3][3], T wgt, c2<T> dsym[6],
-                                              c2<T> danti[3]) {
-  T A[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int k = i; k < 3; k++) {
-      T a = 0;
-#pragma unroll
-      for (int j = 0; j < 3; j++)
-#pragma unroll
-        for (int l = 0; l < 3; l++) a += c0_at<T>(gc, ((i * 3 + j) * 3 + k) * 3 + l) * n[j] * n[l];
-      A[i][k] = a;
-      A[k][i] = a;
-    }
-  T det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
-          A[0][2] * (A[1][0] * A[2][1] - A[2][0] * A[1][1]);
-  T id = (T)1 / det;
-  T O[3][3];
-  O[0][0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) * id;
-  O[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id;
-  O[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
-  O[1][0] = O[0][1];
-  O[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id;
-  O[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
-  O[2][0] = O[0][2];
-  O[2][1] = O[1][2];
-  O[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
-  c2<T> t[3], v[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    t[k] = mk<T>(s[k][0].x * n[0] + s[k][1].x * n[1] + s[k][2].x * n[2],
-                 s[k][0].y * n[0] + s[k][1].y * n[1] + s[k][2].y * n[2]);
-  }
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-    v[i] = mk<T>(-(O[i][0] * t[0].x + O[i][1] * t[1].x + O[i][2] * t[2].x) * wgt,
-                 -(O[i][0] * t[0].y + O[i][1] * t[1].y + O[i][2] * t[2].y) * wgt);
-  // Delta_ij = v_i n_j
-  T r2 = (T)RSQ2, r3 = (T)RSQ3, r6 = (T)RSQ6;
-  c2<T> d00 = cscale<T>(v[0], n[0]), d11 = cscale<T>(v[1], n[1]), d22 = cscale<T>(v[2], n[2]);
-  c2<T> d12 = cscale<T>(v[1], n[2]), d21 = cscale<T>(v[2], n[1]);
-  c2<T> d02 = cscale<T>(v[0], n[2]), d20 = cscale<T>(v[2], n[0]);
-  c2<T> d01 = cscale<T>(v[0], n[1]), d10 = cscale<T>(v[1], n[0]);
-  dsym[0] = cadd<T>(dsym[0], cscale<T>(csub<T>(d11, d00), r2));
-  dsym[1] = cadd<T>(dsym[1], cscale<T>(csub<T>(cscale<T>(d22, (T)2), cadd<T>(d00, d11)), r6));
-  dsym[2] = cadd<T>(dsym[2], cscale<T>(cadd<T>(d12, d21), r2));
-  dsym[3] = cadd<T>(dsym[3], cscale<T>(cadd<T>(d02, d20), r2));
-  dsym[4] = cadd<T>(dsym[4], cscale<T>(cadd<T>(d01, d10), r2));
-  dsym[5] = cadd<T>(dsym[5], cscale<T>(cadd<T>(cadd<T>(d00, d11), d22), r3));
-  danti[0] = cadd<T>(danti[0], cscale<T>(csub<T>(d21, d12), (T)0.5));
-  danti[1] = cadd<T>(danti[1], cscale<T>(csub<T>(d02, d20), (T)0.5));
-  danti[2] = cadd<T>(danti[2], cscale<T>(csub<T>(d10, d01), (T)0.5));
-}
-
-// sig: LT components of sigma-hat at k (in), replaced by LT of sym(Delta);
-// anti: antisymmetric part of Delta.  When k has Nyquist components the
-// operator is the mean of Gamma at n(k) and n(-k): the reference keeps only
-// the real part of its complex inverse transform (src/evolution.c:1402),
-// which equals the transform of the Hermitian part of Delta-hat.
-template <typename T>
-__device__ __forceinline__ void green_point(const GreenConst& gc, int kx, int ky, int kz, int n0, int n1, int n2,
-                                            c2<T> sig[6], c2<T> anti[3]) {
-  c2<T> dsym[6], danti[3];
-#pragma unroll
-  for (int i = 0; i < 6; i++) dsym[i] = mk<T>(0, 0);
-#pragma unroll
-  for (int i = 0; i < 3; i++) danti[i] = mk<T>(0, 0);
-  if (kx == 0 && ky == 0 && kz == 0) {
-    if (gc.elast_bc == 0) {
-      for (int i = 0; i < 6; i++) {
-        T re = 0, im = 0;
-        for (int j = 0; j < 6; j++) {
-          re -= s066_at<T>(gc, i * 6 + j) * sig[j].x;
-          im -= s066_at<T>(gc, i * 6 + j) * sig[j].y;
-        }
-        dsym[i] = mk<T>(re, im);
-      }
-    }
-  } else {
-    c2<T> s[3][3];
-    {
-      T re[6], im[6], tr[3][3], ti[3][3];
-#pragma unroll
-      for (int i = 0; i < 6; i++) { re[i] = sig[i].x; im[i] = sig[i].y; }
-      lt_to_cart<T>(re, tr);
-      lt_to_cart<T>(im, ti);
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) s[i][j] = mk<T>(tr[i][j], ti[i][j]);
-    }
-    T f[3] = {freq<T>(kx, n0), freq<T>(ky, n1), freq<T>(kz, n2)};
-    const bool q0 = (2 * kx == n0), q1 = (2 * ky == n1), q2 = (2 * kz == n2);
-    T nrm = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-    T n[3] = {f[0] / nrm, f[1] / nrm, f[2] / nrm};
-    const bool anyq = q0 || q1 || q2;
-    const bool anyv = (!q0 && kx != 0) || (!q1 && ky != 0) || (!q2 && kz != 0);
-    if (anyq && anyv) {
-      green_apply_n<T>(gc, n, s, (T)0.5, dsym, danti);
-      T m[3] = {q0 ? n[0] : -n[0], q1 ? n[1] : -n[1], q2 ? n[2] : -n[2]};
-      green_apply_n<T>(gc, m, s, (T)0.5, dsym, danti);
-    } else {
-      green_apply_n<T>(gc, n, s, (T)1, dsym, danti);
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 6; i++) sig[i] = dsym[i];
-#pragma unroll
-  for (int i = 0; i < 3; i++) anti[i] = danti[i];
-}
-
 // x pass fused with Gamma0: forward transform along x of the 6 stress
 // spectra, Delta = Gamma0 : sigma-hat per k, antisymmetric part added to
 // the spin accumulator, inverse transform along x.  One block: fixed y,
 // kb consecutive kz.
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c2<T>* __restrict__ spec, c2<T>* __restrict__ anti_acc,
-                                                          long long kplane, int n0_, int n1, int n2, int kzn, int kb,
+                                                          long long kplane, int n0_, int n1, int n2, int kzn, int kzs, int kb,
                                                           FftPlan pl, const c2<T>* __restrict__ twf,
                                                           const c2<T>* __restrict__ twi) {
   const int n0 = NC > 0 ? NC : n0_;
@@ -450,8 +280,8 @@ __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c
   c2<T>* d1 = d0 + nl * ls;
   const int k0 = blockIdx.x * kb;
   const int y = blockIdx.y;
-  const long long S = (long long)n1 * kzn;
-  const long long base = (long long)y * kzn + k0;
+  const long long S = (long long)n1 * kzs;
+  const long long base = (long long)y * kzs + k0;
   load_twiddles<T>(tw_f, twf, n0);
   load_twiddles<T>(tw_i, twi, n0);
   for (int idx = threadIdx.x; idx < 6 * n0 * kb; idx += blockDim.x) {
@@ -518,7 +348,7 @@ cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncom
     default: break;
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(in, out, ncomp, g.plane, g.kplane, nlines, g.n2, lb, g.pz, tw);
+  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(in, out, ncomp, g.plane, g.kplane, nlines, g.n2, g.kzs, lb, g.pz, tw);
   return cudaGetLastError();
 }
 
@@ -537,8 +367,8 @@ cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int 
     default: break;
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(spec, field, ncomp, g.plane, g.kplane, nlines, g.n2, lb, g.pz, tw,
-                                             scale, add, mode);
+  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(spec, field, ncomp, g.plane, g.kplane, nlines, g.n2, g.kzs, lb, g.pz,
+                                             tw, scale, add, mode);
   return cudaGetLastError();
 }
 
@@ -556,8 +386,8 @@ template <typename T>
 cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axis, int sign, const c2<T>* tw,
                                cudaStream_t st) {
   const int L = axis == 1 ? g.n1 : g.n0;
-  const long long S = axis == 1 ? g.kz : (long long)g.n1 * g.kz;
-  const long long ostride = axis == 1 ? (long long)g.n1 * g.kz : g.kz;
+  const long long S = axis == 1 ? g.kzs : (long long)g.n1 * g.kzs;
+  const long long ostride = axis == 1 ? (long long)g.n1 * g.kzs : g.kzs;
   const int nouter = axis == 1 ? g.n0 : g.n1;
   const FftPlan& pl = axis == 1 ? g.py : g.px;
   const int kb = pick_kb<T>(L, ncomp, g.smem_budget, 1);
@@ -589,7 +419,7 @@ cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* sp
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kz + kb - 1) / kb, g.n1);
-  k<<<grid, 256, sm, st>>>(gc, spec, anti, g.kplane, g.n0, g.n1, g.n2, g.kz, kb, g.px, twf, twi);
+  k<<<grid, 256, sm, st>>>(gc, spec, anti, g.kplane, g.n0, g.n1, g.n2, g.kz, g.kzs, kb, g.px, twf, twi);
   return cudaGetLastError();
 }
 

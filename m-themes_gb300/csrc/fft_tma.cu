@@ -1,0 +1,578 @@
+// fft_tma.cu -- TMA-staged FFT passes of one Green iteration for the line
+// lengths with compile-time plans (16, 32, 48, 64, 96, 128, 256).
+//
+// Same passes and results as fft_green.cu (src/evolution.c:1361-1405), laid
+// out for GB300:
+//   * every tile moves between HBM and shared memory with the tensor memory
+//     accelerator (cp.async.bulk.tensor loads completing on an mbarrier,
+//     bulk-group stores), so a block has its whole tile in flight at once
+//     and no register round trip;
+//   * the 1-D transforms run in place: each Stockham stage reads its
+//     butterfly inputs into registers, synchronises, and writes the outputs
+//     back into the same tile, which halves the shared memory of a two-buffer
+//     Stockham and raises the number of resident blocks;
+//   * the y and x passes take one spectrum component per block (the Green
+//     pass needs all six at a wave vector and takes them together);
+//   * the z passes transform a real line of N points as an N/2-point complex
+//     line (even samples real, odd samples imaginary) plus the split step of
+//     the real FFT, so the tile read by TMA is the complex input as it lies.
+// Waits on the mbarrier are bounded (about one second); on time-out the
+// block raises the error flag the host reads after the iteration.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cstdio>
+#include <cstring>
+#include "mth_common.cuh"
+#include "mth_internal.h"
+#include "green_op.cuh"
+#include "fft_core.cuh"
+
+namespace mth {
+
+// ------------------------------------------------------------ TMA helpers
+namespace {
+
+constexpr unsigned long long WAIT_NS = 1000000000ULL;   // bounded mbarrier wait
+
+__device__ __forceinline__ uint32_t sh(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sh(b)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sh(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(sh(b)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (gtimer() - t0 > WAIT_NS) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* m, int x, int y, int z, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(sh(dst)),
+      "l"(reinterpret_cast<uint64_t>(m)), "r"(x), "r"(y), "r"(z), "r"(sh(b))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load4(void* dst, const CUtensorMap* m, int x, int y, int z, int w, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(sh(dst)),
+      "l"(reinterpret_cast<uint64_t>(m)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(sh(b))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store3(const CUtensorMap* m, const void* src, int x, int y, int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(m)),
+               "r"(sh(src)), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void tma_store4(const CUtensorMap* m, const void* src, int x, int y, int z, int w) {
+  asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(m)),
+               "r"(sh(src)), "r"(x), "r"(y), "r"(z), "r"(w)
+               : "memory");
+}
+__device__ __forceinline__ void tma_store_commit_wait() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// generic-proxy writes to shared memory visible to the following TMA store
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Thread 0 has issued the loads that complete on bar; all threads learn
+// whether they arrived.  On time-out the error flag is raised, the copies
+// still in flight get a second bounded wait, and false is returned.
+__device__ __forceinline__ bool block_wait_loads(uint64_t* bar, int* ok_s, int* err) {
+  if (threadIdx.x == 0) {
+    bool ok = mbar_wait(bar, 0);
+    if (!ok) {
+      atomicOr(err, 1);
+      mbar_wait(bar, 0);
+    }
+    *ok_s = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return *ok_s != 0;
+}
+
+// ---------------------------------------------------- in-place tile FFT
+// NG groups of QN lines of N points; element e of line (g, q) sits at
+// d[g*GS + q + e*ES].  Work item w: q = w % QN fastest, then the butterfly
+// index j, then the group, so a warp reads consecutive addresses.  Stage s
+// of radix R maps element j + r*N/R (times W^(k r), k = j mod Ns) to
+// (j/Ns)*Ns*R + k + r*Ns (Stockham autosort); inputs go through registers so
+// the stage is done in place.  Twiddles W_N^i = tw[i*TWM] (table of N*TWM
+// points, the sign of the transform).
+template <typename T, int N, int QN, int ES, int GS, int NG, int TWM, int SG, int NT, int S = 0, int NS = 1>
+__device__ __forceinline__ void tile_fft(c2<T>* d, const c2<T>* __restrict__ tw) {
+  if constexpr (S < ct_nst(N)) {
+    constexpr int R = ct_radix(N, S);
+    constexpr int NB = N / R;
+    constexpr int TWS = N / (NS * R);
+    constexpr int TOTAL = NG * NB * QN;
+    constexpr int IPT = (TOTAL + NT - 1) / NT;
+    c2<T> v[IPT][R];
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+      const int w = threadIdx.x + i * NT;
+      if (TOTAL % NT == 0 || w < TOTAL) {
+        const int q = w % QN, t = w / QN;
+        const int j = t % NB, g = t / NB;
+        const int k = j % NS;
+        const c2<T>* in = d + g * GS + q;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          c2<T> x = in[(j + r * NB) * ES];
+          if (r && NS > 1) x = cmul<T>(x, __ldg(&tw[k * r * TWS * TWM]));
+          v[i][r] = x;
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+      const int w = threadIdx.x + i * NT;
+      if (TOTAL % NT == 0 || w < TOTAL) {
+        const int q = w % QN, t = w / QN;
+        const int j = t % NB, g = t / NB;
+        const int k = j % NS;
+        butterfly<T, R>(v[i], SG);
+        c2<T>* out = d + g * GS + q;
+        const int idxD = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) out[(idxD + r * NS) * ES] = v[i][r];
+      }
+    }
+    __syncthreads();
+    tile_fft<T, N, QN, ES, GS, NG, TWM, SG, NT, S + 1, NS * R>(d, tw);
+  }
+}
+
+constexpr int NT = 256;   // threads per block of every TMA pass
+
+}  // namespace
+
+// Tile parameters, shared with the host launchers.
+template <typename T> __host__ __device__ constexpr int cw() { return (int)(sizeof(c2<T>) / 8); }   // 8-byte words per complex
+template <typename T> __host__ __device__ constexpr int kb_strided() { return sizeof(T) == 4 ? 8 : 4; }
+template <typename T> __host__ __device__ constexpr int kb_green() { return sizeof(T) == 4 ? 4 : 2; }
+template <typename T> __host__ __device__ constexpr int lb_z(int n) {
+  int lb = 2048 / (n / 2);
+  int p = 8;
+  while (p * 2 <= lb && p < 64) p *= 2;
+  if (sizeof(T) == 8 && p > 8) p /= 2;
+  return p;
+}
+
+// ------------------------------------------------------------- z passes
+// r2c: one block = LB consecutive (x,y) lines of one stress component.
+template <typename T, int N, int LB>
+__global__ void __launch_bounds__(NT) fft_zr_tma_kernel(const __grid_constant__ CUtensorMap mreal,
+                                                        const __grid_constant__ CUtensorMap mspec,
+                                                        const c2<T>* __restrict__ tw, int* err) {
+  constexpr int M = N / 2, KZ = M + 1, KZS = (KZ + 1) & ~1;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ uint64_t bar;
+  __shared__ int ok_s;
+  c2<T>* A = reinterpret_cast<c2<T>*>(smraw);        // LB x M complex = LB x N real
+  c2<T>* C = A + ((LB * M + 15) & ~15);              // LB x KZS output rows
+  const int line0 = blockIdx.x * LB, comp = blockIdx.y;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    mbar_expect(&bar, (uint32_t)(LB * N * sizeof(T)));
+    tma_load3(A, &mreal, 0, line0, comp, &bar);
+  }
+  if (!block_wait_loads(&bar, &ok_s, err)) return;
+  tile_fft<T, M, 1, 1, M, LB, 2, -1, NT>(A, tw);
+  // split step: X_k = (Z_k + conj Z_{M-k})/2 - i W_N^k (Z_k - conj Z_{M-k})/2
+  for (int idx = threadIdx.x; idx < LB * KZS; idx += NT) {
+    const int l = idx / KZS, k = idx - l * KZS;
+    c2<T> X = mk<T>(0, 0);
+    if (k < KZ) {
+      const c2<T> z = A[l * M + (k % M)], zm = A[l * M + ((M - k) % M)];
+      const c2<T> e = mk<T>((T)0.5 * (z.x + zm.x), (T)0.5 * (z.y - zm.y));   // (Z + conj Zm)/2
+      const c2<T> o = mk<T>((T)0.5 * (z.x - zm.x), (T)0.5 * (z.y + zm.y));   // (Z - conj Zm)/2
+      const c2<T> wo = cmul<T>(__ldg(&tw[k]), o);
+      X = mk<T>(e.x + wo.y, e.y - wo.x);   // e - i wo
+    }
+    C[l * KZS + k] = X;
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tma_store3(&mspec, C, 0, line0, comp);
+    tma_store_commit_wait();
+  }
+}
+
+// c2r fused with the strain update (MODE 1: field += Re(.)*scale + add[c];
+// MODE 0: field = Re(.)*scale + add[c]).  The imaginary parts of X_0 and
+// X_{N/2} are dropped, as the real part of the reference's complex inverse.
+template <typename T, int N, int LB, int MODE>
+__global__ void __launch_bounds__(NT) fft_zc_tma_kernel(const __grid_constant__ CUtensorMap mspec,
+                                                        const __grid_constant__ CUtensorMap mreal,
+                                                        const c2<T>* __restrict__ tw, T scale, AddVec add, int* err) {
+  constexpr int M = N / 2, KZS = (M + 2) & ~1;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ uint64_t bar;
+  __shared__ int ok_s;
+  c2<T>* S = reinterpret_cast<c2<T>*>(smraw);        // LB x KZS spectrum rows
+  c2<T>* A = S + ((LB * KZS + 15) & ~15);            // LB x M work
+  T* F = reinterpret_cast<T*>(A + ((LB * M + 15) & ~15));   // LB x N real field
+  const int line0 = blockIdx.x * LB, comp = blockIdx.y;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    mbar_expect(&bar, (uint32_t)(LB * KZS * sizeof(c2<T>) + (MODE ? LB * N * sizeof(T) : 0)));
+    tma_load3(S, &mspec, 0, line0, comp, &bar);
+    if (MODE) tma_load3(F, &mreal, 0, line0, comp, &bar);
+  }
+  if (!block_wait_loads(&bar, &ok_s, err)) return;
+  // merge step: Z_k = (X_k + conj X_{M-k}) + i W_N^-k (X_k - conj X_{M-k})
+  for (int idx = threadIdx.x; idx < LB * M; idx += NT) {
+    const int l = idx / M, k = idx - l * M;
+    c2<T> x = S[l * KZS + k], xm = S[l * KZS + (M - k)];
+    if (k == 0) { x.y = 0; xm.y = 0; }
+    const c2<T> e = mk<T>(x.x + xm.x, x.y - xm.y);
+    const c2<T> o = cmul<T>(__ldg(&tw[k]), mk<T>(x.x - xm.x, x.y + xm.y));
+    A[l * M + k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i o
+  }
+  __syncthreads();
+  tile_fft<T, M, 1, 1, M, LB, 2, +1, NT>(A, tw);
+  const T ad = (T)add.v[comp];
+  for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
+    const int l = idx / N, z = idx - l * N;
+    const c2<T> a = A[l * M + (z >> 1)];
+    const T v = ((z & 1) ? a.y : a.x) * scale + ad;
+    F[idx] = MODE ? F[idx] + v : v;
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tma_store3(&mreal, F, 0, line0, comp);
+    tma_store_commit_wait();
+  }
+}
+
+// ------------------------------------------------------- strided passes
+// One block: KB consecutive kz columns of one component at one outer index,
+// lines of L points along y (axis 1) or x (axis 0).
+template <typename T, int L, int KB, int SG>
+__global__ void __launch_bounds__(NT) fft_s_tma_kernel(const __grid_constant__ CUtensorMap m, int axis,
+                                                       const c2<T>* __restrict__ tw, int* err) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ uint64_t bar;
+  __shared__ int ok_s;
+  c2<T>* D = reinterpret_cast<c2<T>*>(smraw);   // L x KB
+  const int x0 = blockIdx.x * KB * cw<T>(), outer = blockIdx.y, comp = blockIdx.z;
+  const int c1 = axis == 1 ? 0 : outer, c2i = axis == 1 ? outer : 0;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    mbar_expect(&bar, (uint32_t)(L * KB * sizeof(c2<T>)));
+    tma_load4(D, &m, x0, c1, c2i, comp, &bar);
+  }
+  if (!block_wait_loads(&bar, &ok_s, err)) return;
+  tile_fft<T, L, KB, KB, 0, 1, 1, SG, NT>(D, tw);
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tma_store4(&m, D, x0, c1, c2i, comp);
+    tma_store_commit_wait();
+  }
+}
+
+// x pass fused with Gamma0: six stress components forward along x, Delta =
+// Gamma0 : sigma-hat at every wave vector of the tile, antisymmetric part
+// added to the spin accumulator tile, inverse along x.  One block: fixed y,
+// KB consecutive kz.
+template <typename T, int L, int KB>
+__global__ void __launch_bounds__(NT) fft_xg_tma_kernel(const GreenConst gc, const __grid_constant__ CUtensorMap mspec,
+                                                        const __grid_constant__ CUtensorMap manti, int n1, int n2,
+                                                        int kz, const c2<T>* __restrict__ twf,
+                                                        const c2<T>* __restrict__ twi, int* err) {
+  constexpr int SLAB = L * KB;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ uint64_t bar;
+  __shared__ int ok_s;
+  c2<T>* D = reinterpret_cast<c2<T>*>(smraw);   // 6 x L x KB
+  c2<T>* Aq = D + 6 * SLAB;                     // 3 x L x KB
+  const int k0 = blockIdx.x * KB, y = blockIdx.y;
+  const int x0 = k0 * cw<T>();
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    mbar_expect(&bar, (uint32_t)(9 * SLAB * sizeof(c2<T>)));
+#pragma unroll
+    for (int c = 0; c < 6; c++) tma_load4(D + c * SLAB, &mspec, x0, y, 0, c, &bar);
+#pragma unroll
+    for (int c = 0; c < 3; c++) tma_load4(Aq + c * SLAB, &manti, x0, y, 0, c, &bar);
+  }
+  if (!block_wait_loads(&bar, &ok_s, err)) return;
+  tile_fft<T, L, KB, KB, SLAB, 6, 1, -1, NT>(D, twf);
+  for (int idx = threadIdx.x; idx < SLAB; idx += NT) {
+    const int kk = idx % KB, kx = idx / KB;
+    if (k0 + kk >= kz) continue;
+    c2<T> s[6], a[3];
+#pragma unroll
+    for (int c = 0; c < 6; c++) s[c] = D[c * SLAB + idx];
+    green_point<T>(gc, kx, y, k0 + kk, L, n1, n2, s, a);
+#pragma unroll
+    for (int c = 0; c < 6; c++) D[c * SLAB + idx] = s[c];
+#pragma unroll
+    for (int c = 0; c < 3; c++) Aq[c * SLAB + idx] = cadd<T>(Aq[c * SLAB + idx], a[c]);
+  }
+  __syncthreads();
+  tile_fft<T, L, KB, KB, SLAB, 6, 1, +1, NT>(D, twi);
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) tma_store4(&mspec, D + c * SLAB, x0, y, 0, c);
+#pragma unroll
+    for (int c = 0; c < 3; c++) tma_store4(&manti, Aq + c * SLAB, x0, y, 0, c);
+    tma_store_commit_wait();
+  }
+}
+
+// ------------------------------------------------------------ host side
+static bool ct_size(int n) {
+  switch (n) {
+    case 16: case 32: case 48: case 64: case 96: case 128: case 256: return true;
+    default: return false;
+  }
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// rank-r tiled map, element type dt of esz bytes; dims/box innermost first,
+// strides in bytes for dims 1..r-1
+static bool encode(CUtensorMap* m, CUtensorMapDataType dt, int rank, void* base, const cuuint64_t* dims,
+                   const cuuint64_t* strides, const cuuint32_t* box) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return false;
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return fn(m, dt, (cuuint32_t)rank, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct TmaMaps {
+  CUtensorMap real_sig, real_strain, real_wspin;   // z passes, real fields
+  CUtensorMap spec_z, anti_z;                      // z passes, half spectra
+  CUtensorMap spec_y, anti_y, anti_x;              // strided passes
+  CUtensorMap spec_g, anti_g;                      // Green x pass
+  bool z, s, g;                                    // passes with maps
+};
+
+template <typename T>
+TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti) {
+  TmaMaps* t = new TmaMaps();
+  memset(t, 0, sizeof(*t));
+  if (!ct_size(g.n0) || !ct_size(g.n1) || !ct_size(g.n2) || !encode_fn()) return t;
+  const CUtensorMapDataType rt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const CUtensorMapDataType wt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;   // spectra in 8-byte words
+  const cuuint64_t C = (cuuint64_t)cw<T>(), cb = sizeof(c2<T>), ws = sizeof(T);
+  const cuuint64_t lines = (cuuint64_t)g.n0 * g.n1;
+  const int lb = lb_z<T>(g.n2);
+  bool ok = true;
+  // z passes: real [c][line][z] and spectrum [c][line][kzs]
+  if ((cuuint64_t)g.kzs * C <= 256) {
+    cuuint64_t d6[3] = {(cuuint64_t)g.n2, lines, 6}, d3[3] = {(cuuint64_t)g.n2, lines, 3};
+    cuuint64_t st[2] = {g.n2 * ws, (cuuint64_t)g.plane * ws};
+    cuuint32_t bx[3] = {(cuuint32_t)g.n2, (cuuint32_t)lb, 1};
+    ok = ok && encode(&t->real_sig, rt, 3, sig, d6, st, bx) && encode(&t->real_strain, rt, 3, strain, d6, st, bx) &&
+         encode(&t->real_wspin, rt, 3, wspin, d3, st, bx);
+    cuuint64_t k6[3] = {(cuuint64_t)g.kzs * C, lines, 6}, k3[3] = {(cuuint64_t)g.kzs * C, lines, 3};
+    cuuint64_t ks[2] = {(cuuint64_t)g.kzs * cb, (cuuint64_t)g.kplane * cb};
+    cuuint32_t kbx[3] = {(cuuint32_t)(g.kzs * C), (cuuint32_t)lb, 1};
+    ok = ok && encode(&t->spec_z, wt, 3, spec, k6, ks, kbx) && encode(&t->anti_z, wt, 3, anti, k3, ks, kbx);
+    t->z = ok;
+  }
+  // strided and Green passes: [c][x][y][kzs] as 4-D
+  {
+    cuuint64_t k6[4] = {(cuuint64_t)g.kzs * C, (cuuint64_t)g.n1, (cuuint64_t)g.n0, 6};
+    cuuint64_t k3[4] = {(cuuint64_t)g.kzs * C, (cuuint64_t)g.n1, (cuuint64_t)g.n0, 3};
+    cuuint64_t st[3] = {(cuuint64_t)g.kzs * cb, (cuuint64_t)g.n1 * g.kzs * cb, (cuuint64_t)g.kplane * cb};
+    const cuuint32_t ks = (cuuint32_t)(kb_strided<T>() * C), kg = (cuuint32_t)(kb_green<T>() * C);
+    cuuint32_t by[4] = {ks, (cuuint32_t)g.n1, 1, 1}, bxs[4] = {ks, 1, (cuuint32_t)g.n0, 1};
+    cuuint32_t bg[4] = {kg, 1, (cuuint32_t)g.n0, 1};
+    bool s_ok = encode(&t->spec_y, wt, 4, spec, k6, st, by) && encode(&t->anti_y, wt, 4, anti, k3, st, by) &&
+                encode(&t->anti_x, wt, 4, anti, k3, st, bxs);
+    bool g_ok = encode(&t->spec_g, wt, 4, spec, k6, st, bg) && encode(&t->anti_g, wt, 4, anti, k3, st, bg);
+    t->s = s_ok;
+    t->g = g_ok;
+  }
+  return t;
+}
+
+void tma_destroy(TmaMaps* t) { delete t; }
+bool tma_has(const TmaMaps* t, int pass) { return t && (pass == 0 ? t->z : pass == 1 ? t->s : t->g); }
+
+static size_t zr_smem(int n, int lb, size_t cb) {
+  const int M = n / 2, KZS = (M + 2) & ~1;
+  return cb * (size_t)(((lb * M + 15) & ~15) + lb * KZS);
+}
+static size_t zc_smem(int n, int lb, size_t cb) {
+  const int M = n / 2, KZS = (M + 2) & ~1;
+  return cb * (size_t)(((lb * KZS + 15) & ~15) + ((lb * M + 15) & ~15) + lb * M);
+}
+
+template <typename T, int N>
+static cudaError_t zr_launch(const TmaMaps* t, int ncomp, long long lines, const c2<T>* tw, int* err,
+                             cudaStream_t st) {
+  constexpr int LB = lb_z<T>(N);
+  const size_t sm = zr_smem(N, LB, sizeof(c2<T>));
+  auto k = fft_zr_tma_kernel<T, N, LB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((unsigned)((lines + LB - 1) / LB), ncomp);
+  k<<<grid, NT, sm, st>>>(t->real_sig, t->spec_z, tw, err);
+  return cudaGetLastError();
+}
+
+template <typename T, int N>
+static cudaError_t zc_launch(const CUtensorMap& ms, const CUtensorMap& mr, int ncomp, long long lines,
+                             const c2<T>* tw, T scale, const AddVec& add, int mode, int* err, cudaStream_t st) {
+  constexpr int LB = lb_z<T>(N);
+  const size_t sm = zc_smem(N, LB, sizeof(c2<T>));
+  dim3 grid((unsigned)((lines + LB - 1) / LB), ncomp);
+  if (mode) {
+    auto k = fft_zc_tma_kernel<T, N, LB, 1>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, add, err);
+  } else {
+    auto k = fft_zc_tma_kernel<T, N, LB, 0>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, add, err);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T, int L>
+static cudaError_t s_launch(const CUtensorMap& m, int axis, int ncomp, int nouter, int kzs, int sign,
+                            const c2<T>* tw, int* err, cudaStream_t st) {
+  constexpr int KB = kb_strided<T>();
+  const size_t sm = (size_t)L * KB * sizeof(c2<T>);
+  dim3 grid((kzs + KB - 1) / KB, nouter, ncomp);
+  if (sign < 0) {
+    auto k = fft_s_tma_kernel<T, L, KB, -1>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, NT, sm, st>>>(m, axis, tw, err);
+  } else {
+    auto k = fft_s_tma_kernel<T, L, KB, +1>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<grid, NT, sm, st>>>(m, axis, tw, err);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T, int L>
+static cudaError_t g_launch(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
+                            const c2<T>* twi, int* err, cudaStream_t st) {
+  constexpr int KB = kb_green<T>();
+  const size_t sm = (size_t)9 * L * KB * sizeof(c2<T>);
+  auto k = fft_xg_tma_kernel<T, L, KB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((g.kzs + KB - 1) / KB, g.n1);
+  k<<<grid, NT, sm, st>>>(gc, t->spec_g, t->anti_g, g.n1, g.n2, g.kz, twf, twi, err);
+  return cudaGetLastError();
+}
+
+#define MTH_TMA_SIZES(X) X(16) X(32) X(48) X(64) X(96) X(128) X(256)
+
+template <typename T>
+cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, int* err, cudaStream_t st) {
+  const long long lines = (long long)g.n0 * g.n1;
+  switch (g.n2) {
+#define MTH_CASE(N) case N: return zr_launch<T, N>(t, 6, lines, tw, err, st);
+    MTH_TMA_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// which = 0: stress spectrum -> strain field (mode 1); 1: spin spectrum ->
+// spin field (mode 0)
+template <typename T>
+cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const AddVec& add,
+                          int* err, cudaStream_t st) {
+  const long long lines = (long long)g.n0 * g.n1;
+  const CUtensorMap& ms = which ? t->anti_z : t->spec_z;
+  const CUtensorMap& mr = which ? t->real_wspin : t->real_strain;
+  const int ncomp = which ? 3 : 6, mode = which ? 0 : 1;
+  switch (g.n2) {
+#define MTH_CASE(N) case N: return zc_launch<T, N>(ms, mr, ncomp, lines, tw, scale, add, mode, err, st);
+    MTH_TMA_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// which = 0: stress spectrum along y; 1: spin spectrum along y; 2: spin
+// spectrum along x
+template <typename T>
+cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int sign, const c2<T>* tw, int* err,
+                            cudaStream_t st) {
+  const CUtensorMap& m = which == 0 ? t->spec_y : which == 1 ? t->anti_y : t->anti_x;
+  const int axis = which == 2 ? 0 : 1;
+  const int L = axis == 1 ? g.n1 : g.n0, nouter = axis == 1 ? g.n0 : g.n1;
+  const int ncomp = which == 0 ? 6 : 3;
+  switch (L) {
+#define MTH_CASE(N) case N: return s_launch<T, N>(m, axis, ncomp, nouter, g.kzs, sign, tw, err, st);
+    MTH_TMA_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
+                            const c2<T>* twi, int* err, cudaStream_t st) {
+  switch (g.n0) {
+#define MTH_CASE(N) case N: return g_launch<T, N>(t, g, gc, twf, twi, err, st);
+    MTH_TMA_SIZES(MTH_CASE)
+#undef MTH_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+#define INST(T)                                                                                                    \
+  template TmaMaps* tma_create<T>(const FftGeom&, T*, T*, T*, c2<T>*, c2<T>*);                                     \
+  template cudaError_t tma_fft_z_r2c<T>(const TmaMaps*, const FftGeom&, const c2<T>*, int*, cudaStream_t);         \
+  template cudaError_t tma_fft_z_c2r<T>(const TmaMaps*, const FftGeom&, int, const c2<T>*, T, const AddVec&, int*, \
+                                        cudaStream_t);                                                             \
+  template cudaError_t tma_fft_strided<T>(const TmaMaps*, const FftGeom&, int, int, const c2<T>*, int*,            \
+                                          cudaStream_t);                                                           \
+  template cudaError_t tma_fft_x_green<T>(const TmaMaps*, const FftGeom&, const GreenConst&, const c2<T>*,         \
+                                          const c2<T>*, int*, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace mth

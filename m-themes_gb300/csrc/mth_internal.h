@@ -15,7 +15,9 @@ struct FftPlan {
 
 struct FftGeom {
   int n0, n1, n2, kz;      // grid and half-spectrum length along z
-  long long plane, kplane; // elements per real plane / per spectrum plane
+  int kzs;                 // half-spectrum row stride: kz rounded up to even, so
+                           // that FP32 spectrum rows start on 16-byte boundaries
+  long long plane, kplane; // elements per real plane / per spectrum plane (n0*n1*kzs)
   FftPlan px, py, pz;
   size_t smem_budget;      // dynamic shared memory per block (bytes)
 };
@@ -49,6 +51,27 @@ struct NewtonConst {
 void fill_float_consts(NewtonConst& nc);
 
 bool make_plan(int n, FftPlan* p);
+
+// TMA-staged passes (fft_tma.cu) for grids whose three line lengths have
+// compile-time plans.  tma_create builds the tensor maps over the fields and
+// spectra; tma_has(t, pass) says whether pass 0 (z), 1 (y / x strided) or
+// 2 (x + Green) has them.  err: device flag raised by a timed-out wait.
+struct TmaMaps;
+template <typename T>
+TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti);
+void tma_destroy(TmaMaps* t);
+bool tma_has(const TmaMaps* t, int pass);
+template <typename T>
+cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, int* err, cudaStream_t st);
+template <typename T>
+cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const AddVec& add,
+                          int* err, cudaStream_t st);
+template <typename T>
+cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int sign, const c2<T>* tw, int* err,
+                            cudaStream_t st);
+template <typename T>
+cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
+                            const c2<T>* twi, int* err, cudaStream_t st);
 
 template <typename T>
 cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, cudaStream_t st);

@@ -65,7 +65,9 @@ def test_mixed_within_tolerance(name):
     s.close()
 
 
-@pytest.mark.parametrize("dims", [(48, 8, 16), (8, 24, 6), (32, 32, 32)])
+# (48, 8, 16), (8, 24, 6): shared-memory passes (a line length without a
+# compile-time plan); the others: TMA passes, incl. radix-3 and anisotropic
+@pytest.mark.parametrize("dims", [(48, 8, 16), (8, 24, 6), (32, 32, 32), (48, 32, 16), (32, 16, 96)])
 def test_fp64_matches_oracle_shapes(dims):
     cfg = synth.Config(cell_dim=dims, n_grains=12, n_steps=3, seed=31, iter_max=12)
     o, ro = run_oracle(cfg)
@@ -76,6 +78,18 @@ def test_fp64_matches_oracle_shapes(dims):
         assert rel(a["disgrad_avg"], b["disgrad_avg"]) < FP64_MACRO
     assert rel_l2(s.field("sig"), o.field("sig")) < FP64_FIELD
     assert rel(s.field("rot"), o.field("rot")) < 1e-8
+    s.close()
+
+
+@pytest.mark.parametrize("dims", [(48, 32, 16), (64, 64, 64)])
+def test_mixed_matches_oracle_shapes(dims):
+    cfg = synth.Config(cell_dim=dims, n_grains=12, n_steps=2, seed=37, iter_max=10)
+    o, ro = run_oracle(cfg)
+    s, rg = run_gpu(cfg, capi.MTH_MIXED)
+    for a, b in zip(rg, ro):
+        assert rel(a["sig_avg"], b["sig_avg"]) < MIXED_MACRO
+        assert rel(a["disgrad_avg"], b["disgrad_avg"]) < MIXED_MACRO
+    assert rel_l2(s.field("sig"), o.field("sig")) < 1e-4
     s.close()
 
 
