@@ -216,6 +216,24 @@ mth_status mth_local_solve_noalloc(const mth_params* params, const double c066[3
                                    const double* d_rot, const double* d_crss, double* d_edot,
                                    double* d_err, long long* newton_iters, void* stream);
 
+/* Batches of independent volumes (RVEs) on one GPU.  Each member has its own
+ * parameters (material, loading, precision), microstructure and grid size;
+ * mth_batch_step advances every member by one mechanical step, with the same
+ * results as mth_step on each member alone.  One Green iteration of all
+ * members still iterating is one CUDA-graph launch (the members' kernels as
+ * parallel branches); converged members are switched off on the device.
+ * The reference runs one volume per job (src/evp.c:7-32) and has no
+ * counterpart.  Recrystallisation (pf_substeps > 0) is not supported in a
+ * batch (MTH_ERR_UNSUPPORTED); all members must name the same device. */
+typedef struct mth_batch mth_batch;
+mth_status mth_batch_create(const mth_params* params, int n, mth_batch** out);
+mth_status mth_batch_upload(mth_batch* batch, int member, const int* grain, const int* phase,
+                            const double* euler_deg, size_t n_voxels);
+/* reports: n entries (may be NULL) */
+mth_status mth_batch_step(mth_batch* batch, mth_step_report* reports);
+mth_status mth_batch_download_field(mth_batch* batch, int member, int field, double* host, size_t n_values);
+mth_status mth_batch_destroy(mth_batch* batch);
+
 /* Per-kernel device timing.  When enabled, every kernel launch of the context
  * is bracketed by CUDA events on the context's stream; times are summed per
  * kernel class.  Launch counts are kept whether or not timing is enabled.

@@ -263,6 +263,14 @@ struct mth_ctx {
   TmaMaps* tma;       // tensor maps of the TMA passes (null members: shared-memory passes)
   int* err_d;         // raised by a timed-out wait in a kernel
   int* err_h;         // pinned copy
+  double* add_d;      // uniform strain increment of the current Green iteration (6, device)
+  double* add_h;      // pinned staging of add_d
+  int* live_d;        // live flag read by the iteration kernels (1 outside a batch)
+  bool in_batch;      // red, err_d, add_d, live_d and the stream belong to a batch
+  bool tma_off;       // shared-memory passes even where tensor maps exist (tuning)
+  // state of the mechanical step in progress (mth_step and the batch driver)
+  int it_iter, it_nnew;
+  long long it_nit, it_nbad;
   uint8_t* phase_d;
   int* grain_d;
   int* eclass_d;
@@ -320,19 +328,24 @@ static void ctx_free(mth_ctx* c) {
   cudaFree(c->spec);
   cudaFree(c->anti);
   tma_destroy(c->tma);
-  cudaFree(c->err_d);
+  if (!c->in_batch) {
+    cudaFree(c->err_d);
+    cudaFree(c->red);
+    cudaFree(c->add_d);
+    cudaFree(c->live_d);
+  }
   if (c->err_h) cudaFreeHost(c->err_h);
+  if (c->add_h) cudaFreeHost(c->add_h);
   cudaFree(c->phase_d);
   cudaFree(c->grain_d);
   cudaFree(c->eclass_d);
   cudaFree(c->etab_d);
   cudaFree(c->etabf_d);
   cudaFree(c->partials);
-  cudaFree(c->red);
   if (c->red_h) cudaFreeHost(c->red_h);
   for (int a = 0; a < 3; a++)
     for (int d = 0; d < 2; d++) cudaFree(c->tw[a][d]);
-  if (c->st) cudaStreamDestroy(c->st);
+  if (c->st && !c->in_batch) cudaStreamDestroy(c->st);
   if (c->ev_pool) {
     for (cudaEvent_t e : *c->ev_pool) cudaEventDestroy(e);
     delete c->ev_pool;
@@ -543,6 +556,14 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   CKC(cudaMemset(c->err_d, 0, sizeof(int)));
   CKC(cudaMallocHost(&c->err_h, sizeof(int)));
   *c->err_h = 0;
+  CKC(cudaMalloc(&c->add_d, sizeof(double) * 8));
+  CKC(cudaMemset(c->add_d, 0, sizeof(double) * 8));
+  CKC(cudaMallocHost(&c->add_h, sizeof(double) * 8));
+  CKC(cudaMalloc(&c->live_d, sizeof(int)));
+  {
+    const int one = 1;
+    CKC(cudaMemcpy(c->live_d, &one, sizeof(int), cudaMemcpyHostToDevice));
+  }
   auto carve = [&](auto* base, auto& f) {
     long long o = 0;
     f.sig = base + o; o += 6 * P;
@@ -618,8 +639,19 @@ extern "C" mth_status mth_destroy(mth_ctx* c) {
   return MTH_OK;
 }
 
+static IterIn iter_in(const mth_ctx* c) { return IterIn{c->add_d, c->live_d}; }
+
+// gated: the kernel follows the live flag (inside a batch graph)
+static mth_status launch_reduce(mth_ctx* c, int width, bool gated) {
+  LAUNCH(K_REDUCE, 8.0 * width * (c->nblocks + 1),
+         launch_reduce_partials(c->partials, c->nblocks, width, c->red, gated ? iter_in(c) : IterIn{nullptr, nullptr},
+                                c->st));
+  return MTH_OK;
+}
+
 static mth_status reduce_to_host(mth_ctx* c, int width, double* out) {
-  LAUNCH(K_REDUCE, 8.0 * width * (c->nblocks + 1), launch_reduce_partials(c->partials, c->nblocks, width, c->red, c->st));
+  mth_status s = launch_reduce(c, width, false);
+  if (s) return s;
   CK(cudaMemcpyAsync(c->red_h, c->red, sizeof(double) * width, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(c->err_h, c->err_d, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -797,7 +829,8 @@ static void get_smacro(mth_ctx* c, const double* red) {
 }
 
 template <typename T>
-static mth_status green_iteration(mth_ctx* c, const AddVec& add) {
+static mth_status green_iteration(mth_ctx* c) {
+  const IterIn it = iter_in(c);
   const FftGeom& g = c->geom;
   Fields<T>& f = *reinterpret_cast<Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
   c2<T>* spec = static_cast<c2<T>*>(c->spec);
@@ -805,27 +838,28 @@ static mth_status green_iteration(mth_ctx* c, const AddVec& add) {
   auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
   // algorithmic bytes: real plane = w*nv, complex spectrum plane = 2w*kplane
   const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.n0 * g.n1 * g.kz;
-  const bool tz = tma_has(c->tma, 0), ts = tma_has(c->tma, 1), tg = tma_has(c->tma, 2);
+  const bool tz = !c->tma_off && tma_has(c->tma, 0), ts = !c->tma_off && tma_has(c->tma, 1),
+             tg = !c->tma_off && tma_has(c->tma, 2);
   const T scale = (T)(1.0 / (double)c->nv);
   LAUNCH(K_FFT_Z_R2C, 6 * rp + 6 * kp,
-         tz ? tma_fft_z_r2c<T>(c->tma, g, tw(2, 0), c->err_d, c->st)
-            : launch_fft_z_r2c<T>(g, f.sig, spec, 6, tw(2, 0), c->st));
+         tz ? tma_fft_z_r2c<T>(c->tma, g, tw(2, 0), it, c->err_d, c->st)
+            : launch_fft_z_r2c<T>(g, f.sig, spec, 6, tw(2, 0), it, c->st));
   LAUNCH(K_FFT_Y, 12 * kp,
-         ts ? tma_fft_strided<T>(c->tma, g, 0, -1, tw(1, 0), c->err_d, c->st)
-            : launch_fft_strided<T>(g, spec, 6, 1, -1, tw(1, 0), c->st));
+         ts ? tma_fft_strided<T>(c->tma, g, 0, -1, tw(1, 0), it, c->err_d, c->st)
+            : launch_fft_strided<T>(g, spec, 6, 1, -1, tw(1, 0), it, c->st));
   LAUNCH(K_FFT_X_GREEN, 12 * kp + 6 * kp,
-         tg ? tma_fft_x_green<T>(c->tma, g, c->gc, tw(0, 0), tw(0, 1), c->err_d, c->st)
-            : launch_fft_x_green<T>(g, c->gc, spec, anti, tw(0, 0), tw(0, 1), c->st));
+         tg ? tma_fft_x_green<T>(c->tma, g, c->gc, tw(0, 0), tw(0, 1), it, c->err_d, c->st)
+            : launch_fft_x_green<T>(g, c->gc, spec, anti, tw(0, 0), tw(0, 1), it, c->st));
   LAUNCH(K_FFT_Y, 12 * kp,
-         ts ? tma_fft_strided<T>(c->tma, g, 0, +1, tw(1, 1), c->err_d, c->st)
-            : launch_fft_strided<T>(g, spec, 6, 1, +1, tw(1, 1), c->st));
+         ts ? tma_fft_strided<T>(c->tma, g, 0, +1, tw(1, 1), it, c->err_d, c->st)
+            : launch_fft_strided<T>(g, spec, 6, 1, +1, tw(1, 1), it, c->st));
   LAUNCH(K_FFT_Z_C2R, 6 * kp + 12 * rp,
-         tz ? tma_fft_z_c2r<T>(c->tma, g, 0, tw(2, 1), scale, add, c->err_d, c->st)
-            : launch_fft_z_c2r<T>(g, spec, f.strain, 6, tw(2, 1), scale, add, 1, c->st));
+         tz ? tma_fft_z_c2r<T>(c->tma, g, 0, tw(2, 1), scale, it, c->err_d, c->st)
+            : launch_fft_z_c2r<T>(g, spec, f.strain, 6, tw(2, 1), scale, it, 1, c->st));
   // Newton: read sigma, strain, eps_p (18), rot (9), CRSS (12); write sigma, edot (12);
   // phase (1 B) and elastic class (4 B) per voxel
   LAUNCH(K_NEWTON, (18 + 9 + 12 + 12) * rp + 5.0 * (double)c->nv,
-         launch_newton(c->mixed, c->nc, &f, c->partials, c->nblocks, c->st));
+         launch_newton(c->mixed, c->nc, &f, c->partials, c->nblocks, it, c->st));
   return MTH_OK;
 }
 
@@ -835,20 +869,19 @@ static mth_status spin_field(mth_ctx* c) {
   Fields<T>& f = *reinterpret_cast<Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
   c2<T>* anti = static_cast<c2<T>*>(c->anti);
   auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
-  AddVec zero;
-  memset(&zero, 0, sizeof(zero));
+  const IterIn it{nullptr, nullptr};   // no uniform part; always live
   const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.n0 * g.n1 * g.kz;
-  const bool tz = tma_has(c->tma, 0), ts = tma_has(c->tma, 1);
+  const bool tz = !c->tma_off && tma_has(c->tma, 0), ts = !c->tma_off && tma_has(c->tma, 1);
   const T scale = (T)(1.0 / (double)c->nv);
   LAUNCH(K_SPIN, 6 * kp,
-         ts ? tma_fft_strided<T>(c->tma, g, 2, +1, tw(0, 1), c->err_d, c->st)
-            : launch_fft_strided<T>(g, anti, 3, 0, +1, tw(0, 1), c->st));
+         ts ? tma_fft_strided<T>(c->tma, g, 2, +1, tw(0, 1), it, c->err_d, c->st)
+            : launch_fft_strided<T>(g, anti, 3, 0, +1, tw(0, 1), it, c->st));
   LAUNCH(K_SPIN, 6 * kp,
-         ts ? tma_fft_strided<T>(c->tma, g, 1, +1, tw(1, 1), c->err_d, c->st)
-            : launch_fft_strided<T>(g, anti, 3, 1, +1, tw(1, 1), c->st));
+         ts ? tma_fft_strided<T>(c->tma, g, 1, +1, tw(1, 1), it, c->err_d, c->st)
+            : launch_fft_strided<T>(g, anti, 3, 1, +1, tw(1, 1), it, c->st));
   LAUNCH(K_SPIN, 3 * kp + 3 * rp,
-         tz ? tma_fft_z_c2r<T>(c->tma, g, 1, tw(2, 1), scale, zero, c->err_d, c->st)
-            : launch_fft_z_c2r<T>(g, anti, f.wspin, 3, tw(2, 1), scale, zero, 0, c->st));
+         tz ? tma_fft_z_c2r<T>(c->tma, g, 1, tw(2, 1), scale, it, c->err_d, c->st)
+            : launch_fft_z_c2r<T>(g, anti, f.wspin, 3, tw(2, 1), scale, it, 0, c->st));
   return MTH_OK;
 }
 
@@ -988,55 +1021,69 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   return refresh_reference_medium(c);
 }
 
-extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
-  if (!c) return set_err(MTH_ERR_ARG, "null context");
-  if (!c->uploaded) return set_err(MTH_ERR_STATE, "mth_step before mth_upload_microstructure");
-  SETDEV(c);
-  const int istep = c->istep;
-  const double dt = c->p.time_step;
-  int n_new = 0;
-  if (c->drx && istep > 0) {
-    mth_status s = drx_step(c, &n_new);
+// A mechanical step in phases, shared by mth_step and the batch driver:
+// step_begin (DRX, per-step flags, spin accumulator), then per Green
+// iteration iter_add (host: the uniform strain increment of the iteration
+// into add_h) / the iteration kernels / iter_finish (host: error norms and
+// the macroscopic stress update from the reduced partial sums) while
+// iter_more, and step_end (end-of-step updates and the report).
+static mth_status step_begin(mth_ctx* c) {
+  c->it_nnew = 0;
+  if (c->drx && c->istep > 0) {
+    mth_status s = drx_step(c, &c->it_nnew);
     if (s) return s;
   }
-  c->nc.flow_off = (istep == 0 && c->p.update_flag != 1) ? 1 : 0;
+  c->nc.flow_off = (c->istep == 0 && c->p.update_flag != 1) ? 1 : 0;
   memset(c->ddg, 0, sizeof(c->ddg));
   memset(c->ddg_acum, 0, sizeof(c->ddg_acum));
   memset(c->ddg_applied, 0, sizeof(c->ddg_applied));
   const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
   CK(cudaMemsetAsync(c->anti, 0, 2 * esz * c->geom.kplane * 3, c->st));
-  int iter = 0;
+  c->it_iter = 0;
+  c->it_nit = 0;
+  c->it_nbad = 0;
   c->err_e = 2. * c->p.err;
   c->err_s = 2. * c->p.err;
-  long long nit = 0, nbad = 0;
-  while (iter < c->p.iter_max && fmax(fabs(c->err_s), fabs(c->err_e)) > c->p.err) {
-    iter++;
-    // uniform strain added this iteration: dDisGradAvg of the previous
-    // get_smacro, plus Udot dt on the first one (src/evolution.c:1319-1332)
-    t33 u;
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) {
-        u[i][j] = c->ddg[i][j] + (iter == 1 ? c->udot[i][j] * dt : 0.0);
-        c->ddg_applied[i][j] += c->ddg[i][j];
-      }
-    AddVec add;
-    t2v(u, add.v, 6);
-    mth_status s = c->mixed ? green_iteration<float>(c, add) : green_iteration<double>(c, add);
-    if (s) return s;
-    double red[NPART];
-    s = reduce_to_host(c, NPART, red);
-    if (s) return s;
-    for (int i = 0; i < NPART; i++)
-      if (!std::isfinite(red[i])) return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", istep, iter);
-    nit += (long long)red[14];
-    nbad += (long long)red[15];
-    c->err_s = red[0] * c->wgt;
-    c->err_e = red[1] * c->wgt;
-    get_smacro(c, red);
-    if (fabs(c->e_vm) < 1E-5) c->err_e = 0.0;
-    else c->err_e /= c->e_vm;
-    c->err_s /= c->s_vm;
-  }
+  return MTH_OK;
+}
+
+static bool iter_more(const mth_ctx* c) {
+  return c->it_iter < c->p.iter_max && fmax(fabs(c->err_s), fabs(c->err_e)) > c->p.err;
+}
+
+// uniform strain added this iteration: dDisGradAvg of the previous
+// get_smacro, plus Udot dt on the first one (src/evolution.c:1319-1332)
+static void iter_add(mth_ctx* c) {
+  c->it_iter++;
+  const double dt = c->p.time_step;
+  t33 u;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      u[i][j] = c->ddg[i][j] + (c->it_iter == 1 ? c->udot[i][j] * dt : 0.0);
+      c->ddg_applied[i][j] += c->ddg[i][j];
+    }
+  t2v(u, c->add_h, 6);
+}
+
+static mth_status iter_finish(mth_ctx* c, const double* red) {
+  for (int i = 0; i < NPART; i++)
+    if (!std::isfinite(red[i]))
+      return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", c->istep,
+                     c->it_iter);
+  c->it_nit += (long long)red[14];
+  c->it_nbad += (long long)red[15];
+  c->err_s = red[0] * c->wgt;
+  c->err_e = red[1] * c->wgt;
+  get_smacro(c, red);
+  if (fabs(c->e_vm) < 1E-5) c->err_e = 0.0;
+  else c->err_e /= c->e_vm;
+  c->err_s /= c->s_vm;
+  return MTH_OK;
+}
+
+static mth_status step_end(mth_ctx* c, mth_step_report* rep) {
+  const int istep = c->istep;
+  const double dt = c->p.time_step;
   // end of step (src/evolution.c:1471-1546)
   t33 actual, vg;
   for (int i = 0; i < 3; i++)
@@ -1091,7 +1138,7 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
   if (rep) {
     memset(rep, 0, sizeof(*rep));
     rep->step = istep;
-    rep->iterations = iter;
+    rep->iterations = c->it_iter;
     rep->time = c->time_tot;
     memcpy(rep->sig_avg, c->sig_avg, sizeof(t33));
     memcpy(rep->sig_avg_ph1, c->sig_avg1, sizeof(t33));
@@ -1101,14 +1148,35 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
     rep->e_vm = c->e_vm; rep->evmp = evmp; rep->d_vm = c->d_vm; rep->dvmp = dvmp;
     rep->s_vm = c->s_vm; rep->s_vm1 = c->s_vm1;
     rep->err_s = c->err_s; rep->err_e = c->err_e;
-    rep->newton_iters = nit;
-    rep->newton_failed = nbad;
-    rep->n_new_grains = n_new;
+    rep->newton_iters = c->it_nit;
+    rep->newton_failed = c->it_nbad;
+    rep->n_new_grains = c->it_nnew;
   }
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) c->disgrad_avg[i][j] = c->disgrad_avg_t[i][j] + c->udot[i][j] * dt;
   c->istep++;
   return MTH_OK;
+}
+
+extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
+  if (!c) return set_err(MTH_ERR_ARG, "null context");
+  if (!c->uploaded) return set_err(MTH_ERR_STATE, "mth_step before mth_upload_microstructure");
+  if (c->in_batch) return set_err(MTH_ERR_STATE, "context belongs to a batch: use mth_batch_step");
+  SETDEV(c);
+  mth_status s = step_begin(c);
+  if (s) return s;
+  while (iter_more(c)) {
+    iter_add(c);
+    CK(cudaMemcpyAsync(c->add_d, c->add_h, sizeof(double) * 6, cudaMemcpyHostToDevice, c->st));
+    s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+    if (s) return s;
+    double red[NPART];
+    s = reduce_to_host(c, NPART, red);
+    if (s) return s;
+    s = iter_finish(c, red);
+    if (s) return s;
+  }
+  return step_end(c, rep);
 }
 
 // ------------------------------------------------------------- downloads
@@ -1428,5 +1496,302 @@ extern "C" mth_status mth_local_solve(const mth_params* p, const double c066[36]
   cudaFree(ds); cudaFree(de); cudaFree(dst); cudaFree(dr); cudaFree(dc); cudaFree(ded); cudaFree(der); cudaFree(dit);
   cudaFree(det);
   cudaStreamDestroy(st);
+  return MTH_OK;
+}
+
+// ------------------------------------------------------------ RVE batches
+// n independent volumes (own parameters, microstructure and grid size) on
+// one GPU.  Every member is an ordinary context whose stream, reduction
+// slot, error flag, strain-increment and live flag live in the batch.  One
+// Green iteration of the whole batch is one launch of a CUDA graph:
+//   H2D (strain increments and live flags of all members)
+//   -> per member, as parallel branches: its FFT passes, Newton, reduction
+//   -> D2H (reduced sums and error flags of all members).
+// A member that has converged keeps its branch but its live flag is 0, so
+// its kernels return at once.  The graph is captured again when the Newton
+// constants baked into its kernel parameters change (the first step runs
+// with the flow rule off).  For each distinct grid size and precision the
+// batch times the TMA and the shared-memory FFT passes once on a scratch
+// volume and keeps the faster (cached for the process).
+struct mth_batch {
+  int n = 0;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::vector<mth_ctx*> rve;
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr;
+  double* add_d = nullptr;
+  double* add_h = nullptr;
+  int* live_d = nullptr;
+  int* live_h = nullptr;
+  double* red_d = nullptr;
+  double* red_h = nullptr;
+  int* err_d = nullptr;
+  int* err_h = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<NewtonConst> cap_nc;
+};
+
+namespace {
+constexpr int BATCH_RED = 32;   // reduction slot of a member (doubles)
+
+void batch_free(mth_batch* b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (mth_ctx* c : b->rve) ctx_free(c);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (cudaStream_t s : b->branch) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  cudaFree(b->add_d);
+  cudaFree(b->live_d);
+  cudaFree(b->red_d);
+  cudaFree(b->err_d);
+  if (b->add_h) cudaFreeHost(b->add_h);
+  if (b->live_h) cudaFreeHost(b->live_h);
+  if (b->red_h) cudaFreeHost(b->red_h);
+  if (b->err_h) cudaFreeHost(b->err_h);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+// FFT pass choice per (grid, precision): 1 TMA, 0 shared memory
+std::map<std::vector<int>, int>& tuned_passes() {
+  static std::map<std::vector<int>, int> m;
+  return m;
+}
+
+// Time `its` Green iterations of a scratch volume with the parameters of p
+// (single grain, no pores) with the TMA and the shared-memory passes.
+mth_status tune_passes(const mth_params& p, int* use_tma) {
+  std::vector<int> key = {p.cell_dim[0], p.cell_dim[1], p.cell_dim[2], p.precision};
+  auto it = tuned_passes().find(key);
+  if (it != tuned_passes().end()) { *use_tma = it->second; return MTH_OK; }
+  mth_ctx* c = nullptr;
+  mth_status s = mth_create(&p, &c);
+  if (s) return s;
+  if (!tma_has(c->tma, 0) && !tma_has(c->tma, 1) && !tma_has(c->tma, 2)) {
+    ctx_free(c);
+    tuned_passes()[key] = 0;
+    *use_tma = 0;
+    return MTH_OK;
+  }
+  const size_t nv = (size_t)c->nv;
+  std::vector<int> grain(nv, 1), phase(nv, 1);
+  std::vector<double> eul(3 * nv, 0.0);
+  s = mth_upload_microstructure(c, grain.data(), phase.data(), eul.data(), nv);
+  if (s) { ctx_free(c); return s; }
+  c->add_h[0] = c->add_h[1] = c->add_h[2] = c->add_h[3] = c->add_h[4] = c->add_h[5] = 0.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float ms[2] = {0, 0};
+  for (int variant = 0; variant < 2; variant++) {
+    c->tma_off = variant == 1;
+    for (int rep = 0; rep < 2; rep++) {   // first pass warms up
+      if (cudaEventRecord(e0, c->st) != cudaSuccess) break;
+      for (int k = 0; k < 3; k++) {
+        s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+        if (s) break;
+      }
+      if (s) break;
+      cudaEventRecord(e1, c->st);
+      cudaStreamSynchronize(c->st);
+      cudaEventElapsedTime(&ms[variant], e0, e1);
+    }
+    if (s) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "pass tuning failed");
+  if (!s && *c->err_h) s = set_err(MTH_ERR_TIMEOUT, "pass tuning timed out");
+  ctx_free(c);
+  if (s) return s;
+  *use_tma = ms[0] <= ms[1] ? 1 : 0;
+  tuned_passes()[key] = *use_tma;
+  return MTH_OK;
+}
+
+// one Green iteration of every member as parallel graph branches
+mth_status batch_capture(mth_batch* b) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  const int n = b->n;
+  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  mth_status s = MTH_OK;
+  auto ck = [&](cudaError_t e) {
+    if (e != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  };
+  ck(cudaMemcpyAsync(b->add_d, b->add_h, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, b->st));
+  ck(cudaMemcpyAsync(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
+  ck(cudaEventRecord(b->fork, b->st));
+  for (int i = 0; i < n && !s; i++) {
+    mth_ctx* c = b->rve[i];
+    ck(cudaStreamWaitEvent(b->branch[i], b->fork, 0));
+    const int prof = c->prof_on;
+    c->prof_on = 0;
+    c->st = b->branch[i];
+    if (!s) s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+    if (!s) s = launch_reduce(c, NPART, true);
+    c->st = b->st;
+    c->prof_on = prof;
+    ck(cudaEventRecord(b->join[i], b->branch[i]));
+    ck(cudaStreamWaitEvent(b->st, b->join[i], 0));
+  }
+  ck(cudaMemcpyAsync(b->red_h, b->red_d, sizeof(double) * BATCH_RED * n, cudaMemcpyDeviceToHost, b->st));
+  ck(cudaMemcpyAsync(b->err_h, b->err_d, sizeof(int) * n, cudaMemcpyDeviceToHost, b->st));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (!s && e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  if (!s) {
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+  }
+  if (g) cudaGraphDestroy(g);
+  if (s) return s;
+  b->cap_nc.resize(n);
+  for (int i = 0; i < n; i++) b->cap_nc[i] = b->rve[i]->nc;
+  return MTH_OK;
+}
+}  // namespace
+
+extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batch** out) {
+  if (!params || !out || n <= 0) return set_err(MTH_ERR_ARG, "batch needs params, out and n > 0");
+  *out = nullptr;
+  for (int i = 0; i < n; i++) {
+    if (params[i].device != params[0].device) return set_err(MTH_ERR_ARG, "batch members on different devices");
+    if (params[i].pf_substeps > 0) return set_err(MTH_ERR_UNSUPPORTED, "recrystallisation in a batch member");
+  }
+  mth_batch* b = new mth_batch();
+  b->n = n;
+  b->device = params[0].device;
+  mth_status s = MTH_OK;
+  auto ck = [&](cudaError_t e) {
+    if (e != cudaSuccess && !s)
+      s = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
+  };
+  for (int i = 0; i < n && !s; i++) {
+    mth_ctx* c = nullptr;
+    s = mth_create(&params[i], &c);
+    if (!s) b->rve.push_back(c);
+  }
+  if (!s) {
+    ck(cudaSetDevice(b->device));
+    ck(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    ck(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->branch.resize(n, nullptr);
+    b->join.resize(n, nullptr);
+    for (int i = 0; i < n; i++) {
+      ck(cudaStreamCreateWithFlags(&b->branch[i], cudaStreamNonBlocking));
+      ck(cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming));
+    }
+    ck(cudaMalloc(&b->add_d, sizeof(double) * 8 * n));
+    ck(cudaMalloc(&b->live_d, sizeof(int) * n));
+    ck(cudaMalloc(&b->red_d, sizeof(double) * BATCH_RED * n));
+    ck(cudaMalloc(&b->err_d, sizeof(int) * n));
+    ck(cudaMallocHost(&b->add_h, sizeof(double) * 8 * n));
+    ck(cudaMallocHost(&b->live_h, sizeof(int) * n));
+    ck(cudaMallocHost(&b->red_h, sizeof(double) * BATCH_RED * n));
+    ck(cudaMallocHost(&b->err_h, sizeof(int) * n));
+  }
+  if (!s) {
+    ck(cudaMemset(b->add_d, 0, sizeof(double) * 8 * n));
+    ck(cudaMemset(b->err_d, 0, sizeof(int) * n));
+    memset(b->add_h, 0, sizeof(double) * 8 * n);
+    memset(b->err_h, 0, sizeof(int) * n);
+    for (int i = 0; i < n; i++) b->live_h[i] = 1;
+    ck(cudaMemcpy(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice));
+  }
+  for (int i = 0; i < n && !s; i++) {
+    mth_ctx* c = b->rve[i];
+    int use_tma = 1;
+    s = tune_passes(params[i], &use_tma);
+    if (s) break;
+    c->tma_off = !use_tma;
+    ck(cudaStreamSynchronize(c->st));
+    cudaStreamDestroy(c->st);
+    cudaFree(c->red);
+    cudaFree(c->err_d);
+    cudaFree(c->add_d);
+    cudaFree(c->live_d);
+    c->st = b->st;
+    c->red = b->red_d + (size_t)BATCH_RED * i;
+    c->err_d = b->err_d + i;
+    c->add_d = b->add_d + (size_t)8 * i;
+    c->live_d = b->live_d + i;
+    c->in_batch = true;
+  }
+  if (s) {
+    batch_free(b);
+    return s;
+  }
+  *out = b;
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_batch_upload(mth_batch* b, int i, const int* grain, const int* phase, const double* euler_deg,
+                                       size_t n_voxels) {
+  if (!b || i < 0 || i >= b->n) return set_err(MTH_ERR_ARG, "batch member %d", i);
+  return mth_upload_microstructure(b->rve[i], grain, phase, euler_deg, n_voxels);
+}
+
+extern "C" mth_status mth_batch_step(mth_batch* b, mth_step_report* reports) {
+  if (!b) return set_err(MTH_ERR_ARG, "null batch");
+  CK(cudaSetDevice(b->device));
+  const int n = b->n;
+  for (int i = 0; i < n; i++)
+    if (!b->rve[i]->uploaded) return set_err(MTH_ERR_STATE, "batch member %d has no microstructure", i);
+  for (int i = 0; i < n; i++) {
+    mth_status s = step_begin(b->rve[i]);
+    if (s) return s;
+  }
+  bool recapture = !b->exec;
+  for (int i = 0; i < n && !recapture; i++)
+    recapture = memcmp(&b->cap_nc[i], &b->rve[i]->nc, sizeof(NewtonConst)) != 0;
+  if (recapture) {
+    mth_status s = batch_capture(b);
+    if (s) return s;
+  }
+  std::vector<char> active(n);
+  int nact = 0;
+  for (int i = 0; i < n; i++) nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
+  while (nact > 0) {
+    for (int i = 0; i < n; i++) {
+      b->live_h[i] = active[i];
+      if (active[i]) {
+        iter_add(b->rve[i]);
+        memcpy(b->add_h + (size_t)8 * i, b->rve[i]->add_h, sizeof(double) * 6);
+      }
+    }
+    CK(cudaGraphLaunch(b->exec, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    nact = 0;
+    for (int i = 0; i < n; i++) {
+      if (b->err_h[i]) return set_err(MTH_ERR_TIMEOUT, "batch member %d: a kernel timed out waiting for its tile copies", i);
+      if (!active[i]) continue;
+      mth_status s = iter_finish(b->rve[i], b->red_h + (size_t)BATCH_RED * i);
+      if (s) return s;
+      nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    mth_status s = step_end(b->rve[i], reports ? &reports[i] : nullptr);
+    if (s) return s;
+  }
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_batch_download_field(mth_batch* b, int i, int field, double* host, size_t n_values) {
+  if (!b || i < 0 || i >= b->n) return set_err(MTH_ERR_ARG, "batch member %d", i);
+  return mth_download_field(b->rve[i], field, host, n_values);
+}
+
+extern "C" mth_status mth_batch_destroy(mth_batch* b) {
+  if (!b) return set_err(MTH_ERR_ARG, "null batch");
+  cudaSetDevice(b->device);
+  batch_free(b);
   return MTH_OK;
 }

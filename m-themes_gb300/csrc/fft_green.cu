@@ -132,7 +132,9 @@ __device__ __forceinline__ c2<T>* do_fft(c2<T>* d0, c2<T>* d1, int n, int ls, in
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_z_r2c_kernel(const T* __restrict__ in, c2<T>* __restrict__ out, int ncomp,
                                                         long long plane, long long kplane, int nlines, int n2_,
-                                                        int kzs, int lb, FftPlan pl, const c2<T>* __restrict__ twg) {
+                                                        int kzs, int lb, FftPlan pl, const c2<T>* __restrict__ twg,
+                                                        IterIn it) {
+  if (!is_live(it)) return;
   const int n2 = NC > 0 ? NC : n2_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
@@ -179,7 +181,8 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict__ spec, T* __restrict__ field, int ncomp,
                                                         long long plane, long long kplane, int nlines, int n2_,
                                                         int kzs, int lb, FftPlan pl, const c2<T>* __restrict__ twg, T scale,
-                                                        AddVec add, int mode) {
+                                                        IterIn it, int mode) {
+  if (!is_live(it)) return;
   const int n2 = NC > 0 ? NC : n2_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict_
   __syncthreads();
   c2<T>* r = do_fft<T, NC>(d0, d1, n2, ls, npair * lb, pl, tw, +1);
   __shared__ T addv[6];
-  if (threadIdx.x < 6) addv[threadIdx.x] = (T)add.v[threadIdx.x];
+  if (threadIdx.x < 6) addv[threadIdx.x] = it.add ? (T)it.add[threadIdx.x] : (T)0;
   __syncthreads();
   for (int idx = threadIdx.x; idx < ncomp * lb * n2; idx += blockDim.x) {
     const int z = idx % n2;
@@ -232,7 +235,8 @@ __global__ void __launch_bounds__(256) fft_z_c2r_kernel(const c2<T>* __restrict_
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_strided_kernel(c2<T>* __restrict__ spec, int ncomp, long long kplane,
                                                           int L_, long long S, long long ostride, int kzn, int kb,
-                                                          FftPlan pl, const c2<T>* __restrict__ twg, int sign) {
+                                                          FftPlan pl, const c2<T>* __restrict__ twg, int sign, IterIn it) {
+  if (!is_live(it)) return;
   const int L = NC > 0 ? NC : L_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smraw);
@@ -269,7 +273,8 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(256) fft_x_green_kernel(const GreenConst gc, c2<T>* __restrict__ spec, c2<T>* __restrict__ anti_acc,
                                                           long long kplane, int n0_, int n1, int n2, int kzn, int kzs, int kb,
                                                           FftPlan pl, const c2<T>* __restrict__ twf,
-                                                          const c2<T>* __restrict__ twi) {
+                                                          const c2<T>* __restrict__ twi, IterIn it) {
+  if (!is_live(it)) return;
   const int n0 = NC > 0 ? NC : n0_;
   extern __shared__ unsigned char smraw[];
   c2<T>* tw_f = reinterpret_cast<c2<T>*>(smraw);
@@ -335,7 +340,8 @@ static int pick_lb(int n2, int npair, int nlines, size_t budget) {
 }
 
 template <typename T>
-cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, cudaStream_t st) {
+cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, const IterIn& it,
+                             cudaStream_t st) {
   const int npair = (ncomp + 1) / 2;
   const int nlines = g.n0 * g.n1;
   const int lb = pick_lb<T>(g.n2, npair, nlines, g.smem_budget);
@@ -348,13 +354,13 @@ cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncom
     default: break;
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(in, out, ncomp, g.plane, g.kplane, nlines, g.n2, g.kzs, lb, g.pz, tw);
+  k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(in, out, ncomp, g.plane, g.kplane, nlines, g.n2, g.kzs, lb, g.pz, tw, it);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int ncomp, const c2<T>* tw, T scale,
-                             const AddVec& add, int mode, cudaStream_t st) {
+                             const IterIn& it, int mode, cudaStream_t st) {
   const int npair = (ncomp + 1) / 2;
   const int nlines = g.n0 * g.n1;
   const int lb = pick_lb<T>(g.n2, npair, nlines, g.smem_budget);
@@ -368,7 +374,7 @@ cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int 
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<(nlines + lb - 1) / lb, 256, sm, st>>>(spec, field, ncomp, g.plane, g.kplane, nlines, g.n2, g.kzs, lb, g.pz,
-                                             tw, scale, add, mode);
+                                             tw, scale, it, mode);
   return cudaGetLastError();
 }
 
@@ -384,7 +390,7 @@ static int pick_kb(int L, int ncomp, size_t budget, int ntw) {
 // axis 1 (y) or 0 (x)
 template <typename T>
 cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axis, int sign, const c2<T>* tw,
-                               cudaStream_t st) {
+                               const IterIn& it, cudaStream_t st) {
   const int L = axis == 1 ? g.n1 : g.n0;
   const long long S = axis == 1 ? g.kzs : (long long)g.n1 * g.kzs;
   const long long ostride = axis == 1 ? (long long)g.n1 * g.kzs : g.kzs;
@@ -401,13 +407,13 @@ cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axi
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kz + kb - 1) / kb, nouter);
-  k<<<grid, 256, sm, st>>>(spec, ncomp, g.kplane, L, S, ostride, g.kz, kb, pl, tw, sign);
+  k<<<grid, 256, sm, st>>>(spec, ncomp, g.kplane, L, S, ostride, g.kz, kb, pl, tw, sign, it);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* spec, c2<T>* anti, const c2<T>* twf,
-                               const c2<T>* twi, cudaStream_t st) {
+                               const c2<T>* twi, const IterIn& it, cudaStream_t st) {
   const int kb = pick_kb<T>(g.n0, 6, g.smem_budget, 2);
   const size_t sm = s_smem(g.n0, 6 * kb, sizeof(c2<T>), 2);
   auto k = fft_x_green_kernel<T, 0>;
@@ -419,17 +425,19 @@ cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* sp
   }
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kz + kb - 1) / kb, g.n1);
-  k<<<grid, 256, sm, st>>>(gc, spec, anti, g.kplane, g.n0, g.n1, g.n2, g.kz, g.kzs, kb, g.px, twf, twi);
+  k<<<grid, 256, sm, st>>>(gc, spec, anti, g.kplane, g.n0, g.n1, g.n2, g.kz, g.kzs, kb, g.px, twf, twi, it);
   return cudaGetLastError();
 }
 
 #define INST(T)                                                                                                      \
-  template cudaError_t launch_fft_z_r2c<T>(const FftGeom&, const T*, c2<T>*, int, const c2<T>*, cudaStream_t);        \
-  template cudaError_t launch_fft_z_c2r<T>(const FftGeom&, const c2<T>*, T*, int, const c2<T>*, T, const AddVec&, int, \
+  template cudaError_t launch_fft_z_r2c<T>(const FftGeom&, const T*, c2<T>*, int, const c2<T>*, const IterIn&,     \
                                            cudaStream_t);                                                            \
-  template cudaError_t launch_fft_strided<T>(const FftGeom&, c2<T>*, int, int, int, const c2<T>*, cudaStream_t);      \
+  template cudaError_t launch_fft_z_c2r<T>(const FftGeom&, const c2<T>*, T*, int, const c2<T>*, T, const IterIn&, int, \
+                                           cudaStream_t);                                                            \
+  template cudaError_t launch_fft_strided<T>(const FftGeom&, c2<T>*, int, int, int, const c2<T>*, const IterIn&,      \
+                                             cudaStream_t);                                                          \
   template cudaError_t launch_fft_x_green<T>(const FftGeom&, const GreenConst&, c2<T>*, c2<T>*, const c2<T>*, const c2<T>*, \
-                                            cudaStream_t);
+                                            const IterIn&, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

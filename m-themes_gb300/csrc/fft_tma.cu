@@ -188,7 +188,8 @@ template <typename T> __host__ __device__ constexpr int lb_z(int n) {
 template <typename T, int N, int LB>
 __global__ void __launch_bounds__(NT) fft_zr_tma_kernel(const __grid_constant__ CUtensorMap mreal,
                                                         const __grid_constant__ CUtensorMap mspec,
-                                                        const c2<T>* __restrict__ tw, int* err) {
+                                                        const c2<T>* __restrict__ tw, IterIn it, int* err) {
+  if (!is_live(it)) return;
   constexpr int M = N / 2, KZ = M + 1, KZS = (KZ + 1) & ~1;
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ uint64_t bar;
@@ -230,7 +231,8 @@ __global__ void __launch_bounds__(NT) fft_zr_tma_kernel(const __grid_constant__ 
 template <typename T, int N, int LB, int MODE>
 __global__ void __launch_bounds__(NT) fft_zc_tma_kernel(const __grid_constant__ CUtensorMap mspec,
                                                         const __grid_constant__ CUtensorMap mreal,
-                                                        const c2<T>* __restrict__ tw, T scale, AddVec add, int* err) {
+                                                        const c2<T>* __restrict__ tw, T scale, IterIn it, int* err) {
+  if (!is_live(it)) return;
   constexpr int M = N / 2, KZS = (M + 2) & ~1;
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ uint64_t bar;
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(NT) fft_zc_tma_kernel(const __grid_constant__ 
   }
   __syncthreads();
   tile_fft<T, M, 1, 1, M, LB, 2, +1, NT>(A, tw);
-  const T ad = (T)add.v[comp];
+  const T ad = it.add ? (T)it.add[comp] : (T)0;
   for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
     const int l = idx / N, z = idx - l * N;
     const c2<T> a = A[l * M + (z >> 1)];
@@ -277,7 +279,8 @@ __global__ void __launch_bounds__(NT) fft_zc_tma_kernel(const __grid_constant__ 
 // lines of L points along y (axis 1) or x (axis 0).
 template <typename T, int L, int KB, int SG>
 __global__ void __launch_bounds__(NT) fft_s_tma_kernel(const __grid_constant__ CUtensorMap m, int axis,
-                                                       const c2<T>* __restrict__ tw, int* err) {
+                                                       const c2<T>* __restrict__ tw, IterIn it, int* err) {
+  if (!is_live(it)) return;
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ uint64_t bar;
   __shared__ int ok_s;
@@ -307,7 +310,8 @@ template <typename T, int L, int KB>
 __global__ void __launch_bounds__(NT) fft_xg_tma_kernel(const GreenConst gc, const __grid_constant__ CUtensorMap mspec,
                                                         const __grid_constant__ CUtensorMap manti, int n1, int n2,
                                                         int kz, const c2<T>* __restrict__ twf,
-                                                        const c2<T>* __restrict__ twi, int* err) {
+                                                        const c2<T>* __restrict__ twi, IterIn it, int* err) {
+  if (!is_live(it)) return;
   constexpr int SLAB = L * KB;
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ uint64_t bar;
@@ -445,72 +449,73 @@ static size_t zc_smem(int n, int lb, size_t cb) {
 }
 
 template <typename T, int N>
-static cudaError_t zr_launch(const TmaMaps* t, int ncomp, long long lines, const c2<T>* tw, int* err,
-                             cudaStream_t st) {
+static cudaError_t zr_launch(const TmaMaps* t, int ncomp, long long lines, const c2<T>* tw, const IterIn& it,
+                             int* err, cudaStream_t st) {
   constexpr int LB = lb_z<T>(N);
   const size_t sm = zr_smem(N, LB, sizeof(c2<T>));
   auto k = fft_zr_tma_kernel<T, N, LB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((unsigned)((lines + LB - 1) / LB), ncomp);
-  k<<<grid, NT, sm, st>>>(t->real_sig, t->spec_z, tw, err);
+  k<<<grid, NT, sm, st>>>(t->real_sig, t->spec_z, tw, it, err);
   return cudaGetLastError();
 }
 
 template <typename T, int N>
 static cudaError_t zc_launch(const CUtensorMap& ms, const CUtensorMap& mr, int ncomp, long long lines,
-                             const c2<T>* tw, T scale, const AddVec& add, int mode, int* err, cudaStream_t st) {
+                             const c2<T>* tw, T scale, const IterIn& it, int mode, int* err, cudaStream_t st) {
   constexpr int LB = lb_z<T>(N);
   const size_t sm = zc_smem(N, LB, sizeof(c2<T>));
   dim3 grid((unsigned)((lines + LB - 1) / LB), ncomp);
   if (mode) {
     auto k = fft_zc_tma_kernel<T, N, LB, 1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, add, err);
+    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, it, err);
   } else {
     auto k = fft_zc_tma_kernel<T, N, LB, 0>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, add, err);
+    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, it, err);
   }
   return cudaGetLastError();
 }
 
 template <typename T, int L>
 static cudaError_t s_launch(const CUtensorMap& m, int axis, int ncomp, int nouter, int kzs, int sign,
-                            const c2<T>* tw, int* err, cudaStream_t st) {
+                            const c2<T>* tw, const IterIn& it, int* err, cudaStream_t st) {
   constexpr int KB = kb_strided<T>();
   const size_t sm = (size_t)L * KB * sizeof(c2<T>);
   dim3 grid((kzs + KB - 1) / KB, nouter, ncomp);
   if (sign < 0) {
     auto k = fft_s_tma_kernel<T, L, KB, -1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(m, axis, tw, err);
+    k<<<grid, NT, sm, st>>>(m, axis, tw, it, err);
   } else {
     auto k = fft_s_tma_kernel<T, L, KB, +1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(m, axis, tw, err);
+    k<<<grid, NT, sm, st>>>(m, axis, tw, it, err);
   }
   return cudaGetLastError();
 }
 
 template <typename T, int L>
 static cudaError_t g_launch(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
-                            const c2<T>* twi, int* err, cudaStream_t st) {
+                            const c2<T>* twi, const IterIn& it, int* err, cudaStream_t st) {
   constexpr int KB = kb_green<T>();
   const size_t sm = (size_t)9 * L * KB * sizeof(c2<T>);
   auto k = fft_xg_tma_kernel<T, L, KB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kzs + KB - 1) / KB, g.n1);
-  k<<<grid, NT, sm, st>>>(gc, t->spec_g, t->anti_g, g.n1, g.n2, g.kz, twf, twi, err);
+  k<<<grid, NT, sm, st>>>(gc, t->spec_g, t->anti_g, g.n1, g.n2, g.kz, twf, twi, it, err);
   return cudaGetLastError();
 }
 
 #define MTH_TMA_SIZES(X) X(16) X(32) X(48) X(64) X(96) X(128) X(256)
 
 template <typename T>
-cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, int* err, cudaStream_t st) {
+cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, const IterIn& it, int* err,
+                          cudaStream_t st) {
   const long long lines = (long long)g.n0 * g.n1;
   switch (g.n2) {
-#define MTH_CASE(N) case N: return zr_launch<T, N>(t, 6, lines, tw, err, st);
+#define MTH_CASE(N) case N: return zr_launch<T, N>(t, 6, lines, tw, it, err, st);
     MTH_TMA_SIZES(MTH_CASE)
 #undef MTH_CASE
     default: return cudaErrorInvalidValue;
@@ -520,14 +525,14 @@ cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, i
 // which = 0: stress spectrum -> strain field (mode 1); 1: spin spectrum ->
 // spin field (mode 0)
 template <typename T>
-cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const AddVec& add,
+cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const IterIn& it,
                           int* err, cudaStream_t st) {
   const long long lines = (long long)g.n0 * g.n1;
   const CUtensorMap& ms = which ? t->anti_z : t->spec_z;
   const CUtensorMap& mr = which ? t->real_wspin : t->real_strain;
   const int ncomp = which ? 3 : 6, mode = which ? 0 : 1;
   switch (g.n2) {
-#define MTH_CASE(N) case N: return zc_launch<T, N>(ms, mr, ncomp, lines, tw, scale, add, mode, err, st);
+#define MTH_CASE(N) case N: return zc_launch<T, N>(ms, mr, ncomp, lines, tw, scale, it, mode, err, st);
     MTH_TMA_SIZES(MTH_CASE)
 #undef MTH_CASE
     default: return cudaErrorInvalidValue;
@@ -537,14 +542,14 @@ cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c
 // which = 0: stress spectrum along y; 1: spin spectrum along y; 2: spin
 // spectrum along x
 template <typename T>
-cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int sign, const c2<T>* tw, int* err,
-                            cudaStream_t st) {
+cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int sign, const c2<T>* tw,
+                            const IterIn& it, int* err, cudaStream_t st) {
   const CUtensorMap& m = which == 0 ? t->spec_y : which == 1 ? t->anti_y : t->anti_x;
   const int axis = which == 2 ? 0 : 1;
   const int L = axis == 1 ? g.n1 : g.n0, nouter = axis == 1 ? g.n0 : g.n1;
   const int ncomp = which == 0 ? 6 : 3;
   switch (L) {
-#define MTH_CASE(N) case N: return s_launch<T, N>(m, axis, ncomp, nouter, g.kzs, sign, tw, err, st);
+#define MTH_CASE(N) case N: return s_launch<T, N>(m, axis, ncomp, nouter, g.kzs, sign, tw, it, err, st);
     MTH_TMA_SIZES(MTH_CASE)
 #undef MTH_CASE
     default: return cudaErrorInvalidValue;
@@ -553,9 +558,9 @@ cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int s
 
 template <typename T>
 cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
-                            const c2<T>* twi, int* err, cudaStream_t st) {
+                            const c2<T>* twi, const IterIn& it, int* err, cudaStream_t st) {
   switch (g.n0) {
-#define MTH_CASE(N) case N: return g_launch<T, N>(t, g, gc, twf, twi, err, st);
+#define MTH_CASE(N) case N: return g_launch<T, N>(t, g, gc, twf, twi, it, err, st);
     MTH_TMA_SIZES(MTH_CASE)
 #undef MTH_CASE
     default: return cudaErrorInvalidValue;
@@ -564,13 +569,14 @@ cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst
 
 #define INST(T)                                                                                                    \
   template TmaMaps* tma_create<T>(const FftGeom&, T*, T*, T*, c2<T>*, c2<T>*);                                     \
-  template cudaError_t tma_fft_z_r2c<T>(const TmaMaps*, const FftGeom&, const c2<T>*, int*, cudaStream_t);         \
-  template cudaError_t tma_fft_z_c2r<T>(const TmaMaps*, const FftGeom&, int, const c2<T>*, T, const AddVec&, int*, \
+  template cudaError_t tma_fft_z_r2c<T>(const TmaMaps*, const FftGeom&, const c2<T>*, const IterIn&, int*,        \
                                         cudaStream_t);                                                             \
-  template cudaError_t tma_fft_strided<T>(const TmaMaps*, const FftGeom&, int, int, const c2<T>*, int*,            \
-                                          cudaStream_t);                                                           \
+  template cudaError_t tma_fft_z_c2r<T>(const TmaMaps*, const FftGeom&, int, const c2<T>*, T, const IterIn&, int*, \
+                                        cudaStream_t);                                                             \
+  template cudaError_t tma_fft_strided<T>(const TmaMaps*, const FftGeom&, int, int, const c2<T>*, const IterIn&,   \
+                                          int*, cudaStream_t);                                                     \
   template cudaError_t tma_fft_x_green<T>(const TmaMaps*, const FftGeom&, const GreenConst&, const c2<T>*,         \
-                                          const c2<T>*, int*, cudaStream_t);
+                                          const c2<T>*, const IterIn&, int*, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

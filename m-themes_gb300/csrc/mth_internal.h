@@ -24,6 +24,17 @@ struct FftGeom {
 
 struct AddVec { double v[6]; };
 
+// Per-iteration inputs of the Green-iteration kernels, read from device
+// memory so that a captured graph replays unchanged: the uniform strain
+// increment added by the inverse z pass (6 doubles, LT basis; null: none)
+// and the live flag of the volume (null: live; 0: the kernels return at
+// once, which switches a converged volume of a batch off).
+struct IterIn {
+  const double* add;
+  const int* live;
+};
+__device__ __forceinline__ bool is_live(const IterIn& in) { return !in.live || *in.live; }
+
 // Green-operator constants, passed by value (kernel parameter space).
 struct GreenConst {
   double c0[81];      // C0_ijkl (chg_basis of C066, src/init.c:376)
@@ -62,28 +73,30 @@ TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, 
 void tma_destroy(TmaMaps* t);
 bool tma_has(const TmaMaps* t, int pass);
 template <typename T>
-cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, int* err, cudaStream_t st);
+cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, const IterIn& it, int* err,
+                          cudaStream_t st);
 template <typename T>
-cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const AddVec& add,
+cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const IterIn& it,
                           int* err, cudaStream_t st);
 template <typename T>
-cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int sign, const c2<T>* tw, int* err,
-                            cudaStream_t st);
+cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int sign, const c2<T>* tw,
+                            const IterIn& it, int* err, cudaStream_t st);
 template <typename T>
 cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
-                            const c2<T>* twi, int* err, cudaStream_t st);
+                            const c2<T>* twi, const IterIn& it, int* err, cudaStream_t st);
 
 template <typename T>
-cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, cudaStream_t st);
+cudaError_t launch_fft_z_r2c(const FftGeom& g, const T* in, c2<T>* out, int ncomp, const c2<T>* tw, const IterIn& it,
+                             cudaStream_t st);
 template <typename T>
 cudaError_t launch_fft_z_c2r(const FftGeom& g, const c2<T>* spec, T* field, int ncomp, const c2<T>* tw, T scale,
-                             const AddVec& add, int mode, cudaStream_t st);
+                             const IterIn& it, int mode, cudaStream_t st);
 template <typename T>
 cudaError_t launch_fft_strided(const FftGeom& g, c2<T>* spec, int ncomp, int axis, int sign, const c2<T>* tw,
-                               cudaStream_t st);
+                               const IterIn& it, cudaStream_t st);
 template <typename T>
 cudaError_t launch_fft_x_green(const FftGeom& g, const GreenConst& gc, c2<T>* spec, c2<T>* anti, const c2<T>* twf,
-                               const c2<T>* twi, cudaStream_t st);
+                               const c2<T>* twi, const IterIn& it, cudaStream_t st);
 
 // Per-voxel field pointers of one RVE; TSt is the storage type.
 template <typename TSt>
@@ -121,6 +134,7 @@ constexpr int NPART = 16;   // err_s, err_e, sig[6], sig_ph1[6], newton_iters, n
 constexpr int NPART_END = 12;  // epsp[6], edot[6]
 
 cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
+                          const IterIn& it,
                           cudaStream_t st);
 cudaError_t launch_end_step(int mixed, const NewtonConst& nc, const void* fields, const double anti_uniform[3],
                             int do_orient, int do_harden, double* partials, int nblocks, cudaStream_t st);
@@ -167,6 +181,7 @@ long long noalloc_max_voxels();
 cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,
                                        const double* strain, const double* rot, const double* crss, double* edot,
                                        double* err, long long* iters_host, cudaStream_t st);
-cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, cudaStream_t st);
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
+                                   cudaStream_t st);
 
 }  // namespace mth

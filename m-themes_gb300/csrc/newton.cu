@@ -53,11 +53,13 @@ __device__ __forceinline__ const float* cpick_ptr<float>(const double*, const fl
 template <>
 __device__ __forceinline__ const double* cpick_ptr<double>(const double* d, const float*) { return d; }
 
-// Flow rule in crystal axes at deviatoric stress x (5).  Returns edot (5),
-// optional Hessian contribution D (15, packed upper triangle) and psi.
+// Flow rule in crystal axes at deviatoric stress x (5).  itf: inverse
+// forward CRSS per system; the backward CRSS is forward + tau_off.  Returns
+// edot (5), optional Hessian contribution D (15, packed upper triangle) and
+// psi = sum gamd0 tau |r|^(n+1)/(n+1) = sum gamd0 |rss| |r|^n/(n+1).
 // gam (optional) receives the shear rates.
 template <typename TF, bool WANT_D>
-__device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], const TF* tauf, TF tau_off, TF ed[5],
+__device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], const TF* itf, TF tau_off, TF ed[5],
                                           TF D[15], TF& psi, TF* gam) {
 #pragma unroll
   for (int i = 0; i < 5; i++) ed[i] = 0;
@@ -79,8 +81,8 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
 #pragma unroll
       for (int i = 0; i < 5; i++) m[i] = cpick<TF>(ph.m_xt[s][i], ph.m_xtf[s][i]);
       const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
-      const TF tau = rss < (TF)0 ? tauf[s] + tau_off : tauf[s];
-      const TF itau = (TF)1 / tau;
+      TF itau = itf[s];
+      if (tau_off != (TF)0 && rss < (TF)0) itau = itau / ((TF)1 + tau_off * itau);   // 1/(tau_f + tau_off)
       const TF r = rss * itau;
       const TF ar = fabs(r);
       const TF pnm1 = pow_abs<TF>(ar, nm1, n - (TF)1);   // |r|^(n-1)
@@ -97,7 +99,7 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
 #pragma unroll
           for (int j = i; j < 5; j++) D[q++] += w * m[i] * m[j];
       }
-      psi += g0 * tau * pn * ar * inv_np1;
+      psi += g0 * fabs(rss) * pn * inv_np1;
     } else if (gam) {
       gam[s] = 0;
     }
@@ -192,7 +194,7 @@ struct VoxelOut {
 // Local solve of one crystal voxel.  lam6/eps6/ep6: LT sample-frame inputs
 // (lambda = current stress, total strain, plastic strain); Q: sample->crystal
 // 5x5 of the current lattice orientation; et: elastic-class row (initial
-// orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
+// orientation); itf: inverse forward CRSS.  Outputs sig6 (sample frame) and ed6
 // (plastic strain rate, sample frame).
 // TF: flow rule, residual, Hessian assembly, line search and frame
 // transforms; TL: accuracy of the Jacobian (Hessian) solve.  FP64 mode: both
@@ -204,7 +206,7 @@ struct VoxelOut {
 // mode: all float.
 template <typename TF, typename TL>
 __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const TF* __restrict__ et,
-                                const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* tauf, TF* sig6,
+                                const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* itf, TF* sig6,
                                 TF* ed6) {
   VoxelOut o = {0.0, 0.0, 0, 0};
   const TF dt = cpick<TF>(nc.dt, nc.dtf);
@@ -284,7 +286,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       for (int i = 0; i < 15; i++) Df[i] = 0;
       psif = 0;
     } else {
-      flow_rule<TF, true>(ph, x, tauf, tau_off, edf, Df, psif, nullptr);
+      flow_rule<TF, true>(ph, x, itf, tau_off, edf, Df, psif, nullptr);
     }
     TF g[5], Kx[5];
     symv5<TF>(K, x, Kx);
@@ -323,7 +325,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
         for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
         TF edt[5], psit;
-        flow_rule<TF, false>(ph, xt, tauf, tau_off, edt, nullptr, psit, nullptr);
+        flow_rule<TF, false>(ph, xt, itf, tau_off, edt, nullptr, psit, nullptr);
         TF Kxt[5];
         symv5<TF>(K, xt, Kxt);
         TF phi = 0;
@@ -355,7 +357,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
     for (int i = 0; i < 5; i++) edx[i] = 0;
   } else {
-    flow_rule<TF, false>(ph, x, tauf, tau_off, edx, nullptr, psid, nullptr);
+    flow_rule<TF, false>(ph, x, itf, tau_off, edx, nullptr, psid, nullptr);
   }
   // back to sample axes: s = Q^T x, edot = Q^T edot_x
   TF ss[5], es[5];
@@ -454,7 +456,9 @@ __device__ __forceinline__ void block_reduce_smem(const TV (&v)[W], double* out)
 
 // ------------------------------------------------------------ Newton kernel
 template <typename TSt, typename TF, typename TS, int MINB>
-__global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials) {
+__global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials,
+                                                                IterIn it) {
+  if (!is_live(it)) return;
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   TF acc[NPART];
@@ -474,7 +478,7 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
 #pragma unroll
       for (int i = 0; i < 9; i++) R[i] = (TF)f.rot[i * P + v];
 #pragma unroll
-      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)1 / (TF)f.crss[s * P + v] : (TF)1;   // inverse
       rot_to_q<TF>(R, Q);
       TF s6[6], e6[6];
       const TF* et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
@@ -520,18 +524,18 @@ void fill_float_consts(NewtonConst& nc) {
 }
 
 cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* fields, double* partials, int nblocks,
-                          cudaStream_t st) {
+                          const IterIn& it, cudaStream_t st) {
   NewtonConst nc = nc_in;
   fill_float_consts(nc);
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, float, 2><<<nblocks, 256, 0, st>>>(nc, f, partials);
+    newton_kernel<float, float, float, 2><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double, 2><<<nblocks, 256, 0, st>>>(nc, f, partials);
+    newton_kernel<float, float, double, 2><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials);
+    newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   }
   return cudaGetLastError();
 }
@@ -580,7 +584,12 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       }
 #pragma unroll
       for (int s = 0; s < NSYS; s++) gam[s] = 0;
-      if (!nc.flow_off) flow_rule<TF, false>(ph, x, tauf, (TF)ph.tau_back_minus_fwd, ed, nullptr, psi, gam);
+      if (!nc.flow_off) {
+        TF itf[NSYS];
+#pragma unroll
+        for (int s = 0; s < NSYS; s++) itf[s] = (TF)1 / tauf[s];
+        flow_rule<TF, false>(ph, x, itf, (TF)ph.tau_back_minus_fwd, ed, nullptr, psi, gam);
+      }
       if (do_orient) {
         // plastic spin: RotSlip = -1/2 T sum_a gam_a (b_a x n_a)
         TF cx = 0, cy = 0, cz = 0;
@@ -762,7 +771,7 @@ __global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, 
     ep6[i] = epsp[6 * v + i];
   }
   for (int i = 0; i < 9; i++) R[i] = rot[9 * v + i];
-  for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? crss[NSYS * v + s] : 1.0;
+  for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? 1.0 / crss[NSYS * v + s] : 1.0;   // inverse
   rot_to_q<double>(R, Q);
   VoxelOut o = solve_voxel<double, double>(nc, ph, Q, etab + (size_t)v * ETAB_W, lam6, eps6, ep6, tauf, s6, e6);
   for (int i = 0; i < 6; i++) {
@@ -785,7 +794,8 @@ cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, 
 // --------------------------------------------------- deterministic reduction
 // out[w] = sum over blocks (fixed order) of partials[b*width + w].
 __global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, int width,
-                                       double* __restrict__ out) {
+                                       double* __restrict__ out, IterIn it) {
+  if (!is_live(it)) return;
   __shared__ double sm[256];
   for (int w = blockIdx.x; w < width; w += gridDim.x) {
     double a = 0;
@@ -801,8 +811,9 @@ __global__ void reduce_partials_kernel(const double* __restrict__ partials, int 
   }
 }
 
-cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, cudaStream_t st) {
-  reduce_partials_kernel<<<width, 256, 0, st>>>(partials, nblocks, width, out);
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
+                                   cudaStream_t st) {
+  reduce_partials_kernel<<<width, 256, 0, st>>>(partials, nblocks, width, out, it);
   return cudaGetLastError();
 }
 
@@ -837,7 +848,7 @@ __global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonCo
       ep6[i] = epsp[6 * v + i];
     }
     for (int i = 0; i < 9; i++) R[i] = rot[9 * v + i];
-    for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? crss[NSYS * v + s] : 1.0;
+    for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? 1.0 / crss[NSYS * v + s] : 1.0;   // inverse
     rot_to_q<double>(R, Q);
     // elastic row of this voxel: S_gr = Q^T diag(s_xt) Q, S_tot = S0 + S_gr
     for (int i = 0; i < 5; i++)

@@ -191,6 +191,12 @@ def load(path: str | None = None):
     lib.mth_read_sx.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_int]
     lib.mth_read_microstructure.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
+    lib.mth_batch_create.argtypes = [C.POINTER(MthParams), C.c_int, C.POINTER(C.c_void_p)]
+    lib.mth_batch_upload.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double), C.c_size_t]
+    lib.mth_batch_step.argtypes = [C.c_void_p, C.POINTER(MthStepReport)]
+    lib.mth_batch_download_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_size_t]
+    lib.mth_batch_destroy.argtypes = [C.c_void_p]
     if path is None:
         _lib = lib
     return lib

@@ -80,3 +80,55 @@ def local_solve(params, c066, sig, eps_p, strain, rot, crss):
                                         capi._dptr(a[2]), capi._dptr(a[3]), capi._dptr(a[4]), capi._dptr(edot),
                                         capi._dptr(err), C.byref(it)))
     return sig, edot, err, it.value
+
+
+class Batch:
+    """Independent RVEs advanced together on one GPU (mth_batch_*): members
+    may differ in grid size, material and loading.  `step()` returns one
+    report per member; results equal those of a `Solver` per member."""
+
+    def __init__(self, params_list, microstructures):
+        self.lib = capi.load()
+        self.n = len(params_list)
+        arr = (capi.MthParams * self.n)(*params_list)
+        self.nv = [int(np.prod(list(p.cell_dim))) for p in params_list]
+        b = C.c_void_p()
+        capi.check(self.lib, self.lib.mth_batch_create(arr, self.n, C.byref(b)))
+        self.b = b
+        for i, (grain, phase, euler) in enumerate(microstructures):
+            g = np.ascontiguousarray(grain, dtype=np.int32)
+            p = np.ascontiguousarray(phase, dtype=np.int32)
+            e = np.ascontiguousarray(euler, dtype=np.float64)
+            if g.size != self.nv[i] or p.size != self.nv[i] or e.size != 3 * self.nv[i]:
+                self.close()
+                raise ValueError(f"microstructure {i} does not match its cell_dim")
+            capi.check(self.lib, self.lib.mth_batch_upload(self.b, i, capi._iptr(g), capi._iptr(p), capi._dptr(e),
+                                                           self.nv[i]))
+
+    def step(self) -> list:
+        reps = (capi.MthStepReport * self.n)()
+        capi.check(self.lib, self.lib.mth_batch_step(self.b, reps))
+        return [r.to_dict() for r in reps]
+
+    def field(self, i: int, name: str) -> np.ndarray:
+        f = capi.FIELD[name]
+        out = np.zeros(self.nv[i] * capi.FIELD_NCOMP[f])
+        capi.check(self.lib, self.lib.mth_batch_download_field(self.b, i, f, capi._dptr(out), out.size))
+        return out.reshape(self.nv[i], -1)
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.mth_batch_destroy(self.b)
+            self.b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -303,3 +303,26 @@ def workload(name: str) -> Config:
         return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
                       n_steps=100, seed=20240103)
     raise KeyError(name)
+
+
+def batch_workload(name: str = "c3", master_seed: int = 20240106) -> list:
+    """Batched-RVE workloads.  'c3': 64 independent RVEs, 24 x 32^3, 24 x 48^3
+    and 16 x 64^3; RVE i has seed master + i, a grain count drawn uniformly
+    from [32, 256], uniform orientations, tau0 ~ U[12, 20] MPa (forward and
+    backward CRSS) and n drawn from {8, 10, 15, 20}; uniaxial tension for 50
+    steps of 1e-3.  'c3s': the first 2 RVEs of each size (6), for tests."""
+    sizes = [32] * 24 + [48] * 24 + [64] * 16
+    if name == "c3s":
+        sizes = [32, 32, 48, 48, 64, 64]
+    elif name != "c3":
+        raise KeyError(name)
+    out = []
+    for i, n in enumerate(sizes):
+        seed = master_seed + i
+        rng = np.random.default_rng(seed)
+        n_grains = int(rng.integers(32, 257))
+        tau0 = float(rng.uniform(12.0, 20.0))
+        nrs = float(rng.choice([8.0, 10.0, 15.0, 20.0]))
+        mat = Material(tau0f=tau0, tau0b=tau0, nrs=nrs)
+        out.append(Config(cell_dim=(n, n, n), n_grains=n_grains, n_steps=50, seed=seed, material=mat))
+    return out

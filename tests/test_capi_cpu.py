@@ -99,3 +99,21 @@ def test_null_arguments(lib):
     assert lib.mth_create(None, None) == 1
     assert lib.mth_step(None, None) == 1
     assert lib.mth_destroy(None) == 1
+
+
+def test_batch_argument_checks(lib):
+    """Batch arguments are checked before any device call."""
+    out = C.c_void_p()
+    assert lib.mth_batch_create(None, 1, C.byref(out)) == 1
+    p = (capi.MthParams * 2)(capi.params_from_config(synth.Config(cell_dim=(8, 8, 8))),
+                             capi.params_from_config(synth.Config(cell_dim=(16, 16, 16))))
+    assert lib.mth_batch_create(p, 0, C.byref(out)) == 1
+    p[1].device = 1                                   # members on different devices
+    assert lib.mth_batch_create(p, 2, C.byref(out)) == 1
+    p[1].device = 0
+    p[1].pf_substeps = 10                             # recrystallisation in a member
+    assert lib.mth_batch_create(p, 2, C.byref(out)) == 10
+    assert not out.value
+    assert lib.mth_batch_step(None, None) == 1
+    assert lib.mth_batch_destroy(None) == 1
+    assert lib.mth_batch_upload(None, 0, None, None, None, 0) == 1

@@ -1,0 +1,68 @@
+"""Batched RVEs (mth_batch_*) against one Solver per member: uneven grid
+sizes, per-member material and precision, members converging at different
+Green iterations."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import rel
+from mth import Batch, Solver, capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _members(precision):
+    cfgs = [
+        synth.Config(cell_dim=(16, 16, 16), n_grains=6, n_steps=3, seed=301, iter_max=40),
+        synth.Config(cell_dim=(32, 16, 48), n_grains=9, n_steps=3, seed=302, iter_max=40,
+                     material=synth.Material(tau0f=12.5, tau0b=12.5, nrs=20.0)),
+        synth.Config(cell_dim=(8, 8, 8), n_grains=3, n_steps=3, seed=303, iter_max=40, n_pores=1, pore_radius=1,
+                     material=synth.Material(tau0f=19.0, tau0b=19.0, nrs=8.0)),
+        # nearly elastic: converges before IterMax
+        synth.Config(cell_dim=(24, 24, 24), n_grains=5, n_steps=3, seed=304, iter_max=40, err=1e-4,
+                     material=synth.Material(tau0f=400.0, tau0b=400.0)),
+        # single crystal: equilibrium after one Green iteration
+        synth.Config(cell_dim=(16, 32, 16), n_grains=1, n_steps=3, seed=305, iter_max=40, err=2e-3),
+    ]
+    params = [capi.params_from_config(c, precision=precision) for c in cfgs]
+    micro = [synth.microstructure(c) for c in cfgs]
+    return cfgs, params, micro
+
+
+@pytest.mark.parametrize("precision,tol", [(capi.MTH_FP64, 1e-9), (capi.MTH_MIXED, 2e-5)])
+def test_batch_matches_single_solvers(precision, tol):
+    cfgs, params, micro = _members(precision)
+    ref = []
+    for p, m in zip(params, micro):
+        s = Solver(p, *m)
+        ref.append(([s.step() for _ in range(3)], s.field("sig")))
+        s.close()
+    with Batch(params, micro) as b:
+        reps = [b.step() for _ in range(3)]
+        sig = [b.field(i, "sig") for i in range(len(cfgs))]
+    its = set()
+    for i in range(len(cfgs)):
+        for k in range(3):
+            a, r = reps[k][i], ref[i][0][k]
+            assert a["iterations"] == r["iterations"], (i, k)
+            assert rel(a["sig_avg"], r["sig_avg"]) < tol, (i, k)
+            assert rel(a["disgrad_avg"], r["disgrad_avg"]) < tol, (i, k)
+            its.add(a["iterations"])
+        assert rel(sig[i], ref[i][1]) < 100 * tol
+    assert len(its) > 1   # members stopped at different Green iterations
+
+
+def test_batch_workload_small():
+    """The 6-member slice of the 64-RVE workload: steps run, reports finite,
+    the imposed strain rate reached by every member."""
+    cfgs = synth.batch_workload("c3s")
+    params = [capi.params_from_config(c, precision=capi.MTH_MIXED) for c in cfgs]
+    micro = [synth.microstructure(c) for c in cfgs]
+    with Batch(params, micro) as b:
+        for k in range(2):
+            reps = b.step()
+            for c, r in zip(cfgs, reps):
+                assert np.all(np.isfinite(r["sig_avg"]))
+                assert abs(r["disgrad_avg"][2, 2] - (k + 1) * c.time_step) < 1e-12
+                assert 1 <= r["iterations"] <= c.iter_max
