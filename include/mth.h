@@ -216,6 +216,32 @@ mth_status mth_local_solve_noalloc(const mth_params* params, const double c066[3
                                    const double* d_rot, const double* d_crss, double* d_edot,
                                    double* d_err, long long* newton_iters, void* stream);
 
+/* Field files in the format of the reference's writers (src/io.c:247-541):
+ * raw native values, no header, voxels in pIDX order (z fastest).
+ *   MTH_IOUT_SIG, _EPS (plastic strain), _EDOT, _ELS (elastic strain
+ *   sym(grad u) - eps_p, WriteElsMPI): six files "<prefix>_<c>_S<step>.iout"
+ *   of doubles, c = 1..6 for the components 11, 22, 33, 23, 13, 12;
+ *   MTH_IOUT_GRAIN: "<prefix>_S<step>.iout", int32 grain ids (WriteGrainMPI);
+ *   MTH_IOUT_TEXTURE: "<prefix>_S<step>.iout", 48-byte records {double
+ *   Bunge angles in degrees [3]; int 1-based coordinates [3]; int grain;
+ *   int phase; int 0} (WriteTextureMPI).
+ * <step> is printed with 6 digits (%06d).  The fields are copied on the
+ * device when mth_write_iout is called (in order with the context's work);
+ * the copy to the host, the conversion and the file writes run on a
+ * background thread while the caller continues.  One write is in flight per
+ * context: the next mth_write_iout waits for the previous one and returns
+ * its error if it failed; mth_iout_wait waits and returns the status. */
+typedef enum {
+  MTH_IOUT_SIG = 0,
+  MTH_IOUT_EPS = 1,
+  MTH_IOUT_EDOT = 2,
+  MTH_IOUT_ELS = 3,
+  MTH_IOUT_GRAIN = 4,
+  MTH_IOUT_TEXTURE = 5
+} mth_iout_kind;
+mth_status mth_write_iout(mth_ctx* ctx, int kind, const char* prefix, int step);
+mth_status mth_iout_wait(mth_ctx* ctx);
+
 /* Batches of independent volumes (RVEs) on one GPU.  Each member has its own
  * parameters (material, loading, precision), microstructure and grid size;
  * mth_batch_step advances every member by one mechanical step, with the same

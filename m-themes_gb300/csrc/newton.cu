@@ -53,13 +53,13 @@ __device__ __forceinline__ const float* cpick_ptr<float>(const double*, const fl
 template <>
 __device__ __forceinline__ const double* cpick_ptr<double>(const double* d, const float*) { return d; }
 
-// Flow rule in crystal axes at deviatoric stress x (5).  itf: inverse
-// forward CRSS per system; the backward CRSS is forward + tau_off.  Returns
-// edot (5), optional Hessian contribution D (15, packed upper triangle) and
+// Flow rule in crystal axes at deviatoric stress x (5).  tauf: forward CRSS
+// per system; the backward CRSS is forward + tau_off.  Returns edot (5),
+// optional Hessian contribution D (15, packed upper triangle) and
 // psi = sum gamd0 tau |r|^(n+1)/(n+1) = sum gamd0 |rss| |r|^n/(n+1).
 // gam (optional) receives the shear rates.
 template <typename TF, bool WANT_D>
-__device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], const TF* itf, TF tau_off, TF ed[5],
+__device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], const TF* tauf, TF tau_off, TF ed[5],
                                           TF D[15], TF& psi, TF* gam) {
 #pragma unroll
   for (int i = 0; i < 5; i++) ed[i] = 0;
@@ -81,8 +81,8 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
 #pragma unroll
       for (int i = 0; i < 5; i++) m[i] = cpick<TF>(ph.m_xt[s][i], ph.m_xtf[s][i]);
       const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
-      TF itau = itf[s];
-      if (tau_off != (TF)0 && rss < (TF)0) itau = itau / ((TF)1 + tau_off * itau);   // 1/(tau_f + tau_off)
+      const TF tau = rss < (TF)0 ? tauf[s] + tau_off : tauf[s];
+      const TF itau = (TF)1 / tau;
       const TF r = rss * itau;
       const TF ar = fabs(r);
       const TF pnm1 = pow_abs<TF>(ar, nm1, n - (TF)1);   // |r|^(n-1)
@@ -194,7 +194,7 @@ struct VoxelOut {
 // Local solve of one crystal voxel.  lam6/eps6/ep6: LT sample-frame inputs
 // (lambda = current stress, total strain, plastic strain); Q: sample->crystal
 // 5x5 of the current lattice orientation; et: elastic-class row (initial
-// orientation); itf: inverse forward CRSS.  Outputs sig6 (sample frame) and ed6
+// orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
 // (plastic strain rate, sample frame).
 // TF: flow rule, residual, Hessian assembly, line search and frame
 // transforms; TL: accuracy of the Jacobian (Hessian) solve.  FP64 mode: both
@@ -204,14 +204,27 @@ struct VoxelOut {
 // early steps, whose direction only has to be a descent direction, use the
 // FP32 factorisation (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
 // mode: all float.
-template <typename TF, typename TL>
-__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF Q[25], const TF* __restrict__ et,
-                                const TF lam6[6], const TF eps6[6], const TF ep6[6], const TF* itf, TF* sig6,
-                                TF* ed6) {
+// load(lam6, eps6, ep6, R, again) fills the voxel's inputs; it is called
+// at the start and again (again = true: loads the compiler may not merge
+// with the first) for the back-transform and the error norms, so neither
+// the inputs nor the 5x5 frame rotation stay live across the Newton loop.
+template <typename TF, typename TL, typename Load>
+__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const TF* tauf,
+                                const Load& load, TF* sig6, TF* ed6) {
   VoxelOut o = {0.0, 0.0, 0, 0};
   const TF dt = cpick<TF>(nc.dt, nc.dtf);
+  TF x[5], c[5], K[15];
+  TF h, ref2, dh;
+  const TF shh = et[ET_SEL_HH];
+  {
+  TF lam6[6], eps6[6], ep6[6], Q[25];
+  {
+    TF R[9];
+    load(lam6, eps6, ep6, R, false);
+    rot_to_q<TF>(R, Q);
+  }
   // crystal-frame inputs
-  TF lamx[5], epsx[5], epx[5], s0s[5], c[5];
+  TF lamx[5], epsx[5], epx[5], s0s[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) {
     TF a = 0;
@@ -233,7 +246,6 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
     c[i] = -d + e - b;   // gradient of Phi = K x + c + dt edot
   }
   // Hessian base K = Q (S0 + S_gr) Q^T in crystal axes of the current lattice
-  TF K[15];
   {
     TF St[25], t[25];
 #pragma unroll
@@ -260,18 +272,17 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       }
   }
   // hydrostatic part in closed form
-  const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf), shh = et[ET_SEL_HH];
-  const TF h = (s0hh * lam6[5] + eps6[5] - ep6[5]) / (s0hh + shh);
-  TF ref2 = 0;
+  const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf);
+  h = (s0hh * lam6[5] + eps6[5] - ep6[5]) / (s0hh + shh);
+  ref2 = 0;
 #pragma unroll
   for (int i = 0; i < 6; i++) ref2 += lam6[i] * lam6[i];
-  const TF dh = h - lam6[5];
-  const TF tol2 = cpick<TF>(nc.tol, nc.tolf) * cpick<TF>(nc.tol, nc.tolf);
-  const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
-
-  TF x[5];
+  dh = h - lam6[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) x[i] = lamx[i];
+  }
+  const TF tol2 = cpick<TF>(nc.tol, nc.tolf) * cpick<TF>(nc.tol, nc.tolf);
+  const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
   const TF tau_off = cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf);
   int it = 0;
   bool done = false;
@@ -286,7 +297,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       for (int i = 0; i < 15; i++) Df[i] = 0;
       psif = 0;
     } else {
-      flow_rule<TF, true>(ph, x, itf, tau_off, edf, Df, psif, nullptr);
+      flow_rule<TF, true>(ph, x, tauf, tau_off, edf, Df, psif, nullptr);
     }
     TF g[5], Kx[5];
     symv5<TF>(K, x, Kx);
@@ -325,7 +336,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
         for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
         TF edt[5], psit;
-        flow_rule<TF, false>(ph, xt, itf, tau_off, edt, nullptr, psit, nullptr);
+        flow_rule<TF, false>(ph, xt, tauf, tau_off, edt, nullptr, psit, nullptr);
         TF Kxt[5];
         symv5<TF>(K, xt, Kxt);
         TF phi = 0;
@@ -357,7 +368,13 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
     for (int i = 0; i < 5; i++) edx[i] = 0;
   } else {
-    flow_rule<TF, false>(ph, x, itf, tau_off, edx, nullptr, psid, nullptr);
+    flow_rule<TF, false>(ph, x, tauf, tau_off, edx, nullptr, psid, nullptr);
+  }
+  TF lam6[6], eps6[6], ep6[6], Q[25];
+  {
+    TF R[9];
+    load(lam6, eps6, ep6, R, true);
+    rot_to_q<TF>(R, Q);
   }
   // back to sample axes: s = Q^T x, edot = Q^T edot_x
   TF ss[5], es[5];
@@ -454,6 +471,21 @@ __device__ __forceinline__ void block_reduce_smem(const TV (&v)[W], double* out)
   }
 }
 
+// Loads of a global value that the compiler keeps as separate loads (used to
+// re-read a voxel's inputs after the Newton loop instead of holding them).
+__device__ __forceinline__ float ld_again(const float* p) {
+  float v;
+  asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(__cvta_generic_to_global(p)));
+  return v;
+}
+__device__ __forceinline__ double ld_again(const double* p) {
+  double v;
+  asm volatile("ld.global.cg.f64 %0, [%1];" : "=d"(v) : "l"(__cvta_generic_to_global(p)));
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T ld_sel(const T* p, bool again) { return again ? ld_again(p) : *p; }
+
 // ------------------------------------------------------------ Newton kernel
 template <typename TSt, typename TF, typename TS, int MINB>
 __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials,
@@ -468,21 +500,22 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
     const int jph = f.phase[v];
     const PhaseConst& ph = nc.ph[jph];
     if (ph.type == 0) {
-      TF lam6[6], eps6[6], ep6[6], R[9], Q[25], tauf[NSYS];
+      TF tauf[NSYS];
 #pragma unroll
-      for (int i = 0; i < 6; i++) {
-        lam6[i] = (TF)f.sig[i * P + v];
-        eps6[i] = (TF)f.strain[i * P + v];
-        ep6[i] = (TF)f.epsp[i * P + v];
-      }
+      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+      auto load = [&](TF* lam6, TF* eps6, TF* ep6, TF* R, bool again) {
 #pragma unroll
-      for (int i = 0; i < 9; i++) R[i] = (TF)f.rot[i * P + v];
+        for (int i = 0; i < 6; i++) {
+          lam6[i] = (TF)ld_sel(f.sig + i * P + v, again);
+          eps6[i] = (TF)ld_sel(f.strain + i * P + v, again);
+          ep6[i] = (TF)ld_sel(f.epsp + i * P + v, again);
+        }
 #pragma unroll
-      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)1 / (TF)f.crss[s * P + v] : (TF)1;   // inverse
-      rot_to_q<TF>(R, Q);
+        for (int i = 0; i < 9; i++) R[i] = (TF)ld_sel(f.rot + i * P + v, again);
+      };
       TF s6[6], e6[6];
       const TF* et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
-      VoxelOut o = solve_voxel<TF, TS>(nc, ph, Q, et, lam6, eps6, ep6, tauf, s6, e6);
+      VoxelOut o = solve_voxel<TF, TS>(nc, ph, et, tauf, load, s6, e6);
 #pragma unroll
       for (int i = 0; i < 6; i++) {
         f.sig[i * P + v] = (TSt)s6[i];
@@ -529,7 +562,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
   fill_float_consts(nc);
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, float, 2><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    newton_kernel<float, float, float, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     newton_kernel<float, float, double, 2><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
@@ -584,12 +617,7 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       }
 #pragma unroll
       for (int s = 0; s < NSYS; s++) gam[s] = 0;
-      if (!nc.flow_off) {
-        TF itf[NSYS];
-#pragma unroll
-        for (int s = 0; s < NSYS; s++) itf[s] = (TF)1 / tauf[s];
-        flow_rule<TF, false>(ph, x, itf, (TF)ph.tau_back_minus_fwd, ed, nullptr, psi, gam);
-      }
+      if (!nc.flow_off) flow_rule<TF, false>(ph, x, tauf, (TF)ph.tau_back_minus_fwd, ed, nullptr, psi, gam);
       if (do_orient) {
         // plastic spin: RotSlip = -1/2 T sum_a gam_a (b_a x n_a)
         TF cx = 0, cy = 0, cz = 0;
@@ -764,16 +792,19 @@ __global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, 
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   const PhaseConst& ph = nc.ph[0];
-  double lam6[6], eps6[6], ep6[6], R[9], Q[25], tauf[NSYS], s6[6], e6[6];
+  double lam6[6], eps6[6], ep6[6], R[9], tauf[NSYS], s6[6], e6[6];
   for (int i = 0; i < 6; i++) {
     lam6[i] = sig[6 * v + i];
     eps6[i] = strain[6 * v + i];
     ep6[i] = epsp[6 * v + i];
   }
   for (int i = 0; i < 9; i++) R[i] = rot[9 * v + i];
-  for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? 1.0 / crss[NSYS * v + s] : 1.0;   // inverse
-  rot_to_q<double>(R, Q);
-  VoxelOut o = solve_voxel<double, double>(nc, ph, Q, etab + (size_t)v * ETAB_W, lam6, eps6, ep6, tauf, s6, e6);
+  for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? crss[NSYS * v + s] : 1.0;
+  auto load = [&](double* l, double* e, double* q, double* r, bool) {
+    for (int i = 0; i < 6; i++) { l[i] = lam6[i]; e[i] = eps6[i]; q[i] = ep6[i]; }
+    for (int i = 0; i < 9; i++) r[i] = R[i];
+  };
+  VoxelOut o = solve_voxel<double, double>(nc, ph, etab + (size_t)v * ETAB_W, tauf, load, s6, e6);
   for (int i = 0; i < 6; i++) {
     sig[6 * v + i] = s6[i];
     edot[6 * v + i] = e6[i];
@@ -848,7 +879,7 @@ __global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonCo
       ep6[i] = epsp[6 * v + i];
     }
     for (int i = 0; i < 9; i++) R[i] = rot[9 * v + i];
-    for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? 1.0 / crss[NSYS * v + s] : 1.0;   // inverse
+    for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? crss[NSYS * v + s] : 1.0;
     rot_to_q<double>(R, Q);
     // elastic row of this voxel: S_gr = Q^T diag(s_xt) Q, S_tot = S0 + S_gr
     for (int i = 0; i < 5; i++)
@@ -859,7 +890,11 @@ __global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonCo
         et[ET_STOT + pk(i, j)] = nc.s0dev[i * 5 + j] + sg;
       }
     et[ET_SEL_HH] = ph.s_xt[5];
-    VoxelOut o = solve_voxel<double, double>(nc, ph, Q, et, lam6, eps6, ep6, tauf, s6, e6);
+    auto load = [&](double* l, double* e, double* q, double* r, bool) {
+      for (int i = 0; i < 6; i++) { l[i] = lam6[i]; e[i] = eps6[i]; q[i] = ep6[i]; }
+      for (int i = 0; i < 9; i++) r[i] = R[i];
+    };
+    VoxelOut o = solve_voxel<double, double>(nc, ph, et, tauf, load, s6, e6);
     for (int i = 0; i < 6; i++) {
       sig[6 * v + i] = s6[i];
       edot[6 * v + i] = e6[i];

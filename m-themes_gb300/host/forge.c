@@ -5,9 +5,13 @@
  * include/mth.h; the per-step scalars go to vm.out in the reference's columns
  * (TIME EVM EVMP DVM DVMP SVM SVM_1, src/init.c:497 and
  * src/evolution.c:1621-1625), and the macroscopic stress-strain curve (which
- * the reference keeps only in globals) to ss.out.
+ * the reference keeps only in globals) to ss.out.  With --iout-every K the
+ * elastic-strain and stress fields are written every K steps in the format
+ * of WriteElsMPI / WriteSigMPI (src/io.c:322-437; the reference's print
+ * block at src/evolution.c:1633-1648 writes the same two every 500 steps),
+ * in the background while the next steps run.
  *
- * Usage: forge input.in [--mixed]
+ * Usage: forge input.in [--mixed] [--iout-every K]
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -16,7 +20,7 @@
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    fprintf(stderr, "usage: %s input.in [--mixed]\n", argv[0]);
+    fprintf(stderr, "usage: %s input.in [--mixed] [--iout-every K]\n", argv[0]);
     return 2;
   }
   mth_params p;
@@ -26,8 +30,11 @@ int main(int argc, char** argv) {
     fprintf(stderr, "Input file not found!\n");
     return 1;
   }
-  for (int i = 2; i < argc; i++)
+  int iout_every = 0;
+  for (int i = 2; i < argc; i++) {
     if (!strcmp(argv[i], "--mixed")) p.precision = MTH_MIXED;
+    else if (!strcmp(argv[i], "--iout-every") && i + 1 < argc) iout_every = atoi(argv[++i]);
+  }
   if (p.n_phases >= 1 && p.phase[0].type == 0 && mth_read_sx(sx1, &p, 0) != MTH_OK) {
     fprintf(stderr, "cannot read %s\n", sx1);
     return 1;
@@ -68,7 +75,17 @@ int main(int argc, char** argv) {
             r.sig_avg[2][2], r.err_s, r.err_e);
     fflush(vm);
     fflush(ss);
+    if (iout_every > 0 && istep % iout_every == 0) {
+      s = mth_write_iout(ctx, MTH_IOUT_ELS, "els", istep);
+      if (s == MTH_OK) s = mth_write_iout(ctx, MTH_IOUT_SIG, "sig", istep);
+      if (s != MTH_OK) {
+        fprintf(stderr, "field files of step %d failed (%d): %s\n", istep, (int)s, mth_last_error());
+        break;
+      }
+    }
   }
+  if (s == MTH_OK) s = mth_iout_wait(ctx);
+  if (s != MTH_OK) fprintf(stderr, "%s\n", mth_last_error());
   fclose(vm);
   fclose(ss);
   mth_destroy(ctx);

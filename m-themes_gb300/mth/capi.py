@@ -147,6 +147,9 @@ def _iptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
+IOUT = {"sig": 0, "eps": 1, "edot": 2, "els": 3, "grain": 4, "texture": 5}
+
+
 class MthError(RuntimeError):
     pass
 
@@ -191,6 +194,8 @@ def load(path: str | None = None):
     lib.mth_read_sx.argtypes = [C.c_char_p, C.POINTER(MthParams), C.c_int]
     lib.mth_read_microstructure.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
+    lib.mth_write_iout.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
+    lib.mth_iout_wait.argtypes = [C.c_void_p]
     lib.mth_batch_create.argtypes = [C.POINTER(MthParams), C.c_int, C.POINTER(C.c_void_p)]
     lib.mth_batch_upload.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_double), C.c_size_t]

@@ -40,6 +40,14 @@ class Solver:
         capi.check(self.lib, self.lib.mth_download_field(self.ctx, f, capi._dptr(out), out.size))
         return out.reshape(self.nv, -1)
 
+    def write_iout(self, kind: str, prefix: str, step: int):
+        """Start writing a field in the reference's .iout format (mth_write_iout);
+        the files are complete after wait_iout()."""
+        capi.check(self.lib, self.lib.mth_write_iout(self.ctx, capi.IOUT[kind], prefix.encode(), step))
+
+    def wait_iout(self):
+        capi.check(self.lib, self.lib.mth_iout_wait(self.ctx))
+
     def profile(self, enable=None, reset=False):
         """Per-kernel device times (CUDA events on the context's stream),
         launch counts and algorithmic bytes; optionally switch timing on/off."""

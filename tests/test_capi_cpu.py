@@ -117,3 +117,8 @@ def test_batch_argument_checks(lib):
     assert lib.mth_batch_step(None, None) == 1
     assert lib.mth_batch_destroy(None) == 1
     assert lib.mth_batch_upload(None, 0, None, None, None, 0) == 1
+
+
+def test_iout_argument_checks(lib):
+    assert lib.mth_write_iout(None, 0, b"x", 0) == 1
+    assert lib.mth_iout_wait(None) == 1

@@ -37,3 +37,17 @@ def test_forge_driver_matches_oracle(tmp_path):
         assert np.allclose(vm[k], ref, rtol=2e-6, atol=1e-12), (k, vm[k], ref)
         assert int(ss[k, 1]) == rep["iterations"]
         assert abs(ss[k, 8] - rep["sig_avg"][2, 2]) <= 1e-6 * abs(rep["sig_avg"][2, 2])
+
+
+def test_forge_writes_field_files(tmp_path):
+    cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=3, n_steps=3, seed=64, iter_max=10)
+    synth.write_case(str(tmp_path), cfg)
+    forge = os.path.join(REPO, "m-themes_gb300", "lib", "forge")
+    r = subprocess.run([forge, "input.in", "--iout-every", "2"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for pre in ("els", "sig"):
+        for step in (0, 2):
+            for c in range(1, 7):
+                f = tmp_path / f"{pre}_{c}_S{step:06d}.iout"
+                assert f.stat().st_size == 8 * 8 ** 3
+    assert not (tmp_path / "sig_1_S000001.iout").exists()
