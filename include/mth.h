@@ -99,6 +99,11 @@ typedef struct {
   uint64_t seed;             /* counter-based RNG seed */
   double nucleation_prob;    /* per-step nucleation probability of a candidate voxel */
   int    device;             /* CUDA device ordinal the context runs on */
+  int    pf_cell_dim[3];     /* CellDim_pf: grid of the phase field.  Zeros or equal to
+                                cell_dim: the mechanical grid.  Otherwise grain ids and rho
+                                are carried to the PF grid and the relaxed ids back as
+                                InterpolateGrid and Update_microstructure do
+                                (src/integrated.c:496-760,821-860); each entry >= 2. */
 } mth_params;
 
 /* Per-step record; the reference prints the scalars to vm.out

@@ -95,6 +95,9 @@ struct PhaseConst {
   // float copies for the FP32 flow rule (filled by fill_float_consts)
   float nrsf, gamd0f, tau_offf;
   float m_xtf[NSYS][5];
+  float bnf[NSYS][3], bbf[NSYS][3];
+  float hardf[NSYS][NSYS];
+  float tau0ff, tau1f, thet0f, thet1f;
 };
 
 // Constant of precision T from its double and float copies: the FP32 paths

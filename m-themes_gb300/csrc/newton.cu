@@ -547,8 +547,18 @@ void fill_float_consts(NewtonConst& nc) {
     ph.nrsf = (float)ph.nrs;
     ph.gamd0f = (float)ph.gamd0;
     ph.tau_offf = (float)ph.tau_back_minus_fwd;
-    for (int s = 0; s < NSYS; s++)
+    for (int s = 0; s < NSYS; s++) {
       for (int i = 0; i < 5; i++) ph.m_xtf[s][i] = (float)ph.m_xt[s][i];
+      for (int i = 0; i < 3; i++) {
+        ph.bnf[s][i] = (float)ph.bn[s][i];
+        ph.bbf[s][i] = (float)ph.bb[s][i];
+      }
+      for (int j = 0; j < NSYS; j++) ph.hardf[s][j] = (float)ph.hard[s][j];
+    }
+    ph.tau0ff = (float)ph.tau0f;
+    ph.tau1f = (float)ph.tau1;
+    ph.thet0f = (float)ph.thet0;
+    ph.thet1f = (float)ph.thet1;
   }
   for (int i = 0; i < 25; i++) nc.s0devf[i] = (float)nc.s0dev[i];
   nc.s0hhf = (float)nc.s0hh;
@@ -584,20 +594,20 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
                                                        double* __restrict__ partials) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
-  double acc[NPART_END];
+  TF acc[NPART_END];
 #pragma unroll
-  for (int i = 0; i < NPART_END; i++) acc[i] = 0.0;
+  for (int i = 0; i < NPART_END; i++) acc[i] = (TF)0;
   if (v < P) {
     const int jph = f.phase[v];
     const PhaseConst& ph = nc.ph[jph];
-    const TF dt = (TF)nc.dt;
+    const TF dt = cpick<TF>(nc.dt, nc.dtf);
 #pragma unroll
     for (int i = 0; i < 6; i++) {
       const TF ed = (TF)f.edot[i * P + v];
       const TF ep = (TF)f.epsp[i * P + v] + ed * dt;
       f.epsp[i * P + v] = (TSt)ep;
-      acc[i] = (double)ep;
-      acc[6 + i] = (double)ed;
+      acc[i] = ep;
+      acc[6 + i] = ed;
     }
     if (ph.type == 0 && (do_orient || do_harden)) {
       TF R[9], Q[25], s6[6], x[5], tauf[NSYS], gam[NSYS], ed[5], psi;
@@ -617,13 +627,17 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       }
 #pragma unroll
       for (int s = 0; s < NSYS; s++) gam[s] = 0;
-      if (!nc.flow_off) flow_rule<TF, false>(ph, x, tauf, (TF)ph.tau_back_minus_fwd, ed, nullptr, psi, gam);
+      if (!nc.flow_off) flow_rule<TF, false>(ph, x, tauf, cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf), ed, nullptr, psi, gam);
       if (do_orient) {
         // plastic spin: RotSlip = -1/2 T sum_a gam_a (b_a x n_a)
         TF cx = 0, cy = 0, cz = 0;
-        for (int s = 0; s < ph.nsys; s++) {
-          const TF b0 = (TF)ph.bb[s][0], b1 = (TF)ph.bb[s][1], b2 = (TF)ph.bb[s][2];
-          const TF n0 = (TF)ph.bn[s][0], n1 = (TF)ph.bn[s][1], n2 = (TF)ph.bn[s][2];
+#pragma unroll
+        for (int s = 0; s < NSYS; s++) {
+          if (s >= ph.nsys) break;
+          const TF b0 = cpick<TF>(ph.bb[s][0], ph.bbf[s][0]), b1 = cpick<TF>(ph.bb[s][1], ph.bbf[s][1]),
+                   b2 = cpick<TF>(ph.bb[s][2], ph.bbf[s][2]);
+          const TF n0 = cpick<TF>(ph.bn[s][0], ph.bnf[s][0]), n1 = cpick<TF>(ph.bn[s][1], ph.bnf[s][1]),
+                   n2 = cpick<TF>(ph.bn[s][2], ph.bnf[s][2]);
           cx += gam[s] * (b1 * n2 - b2 * n1);
           cy += gam[s] * (b2 * n0 - b0 * n2);
           cz += gam[s] * (b0 * n1 - b1 * n0);
@@ -663,24 +677,34 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       if (do_harden) {
         const TF gamtot = (TF)f.gamacum[v];
         TF deltgam = 0;
-        for (int s = 0; s < ph.nsys; s++) deltgam += fabs(gam[s]) * dt;
+#pragma unroll
+        for (int s = 0; s < NSYS; s++) deltgam += fabs(gam[s]) * dt;   // gam is 0 past nsys
         if (deltgam > (TF)0) {
-          const TF tau0 = (TF)ph.tau0f, tau1 = (TF)ph.tau1, th0 = (TF)ph.thet0, th1 = (TF)ph.thet1;
+          const TF tau0 = cpick<TF>(ph.tau0f, ph.tau0ff), tau1 = cpick<TF>(ph.tau1, ph.tau1f),
+                   th0 = cpick<TF>(ph.thet0, ph.thet0f), th1 = cpick<TF>(ph.thet1, ph.thet1f);
           const TF tiny = (TF)1e-4 * tau0;
           TF voce = 0;
           if (fabs(th0) > tiny) {
             voce = th1 * deltgam;
             if (fabs(tau1) > tiny) {
+              // the Voce increment of harden (src/constitutive.c:293-316) with
+              // exp(-dgam fact) - 1 as expm1 and the second bracket regrouped
+              // as (e - 1)(gam fact + 1) + e dgam fact: the same value without
+              // the cancellation of nearly equal terms (FP32 in mixed mode)
               const TF fact = fabs(th0 / tau1);
               const TF exp_ini = exp((TF)-1 * gamtot * fact);
-              const TF exp_del = exp((TF)-1 * deltgam * fact);
-              voce += (TF)-1 * (fact * tau1 - th1) / fact * exp_ini * (exp_del - (TF)1) -
-                      th1 / fact * exp_ini * (exp_del * ((gamtot + deltgam) * fact + (TF)1) - (gamtot * fact + (TF)1));
+              const TF em1 = expm1((TF)-1 * deltgam * fact);
+              const TF exp_del = em1 + (TF)1;
+              voce += (TF)-1 * (fact * tau1 - th1) / fact * exp_ini * em1 -
+                      th1 / fact * exp_ini * (em1 * (gamtot * fact + (TF)1) + exp_del * deltgam * fact);
             }
           }
-          for (int s = 0; s < ph.nsys; s++) {
+#pragma unroll
+          for (int s = 0; s < NSYS; s++) {
+            if (s >= ph.nsys) break;
             TF dtau = 0;
-            for (int j = 0; j < ph.nsys; j++) dtau += (TF)ph.hard[s][j] * fabs(gam[j]) * dt;
+#pragma unroll
+            for (int j = 0; j < NSYS; j++) dtau += cpick<TF>(ph.hard[s][j], ph.hardf[s][j]) * fabs(gam[j]) * dt;
             f.crss[s * P + v] = (TSt)((TF)f.crss[s * P + v] + dtau * voce / deltgam);
           }
           f.gamacum[v] = (TSt)(gamtot + deltgam);
@@ -688,7 +712,7 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       }
     }
   }
-  block_reduce_store<NPART_END>(acc, partials);
+  block_reduce_smem<TF, NPART_END>(acc, partials);
 }
 
 cudaError_t launch_end_step(int mixed, const NewtonConst& nc_in, const void* fields, const double au[3], int do_orient,
@@ -697,7 +721,7 @@ cudaError_t launch_end_step(int mixed, const NewtonConst& nc_in, const void* fie
   fill_float_consts(nc);
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    end_step_kernel<float, double><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);
+    end_step_kernel<float, float><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
     end_step_kernel<double, double><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);

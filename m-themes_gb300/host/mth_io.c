@@ -96,6 +96,7 @@ mth_status mth_read_namelist(const char* path, mth_params* p, char* slip1, char*
   p->phase[1].c11 = s_el2[0]; p->phase[1].c12 = s_el2[1]; p->phase[1].c44 = s_el2[2];
   p->nucleus_radius = s_nuclr;
   if (s_randseed) p->seed = (uint64_t)s_randseed;
+  for (int i = 0; i < 3; i++) p->pf_cell_dim[i] = s_celldim_pf[i];
   if (slip1 && cap) { strncpy(slip1, sx1, cap - 1); slip1[cap - 1] = 0; }
   if (slip2 && cap) { strncpy(slip2, sx2, cap - 1); slip2[cap - 1] = 0; }
   if (ms && cap) { strncpy(ms, msf, cap - 1); ms[cap - 1] = 0; }

@@ -50,7 +50,7 @@ class MthParams(C.Structure):
                 ("shear_modulus", C.c_double), ("burgers", C.c_double), ("nucleus_radius", C.c_int),
                 ("rho_nucleation", C.c_double), ("rho0", C.c_double), ("rho_k", C.c_double),
                 ("pf_substeps", C.c_int), ("seed", C.c_uint64), ("nucleation_prob", C.c_double),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("pf_cell_dim", C.c_int * 3)]
 
 
 T33 = (C.c_double * 3) * 3
@@ -136,6 +136,9 @@ def params_from_config(cfg, precision=MTH_FP64, newton_tol=0.0, newton_itmax=0) 
         p.nucleation_prob = d.nucleation_prob
         p.nucleus_radius = d.nucleus_radius
         p.seed = d.seed
+        if d.pf_cell_dim:
+            for i in range(3):
+                p.pf_cell_dim[i] = d.pf_cell_dim[i]
     return p
 
 

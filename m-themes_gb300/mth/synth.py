@@ -64,6 +64,7 @@ class Drx:
     nucleation_prob: float = 2e-5
     nucleus_radius: int = 2
     seed: int = 12345
+    pf_cell_dim: tuple = None   # CellDim_pf; None: the mechanical grid
 
 
 def shear_modulus(m: "Material") -> float:
@@ -198,6 +199,7 @@ def write_sx(path, m: Material):
 
 def write_input(path, cfg: Config, ms_name="ms.txt", sx_name="cu.sx"):
     m = cfg.material
+    pfd = cfg.drx.pf_cell_dim if (cfg.drx is not None and cfg.drx.pf_cell_dim) else cfg.cell_dim
     n_phases = 2 if cfg.n_pores else 1
 
     def vec(v):
@@ -248,7 +250,7 @@ HirthLock 0.05 0.0
 LomerCottrellLock 0.18 0.0
 D_0 4E-05
 nucleus_radius 2
-CellDim_pf {cfg.cell_dim[0]} {cfg.cell_dim[1]} {cfg.cell_dim[2]}
+CellDim_pf {pfd[0]} {pfd[1]} {pfd[2]}
 RandSeed 123
 E_gb 0.625
 M_gb 7.4E-11

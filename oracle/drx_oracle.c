@@ -284,3 +284,77 @@ int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const doub
   free(ids); free(ids2); free(phi); free(phi2); free(cnt); free(cnt2);
   return MTH_OK;
 }
+
+/* ------------------------------------------------ PF <-> FFT grid transfer
+ * InterpolateGrid / InterpolateGID (src/integrated.c:621-760) and the
+ * coarse-graining of gID_new in Update_microstructure
+ * (src/integrated.c:821-860): node-based coordinates x = i/(N-1) on [0,1]
+ * (x0 = 0), source cell index floor(x/dx) with dx = 1/(Ns-1), upper corner
+ * clamped to the last node.  The reference aborts (PError 1203) when
+ * rounding puts a destination node past the last source node; here the last
+ * cell is used.  An axis of one node maps everything to node 0. */
+static void axis_pos(int i, int nd, int ns, int* i0, int* i1, double* s) {
+  if (nd < 2 || ns < 2) { *i0 = 0; *i1 = 0; *s = 0.0; return; }
+  const double dxd = 1.0 / (nd - 1), dxs = 1.0 / (ns - 1);
+  const double x = 0.0 + (double)i * dxd;
+  int ix = (int)floor(x / dxs);
+  if (ix > ns - 1) ix = ns - 1;
+  if (ix < 0) ix = 0;
+  *s = x / dxs - (double)ix;
+  *i0 = ix;
+  *i1 = ix + 1 < ns ? ix + 1 : ns - 1;
+}
+
+/* Integer field: value of the nearest of the eight corners of the source
+ * cell, first minimum in the order 000,100,110,010,001,101,111,011
+ * (TrilinearInterpolationINT, src/integrated.c:496-565). */
+void orc_resample_nearest(const int* ns, const int* src, const int* nd, int* dst) {
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nd[0]; i++)
+    for (int j = 0; j < nd[1]; j++)
+      for (int k = 0; k < nd[2]; k++) {
+        int x0, x1, y0, y1, z0, z1;
+        double sx, sy, sz;
+        axis_pos(i, nd[0], ns[0], &x0, &x1, &sx);
+        axis_pos(j, nd[1], ns[1], &y0, &y1, &sy);
+        axis_pos(k, nd[2], ns[2], &z0, &z1, &sz);
+        double dist[8];
+        dist[0] = sx * sx + sy * sy + sz * sz;
+        dist[1] = (1 - sx) * (1 - sx) + sy * sy + sz * sz;
+        dist[2] = (1 - sx) * (1 - sx) + (1 - sy) * (1 - sy) + sz * sz;
+        dist[3] = sx * sx + (1 - sy) * (1 - sy) + sz * sz;
+        dist[4] = sx * sx + sy * sy + (1 - sz) * (1 - sz);
+        dist[5] = (1 - sx) * (1 - sx) + sy * sy + (1 - sz) * (1 - sz);
+        dist[6] = (1 - sx) * (1 - sx) + (1 - sy) * (1 - sy) + (1 - sz) * (1 - sz);
+        dist[7] = sx * sx + (1 - sy) * (1 - sy) + (1 - sz) * (1 - sz);
+        const int cx[8] = {x0, x1, x1, x0, x0, x1, x1, x0};
+        const int cy[8] = {y0, y0, y1, y1, y0, y0, y1, y1};
+        const int cz[8] = {z0, z0, z0, z0, z1, z1, z1, z1};
+        int m = 0;
+        for (int c = 1; c < 8; c++)
+          if (dist[m] > dist[c]) m = c;
+        dst[((long long)i * nd[1] + j) * nd[2] + k] = src[((long long)cx[m] * ns[1] + cy[m]) * ns[2] + cz[m]];
+      }
+}
+
+/* Double field: trilinear interpolation (TrilinearInterpolation,
+ * src/integrated.c:567-619), terms in the reference's order. */
+void orc_resample_trilinear(const int* ns, const double* src, const int* nd, double* dst) {
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nd[0]; i++)
+    for (int j = 0; j < nd[1]; j++)
+      for (int k = 0; k < nd[2]; k++) {
+        int x0, x1, y0, y1, z0, z1;
+        double sx, sy, sz;
+        axis_pos(i, nd[0], ns[0], &x0, &x1, &sx);
+        axis_pos(j, nd[1], ns[1], &y0, &y1, &sy);
+        axis_pos(k, nd[2], ns[2], &z0, &z1, &sz);
+#define V(a, b, c) src[((long long)(a) * ns[1] + (b)) * ns[2] + (c)]
+        dst[((long long)i * nd[1] + j) * nd[2] + k] =
+            V(x0, y0, z0) * (1.0 - sx) * (1.0 - sy) * (1.0 - sz) + V(x1, y0, z0) * sx * (1.0 - sy) * (1.0 - sz) +
+            V(x0, y1, z0) * sy * (1.0 - sx) * (1.0 - sz) + V(x0, y0, z1) * sz * (1.0 - sy) * (1.0 - sx) +
+            V(x1, y0, z1) * sx * (1.0 - sy) * sz + V(x0, y1, z1) * sy * (1.0 - sx) * sz +
+            V(x1, y1, z0) * sx * (1.0 - sz) * sy + V(x1, y1, z1) * sx * sy * sz;
+#undef V
+      }
+}

@@ -53,6 +53,12 @@ void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, 
 int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps, int K,
                  int* grain_out, int* ids_out, double* phi_out, int* cnt_out);
 
+/* Transfer between the mechanical grid and a phase-field grid of another
+ * size (InterpolateGrid, src/integrated.c:496-760): nearest-corner for
+ * integer fields, trilinear for doubles; ns, nd: source / destination dims. */
+void orc_resample_nearest(const int* ns, const int* src, const int* nd, int* dst);
+void orc_resample_trilinear(const int* ns, const double* src, const int* nd, double* dst);
+
 /* Complex FFT used by the oracle: in-place 3-D transform of an n0*n1*n2
  * array of interleaved (re,im) doubles, un-normalised, sign -1 forward,
  * +1 backward (FFTW 2.1.5 convention used at src/evolution.c:1367,1399). */
