@@ -320,6 +320,14 @@ struct mth_ctx {
   uint8_t* crystal_d;
   unsigned long long* hist_d;
   double* gather_d;
+  // phase field on a grid of its own (CellDim_pf != CellDim)
+  bool pf_resample;
+  int npf[3];
+  long long nvpf;
+  int* grain_pf_d;      // grain ids carried to the PF grid
+  double* rho_pf_d;     // rho on the PF grid (FP64)
+  void* rho_pf_t;       // rho on the PF grid in the PF precision
+  int* gid_coarse_d;    // relaxed ids carried back to the mechanical grid
   size_t hist_cap;
   double tau0f;
   int nsys;
@@ -377,6 +385,10 @@ static void ctx_free(mth_ctx* c) {
   cudaFree(c->crystal_d);
   cudaFree(c->hist_d);
   cudaFree(c->gather_d);
+  cudaFree(c->grain_pf_d);
+  cudaFree(c->rho_pf_d);
+  cudaFree(c->rho_pf_t);
+  cudaFree(c->gid_coarse_d);
   delete c;
 }
 
@@ -607,12 +619,30 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     c->pfc.kappa = 3.0 / 4.0 * p->e_gb * (p->pf_width_cells * p->pf_length_scale) / p->pf_length_scale / p->pf_length_scale;
     c->pfc.mwell = 6 * p->e_gb / (p->pf_width_cells * p->pf_length_scale);
     c->pfc.edisl = p->stored_energy_scale * p->shear_modulus * p->burgers * p->burgers;
+    // phase-field grid: the mechanical one unless CellDim_pf names another
+    const bool pf_zero = p->pf_cell_dim[0] == 0 && p->pf_cell_dim[1] == 0 && p->pf_cell_dim[2] == 0;
+    for (int i = 0; i < 3; i++) c->npf[i] = pf_zero ? c->n[i] : p->pf_cell_dim[i];
+    if (!pf_zero)
+      for (int i = 0; i < 3; i++)
+        if (c->npf[i] < 2 || c->npf[i] > 4096 || c->n[i] < 2) {
+          ctx_free(c);
+          return set_err(MTH_ERR_ARG, "pf_cell_dim must be 0 0 0 or >= 2 per axis (with cell_dim >= 2)");
+        }
+    c->pf_resample = c->npf[0] != c->n[0] || c->npf[1] != c->n[1] || c->npf[2] != c->n[2];
+    c->nvpf = (long long)c->npf[0] * c->npf[1] * c->npf[2];
+    const long long Q = c->nvpf;
     for (int i = 0; i < 2; i++) {
-      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.ids[i] : (void*&)c->pfd.ids[i]), sizeof(int) * PF_K * P));
-      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.phi[i] : (void*&)c->pfd.phi[i]), esz * PF_K * P));
-      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.cnt[i] : (void*&)c->pfd.cnt[i]), P));
+      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.ids[i] : (void*&)c->pfd.ids[i]), sizeof(int) * PF_K * Q));
+      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.phi[i] : (void*&)c->pfd.phi[i]), esz * PF_K * Q));
+      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.cnt[i] : (void*&)c->pfd.cnt[i]), Q));
     }
-    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.gid : (void*&)c->pfd.gid), sizeof(int) * P));
+    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.gid : (void*&)c->pfd.gid), sizeof(int) * Q));
+    if (c->pf_resample) {
+      CKC(cudaMalloc(&c->grain_pf_d, sizeof(int) * Q));
+      CKC(cudaMalloc(&c->rho_pf_d, sizeof(double) * Q));
+      CKC(cudaMalloc(&c->rho_pf_t, esz * Q));
+      CKC(cudaMalloc(&c->gid_coarse_d, sizeof(int) * P));
+    }
     CKC(cudaMalloc(&c->rho_d, sizeof(double) * P));
     CKC(cudaMalloc(&c->rho_t, esz * P));
     CKC(cudaMalloc(&c->grain_prev_d, sizeof(int) * P));
@@ -1011,16 +1041,32 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   }
   CK(cudaMemcpyAsync(c->drx_rot_d, c->drx_rot_h->data(), sizeof(double) * 9 * n_drx, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->drx_class_d, c->drx_class_h->data(), sizeof(int) * n_drx, cudaMemcpyHostToDevice, c->st));
-  // phase-field relaxation from the painted grain map
+  // phase-field relaxation from the painted grain map, on the PF grid
+  // (grain ids and rho carried over first, src/evolution.c:1013-1018)
+  const int* pf_grain = c->grain_d;
+  const void* pf_rho = c->rho_t;
+  if (c->pf_resample) {
+    LAUNCH(K_DRX, (double)c->nvpf * 4 + (double)c->nv * 4,
+           launch_resample_nearest(c->n, c->grain_d, c->npf, c->grain_pf_d, c->st));
+    LAUNCH(K_DRX, (double)c->nvpf * (c->mixed ? 4 : 8) + (double)c->nv * 8,
+           launch_resample_trilinear(c->n, c->rho_d, c->npf, c->rho_pf_t, c->mixed, c->st));
+    pf_grain = c->grain_pf_d;
+    pf_rho = c->rho_pf_t;
+  }
   int* gid_new;
   if (c->mixed) {
-    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nv, sizeof(float), p.pf_substeps),
-            launch_pf_relax<float>(c->n, c->grain_d, (const float*)c->rho_t, p.pf_substeps, c->pfc, c->pff, c->st));
+    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(float), p.pf_substeps),
+            launch_pf_relax<float>(c->npf, pf_grain, (const float*)pf_rho, p.pf_substeps, c->pfc, c->pff, c->st));
     gid_new = c->pff.gid;
   } else {
-    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nv, sizeof(double), p.pf_substeps),
-            launch_pf_relax<double>(c->n, c->grain_d, (const double*)c->rho_t, p.pf_substeps, c->pfc, c->pfd, c->st));
+    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(double), p.pf_substeps),
+            launch_pf_relax<double>(c->npf, pf_grain, (const double*)pf_rho, p.pf_substeps, c->pfc, c->pfd, c->st));
     gid_new = c->pfd.gid;
+  }
+  if (c->pf_resample) {   // relaxed ids back to the mechanical grid (src/integrated.c:821-860)
+    LAUNCH(K_DRX, (double)c->nvpf * 4 + (double)c->nv * 4,
+           launch_resample_nearest(c->npf, gid_new, c->n, c->gid_coarse_d, c->st));
+    gid_new = c->gid_coarse_d;
   }
   LAUNCH(K_DRX, (double)c->nv * 12, launch_drx_update(c->mixed, f, c->grain_d, c->grain_prev_d, gid_new, c->first_drx_id, n_drx,
                                        c->drx_rot_d, c->drx_class_d, c->tau0f, c->nsys, c->st));

@@ -403,6 +403,96 @@ cudaError_t launch_class_histogram(long long nv, const uint8_t* crystal, const i
   return cudaGetLastError();
 }
 
+// ------------------------------------------ PF <-> mechanical grid transfer
+// InterpolateGrid / InterpolateGID (src/integrated.c:496-760) and the
+// coarse-graining of gID_new (src/integrated.c:821-860): node coordinates
+// x = i/(N-1) on [0,1], source cell floor(x/dx), dx = 1/(Ns-1), upper corner
+// clamped to the last node (the reference aborts when rounding puts a node
+// past the last source node; here the last cell is used).  Same operations
+// in the same order as the oracle (this file is compiled without FMA
+// contraction), so FP64 results are bit-identical.
+__device__ __forceinline__ void axis_pos(int i, int nd, int ns, int& i0, int& i1, double& s) {
+  if (nd < 2 || ns < 2) { i0 = 0; i1 = 0; s = 0.0; return; }
+  const double dxd = 1.0 / (nd - 1), dxs = 1.0 / (ns - 1);
+  const double x = 0.0 + (double)i * dxd;
+  int ix = (int)floor(x / dxs);
+  if (ix > ns - 1) ix = ns - 1;
+  if (ix < 0) ix = 0;
+  s = x / dxs - (double)ix;
+  i0 = ix;
+  i1 = ix + 1 < ns ? ix + 1 : ns - 1;
+}
+
+// integer field: value at the nearest of the eight corners, first minimum in
+// the order 000,100,110,010,001,101,111,011 (TrilinearInterpolationINT)
+__global__ void resample_nearest_kernel(Dims ds, const int* __restrict__ src, Dims dd, int* __restrict__ dst) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nv = (long long)dd.n0 * dd.n1 * dd.n2;
+  if (v >= nv) return;
+  const int k = (int)(v % dd.n2), j = (int)((v / dd.n2) % dd.n1), i = (int)(v / ((long long)dd.n1 * dd.n2));
+  int x0, x1, y0, y1, z0, z1;
+  double sx, sy, sz;
+  axis_pos(i, dd.n0, ds.n0, x0, x1, sx);
+  axis_pos(j, dd.n1, ds.n1, y0, y1, sy);
+  axis_pos(k, dd.n2, ds.n2, z0, z1, sz);
+  double dist[8];
+  dist[0] = sx * sx + sy * sy + sz * sz;
+  dist[1] = (1 - sx) * (1 - sx) + sy * sy + sz * sz;
+  dist[2] = (1 - sx) * (1 - sx) + (1 - sy) * (1 - sy) + sz * sz;
+  dist[3] = sx * sx + (1 - sy) * (1 - sy) + sz * sz;
+  dist[4] = sx * sx + sy * sy + (1 - sz) * (1 - sz);
+  dist[5] = (1 - sx) * (1 - sx) + sy * sy + (1 - sz) * (1 - sz);
+  dist[6] = (1 - sx) * (1 - sx) + (1 - sy) * (1 - sy) + (1 - sz) * (1 - sz);
+  dist[7] = sx * sx + (1 - sy) * (1 - sy) + (1 - sz) * (1 - sz);
+  const int cx[8] = {x0, x1, x1, x0, x0, x1, x1, x0};
+  const int cy[8] = {y0, y0, y1, y1, y0, y0, y1, y1};
+  const int cz[8] = {z0, z0, z0, z0, z1, z1, z1, z1};
+  int m = 0;
+#pragma unroll
+  for (int c = 1; c < 8; c++)
+    if (dist[m] > dist[c]) m = c;
+  dst[v] = src[((long long)cx[m] * ds.n1 + cy[m]) * ds.n2 + cz[m]];
+}
+
+// double field: trilinear interpolation, terms in the reference's order
+// (TrilinearInterpolation); stored as TO
+template <typename TO>
+__global__ void resample_trilinear_kernel(Dims ds, const double* __restrict__ src, Dims dd, TO* __restrict__ dst) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nv = (long long)dd.n0 * dd.n1 * dd.n2;
+  if (v >= nv) return;
+  const int k = (int)(v % dd.n2), j = (int)((v / dd.n2) % dd.n1), i = (int)(v / ((long long)dd.n1 * dd.n2));
+  int x0, x1, y0, y1, z0, z1;
+  double sx, sy, sz;
+  axis_pos(i, dd.n0, ds.n0, x0, x1, sx);
+  axis_pos(j, dd.n1, ds.n1, y0, y1, sy);
+  axis_pos(k, dd.n2, ds.n2, z0, z1, sz);
+  auto V = [&](int a, int b, int c) { return src[((long long)a * ds.n1 + b) * ds.n2 + c]; };
+  const double r = V(x0, y0, z0) * (1.0 - sx) * (1.0 - sy) * (1.0 - sz) + V(x1, y0, z0) * sx * (1.0 - sy) * (1.0 - sz) +
+                   V(x0, y1, z0) * sy * (1.0 - sx) * (1.0 - sz) + V(x0, y0, z1) * sz * (1.0 - sy) * (1.0 - sx) +
+                   V(x1, y0, z1) * sx * (1.0 - sy) * sz + V(x0, y1, z1) * sy * (1.0 - sx) * sz +
+                   V(x1, y1, z0) * sx * (1.0 - sz) * sy + V(x1, y1, z1) * sx * sy * sz;
+  dst[v] = (TO)r;
+}
+
+cudaError_t launch_resample_nearest(const int ns[3], const int* src, const int nd[3], int* dst, cudaStream_t st) {
+  const long long nv = (long long)nd[0] * nd[1] * nd[2];
+  resample_nearest_kernel<<<nb(nv, 256), 256, 0, st>>>(Dims{ns[0], ns[1], ns[2]}, src, Dims{nd[0], nd[1], nd[2]}, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resample_trilinear(const int ns[3], const double* src, const int nd[3], void* dst, int to_float,
+                                      cudaStream_t st) {
+  const long long nv = (long long)nd[0] * nd[1] * nd[2];
+  if (to_float)
+    resample_trilinear_kernel<float><<<nb(nv, 256), 256, 0, st>>>(Dims{ns[0], ns[1], ns[2]}, src,
+                                                                  Dims{nd[0], nd[1], nd[2]}, static_cast<float*>(dst));
+  else
+    resample_trilinear_kernel<double><<<nb(nv, 256), 256, 0, st>>>(Dims{ns[0], ns[1], ns[2]}, src,
+                                                                   Dims{nd[0], nd[1], nd[2]}, static_cast<double*>(dst));
+  return cudaGetLastError();
+}
+
 // rotation matrices (9 components, component-major fields) of the parent
 // voxels of the nn nuclei, as double, nucleus-major: out[k*9 + i]
 template <typename TSt>

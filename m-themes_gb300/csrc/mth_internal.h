@@ -174,6 +174,10 @@ cudaError_t launch_drx_update(int mixed, const void* fields, int* grain, const i
                               double tau0f, int nsys, cudaStream_t st);
 cudaError_t launch_class_histogram(long long nv, const uint8_t* crystal, const int* eclass, unsigned long long* hist,
                                    cudaStream_t st);
+// grid transfer between the mechanical and the phase-field grid
+cudaError_t launch_resample_nearest(const int ns[3], const int* src, const int nd[3], int* dst, cudaStream_t st);
+cudaError_t launch_resample_trilinear(const int ns[3], const double* src, const int nd[3], void* dst, int to_float,
+                                      cudaStream_t st);
 cudaError_t launch_gather_rot(int mixed, const void* rot, long long nv, const long long* sites, int nn, double* out,
                               cudaStream_t st);
 

@@ -284,12 +284,36 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
   const TF tol2 = cpick<TF>(nc.tol, nc.tolf) * cpick<TF>(nc.tol, nc.tolf);
   const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
   const TF tau_off = cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf);
+  // Newton with a backtracking line search on Phi for large steps.  One
+  // flow-rule evaluation site: every evaluation (with its Hessian) is at the
+  // point the loop moves to next, so an accepted line-search trial supplies
+  // the next Newton step and the last accepted iterate supplies the final
+  // rates, without evaluating any point twice.
   int it = 0;
   bool done = false;
   bool near_root = false;   // previous step within 1e-3 |lambda|
-  TF hstep2 = dh * dh;   // the first step includes the hydrostatic correction
-  for (; it < nc.itmax && !done; it++) {
-    TF edf[5], Df[15], psif;
+  TF hstep2 = dh * dh;      // the first step includes the hydrostatic correction
+  TF xt[5];                 // point evaluated next
+#pragma unroll
+  for (int i = 0; i < 5; i++) xt[i] = x[i];
+  bool trial = false;       // xt is a line-search trial x + alpha p
+  int ls = 0;
+  TF p[5], pn2 = 0, slope = 0, phi0 = 0, alpha = 1;
+  TF edf[5], psif;          // rates and psi at the last evaluated point
+  auto accept_step = [&]() {
+#pragma unroll
+    for (int i = 0; i < 5; i++) x[i] += alpha * p[i];
+    const TF step2 = alpha * alpha * pn2 + hstep2;
+    hstep2 = 0;
+    near_root = step2 <= ls_thr2;
+    TF den2 = ref2;
+    if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
+    if (!(den2 > (TF)0) || step2 <= tol2 * den2) done = true;
+    it++;
+  };
+  const int max_pass = 41 * (nc.itmax + 1);   // each Newton step: at most 40 trials + 1
+  for (int pass = 0; pass < max_pass; pass++) {
+    TF Df[15];
     if (nc.flow_off) {
 #pragma unroll
       for (int i = 0; i < 5; i++) edf[i] = 0;
@@ -297,13 +321,37 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       for (int i = 0; i < 15; i++) Df[i] = 0;
       psif = 0;
     } else {
-      flow_rule<TF, true>(ph, x, tauf, tau_off, edf, Df, psif, nullptr);
+      flow_rule<TF, true>(ph, xt, tauf, tau_off, edf, Df, psif, nullptr);
     }
-    TF g[5], Kx[5];
-    symv5<TF>(K, x, Kx);
+    TF Kx[5];
+    symv5<TF>(K, xt, Kx);
+    if (trial) {
+      TF phi = 0;
+#pragma unroll
+      for (int i = 0; i < 5; i++) phi += xt[i] * ((TF)0.5 * Kx[i] + c[i]);
+      phi += dt * psif;
+      if (!(phi <= phi0 + (TF)1e-4 * alpha * slope)) {
+        TF den = (TF)2 * (phi - phi0 - slope * alpha);
+        TF an = den > (TF)0 ? -slope * alpha * alpha / den : (TF)0.5 * alpha;
+        an = fmin(an, (TF)0.5 * alpha);
+        alpha = fmax(an, (TF)0.1 * alpha);
+        ls++;
+#pragma unroll
+        for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
+        if (!(alpha * alpha * pn2 <= (TF)1e-28 * (ref2 + (TF)1)) && ls < 40) continue;
+        // step too small or trials exhausted: take it and evaluate there
+        accept_step();
+        trial = false;
+        continue;
+      }
+      accept_step();   // x + alpha p, the point just evaluated
+      trial = false;
+    }
+    // rates, Hessian and psi of the current iterate x are at hand
+    if (done || it >= nc.itmax) break;
+    TF g[5];
 #pragma unroll
     for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * edf[i];
-    TF p[5];
     {
       TF H[15], mg[5];
 #pragma unroll
@@ -320,56 +368,33 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       }
       if (!ok) { o.failed = 1; break; }
     }
-    TF pn2 = 0, slope = 0;
+    pn2 = 0;
+    slope = 0;
 #pragma unroll
     for (int i = 0; i < 5; i++) { pn2 += p[i] * p[i]; slope += g[i] * p[i]; }
-    TF alpha = 1;
-    // Line search on Phi only for large steps; near the root Newton's full
-    // step is taken (quadratic convergence region).
+    alpha = 1;
     if (pn2 > ls_thr2 && !nc.flow_off) {
-      TF phi0 = 0;
+      // line search on Phi for large steps; near the root the full step
+      phi0 = 0;
 #pragma unroll
       for (int i = 0; i < 5; i++) phi0 += x[i] * ((TF)0.5 * Kx[i] + c[i]);
       phi0 += dt * psif;
-      for (int ls = 0; ls < 40; ls++) {
-        TF xt[5];
+      ls = 0;
+      trial = true;
 #pragma unroll
-        for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
-        TF edt[5], psit;
-        flow_rule<TF, false>(ph, xt, tauf, tau_off, edt, nullptr, psit, nullptr);
-        TF Kxt[5];
-        symv5<TF>(K, xt, Kxt);
-        TF phi = 0;
-#pragma unroll
-        for (int i = 0; i < 5; i++) phi += xt[i] * ((TF)0.5 * Kxt[i] + c[i]);
-        phi += dt * psit;
-        if (phi <= phi0 + (TF)1e-4 * alpha * slope) break;
-        TF den = (TF)2 * (phi - phi0 - slope * alpha);
-        TF an = den > (TF)0 ? -slope * alpha * alpha / den : (TF)0.5 * alpha;
-        an = fmin(an, (TF)0.5 * alpha);
-        alpha = fmax(an, (TF)0.1 * alpha);
-        if (alpha * alpha * pn2 <= (TF)1e-28 * (ref2 + (TF)1)) break;
-      }
+      for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
+      continue;
     }
+    accept_step();
 #pragma unroll
-    for (int i = 0; i < 5; i++) x[i] += alpha * p[i];
-    const TF step2 = alpha * alpha * pn2 + hstep2;
-    hstep2 = 0;
-    near_root = step2 <= ls_thr2;
-    TF den2 = ref2;
-    if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
-    if (!(den2 > (TF)0) || step2 <= tol2 * den2) done = true;
+    for (int i = 0; i < 5; i++) xt[i] = x[i];
   }
   o.iters = it;
   if (!done) o.failed = 1;
-  // final rates at the solution
-  TF edx[5], psid;
-  if (nc.flow_off) {
+  // final rates at the solution: the last evaluation was at x
+  TF edx[5];
 #pragma unroll
-    for (int i = 0; i < 5; i++) edx[i] = 0;
-  } else {
-    flow_rule<TF, false>(ph, x, tauf, tau_off, edx, nullptr, psid, nullptr);
-  }
+  for (int i = 0; i < 5; i++) edx[i] = edf[i];
   TF lam6[6], eps6[6], ep6[6], Q[25];
   {
     TF R[9];

@@ -970,7 +970,24 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
   *n_new = nn;
   int st = MTH_OK;
   if (c->n_drx > 0) {
-    st = orc_pf_relax(p, c->n, c->grain, rho, p->pf_substeps, 8, gnew, NULL, NULL, NULL);
+    /* phase field on its own grid when CellDim_pf differs (InterpolateGrid,
+     * src/integrated.c:674-760; coarse-graining src/integrated.c:821-860) */
+    const int pf_zero = p->pf_cell_dim[0] == 0 && p->pf_cell_dim[1] == 0 && p->pf_cell_dim[2] == 0;
+    int npf[3];
+    for (int i = 0; i < 3; i++) npf[i] = pf_zero ? c->n[i] : p->pf_cell_dim[i];
+    if (npf[0] != c->n[0] || npf[1] != c->n[1] || npf[2] != c->n[2]) {
+      const size_t q = (size_t)npf[0] * npf[1] * npf[2];
+      int* gpf = (int*)malloc(sizeof(int) * q);
+      int* gnpf = (int*)malloc(sizeof(int) * q);
+      double* rpf = (double*)malloc(sizeof(double) * q);
+      orc_resample_nearest(c->n, c->grain, npf, gpf);
+      orc_resample_trilinear(c->n, rho, npf, rpf);
+      st = orc_pf_relax(p, npf, gpf, rpf, p->pf_substeps, 8, gnpf, NULL, NULL, NULL);
+      orc_resample_nearest(npf, gnpf, c->n, gnew);
+      free(gpf); free(gnpf); free(rpf);
+    } else {
+      st = orc_pf_relax(p, c->n, c->grain, rho, p->pf_substeps, 8, gnew, NULL, NULL, NULL);
+    }
     for (size_t v = 0; v < nv && st == MTH_OK; v++) {
       const int g = gnew[v];
       c->grain[v] = g;

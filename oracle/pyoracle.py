@@ -67,6 +67,10 @@ def load():
         lib.orc_pf_relax.argtypes = [C.POINTER(capi.MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        lib.orc_resample_nearest.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                             C.POINTER(C.c_int)]
+        lib.orc_resample_trilinear.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                               C.POINTER(C.c_double)]
         _lib = lib
     return _lib
 
@@ -180,3 +184,21 @@ def nucleate(params, dims, grain, crystal, rho, step, first_id, cap=65536):
     lib.orc_paint_nuclei(d, capi._iptr(g), sites.ctypes.data_as(C.POINTER(C.c_longlong)), nn, first_id,
                          params.nucleus_radius)
     return g, sites[:nn]
+
+
+def resample(src, ns, nd):
+    """Oracle grid transfer: nearest corner for integer arrays, trilinear for
+    floating-point arrays (flattened, z fastest)."""
+    lib = load()
+    a = (C.c_int * 3)(*ns)
+    b = (C.c_int * 3)(*nd)
+    n = int(np.prod(nd))
+    if np.issubdtype(np.asarray(src).dtype, np.integer):
+        x = np.ascontiguousarray(src, dtype=np.int32)
+        out = np.zeros(n, np.int32)
+        lib.orc_resample_nearest(a, capi._iptr(x), b, capi._iptr(out))
+    else:
+        x = np.ascontiguousarray(src, dtype=np.float64)
+        out = np.zeros(n)
+        lib.orc_resample_trilinear(a, capi._dptr(x), b, capi._dptr(out))
+    return out

@@ -112,3 +112,26 @@ def test_coupled_drx_matches_oracle():
         assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
     assert total_new > 0
     assert rel(s.field("sig"), o.field("sig")) < 1e-5
+
+
+@pytest.mark.parametrize("pf_dims", [(32, 32, 32), (24, 16, 20)])
+def test_coupled_drx_on_its_own_pf_grid(pf_dims):
+    """CellDim_pf != CellDim: grain ids and rho carried to the PF grid and the
+    relaxed ids back (InterpolateGrid / Update_microstructure), FP64 grain
+    maps identical to the oracle's at every step."""
+    cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=6, n_steps=4, seed=5, iter_max=8,
+                       drx=synth.Drx(rho_k=4000.0, rho_nucleation=30.0, nucleation_prob=0.02, pf_cell_dim=pf_dims))
+    g, p, e = synth.microstructure(cfg)
+    par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
+    from mth import Solver
+    s = Solver(par, g, p, e)
+    o = pyoracle.Oracle(par, g, p, e, nthreads=4)
+    total_new = 0
+    for k in range(cfg.n_steps):
+        a, b = s.step(), o.step()
+        assert a["n_new_grains"] == b["n_new_grains"], k
+        total_new += a["n_new_grains"]
+        assert np.array_equal(s.field("grain"), o.field("grain")), k
+        assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
+    assert total_new > 0
+    s.close()
