@@ -144,6 +144,21 @@ def workload_cfg(args):
     return cfg
 
 
+def describe(cfg):
+    """(data, workload) strings of a synth.Config."""
+    g = "x".join(str(n) for n in cfg.cell_dim)
+    pores = ", %d radius-%d pores" % (cfg.n_pores, cfg.pore_radius) if cfg.n_pores else ""
+    data = "synthetic: seeded periodic Voronoi, %d grains, uniform SO(3) orientations%s" % (cfg.n_grains, pores)
+    e = cfg.velgrad_bc[2]
+    load = "uniaxial %s eps33_dot=%g/s" % ("tension" if e > 0 else "compression", e)
+    m = cfg.material
+    wl = "%s RVE, %d grains%s, FCC Cu power law n=%g + Voce, %s, dt=%g, IterMax=%d" % (
+        g, cfg.n_grains, pores, m.nrs, load, cfg.time_step, cfg.iter_max)
+    if cfg.drx is not None:
+        wl += ", coupled DRX (%d PF substeps, K=8)" % cfg.drx.pf_substeps
+    return data, wl
+
+
 # ------------------------------------------------------------ GPU arm
 def run_gpu(args):
     import torch
@@ -210,16 +225,17 @@ def run_gpu(args):
     vox_it = reduce_sum(float(nv) * iters)
     value = vox_it / (ms_max / 1e3)
 
+    fb = nv * 55 * (8 if prec == capi.MTH_FP64 else 4) / 1e9   # field planes + half spectra
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": {capi.MTH_MIXED: "f32 fields + f64 Newton solve", capi.MTH_FP64: "f64",
                      capi.MTH_MIXED_FAST: "f32"}[prec],
-           "data": "synthetic: seeded periodic Voronoi, 512 grains, uniform SO(3) orientations, 40 radius-3 pores",
-           "config": {"workload": "128^3 RVE, 512 grains, 40 pores, FCC Cu power law n=10 + Voce, uniaxial "
-                                  "tension eps33_dot=1/s, dt=1e-3, IterMax=%d" % cfg.iter_max,
+           "data": describe(cfg)[0],
+           "config": {"workload": describe(cfg)[1],
                       "grid": list(cfg.cell_dim), "voxels": nv, "green_iterations": iters,
                       "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single GPU",
-                      "l2": "fields (~0.5 GB) larger than the 129 MB L2; no flush"}}
+                      "l2": ("fields (%.2f GB) larger than the 129 MB L2; no flush" % fb if fb > 0.129 else
+                             "fields (%.3f GB) fit in the 129 MB L2: a profiling case, not an HBM measurement" % fb)}}
 
     # roofline of the dominant kernel (device time from CUDA events on the library stream)
     dom = max(((k, v) for k, v in prof.items() if v["bytes"] > 0), key=lambda kv: kv[1]["ms"])
@@ -350,9 +366,8 @@ def run_reference(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-           "data": "synthetic: seeded periodic Voronoi, 512 grains, uniform SO(3) orientations, 40 radius-3 pores",
-           "config": {"workload": "128^3 RVE, 512 grains, 40 pores, FCC Cu power law n=10 + Voce, uniaxial "
-                                  "tension eps33_dot=1/s, dt=1e-3", "grid": list(c.cell_dim),
+           "data": describe(c)[0],
+           "config": {"workload": describe(cfg)[1] + " (one Green iteration per step timed)", "grid": list(c.cell_dim),
                       "parallelism": "OpenMP %d threads" % cores},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

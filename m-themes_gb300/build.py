@@ -26,6 +26,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CU_SOURCES = ["fft_green.cu", "fft_tma.cu", "newton.cu", "drx.cu", "capi.cu"]
 # sources compiled without FMA contraction (bit-exact FP64 restatement)
 NO_FMAD = {"drx.cu"}
+# sources whose host code is compiled without FMA contraction: the FP64 host
+# bookkeeping gives the same doubles on x86 and Arm (gcc contracts by default
+# on aarch64), and host-side tensor conversions match the device's rounded,
+# uncontracted ones
+NO_HOST_CONTRACT = {"capi.cu"}
 C_SOURCES = ["mth_io.c"]
 
 
@@ -63,6 +68,8 @@ def build(force=False, verbose=False):
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             extra = ["-fmad=false"] if s in NO_FMAD else []
+            if s in NO_HOST_CONTRACT:
+                extra += ["-Xcompiler", "-ffp-contract=off"]
             jobs.append([nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
     for s in C_SOURCES:
         src = os.path.join(HOST, s)

@@ -271,6 +271,8 @@ struct mth_ctx {
   bool in_batch;      // red, err_d, add_d, live_d and the stream belong to a batch
   bool tma_off;       // shared-memory passes even where tensor maps exist (tuning)
   struct IoutWriter* iout;   // background writer of per-step field files
+  double* dl_d;       // download staging in the host layout
+  size_t dl_cap;      // doubles
   // state of the mechanical step in progress (mth_step and the batch driver)
   int it_iter, it_nnew;
   long long it_nit, it_nbad;
@@ -385,6 +387,7 @@ static void ctx_free(mth_ctx* c) {
   cudaFree(c->crystal_d);
   cudaFree(c->hist_d);
   cudaFree(c->gather_d);
+  cudaFree(c->dl_d);
   cudaFree(c->grain_pf_d);
   cudaFree(c->rho_pf_d);
   cudaFree(c->rho_pf_t);
@@ -731,6 +734,8 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   std::vector<double> rows;
   std::vector<long long> counts;
   long long nph1 = 0;
+  int last_k = -1, last_key[1] = {0};
+  double last_e[3] = {0, 0, 0};
   for (size_t v = 0; v < n; v++) {
     if (phase[v] < 1 || phase[v] > c->p.n_phases)
       return set_err(MTH_ERR_ARG, "voxel %zu has phase %d (N_phases=%d)", v, phase[v], c->p.n_phases);
@@ -739,6 +744,12 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
     const PhaseConst& pc = c->nc.ph[phase[v] - 1];
     if (pc.type != 0) continue;
     const double* e = euler_deg + 3 * v;
+    // consecutive voxels mostly lie in one grain: reuse the previous class
+    if (last_k >= 0 && phase[v] == last_key[0] && e[0] == last_e[0] && e[1] == last_e[1] && e[2] == last_e[2]) {
+      counts[last_k]++;
+      ecl[v] = last_k;
+      continue;
+    }
     auto key = std::make_tuple(phase[v], e[0], e[1], e[2]);
     auto it = key2class.find(key);
     int k;
@@ -755,6 +766,11 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
     }
     counts[k]++;
     ecl[v] = k;
+    last_k = k;
+    last_key[0] = phase[v];
+    last_e[0] = e[0];
+    last_e[1] = e[1];
+    last_e[2] = e[2];
   }
   if (counts.empty()) return set_err(MTH_ERR_ARG, "no crystal voxel in the microstructure");
   memset(c->c066, 0, sizeof(c->c066));
@@ -1248,21 +1264,20 @@ static mth_status download(mth_ctx* c, int field, double* host) {
     case MTH_FIELD_GAMACUM: src = f.gamacum; nc = 1; break;
     default: return set_err(MTH_ERR_ARG, "field %d", field);
   }
-  std::vector<T> h((size_t)nc * P);
-  CK(cudaMemcpyAsync(h.data(), src, sizeof(T) * nc * P, cudaMemcpyDeviceToHost, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  if (nc == 6) {
-    for (long long v = 0; v < P; v++) {
-      double s6[6];
-      t33 t;
-      for (int i = 0; i < 6; i++) s6[i] = (double)h[i * P + v];
-      v2t(s6, t, 6);
-      memcpy(host + 9 * v, t, sizeof(t33));
-    }
-  } else {
-    for (long long v = 0; v < P; v++)
-      for (int i = 0; i < nc; i++) host[nc * v + i] = (double)h[i * P + v];
+  // converted to the host layout on the device, then one copy into the
+  // caller's buffer (a pinned buffer gets the full copy bandwidth)
+  const size_t out = (size_t)(nc == 6 ? 9 : nc) * P;
+  if (c->dl_cap < out) {
+    CK(cudaStreamSynchronize(c->st));
+    cudaFree(c->dl_d);
+    c->dl_d = nullptr;
+    c->dl_cap = 0;
+    CK(cudaMalloc(&c->dl_d, sizeof(double) * out));
+    c->dl_cap = out;
   }
+  CK(launch_to_host_layout(c->mixed, src, P, nc, nc == 6 ? 1 : 0, c->dl_d, c->st));
+  CK(cudaMemcpyAsync(host, c->dl_d, sizeof(double) * out, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return MTH_OK;
 }
 

@@ -185,6 +185,9 @@ long long noalloc_max_voxels();
 cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,
                                        const double* strain, const double* rot, const double* crss, double* edot,
                                        double* err, long long* iters_host, cudaStream_t st);
+// field planes (6 LT planes when sym, else nc planes) -> voxel-major doubles
+cudaError_t launch_to_host_layout(int mixed, const void* src, long long P, int nc, int sym, double* dst,
+                                  cudaStream_t st);
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
                                    cudaStream_t st);
 

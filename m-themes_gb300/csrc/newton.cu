@@ -830,6 +830,45 @@ cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, c
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ downloads
+// Field planes to voxel-major doubles for the host: a symmetric tensor of 6
+// LT planes becomes the 3x3 row-major Cartesian tensor t = sum_i v_i B_i
+// (the products and left-to-right sums of the host conversion, with
+// rounded, uncontracted operations, so both give the same doubles); other
+// fields are interleaved per voxel.
+template <typename TSt>
+__global__ void to_host_layout_kernel(const TSt* __restrict__ src, long long P, int nc, int sym,
+                                      double* __restrict__ dst) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= P) return;
+  if (sym) {
+    double a[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) a[i] = (double)src[i * P + v];
+    const double r2 = RSQ2, r3 = RSQ3, r6 = RSQ6;
+    const double t00 = __dadd_rn(__dadd_rn(__dmul_rn(a[0], -r2), __dmul_rn(a[1], -r6)), __dmul_rn(a[5], r3));
+    const double t11 = __dadd_rn(__dadd_rn(__dmul_rn(a[0], r2), __dmul_rn(a[1], -r6)), __dmul_rn(a[5], r3));
+    const double t22 = __dadd_rn(__dmul_rn(a[1], 2. * r6), __dmul_rn(a[5], r3));
+    const double t12 = __dmul_rn(a[2], r2), t02 = __dmul_rn(a[3], r2), t01 = __dmul_rn(a[4], r2);
+    double* o = dst + 9 * v;
+    o[0] = t00; o[1] = t01; o[2] = t02;
+    o[3] = t01; o[4] = t11; o[5] = t12;
+    o[6] = t02; o[7] = t12; o[8] = t22;
+  } else {
+    for (int i = 0; i < nc; i++) dst[nc * v + i] = (double)src[i * P + v];
+  }
+}
+
+cudaError_t launch_to_host_layout(int mixed, const void* src, long long P, int nc, int sym, double* dst,
+                                  cudaStream_t st) {
+  const int nb = (int)((P + 255) / 256);
+  if (mixed)
+    to_host_layout_kernel<float><<<nb, 256, 0, st>>>(static_cast<const float*>(src), P, nc, sym, dst);
+  else
+    to_host_layout_kernel<double><<<nb, 256, 0, st>>>(static_cast<const double*>(src), P, nc, sym, dst);
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------- batch local solve
 __global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, long long n, double* __restrict__ sig,
                                                           const double* __restrict__ epsp,

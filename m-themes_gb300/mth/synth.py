@@ -301,6 +301,9 @@ def workload(name: str) -> Config:
         return Config(cell_dim=(64, 64, 64), n_grains=125, n_steps=10, seed=20240105, iter_max=10,
                       velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0),
                       drx=Drx(rho_k=40000.0, nucleation_prob=2e-3))
+    if name == "c2f":   # c2 with nucleation from the second step on: the DRX step at 128^3 every step
+        return Config(cell_dim=(128, 128, 128), n_grains=1000, n_steps=500, seed=20240104,
+                      velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0), drx=Drx(rho_k=40000.0, nucleation_prob=2e-4))
     if name == "c1m":   # 96^3 profiling case of c1: fields still larger than L2
         return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
                       n_steps=100, seed=20240103)
