@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--precision", choices=["mixed", "fp64", "mixed_fast"], default="mixed")
+    ap.add_argument("--precision", choices=["mixed", "fp64", "mixed_fast", "mixed_root64"], default="mixed")
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--iter-max", type=int, default=0, help="override IterMax (default: the workload's 100)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
@@ -173,7 +173,8 @@ def run_gpu(args):
     cfg = replicas.replica_config(workload_cfg(args), rank)   # replicas: each rank its own RVE
     grain, phase, euler = synth.microstructure(cfg)
     nv = int(np.prod(cfg.cell_dim))
-    prec = {"mixed": capi.MTH_MIXED, "fp64": capi.MTH_FP64, "mixed_fast": capi.MTH_MIXED_FAST}[args.precision]
+    prec = {"mixed": capi.MTH_MIXED, "fp64": capi.MTH_FP64, "mixed_fast": capi.MTH_MIXED_FAST,
+            "mixed_root64": capi.MTH_MIXED_ROOT64}[args.precision]
 
     def barrier_sync():
         torch.cuda.synchronize()
@@ -229,7 +230,7 @@ def run_gpu(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": {capi.MTH_MIXED: "f32 fields + f64 Newton solve", capi.MTH_FP64: "f64",
-                     capi.MTH_MIXED_FAST: "f32"}[prec],
+                     capi.MTH_MIXED_FAST: "f32", capi.MTH_MIXED_ROOT64: "f32 fields + f64 Newton solve near the root"}[prec],
            "data": describe(cfg)[0],
            "config": {"workload": describe(cfg)[1],
                       "grid": list(cfg.cell_dim), "voxels": nv, "green_iterations": iters,
@@ -253,7 +254,8 @@ def run_gpu(args):
     tot_ms = sum(v["ms"] for v in prof.values())
     out["kernels"] = {k: {"ms": round(v["ms"], 3), "share": round(v["ms"] / tot_ms, 4) if tot_ms else None,
                           "launches": v["launches"],
-                          "gbs": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None}
+                          "gbs": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None,
+                          "hbm_frac": ((v["bytes"] / (v["ms"] / 1e3) / 1e9) / peak) if v["ms"] > 0 else None}
                       for k, v in prof.items() if v["launches"]}
     out["gpu_launches"] = launches
     out["clocks"] = clk
@@ -277,6 +279,13 @@ def run_gpu(args):
         ef = float(np.abs(repsf[-1]["sig_avg"] - b).max() / np.abs(b).max())
         out["mixed_fast"] = {"value": vf, "ms_per_step": msf / args.steps, "rel_stress_err_vs_fp64": ef,
                              "note": "MTH_MIXED_FAST: Jacobian solve in FP32 too"}
+        # opt-in variant with the FP64 solve only near the root
+        msr, itr, repsr, _, _, _ = timed_run(capi.MTH_MIXED_ROOT64, args.steps, args.warmup)
+        msr = reduce_max(msr)
+        vr = reduce_sum(float(nv) * itr) / (msr / 1e3)
+        er = float(np.abs(repsr[-1]["sig_avg"] - b).max() / np.abs(b).max())
+        out["mixed_root64"] = {"value": vr, "ms_per_step": msr / args.steps, "rel_stress_err_vs_fp64": er,
+                               "note": "MTH_MIXED_ROOT64: FP64 Jacobian solve only within 1e-3|lambda| of the root"}
 
     # end to end through the C-ABI with host buffers: create + upload (H2D of
     # the microstructure from pinned memory), K steps each returning the
@@ -382,7 +391,8 @@ def run_batch(args):
     import torch
     from mth import Batch, Solver, capi, synth
     cfgs = synth.batch_workload(args.workload)
-    prec = {"mixed": capi.MTH_MIXED, "fp64": capi.MTH_FP64, "mixed_fast": capi.MTH_MIXED_FAST}[args.precision]
+    prec = {"mixed": capi.MTH_MIXED, "fp64": capi.MTH_FP64, "mixed_fast": capi.MTH_MIXED_FAST,
+            "mixed_root64": capi.MTH_MIXED_ROOT64}[args.precision]
     params = [capi.params_from_config(c, precision=prec) for c in cfgs]
     micro = [synth.microstructure(c) for c in cfgs]
     nvs = [int(np.prod(c.cell_dim)) for c in cfgs]
@@ -407,7 +417,7 @@ def run_batch(args):
            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": {capi.MTH_MIXED: "f32 fields + f64 Newton solve", capi.MTH_FP64: "f64",
-                     capi.MTH_MIXED_FAST: "f32"}[prec],
+                     capi.MTH_MIXED_FAST: "f32", capi.MTH_MIXED_ROOT64: "f32 fields + f64 Newton solve near the root"}[prec],
            "data": "synthetic: per-RVE seeded periodic Voronoi, grains ~U[32,256], uniform SO(3), "
                    "tau0 ~U[12,20] MPa, n in {8,10,15,20}",
            "config": {"workload": "%d RVEs, uniaxial tension, dt=1e-3" % len(cfgs), "rves": len(cfgs),

@@ -42,7 +42,9 @@ typedef enum {
   MTH_FP64 = 0,       /* all fields, FFTs and the local Newton in FP64 */
   MTH_MIXED = 1,      /* FP32 fields/FFT/Green operator/flow rule; FP64 Jacobian solve of the
                          local Newton, FP64 error norms and volume averages */
-  MTH_MIXED_FAST = 2  /* as MTH_MIXED but the 5x5 Jacobian solve in FP32 too */
+  MTH_MIXED_FAST = 2, /* as MTH_MIXED but the 5x5 Jacobian solve in FP32 too */
+  MTH_MIXED_ROOT64 = 3 /* as MTH_MIXED but the Jacobian solve in FP64 only for the Newton steps
+                          within 1e-3 |lambda| of the root, in FP32 for the large early steps */
 } mth_precision;
 
 /* One phase: elastic constants plus the active slip mode of its .sx file

@@ -466,12 +466,14 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   if (p->n_phases < 1 || p->n_phases > MTH_NPH_MAX) return set_err(MTH_ERR_ARG, "N_phases=%d", p->n_phases);
   if (p->iter_max < 1) return set_err(MTH_ERR_ARG, "IterMax must be >= 1");
   if (!(p->time_step > 0)) return set_err(MTH_ERR_ARG, "TimeStep must be > 0");
-  if (p->precision != MTH_FP64 && p->precision != MTH_MIXED && p->precision != MTH_MIXED_FAST)
+  if (p->precision != MTH_FP64 && p->precision != MTH_MIXED && p->precision != MTH_MIXED_FAST &&
+      p->precision != MTH_MIXED_ROOT64)
     return set_err(MTH_ERR_ARG, "precision");
   mth_ctx* c = new mth_ctx();
   memset(c, 0, sizeof(*c));
   c->p = *p;
-  c->mixed = (p->precision == MTH_MIXED) ? 1 : (p->precision == MTH_MIXED_FAST) ? 2 : 0;
+  c->mixed = (p->precision == MTH_MIXED) ? 1 : (p->precision == MTH_MIXED_FAST) ? 2
+             : (p->precision == MTH_MIXED_ROOT64) ? 3 : 0;
   for (int i = 0; i < 3; i++) c->n[i] = p->cell_dim[i];
   c->nv = (long long)c->n[0] * c->n[1] * c->n[2];
   c->wgt = 1.0 / (double)c->nv;

@@ -197,18 +197,19 @@ struct VoxelOut {
 // orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
 // (plastic strain rate, sample frame).
 // TF: flow rule, residual, Hessian assembly, line search and frame
-// transforms; TL: accuracy of the Jacobian (Hessian) solve.  FP64 mode: both
-// double.  Mixed mode: TF = float, TL = double: once the Newton is within
-// 1e-3 |lambda| of the root (the iterations that fix the converged answer)
-// the FP32-assembled 5x5 system is factored and solved in FP64; the large
-// early steps, whose direction only has to be a descent direction, use the
-// FP32 factorisation (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
+// transforms; TL: precision of the Jacobian (Hessian) solve.  FP64 mode:
+// both double.  Mixed mode: TF = float, TL = double: the FP32-assembled 5x5
+// system is factored and solved in FP64 at every Newton step.  Mixed
+// root-FP64 mode (ROOT_ONLY): the FP64 solve only for the steps within
+// 1e-3 |lambda| of the root, which set the converged answer, and the FP32
+// factorisation for the large early steps, whose direction only has to be a
+// descent direction (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
 // mode: all float.
 // load(lam6, eps6, ep6, R, again) fills the voxel's inputs; it is called
 // at the start and again (again = true: loads the compiler may not merge
 // with the first) for the back-transform and the error norms, so neither
 // the inputs nor the 5x5 frame rotation stay live across the Newton loop.
-template <typename TF, typename TL, typename Load>
+template <typename TF, typename TL, bool ROOT_ONLY, typename Load>
 __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const TF* tauf,
                                 const Load& load, TF* sig6, TF* ed6) {
   VoxelOut o = {0.0, 0.0, 0, 0};
@@ -359,9 +360,10 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
 #pragma unroll
       for (int i = 0; i < 5; i++) mg[i] = -g[i];
       bool ok;
-      if (sizeof(TL) > sizeof(TF) && near_root) {
-        // FP64 Jacobian solve of the FP32-assembled system for the steps
-        // that set the converged answer
+      if (sizeof(TL) > sizeof(TF) && (!ROOT_ONLY || near_root)) {
+        // Jacobian solve in TL (FP64) of the TF-assembled system: at every
+        // step, or (ROOT_ONLY) for the steps within 1e-3 |lambda| of the
+        // root, which set the converged answer
         ok = ldl_solve5_wide<TF, TL>(H, mg, p);
       } else {
         ok = ldl_solve5<TF>(H, mg, p);
@@ -512,7 +514,7 @@ template <typename T>
 __device__ __forceinline__ T ld_sel(const T* p, bool again) { return again ? ld_again(p) : *p; }
 
 // ------------------------------------------------------------ Newton kernel
-template <typename TSt, typename TF, typename TS, int MINB>
+template <typename TSt, typename TF, typename TS, int MINB, bool ROOT_ONLY = false>
 __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials,
                                                                 IterIn it) {
   if (!is_live(it)) return;
@@ -540,7 +542,7 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
       };
       TF s6[6], e6[6];
       const TF* et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
-      VoxelOut o = solve_voxel<TF, TS>(nc, ph, et, tauf, load, s6, e6);
+      VoxelOut o = solve_voxel<TF, TS, ROOT_ONLY>(nc, ph, et, tauf, load, s6, e6);
 #pragma unroll
       for (int i = 0; i < 6; i++) {
         f.sig[i * P + v] = (TSt)s6[i];
@@ -598,6 +600,9 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     newton_kernel<float, float, float, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+  } else if (mixed == 3) {
+    const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+    newton_kernel<float, float, double, 2, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     newton_kernel<float, float, double, 2><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
@@ -892,7 +897,7 @@ __global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, 
     for (int i = 0; i < 6; i++) { l[i] = lam6[i]; e[i] = eps6[i]; q[i] = ep6[i]; }
     for (int i = 0; i < 9; i++) r[i] = R[i];
   };
-  VoxelOut o = solve_voxel<double, double>(nc, ph, etab + (size_t)v * ETAB_W, tauf, load, s6, e6);
+  VoxelOut o = solve_voxel<double, double, false>(nc, ph, etab + (size_t)v * ETAB_W, tauf, load, s6, e6);
   for (int i = 0; i < 6; i++) {
     sig[6 * v + i] = s6[i];
     edot[6 * v + i] = e6[i];
@@ -982,7 +987,7 @@ __global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonCo
       for (int i = 0; i < 6; i++) { l[i] = lam6[i]; e[i] = eps6[i]; q[i] = ep6[i]; }
       for (int i = 0; i < 9; i++) r[i] = R[i];
     };
-    VoxelOut o = solve_voxel<double, double>(nc, ph, et, tauf, load, s6, e6);
+    VoxelOut o = solve_voxel<double, double, false>(nc, ph, et, tauf, load, s6, e6);
     for (int i = 0; i < 6; i++) {
       sig[6 * v + i] = s6[i];
       edot[6 * v + i] = e6[i];

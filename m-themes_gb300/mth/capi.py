@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(PKG_ROOT, "lib", "libmth.so")
 MTH_FP64 = 0
 MTH_MIXED = 1
 MTH_MIXED_FAST = 2
+MTH_MIXED_ROOT64 = 3
 
 FIELD = {"sig": 0, "eps": 1, "edot": 2, "strain": 3, "rot": 4, "crss": 5, "gamacum": 6, "grain": 7, "rho": 8}
 FIELD_NCOMP = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 1, 7: 1, 8: 1}

@@ -55,10 +55,11 @@ def test_fp64_matches_reference(name):
     s.close()
 
 
+@pytest.mark.parametrize("precision", [capi.MTH_MIXED, capi.MTH_MIXED_FAST, capi.MTH_MIXED_ROOT64])
 @pytest.mark.parametrize("name", ["g8_poly", "g12_radix3", "g16_pores", "g8_shear"])
-def test_mixed_within_tolerance(name):
+def test_mixed_within_tolerance(name, precision):
     cfg, trace, _ = load_golden(name)
-    s, reps = run_gpu(cfg, capi.MTH_MIXED)
+    s, reps = run_gpu(cfg, precision)
     for k, r in enumerate(reps):
         assert rel(r["sig_avg"], trace[k][T_SIG].reshape(3, 3)) < MIXED_MACRO, k
         assert rel(r["disgrad_avg"], trace[k][T_DG].reshape(3, 3)) < MIXED_MACRO, k
@@ -67,7 +68,8 @@ def test_mixed_within_tolerance(name):
 
 # (48, 8, 16), (8, 24, 6): shared-memory passes (a line length without a
 # compile-time plan); the others: TMA passes, incl. radix-3 and anisotropic
-@pytest.mark.parametrize("dims", [(48, 8, 16), (8, 24, 6), (32, 32, 32), (48, 32, 16), (32, 16, 96)])
+@pytest.mark.parametrize("dims", [(48, 8, 16), (8, 24, 6), (32, 32, 32), (48, 32, 16), (32, 16, 96), (256, 16, 16),
+                                  (16, 16, 256)])
 def test_fp64_matches_oracle_shapes(dims):
     cfg = synth.Config(cell_dim=dims, n_grains=12, n_steps=3, seed=31, iter_max=12)
     o, ro = run_oracle(cfg)
@@ -93,6 +95,22 @@ def test_mixed_matches_oracle_shapes(dims):
     s.close()
 
 
+def test_256cube_mixed_properties():
+    """256^3 (the largest compile-time line length on every axis), mixed
+    precision, one step of 3 Green iterations: size-independent checks."""
+    cfg = synth.Config(cell_dim=(256, 256, 256), n_grains=300, n_steps=1, seed=41, iter_max=3)
+    g, p, e = synth.microstructure(cfg)
+    from mth import Solver
+    s = Solver(capi.params_from_config(cfg, precision=capi.MTH_MIXED), g, p, e)
+    r = s.step()
+    assert r["iterations"] == 3
+    assert np.all(np.isfinite(r["sig_avg"]))
+    assert abs(r["disgrad_avg"][2, 2] - cfg.time_step) < 1e-12
+    sig = s.field("sig").reshape(-1, 3, 3)
+    assert np.all(np.isfinite(sig))
+    s.close()
+
+
 def test_local_solve_matches_oracle():
     import pyoracle
     from test_oracle_cpu import random_states
@@ -111,10 +129,12 @@ def test_local_solve_matches_oracle():
     assert rel(errg[:, 0], erro[:, 0]) < 1e-6
 
 
-def test_deterministic_fp64():
-    cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=6, n_steps=2, seed=9, iter_max=8)
-    s1, r1 = run_gpu(cfg, capi.MTH_FP64)
-    s2, r2 = run_gpu(cfg, capi.MTH_FP64)
+@pytest.mark.parametrize("precision", [capi.MTH_FP64, capi.MTH_MIXED])
+def test_deterministic(precision):
+    """Bitwise-repeatable runs: fixed-order reductions, no atomics on the path."""
+    cfg = synth.Config(cell_dim=(32, 16, 48), n_grains=6, n_steps=2, seed=9, iter_max=8)
+    s1, r1 = run_gpu(cfg, precision)
+    s2, r2 = run_gpu(cfg, precision)
     assert np.array_equal(s1.field("sig"), s2.field("sig"))
     assert all(np.array_equal(a["sig_avg"], b["sig_avg"]) for a, b in zip(r1, r2))
 
