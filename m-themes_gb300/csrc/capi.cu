@@ -378,6 +378,8 @@ static void ctx_free(mth_ctx* c) {
   }
   cudaFree(c->pff.gid);
   cudaFree(c->pfd.gid);
+  cudaFree(c->pff.pl_id); cudaFree(c->pff.pl_sum); cudaFree(c->pff.pl_cnt); cudaFree(c->pff.pl_n);
+  cudaFree(c->pfd.pl_id); cudaFree(c->pfd.pl_sum); cudaFree(c->pfd.pl_cnt); cudaFree(c->pfd.pl_n);
   cudaFree(c->rho_d);
   cudaFree(c->rho_t);
   cudaFree(c->grain_prev_d);
@@ -642,6 +644,10 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
       CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.cnt[i] : (void*&)c->pfd.cnt[i]), Q));
     }
     CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.gid : (void*&)c->pfd.gid), sizeof(int) * Q));
+    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_id : (void*&)c->pfd.pl_id), sizeof(int) * PF_PATCH * Q));
+    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_sum : (void*&)c->pfd.pl_sum), esz * PF_PATCH * Q));
+    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_cnt : (void*&)c->pfd.pl_cnt), (size_t)PF_PATCH * Q));
+    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_n : (void*&)c->pfd.pl_n), (size_t)Q));
     if (c->pf_resample) {
       CKC(cudaMalloc(&c->grain_pf_d, sizeof(int) * Q));
       CKC(cudaMalloc(&c->rho_pf_d, sizeof(double) * Q));
@@ -982,14 +988,16 @@ static mth_status refresh_reference_medium(mth_ctx* c) {
 
 // Algorithmic HBM bytes of one phase-field relaxation of nv voxels with
 // field element size ts: each pass reads and/or writes the sparse state
-// (PF_K ids and order parameters and a count per voxel) once; neighbour
-// reads are served from cache.
+// (PF_K ids and order parameters and a count per voxel) once, the patch pass
+// reads the grain ids and rho and writes the patch lists (about two ids per
+// patch); neighbour reads are served from cache.
 static double pf_relax_bytes(long long nv, size_t ts, int substeps) {
   const double state = PF_K * (4.0 + (double)ts) + 1.0;
   const double init = 4.0 + state + 4.0;                   // grain in; state, grain id out
   const double sub = 2.0 * state + (double)ts + 4.0;       // state in and out, rho, grain id
   const double amax = state + 4.0;                         // state in, grain id out
-  return (double)nv * (init + substeps * (sub + amax));
+  const double patch = 4.0 + (double)ts + 2.0 * (5.0 + (double)ts) + 1.0;   // gid, rho in; ~2 patch entries out
+  return (double)nv * (init + substeps * (sub + amax + patch));
 }
 
 // Dynamic recrystallisation at the start of a mechanical step, the order of
@@ -1073,11 +1081,11 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   }
   int* gid_new;
   if (c->mixed) {
-    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(float), p.pf_substeps),
+    LAUNCHN(K_PF, 1 + 3 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(float), p.pf_substeps),
             launch_pf_relax<float>(c->npf, pf_grain, (const float*)pf_rho, p.pf_substeps, c->pfc, c->pff, c->st));
     gid_new = c->pff.gid;
   } else {
-    LAUNCHN(K_PF, 1 + 2 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(double), p.pf_substeps),
+    LAUNCHN(K_PF, 1 + 3 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(double), p.pf_substeps),
             launch_pf_relax<double>(c->npf, pf_grain, (const double*)pf_rho, p.pf_substeps, c->pfc, c->pfd, c->st));
     gid_new = c->pfd.gid;
   }
@@ -1557,6 +1565,10 @@ static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* 
     if (e == cudaSuccess) e = cudaMalloc(&b.cnt[i], nv);
   }
   if (e == cudaSuccess) e = cudaMalloc(&b.gid, sizeof(int) * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&b.pl_id, sizeof(int) * PF_PATCH * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&b.pl_sum, sizeof(T) * PF_PATCH * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&b.pl_cnt, (size_t)PF_PATCH * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&b.pl_n, (size_t)nv);
   if (e == cudaSuccess) e = cudaMalloc(&g_d, sizeof(int) * nv);
   if (e == cudaSuccess) e = cudaMalloc(&r_d, sizeof(T) * nv);
   if (e == cudaSuccess) e = cudaMemcpyAsync(g_d, grain, sizeof(int) * nv, cudaMemcpyHostToDevice, s);
@@ -1584,6 +1596,10 @@ static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* 
   }
   for (int i = 0; i < 2; i++) { cudaFree(b.ids[i]); cudaFree(b.phi[i]); cudaFree(b.cnt[i]); }
   cudaFree(b.gid);
+  cudaFree(b.pl_id);
+  cudaFree(b.pl_sum);
+  cudaFree(b.pl_cnt);
+  cudaFree(b.pl_n);
   cudaFree(g_d);
   cudaFree(r_d);
   if (s) cudaStreamDestroy(s);

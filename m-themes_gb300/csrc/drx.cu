@@ -127,12 +127,57 @@ __device__ __forceinline__ void sorted_insert(int* list, int& nl, int id) {
   nl++;
 }
 
+// Per voxel (x,y,z): for each grain id in the 7x7 patch of the x plane
+// (y-3..y+3, z-3..z+3) the sum of rho in (y,z) order and the voxel count;
+// up to PF_PATCH ids, else the patch is marked (n = 255) and the substep
+// scans it directly.
+template <typename T>
+__global__ void __launch_bounds__(256) pf_patch_kernel(Dims d, const int* __restrict__ gid, const T* __restrict__ rho,
+                                                       int* __restrict__ pl_id, T* __restrict__ pl_sum,
+                                                       uint8_t* __restrict__ pl_cnt, uint8_t* __restrict__ pl_n) {
+  const long long nv = (long long)d.n0 * d.n1 * d.n2;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int x = (int)(v / ((long long)d.n1 * d.n2)), y = (int)((v / d.n2) % d.n1), z = (int)(v % d.n2);
+  int id[PF_PATCH];
+  T sm[PF_PATCH];
+  int ct[PF_PATCH];
+  int n = 0;
+  bool over = false;
+  for (int dy = -3; dy <= 3 && !over; dy++)
+    for (int dz = -3; dz <= 3; dz++) {
+      const long long w = d.idx(x, y + dy, z + dz);
+      const int g = gid[w];
+      int i = 0;
+      while (i < n && id[i] != g) i++;
+      if (i == n) {
+        if (n == PF_PATCH) { over = true; break; }
+        id[n] = g;
+        sm[n] = (T)0;
+        ct[n] = 0;
+        n++;
+      }
+      sm[i] = sm[i] + rho[w];
+      ct[i]++;
+    }
+  pl_n[v] = over ? (uint8_t)255 : (uint8_t)n;
+  if (over) return;
+  for (int i = 0; i < n; i++) {
+    pl_id[(long long)i * nv + v] = id[i];
+    pl_sum[(long long)i * nv + v] = sm[i];
+    pl_cnt[(long long)i * nv + v] = (uint8_t)ct[i];
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) pf_substep_kernel(Dims d, const int* __restrict__ ids, const T* __restrict__ phi,
                                                          const uint8_t* __restrict__ cnt, int* __restrict__ ids2,
                                                          T* __restrict__ phi2, uint8_t* __restrict__ cnt2,
                                                          const int* __restrict__ gid, const T* __restrict__ rho,
-                                                         T mcoef, T kappa, T mwell, T edisl) {
+                                                         T mcoef, T kappa, T mwell, T edisl,
+                                                         const int* __restrict__ pl_id, const T* __restrict__ pl_sum,
+                                                         const uint8_t* __restrict__ pl_cnt,
+                                                         const uint8_t* __restrict__ pl_n) {
   const long long nv = (long long)d.n0 * d.n1 * d.n2;
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
@@ -166,17 +211,40 @@ __global__ void __launch_bounds__(128) pf_substep_kernel(Dims d, const int* __re
     wsum[i] = (T)0;
     wcnt[i] = 0;
   }
-  for (int dx = -3; dx <= 3; dx++)
-    for (int dy = -3; dy <= 3; dy++)
-      for (int dz = -3; dz <= 3; dz++) {
-        const long long w = d.idx(x + dx, y + dy, z + dz);
-        const int g = gid[w];
-        for (int i = 0; i < nu; i++)
-          if (uid[i] == g) {
-            wsum[i] = wsum[i] + rho[w];
-            wcnt[i]++;
+  // window sums: the seven x planes' patch sums added in x order
+  for (int dx = -3; dx <= 3; dx++) {
+    const long long u = d.idx(x + dx, y, z);
+    const int pn = pl_n[u];
+    if (pn != 255) {
+      for (int i = 0; i < nu; i++) {
+        T ps = (T)0;
+        int pc = 0;
+        for (int j = 0; j < pn; j++)
+          if (pl_id[(long long)j * nv + u] == uid[i]) {
+            ps = pl_sum[(long long)j * nv + u];
+            pc = pl_cnt[(long long)j * nv + u];
+            break;
           }
+        wsum[i] = wsum[i] + ps;
+        wcnt[i] += pc;
       }
+    } else {   // more ids in that patch than the list holds: scan it here
+      for (int i = 0; i < nu; i++) {
+        T ps = (T)0;
+        int pc = 0;
+        for (int dy = -3; dy <= 3; dy++)
+          for (int dz = -3; dz <= 3; dz++) {
+            const long long w = d.idx(x + dx, y + dy, z + dz);
+            if (gid[w] == uid[i]) {
+              ps = ps + rho[w];
+              pc++;
+            }
+          }
+        wsum[i] = wsum[i] + ps;
+        wcnt[i] += pc;
+      }
+    }
+  }
   T rbar[MAXIDS];
   for (int i = 0; i < nu; i++) rbar[i] = wcnt[i] > 0 ? wsum[i] / (T)wcnt[i] : (T)0;
   T sum_rex = 0, sum1 = 0, hdef = 0;
@@ -301,9 +369,13 @@ cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, i
   if (e != cudaSuccess) return e;
   int cur = 0;
   for (int s = 0; s < substeps; s++) {
+    pf_patch_kernel<T><<<nb(nv, 256), 256, 0, st>>>(d, b.gid, rho, b.pl_id, b.pl_sum, b.pl_cnt, b.pl_n);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     pf_substep_kernel<T><<<nb(nv, 128), 128, 0, st>>>(d, b.ids[cur], b.phi[cur], b.cnt[cur], b.ids[1 - cur],
                                                       b.phi[1 - cur], b.cnt[1 - cur], b.gid, rho, (T)co.mcoef,
-                                                      (T)co.kappa, (T)co.mwell, (T)co.edisl);
+                                                      (T)co.kappa, (T)co.mwell, (T)co.edisl, b.pl_id, b.pl_sum,
+                                                      b.pl_cnt, b.pl_n);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     cur = 1 - cur;

@@ -155,7 +155,14 @@ struct PfBuffers {
   uint8_t* cnt[2];
   int* gid;           // current argmax grain id
   int cur;            // buffer holding the result
+  // per voxel: stored energy summed per grain id over its 7x7 (y,z) patch
+  // (PF_PATCH entries, component-major; count 255 = more ids than entries)
+  int* pl_id;
+  T* pl_sum;
+  uint8_t* pl_cnt;
+  uint8_t* pl_n;
 };
+constexpr int PF_PATCH = 8;
 
 cudaError_t launch_nucleation_candidates(const int dims[3], const int* grain, const uint8_t* crystal, const double* rho,
                                          double rho_nuc, double prob, uint64_t seed, uint64_t counter0,

@@ -164,17 +164,24 @@ static void pf_substep(const int* n, int K, const int* ids, const double* phi, c
     int uid[MAXIDS], nu = 0;
     for (int i = 0; i < nn; i++) sorted_insert(uid, &nu, nid[i]);
     for (int s = 0; s < cnt[v]; s++) sorted_insert(uid, &nu, ids[v * K + s]);
+    /* window sums per id, in a fixed association: the 7x7 (y,z) patch of
+       each x plane summed in (y,z) order, then the seven planes in x order */
     double wsum[MAXIDS];
     int wcnt[MAXIDS];
     for (int i = 0; i < nu; i++) { wsum[i] = 0.0; wcnt[i] = 0; }
-    for (int dx = -3; dx <= 3; dx++)
+    for (int dx = -3; dx <= 3; dx++) {
+      double psum[MAXIDS];
+      int pcnt[MAXIDS];
+      for (int i = 0; i < nu; i++) { psum[i] = 0.0; pcnt[i] = 0; }
       for (int dy = -3; dy <= 3; dy++)
         for (int dz = -3; dz <= 3; dz++) {
           long long w = vidx(n, x + dx, y + dy, z + dz);
           const int g = gid[w];
           for (int i = 0; i < nu; i++)
-            if (uid[i] == g) { wsum[i] = wsum[i] + rho[w]; wcnt[i]++; }
+            if (uid[i] == g) { psum[i] = psum[i] + rho[w]; pcnt[i]++; }
         }
+      for (int i = 0; i < nu; i++) { wsum[i] = wsum[i] + psum[i]; wcnt[i] += pcnt[i]; }
+    }
     double rbar[MAXIDS];
     for (int i = 0; i < nu; i++) rbar[i] = wcnt[i] > 0 ? wsum[i] / (double)wcnt[i] : 0.0;
     /* sums over the order parameters held at v (src/pf_xrx.c:1096-1104) */
