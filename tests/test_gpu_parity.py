@@ -181,3 +181,41 @@ def test_status_codes():
     assert lib.mth_download_field(ctx, 0, capi._dptr(out), 10) == 1
     assert lib.mth_step(ctx, C.byref(rep)) == 0
     assert lib.mth_destroy(ctx) == 0
+
+
+def _two_crystal_phases(precision):
+    """Two crystal phases (Type_phases 0 0): phase 2 with its own CRSS, Voce
+    and rate exponent on the odd grains."""
+    import ctypes as C
+    cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=8, n_steps=3, seed=71, iter_max=15)
+    par = capi.params_from_config(cfg, precision=precision)
+    par.n_phases = 2
+    C.memmove(C.byref(par.phase[1]), C.byref(par.phase[0]), C.sizeof(capi.MthPhase))
+    ph = par.phase[1]
+    ph.type = 0
+    ph.tau0f = ph.tau0b = 24.0
+    ph.tau1, ph.thet0, ph.thet1 = 120.0, 400.0, 5.0
+    ph.nrs = 15.0
+    g, p, e = synth.microstructure(cfg)
+    p = np.where(g % 2 == 1, 2, 1).astype(np.int32)
+    return cfg, par, g, p, e
+
+
+@pytest.mark.parametrize("precision,tol", [(capi.MTH_FP64, FP64_MACRO), (capi.MTH_MIXED, MIXED_MACRO)])
+def test_two_crystal_phases_match_oracle(precision, tol):
+    import pyoracle
+    from mth import Solver
+    cfg, par, g, p, e = _two_crystal_phases(precision)
+    s = Solver(par, g, p, e)
+    par64 = _two_crystal_phases(capi.MTH_FP64)[1]
+    o = pyoracle.Oracle(par64, g, p, e, nthreads=4)
+    for k in range(cfg.n_steps):
+        a, b = s.step(), o.step()
+        assert a["iterations"] == b["iterations"] or precision != capi.MTH_FP64, k
+        assert rel(a["sig_avg"], b["sig_avg"]) < tol, k
+        assert rel(a["sig_avg_ph1"], b["sig_avg_ph1"]) < tol, k
+    if precision == capi.MTH_FP64:
+        assert rel_l2(s.field("sig"), o.field("sig")) < FP64_FIELD
+        assert rel(s.field("crss"), o.field("crss")) < 1e-7
+    s.close()
+    o.close()
