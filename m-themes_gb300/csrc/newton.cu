@@ -122,9 +122,29 @@ __device__ __forceinline__ void symv5(const T* K, const T* x, T* y) {
   }
 }
 
+// 1/d for a positive normal FP64 pivot: the hardware estimate
+// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps
+// r <- r + r (1 - d r), each of which doubles the number of correct bits,
+// so the result is within a few ulp of 1/d without the special-case
+// handling of a correctly rounded divide.
+__device__ __forceinline__ double pivot_rcp_nr(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+template <typename T, bool NR>
+__device__ __forceinline__ T pivot_inv(T d) {
+  if constexpr (NR && sizeof(T) == 8) return pivot_rcp_nr(d);
+  else return (T)1 / d;
+}
+
 // LDL^T solve of the packed symmetric positive definite 5x5 matrix A:
-// x = A^-1 b.  Returns false when a pivot is not positive.
-template <typename T>
+// x = A^-1 b.  Returns false when a pivot is not positive.  NR: pivot
+// reciprocals by pivot_rcp_nr (FP64 solves of the mixed modes).
+template <typename T, bool NR = false>
 __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
   T L[5][5], d[5], id[5];
 #pragma unroll
@@ -139,7 +159,7 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
       }
     if (!(dj > (T)0)) return false;
     d[j] = dj;
-    id[j] = (T)1 / dj;
+    id[j] = pivot_inv<T, NR>(dj);
 #pragma unroll
     for (int i = 0; i < 5; i++)
       if (i > j) {
@@ -178,7 +198,7 @@ __device__ __forceinline__ bool ldl_solve5_wide(const TF* H, const TF* b, TF* x)
   for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
 #pragma unroll
   for (int i = 0; i < 5; i++) bl[i] = (TL)b[i];
-  const bool ok = ldl_solve5<TL>(Hl, bl, pl);
+  const bool ok = ldl_solve5<TL, true>(Hl, bl, pl);
 #pragma unroll
   for (int i = 0; i < 5; i++) x[i] = (TF)pl[i];
   return ok;
