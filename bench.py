@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration measurement")
     return ap.parse_args()
 
 
@@ -321,10 +322,53 @@ def run_gpu(args):
 
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_sample(cfg)
+    if not args.no_adjoint and args.workload == "c1":
+        out["adjoint"] = adjoint_measure(dev_index)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------------ calibration adjoint
+def adjoint_measure(dev_index, name="c4"):
+    """Cost of the calibration gradient (mth_adjoint: forward sweep with
+    stored states every 10 steps, recomputation, reverse sweep) against a
+    plain forward run of the same 64^3 / 256-grain, 50-step tension, mixed
+    precision with the FP64 Jacobian solve.  The target curve comes from the
+    forward model at tau0 = 18, thet0 = 280, tau1 = 160, n = 12."""
+    import dataclasses
+    import torch
+    from mth import Solver, capi, synth
+    cfg = synth.workload(name)
+    micro = synth.microstructure(cfg)
+
+    def params(c):
+        p = capi.params_from_config(c, precision=capi.MTH_MIXED)
+        p.device = dev_index
+        return p
+
+    tcfg = dataclasses.replace(cfg, material=synth.calibration_target_material())
+    with Solver(params(tcfg), *micro) as s:
+        target = np.array([s.step()["sig_avg"][2][2] for _ in range(cfg.n_steps)])
+    with Solver(params(cfg), *micro) as s:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its = 0
+        for _ in range(cfg.n_steps):
+            its += s.step()["iterations"]
+        torch.cuda.synchronize()
+        fwd_ms = (time.perf_counter() - t0) * 1e3
+    with Solver(params(cfg), *micro) as s:
+        J, g, s33, info = s.adjoint(target, checkpoint_every=10)
+    grad_ms = info["forward_ms"] + info["reverse_ms"]
+    return {"workload": "64x64x64 RVE, 256 grains, tension eps33_dot=1/s, 50 steps of 1e-3, mixed precision, "
+                        "misfit of <sigma_33> against the curve of (tau0, thet0, tau1, n) = (18, 280, 160, 12)",
+            "forward_ms": fwd_ms, "green_iterations": its, "gradient_ms": grad_ms,
+            "gradient_over_forward": grad_ms / fwd_ms, "reverse_over_forward": info["reverse_ms"] / fwd_ms,
+            "checkpoint_every": 10, "recomputed_steps": info["recomputed_steps"],
+            "cg_iterations": info["cg_iterations"], "cg_iterations_max_step": info["cg_iterations_max"],
+            "misfit": J, "grad": dict(zip(capi.ADJOINT_PARAMS, g.tolist()))}
 
 
 # ------------------------------------------------------------ CPU (oracle)

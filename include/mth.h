@@ -284,6 +284,45 @@ typedef struct {
 mth_status mth_profile_enable(mth_ctx* ctx, int on);
 mth_status mth_profile_read(mth_ctx* ctx, mth_profile* out, int reset);
 
+/* Calibration gradient by the adjoint of the converged fixed point.  The
+ * reference computes no gradients; this entry point runs the forward
+ * solve for n_steps mechanical steps from a freshly uploaded context and
+ * returns the misfit of the volume-averaged stress-strain curve
+ *   J = sum_n (<sigma_33>_n - target_n)^2
+ * and its derivatives with respect to the phase-1 parameters
+ * (tau0, tau1, thet0, thet1, nrs): tau0 shifts the forward and the
+ * backward initial CRSS together; tau1, thet0, thet1 are the Voce
+ * parameters of harden (src/constitutive.c:275-326) and nrs the exponent
+ * of the power law (src/constitutive.c:5-67).  Per mechanical step, in
+ * reverse order, one linear solve of the projected tangent problem (the
+ * transposed linearised Green iteration at the converged state) and the
+ * transposed local Jacobians of the flow rule, the Voce update and the
+ * lattice rotation.  States are stored every checkpoint_every steps and
+ * the steps between are recomputed.  Requires: every voxel of phase 1,
+ * a crystal; no phase-field DRX; ElastBC = 1; stress-controlled components
+ * only on the diagonal (11, 22, 33), with Stress_BC_Flag the complement of
+ * VelGrad_BC_Flag.  After the call the context holds the state after
+ * n_steps. */
+typedef struct {
+  int n_steps;              /* mechanical steps of the forward run (>= 1) */
+  int checkpoint_every;     /* steps between stored states; <= 0 selects 10 */
+  const double* target;     /* n_steps values of <sigma_33> to fit */
+  double cg_tol;            /* relative residual of each linear solve; <= 0 selects
+                               1e-7 (MTH_FP64) or 1e-5 (mixed modes) */
+  int cg_itmax;             /* <= 0 selects 2000 */
+} mth_adjoint_opts;
+typedef struct {
+  double misfit;            /* J */
+  double grad[5];           /* dJ/d(tau0, tau1, thet0, thet1, nrs) */
+  long long cg_iterations;  /* summed over the reverse steps */
+  int cg_iterations_max;    /* largest count of one step */
+  int recomputed_steps;     /* forward steps run again from checkpoints */
+  double forward_ms;        /* wall time of the first forward sweep */
+  double reverse_ms;        /* recomputation + reverse sweep */
+} mth_adjoint_result;
+/* s33 (may be NULL): n_steps values of <sigma_33> of the forward run. */
+mth_status mth_adjoint(mth_ctx* ctx, const mth_adjoint_opts* opts, double* s33, mth_adjoint_result* result);
+
 /* Host-side readers for the reference's input files. */
 /* input.in namelist (src/io.c:96-164); fills params and copies the file
  * names of the .sx files and the microstructure. */

@@ -87,6 +87,27 @@ class MthProfile(C.Structure):
         return out
 
 
+class MthAdjointOpts(C.Structure):
+    _fields_ = [("n_steps", C.c_int), ("checkpoint_every", C.c_int), ("target", C.POINTER(C.c_double)),
+                ("cg_tol", C.c_double), ("cg_itmax", C.c_int)]
+
+
+class MthAdjointResult(C.Structure):
+    _fields_ = [("misfit", C.c_double), ("grad", C.c_double * 5), ("cg_iterations", C.c_longlong),
+                ("cg_iterations_max", C.c_int), ("recomputed_steps", C.c_int), ("forward_ms", C.c_double),
+                ("reverse_ms", C.c_double)]
+
+    def to_dict(self):
+        return {"misfit": self.misfit, "grad": [self.grad[i] for i in range(5)],
+                "cg_iterations": self.cg_iterations, "cg_iterations_max": self.cg_iterations_max,
+                "recomputed_steps": self.recomputed_steps, "forward_ms": self.forward_ms,
+                "reverse_ms": self.reverse_ms}
+
+
+# order of the calibration parameters of mth_adjoint's gradient
+ADJOINT_PARAMS = ("tau0", "tau1", "thet0", "thet1", "nrs")
+
+
 def params_from_config(cfg, precision=MTH_FP64, newton_tol=0.0, newton_itmax=0) -> MthParams:
     """Fill MthParams from a synth.Config (power-law/Voce FCC, optional gas phase)."""
     from . import synth
@@ -206,6 +227,8 @@ def load(path: str | None = None):
     lib.mth_batch_step.argtypes = [C.c_void_p, C.POINTER(MthStepReport)]
     lib.mth_batch_download_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_size_t]
     lib.mth_batch_destroy.argtypes = [C.c_void_p]
+    lib.mth_adjoint.argtypes = [C.c_void_p, C.POINTER(MthAdjointOpts), C.POINTER(C.c_double),
+                                C.POINTER(MthAdjointResult)]
     if path is None:
         _lib = lib
     return lib

@@ -48,6 +48,24 @@ class Solver:
     def wait_iout(self):
         capi.check(self.lib, self.lib.mth_iout_wait(self.ctx))
 
+    def adjoint(self, target, checkpoint_every=10, cg_tol=0.0, cg_itmax=0):
+        """Misfit J = sum_n (<sigma_33>_n - target_n)^2 of a forward run of
+        len(target) steps from this (fresh) context and dJ/d(tau0, tau1,
+        thet0, thet1, nrs) by the adjoint (mth_adjoint).  Returns
+        (J, grad, s33, info)."""
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        opts = capi.MthAdjointOpts()
+        opts.n_steps = t.size
+        opts.checkpoint_every = checkpoint_every
+        opts.target = capi._dptr(t)
+        opts.cg_tol = cg_tol
+        opts.cg_itmax = cg_itmax
+        s33 = np.zeros(t.size)
+        res = capi.MthAdjointResult()
+        capi.check(self.lib, self.lib.mth_adjoint(self.ctx, C.byref(opts), capi._dptr(s33), C.byref(res)))
+        info = res.to_dict()
+        return info["misfit"], np.array(info["grad"]), s33, info
+
     def profile(self, enable=None, reset=False):
         """Per-kernel device times (CUDA events on the context's stream),
         launch counts and algorithmic bytes; optionally switch timing on/off."""

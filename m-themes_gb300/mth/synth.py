@@ -304,6 +304,10 @@ def workload(name: str) -> Config:
     if name == "c2f":   # c2 with nucleation from the second step on: the DRX step at 128^3 every step
         return Config(cell_dim=(128, 128, 128), n_grains=1000, n_steps=500, seed=20240104,
                       velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0), drx=Drx(rho_k=40000.0, nucleation_prob=2e-4))
+    if name == "c4":    # adjoint calibration: 64^3, 256 grains, tension for 50 steps of 1e-3
+        return Config(cell_dim=(64, 64, 64), n_grains=256, n_steps=50, seed=20240107)
+    if name == "c4s":   # small case of c4 for tests: 16^3, 8 grains, 5 steps
+        return Config(cell_dim=(16, 16, 16), n_grains=8, n_steps=5, seed=777)
     if name == "c1m":   # 96^3 profiling case of c1: fields still larger than L2
         return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
                       n_steps=100, seed=20240103)
@@ -331,3 +335,36 @@ def batch_workload(name: str = "c3", master_seed: int = 20240106) -> list:
         mat = Material(tau0f=tau0, tau0b=tau0, nrs=nrs)
         out.append(Config(cell_dim=(n, n, n), n_grains=n_grains, n_steps=50, seed=seed, material=mat))
     return out
+
+
+def calibration_target_material() -> Material:
+    """Parameters that generate the target stress-strain curve of the
+    adjoint calibration workload: tau0 = 18 MPa, thet0 = 280 MPa,
+    tau1 = 160 MPa, n = 12 (the other Cu values as Material())."""
+    return Material(tau0f=18.0, tau0b=18.0, thet0=280.0, tau1=160.0, nrs=12.0)
+
+
+def perturb_material(m: Material, k: int, h: float) -> Material:
+    """Copy of m with calibration parameter k (tau0, tau1, thet0, thet1, nrs
+    in that order; tau0 moves the forward and backward CRSS together)
+    shifted by h."""
+    r = dataclasses.replace(m)
+    if k == 0:
+        r.tau0f += h
+        r.tau0b += h
+    elif k == 1:
+        r.tau1 += h
+    elif k == 2:
+        r.thet0 += h
+    elif k == 3:
+        r.thet1 += h
+    elif k == 4:
+        r.nrs += h
+    else:
+        raise IndexError(k)
+    return r
+
+
+def calibration_values(m: Material) -> list:
+    """(tau0, tau1, thet0, thet1, nrs) of m."""
+    return [m.tau0f, m.tau1, m.thet0, m.thet1, m.nrs]

@@ -1,0 +1,158 @@
+"""Calibration adjoint (mth_adjoint): the gradient of the stress-strain
+misfit with respect to (tau0, tau1, thet0, thet1, nrs) against central
+finite differences (relative step 1e-4) of the FP64 forward, the mixed
+adjoint against the FP64 one, checkpoint spacing, the torch.autograd
+wrapper of the verification harness, and the rejected set-ups."""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+from mth import MthError, Solver, capi, synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _cfg(mat, precision, steps=4, **kw):
+    base = dict(cell_dim=(16, 16, 16), n_grains=8, n_steps=steps, seed=777, material=mat)
+    if precision == capi.MTH_FP64:
+        base.update(err=1e-10, iter_max=2500)   # converged far below the finite-difference step
+    else:
+        base.update(err=1e-6, iter_max=400)
+    base.update(kw)
+    return synth.Config(**base)
+
+
+def _forward(cfg, precision):
+    p = capi.params_from_config(cfg, precision=precision)
+    with Solver(p, *synth.microstructure(cfg)) as s:
+        return np.array([s.step()["sig_avg"][2][2] for _ in range(cfg.n_steps)])
+
+
+def _adjoint(cfg, precision, target, k=2):
+    p = capi.params_from_config(cfg, precision=precision)
+    with Solver(p, *synth.microstructure(cfg)) as s:
+        return s.adjoint(target, checkpoint_every=k)
+
+
+@pytest.fixture(scope="module")
+def fp64_case():
+    tgt = _forward(_cfg(synth.calibration_target_material(), capi.MTH_FP64), capi.MTH_FP64)
+    base = synth.Material()
+    J, grad, s33, info = _adjoint(_cfg(base, capi.MTH_FP64), capi.MTH_FP64, tgt)
+    return base, tgt, J, grad, s33, info
+
+
+def test_adjoint_forward_is_the_plain_forward(fp64_case):
+    base, tgt, J, grad, s33, info = fp64_case
+    ref = _forward(_cfg(base, capi.MTH_FP64), capi.MTH_FP64)
+    np.testing.assert_array_equal(s33, ref)        # same kernels, same order: bit-identical
+    assert J == pytest.approx(float(np.sum((ref - tgt) ** 2)), rel=1e-14)
+    assert info["recomputed_steps"] == 2           # 4 steps, states every 2: the first pair again
+
+
+def test_adjoint_matches_central_differences(fp64_case):
+    """Spec bar: each gradient entry within 1e-3 relative of central
+    differences with a relative step of 1e-4."""
+    base, tgt, J, grad, s33, info = fp64_case
+    vals = synth.calibration_values(base)
+    for k in range(5):
+        h = 1e-4 * vals[k]
+        jp = np.sum((_forward(_cfg(synth.perturb_material(base, k, h), capi.MTH_FP64), capi.MTH_FP64) - tgt) ** 2)
+        jm = np.sum((_forward(_cfg(synth.perturb_material(base, k, -h), capi.MTH_FP64), capi.MTH_FP64) - tgt) ** 2)
+        fd = (jp - jm) / (2 * h)
+        assert abs(grad[k] - fd) <= 1e-3 * abs(fd), (capi.ADJOINT_PARAMS[k], grad[k], fd)
+
+
+def test_mixed_adjoint_matches_fp64(fp64_case):
+    """The mixed forward stops at Err = 1e-6 with FP32 fields, so its curve
+    (and the misfit built from it) differs from the FP64 one by ~1e-4
+    relative per point; the gradient follows within a few 1e-3."""
+    base, tgt, J64, g64, s64, _ = fp64_case
+    J, g, s33, info = _adjoint(_cfg(base, capi.MTH_MIXED), capi.MTH_MIXED, tgt)
+    assert np.abs(s33 - s64).max() <= 2e-4 * np.abs(s64).max()
+    assert abs(J - J64) <= 5e-3 * J64
+    for k in range(5):
+        assert abs(g[k] - g64[k]) <= 2e-2 * abs(g64[k]), (capi.ADJOINT_PARAMS[k], g.tolist(), g64.tolist())
+
+
+def test_checkpoint_spacing_does_not_change_the_gradient():
+    tgt = _forward(_cfg(synth.calibration_target_material(), capi.MTH_MIXED, steps=5), capi.MTH_MIXED)
+    out = [_adjoint(_cfg(synth.Material(), capi.MTH_MIXED, steps=5), capi.MTH_MIXED, tgt, k=k) for k in (1, 2, 5)]
+    for J, g, s33, info in out[1:]:
+        assert J == out[0][0]
+        np.testing.assert_array_equal(g, out[0][1])
+    assert [o[3]["recomputed_steps"] for o in out] == [4, 4, 0]
+
+
+def test_adjoint_without_rotation_or_hardening():
+    """With Update_Flag = 0 (first step elastic, no lattice rotation) and
+    Hard_Flag = 0 the Voce gradients vanish and tau0 / n stay right."""
+    kw = dict(update_flag=0, hard_flag=0)
+    tgt = _forward(_cfg(synth.calibration_target_material(), capi.MTH_FP64, steps=3, **kw), capi.MTH_FP64)
+    base = synth.Material()
+    J, g, s33, info = _adjoint(_cfg(base, capi.MTH_FP64, steps=3, **kw), capi.MTH_FP64, tgt)
+    assert g[1] == 0.0 and g[2] == 0.0 and g[3] == 0.0
+    for k in (0, 4):
+        h = 1e-4 * synth.calibration_values(base)[k]
+        jp = np.sum((_forward(_cfg(synth.perturb_material(base, k, h), capi.MTH_FP64, steps=3, **kw),
+                              capi.MTH_FP64) - tgt) ** 2)
+        jm = np.sum((_forward(_cfg(synth.perturb_material(base, k, -h), capi.MTH_FP64, steps=3, **kw),
+                              capi.MTH_FP64) - tgt) ** 2)
+        fd = (jp - jm) / (2 * h)
+        assert abs(g[k] - fd) <= 1e-3 * abs(fd)
+
+
+class Misfit(torch.autograd.Function):
+    """J(theta) of the calibration workload as a torch function: forward
+    runs mth_adjoint, backward returns its gradient (verification harness
+    only; the library has no torch types at its boundary)."""
+
+    @staticmethod
+    def forward(ctx, theta, cfg, precision, target):
+        mat = dataclasses.replace(cfg.material)
+        t = theta.detach().cpu().double().numpy()
+        mat.tau0f = mat.tau0b = float(t[0])
+        mat.tau1, mat.thet0, mat.thet1, mat.nrs = (float(x) for x in t[1:])
+        J, g, _, _ = _adjoint(dataclasses.replace(cfg, material=mat), precision, target)
+        ctx.save_for_backward(torch.from_numpy(g))
+        return theta.new_tensor(J)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (g,) = ctx.saved_tensors
+        return gout * g.to(gout.dtype), None, None, None
+
+
+def test_torch_autograd_wrapper():
+    prec = capi.MTH_MIXED
+    tgt = _forward(_cfg(synth.calibration_target_material(), prec), prec)
+    cfg = _cfg(synth.Material(), prec)
+    theta = torch.tensor(synth.calibration_values(cfg.material), dtype=torch.float64, requires_grad=True)
+    J = Misfit.apply(theta, cfg, prec, tgt)
+    (g,) = torch.autograd.grad(J, theta)
+    J2, g2, _, _ = _adjoint(cfg, prec, tgt)
+    assert float(J.detach()) == J2
+    np.testing.assert_array_equal(g.numpy(), g2)
+    # a small step against the gradient lowers the misfit
+    with torch.no_grad():
+        step = -1e-3 * theta.abs() * torch.sign(g)
+        J_new = Misfit.apply(theta + step, cfg, prec, tgt)
+    assert float(J_new) < float(J)
+
+
+def test_adjoint_rejects_unsupported_setups():
+    tgt = np.zeros(2)
+    cfg = _cfg(synth.Material(), capi.MTH_MIXED, steps=2, n_pores=1, pore_radius=2)
+    with pytest.raises(MthError, match="UNSUPPORTED"):
+        _adjoint(cfg, capi.MTH_MIXED, tgt)
+    cfg = _cfg(synth.Material(), capi.MTH_MIXED, steps=2)
+    p = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
+    with Solver(p, *synth.microstructure(cfg)) as s:
+        s.step()
+        with pytest.raises(MthError, match="STATE"):
+            s.adjoint(tgt)
