@@ -106,6 +106,22 @@ typedef struct {
                                 are carried to the PF grid and the relaxed ids back as
                                 InterpolateGrid and Update_microstructure do
                                 (src/integrated.c:496-760,821-860); each entry >= 2. */
+  /* Dislocation-density law of phase 1: the reference's shipped
+   * DD_BASED_FLAG path (StrainRate_Orowan src/constitutive.c:507-721,
+   * DislocationEvolution :1346-1520 with first-order GNDs, AvgDislocation
+   * :1669-1760); namelist keys of src/io.c:47-68. */
+  int    flow_law;           /* 0: power law + Voce harden; 1: dislocation density */
+  double dd_a0;              /* a0: lattice parameter [nm]; b = a0/sqrt(2) */
+  double dd_L0;              /* L0: GND length scale */
+  double dd_T;               /* T__K [K] */
+  double dd_q_slip;          /* Q_slip [1e-19 J] */
+  double dd_q_bulk;          /* Q_bulk [1e-19 J] */
+  double dd_c[8];            /* C_1 .. C_8 */
+  double dd_chi[6];          /* Selfinter, Coplanar, CrossSlip, GlissileJunction, HirthLock,
+                                LomerCottrellLock */
+  double dd_rho_ssd0;        /* rho_SSD_initial [1e12/m^2] */
+  double dd_d0;              /* D_0 */
+  double dd_nu;              /* Poisson ratio (4th value of ElastConst_PhaseI) */
 } mth_params;
 
 /* Per-step record; the reference prints the scalars to vm.out
@@ -124,6 +140,10 @@ typedef struct {
   long long newton_iters;    /* local Newton iterations summed over voxels and Green iterations */
   long long newton_failed;   /* voxel solves that hit the iteration cap */
   int    n_new_grains;       /* DRX nuclei seeded this step */
+  /* dislocation-density law: the dd.out columns after TIME and EVM
+   * (src/evolution.c:1566-1569): volume averages of the per-system sums of
+   * rho_F, rho_P, rho_s, rho_m, |rho_GND|, rho_dipole, rho_forest */
+  double dd_avg[7];
 } mth_step_report;
 
 typedef enum {
@@ -135,7 +155,9 @@ typedef enum {
   MTH_FIELD_CRSS = 5,     /* 12: forward CRSS per slip system */
   MTH_FIELD_GAMACUM = 6,  /* 1: accumulated shear */
   MTH_FIELD_GRAIN = 7,    /* 1: grain id (as double) */
-  MTH_FIELD_RHO = 8       /* 1: total dislocation density */
+  MTH_FIELD_RHO = 8,      /* 1: total dislocation density */
+  MTH_FIELD_RHO_SSD = 9,  /* 12: statistically stored density per system (dislocation-density law) */
+  MTH_FIELD_RHO_GND = 10  /* 36: GND densities per system: screw (12), edge I (12), edge II (12) */
 } mth_field;
 
 /* Library */

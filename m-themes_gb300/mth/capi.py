@@ -23,8 +23,9 @@ MTH_MIXED = 1
 MTH_MIXED_FAST = 2
 MTH_MIXED_ROOT64 = 3
 
-FIELD = {"sig": 0, "eps": 1, "edot": 2, "strain": 3, "rot": 4, "crss": 5, "gamacum": 6, "grain": 7, "rho": 8}
-FIELD_NCOMP = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 1, 7: 1, 8: 1}
+FIELD = {"sig": 0, "eps": 1, "edot": 2, "strain": 3, "rot": 4, "crss": 5, "gamacum": 6, "grain": 7, "rho": 8,
+         "rho_ssd": 9, "rho_gnd": 10}
+FIELD_NCOMP = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 1, 7: 1, 8: 1, 9: 12, 10: 36}
 
 STATUS = {0: "MTH_OK", 1: "MTH_ERR_ARG", 2: "MTH_ERR_CUDA", 3: "MTH_ERR_NOMEM", 4: "MTH_ERR_SINGULAR",
           5: "MTH_ERR_NOT_CONVERGED", 6: "MTH_ERR_IO", 7: "MTH_ERR_STATE", 8: "MTH_ERR_TIMEOUT",
@@ -51,7 +52,11 @@ class MthParams(C.Structure):
                 ("shear_modulus", C.c_double), ("burgers", C.c_double), ("nucleus_radius", C.c_int),
                 ("rho_nucleation", C.c_double), ("rho0", C.c_double), ("rho_k", C.c_double),
                 ("pf_substeps", C.c_int), ("seed", C.c_uint64), ("nucleation_prob", C.c_double),
-                ("device", C.c_int), ("pf_cell_dim", C.c_int * 3)]
+                ("device", C.c_int), ("pf_cell_dim", C.c_int * 3),
+                ("flow_law", C.c_int), ("dd_a0", C.c_double), ("dd_L0", C.c_double), ("dd_T", C.c_double),
+                ("dd_q_slip", C.c_double), ("dd_q_bulk", C.c_double), ("dd_c", C.c_double * 8),
+                ("dd_chi", C.c_double * 6), ("dd_rho_ssd0", C.c_double), ("dd_d0", C.c_double),
+                ("dd_nu", C.c_double)]
 
 
 T33 = (C.c_double * 3) * 3
@@ -63,13 +68,15 @@ class MthStepReport(C.Structure):
                 ("edot_avg", T33), ("e_vm", C.c_double), ("evmp", C.c_double), ("d_vm", C.c_double),
                 ("dvmp", C.c_double), ("s_vm", C.c_double), ("s_vm1", C.c_double),
                 ("err_s", C.c_double), ("err_e", C.c_double), ("newton_iters", C.c_longlong),
-                ("newton_failed", C.c_longlong), ("n_new_grains", C.c_int)]
+                ("newton_failed", C.c_longlong), ("n_new_grains", C.c_int), ("dd_avg", C.c_double * 7)]
 
     def to_dict(self):
         d = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            if isinstance(v, C.Array):
+            if name == "dd_avg":
+                v = np.array([v[i] for i in range(7)])
+            elif isinstance(v, C.Array):
                 v = np.array([[v[i][j] for j in range(3)] for i in range(3)])
             d[name] = v
         return d
@@ -141,6 +148,13 @@ def params_from_config(cfg, precision=MTH_FP64, newton_tol=0.0, newton_itmax=0) 
     p.precision = precision
     p.newton_tol = newton_tol
     p.newton_itmax = newton_itmax
+    dd = getattr(cfg, "dd", None)
+    if dd is not None:
+        p.flow_law = 1
+        p.dd_a0, p.dd_L0, p.dd_T, p.dd_q_slip, p.dd_q_bulk = dd.a0, dd.L0, dd.T, dd.q_slip, dd.q_bulk
+        p.dd_c[:] = [float(x) for x in dd.c]
+        p.dd_chi[:] = [float(x) for x in dd.chi]
+        p.dd_rho_ssd0, p.dd_d0, p.dd_nu = dd.rho_ssd0, dd.d0, dd.nu
     d = getattr(cfg, "drx", None)
     if d is not None:
         p.pf_substeps = d.pf_substeps

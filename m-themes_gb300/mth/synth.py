@@ -74,6 +74,27 @@ def shear_modulus(m: "Material") -> float:
 
 
 @dataclasses.dataclass
+class DD:
+    """Parameters of the dislocation-density law (the namelist keys a0, L0,
+    T__K, Q_slip, Q_bulk, C_1..C_8, the six interaction strengths,
+    rho_SSD_initial, D_0 and the Poisson ratio of ElastConst_PhaseI).  The
+    defaults are test_run/input.in's except T__K, Q_slip and Q_bulk, which
+    there switch thermally activated slip and climb off (T = 30 K with
+    activation energies of 2e10 and 3e11 x 1e-19 J); here slip is active at
+    the workloads' strain rate of 1/s."""
+    a0: float = 0.362
+    L0: float = 0.003
+    T: float = 300.0
+    q_slip: float = 0.25
+    q_bulk: float = 1.0
+    c: tuple = (0.48, 3.0, 3.0, 800.0, 16.0, 1100.0, 1.25e-8, 0.24)
+    chi: tuple = (0.125, 0.125, 0.725, 0.125, 0.05, 0.18)   # self, coplanar, cross, glissile, Hirth, Lomer
+    rho_ssd0: float = 0.05
+    d0: float = 4e-5
+    nu: float = 0.35
+
+
+@dataclasses.dataclass
 class Config:
     """One run: grid, loading and control parameters (namelist keys)."""
     cell_dim: tuple = (32, 32, 32)
@@ -94,6 +115,7 @@ class Config:
     update_flag: int = 1
     hard_flag: int = 1
     drx: Drx = None
+    dd: DD = None           # dislocation-density law instead of the power law + Voce
 
 
 def voronoi(cell_dim, n_grains, rng):
@@ -201,6 +223,9 @@ def write_input(path, cfg: Config, ms_name="ms.txt", sx_name="cu.sx"):
     m = cfg.material
     pfd = cfg.drx.pf_cell_dim if (cfg.drx is not None and cfg.drx.pf_cell_dim) else cfg.cell_dim
     n_phases = 2 if cfg.n_pores else 1
+    dd = cfg.dd if cfg.dd is not None else DD(T=30.0, q_slip=20000000000.0, q_bulk=300000000000.51)
+    c = dd.c
+    x = dd.chi
 
     def vec(v):
         return " ".join(repr(float(x)) if isinstance(x, float) else str(x) for x in v)
@@ -210,7 +235,7 @@ N_phases\t{n_phases}
 CellDim {cfg.cell_dim[0]} {cfg.cell_dim[1]} {cfg.cell_dim[2]}
 initial_ms {ms_name}
 Type_phases 0 1
-ElastConst_PhaseI {m.c11!r} {m.c12!r} {m.c44!r} 0.35
+ElastConst_PhaseI {m.c11!r} {m.c12!r} {m.c44!r} {dd.nu!r}
 Slip_PhaseI {sx_name}
 ElastConst_PhaseII 0.0 0.0 0.0 0.0
 Slip_PhaseII {sx_name}
@@ -227,28 +252,28 @@ PrintControl 0 2000
 Update_Flag {cfg.update_flag}
 Hard_Flag {cfg.hard_flag}
 Tex_Flag 0
-a0 0.362 0.0
-L0 0.003
+a0 {dd.a0!r} 0.0
+L0 {dd.L0!r}
 GND_ScaleRatio 6000.0
-Q_slip 20000000000.0 0.0
-Q_bulk 300000000000.51 0.0
-rho_SSD_initial 0.05
-T__K 30
-C_1 0.48 0.0
-C_2 3.0 0.0
-C_3 3.0 0.0
-C_4 800.0 0.0
-C_5 16.0 0.0
-C_6 1100E0 0.0
-C_7 1.25E-8 0.0
-C_8 0.24 0.0
-Selfinter 0.125 0.0
-Coplanar 0.125 0.0
-CrossSlip 0.725 0.0
-GlissileJunction 0.125 0.0
-HirthLock 0.05 0.0
-LomerCottrellLock 0.18 0.0
-D_0 4E-05
+Q_slip {dd.q_slip!r} 0.0
+Q_bulk {dd.q_bulk!r} 0.0
+rho_SSD_initial {dd.rho_ssd0!r}
+T__K {dd.T!r}
+C_1 {c[0]!r} 0.0
+C_2 {c[1]!r} 0.0
+C_3 {c[2]!r} 0.0
+C_4 {c[3]!r} 0.0
+C_5 {c[4]!r} 0.0
+C_6 {c[5]!r} 0.0
+C_7 {c[6]!r} 0.0
+C_8 {c[7]!r} 0.0
+Selfinter {x[0]!r} 0.0
+Coplanar {x[1]!r} 0.0
+CrossSlip {x[2]!r} 0.0
+GlissileJunction {x[3]!r} 0.0
+HirthLock {x[4]!r} 0.0
+LomerCottrellLock {x[5]!r} 0.0
+D_0 {dd.d0!r}
 nucleus_radius 2
 CellDim_pf {pfd[0]} {pfd[1]} {pfd[2]}
 RandSeed 123

@@ -32,6 +32,11 @@ for s in evp.c io.c init.c kinematics.c evolution.c constitutive.c integrated.c 
   OBJS+=("$o")
 done
 $CXX "${COMMON[@]}" -c "$HERE/refshim/refshim.cc" -o "$OUT/obj/refshim.o" &
+# the shipped dislocation-density path: evolution.c with only the trace hooks
+$CXX -x c++ "${COMMON[@]}" -DAvgDislocation=mth_ref_dd_after_step -DVonMises=mth_ref_VonMises \
+  -c "$REF/src/evolution.c" -o "$OUT/obj/evolution_dd.o" &
 wait
 $CXX -o "$OUT/forge_ref" "${OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
-echo "built $OUT/forge_ref"
+DD_OBJS=("${OBJS[@]/evolution.o/evolution_dd.o}")
+$CXX -o "$OUT/forge_ref_dd" "${DD_OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
+echo "built $OUT/forge_ref $OUT/forge_ref_dd"

@@ -317,6 +317,11 @@ typedef struct {
   double bn[NS][3], bb[NS][3];
   double schm_xt[NS][5];
   t3333 cijkl;
+  /* dislocation-density law (src/init.c:179-205,816-830,1096-1126) */
+  int dd;
+  double dd_b, dd_G, dd_nu, dd_c[8], dd_kT, dd_qslip, dd_qbulk, dd_L0, dd_d0, dd_T;
+  double chi[NS][NS], cs[NS][NS], ss[NS][NS], cg1[NS][NS], sg1[NS][NS], cg3[NS][NS], sg3[NS][NS];
+  double bp[NS][3];
 } phase_t;
 
 static int phase_init(const mth_phase* in, phase_t* ph) {
@@ -350,12 +355,136 @@ static int phase_init(const mth_phase* in, phase_t* ph) {
   return MTH_OK;
 }
 
+/* Constants of the dislocation-density law (src/evp.h:77-86). */
+#define DD_TRIAL_FREQ 1.0E10
+#define DD_EV_IN_J 1.60217733e-19
+#define DD_MY_J_IN_EV 0.62415063631
+#define DD_BOLZ 1.380658e-23
+#define DD_TAU0 1000.0        /* tau_0 of StrainRate_Orowan (src/constitutive.c:535) */
+#define DD_EPS 5.0E-3         /* EPSILON of src/PFgrid.h:50, seen by DislocationEvolution */
+
+/* Junction strength of slip systems i, j of an FCC crystal from their
+ * geometry: self, coplanar (same plane), cross slip (collinear b), Hirth
+ * (orthogonal b), and for 60-degree pairs on different planes glissile when
+ * the junction b_i -/+ b_j lies in one of the two planes, Lomer-Cottrell when
+ * it lies in neither.  For the system order of the FCC .sx files this gives
+ * the matrix of InteractionStrengthMatrix (src/init.c:593-702). */
+static double dd_junction(const phase_t* ph, int i, int j, const double str[6]) {
+  if (i == j) return str[0];
+  const double* ni = ph->bn[i]; const double* nj = ph->bn[j];
+  const double* bi = ph->bb[i]; const double* bj = ph->bb[j];
+  double nn = ni[0] * nj[0] + ni[1] * nj[1] + ni[2] * nj[2];
+  double bbd = bi[0] * bj[0] + bi[1] * bj[1] + bi[2] * bj[2];
+  if (fabs(fabs(nn) - 1.0) < 1e-6) return str[1];
+  if (fabs(fabs(bbd) - 1.0) < 1e-6) return str[2];
+  if (fabs(bbd) < 1e-6) return str[4];
+  double sg = bbd > 0 ? 1.0 : -1.0, p[3];
+  for (int m = 0; m < 3; m++) p[m] = bi[m] - sg * bj[m];
+  double pi = p[0] * ni[0] + p[1] * ni[1] + p[2] * ni[2];
+  double pj = p[0] * nj[0] + p[1] * nj[1] + p[2] * nj[2];
+  return (fabs(pi) < 1e-6 || fabs(pj) < 1e-6) ? str[3] : str[5];
+}
+
+/* DD constants of a crystal phase from the run parameters: Burgers vector
+ * b = a0/sqrt(2) (src/init.c:182), shear modulus of src/init.c:826, kT,
+ * reduced activation energies, junction matrix and the projection cosines
+ * of src/init.c:1107-1126 (screw sense vector n_j x b_j). */
+static void dd_phase_init(const mth_params* p, const mth_phase* in, phase_t* ph) {
+  ph->dd = 1;
+  ph->dd_b = p->dd_a0 / sqrt(2.0);
+  const double c11 = in->c11, c12 = in->c12, c44 = in->c44;
+  ph->dd_G = 0.1 * (c11 - c12 + 3 * c44) + (0.5) * (5 * (c11 - c12) * c44) / (4 * c44 + 3 * (c11 - c12));
+  ph->dd_nu = p->dd_nu;
+  for (int k = 0; k < 8; k++) ph->dd_c[k] = p->dd_c[k];
+  ph->dd_T = p->dd_T;
+  ph->dd_kT = p->dd_T * DD_BOLZ * (1.0 / DD_EV_IN_J);
+  ph->dd_qslip = p->dd_q_slip * DD_MY_J_IN_EV / ph->dd_kT;
+  ph->dd_qbulk = p->dd_q_bulk * DD_MY_J_IN_EV / ph->dd_kT;
+  ph->dd_L0 = p->dd_L0;
+  ph->dd_d0 = p->dd_d0;
+  for (int i = 0; i < ph->nsys; i++) {
+    ph->bp[i][0] = ph->bb[i][1] * ph->bn[i][2] - ph->bb[i][2] * ph->bn[i][1];
+    ph->bp[i][1] = ph->bb[i][2] * ph->bn[i][0] - ph->bb[i][0] * ph->bn[i][2];
+    ph->bp[i][2] = ph->bb[i][0] * ph->bn[i][1] - ph->bb[i][1] * ph->bn[i][0];
+  }
+  for (int i = 0; i < ph->nsys; i++)
+    for (int j = 0; j < ph->nsys; j++) {
+      ph->chi[i][j] = dd_junction(ph, i, j, p->dd_chi);
+      double sv[3] = {ph->bn[j][1] * ph->bb[j][2] - ph->bn[j][2] * ph->bb[j][1],
+                      ph->bn[j][2] * ph->bb[j][0] - ph->bn[j][0] * ph->bb[j][2],
+                      ph->bn[j][0] * ph->bb[j][1] - ph->bn[j][1] * ph->bb[j][0]};
+      ph->cs[i][j] = fabs(ph->bn[i][0] * sv[0] + ph->bn[i][1] * sv[1] + ph->bn[i][2] * sv[2]);
+      ph->ss[i][j] = fabs(sqrt(fabs(1.0 - ph->cs[i][j] * ph->cs[i][j])));
+      ph->cg1[i][j] = fabs(ph->bn[i][0] * ph->bb[j][0] + ph->bn[i][1] * ph->bb[j][1] + ph->bn[i][2] * ph->bb[j][2]);
+      ph->sg1[i][j] = fabs(sqrt(fabs(1.0 - ph->cg1[i][j] * ph->cg1[i][j])));
+      ph->cg3[i][j] = fabs(ph->bn[i][0] * ph->bn[j][0] + ph->bn[i][1] * ph->bn[j][1] + ph->bn[i][2] * ph->bn[j][2]);
+      ph->sg3[i][j] = fabs(sqrt(fabs(1.0 - ph->cg3[i][j] * ph->cg3[i][j])));
+    }
+}
+
+/* Per-voxel state of the dislocation-density law (rows of NS). */
+typedef struct {
+  double *rho_s, *g1, *g2, *g3, *rho_m, *rho_F, *rho_P, *gam_acum, *trial_gam_acum;
+  double dt;
+} ddv_t;
+
+/* StrainRate_Orowan, FORWARD_PLUS_BACKWARD branch (src/constitutive.c:
+ * 507-721): forest/parallel densities from the trial densities, passing
+ * stress from the mobile density of the previous evaluation, then the
+ * mobile density, cutting stress and sinh rate law; writes rho_F, rho_P,
+ * rho_m and trial_gam_acum as the reference does. */
+static void flow_rule_dd(const phase_t* ph, const double sc[NS][5], const ddv_t* d, const double* s, double* edot,
+                         m66 dedot, double* gamdot) {
+  const int ns = ph->nsys;
+  const double G = ph->dd_G, c1 = ph->dd_c[0], c2 = ph->dd_c[1], c3 = ph->dd_c[2], kT = ph->dd_kT;
+  double gam[NS], gam2[NS];
+  for (int i = 0; i < ns; i++) {
+    double f = 0.0, pp = 0.0;
+    for (int j = 0; j < ns; j++) {
+      f += ph->chi[i][j] * (d->rho_s[j] * ph->cs[i][j] + fabs(d->g1[j] * ph->cg1[i][j]) +
+                            fabs(d->g2[j] * ph->cs[i][j]) + fabs(d->g3[j] * ph->cg3[i][j]));
+      pp += ph->chi[i][j] * (d->rho_s[j] * ph->ss[i][j] + fabs(d->g1[j] * ph->sg1[i][j]) +
+                             fabs(d->g2[j] * ph->ss[i][j]) + fabs(d->g3[j] * ph->sg3[i][j]));
+    }
+    d->rho_F[i] = f;
+    d->rho_P[i] = pp;
+  }
+  for (int i = 0; i < ns; i++) {
+    const double b = ph->dd_b;
+    double tau_pass = c1 * G * b * sqrt(fabs(d->rho_P[i] + d->rho_m[i])) * 1.0E-3;
+    double rss = sc[i][0] * s[0] + sc[i][1] * s[1] + sc[i][2] * s[2] + sc[i][3] * s[3] + sc[i][4] * s[4];
+    double tau_eff = fabs(rss) - tau_pass;
+    double tau_cut = (kT / DD_MY_J_IN_EV) * sqrt(d->rho_F[i]) / c2 / c3 / b / b * 0.1;
+    d->rho_m[i] = 2.0 * kT / c1 / c2 / c3 / G / (pow(b, 3.0)) * sqrt(d->rho_P[i] * d->rho_F[i]) * 160.2177;
+    double gam_o = 1E-3 * (d->rho_m[i]) * DD_TRIAL_FREQ * c2 * b * exp(-1.0 * ph->dd_qslip) / sqrt(d->rho_F[i]);
+    double t = fabs(rss) > tau_pass ? gam_o * sinh(tau_eff / (DD_TAU0 + tau_cut)) : 0.0;
+    gam[i] = t * ((double)(2 * (rss > 0) - 1));
+    gam2[i] = fabs(rss) > tau_pass ? gam_o * cosh(tau_eff / (tau_cut + DD_TAU0)) / (tau_cut + DD_TAU0) : 0.0;
+    if (gamdot) gamdot[i] = gam[i];
+    d->trial_gam_acum[i] = d->gam_acum[i] + gam[i] * d->dt;
+  }
+  for (int i = 0; i < 5; i++) {
+    double e = 0.;
+    for (int j = 0; j < ns; j++) e += sc[j][i] * gam[j];
+    edot[i] = e;
+  }
+  edot[5] = 0.0;
+  if (dedot) {
+    for (int i = 0; i < 5; i++) for (int j = 0; j < 5; j++) {
+      double a = 0.0;
+      for (int k = 0; k < ns; k++) a += sc[k][i] * sc[k][j] * gam2[k];
+      dedot[i][j] = a;
+    }
+    for (int i = 0; i < 6; i++) { dedot[i][5] = 0.0; dedot[5][i] = 0.0; }
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* Flow rule StrainRate_eval (src/constitutive.c:5-67); xkin is zero    */
 /* throughout the reference (initialised at src/init.c:1165, never set). */
 /* ------------------------------------------------------------------ */
-static void flow_rule(const phase_t* ph, const double sc[NS][5], const double tau_t[NS][2],
-                      const double* s, double* edot, m66 dedot, double* gamdot) {
+static void flow_rule_pl(const phase_t* ph, const double sc[NS][5], const double tau_t[NS][2],
+                         const double* s, double* edot, m66 dedot, double* gamdot) {
   double rss1[NS], rss2[NS];
   const int ns = ph->nsys;
   const double nsr = ph->nsr;
@@ -383,12 +512,20 @@ static void flow_rule(const phase_t* ph, const double sc[NS][5], const double ta
   }
 }
 
+/* the flow rule of the run: StrainRate_Orowan with per-voxel densities,
+ * else StrainRate_eval */
+static void flow_rule(const phase_t* ph, const double sc[NS][5], const double tau_t[NS][2], const ddv_t* d,
+                      const double* s, double* edot, m66 dedot, double* gamdot) {
+  if (d) flow_rule_dd(ph, sc, d, s, edot, dedot, gamdot);
+  else flow_rule_pl(ph, sc, tau_t, s, edot, dedot, gamdot);
+}
+
 /* NR_quality (src/evolution.c:2-41): f = |R|^2/2 at sig */
-static double nr_quality(const phase_t* ph, const double sc[NS][5], const double tau_t[NS][2],
+static double nr_quality(const phase_t* ph, const double sc[NS][5], const double tau_t[NS][2], const ddv_t* d,
                          const m66 c066, double dt, const double* sig, const double* xlam,
                          const double* eps, const double* strain, const m66 sg, double* gamdot) {
   double edotp[6], tot[6], res[6], f = 0.0;
-  flow_rule(ph, sc, tau_t, sig, edotp, NULL, gamdot);
+  flow_rule(ph, sc, tau_t, d, sig, edotp, NULL, gamdot);
   for (int i = 0; i < 6; i++) {
     tot[i] = eps[i] + edotp[i] * dt;
     for (int j = 0; j < 6; j++) tot[i] += sg[i][j] * sig[j];
@@ -407,7 +544,7 @@ static double nr_quality(const phase_t* ph, const double sc[NS][5], const double
 typedef struct { double conv_s, conv_e; int iters; int cubic; int status; } newton_out;
 
 static newton_out newton_voxel(const phase_t* ph, const double sc[NS][5], const double tau_t[NS][2],
-                               const m66 c066, double dt, const m66 sg66, double* sig6,
+                               const ddv_t* dd, const m66 c066, double dt, const m66 sg66, double* sig6,
                                const double* xlam6, const double* eps6, const double* strain6,
                                double* edotp6, double* gamdot, double tol, int itmax) {
   newton_out o = {0.0, 0.0, 0, 0, MTH_OK};
@@ -426,7 +563,7 @@ static newton_out newton_voxel(const phase_t* ph, const double sc[NS][5], const 
     double sig_old[6], tot[6], res[6];
     m66 dedot, jinv, jac;
     for (int i = 0; i < 6; i++) sig_old[i] = sig6[i];
-    flow_rule(ph, sc, tau_t, sig6, edotp6, dedot, gamdot);
+    flow_rule(ph, sc, tau_t, dd, sig6, edotp6, dedot, gamdot);
     for (int i = 0; i < 6; i++) {
       tot[i] = eps6[i] + edotp6[i] * dt;
       for (int j = 0; j < 6; j++) tot[i] += sg66[i][j] * sig6[j];
@@ -467,7 +604,7 @@ static newton_out newton_voxel(const phase_t* ph, const double sc[NS][5], const 
     double alamin = TOLX / test, alam = 1.0, alam2 = 0.0, f2 = 0.0, tmplam = 0.0;
     while (1) {
       for (int i = 0; i < 6; i++) sig6[i] = sig_old[i] + alam * step[i];
-      double f_new = nr_quality(ph, sc, tau_t, c066, dt, sig6, xlam6, eps6, strain6, sg66, gamdot);
+      double f_new = nr_quality(ph, sc, tau_t, dd, c066, dt, sig6, xlam6, eps6, strain6, sg66, gamdot);
       if (alam < alamin) {
         for (int i = 0; i < 6; i++) sig6[i] = sig_old[i];
         break;
@@ -569,6 +706,13 @@ struct orc_ctx {
   t33 disgrad_avg, ddisgrad_avg, ddisgrad_acum, disgrad_avg_t;
   t33 sig_avg, sig_avg1, sig_dev_avg, eps_avg, edot_avg;
   long long cubic_total;
+  /* dislocation-density law (src/init.c:1055-1095) */
+  int dd;
+  double (*rho_s)[NS], (*rho_g1)[NS], (*rho_g2)[NS], (*rho_g3)[NS], (*rho_m)[NS], (*rho_F)[NS], (*rho_P)[NS];
+  double (*rho_dipole)[NS], (*rho_forest)[NS], (*gam_acum)[NS], (*trial_gam_acum)[NS];
+  double (*gadot_grad)[NS][3];
+  unsigned char (*gbchk)[6];   /* GB_checkX/Y/Z of Gradient_ExchangeGrainID: [+x,-x,+y,-y,+z,(-y)] */
+  double dd_avg[7];
 };
 
 static void* xcalloc(size_t n, size_t s) { return calloc(n ? n : 1, s); }
@@ -737,6 +881,39 @@ orc_ctx* orc_create(const mth_params* p, const int* grain, const int* phase, con
   }
   c->e_vm = c->d_vm * c->dt;
   c->istep = 0;
+  if (p->flow_law == 1) {
+    if (c->ph[0].type != 0 || (c->nphases == 2 && c->ph[1].type == 0)) { st = MTH_ERR_UNSUPPORTED; goto fail; }
+    dd_phase_init(p, &p->phase[0], &c->ph[0]);
+    c->dd = 1;
+    c->rho_s = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_g1 = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_g2 = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_g3 = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_m = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_F = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_P = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_dipole = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->rho_forest = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->gam_acum = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->trial_gam_acum = (double(*)[NS])xcalloc(nv, sizeof(double[NS]));
+    c->gadot_grad = (double(*)[NS][3])xcalloc(nv, sizeof(double[NS][3]));
+    c->gbchk = (unsigned char(*)[6])xcalloc(nv, 6);
+    for (size_t v = 0; v < nv; v++)
+      for (int i = 0; i < NS; i++) c->rho_s[v][i] = p->dd_rho_ssd0;
+    const int n0 = c->n[0], n1 = c->n[1], n2 = c->n[2];
+    for (int x = 0; x < n0; x++) for (int y = 0; y < n1; y++) for (int z = 0; z < n2; z++) {
+      size_t v = ((size_t)x * n1 + y) * n2 + z;
+      int xp = (x + 1) % n0, xm = (x + n0 - 1) % n0, yp = (y + 1) % n1, ym = (y + n1 - 1) % n1;
+      int zp = (z + 1) % n2;
+      int g = c->grain[v];
+      c->gbchk[v][0] = g == c->grain[((size_t)xp * n1 + y) * n2 + z];
+      c->gbchk[v][1] = g == c->grain[((size_t)xm * n1 + y) * n2 + z];
+      c->gbchk[v][2] = g == c->grain[((size_t)x * n1 + yp) * n2 + z];
+      c->gbchk[v][3] = g == c->grain[((size_t)x * n1 + ym) * n2 + z];
+      c->gbchk[v][4] = g == c->grain[((size_t)x * n1 + y) * n2 + zp];
+      c->gbchk[v][5] = g == c->grain[((size_t)x * n1 + ym) * n2 + z];   /* -z flag compares with -y */
+    }
+  }
   if (status) *status = MTH_OK;
   return c;
 fail:
@@ -752,6 +929,9 @@ void orc_destroy(orc_ctx* c) {
   free(c->gamacum); free(c->kbuf); free(c->nvec); free(c->conv_s); free(c->conv_e);
   free(c->newton_it); free(c->newton_bad);
   free(c->cgr); free(c->drx_rot);
+  free(c->rho_s); free(c->rho_g1); free(c->rho_g2); free(c->rho_g3); free(c->rho_m); free(c->rho_F);
+  free(c->rho_P); free(c->rho_dipole); free(c->rho_forest); free(c->gam_acum); free(c->trial_gam_acum);
+  free(c->gadot_grad); free(c->gbchk);
   free(c);
 }
 
@@ -936,6 +1116,86 @@ static void harden(orc_ctx* c) {
   }
 }
 
+/* Gradient_ShearRate (src/constitutive.c:875-1108): per system, one-sided
+ * or central differences of the shear rate across the x, y, z neighbours
+ * that lie in the same grain (GB_check flags), 0 where neither does;
+ * periodic. */
+static void dd_gradient_rate(orc_ctx* c) {
+  const int n0 = c->n[0], n1 = c->n[1], n2 = c->n[2];
+#pragma omp parallel for schedule(static)
+  for (int x = 0; x < n0; x++)
+    for (int y = 0; y < n1; y++)
+      for (int z = 0; z < n2; z++) {
+        const size_t v = ((size_t)x * n1 + y) * n2 + z;
+        const size_t nb[6] = {((size_t)((x + 1) % n0) * n1 + y) * n2 + z, ((size_t)((x + n0 - 1) % n0) * n1 + y) * n2 + z,
+                              ((size_t)x * n1 + (y + 1) % n1) * n2 + z, ((size_t)x * n1 + (y + n1 - 1) % n1) * n2 + z,
+                              ((size_t)x * n1 + y) * n2 + (z + 1) % n2, ((size_t)x * n1 + y) * n2 + (z + n2 - 1) % n2};
+        for (int i = 0; i < NS; i++)
+          for (int a = 0; a < 3; a++) {
+            const int up = c->gbchk[v][2 * a], dn = c->gbchk[v][2 * a + 1];
+            double g;
+            if (!up && dn) g = c->gamdot[v][i] - c->gamdot[nb[2 * a + 1]][i];
+            else if (up && !dn) g = c->gamdot[nb[2 * a]][i] - c->gamdot[v][i];
+            else if (up && dn) g = (c->gamdot[nb[2 * a]][i] - c->gamdot[nb[2 * a + 1]][i]) / 2.0;
+            else g = 0.0;
+            c->gadot_grad[v][i][a] = g;
+          }
+      }
+}
+
+/* DislocationEvolution with first-order GNDs (src/constitutive.c:1346-1520)
+ * and AvgDislocation (src/constitutive.c:1669-1760). */
+static void dd_evolution(orc_ctx* c) {
+  const size_t nv = c->nv;
+#pragma omp parallel for schedule(static)
+  for (long long v = 0; v < (long long)nv; v++) {
+    const phase_t* ph = &c->ph[c->phase[v] - 1];
+    if (ph->type != 0) continue;
+    const double b = ph->dd_b, G = ph->dd_G;
+    double sig6[6];
+    t2v((const double(*)[3])c->sig[v], sig6, 6);
+    for (int i = 0; i < ph->nsys; i++) {
+      const double* sc = c->schm[v][i];
+      double rss = sc[0] * sig6[0] + sc[1] * sig6[1] + sc[2] * sig6[2] + sc[3] * sig6[3] + sc[4] * sig6[4];
+      double hydro = (sig6[0] + sig6[1] + sig6[2]) / 3.0;
+      double d_dipole = sqrt(3.0) * G * b / 16.0 / R_PI / (1 - ph->dd_nu) / (fabs(rss) + DD_EPS);
+      double ag = fabs(c->gamdot[v][i]);
+      const double c4 = ph->dd_c[3], c5 = ph->dd_c[4], c6 = ph->dd_c[5], c7 = ph->dd_c[6];
+      c->rho_dipole[v][i] += ag * (c6 * (d_dipole)*c->rho_m[v][i]) * c->dt;
+      c->rho_forest[v][i] += ag * (c4 * sqrt(c->rho_F[v][i])) * c->dt;
+      double rs = c->rho_s[v][i];
+      double dot_ssd = ag * (c4 * sqrt(c->rho_F[v][i]) + c6 * (d_dipole)*c->rho_m[v][i] - c5 * rs) -
+                       c7 * 1.6 * 1E12 * 1E-9 * rs * rs -
+                       4 * 1E12 * (d_dipole) * (ph->dd_d0 / b) * pow(rs, 2.0) *
+                           exp((fabs(hydro) * b * b * b * 100 / (1.38 * ph->dd_T)) - 1.0) * exp(-1.0 * ph->dd_qbulk);
+      c->rho_s[v][i] += dot_ssd * c->dt;
+      c->gam_acum[v][i] = c->trial_gam_acum[v][i];
+      const double* gg = c->gadot_grad[v][i];
+      double g_screw = gg[0] * ph->bp[i][0] + gg[1] * ph->bp[i][1] + gg[2] * ph->bp[i][2];
+      c->rho_g1[v][i] += g_screw / b / ph->dd_L0 * c->dt;
+      double g_edge = gg[0] * ph->bb[i][0] + gg[1] * ph->bb[i][1] + gg[2] * ph->bb[i][2];
+      c->rho_g2[v][i] += -1.0 * g_edge / b / ph->dd_L0 * c->dt;
+      c->rho_g3[v][i] += 0.0 * c->dt;
+    }
+  }
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (size_t v = 0; v < nv; v++) {
+    const phase_t* ph = &c->ph[c->phase[v] - 1];
+    if (ph->type != 0) continue;
+    for (int i = 0; i < ph->nsys; i++) {
+      s[0] += c->rho_F[v][i];
+      s[1] += c->rho_P[v][i];
+      s[2] += c->rho_s[v][i];
+      s[3] += c->rho_m[v][i];
+      s[4] += sqrt(c->rho_g1[v][i] * c->rho_g1[v][i] + c->rho_g2[v][i] * c->rho_g2[v][i] +
+                   c->rho_g3[v][i] * c->rho_g3[v][i]);
+      s[5] += c->rho_dipole[v][i];
+      s[6] += c->rho_forest[v][i];
+    }
+  }
+  for (int k = 0; k < 7; k++) c->dd_avg[k] = s[k] * (1.0 / (double)nv);
+}
+
 /* Dynamic recrystallisation at the start of a mechanical step, in the order
  * of Evolution (src/evolution.c:850-1253), restated as in drx_oracle.c:
  * rho from accumulated slip, nucleation, phase-field relaxation, adoption
@@ -1093,7 +1353,14 @@ int orc_step(orc_ctx* c, mth_step_report* rep) {
         t2v((const double(*)[3])c->sig[v], s6, 6);
         t2v((const double(*)[3])c->eps[v], e6, 6);
         t2v((const double(*)[3])strain, st6, 6);
-        newton_out o = newton_voxel(ph, (const double(*)[5])c->schm[v], (const double(*)[2])c->crss[v],
+        ddv_t ddv, *dp = NULL;
+        if (c->dd) {
+          ddv.rho_s = c->rho_s[v]; ddv.g1 = c->rho_g1[v]; ddv.g2 = c->rho_g2[v]; ddv.g3 = c->rho_g3[v];
+          ddv.rho_m = c->rho_m[v]; ddv.rho_F = c->rho_F[v]; ddv.rho_P = c->rho_P[v];
+          ddv.gam_acum = c->gam_acum[v]; ddv.trial_gam_acum = c->trial_gam_acum[v]; ddv.dt = c->dt;
+          dp = &ddv;
+        }
+        newton_out o = newton_voxel(ph, (const double(*)[5])c->schm[v], (const double(*)[2])c->crss[v], dp,
                                     (const double(*)[6])c->c066, c->dt, (const double(*)[6])c->sg66[v],
                                     s6, xl6, e6, st6, ed6, c->gamdot[v], c->newton_tol, c->newton_itmax);
         if (o.status == MTH_ERR_SINGULAR) bad_status = MTH_ERR_SINGULAR;
@@ -1164,7 +1431,12 @@ int orc_step(orc_ctx* c, mth_step_report* rep) {
   evmp = sqrt(2. / 3. * evmp);
   dvmp = sqrt(2. / 3. * dvmp);
   if (c->update_flag == 1 && istep > 1) update_orient(c);      /* src/evolution.c:1543-1546 */
-  if (c->hard_flag == 1) harden(c);                             /* oracle patch point, src/evolution.c:1574 */
+  if (c->dd) {
+    if (c->hard_flag == 1 && istep > 1) dd_gradient_rate(c);    /* src/evolution.c:1551-1559 */
+    dd_evolution(c);                                            /* src/evolution.c:1564-1565 */
+  } else if (c->hard_flag == 1) {
+    harden(c);                                                  /* oracle patch point, src/evolution.c:1574 */
+  }
   if (rep) {
     memset(rep, 0, sizeof(*rep));
     rep->step = istep;
@@ -1181,6 +1453,7 @@ int orc_step(orc_ctx* c, mth_step_report* rep) {
     rep->newton_iters = nit_total;
     rep->newton_failed = nbad_total;
     rep->n_new_grains = n_new;
+    if (c->dd) memcpy(rep->dd_avg, c->dd_avg, sizeof(c->dd_avg));
   }
   /* next macro guess (src/evolution.c:1691-1693) */
   for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++)
@@ -1205,6 +1478,18 @@ int orc_get_field(orc_ctx* c, int field, double* out) {
         for (int i = 0; i < NS; i++) out[NS * v + i] = c->crss[v][i][0];
         break;
       case MTH_FIELD_GAMACUM: out[v] = c->gamacum[v]; break;
+      case MTH_FIELD_RHO_SSD:
+        if (!c->dd) return MTH_ERR_ARG;
+        for (int i = 0; i < NS; i++) out[NS * v + i] = c->rho_s[v][i];
+        break;
+      case MTH_FIELD_RHO_GND:
+        if (!c->dd) return MTH_ERR_ARG;
+        for (int i = 0; i < NS; i++) {
+          out[3 * NS * v + i] = c->rho_g1[v][i];
+          out[3 * NS * v + NS + i] = c->rho_g2[v][i];
+          out[3 * NS * v + 2 * NS + i] = c->rho_g3[v][i];
+        }
+        break;
       case MTH_FIELD_GRAIN: out[v] = (double)c->grain[v]; break;
       case MTH_FIELD_RHO:
         out[v] = c->ph[c->phase[v] - 1].type == 0 ? c->par.rho0 + c->par.rho_k * c->gamacum[v] : 0.0;
@@ -1249,7 +1534,7 @@ int orc_local_solve(const mth_params* p, const double c066[36], size_t n, double
     schmid_sample(&ph, (const double(*)[3])tm, sc);
     for (int i = 0; i < ph.nsys; i++) { tau[i][0] = crss[NS * v + i]; tau[i][1] = crss[NS * v + i] + (ph.tau[1] - ph.tau[0]); }
     for (int i = 0; i < 6; i++) xl[i] = sig[6 * v + i];
-    newton_out o = newton_voxel(&ph, (const double(*)[5])sc, (const double(*)[2])tau, (const double(*)[6])c6,
+    newton_out o = newton_voxel(&ph, (const double(*)[5])sc, (const double(*)[2])tau, NULL, (const double(*)[6])c6,
                                 p->time_step, (const double(*)[6])cgr, sig + 6 * v, xl, eps_p + 6 * v,
                                 strain + 6 * v, edot + 6 * v, gd, tol, itmax);
     err[2 * v] = o.conv_s;

@@ -238,6 +238,28 @@ void mth_ref_after_step(int istep) {
   fflush(g_trace);
 }
 
+/* Dislocation-density build: called where src/evolution.c:1565 calls
+ * AvgDislocation(); writes the power-law trace line plus the dd.out averages
+ * (src/evolution.c:1566-1569). */
+void mth_ref_dd_after_step(void) {
+  static int calls = 0;
+  AvgDislocation();
+  /* 9 inverse transforms per Green iteration, plus the 3 of the previous
+     step's displacement block (src/evolution.c:1578-1607) */
+  long long inv = g_inverse_calls - g_inv_at_last_step - (calls > 0 ? 3 : 0);
+  g_inv_at_last_step = g_inverse_calls;
+  const double* oob = &((const double*)SigDevAvg)[0] + 12;
+  fprintf(g_trace, "%d %lld", calls++, inv / 9);
+  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) fprintf(g_trace, " %.17e", SigAvg[i][j]);
+  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) fprintf(g_trace, " %.17e", g_disgrad_actual[i][j]);
+  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) fprintf(g_trace, " %.17e", EpsAvg[i][j]);
+  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) fprintf(g_trace, " %.17e", EdotAvg[i][j]);
+  fprintf(g_trace, " %.17e %.17e %.17e %.17e %.17e %.17e %.17e", s_vm, s_vm1, e_vm, d_vm, Err_s, Err_e, *oob);
+  fprintf(g_trace, " %.17e %.17e %.17e %.17e %.17e %.17e %.17e\n", rho_F_avg, rho_P_avg, rho_s_avg, rho_m_avg,
+          rho_g_avg, rho_dipole_avg, rho_forest_avg);
+  fflush(g_trace);
+}
+
 static void dump(const char* dir, const char* name, const void* p, size_t bytes) {
   char path[512];
   snprintf(path, sizeof(path), "%s/%s.bin", dir, name);
@@ -265,6 +287,18 @@ void mth_ref_DestroyJob(void) {
     dump(dir, "crss", cr, n * NSYSMX * sizeof(double));
     free(cr);
     dump(dir, "gamacum", gamacum, n * sizeof(double));
+    if (getenv("MTH_REF_DD")) {
+      double* rr = (double*)calloc(n * NSYSMX * 4, sizeof(double));
+      for (size_t v = 0; v < n; v++)
+        for (int i = 0; i < NSYSMX; i++) {
+          rr[(v * 4 + 0) * NSYSMX + i] = rho_s[v][i];
+          rr[(v * 4 + 1) * NSYSMX + i] = rho_g1[v][i];
+          rr[(v * 4 + 2) * NSYSMX + i] = rho_g2[v][i];
+          rr[(v * 4 + 3) * NSYSMX + i] = rho_g3[v][i];
+        }
+      dump(dir, "rho", rr, n * NSYSMX * 4 * sizeof(double));
+      free(rr);
+    }
   }
   if (g_trace) fclose(g_trace);
   DestroyJob();

@@ -48,6 +48,19 @@ CASES = {
 }
 
 
+# dislocation-density law (the reference's shipped DD_BASED_FLAG path, built as
+# oracle/_ref/forge_ref_dd): per-step trace with the dd.out averages and the
+# final SSD / GND densities
+DD_CASES = {
+    "dd8_poly": synth.Config(cell_dim=(8, 8, 8), n_grains=4, n_steps=4, seed=201, iter_max=40, dd=synth.DD()),
+    "dd8_pores": synth.Config(cell_dim=(8, 8, 8), n_grains=4, n_pores=1, pore_radius=1, n_steps=4, seed=202,
+                              iter_max=30, dd=synth.DD(q_slip=0.22, L0=0.002)),
+    # test_run/input.in's DD values: thermally activated slip switched off
+    "dd8_test_run_values": synth.Config(cell_dim=(8, 8, 8), n_grains=4, n_steps=3, seed=203, iter_max=30,
+                                        dd=synth.DD(T=30.0, q_slip=20000000000.0, q_bulk=300000000000.51)),
+}
+
+
 def cfg_to_json(cfg):
     d = dataclasses.asdict(cfg)
     return json.dumps(d)
@@ -77,5 +90,27 @@ def main():
         print(name, trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
 
 
+def main_dd():
+    ref = os.path.join(REPO, "oracle", "_ref", "forge_ref_dd")
+    for name, cfg in DD_CASES.items():
+        d = os.path.join("/tmp", "mth_golden_" + name)
+        synth.write_case(d, cfg)
+        env = dict(os.environ, MTH_REF_TRACE=os.path.join(d, "trace.txt"), MTH_REF_DUMP=d, MTH_REF_SEED="1",
+                   MTH_REF_DD="1")
+        subprocess.run(["bash", "-c", f"ulimit -s unlimited; {ref} input.in > ref.log 2>&1"], cwd=d, env=env,
+                       check=True)
+        trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))
+        nv = int(np.prod(cfg.cell_dim))
+        fields = {fn: np.fromfile(os.path.join(d, fn + ".bin")).reshape(nv, nc)
+                  for fn, nc in [("sig", 9), ("rot", 9)]}
+        rho = np.fromfile(os.path.join(d, "rho.bin")).reshape(nv, 4, 12)
+        fields["rho_ssd"] = rho[:, 0]
+        fields["rho_gnd"] = rho[:, 1:].reshape(nv, 36)
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out, config=cfg_to_json(cfg), trace=trace, **fields)
+        print(name, trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
+
+
 if __name__ == "__main__":
     main()
+    main_dd()

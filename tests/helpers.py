@@ -10,7 +10,10 @@ from mth import capi, synth
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("dd"))
+# dislocation-density law: the trace rows end with the 7 dd.out averages
+DD_GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("dd"))
+T_DD = slice(45, 52)
 
 # trace columns written by the reference hook (oracle/refshim/refshim.cc)
 T_ITER, T_SIG, T_DG, T_EPS, T_EDOT = 1, slice(2, 11), slice(11, 20), slice(20, 29), slice(29, 38)
@@ -23,7 +26,10 @@ def load_golden(name):
     mat = synth.Material(**d.pop("material"))
     for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
         d[k] = tuple(d[k])
-    cfg = synth.Config(material=mat, **d)
+    dd = d.pop("dd", None)
+    if dd is not None:
+        dd = synth.DD(**{k: (tuple(v) if isinstance(v, list) else v) for k, v in dd.items()})
+    cfg = synth.Config(material=mat, dd=dd, **d)
     fields = {k: z[k] for k in z.files if k not in ("config", "trace")}
     return cfg, z["trace"], fields
 

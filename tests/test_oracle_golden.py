@@ -7,8 +7,8 @@ reproduce their per-step trace and final fields to round-off.
 import numpy as np
 import pytest
 
-from helpers import (GOLDEN_CASES, T_DG, T_EDOT, T_EPS, T_ERRE, T_ERRS, T_ITER, T_SIG, T_SVM, T_SVM1, load_golden,
-                     rel, run_oracle)
+from helpers import (DD_GOLDEN_CASES, GOLDEN_CASES, T_DD, T_DG, T_EDOT, T_EPS, T_ERRE, T_ERRS, T_ITER, T_SIG, T_SVM,
+                     T_SVM1, load_golden, rel, run_oracle)
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
@@ -36,3 +36,26 @@ def test_oracle_matches_reference_trace(name):
         strain = 0.5 * (dg + dg.transpose(0, 2, 1))
         assert rel(o.field("strain"), strain.reshape(-1, 9)) < 1e-10
     assert o.second_backtracks() == 0
+
+
+@pytest.mark.parametrize("name", DD_GOLDEN_CASES)
+def test_oracle_matches_reference_dd_trace(name):
+    """Dislocation-density law: the reference built with its shipped
+    DD_BASED_FLAG path (StrainRate_Orowan, DislocationEvolution with
+    first-order GNDs, AvgDislocation) against the oracle's restatement."""
+    cfg, trace, fields = load_golden(name)
+    o, reps = run_oracle(cfg, nthreads=4)
+    for s, r in enumerate(reps):
+        row = trace[s]
+        assert r["iterations"] == int(row[T_ITER]), (s, r["iterations"], row[T_ITER])
+        assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-11
+        assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-11
+        assert rel(r["eps_avg"], row[T_EPS].reshape(3, 3)) < 1e-9
+        ref_dd = row[T_DD]
+        for k in range(7):
+            assert abs(r["dd_avg"][k] - ref_dd[k]) <= 1e-11 * abs(ref_dd[k]) + 1e-300, (s, k, r["dd_avg"], ref_dd)
+    assert rel(o.field("sig"), fields["sig"]) < 1e-10
+    assert rel(o.field("rot"), fields["rot"]) < 1e-12
+    assert rel(o.field("rho_ssd"), fields["rho_ssd"]) < 1e-11
+    if np.abs(fields["rho_gnd"]).max() > 0:
+        assert rel(o.field("rho_gnd"), fields["rho_gnd"]) < 1e-10
