@@ -23,7 +23,7 @@ LIB = os.path.join(HERE, "lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + os.path.join(REPO, "include")]
-CU_SOURCES = ["fft_green.cu", "fft_tma.cu", "newton.cu", "drx.cu", "adjoint.cu", "capi.cu"]
+CU_SOURCES = ["fft_green.cu", "fft_tma.cu", "newton.cu", "drx.cu", "dd.cu", "adjoint.cu", "capi.cu"]
 # sources compiled without FMA contraction (bit-exact FP64 restatement)
 NO_FMAD = {"drx.cu"}
 # sources whose host code is compiled without FMA contraction: the FP64 host

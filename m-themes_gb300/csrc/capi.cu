@@ -337,6 +337,14 @@ struct mth_ctx {
   int nsys;
   int adj_solid;        // every voxel is of phase 1 and crystalline (adjoint precondition)
   double last_au[3];    // uniform spin increment of the last end of step
+  // dislocation-density law
+  int dd;
+  DdConst* ddc_d;       // device copy of the phase-1 constants
+  void* dd_mem;         // 84 state planes + 36 per-step constant planes
+  DdFields<float> ddf;
+  DdFields<double> ddd;
+  uint8_t* gb_d;        // same-grain neighbour flags per voxel
+  double dd_avg[NPART_DD];
 };
 
 static void iout_free(IoutWriter* w);
@@ -398,15 +406,18 @@ static void ctx_free(mth_ctx* c) {
   cudaFree(c->rho_pf_d);
   cudaFree(c->rho_pf_t);
   cudaFree(c->gid_coarse_d);
+  cudaFree(c->ddc_d);
+  cudaFree(c->dd_mem);
+  cudaFree(c->gb_d);
   delete c;
 }
 
 // ------------------------------------------------------------- profiling
 enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_DRX,
-       K_PF, K_ADJ_LOCAL, K_ADJ_CG, K_NCLASS };
+       K_PF, K_ADJ_LOCAL, K_ADJ_CG, K_DD, K_NCLASS };
 static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain", "newton",
                                         "reduce", "end_step", "spin_fft", "setup", "drx",
-                                        "pf_relax", "adj_local", "adj_cg"};
+                                        "pf_relax", "adj_local", "adj_cg", "dislocation_density"};
 
 static void prof_begin(mth_ctx* c) {
   if (!c->prof_on) return;
@@ -462,6 +473,66 @@ static mth_status make_twiddles(int n, int sign, void** out) {
   return MTH_OK;
 }
 
+// Constants of the dislocation-density law for phase 1: b = a0/sqrt(2)
+// (src/init.c:182), the shear modulus of src/init.c:826, kT and the reduced
+// activation energies (src/constitutive.c:540, src/evp.h:81-86), the junction
+// strengths (FCC junction type of each pair of systems from their geometry:
+// self, coplanar, collinear, Hirth, and for 60-degree pairs glissile when
+// the junction b_i -/+ b_j lies in one of the two planes, Lomer-Cottrell
+// otherwise; for the system order of the FCC .sx files this is the matrix of
+// InteractionStrengthMatrix, src/init.c:593-702) and the projections of
+// src/init.c:1107-1126.
+static void dd_constants(const mth_params& p, const PhaseConst& ph, DdConst& dc) {
+  memset(&dc, 0, sizeof(dc));
+  const mth_phase& in = p.phase[0];
+  dc.nsys = ph.nsys;
+  dc.b = p.dd_a0 / sqrt(2.0);
+  dc.G = 0.1 * (in.c11 - in.c12 + 3 * in.c44) +
+         (0.5) * (5 * (in.c11 - in.c12) * in.c44) / (4 * in.c44 + 3 * (in.c11 - in.c12));
+  dc.nu = p.dd_nu;
+  for (int k = 0; k < 8; k++) dc.c[k] = p.dd_c[k];
+  dc.T = p.dd_T;
+  dc.kT = p.dd_T * 1.380658e-23 * (1.0 / 1.60217733e-19);
+  dc.qslip = p.dd_q_slip * 0.62415063631 / dc.kT;
+  dc.qbulk = p.dd_q_bulk * 0.62415063631 / dc.kT;
+  dc.L0 = p.dd_L0;
+  dc.d0 = p.dd_d0;
+  const int ns = ph.nsys;
+  for (int i = 0; i < ns; i++) {
+    for (int k = 0; k < 5; k++) dc.m_xt[i][k] = ph.m_xt[i][k];
+    for (int m = 0; m < 3; m++) dc.bb[i][m] = ph.bb[i][m];
+    dc.bp[i][0] = ph.bb[i][1] * ph.bn[i][2] - ph.bb[i][2] * ph.bn[i][1];
+    dc.bp[i][1] = ph.bb[i][2] * ph.bn[i][0] - ph.bb[i][0] * ph.bn[i][2];
+    dc.bp[i][2] = ph.bb[i][0] * ph.bn[i][1] - ph.bb[i][1] * ph.bn[i][0];
+  }
+  auto dot3 = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  for (int i = 0; i < ns; i++)
+    for (int j = 0; j < ns; j++) {
+      const double* ni = ph.bn[i];
+      const double* nj = ph.bn[j];
+      const double* bi = ph.bb[i];
+      const double* bj = ph.bb[j];
+      double chi;
+      if (i == j) chi = p.dd_chi[0];
+      else if (fabs(fabs(dot3(ni, nj)) - 1.0) < 1e-6) chi = p.dd_chi[1];
+      else if (fabs(fabs(dot3(bi, bj)) - 1.0) < 1e-6) chi = p.dd_chi[2];
+      else if (fabs(dot3(bi, bj)) < 1e-6) chi = p.dd_chi[4];
+      else {
+        const double sg = dot3(bi, bj) > 0 ? 1.0 : -1.0;
+        const double q[3] = {bi[0] - sg * bj[0], bi[1] - sg * bj[1], bi[2] - sg * bj[2]};
+        chi = (fabs(dot3(q, ni)) < 1e-6 || fabs(dot3(q, nj)) < 1e-6) ? p.dd_chi[3] : p.dd_chi[5];
+      }
+      dc.chi[i][j] = chi;
+      const double sv[3] = {nj[1] * bj[2] - nj[2] * bj[1], nj[2] * bj[0] - nj[0] * bj[2], nj[0] * bj[1] - nj[1] * bj[0]};
+      dc.cs[i][j] = fabs(dot3(ni, sv));
+      dc.ss[i][j] = fabs(sqrt(fabs(1.0 - dc.cs[i][j] * dc.cs[i][j])));
+      dc.cg1[i][j] = fabs(dot3(ni, bj));
+      dc.sg1[i][j] = fabs(sqrt(fabs(1.0 - dc.cg1[i][j] * dc.cg1[i][j])));
+      dc.cg3[i][j] = fabs(dot3(ni, nj));
+      dc.sg3[i][j] = fabs(sqrt(fabs(1.0 - dc.cg3[i][j] * dc.cg3[i][j])));
+    }
+}
+
 extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   if (!p || !out) return set_err(MTH_ERR_ARG, "null argument");
   *out = nullptr;
@@ -486,6 +557,28 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   for (int k = 0; k < p->n_phases; k++) {
     mth_status s = fill_phase(p->phase[k], c->nc.ph[k]);
     if (s) { delete c; return s; }
+  }
+  c->dd = p->flow_law == 1 ? 1 : 0;
+  if (p->flow_law != 0 && p->flow_law != 1) { delete c; return set_err(MTH_ERR_ARG, "flow_law=%d", p->flow_law); }
+  if (c->dd) {
+    if (c->nc.ph[0].type != 0 || (p->n_phases == 2 && c->nc.ph[1].type == 0)) {
+      delete c;
+      return set_err(MTH_ERR_UNSUPPORTED, "dislocation-density law: phase 1 crystalline, phase 2 (if any) gas");
+    }
+    if (c->nc.ph[0].nsys != 12) {
+      delete c;
+      return set_err(MTH_ERR_UNSUPPORTED, "dislocation-density law: the 12 FCC {111}<110> systems (nsys=%d)",
+                     c->nc.ph[0].nsys);
+    }
+    if (p->pf_substeps > 0) {
+      delete c;
+      return set_err(MTH_ERR_UNSUPPORTED, "dislocation-density law with phase-field DRX");
+    }
+    if (!(p->dd_a0 > 0) || !(p->dd_T > 0) || !(p->dd_L0 > 0) || !(p->dd_c[0] > 0) || !(p->dd_c[1] > 0) ||
+        !(p->dd_c[2] > 0) || !(p->dd_nu < 1)) {
+      delete c;
+      return set_err(MTH_ERR_ARG, "dislocation-density parameters: a0, T__K, L0, C_1..C_3 > 0 and nu < 1");
+    }
   }
   c->nc.dt = p->time_step;
   c->nc.tol = p->newton_tol > 0 ? p->newton_tol : (c->mixed ? 1e-6 : 1e-10);
@@ -603,6 +696,7 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     f.crss = base + o; o += 12 * P;
     f.gamacum = base + o; o += P;
     f.wspin = base + o; o += 3 * P;
+    f.ddc = nullptr;
     f.phase = c->phase_d;
     f.eclass = c->eclass_d;
     f.etab = nullptr;
@@ -611,6 +705,28 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   };
   if (c->mixed) carve(static_cast<float*>(c->fieldmem), c->ff);
   else carve(static_cast<double*>(c->fieldmem), c->fd);
+  if (c->dd) {
+    DdConst dc;
+    dd_constants(*p, c->nc.ph[0], dc);
+    CKC(cudaMalloc(&c->ddc_d, sizeof(DdConst)));
+    CKC(cudaMemcpy(c->ddc_d, &dc, sizeof(DdConst), cudaMemcpyHostToDevice));
+    CKC(cudaMalloc(&c->dd_mem, esz * P * (7 * NSYS + 3 * NSYS)));
+    CKC(cudaMalloc(&c->gb_d, P));
+    auto carve_dd = [&](auto* base, auto& d, auto& f) {
+      long long o = 0;
+      d.rho_s = base + o; o += NSYS * P;
+      d.g1 = base + o; o += NSYS * P;
+      d.g2 = base + o; o += NSYS * P;
+      d.g3 = base + o; o += NSYS * P;
+      d.dipole = base + o; o += NSYS * P;
+      d.forest = base + o; o += NSYS * P;
+      d.gamdot = base + o; o += NSYS * P;
+      f.ddc = base + o; o += 3 * NSYS * P;
+      d.gb = c->gb_d;
+    };
+    if (c->mixed) carve_dd(static_cast<float*>(c->dd_mem), c->ddf, c->ff);
+    else carve_dd(static_cast<double*>(c->dd_mem), c->ddd, c->fd);
+  }
   c->tma = c->mixed ? tma_create<float>(g, c->ff.sig, c->ff.strain, c->ff.wspin, static_cast<c2<float>*>(c->spec),
                                         static_cast<c2<float>*>(c->anti))
                     : tma_create<double>(g, c->fd.sig, c->fd.strain, c->fd.wspin, static_cast<c2<double>*>(c->spec),
@@ -838,6 +954,27 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   t2v(c->disgrad_avg, d6, 6);
   const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
   LAUNCH(K_SETUP, 0.0, launch_setup(c->mixed, c->nc, f, eul_d, d6, c->nblocks, c->st));
+  if (c->dd) {
+    // same-grain flags of the six face neighbours (Gradient_ExchangeGrainID,
+    // src/constitutive.c:724-873; its -z flag compares with the -y neighbour)
+    std::vector<uint8_t> gb(n);
+    const int n0 = c->n[0], n1 = c->n[1], n2 = c->n[2];
+    for (int x = 0; x < n0; x++)
+      for (int y = 0; y < n1; y++)
+        for (int z = 0; z < n2; z++) {
+          const size_t v = ((size_t)x * n1 + y) * n2 + z;
+          auto at = [&](int a, int b, int cz) { return grain[((size_t)a * n1 + b) * n2 + cz]; };
+          const int g0 = grain[v];
+          const int ym = at(x, (y + n1 - 1) % n1, z);
+          gb[v] = (uint8_t)((g0 == at((x + 1) % n0, y, z)) | ((g0 == at((x + n0 - 1) % n0, y, z)) << 1) |
+                            ((g0 == at(x, (y + 1) % n1, z)) << 2) | ((g0 == ym) << 3) |
+                            ((g0 == at(x, y, (z + 1) % n2)) << 4) | ((g0 == ym) << 5));
+        }
+    CK(cudaMemcpyAsync(c->gb_d, gb.data(), n, cudaMemcpyHostToDevice, c->st));
+    const void* dd = c->mixed ? (const void*)&c->ddf : (const void*)&c->ddd;
+    LAUNCH(K_DD, 0.0, launch_dd_init(c->mixed, dd, c->phase_d, c->nv, c->p.dd_rho_ssd0, c->st));
+    CK(cudaStreamSynchronize(c->st));   // gb is a local buffer
+  }
   CK(cudaStreamSynchronize(c->st));
   prof_resolve(c);
   cudaFree(eul_d);
@@ -924,7 +1061,7 @@ static mth_status green_iteration(mth_ctx* c) {
   // Newton: read sigma, strain, eps_p (18), rot (9), CRSS (12); write sigma, edot (12);
   // phase (1 B) and elastic class (4 B) per voxel
   LAUNCH(K_NEWTON, (18 + 9 + 12 + 12) * rp + 5.0 * (double)c->nv,
-         launch_newton(c->mixed, c->nc, &f, c->partials, c->nblocks, it, c->st));
+         launch_newton(c->mixed, c->nc, &f, c->partials, c->nblocks, it, c->st, c->dd));
   return MTH_OK;
 }
 
@@ -1117,6 +1254,14 @@ static mth_status step_begin(mth_ctx* c) {
     if (s) return s;
   }
   c->nc.flow_off = (c->istep == 0 && c->p.update_flag != 1) ? 1 : 0;
+  if (c->dd) {
+    // the step's passing stress, tau_0 + cutting stress and reference rate
+    // per system, from the densities at the start of the step
+    const void* dd = c->mixed ? (const void*)&c->ddf : (const void*)&c->ddd;
+    const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+    const double w = c->mixed ? 4.0 : 8.0;
+    LAUNCH(K_DD, (double)c->nv * w * (4 * NSYS + 3 * NSYS), launch_dd_prep(c->mixed, c->ddc_d, dd, f, c->st));
+  }
   memset(c->ddg, 0, sizeof(c->ddg));
   memset(c->ddg_acum, 0, sizeof(c->ddg_acum));
   memset(c->ddg_applied, 0, sizeof(c->ddg_applied));
@@ -1200,11 +1345,27 @@ static mth_status step_end(mth_ctx* c, mth_step_report* rep) {
   }
   for (int i = 0; i < 3; i++) c->last_au[i] = au[i];
   const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+  if (c->dd) {
+    // shear rates at the converged stress, then DislocationEvolution (with
+    // the shear-rate gradients from the third step on when Hard_Flag = 1,
+    // src/evolution.c:1551-1565) on the rotation of the start of the step,
+    // before the lattice rotation of end_step
+    const void* dd = c->mixed ? (const void*)&c->ddf : (const void*)&c->ddd;
+    const double w = c->mixed ? 4.0 : 8.0, nv = (double)c->nv;
+    LAUNCH(K_DD, nv * w * (6 + 9 + 3 * NSYS + NSYS), launch_dd_gamdot(c->mixed, c->ddc_d, dd, f, c->nc.flow_off, c->st));
+    const int do_grad = (c->p.hard_flag == 1 && istep > 1) ? 1 : 0;
+    LAUNCH(K_DD, nv * w * (6 + 9 + 7 * NSYS + 5 * NSYS) + nv,
+           launch_dd_evolve(c->mixed, c->ddc_d, dd, f, c->n, dt, do_grad, c->partials, c->st));
+    double red[NPART_DD];
+    mth_status s = reduce_to_host(c, NPART_DD, red);
+    if (s) return s;
+    for (int k = 0; k < NPART_DD; k++) c->dd_avg[k] = red[k] * c->wgt;
+  }
   {
     // end-of-step bytes: eps_p RMW + edot (18), sigma (6), rot RMW (18), CRSS RMW (24), gamacum RMW (2), spin (3)
     const double rp = (double)(c->mixed ? sizeof(float) : sizeof(double)) * (double)c->nv;
     LAUNCH(K_END_STEP, (18 + 6 + 18 + 24 + 2 + 3) * rp + (double)c->nv,
-           launch_end_step(c->mixed, c->nc, f, au, do_orient, do_harden, c->partials, c->nblocks, c->st));
+           launch_end_step(c->mixed, c->nc, f, au, do_orient, do_harden, c->partials, c->nblocks, c->st, c->dd));
   }
   double red[NPART_END];
   mth_status s = reduce_to_host(c, NPART_END, red);
@@ -1235,6 +1396,7 @@ static mth_status step_end(mth_ctx* c, mth_step_report* rep) {
     rep->newton_iters = c->it_nit;
     rep->newton_failed = c->it_nbad;
     rep->n_new_grains = c->it_nnew;
+    if (c->dd) memcpy(rep->dd_avg, c->dd_avg, sizeof(c->dd_avg));
   }
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) c->disgrad_avg[i][j] = c->disgrad_avg_t[i][j] + c->udot[i][j] * dt;
@@ -1278,6 +1440,14 @@ static mth_status download(mth_ctx* c, int field, double* host) {
     case MTH_FIELD_ROT: src = f.rot; nc = 9; break;
     case MTH_FIELD_CRSS: src = f.crss; nc = 12; break;
     case MTH_FIELD_GAMACUM: src = f.gamacum; nc = 1; break;
+    case MTH_FIELD_RHO_SSD:
+    case MTH_FIELD_RHO_GND: {
+      if (!c->dd) return set_err(MTH_ERR_STATE, "dislocation densities exist with the dislocation-density law only");
+      const DdFields<T>& d = *reinterpret_cast<const DdFields<T>*>(c->mixed ? (void*)&c->ddf : (void*)&c->ddd);
+      src = field == MTH_FIELD_RHO_SSD ? d.rho_s : d.g1;   // g1, g2, g3 are consecutive planes
+      nc = field == MTH_FIELD_RHO_SSD ? NSYS : 3 * NSYS;
+      break;
+    }
     default: return set_err(MTH_ERR_ARG, "field %d", field);
   }
   // converted to the host layout on the device, then one copy into the
@@ -1318,7 +1488,10 @@ extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, si
     for (long long v = 0; v < c->nv; v++) host[v] = h[v];
     return MTH_OK;
   }
-  const int ncomp = (field == MTH_FIELD_CRSS) ? 12 : (field == MTH_FIELD_GAMACUM || field == MTH_FIELD_RHO) ? 1 : 9;
+  const int ncomp = (field == MTH_FIELD_CRSS || field == MTH_FIELD_RHO_SSD) ? 12
+                    : (field == MTH_FIELD_RHO_GND)                          ? 36
+                    : (field == MTH_FIELD_GAMACUM || field == MTH_FIELD_RHO) ? 1
+                                                                             : 9;
   if (count != (size_t)ncomp * c->nv) return set_err(MTH_ERR_ARG, "count=%zu, expected %lld", count, ncomp * c->nv);
   return c->mixed ? download<float>(c, field, host) : download<double>(c, field, host);
 }
@@ -1974,6 +2147,7 @@ extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batc
   for (int i = 0; i < n; i++) {
     if (params[i].device != params[0].device) return set_err(MTH_ERR_ARG, "batch members on different devices");
     if (params[i].pf_substeps > 0) return set_err(MTH_ERR_UNSUPPORTED, "recrystallisation in a batch member");
+    if (params[i].flow_law != 0) return set_err(MTH_ERR_UNSUPPORTED, "dislocation-density law in a batch member");
   }
   mth_batch* b = new mth_batch();
   b->n = n;
@@ -2359,6 +2533,7 @@ extern "C" mth_status mth_adjoint(mth_ctx* c, const mth_adjoint_opts* o, double*
   if (c->in_batch) return set_err(MTH_ERR_STATE, "context belongs to a batch");
   if (o->n_steps < 1 || !o->target) return set_err(MTH_ERR_ARG, "n_steps >= 1 and a target curve are required");
   if (c->drx) return set_err(MTH_ERR_UNSUPPORTED, "adjoint with phase-field DRX");
+  if (c->dd) return set_err(MTH_ERR_UNSUPPORTED, "adjoint of the dislocation-density law");
   if (!c->adj_solid) return set_err(MTH_ERR_UNSUPPORTED, "adjoint needs every voxel of phase 1 and crystalline");
   if (c->p.elast_bc != 1) return set_err(MTH_ERR_UNSUPPORTED, "adjoint needs ElastBC = 1");
   for (int a = 0; a < 6; a++) {

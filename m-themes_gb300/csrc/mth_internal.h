@@ -109,6 +109,8 @@ struct Fields {
   TSt* crss;     // 12 planes: forward CRSS
   TSt* gamacum;  // 1 plane
   TSt* wspin;    // 3 planes: antisymmetric part of the accumulated grad-u increment
+  TSt* ddc;      // dislocation-density law: 36 planes, per system passing stress (12),
+                 // tau_0 + cutting stress (12), reference rate (12) of the step; else null
   const uint8_t* phase;  // 0-based phase index
   const int* eclass;     // elastic class of the voxel (row of etab)
   const double* etab;    // ETAB_W doubles per class
@@ -133,11 +135,12 @@ constexpr int NPART = 16;   // err_s, err_e, sig[6], sig_ph1[6], newton_iters, n
 // Partial sums written per block by the end-of-step kernel.
 constexpr int NPART_END = 12;  // epsp[6], edot[6]
 
+// law: 0 power law + Voce, 1 dislocation density (per-system constants in
+// Fields::ddc, harden off)
 cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
-                          const IterIn& it,
-                          cudaStream_t st);
+                          const IterIn& it, cudaStream_t st, int law = 0);
 cudaError_t launch_end_step(int mixed, const NewtonConst& nc, const void* fields, const double anti_uniform[3],
-                            int do_orient, int do_harden, double* partials, int nblocks, cudaStream_t st);
+                            int do_orient, int do_harden, double* partials, int nblocks, cudaStream_t st, int law = 0);
 cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, const double* euler,
                          const double d6[6], int nblocks, cudaStream_t st);
 cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, const double* epsp,
@@ -187,6 +190,39 @@ cudaError_t launch_resample_trilinear(const int ns[3], const double* src, const 
                                       cudaStream_t st);
 cudaError_t launch_gather_rot(int mixed, const void* rot, long long nv, const long long* sites, int nn, double* out,
                               cudaStream_t st);
+
+// ------------------------------------------------- dislocation-density law
+// Constants of phase 1 (device-resident copy per context): Burgers vector,
+// shear modulus, Poisson ratio, C_1..C_8, kT [eV], reduced activation
+// energies, L0, D_0, T; junction strengths and the projection cosines/sines
+// of the forest and parallel densities (src/init.c:1096-1126); crystal-axes
+// Schmid vectors, screw sense vectors b x n and slip directions.
+struct DdConst {
+  int nsys;
+  double b, G, nu, c[8], kT, qslip, qbulk, L0, d0, T;
+  double chi[NSYS][NSYS], cs[NSYS][NSYS], ss[NSYS][NSYS], cg1[NSYS][NSYS], sg1[NSYS][NSYS], cg3[NSYS][NSYS],
+      sg3[NSYS][NSYS];
+  double m_xt[NSYS][5], bp[NSYS][3], bb[NSYS][3];
+};
+// Per-voxel state, 12 planes each (voxel index fastest).
+template <typename T>
+struct DdFields {
+  T* rho_s;    // statistically stored density
+  T* g1;       // GND: screw
+  T* g2;       // GND: edge I
+  T* g3;       // GND: edge II (stays 0 with first-order GNDs)
+  T* dipole;   // rho_dipole, rho_forest: accumulated for the dd.out averages
+  T* forest;
+  T* gamdot;   // shear rate at the converged stress of the step
+  const uint8_t* gb;   // per voxel: bit 2a / 2a+1 = neighbour +/- along axis a in the same grain
+};
+cudaError_t launch_dd_init(int mixed, const void* dd, const uint8_t* phase, long long P, double rho0, cudaStream_t st);
+cudaError_t launch_dd_prep(int mixed, const DdConst* dc, const void* dd, const void* fields, cudaStream_t st);
+cudaError_t launch_dd_gamdot(int mixed, const DdConst* dc, const void* dd, const void* fields, int flow_off,
+                             cudaStream_t st);
+cudaError_t launch_dd_evolve(int mixed, const DdConst* dc, const void* dd, const void* fields, const int dims[3],
+                             double dt, int do_grad, double* partials, cudaStream_t st);
+constexpr int NPART_DD = 7;
 
 long long noalloc_max_voxels();
 cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, double* sig, const double* epsp,

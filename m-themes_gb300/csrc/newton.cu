@@ -106,6 +106,107 @@ __device__ __forceinline__ void flow_rule(const PhaseConst& ph, const TF x[5], c
   }
 }
 
+// Dislocation-density flow rule of StrainRate_Orowan, forward plus backward
+// jumps (src/constitutive.c:507-721), in crystal axes: per system
+// gdot = g0 sinh((|rss| - tp)/td) sign(rss) where |rss| > tp, else 0, with
+// tp the passing stress, td = tau_0 + cutting stress and g0 the reference
+// rate of the step (from the dislocation densities, dd.cu).  It is the
+// gradient of the convex potential psi = sum g0 td (cosh(t) - 1),
+// t = max(|rss| - tp, 0)/td, written 2 g0 td sinh^2(t/2).
+template <typename TF, bool WANT_D>
+__device__ __forceinline__ void flow_rule_dd(const PhaseConst& ph, const TF x[5], const TF* tp, const TF* td,
+                                             const TF* g0, TF ed[5], TF D[15], TF& psi, TF* gam) {
+#pragma unroll
+  for (int i = 0; i < 5; i++) ed[i] = 0;
+  if (WANT_D) {
+#pragma unroll
+    for (int i = 0; i < 15; i++) D[i] = 0;
+  }
+  psi = 0;
+  const int ns = ph.nsys;
+#pragma unroll
+  for (int s = 0; s < NSYS; s++) {
+    if (s < ns) {
+      TF m[5];
+#pragma unroll
+      for (int i = 0; i < 5; i++) m[i] = cpick<TF>(ph.m_xt[s][i], ph.m_xtf[s][i]);
+      const TF rss = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4];
+      const TF ar = fabs(rss);
+      TF g = 0, w = 0;
+      if (ar > tp[s]) {
+        const TF t = (ar - tp[s]) / td[s];
+        const TF sh = sinh(t);
+        g = g0[s] * (rss > (TF)0 ? sh : -sh);
+        if (WANT_D) w = g0[s] * cosh(t) / td[s];
+        const TF h = sinh((TF)0.5 * t);
+        psi += (TF)2 * g0[s] * td[s] * h * h;
+      }
+      if (gam) gam[s] = g;
+#pragma unroll
+      for (int i = 0; i < 5; i++) ed[i] += m[i] * g;
+      if (WANT_D) {
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < 5; i++)
+#pragma unroll
+          for (int j = i; j < 5; j++) D[q++] += w * m[i] * m[j];
+      }
+    } else if (gam) {
+      gam[s] = 0;
+    }
+  }
+}
+
+// Slip laws of the local solve.  Power law: forward CRSS per system, the
+// backward one offset by tau_off.  Dislocation density: passing stress,
+// tau_0 + cutting stress and reference rate per system.
+template <typename TF>
+struct PlSlip {
+  TF tauf[NSYS];
+  TF tau_off;
+  template <bool WANT_D>
+  __device__ __forceinline__ void flow(const PhaseConst& ph, const TF x[5], TF ed[5], TF D[15], TF& psi,
+                                       TF* gam) const {
+    flow_rule<TF, WANT_D>(ph, x, tauf, tau_off, ed, D, psi, gam);
+  }
+};
+template <typename TF>
+struct DdSlip {
+  TF tp[NSYS], td[NSYS], g0[NSYS];
+  template <bool WANT_D>
+  __device__ __forceinline__ void flow(const PhaseConst& ph, const TF x[5], TF ed[5], TF D[15], TF& psi,
+                                       TF* gam) const {
+    flow_rule_dd<TF, WANT_D>(ph, x, tp, td, g0, ed, D, psi, gam);
+  }
+};
+// slip-law state of voxel v from the fields (LAW 0: power law, 1: dislocation density)
+template <int LAW, typename TF, typename TSt>
+struct SlipOf;
+template <typename TF, typename TSt>
+struct SlipOf<0, TF, TSt> {
+  using type = PlSlip<TF>;
+  __device__ __forceinline__ static void load(const PhaseConst& ph, const Fields<TSt>& f, long long v, type& sl) {
+    const long long P = f.nv;
+#pragma unroll
+    for (int s = 0; s < NSYS; s++) sl.tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+    sl.tau_off = cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf);
+  }
+};
+template <typename TF, typename TSt>
+struct SlipOf<1, TF, TSt> {
+  using type = DdSlip<TF>;
+  __device__ __forceinline__ static void load(const PhaseConst& ph, const Fields<TSt>& f, long long v, type& sl) {
+    const long long P = f.nv;
+#pragma unroll
+    for (int s = 0; s < NSYS; s++) {
+      const bool a = s < ph.nsys;
+      sl.tp[s] = a ? (TF)f.ddc[s * P + v] : (TF)0;
+      sl.td[s] = a ? (TF)f.ddc[(NSYS + s) * P + v] : (TF)1;
+      sl.g0[s] = a ? (TF)f.ddc[(2 * NSYS + s) * P + v] : (TF)0;
+    }
+  }
+};
+
 __device__ __forceinline__ int pk(int i, int j) {  // packed upper-triangle index of 5x5
   if (i > j) { int t = i; i = j; j = t; }
   return i * 5 - (i * (i - 1)) / 2 + (j - i);
@@ -229,8 +330,8 @@ struct VoxelOut {
 // at the start and again (again = true: loads the compiler may not merge
 // with the first) for the back-transform and the error norms, so neither
 // the inputs nor the 5x5 frame rotation stay live across the Newton loop.
-template <typename TF, typename TL, bool ROOT_ONLY, typename Load>
-__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const TF* tauf,
+template <typename TF, typename TL, bool ROOT_ONLY, typename Slip, typename Load>
+__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const Slip& slip,
                                 const Load& load, TF* sig6, TF* ed6) {
   VoxelOut o = {0.0, 0.0, 0, 0};
   const TF dt = cpick<TF>(nc.dt, nc.dtf);
@@ -304,7 +405,6 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
   }
   const TF tol2 = cpick<TF>(nc.tol, nc.tolf) * cpick<TF>(nc.tol, nc.tolf);
   const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
-  const TF tau_off = cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf);
   // Newton with a backtracking line search on Phi for large steps.  One
   // flow-rule evaluation site: every evaluation (with its Hessian) is at the
   // point the loop moves to next, so an accepted line-search trial supplies
@@ -342,7 +442,7 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
       for (int i = 0; i < 15; i++) Df[i] = 0;
       psif = 0;
     } else {
-      flow_rule<TF, true>(ph, xt, tauf, tau_off, edf, Df, psif, nullptr);
+      slip.template flow<true>(ph, xt, edf, Df, psif, nullptr);
     }
     TF Kx[5];
     symv5<TF>(K, xt, Kx);
@@ -534,7 +634,7 @@ template <typename T>
 __device__ __forceinline__ T ld_sel(const T* p, bool again) { return again ? ld_again(p) : *p; }
 
 // ------------------------------------------------------------ Newton kernel
-template <typename TSt, typename TF, typename TS, int MINB, bool ROOT_ONLY = false>
+template <typename TSt, typename TF, typename TS, int MINB, bool ROOT_ONLY = false, int LAW = 0>
 __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc, Fields<TSt> f, double* __restrict__ partials,
                                                                 IterIn it) {
   if (!is_live(it)) return;
@@ -547,9 +647,8 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
     const int jph = f.phase[v];
     const PhaseConst& ph = nc.ph[jph];
     if (ph.type == 0) {
-      TF tauf[NSYS];
-#pragma unroll
-      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+      typename SlipOf<LAW, TF, TSt>::type slip;
+      SlipOf<LAW, TF, TSt>::load(ph, f, v, slip);
       auto load = [&](TF* lam6, TF* eps6, TF* ep6, TF* R, bool again) {
 #pragma unroll
         for (int i = 0; i < 6; i++) {
@@ -562,7 +661,7 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
       };
       TF s6[6], e6[6];
       const TF* et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
-      VoxelOut o = solve_voxel<TF, TS, ROOT_ONLY>(nc, ph, et, tauf, load, s6, e6);
+      VoxelOut o = solve_voxel<TF, TS, ROOT_ONLY>(nc, ph, et, slip, load, s6, e6);
 #pragma unroll
       for (int i = 0; i < 6; i++) {
         f.sig[i * P + v] = (TSt)s6[i];
@@ -614,9 +713,21 @@ void fill_float_consts(NewtonConst& nc) {
 }
 
 cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* fields, double* partials, int nblocks,
-                          const IterIn& it, cudaStream_t st) {
+                          const IterIn& it, cudaStream_t st, int law) {
   NewtonConst nc = nc_in;
   fill_float_consts(nc);
+  if (law == 1) {
+    // dislocation-density law: the FP64 Jacobian solve at every step in the
+    // mixed modes (no FP32-solve variants)
+    if (mixed) {
+      const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+      newton_kernel<float, float, double, 1, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    } else {
+      const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
+      newton_kernel<double, double, double, 1, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    }
+    return cudaGetLastError();
+  }
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     newton_kernel<float, float, float, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
@@ -638,7 +749,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
 // (src/constitutive.c:142-273) and harden (src/constitutive.c:275-326).
 // anti_u: uniform part of the lattice spin increment, (2,1),(0,2),(1,0)
 // components of 2 Udot_a dt + antisym(sum dDisGradAvg).
-template <typename TSt, typename TF>
+template <typename TSt, typename TF, int LAW = 0>
 __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fields<TSt> f, double au0, double au1,
                                                        double au2, int do_orient, int do_harden,
                                                        double* __restrict__ partials) {
@@ -660,13 +771,13 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       acc[6 + i] = ed;
     }
     if (ph.type == 0 && (do_orient || do_harden)) {
-      TF R[9], Q[25], s6[6], x[5], tauf[NSYS], gam[NSYS], ed[5], psi;
+      TF R[9], Q[25], s6[6], x[5], gam[NSYS], ed[5], psi;
 #pragma unroll
       for (int i = 0; i < 9; i++) R[i] = (TF)f.rot[i * P + v];
 #pragma unroll
       for (int i = 0; i < 6; i++) s6[i] = (TF)f.sig[i * P + v];
-#pragma unroll
-      for (int s = 0; s < NSYS; s++) tauf[s] = s < ph.nsys ? (TF)f.crss[s * P + v] : (TF)1;
+      typename SlipOf<LAW, TF, TSt>::type slip;
+      SlipOf<LAW, TF, TSt>::load(ph, f, v, slip);
       rot_to_q<TF>(R, Q);
 #pragma unroll
       for (int i = 0; i < 5; i++) {
@@ -677,7 +788,7 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
       }
 #pragma unroll
       for (int s = 0; s < NSYS; s++) gam[s] = 0;
-      if (!nc.flow_off) flow_rule<TF, false>(ph, x, tauf, cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf), ed, nullptr, psi, gam);
+      if (!nc.flow_off) slip.template flow<false>(ph, x, ed, nullptr, psi, gam);
       if (do_orient) {
         // plastic spin: RotSlip = -1/2 T sum_a gam_a (b_a x n_a)
         TF cx = 0, cy = 0, cz = 0;
@@ -766,9 +877,19 @@ __global__ void __launch_bounds__(256) end_step_kernel(const NewtonConst nc, Fie
 }
 
 cudaError_t launch_end_step(int mixed, const NewtonConst& nc_in, const void* fields, const double au[3], int do_orient,
-                            int do_harden, double* partials, int nblocks, cudaStream_t st) {
+                            int do_harden, double* partials, int nblocks, cudaStream_t st, int law) {
   NewtonConst nc = nc_in;
   fill_float_consts(nc);
+  if (law == 1) {
+    if (mixed) {
+      const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+      end_step_kernel<float, float, 1><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, 0, partials);
+    } else {
+      const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
+      end_step_kernel<double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, 0, partials);
+    }
+    return cudaGetLastError();
+  }
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     end_step_kernel<float, float><<<nblocks, 256, 0, st>>>(nc, f, au[0], au[1], au[2], do_orient, do_harden, partials);
@@ -917,7 +1038,10 @@ __global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, 
     for (int i = 0; i < 6; i++) { l[i] = lam6[i]; e[i] = eps6[i]; q[i] = ep6[i]; }
     for (int i = 0; i < 9; i++) r[i] = R[i];
   };
-  VoxelOut o = solve_voxel<double, double, false>(nc, ph, etab + (size_t)v * ETAB_W, tauf, load, s6, e6);
+  PlSlip<double> pl;
+  for (int k = 0; k < NSYS; k++) pl.tauf[k] = tauf[k];
+  pl.tau_off = ph.tau_back_minus_fwd;
+  VoxelOut o = solve_voxel<double, double, false>(nc, ph, etab + (size_t)v * ETAB_W, pl, load, s6, e6);
   for (int i = 0; i < 6; i++) {
     sig[6 * v + i] = s6[i];
     edot[6 * v + i] = e6[i];
@@ -1007,7 +1131,10 @@ __global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonCo
       for (int i = 0; i < 6; i++) { l[i] = lam6[i]; e[i] = eps6[i]; q[i] = ep6[i]; }
       for (int i = 0; i < 9; i++) r[i] = R[i];
     };
-    VoxelOut o = solve_voxel<double, double, false>(nc, ph, et, tauf, load, s6, e6);
+    PlSlip<double> pl;
+    for (int k = 0; k < NSYS; k++) pl.tauf[k] = tauf[k];
+    pl.tau_off = ph.tau_back_minus_fwd;
+    VoxelOut o = solve_voxel<double, double, false>(nc, ph, et, pl, load, s6, e6);
     for (int i = 0; i < 6; i++) {
       sig[6 * v + i] = s6[i];
       edot[6 * v + i] = e6[i];

@@ -11,7 +11,9 @@
  * block at src/evolution.c:1633-1648 writes the same two every 500 steps),
  * in the background while the next steps run.
  *
- * Usage: forge input.in [--mixed] [--iout-every K]
+ * Usage: forge input.in [--mixed] [--iout-every K] [--dd]
+ * --dd runs the dislocation-density law (the reference's DD_BASED_FLAG build)
+ * with the namelist's DD block and writes dd.out.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -20,7 +22,7 @@
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    fprintf(stderr, "usage: %s input.in [--mixed] [--iout-every K]\n", argv[0]);
+    fprintf(stderr, "usage: %s input.in [--mixed] [--iout-every K] [--dd]\n", argv[0]);
     return 2;
   }
   mth_params p;
@@ -34,6 +36,7 @@ int main(int argc, char** argv) {
   for (int i = 2; i < argc; i++) {
     if (!strcmp(argv[i], "--mixed")) p.precision = MTH_MIXED;
     else if (!strcmp(argv[i], "--iout-every") && i + 1 < argc) iout_every = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--dd")) p.flow_law = 1;
   }
   if (p.n_phases >= 1 && p.phase[0].type == 0 && mth_read_sx(sx1, &p, 0) != MTH_OK) {
     fprintf(stderr, "cannot read %s\n", sx1);
@@ -60,7 +63,9 @@ int main(int argc, char** argv) {
   }
   FILE* vm = fopen("vm.out", "w");
   FILE* ss = fopen("ss.out", "w");
+  FILE* dd = p.flow_law == 1 ? fopen("dd.out", "w") : NULL;
   fprintf(vm, "TIME\tEVM\tEVMP\tDVM\tDVMP\tSVM\tSVMSVM_1\n");
+  if (dd) fprintf(dd, "TIME\tEVM\tDD_F\tDD_P\tDD_s\tDD_m\tDD_g\n");   /* src/init.c:499 */
   fprintf(ss, "STEP\tITER\tTIME\tE11\tE22\tE33\tS11\tS22\tS33\tERRS\tERRE\n");
   for (int istep = 0; istep < p.n_steps; istep++) {
     mth_step_report r;
@@ -73,6 +78,12 @@ int main(int argc, char** argv) {
     fprintf(ss, "%d\t%d\t%e\t%.9e\t%.9e\t%.9e\t%.9e\t%.9e\t%.9e\t%e\t%e\n", istep, r.iterations, r.time,
             r.disgrad_avg[0][0], r.disgrad_avg[1][1], r.disgrad_avg[2][2], r.sig_avg[0][0], r.sig_avg[1][1],
             r.sig_avg[2][2], r.err_s, r.err_e);
+    if (dd) {   /* src/evolution.c:1566-1569 */
+      fprintf(dd, "%e\t%e", r.time, r.e_vm);
+      for (int k = 0; k < 7; k++) fprintf(dd, "\t%e", r.dd_avg[k]);
+      fprintf(dd, "\n");
+      fflush(dd);
+    }
     fflush(vm);
     fflush(ss);
     if (iout_every > 0 && istep % iout_every == 0) {
@@ -88,6 +99,7 @@ int main(int argc, char** argv) {
   if (s != MTH_OK) fprintf(stderr, "%s\n", mth_last_error());
   fclose(vm);
   fclose(ss);
+  if (dd) fclose(dd);
   mth_destroy(ctx);
   free(grain);
   free(phase);

@@ -28,6 +28,8 @@ typedef struct {
 /* values the EVPFFT/PF solve does not need but the namelist carries */
 static int s_ntype[2], s_printctl[2], s_texflag, s_nuclr, s_celldim_pf[3], s_randseed;
 static double s_el1[4], s_el2[4];
+/* dislocation-density block (src/io.c:47-68): per-phase pairs, phase 1 kept */
+static double s_a0[2], s_qslip[2], s_qbulk[2], s_cc[8][2], s_inter[6][2];
 
 mth_status mth_read_namelist(const char* path, mth_params* p, char* slip1, char* slip2, char* ms, size_t cap) {
   if (!path || !p) return MTH_ERR_ARG;
@@ -66,6 +68,27 @@ mth_status mth_read_namelist(const char* path, mth_params* p, char* slip1, char*
       {"Scale_Fdeform", K_R, 1, &p->stored_energy_scale, 0},
       {"pf_length_scale", K_R, 1, &p->pf_length_scale, 0},
       {"pf_time_step", K_R, 1, &p->pf_time_step, 0},
+      {"a0", K_R, 2, s_a0, 0},
+      {"L0", K_R, 1, &p->dd_L0, 0},
+      {"T__K", K_R, 1, &p->dd_T, 0},
+      {"Q_slip", K_R, 2, s_qslip, 0},
+      {"Q_bulk", K_R, 2, s_qbulk, 0},
+      {"C_1", K_R, 2, s_cc[0], 0},
+      {"C_2", K_R, 2, s_cc[1], 0},
+      {"C_3", K_R, 2, s_cc[2], 0},
+      {"C_4", K_R, 2, s_cc[3], 0},
+      {"C_5", K_R, 2, s_cc[4], 0},
+      {"C_6", K_R, 2, s_cc[5], 0},
+      {"C_7", K_R, 2, s_cc[6], 0},
+      {"C_8", K_R, 2, s_cc[7], 0},
+      {"Selfinter", K_R, 2, s_inter[0], 0},
+      {"Coplanar", K_R, 2, s_inter[1], 0},
+      {"CrossSlip", K_R, 2, s_inter[2], 0},
+      {"GlissileJunction", K_R, 2, s_inter[3], 0},
+      {"HirthLock", K_R, 2, s_inter[4], 0},
+      {"LomerCottrellLock", K_R, 2, s_inter[5], 0},
+      {"rho_SSD_initial", K_R, 1, &p->dd_rho_ssd0, 0},
+      {"D_0", K_R, 1, &p->dd_d0, 0},
   };
   const int nk = (int)(sizeof(keys) / sizeof(keys[0]));
   char buff[200];
@@ -97,6 +120,12 @@ mth_status mth_read_namelist(const char* path, mth_params* p, char* slip1, char*
   p->nucleus_radius = s_nuclr;
   if (s_randseed) p->seed = (uint64_t)s_randseed;
   for (int i = 0; i < 3; i++) p->pf_cell_dim[i] = s_celldim_pf[i];
+  p->dd_a0 = s_a0[0];
+  p->dd_q_slip = s_qslip[0];
+  p->dd_q_bulk = s_qbulk[0];
+  for (int k = 0; k < 8; k++) p->dd_c[k] = s_cc[k][0];
+  for (int k = 0; k < 6; k++) p->dd_chi[k] = s_inter[k][0];
+  p->dd_nu = s_el1[3];
   if (slip1 && cap) { strncpy(slip1, sx1, cap - 1); slip1[cap - 1] = 0; }
   if (slip2 && cap) { strncpy(slip2, sx2, cap - 1); slip2[cap - 1] = 0; }
   if (ms && cap) { strncpy(ms, msf, cap - 1); ms[cap - 1] = 0; }

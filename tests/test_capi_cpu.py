@@ -122,3 +122,21 @@ def test_batch_argument_checks(lib):
 def test_iout_argument_checks(lib):
     assert lib.mth_write_iout(None, 0, b"x", 0) == 1
     assert lib.mth_iout_wait(None) == 1
+
+
+def test_namelist_dislocation_density_block(lib, tmp_path):
+    """The DD keys of the namelist (a0, L0, T__K, Q_slip, Q_bulk, C_1..C_8,
+    the six junction strengths, rho_SSD_initial, D_0, the Poisson ratio of
+    ElastConst_PhaseI) land in mth_params as params_from_config puts them."""
+    cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=3, seed=5,
+                       dd=synth.DD(T=293.0, q_slip=0.31, c=(0.5, 3.1, 2.9, 810.0, 15.0, 1000.0, 1.2e-8, 0.3),
+                                   chi=(0.12, 0.13, 0.7, 0.11, 0.06, 0.2), rho_ssd0=0.07, nu=0.34))
+    synth.write_case(str(tmp_path), cfg)
+    par = capi.MthParams()
+    capi.check(lib, lib.mth_read_namelist(str(tmp_path / "input.in").encode(), C.byref(par), None, None, None, 0))
+    ref = capi.params_from_config(cfg)
+    for k in ("dd_a0", "dd_L0", "dd_T", "dd_q_slip", "dd_q_bulk", "dd_rho_ssd0", "dd_d0", "dd_nu"):
+        assert getattr(par, k) == getattr(ref, k), k
+    assert list(par.dd_c) == list(ref.dd_c)
+    assert list(par.dd_chi) == list(ref.dd_chi)
+    assert ref.flow_law == 1 and par.flow_law == 0   # the law is chosen by the caller (forge --dd)

@@ -142,7 +142,7 @@ def test_torch_autograd_wrapper():
     with torch.no_grad():
         step = -1e-3 * theta.abs() * torch.sign(g)
         J_new = Misfit.apply(theta + step, cfg, prec, tgt)
-    assert float(J_new) < float(J)
+    assert float(J_new.detach()) < float(J.detach())
 
 
 def test_adjoint_rejects_unsupported_setups():
