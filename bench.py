@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration measurement")
+    ap.add_argument("--no-dd", action="store_true", help="skip the dislocation-density law measurement")
     return ap.parse_args()
 
 
@@ -324,10 +325,44 @@ def run_gpu(args):
         out["cpu_baseline"] = cpu_sample(cfg)
     if not args.no_adjoint and args.workload == "c1":
         out["adjoint"] = adjoint_measure(dev_index)
+    if not args.no_dd and args.workload == "c1":
+        out["dislocation_density"] = dd_measure(dev_index, args)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------- dislocation-density law
+def dd_measure(dev_index, args):
+    """The same 128^3 workload with the reference's shipped dislocation-density
+    law instead of the power law + Voce (flow_law = 1, mixed precision):
+    voxel-iterations/s over the timed steps, with the per-step density
+    update (SSD/GND evolution and averages) inside the timed region."""
+    import dataclasses
+    import torch
+    from mth import Solver, capi, synth
+    cfg = dataclasses.replace(synth.workload("c1"), dd=synth.DD())
+    par = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
+    par.device = dev_index
+    nv = int(np.prod(cfg.cell_dim))
+    with Solver(par, *synth.microstructure(cfg)) as s:
+        for _ in range(2):
+            s.step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its = 0
+        reps = []
+        for _ in range(max(2, args.steps // 2)):
+            r = s.step()
+            its += r["iterations"]
+            reps.append(r)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    return {"workload": "128x128x128 RVE, 512 grains, 40 radius-3 pores, dislocation-density law (sinh slip, "
+                        "SSD + first-order GND evolution), tension eps33_dot=1/s, dt=0.001, IterMax=100, mixed",
+            "value": nv * its / dt, "unit": UNIT, "ms_per_step": dt * 1e3 / len(reps), "green_iterations": its,
+            "dd_avg_last_step": [float(x) for x in reps[-1]["dd_avg"]]}
 
 
 # ------------------------------------------------------ calibration adjoint

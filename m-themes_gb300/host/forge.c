@@ -11,9 +11,11 @@
  * block at src/evolution.c:1633-1648 writes the same two every 500 steps),
  * in the background while the next steps run.
  *
- * Usage: forge input.in [--mixed] [--iout-every K] [--dd]
+ * Usage: forge input.in [--mixed] [--iout-every K] [--dd | --dd-cu]
  * --dd runs the dislocation-density law (the reference's DD_BASED_FLAG build)
- * with the namelist's DD block and writes dd.out.
+ * with the namelist's DD block and writes dd.out; --dd-cu also applies the
+ * DD_CU switch of the shipped flags (fixed Cu elastic constants), which is
+ * what the reference's test_run/ is run with.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -22,7 +24,7 @@
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    fprintf(stderr, "usage: %s input.in [--mixed] [--iout-every K] [--dd]\n", argv[0]);
+    fprintf(stderr, "usage: %s input.in [--mixed] [--iout-every K] [--dd | --dd-cu]\n", argv[0]);
     return 2;
   }
   mth_params p;
@@ -37,6 +39,7 @@ int main(int argc, char** argv) {
     if (!strcmp(argv[i], "--mixed")) p.precision = MTH_MIXED;
     else if (!strcmp(argv[i], "--iout-every") && i + 1 < argc) iout_every = atoi(argv[++i]);
     else if (!strcmp(argv[i], "--dd")) p.flow_law = 1;
+    else if (!strcmp(argv[i], "--dd-cu")) p.flow_law = 2;   /* resolved after the .sx files are read */
   }
   if (p.n_phases >= 1 && p.phase[0].type == 0 && mth_read_sx(sx1, &p, 0) != MTH_OK) {
     fprintf(stderr, "cannot read %s\n", sx1);
@@ -45,6 +48,14 @@ int main(int argc, char** argv) {
   if (p.n_phases == 2 && p.phase[1].type == 0 && mth_read_sx(sx2, &p, 1) != MTH_OK) {
     fprintf(stderr, "cannot read %s\n", sx2);
     return 1;
+  }
+  if (p.flow_law == 2) {
+    /* the DD_CU switch of the reference's shipped flags: fixed Cu elastic
+       constants replace input.in's (src/init.c:821-825) */
+    p.flow_law = 1;
+    p.phase[0].c11 = 241.1674 * 1000;
+    p.phase[0].c12 = 89.1989 * 1000;
+    p.phase[0].c44 = 151.9685 * 1000;
   }
   size_t nv = (size_t)p.cell_dim[0] * p.cell_dim[1] * p.cell_dim[2];
   int* grain = (int*)malloc(sizeof(int) * nv);

@@ -35,8 +35,13 @@ $CXX "${COMMON[@]}" -c "$HERE/refshim/refshim.cc" -o "$OUT/obj/refshim.o" &
 # the shipped dislocation-density path: evolution.c with only the trace hooks
 $CXX -x c++ "${COMMON[@]}" -DAvgDislocation=mth_ref_dd_after_step -DVonMises=mth_ref_VonMises \
   -c "$REF/src/evolution.c" -o "$OUT/obj/evolution_dd.o" &
+# and with DD_CU as src/evpFlags.h ships it (fixed Cu elastic constants,
+# src/init.c:821-825), for runs on the unmodified test_run/ inputs
+$CXX -x c++ "${COMMON[@]}" -DDD_CU -c "$REF/src/init.c" -o "$OUT/obj/init_ddcu.o" &
 wait
 $CXX -o "$OUT/forge_ref" "${OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
 DD_OBJS=("${OBJS[@]/evolution.o/evolution_dd.o}")
 $CXX -o "$OUT/forge_ref_dd" "${DD_OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
-echo "built $OUT/forge_ref $OUT/forge_ref_dd"
+DDCU_OBJS=("${DD_OBJS[@]/init.o/init_ddcu.o}")
+$CXX -o "$OUT/forge_ref_dd_cu" "${DDCU_OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
+echo "built $OUT/forge_ref $OUT/forge_ref_dd $OUT/forge_ref_dd_cu"

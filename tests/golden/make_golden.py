@@ -111,6 +111,48 @@ def main_dd():
         print(name, trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
 
 
+# The elastic constants that the DD_CU switch of the shipped flags writes over
+# input.in's (src/init.c:821-825), MPa.
+DD_CU_ELASTIC = (241.1674 * 1000, 89.1989 * 1000, 151.9685 * 1000)
+
+
+def main_test_run():
+    """The reference's own test_run/ inputs, unmodified, through the build with
+    the shipped flags (DD law, DD_CU).  That build stops with a segmentation
+    fault during the second mechanical step of this input; the first step's
+    trace is kept, with the parameters and microstructure as this project's
+    readers parse them."""
+    import ctypes as C
+    import shutil
+    from mth import capi
+    src = os.path.join(os.environ.get("MTH_REFERENCE", "/root/reference"), "test_run")
+    d = "/tmp/mth_golden_test_run"
+    shutil.rmtree(d, ignore_errors=True)
+    shutil.copytree(src, d)
+    for f in os.listdir(d):
+        os.chmod(os.path.join(d, f), 0o644)
+    ref = os.path.join(REPO, "oracle", "_ref", "forge_ref_dd_cu")
+    env = dict(os.environ, MTH_REF_TRACE=os.path.join(d, "trace.txt"), MTH_REF_SEED="1")
+    subprocess.run(["bash", "-c", f"ulimit -s unlimited; {ref} input.in > ref.log 2>&1"], cwd=d, env=env)
+    trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))[:1]
+    lib = capi.load()
+    par = capi.MthParams()
+    s1, s2, ms = C.create_string_buffer(256), C.create_string_buffer(256), C.create_string_buffer(256)
+    capi.check(lib, lib.mth_read_namelist(os.path.join(d, "input.in").encode(), C.byref(par), s1, s2, ms, 256))
+    capi.check(lib, lib.mth_read_sx(os.path.join(d, s1.value.decode()).encode(), C.byref(par), 0))
+    nv = int(np.prod(list(par.cell_dim)))
+    g = np.zeros(nv, np.int32)
+    ph = np.zeros(nv, np.int32)
+    e = np.zeros(3 * nv)
+    capi.check(lib, lib.mth_read_microstructure(os.path.join(d, ms.value.decode()).encode(), par.cell_dim,
+                                                capi._iptr(g), capi._iptr(ph), capi._dptr(e)))
+    out = os.path.join(HERE, "tr_dd_step0.npz")
+    np.savez_compressed(out, params=np.frombuffer(bytes(par), dtype=np.uint8), dd_cu=np.array(DD_CU_ELASTIC),
+                        grain=g, phase=ph, euler=e.reshape(nv, 3), trace=trace)
+    print("test_run step 0: iterations", int(trace[0, 1]), "->", os.path.relpath(out, REPO))
+
+
 if __name__ == "__main__":
     main()
     main_dd()
+    main_test_run()

@@ -93,3 +93,26 @@ def test_dd_rejected_setups():
     with Solver(capi.params_from_config(plain), *synth.microstructure(plain)) as s:
         with pytest.raises(MthError, match="STATE"):
             s.field("rho_ssd")
+
+
+def test_reference_test_run_unmodified():
+    """The reference's own test_run/ inputs (32^3 single crystal with a pore,
+    the shipped DD parameters, DD_CU elastic constants, Err 5e-5), parsed by
+    this project's readers, against the reference's first step."""
+    import ctypes as C
+    from helpers import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "tr_dd_step0.npz"))
+    par = capi.MthParams.from_buffer_copy(z["params"].tobytes())
+    par.phase[0].c11, par.phase[0].c12, par.phase[0].c44 = (float(x) for x in z["dd_cu"])
+    par.flow_law = 1
+    par.precision = capi.MTH_FP64
+    par.device = 0
+    row = z["trace"][0]
+    with Solver(par, z["grain"], z["phase"], z["euler"]) as s:
+        r = s.step()
+    assert abs(r["iterations"] - int(row[T_ITER])) <= 2, (r["iterations"], row[T_ITER])
+    assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-6
+    assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-6
+    ref = row[T_DD]
+    for j in range(7):
+        assert abs(r["dd_avg"][j] - ref[j]) <= 1e-6 * abs(ref[j]), (j, r["dd_avg"], ref)
