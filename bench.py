@@ -396,14 +396,22 @@ def adjoint_measure(dev_index, name="c4"):
         fwd_ms = (time.perf_counter() - t0) * 1e3
     with Solver(params(cfg), *micro) as s:
         J, g, s33, info = s.adjoint(target, checkpoint_every=10)
+    with Solver(params(cfg), *micro) as s:   # again with per-kernel events, for the breakdown only
+        s.profile(enable=True)
+        s.adjoint(target, checkpoint_every=10)
+        prof, launches = s.profile()
     grad_ms = info["forward_ms"] + info["reverse_ms"]
+    classes = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                   "gbs": (v["bytes"] / (v["ms"] * 1e-3) / 1e9) if v["ms"] > 0 else None}
+               for k, v in prof.items() if v["launches"]}
     return {"workload": "64x64x64 RVE, 256 grains, tension eps33_dot=1/s, 50 steps of 1e-3, mixed precision, "
                         "misfit of <sigma_33> against the curve of (tau0, thet0, tau1, n) = (18, 280, 160, 12)",
             "forward_ms": fwd_ms, "green_iterations": its, "gradient_ms": grad_ms,
             "gradient_over_forward": grad_ms / fwd_ms, "reverse_over_forward": info["reverse_ms"] / fwd_ms,
             "checkpoint_every": 10, "recomputed_steps": info["recomputed_steps"],
             "cg_iterations": info["cg_iterations"], "cg_iterations_max_step": info["cg_iterations_max"],
-            "misfit": J, "grad": dict(zip(capi.ADJOINT_PARAMS, g.tolist()))}
+            "misfit": J, "grad": dict(zip(capi.ADJOINT_PARAMS, g.tolist())),
+            "kernels_during_gradient": classes, "gpu_launches_during_gradient": launches}
 
 
 # ------------------------------------------------------------ CPU (oracle)
@@ -531,6 +539,12 @@ def main():
         run_reference(args)
     elif args.workload in ("c3", "c3s"):
         run_batch(args)
+    elif args.workload == "c4":
+        # the calibration gradient alone (the adjoint block of the default line)
+        print(json.dumps({"workload": "c4", "adjoint": adjoint_measure(0)}), flush=True)
+    elif args.workload == "c1dd":
+        # the dislocation-density law alone (the dislocation_density block of the default line)
+        print(json.dumps({"workload": "c1dd", "dislocation_density": dd_measure(0, args)}), flush=True)
     else:
         run_gpu(args)
 
