@@ -530,6 +530,13 @@ static void dd_constants(const mth_params& p, const PhaseConst& ph, DdConst& dc)
       dc.sg1[i][j] = fabs(sqrt(fabs(1.0 - dc.cg1[i][j] * dc.cg1[i][j])));
       dc.cg3[i][j] = fabs(dot3(ni, nj));
       dc.sg3[i][j] = fabs(sqrt(fabs(1.0 - dc.cg3[i][j] * dc.cg3[i][j])));
+      dc.chif[i][j] = (float)dc.chi[i][j];
+      dc.csf[i][j] = (float)dc.cs[i][j];
+      dc.ssf[i][j] = (float)dc.ss[i][j];
+      dc.cg1f[i][j] = (float)dc.cg1[i][j];
+      dc.sg1f[i][j] = (float)dc.sg1[i][j];
+      dc.cg3f[i][j] = (float)dc.cg3[i][j];
+      dc.sg3f[i][j] = (float)dc.sg3[i][j];
     }
 }
 

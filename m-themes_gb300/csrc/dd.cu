@@ -12,7 +12,8 @@
 // differs from the current one only at the first evaluation of a step; the
 // converged stress is the same.)
 //
-// All arithmetic in FP64; the densities are stored in the field precision.
+// Arithmetic in FP64 except the forest/parallel sums, which run in the field
+// precision (FP32 in the mixed modes); the densities are stored in it too.
 #include <cstdio>
 #include "mth_common.cuh"
 #include "mth_internal.h"
@@ -47,25 +48,30 @@ __device__ __forceinline__ void dd_block_sum(double (&v)[W], double* out) {
 }
 
 // forest and parallel densities of every system of voxel v (from the
-// densities at the start of the step)
+// densities at the start of the step), summed in the field precision T
+// (the 12 x 12 sums are the bulk of the density kernels' arithmetic)
 template <typename T>
 __device__ __forceinline__ void forest_parallel(const DdConst& dc, const DdFields<T>& d, long long P, long long v,
                                                 double* rf, double* rp) {
-  double s[NSYS], a1[NSYS], a2[NSYS], a3[NSYS];
+  T s[NSYS], a1[NSYS], a2[NSYS], a3[NSYS];
   for (int j = 0; j < NSYS; j++) {
-    s[j] = (double)d.rho_s[j * P + v];
-    a1[j] = fabs((double)d.g1[j * P + v]);
-    a2[j] = fabs((double)d.g2[j * P + v]);
-    a3[j] = fabs((double)d.g3[j * P + v]);
+    s[j] = d.rho_s[j * P + v];
+    a1[j] = fabs(d.g1[j * P + v]);
+    a2[j] = fabs(d.g2[j * P + v]);
+    a3[j] = fabs(d.g3[j * P + v]);
   }
   for (int i = 0; i < dc.nsys; i++) {
-    double f = 0.0, p = 0.0;
+    T f = 0, p = 0;
     for (int j = 0; j < dc.nsys; j++) {
-      f += dc.chi[i][j] * (s[j] * dc.cs[i][j] + a1[j] * dc.cg1[i][j] + a2[j] * dc.cs[i][j] + a3[j] * dc.cg3[i][j]);
-      p += dc.chi[i][j] * (s[j] * dc.ss[i][j] + a1[j] * dc.sg1[i][j] + a2[j] * dc.ss[i][j] + a3[j] * dc.sg3[i][j]);
+      const T chi = cpick<T>(dc.chi[i][j], dc.chif[i][j]), cs = cpick<T>(dc.cs[i][j], dc.csf[i][j]);
+      const T ss = cpick<T>(dc.ss[i][j], dc.ssf[i][j]);
+      f += chi * (s[j] * cs + a1[j] * cpick<T>(dc.cg1[i][j], dc.cg1f[i][j]) + a2[j] * cs +
+                  a3[j] * cpick<T>(dc.cg3[i][j], dc.cg3f[i][j]));
+      p += chi * (s[j] * ss + a1[j] * cpick<T>(dc.sg1[i][j], dc.sg1f[i][j]) + a2[j] * ss +
+                  a3[j] * cpick<T>(dc.sg3[i][j], dc.sg3f[i][j]));
     }
-    rf[i] = f;
-    rp[i] = p;
+    rf[i] = (double)f;
+    rp[i] = (double)p;
   }
 }
 

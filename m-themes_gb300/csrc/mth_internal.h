@@ -203,6 +203,9 @@ struct DdConst {
   double chi[NSYS][NSYS], cs[NSYS][NSYS], ss[NSYS][NSYS], cg1[NSYS][NSYS], sg1[NSYS][NSYS], cg3[NSYS][NSYS],
       sg3[NSYS][NSYS];
   double m_xt[NSYS][5], bp[NSYS][3], bb[NSYS][3];
+  // float copies of the projection tables for the FP32 forest/parallel sums
+  float chif[NSYS][NSYS], csf[NSYS][NSYS], ssf[NSYS][NSYS], cg1f[NSYS][NSYS], sg1f[NSYS][NSYS], cg3f[NSYS][NSYS],
+      sg3f[NSYS][NSYS];
 };
 // Per-voxel state, 12 planes each (voxel index fastest).
 template <typename T>

@@ -721,7 +721,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     // mixed modes (no FP32-solve variants)
     if (mixed) {
       const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-      newton_kernel<float, float, double, 1, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+      newton_kernel<float, float, double, 2, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
     } else {
       const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
       newton_kernel<double, double, double, 1, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
