@@ -588,6 +588,7 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     }
   }
   c->nc.dt = p->time_step;
+  c->nc.ph1_only = (p->n_phases == 1 || c->nc.ph[1].type != 0) ? 1 : 0;
   c->nc.tol = p->newton_tol > 0 ? p->newton_tol : (c->mixed ? 1e-6 : 1e-10);
   c->nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
   // boundary conditions (src/init.c:861-900)

@@ -53,6 +53,8 @@ struct NewtonConst {
   double tol;
   int itmax;
   int flow_off;         // 1: Schmid tensors zero (Update_Flag=0 at istep 0)
+  int ph1_only;         // 1: no crystal phase but phase 1 (sigma is 0 elsewhere), so the
+                        // phase-1 stress sums equal the total ones
   // float copies (fill_float_consts)
   float s0devf[25];
   float s0hhf, dtf, tolf;

@@ -618,6 +618,45 @@ __device__ __forceinline__ void block_reduce_smem(const TV (&v)[W], double* out)
   }
 }
 
+// Block sums of the Newton kernel's NPART values, as block_reduce_smem, with
+// two exact savings: when ph1_only the phase-1 stress sums (components
+// 8..13) are the total ones (2..7), added once and written twice; the
+// Newton-iteration and failure counts (14, 15: small integers) are summed in
+// the staging precision, exact below 2^24.
+template <typename TV>
+__device__ __forceinline__ void newton_block_reduce(const TV (&v)[NPART], double* out, bool ph1_only) {
+  constexpr int NT = 256, LD = NT + 16;
+  __shared__ TV sv[NPART][LD];
+  __shared__ double sp[NPART][16];
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < NPART; i++)
+    if (!ph1_only || i < 8 || i >= 14) sv[i][t] = v[i];
+  __syncthreads();
+  {
+    const int comp = t >> 4, chunk = t & 15;
+    if (comp >= 14) {
+      TV a = 0;
+#pragma unroll
+      for (int k = 0; k < NT / 16; k++) a += sv[comp][k * 16 + chunk];
+      sp[comp][chunk] = (double)a;
+    } else if (!ph1_only || comp < 8) {
+      double a = 0.0;
+#pragma unroll
+      for (int k = 0; k < NT / 16; k++) a += (double)sv[comp][k * 16 + chunk];
+      sp[comp][chunk] = a;
+    }
+  }
+  __syncthreads();
+  if (t < NPART) {
+    const int src = (ph1_only && t >= 8 && t < 14) ? t - 6 : t;
+    double a = 0.0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) a += sp[src][k];
+    out[(size_t)blockIdx.x * NPART + t] = a;
+  }
+}
+
 // Loads of a global value that the compiler keeps as separate loads (used to
 // re-read a voxel's inputs after the Newton loop instead of holding them).
 __device__ __forceinline__ float ld_again(const float* p) {
@@ -684,7 +723,7 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
       }
     }
   }
-  block_reduce_smem<TF, NPART>(acc, partials);
+  newton_block_reduce<TF>(acc, partials, nc.ph1_only != 0);
 }
 
 void fill_float_consts(NewtonConst& nc) {
