@@ -772,10 +772,10 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     newton_kernel<float, float, float, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed == 3) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double, 2, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    newton_kernel<float, float, double, 3, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double, 2><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    newton_kernel<float, float, double, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
     newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
