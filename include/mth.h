@@ -190,7 +190,8 @@ mth_status mth_destroy(mth_ctx* ctx);
  *   crss [n*12] forward CRSS per system (backward = forward + (tau0b-tau0f))
  *   edot [n*6]  out: plastic strain rate
  *   err [n*2]   out: |sig-lambda|, |eps_tot-strain| (src/evolution.c:291-299)
- * c066 is the 6x6 reference stiffness.  Phase 1 parameters come from params. */
+ * c066 is the 6x6 reference stiffness.  Phase 1 parameters come from params;
+ * power law only (flow_law = 1 returns MTH_ERR_UNSUPPORTED). */
 mth_status mth_local_solve(const mth_params* params, const double c066[36], size_t n,
                            double* sig, const double* eps_p, const double* strain,
                            const double* rot, const double* crss, double* edot,

@@ -8,28 +8,11 @@
 // updates (src/evolution.c:1471-1535,1691-1693) run on the host in FP64 on
 // the reduced sums that the kernels produce; everything per voxel or per
 // wave vector runs on the GPU.
-#include <cmath>
-#include <cstdarg>
-#include <cstdio>
-#include <cstdlib>
-#include <cstring>
-#include <algorithm>
-#include <chrono>
-#include <map>
-#include <string>
-#include <thread>
-#include <tuple>
-#include <vector>
-#include "../../include/mth.h"
-#include "mth_common.cuh"
-#include "mth_internal.h"
-#include "adjoint.h"
-
-using namespace mth;
+#include "capi_internal.h"
 
 static thread_local char g_err[512] = "";
 
-static mth_status set_err(mth_status s, const char* fmt, ...) {
+mth_status set_err(mth_status s, const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(g_err, sizeof(g_err), fmt, ap);
@@ -37,20 +20,12 @@ static mth_status set_err(mth_status s, const char* fmt, ...) {
   return s;
 }
 
-#define CK(call)                                                                              \
-  do {                                                                                        \
-    cudaError_t e_ = (call);                                                                  \
-    if (e_ != cudaSuccess)                                                                    \
-      return set_err(MTH_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                     __FILE__, __LINE__);                                                     \
-  } while (0)
 
 extern "C" const char* mth_version(void) { return "mth-gb300 0.1 (sm_103a)"; }
 extern "C" const char* mth_last_error(void) { return g_err; }
 
 // ------------------------------------------------------------ host math
-namespace {
-typedef double t33[3][3];
+namespace capi_host {
 
 const double Bh[6][3][3] = {
     {{-RSQ2, 0, 0}, {0, RSQ2, 0}, {0, 0, 0}},
@@ -182,10 +157,10 @@ mth_status fill_phase(const mth_phase& in, PhaseConst& ph) {
     for (int j = 0; j < ph.nsys; j++) ph.hard[i][j] = (i == j) ? in.hself : in.hlat;
   return MTH_OK;
 }
-}  // namespace
+}  // namespace capi_host
 
 
-namespace {
+namespace capi_host {
 int pkh(int i, int j) {
   if (i > j) { int t = i; i = j; j = t; }
   return i * 5 - (i * (i - 1)) / 2 + (j - i);
@@ -232,7 +207,7 @@ void class_row_add_s0(double* row, const double s066[6][6]) {
   for (int i = 0; i < 5; i++)
     for (int j = i; j < 5; j++) row[ET_STOT + pkh(i, j)] = s066[i][j] + row[ET_SEL + pkh(i, j)];
 }
-}  // namespace
+}  // namespace capi_host
 
 bool mth::make_plan(int n, FftPlan* p) {
   p->n = n;
@@ -245,111 +220,8 @@ bool mth::make_plan(int n, FftPlan* p) {
 }
 
 // ---------------------------------------------------------------- context
-constexpr long long MAX_CANDIDATES = 1LL << 20;   // nucleation candidates collected per step
-constexpr int MAX_NUCLEI = 65536;                 // nuclei kept per step (first in voxel order)
 
-struct mth_ctx {
-  mth_params p;
-  int mixed;
-  int n[3];
-  long long nv;
-  FftGeom geom;
-  NewtonConst nc;
-  GreenConst gc;
-  cudaStream_t st;
-  int nblocks;
-  // device memory
-  void* fieldmem;
-  Fields<float> ff;
-  Fields<double> fd;
-  void* spec;
-  void* anti;
-  TmaMaps* tma;       // tensor maps of the TMA passes (null members: shared-memory passes)
-  int* err_d;         // raised by a timed-out wait in a kernel
-  int* err_h;         // pinned copy
-  double* add_d;      // uniform strain increment of the current Green iteration (6, device)
-  double* add_h;      // pinned staging of add_d
-  int* live_d;        // live flag read by the iteration kernels (1 outside a batch)
-  bool in_batch;      // red, err_d, add_d, live_d and the stream belong to a batch
-  bool tma_off;       // shared-memory passes even where tensor maps exist (tuning)
-  struct IoutWriter* iout;   // background writer of per-step field files
-  double* dl_d;       // download staging in the host layout
-  size_t dl_cap;      // doubles
-  // state of the mechanical step in progress (mth_step and the batch driver)
-  int it_iter, it_nnew;
-  long long it_nit, it_nbad;
-  uint8_t* phase_d;
-  int* grain_d;
-  int* eclass_d;
-  double* etab_d;
-  float* etabf_d;      // float copy of the class table for the FP32 paths
-  int nclass;
-  double* partials;
-  double* red;
-  double* red_h;  // pinned
-  void* tw[3][2]; // per axis, forward/inverse
-  // profiling
-  int prof_on;
-  double prof_ms[MTH_PROF_MAX];
-  double prof_bytes[MTH_PROF_MAX];
-  long long prof_launch[MTH_PROF_MAX];
-  std::vector<cudaEvent_t>* ev_pool;
-  std::vector<int>* ev_pending;   // class of each pending pair (events 2i, 2i+1)
-  // macro state (FP64, host)
-  t33 udot, udot_s, udot_a, scauchy;
-  int vbc[6], sbc[6], creep;
-  t33 disgrad_avg, disgrad_avg_t, ddg, ddg_acum, ddg_applied, sig_avg, sig_avg1;
-  double c066[6][6], s066[6][6], s0_4[81];
-  double wgt, wgt_ph1, e_vm, d_vm, s_vm, s_vm1, err_e, err_s, time_tot;
-  int istep;
-  int uploaded;
-  // dynamic recrystallisation
-  int drx;
-  int first_drx_id, next_grain_id;
-  std::vector<double>* etab_h;       // host copy of the elastic-class table
-  std::vector<double>* drx_rot_h;    // 9 per recrystallised grain
-  std::vector<int>* drx_class_h;
-  double* drx_rot_d;
-  int* drx_class_d;
-  size_t drx_cap;
-  PfBuffers<float> pff;
-  PfBuffers<double> pfd;
-  PfCoef pfc;
-  double* rho_d;
-  void* rho_t;
-  int* grain_prev_d;
-  int* winner_d;
-  long long* sites_d;
-  unsigned long long* count_d;
-  uint8_t* crystal_d;
-  unsigned long long* hist_d;
-  double* gather_d;
-  // phase field on a grid of its own (CellDim_pf != CellDim)
-  bool pf_resample;
-  int npf[3];
-  long long nvpf;
-  int* grain_pf_d;      // grain ids carried to the PF grid
-  double* rho_pf_d;     // rho on the PF grid (FP64)
-  void* rho_pf_t;       // rho on the PF grid in the PF precision
-  int* gid_coarse_d;    // relaxed ids carried back to the mechanical grid
-  size_t hist_cap;
-  double tau0f;
-  int nsys;
-  int adj_solid;        // every voxel is of phase 1 and crystalline (adjoint precondition)
-  double last_au[3];    // uniform spin increment of the last end of step
-  // dislocation-density law
-  int dd;
-  DdConst* ddc_d;       // device copy of the phase-1 constants
-  void* dd_mem;         // 84 state planes + 36 per-step constant planes
-  DdFields<float> ddf;
-  DdFields<double> ddd;
-  uint8_t* gb_d;        // same-grain neighbour flags per voxel
-  double dd_avg[NPART_DD];
-};
-
-static void iout_free(IoutWriter* w);
-
-static void ctx_free(mth_ctx* c) {
+void ctx_free(mth_ctx* c) {
   if (!c) return;
   iout_free(c->iout);
   cudaFree(c->fieldmem);
@@ -413,13 +285,11 @@ static void ctx_free(mth_ctx* c) {
 }
 
 // ------------------------------------------------------------- profiling
-enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_DRX,
-       K_PF, K_ADJ_LOCAL, K_ADJ_CG, K_DD, K_NCLASS };
 static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain", "newton",
                                         "reduce", "end_step", "spin_fft", "setup", "drx",
                                         "pf_relax", "adj_local", "adj_cg", "dislocation_density"};
 
-static void prof_begin(mth_ctx* c) {
+void prof_begin(mth_ctx* c) {
   if (!c->prof_on) return;
   size_t i = c->ev_pending->size();
   if (c->ev_pool->size() < 2 * (i + 1)) {
@@ -431,7 +301,7 @@ static void prof_begin(mth_ctx* c) {
   }
   cudaEventRecord((*c->ev_pool)[2 * i], c->st);
 }
-static void prof_end(mth_ctx* c, int cls, int kernels, double bytes) {
+void prof_end(mth_ctx* c, int cls, int kernels, double bytes) {
   c->prof_launch[cls] += kernels;
   c->prof_bytes[cls] += bytes;
   if (!c->prof_on) return;
@@ -440,7 +310,7 @@ static void prof_end(mth_ctx* c, int cls, int kernels, double bytes) {
   c->ev_pending->push_back(cls);
 }
 // after the stream has been synchronised
-static void prof_resolve(mth_ctx* c) {
+void prof_resolve(mth_ctx* c) {
   if (!c->ev_pending) return;
   for (size_t i = 0; i < c->ev_pending->size(); i++) {
     float ms = 0;
@@ -451,14 +321,6 @@ static void prof_resolve(mth_ctx* c) {
 }
 // one launcher call of class cls issuing `kernels` kernels that move
 // `bytes` algorithmic bytes
-#define LAUNCHN(cls, kernels, bytes, call)         \
-  do {                                             \
-    prof_begin(c);                                 \
-    cudaError_t e__ = (call);                      \
-    prof_end(c, cls, (kernels), (double)(bytes));  \
-    if (e__ != cudaSuccess) CK(e__);               \
-  } while (0)
-#define LAUNCH(cls, bytes, call) LAUNCHN(cls, 1, bytes, call)
 
 template <typename T>
 static mth_status make_twiddles(int n, int sign, void** out) {
@@ -804,7 +666,6 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   return MTH_OK;
 }
 
-#define SETDEV(c) CK(cudaSetDevice((c)->p.device))
 
 extern "C" mth_status mth_destroy(mth_ctx* c) {
   if (!c) return set_err(MTH_ERR_ARG, "null context");
@@ -814,17 +675,17 @@ extern "C" mth_status mth_destroy(mth_ctx* c) {
   return MTH_OK;
 }
 
-static IterIn iter_in(const mth_ctx* c) { return IterIn{c->add_d, c->live_d}; }
+IterIn iter_in(const mth_ctx* c) { return IterIn{c->add_d, c->live_d}; }
 
 // gated: the kernel follows the live flag (inside a batch graph)
-static mth_status launch_reduce(mth_ctx* c, int width, bool gated) {
+mth_status launch_reduce(mth_ctx* c, int width, bool gated) {
   LAUNCH(K_REDUCE, 8.0 * width * (c->nblocks + 1),
          launch_reduce_partials(c->partials, c->nblocks, width, c->red, gated ? iter_in(c) : IterIn{nullptr, nullptr},
                                 c->st));
   return MTH_OK;
 }
 
-static mth_status reduce_to_host(mth_ctx* c, int width, double* out) {
+mth_status reduce_to_host(mth_ctx* c, int width, double* out) {
   mth_status s = launch_reduce(c, width, false);
   if (s) return s;
   CK(cudaMemcpyAsync(c->red_h, c->red, sizeof(double) * width, cudaMemcpyDeviceToHost, c->st));
@@ -1039,7 +900,7 @@ static void get_smacro(mth_ctx* c, const double* red) {
 }
 
 template <typename T>
-static mth_status green_iteration(mth_ctx* c) {
+mth_status green_iteration(mth_ctx* c) {
   const IterIn it = iter_in(c);
   const FftGeom& g = c->geom;
   Fields<T>& f = *reinterpret_cast<Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
@@ -1072,6 +933,9 @@ static mth_status green_iteration(mth_ctx* c) {
          launch_newton(c->mixed, c->nc, &f, c->partials, c->nblocks, it, c->st, c->dd));
   return MTH_OK;
 }
+
+template mth_status green_iteration<float>(mth_ctx* c);
+template mth_status green_iteration<double>(mth_ctx* c);
 
 template <typename T>
 static mth_status spin_field(mth_ctx* c) {
@@ -1255,7 +1119,7 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
 // into add_h) / the iteration kernels / iter_finish (host: error norms and
 // the macroscopic stress update from the reduced partial sums) while
 // iter_more, and step_end (end-of-step updates and the report).
-static mth_status step_begin(mth_ctx* c) {
+mth_status step_begin(mth_ctx* c) {
   c->it_nnew = 0;
   if (c->drx && c->istep > 0) {
     mth_status s = drx_step(c, &c->it_nnew);
@@ -1283,13 +1147,13 @@ static mth_status step_begin(mth_ctx* c) {
   return MTH_OK;
 }
 
-static bool iter_more(const mth_ctx* c) {
+bool iter_more(const mth_ctx* c) {
   return c->it_iter < c->p.iter_max && fmax(fabs(c->err_s), fabs(c->err_e)) > c->p.err;
 }
 
 // uniform strain added this iteration: dDisGradAvg of the previous
 // get_smacro, plus Udot dt on the first one (src/evolution.c:1319-1332)
-static void iter_add(mth_ctx* c) {
+void iter_add(mth_ctx* c) {
   c->it_iter++;
   const double dt = c->p.time_step;
   t33 u;
@@ -1301,7 +1165,7 @@ static void iter_add(mth_ctx* c) {
   t2v(u, c->add_h, 6);
 }
 
-static mth_status iter_finish(mth_ctx* c, const double* red) {
+mth_status iter_finish(mth_ctx* c, const double* red) {
   for (int i = 0; i < NPART; i++)
     if (!std::isfinite(red[i]))
       return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", c->istep,
@@ -1317,7 +1181,7 @@ static mth_status iter_finish(mth_ctx* c, const double* red) {
   return MTH_OK;
 }
 
-static mth_status step_end(mth_ctx* c, mth_step_report* rep) {
+mth_status step_end(mth_ctx* c, mth_step_report* rep) {
   const int istep = c->istep;
   const double dt = c->p.time_step;
   // end of step (src/evolution.c:1471-1546)
@@ -1504,393 +1368,6 @@ extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, si
   return c->mixed ? download<float>(c, field, host) : download<double>(c, field, host);
 }
 
-// ------------------------------------------------------ field files (.iout)
-// The reference's writers (src/io.c:247-541) dump raw native values with
-// MPI-IO, one file per component.  Here the fields are copied device to
-// device at the call (ordered with the context's stream, so the next step
-// cannot overwrite them first); a background thread copies the snapshot to
-// pinned host memory on its own stream, converts and writes the files while
-// the caller goes on stepping.
-struct IoutWriter {
-  std::thread th;
-  int device = 0;
-  cudaStream_t io = nullptr;
-  cudaEvent_t snap = nullptr;
-  void* stage_d = nullptr;
-  size_t stage_cap = 0;
-  void* stage_h = nullptr;
-  size_t host_cap = 0;
-  mth_status status = MTH_OK;
-  char msg[512] = "";
-};
-
-// 48-byte record of WriteTextureMPI (src/io.c:480-487)
-struct TexRecord {
-  double angle[3];
-  int coord[3];
-  int jgr, jph, buff;
-};
-static_assert(sizeof(TexRecord) == 48, "texture record layout");
-
-static void iout_join(IoutWriter* w) {
-  if (w && w->th.joinable()) w->th.join();
-}
-
-static void iout_free(IoutWriter* w) {
-  if (!w) return;
-  iout_join(w);
-  cudaSetDevice(w->device);
-  cudaFree(w->stage_d);
-  if (w->stage_h) cudaFreeHost(w->stage_h);
-  if (w->snap) cudaEventDestroy(w->snap);
-  if (w->io) cudaStreamDestroy(w->io);
-  delete w;
-}
-
-// matrix -> Bunge angles in degrees, EulerToTransMatrix opt 1
-// (src/kinematics.c:186-215); a = sample->crystal matrix
-static void rot_to_bunge(const double a[3][3], double out[3]) {
-  const double pi = 3.14159265358979323846;
-  double t1, ph, t2;
-  ph = acos(a[2][2]);
-  if (fabs(a[2][2]) > 0.9999) {
-    t2 = 0.;
-    t1 = atan2(a[0][1], a[0][0]);
-  } else {
-    const double sph = sin(ph);
-    t1 = atan2(a[2][0] / sph, -1.0 * a[2][1] / sph);
-    t2 = atan2(a[0][2] / sph, a[1][2] / sph);
-  }
-  out[0] = t1 * 180. / pi;
-  out[1] = ph * 180. / pi;
-  out[2] = t2 * 180. / pi;
-}
-
-static bool write_file(const std::string& name, const void* data, size_t bytes, char* msg) {
-  FILE* f = fopen(name.c_str(), "wb");
-  if (!f) { snprintf(msg, 512, "cannot open %s", name.c_str()); return false; }
-  const size_t w = fwrite(data, 1, bytes, f);
-  const bool ok = (w == bytes) && fclose(f) == 0;
-  if (w != bytes) fclose(f);
-  if (!ok) snprintf(msg, 512, "short write to %s", name.c_str());
-  return ok;
-}
-
-template <typename T>
-static void iout_work(IoutWriter* w, int kind, std::string prefix, int step, long long P, int n0, int n1, int n2,
-                      size_t bytes) {
-  w->status = MTH_OK;
-  auto fail = [&](mth_status s, const char* m) {
-    w->status = s;
-    snprintf(w->msg, sizeof(w->msg), "%s", m);
-  };
-  if (cudaSetDevice(w->device) != cudaSuccess || cudaStreamWaitEvent(w->io, w->snap, 0) != cudaSuccess ||
-      cudaMemcpyAsync(w->stage_h, w->stage_d, bytes, cudaMemcpyDeviceToHost, w->io) != cudaSuccess ||
-      cudaStreamSynchronize(w->io) != cudaSuccess)
-    return fail(MTH_ERR_CUDA, "field file copy failed");
-  char sfx[32];
-  snprintf(sfx, sizeof(sfx), "S%06d.iout", step);
-  if (kind == MTH_IOUT_GRAIN) {
-    if (!write_file(prefix + "_" + sfx, w->stage_h, sizeof(int) * P, w->msg)) w->status = MTH_ERR_IO;
-    return;
-  }
-  if (kind == MTH_IOUT_TEXTURE) {
-    const T* rot = static_cast<const T*>(w->stage_h);
-    const int* grain = reinterpret_cast<const int*>(rot + 9 * P);
-    const uint8_t* phase = reinterpret_cast<const uint8_t*>(grain + P);
-    std::vector<TexRecord> rec(P);
-    for (long long v = 0; v < P; v++) {
-      double a[3][3];
-      for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) a[i][j] = (double)rot[(j * 3 + i) * P + v];   // transpose: sample->crystal
-      TexRecord& r = rec[v];
-      rot_to_bunge(a, r.angle);
-      r.coord[0] = (int)(v / ((long long)n1 * n2)) + 1;
-      r.coord[1] = (int)((v / n2) % n1) + 1;
-      r.coord[2] = (int)(v % n2) + 1;
-      r.jgr = grain[v];
-      r.jph = (int)phase[v] + 1;
-      r.buff = 0;
-    }
-    (void)n0;
-    if (!write_file(prefix + "_" + sfx, rec.data(), sizeof(TexRecord) * P, w->msg)) w->status = MTH_ERR_IO;
-    return;
-  }
-  // symmetric tensors: components 11, 22, 33, 23, 13, 12 (src/io.c:404-418)
-  const T* a = static_cast<const T*>(w->stage_h);
-  const T* b = kind == MTH_IOUT_ELS ? a + 6 * P : nullptr;   // ELS: strain - plastic strain
-  static const int ci[6][2] = {{0, 0}, {1, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
-  std::vector<double> comp((size_t)6 * P);
-  for (long long v = 0; v < P; v++) {
-    double s6[6];
-    t33 t;
-    for (int i = 0; i < 6; i++) s6[i] = (double)a[i * P + v] - (b ? (double)b[i * P + v] : 0.0);
-    v2t(s6, t, 6);
-    for (int c = 0; c < 6; c++) comp[c * P + v] = t[ci[c][0]][ci[c][1]];
-  }
-  for (int c = 0; c < 6; c++) {
-    if (!write_file(prefix + "_" + std::to_string(c + 1) + "_" + sfx, comp.data() + c * P, sizeof(double) * P,
-                    w->msg)) {
-      w->status = MTH_ERR_IO;
-      return;
-    }
-  }
-}
-
-template <typename T>
-static mth_status iout_start(mth_ctx* c, int kind, const char* prefix, int step) {
-  const Fields<T>& f = *reinterpret_cast<const Fields<T>*>(c->mixed ? (void*)&c->ff : (void*)&c->fd);
-  const long long P = c->nv;
-  const size_t w = sizeof(T);
-  size_t bytes;
-  switch (kind) {
-    case MTH_IOUT_SIG: case MTH_IOUT_EPS: case MTH_IOUT_EDOT: bytes = 6 * P * w; break;
-    case MTH_IOUT_ELS: bytes = 12 * P * w; break;
-    case MTH_IOUT_GRAIN: bytes = sizeof(int) * P; break;
-    case MTH_IOUT_TEXTURE: bytes = 9 * P * w + sizeof(int) * P + P; break;
-    default: return set_err(MTH_ERR_ARG, "iout kind %d", kind);
-  }
-  if (!c->iout) {
-    c->iout = new IoutWriter();
-    c->iout->device = c->p.device;
-    CK(cudaStreamCreateWithFlags(&c->iout->io, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&c->iout->snap, cudaEventDisableTiming));
-  }
-  IoutWriter* wr = c->iout;
-  iout_join(wr);   // one write in flight: its staging buffers are reused
-  if (wr->stage_cap < bytes) {
-    cudaFree(wr->stage_d);
-    wr->stage_d = nullptr;
-    wr->stage_cap = 0;
-    CK(cudaMalloc(&wr->stage_d, bytes));
-    wr->stage_cap = bytes;
-  }
-  if (wr->host_cap < bytes) {
-    if (wr->stage_h) cudaFreeHost(wr->stage_h);
-    wr->stage_h = nullptr;
-    wr->host_cap = 0;
-    CK(cudaMallocHost(&wr->stage_h, bytes));
-    wr->host_cap = bytes;
-  }
-  char* d = static_cast<char*>(wr->stage_d);
-  auto snap = [&](const void* src, size_t n) -> cudaError_t {
-    cudaError_t e = cudaMemcpyAsync(d, src, n, cudaMemcpyDeviceToDevice, c->st);
-    d += n;
-    return e;
-  };
-  switch (kind) {
-    case MTH_IOUT_SIG: CK(snap(f.sig, 6 * P * w)); break;
-    case MTH_IOUT_EPS: CK(snap(f.epsp, 6 * P * w)); break;
-    case MTH_IOUT_EDOT: CK(snap(f.edot, 6 * P * w)); break;
-    case MTH_IOUT_ELS: CK(snap(f.strain, 6 * P * w)); CK(snap(f.epsp, 6 * P * w)); break;
-    case MTH_IOUT_GRAIN: CK(snap(c->grain_d, sizeof(int) * P)); break;
-    case MTH_IOUT_TEXTURE:
-      CK(snap(f.rot, 9 * P * w));
-      CK(snap(c->grain_d, sizeof(int) * P));
-      CK(snap(c->phase_d, (size_t)P));
-      break;
-  }
-  CK(cudaEventRecord(wr->snap, c->st));
-  wr->th = std::thread(iout_work<T>, wr, kind, std::string(prefix), step, P, c->n[0], c->n[1], c->n[2], bytes);
-  return MTH_OK;
-}
-
-extern "C" mth_status mth_write_iout(mth_ctx* c, int kind, const char* prefix, int step) {
-  if (!c || !prefix) return set_err(MTH_ERR_ARG, "null argument");
-  if (!c->uploaded) return set_err(MTH_ERR_STATE, "no microstructure uploaded");
-  if (kind < MTH_IOUT_SIG || kind > MTH_IOUT_TEXTURE) return set_err(MTH_ERR_ARG, "iout kind %d", kind);
-  SETDEV(c);
-  if (c->iout) {   // report a failure of the previous write before starting the next
-    iout_join(c->iout);
-    if (c->iout->status) {
-      const mth_status s = c->iout->status;
-      c->iout->status = MTH_OK;
-      return set_err(s, "%s", c->iout->msg);
-    }
-  }
-  return c->mixed ? iout_start<float>(c, kind, prefix, step) : iout_start<double>(c, kind, prefix, step);
-}
-
-extern "C" mth_status mth_iout_wait(mth_ctx* c) {
-  if (!c) return set_err(MTH_ERR_ARG, "null context");
-  if (!c->iout) return MTH_OK;
-  iout_join(c->iout);
-  if (c->iout->status) {
-    const mth_status s = c->iout->status;
-    c->iout->status = MTH_OK;
-    return set_err(s, "%s", c->iout->msg);
-  }
-  return MTH_OK;
-}
-
-// ------------------------------------------------------ array-level DRX
-template <typename T>
-static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps,
-                                  int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
-  const long long nv = (long long)n[0] * n[1] * n[2];
-  PfCoef co;
-  const double lgb = p->pf_width_cells * p->pf_length_scale;
-  co.mcoef = p->pf_time_step * 4.0 / 3.0 * p->m_gb / lgb;
-  co.kappa = 3.0 / 4.0 * p->e_gb * lgb / p->pf_length_scale / p->pf_length_scale;
-  co.mwell = 6 * p->e_gb / lgb;
-  co.edisl = p->stored_energy_scale * p->shear_modulus * p->burgers * p->burgers;
-  PfBuffers<T> b;
-  memset(&b, 0, sizeof(b));
-  int* g_d = nullptr;
-  T* r_d = nullptr;
-  std::vector<T> rt(nv);
-  for (long long v = 0; v < nv; v++) rt[v] = (T)rho[v];
-  mth_status st = MTH_OK;
-  cudaStream_t s = nullptr;
-  auto fail = [&](cudaError_t e, const char* what) {
-    st = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-  };
-  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
-    e = cudaMalloc(&b.ids[i], sizeof(int) * PF_K * nv);
-    if (e == cudaSuccess) e = cudaMalloc(&b.phi[i], sizeof(T) * PF_K * nv);
-    if (e == cudaSuccess) e = cudaMalloc(&b.cnt[i], nv);
-  }
-  if (e == cudaSuccess) e = cudaMalloc(&b.gid, sizeof(int) * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_id, sizeof(int) * PF_PATCH * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_sum, sizeof(T) * PF_PATCH * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_cnt, (size_t)PF_PATCH * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_n, (size_t)nv);
-  if (e == cudaSuccess) e = cudaMalloc(&g_d, sizeof(int) * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&r_d, sizeof(T) * nv);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(g_d, grain, sizeof(int) * nv, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(r_d, rt.data(), sizeof(T) * nv, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = launch_pf_relax<T>(n, g_d, r_d, substeps, co, b, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(grain_out, b.gid, sizeof(int) * nv, cudaMemcpyDeviceToHost, s);
-  std::vector<T> ph;
-  std::vector<uint8_t> cn;
-  if (e == cudaSuccess && ids_out) e = cudaMemcpyAsync(ids_out, b.ids[b.cur], sizeof(int) * PF_K * nv, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && phi_out) {
-    ph.resize((size_t)PF_K * nv);
-    e = cudaMemcpyAsync(ph.data(), b.phi[b.cur], sizeof(T) * PF_K * nv, cudaMemcpyDeviceToHost, s);
-  }
-  if (e == cudaSuccess && cnt_out) {
-    cn.resize(nv);
-    e = cudaMemcpyAsync(cn.data(), b.cnt[b.cur], nv, cudaMemcpyDeviceToHost, s);
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) fail(e, "phase-field relaxation");
-  else {
-    if (phi_out)
-      for (size_t i = 0; i < ph.size(); i++) phi_out[i] = (double)ph[i];
-    if (cnt_out)
-      for (long long v = 0; v < nv; v++) cnt_out[v] = cn[v];
-  }
-  for (int i = 0; i < 2; i++) { cudaFree(b.ids[i]); cudaFree(b.phi[i]); cudaFree(b.cnt[i]); }
-  cudaFree(b.gid);
-  cudaFree(b.pl_id);
-  cudaFree(b.pl_sum);
-  cudaFree(b.pl_cnt);
-  cudaFree(b.pl_n);
-  cudaFree(g_d);
-  cudaFree(r_d);
-  if (s) cudaStreamDestroy(s);
-  return st;
-}
-
-extern "C" mth_status mth_pf_relax(const mth_params* p, const int cell_dim[3], const int* grain, const double* rho,
-                                   int substeps, int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
-  if (!p || !cell_dim || !grain || !rho || !grain_out) return set_err(MTH_ERR_ARG, "null argument");
-  for (int i = 0; i < 3; i++)
-    if (cell_dim[i] < 1) return set_err(MTH_ERR_ARG, "cell_dim");
-  if (substeps < 0) return set_err(MTH_ERR_ARG, "substeps");
-  if (!(p->pf_length_scale > 0) || !(p->pf_width_cells > 0)) return set_err(MTH_ERR_ARG, "phase-field parameters");
-  CK(cudaSetDevice(p->device));
-  return p->precision == MTH_FP64 ? pf_relax_arrays<double>(p, cell_dim, grain, rho, substeps, grain_out, ids_out, phi_out, cnt_out)
-                                  : pf_relax_arrays<float>(p, cell_dim, grain, rho, substeps, grain_out, ids_out, phi_out, cnt_out);
-}
-
-extern "C" mth_status mth_nucleate(const mth_params* p, const int cell_dim[3], int* grain, const int* phase,
-                                   const double* rho, long long step, int first_id, long long* sites, long long cap,
-                                   int* n_new) {
-  if (!p || !cell_dim || !grain || !phase || !rho || !n_new) return set_err(MTH_ERR_ARG, "null argument");
-  const long long nv = (long long)cell_dim[0] * cell_dim[1] * cell_dim[2];
-  if (nv <= 0) return set_err(MTH_ERR_ARG, "cell_dim");
-  std::vector<uint8_t> cry(nv);
-  for (long long v = 0; v < nv; v++) {
-    if (phase[v] < 1 || phase[v] > p->n_phases) return set_err(MTH_ERR_ARG, "phase of voxel %lld", v);
-    cry[v] = p->phase[phase[v] - 1].type == 0;
-  }
-  CK(cudaSetDevice(p->device));
-  int *g_d = nullptr, *w_d = nullptr;
-  uint8_t* c_d = nullptr;
-  double* r_d = nullptr;
-  long long* s_d = nullptr;
-  unsigned long long* n_d = nullptr;
-  CK(cudaMalloc(&g_d, sizeof(int) * nv));
-  CK(cudaMalloc(&w_d, sizeof(int) * nv));
-  CK(cudaMalloc(&c_d, nv));
-  CK(cudaMalloc(&r_d, sizeof(double) * nv));
-  CK(cudaMalloc(&s_d, sizeof(long long) * MAX_CANDIDATES));
-  CK(cudaMalloc(&n_d, sizeof(unsigned long long)));
-  CK(cudaMemcpy(g_d, grain, sizeof(int) * nv, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c_d, cry.data(), nv, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(r_d, rho, sizeof(double) * nv, cudaMemcpyHostToDevice));
-  CK(cudaMemset(w_d, 0xff, sizeof(int) * nv));
-  CK(cudaMemset(n_d, 0, sizeof(unsigned long long)));
-  CK(launch_nucleation_candidates(cell_dim, g_d, c_d, r_d, p->rho_nucleation, p->nucleation_prob, p->seed,
-                                  (uint64_t)step * (uint64_t)nv, s_d, n_d, MAX_CANDIDATES, nullptr));
-  unsigned long long cnt = 0;
-  CK(cudaMemcpy(&cnt, n_d, sizeof(cnt), cudaMemcpyDeviceToHost));
-  mth_status st = MTH_OK;
-  if ((long long)cnt > MAX_CANDIDATES) {
-    st = set_err(MTH_ERR_UNSUPPORTED, "%llu nucleation candidates (limit %lld)", cnt, MAX_CANDIDATES);
-  } else {
-    std::vector<long long> sv(cnt);
-    if (cnt) CK(cudaMemcpy(sv.data(), s_d, sizeof(long long) * cnt, cudaMemcpyDeviceToHost));
-    std::sort(sv.begin(), sv.end());
-    const int nn = (int)std::min<unsigned long long>(cnt, (unsigned long long)MAX_NUCLEI);
-    if (nn) {
-      CK(cudaMemcpy(s_d, sv.data(), sizeof(long long) * nn, cudaMemcpyHostToDevice));
-      CK(launch_paint_nuclei(cell_dim, s_d, nn, p->nucleus_radius, first_id, w_d, g_d, nullptr));
-      CK(cudaMemcpy(grain, g_d, sizeof(int) * nv, cudaMemcpyDeviceToHost));
-    }
-    for (long long k = 0; k < nn && k < cap && sites; k++) sites[k] = sv[k];
-    *n_new = nn;
-  }
-  cudaFree(g_d); cudaFree(w_d); cudaFree(c_d); cudaFree(r_d); cudaFree(s_d); cudaFree(n_d);
-  return st;
-}
-
-// ------------------------------------------------- allocation-free local solve
-extern "C" mth_status mth_local_solve_noalloc(const mth_params* p, const double c066[36], size_t n, double* d_sig,
-                                              const double* d_eps_p, const double* d_strain, const double* d_rot,
-                                              const double* d_crss, double* d_edot, double* d_err,
-                                              long long* newton_iters, void* stream) {
-  if (!p || !c066 || !d_sig || !d_eps_p || !d_strain || !d_rot || !d_crss || !d_edot || !d_err)
-    return set_err(MTH_ERR_ARG, "null argument");
-  if ((long long)n > noalloc_max_voxels())
-    return set_err(MTH_ERR_ARG, "n=%zu exceeds the allocation-free limit of %lld voxels", n, noalloc_max_voxels());
-  if (n == 0) {
-    if (newton_iters) *newton_iters = 0;
-    return MTH_OK;
-  }
-  NewtonConst nc;
-  memset(&nc, 0, sizeof(nc));
-  mth_status s = fill_phase(p->phase[0], nc.ph[0]);
-  if (s) return s;
-  if (p->phase[0].type != 0) return set_err(MTH_ERR_ARG, "phase 1 must be a crystal");
-  double cm[6][6], sm[6][6];
-  for (int i = 0; i < 6; i++)
-    for (int j = 0; j < 6; j++) cm[i][j] = c066[i * 6 + j];
-  if (!inv6(cm, sm)) return set_err(MTH_ERR_SINGULAR, "C066 singular");
-  for (int i = 0; i < 5; i++)
-    for (int j = 0; j < 5; j++) nc.s0dev[i * 5 + j] = sm[i][j];
-  nc.s0hh = sm[5][5];
-  nc.dt = p->time_step;
-  nc.tol = p->newton_tol > 0 ? p->newton_tol : 1e-10;
-  nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
-  CK(cudaSetDevice(p->device));
-  CK(launch_local_solve_noalloc(nc, (long long)n, d_sig, d_eps_p, d_strain, d_rot, d_crss, d_edot, d_err,
-                                newton_iters, static_cast<cudaStream_t>(stream)));
-  return MTH_OK;
-}
-
 // ------------------------------------------------------------- profiling
 extern "C" mth_status mth_profile_enable(mth_ctx* c, int on) {
   if (!c) return set_err(MTH_ERR_ARG, "null context");
@@ -1920,747 +1397,5 @@ extern "C" mth_status mth_profile_read(mth_ctx* c, mth_profile* out, int reset) 
     memset(c->prof_launch, 0, sizeof(c->prof_launch));
     memset(c->prof_bytes, 0, sizeof(c->prof_bytes));
   }
-  return MTH_OK;
-}
-
-// ------------------------------------------------------------ local solve
-extern "C" mth_status mth_local_solve(const mth_params* p, const double c066[36], size_t n, double* sig,
-                                      const double* eps_p, const double* strain, const double* rot,
-                                      const double* crss, double* edot, double* err, long long* newton_iters) {
-  if (!p || !c066 || !sig || !eps_p || !strain || !rot || !crss || !edot || !err)
-    return set_err(MTH_ERR_ARG, "null argument");
-  if (n == 0) {
-    if (newton_iters) *newton_iters = 0;
-    return MTH_OK;
-  }
-  NewtonConst nc;
-  memset(&nc, 0, sizeof(nc));
-  mth_status s = fill_phase(p->phase[0], nc.ph[0]);
-  if (s) return s;
-  if (p->phase[0].type != 0) return set_err(MTH_ERR_ARG, "phase 1 must be a crystal");
-  double cm[6][6], sm[6][6];
-  for (int i = 0; i < 6; i++)
-    for (int j = 0; j < 6; j++) cm[i][j] = c066[i * 6 + j];
-  if (!inv6(cm, sm)) return set_err(MTH_ERR_SINGULAR, "C066 singular");
-  for (int i = 0; i < 5; i++)
-    for (int j = 0; j < 5; j++) nc.s0dev[i * 5 + j] = sm[i][j];
-  nc.s0hh = sm[5][5];
-  nc.dt = p->time_step;
-  nc.tol = p->newton_tol > 0 ? p->newton_tol : 1e-10;
-  nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
-  CK(cudaSetDevice(p->device));
-  cudaStream_t st;
-  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  double *ds, *de, *dst, *dr, *dc, *ded, *der;
-  long long* dit;
-  CK(cudaMalloc(&ds, sizeof(double) * 6 * n));
-  CK(cudaMalloc(&de, sizeof(double) * 6 * n));
-  CK(cudaMalloc(&dst, sizeof(double) * 6 * n));
-  CK(cudaMalloc(&dr, sizeof(double) * 9 * n));
-  CK(cudaMalloc(&dc, sizeof(double) * 12 * n));
-  CK(cudaMalloc(&ded, sizeof(double) * 6 * n));
-  CK(cudaMalloc(&der, sizeof(double) * 2 * n));
-  CK(cudaMalloc(&dit, sizeof(long long) * n));
-  CK(cudaMemcpyAsync(ds, sig, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(de, eps_p, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(dst, strain, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(dr, rot, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(dc, crss, sizeof(double) * 12 * n, cudaMemcpyHostToDevice, st));
-  std::vector<double> rows(n * ETAB_W);
-  for (size_t v = 0; v < n; v++) {
-    class_row(nc.ph[0], rot + 9 * v, &rows[v * ETAB_W]);
-    class_row_add_s0(&rows[v * ETAB_W], sm);
-  }
-  double* det;
-  CK(cudaMalloc(&det, sizeof(double) * rows.size()));
-  CK(cudaMemcpyAsync(det, rows.data(), sizeof(double) * rows.size(), cudaMemcpyHostToDevice, st));
-  CK(launch_local_solve(nc, (long long)n, ds, de, dst, dr, dc, det, ded, der, dit, st));
-  std::vector<long long> it(n);
-  CK(cudaMemcpyAsync(sig, ds, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(edot, ded, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(err, der, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(it.data(), dit, sizeof(long long) * n, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  long long tot = 0;
-  for (size_t v = 0; v < n; v++) tot += it[v];
-  if (newton_iters) *newton_iters = tot;
-  cudaFree(ds); cudaFree(de); cudaFree(dst); cudaFree(dr); cudaFree(dc); cudaFree(ded); cudaFree(der); cudaFree(dit);
-  cudaFree(det);
-  cudaStreamDestroy(st);
-  return MTH_OK;
-}
-
-// ------------------------------------------------------------ RVE batches
-// n independent volumes (own parameters, microstructure and grid size) on
-// one GPU.  Every member is an ordinary context whose stream, reduction
-// slot, error flag, strain-increment and live flag live in the batch.  One
-// Green iteration of the whole batch is one launch of a CUDA graph:
-//   H2D (strain increments and live flags of all members)
-//   -> per member, as parallel branches: its FFT passes, Newton, reduction
-//   -> D2H (reduced sums and error flags of all members).
-// A member that has converged keeps its branch but its live flag is 0, so
-// its kernels return at once.  The graph is captured again when the Newton
-// constants baked into its kernel parameters change (the first step runs
-// with the flow rule off).  For each distinct grid size and precision the
-// batch times the TMA and the shared-memory FFT passes once on a scratch
-// volume and keeps the faster (cached for the process).
-struct mth_batch {
-  int n = 0;
-  int device = 0;
-  cudaStream_t st = nullptr;
-  std::vector<mth_ctx*> rve;
-  std::vector<cudaStream_t> branch;
-  std::vector<cudaEvent_t> join;
-  cudaEvent_t fork = nullptr;
-  double* add_d = nullptr;
-  double* add_h = nullptr;
-  int* live_d = nullptr;
-  int* live_h = nullptr;
-  double* red_d = nullptr;
-  double* red_h = nullptr;
-  int* err_d = nullptr;
-  int* err_h = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  std::vector<NewtonConst> cap_nc;
-};
-
-namespace {
-constexpr int BATCH_RED = 32;   // reduction slot of a member (doubles)
-
-void batch_free(mth_batch* b) {
-  if (!b) return;
-  if (b->st) cudaStreamSynchronize(b->st);
-  for (mth_ctx* c : b->rve) ctx_free(c);
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  for (cudaStream_t s : b->branch) cudaStreamDestroy(s);
-  for (cudaEvent_t e : b->join) cudaEventDestroy(e);
-  if (b->fork) cudaEventDestroy(b->fork);
-  cudaFree(b->add_d);
-  cudaFree(b->live_d);
-  cudaFree(b->red_d);
-  cudaFree(b->err_d);
-  if (b->add_h) cudaFreeHost(b->add_h);
-  if (b->live_h) cudaFreeHost(b->live_h);
-  if (b->red_h) cudaFreeHost(b->red_h);
-  if (b->err_h) cudaFreeHost(b->err_h);
-  if (b->st) cudaStreamDestroy(b->st);
-  delete b;
-}
-
-// FFT pass choice per (grid, precision): 1 TMA, 0 shared memory
-std::map<std::vector<int>, int>& tuned_passes() {
-  static std::map<std::vector<int>, int> m;
-  return m;
-}
-
-// Time `its` Green iterations of a scratch volume with the parameters of p
-// (single grain, no pores) with the TMA and the shared-memory passes.
-mth_status tune_passes(const mth_params& p, int* use_tma) {
-  std::vector<int> key = {p.cell_dim[0], p.cell_dim[1], p.cell_dim[2], p.precision};
-  auto it = tuned_passes().find(key);
-  if (it != tuned_passes().end()) { *use_tma = it->second; return MTH_OK; }
-  mth_ctx* c = nullptr;
-  mth_status s = mth_create(&p, &c);
-  if (s) return s;
-  if (!tma_has(c->tma, 0) && !tma_has(c->tma, 1) && !tma_has(c->tma, 2)) {
-    ctx_free(c);
-    tuned_passes()[key] = 0;
-    *use_tma = 0;
-    return MTH_OK;
-  }
-  const size_t nv = (size_t)c->nv;
-  std::vector<int> grain(nv, 1), phase(nv, 1);
-  std::vector<double> eul(3 * nv, 0.0);
-  s = mth_upload_microstructure(c, grain.data(), phase.data(), eul.data(), nv);
-  if (s) { ctx_free(c); return s; }
-  c->add_h[0] = c->add_h[1] = c->add_h[2] = c->add_h[3] = c->add_h[4] = c->add_h[5] = 0.0;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  float ms[2] = {0, 0};
-  for (int variant = 0; variant < 2; variant++) {
-    c->tma_off = variant == 1;
-    for (int rep = 0; rep < 2; rep++) {   // first pass warms up
-      if (cudaEventRecord(e0, c->st) != cudaSuccess) break;
-      for (int k = 0; k < 3; k++) {
-        s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
-        if (s) break;
-      }
-      if (s) break;
-      cudaEventRecord(e1, c->st);
-      cudaStreamSynchronize(c->st);
-      cudaEventElapsedTime(&ms[variant], e0, e1);
-    }
-    if (s) break;
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (cudaStreamSynchronize(c->st) != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "pass tuning failed");
-  if (!s && *c->err_h) s = set_err(MTH_ERR_TIMEOUT, "pass tuning timed out");
-  ctx_free(c);
-  if (s) return s;
-  *use_tma = ms[0] <= ms[1] ? 1 : 0;
-  tuned_passes()[key] = *use_tma;
-  return MTH_OK;
-}
-
-// one Green iteration of every member as parallel graph branches
-mth_status batch_capture(mth_batch* b) {
-  if (b->exec) {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
-  const int n = b->n;
-  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-  mth_status s = MTH_OK;
-  auto ck = [&](cudaError_t e) {
-    if (e != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
-  };
-  ck(cudaMemcpyAsync(b->add_d, b->add_h, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, b->st));
-  ck(cudaMemcpyAsync(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
-  ck(cudaEventRecord(b->fork, b->st));
-  for (int i = 0; i < n && !s; i++) {
-    mth_ctx* c = b->rve[i];
-    ck(cudaStreamWaitEvent(b->branch[i], b->fork, 0));
-    const int prof = c->prof_on;
-    c->prof_on = 0;
-    c->st = b->branch[i];
-    if (!s) s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
-    if (!s) s = launch_reduce(c, NPART, true);
-    c->st = b->st;
-    c->prof_on = prof;
-    ck(cudaEventRecord(b->join[i], b->branch[i]));
-    ck(cudaStreamWaitEvent(b->st, b->join[i], 0));
-  }
-  ck(cudaMemcpyAsync(b->red_h, b->red_d, sizeof(double) * BATCH_RED * n, cudaMemcpyDeviceToHost, b->st));
-  ck(cudaMemcpyAsync(b->err_h, b->err_d, sizeof(int) * n, cudaMemcpyDeviceToHost, b->st));
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(b->st, &g);
-  if (!s && e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
-  if (!s) {
-    e = cudaGraphInstantiate(&b->exec, g, 0);
-    if (e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
-  }
-  if (g) cudaGraphDestroy(g);
-  if (s) return s;
-  b->cap_nc.resize(n);
-  for (int i = 0; i < n; i++) b->cap_nc[i] = b->rve[i]->nc;
-  return MTH_OK;
-}
-}  // namespace
-
-extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batch** out) {
-  if (!params || !out || n <= 0) return set_err(MTH_ERR_ARG, "batch needs params, out and n > 0");
-  *out = nullptr;
-  for (int i = 0; i < n; i++) {
-    if (params[i].device != params[0].device) return set_err(MTH_ERR_ARG, "batch members on different devices");
-    if (params[i].pf_substeps > 0) return set_err(MTH_ERR_UNSUPPORTED, "recrystallisation in a batch member");
-    if (params[i].flow_law != 0) return set_err(MTH_ERR_UNSUPPORTED, "dislocation-density law in a batch member");
-  }
-  mth_batch* b = new mth_batch();
-  b->n = n;
-  b->device = params[0].device;
-  mth_status s = MTH_OK;
-  auto ck = [&](cudaError_t e) {
-    if (e != cudaSuccess && !s)
-      s = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
-  };
-  for (int i = 0; i < n && !s; i++) {
-    mth_ctx* c = nullptr;
-    s = mth_create(&params[i], &c);
-    if (!s) b->rve.push_back(c);
-  }
-  if (!s) {
-    ck(cudaSetDevice(b->device));
-    ck(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
-    ck(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-    b->branch.resize(n, nullptr);
-    b->join.resize(n, nullptr);
-    for (int i = 0; i < n; i++) {
-      ck(cudaStreamCreateWithFlags(&b->branch[i], cudaStreamNonBlocking));
-      ck(cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming));
-    }
-    ck(cudaMalloc(&b->add_d, sizeof(double) * 8 * n));
-    ck(cudaMalloc(&b->live_d, sizeof(int) * n));
-    ck(cudaMalloc(&b->red_d, sizeof(double) * BATCH_RED * n));
-    ck(cudaMalloc(&b->err_d, sizeof(int) * n));
-    ck(cudaMallocHost(&b->add_h, sizeof(double) * 8 * n));
-    ck(cudaMallocHost(&b->live_h, sizeof(int) * n));
-    ck(cudaMallocHost(&b->red_h, sizeof(double) * BATCH_RED * n));
-    ck(cudaMallocHost(&b->err_h, sizeof(int) * n));
-  }
-  if (!s) {
-    ck(cudaMemset(b->add_d, 0, sizeof(double) * 8 * n));
-    ck(cudaMemset(b->err_d, 0, sizeof(int) * n));
-    memset(b->add_h, 0, sizeof(double) * 8 * n);
-    memset(b->err_h, 0, sizeof(int) * n);
-    for (int i = 0; i < n; i++) b->live_h[i] = 1;
-    ck(cudaMemcpy(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice));
-  }
-  for (int i = 0; i < n && !s; i++) {
-    mth_ctx* c = b->rve[i];
-    int use_tma = 1;
-    s = tune_passes(params[i], &use_tma);
-    if (s) break;
-    c->tma_off = !use_tma;
-    ck(cudaStreamSynchronize(c->st));
-    cudaStreamDestroy(c->st);
-    cudaFree(c->red);
-    cudaFree(c->err_d);
-    cudaFree(c->add_d);
-    cudaFree(c->live_d);
-    c->st = b->st;
-    c->red = b->red_d + (size_t)BATCH_RED * i;
-    c->err_d = b->err_d + i;
-    c->add_d = b->add_d + (size_t)8 * i;
-    c->live_d = b->live_d + i;
-    c->in_batch = true;
-  }
-  if (s) {
-    batch_free(b);
-    return s;
-  }
-  *out = b;
-  return MTH_OK;
-}
-
-extern "C" mth_status mth_batch_upload(mth_batch* b, int i, const int* grain, const int* phase, const double* euler_deg,
-                                       size_t n_voxels) {
-  if (!b || i < 0 || i >= b->n) return set_err(MTH_ERR_ARG, "batch member %d", i);
-  return mth_upload_microstructure(b->rve[i], grain, phase, euler_deg, n_voxels);
-}
-
-extern "C" mth_status mth_batch_step(mth_batch* b, mth_step_report* reports) {
-  if (!b) return set_err(MTH_ERR_ARG, "null batch");
-  CK(cudaSetDevice(b->device));
-  const int n = b->n;
-  for (int i = 0; i < n; i++)
-    if (!b->rve[i]->uploaded) return set_err(MTH_ERR_STATE, "batch member %d has no microstructure", i);
-  for (int i = 0; i < n; i++) {
-    mth_status s = step_begin(b->rve[i]);
-    if (s) return s;
-  }
-  bool recapture = !b->exec;
-  for (int i = 0; i < n && !recapture; i++)
-    recapture = memcmp(&b->cap_nc[i], &b->rve[i]->nc, sizeof(NewtonConst)) != 0;
-  if (recapture) {
-    mth_status s = batch_capture(b);
-    if (s) return s;
-  }
-  std::vector<char> active(n);
-  int nact = 0;
-  for (int i = 0; i < n; i++) nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
-  while (nact > 0) {
-    for (int i = 0; i < n; i++) {
-      b->live_h[i] = active[i];
-      if (active[i]) {
-        iter_add(b->rve[i]);
-        memcpy(b->add_h + (size_t)8 * i, b->rve[i]->add_h, sizeof(double) * 6);
-      }
-    }
-    CK(cudaGraphLaunch(b->exec, b->st));
-    CK(cudaStreamSynchronize(b->st));
-    nact = 0;
-    for (int i = 0; i < n; i++) {
-      if (b->err_h[i]) return set_err(MTH_ERR_TIMEOUT, "batch member %d: a kernel timed out waiting for its tile copies", i);
-      if (!active[i]) continue;
-      mth_status s = iter_finish(b->rve[i], b->red_h + (size_t)BATCH_RED * i);
-      if (s) return s;
-      nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
-    }
-  }
-  for (int i = 0; i < n; i++) {
-    mth_status s = step_end(b->rve[i], reports ? &reports[i] : nullptr);
-    if (s) return s;
-  }
-  return MTH_OK;
-}
-
-extern "C" mth_status mth_batch_download_field(mth_batch* b, int i, int field, double* host, size_t n_values) {
-  if (!b || i < 0 || i >= b->n) return set_err(MTH_ERR_ARG, "batch member %d", i);
-  return mth_download_field(b->rve[i], field, host, n_values);
-}
-
-extern "C" mth_status mth_batch_destroy(mth_batch* b) {
-  if (!b) return set_err(MTH_ERR_ARG, "null batch");
-  cudaSetDevice(b->device);
-  batch_free(b);
-  return MTH_OK;
-}
-
-// ------------------------------------------------------ calibration adjoint
-// Forward sweep with stored states every K steps, then per mechanical step
-// in reverse order: adj_pre (transposed end-of-step Jacobians, tangent
-// stiffness, right-hand side), b = Q(C_t sigbar) + W^T(spin adjoint), CG on
-// Q C_t mu = b, adj_post (explicit dependences of the local law).  The
-// segment of steps between two stored states is recomputed before it is
-// reversed; the last segment's snapshots come from the first sweep.
-namespace {
-struct HostCkpt {
-  t33 disgrad_avg, disgrad_avg_t, sig_avg, sig_avg1;
-  double e_vm, d_vm, s_vm, s_vm1, err_e, err_s, time_tot;
-  int istep;
-};
-constexpr int CKPT_PLANES = 46;   // sig, strain, epsp, edot (6 each), rot 9, crss 12, gamacum 1
-constexpr int SNAP_PLANES = 31;   // before the step: rot 9, crss 12, gamacum 1; after: sig 6, wspin 3
-constexpr int ADJ_STATE_PLANES = 25;   // eps_p 6, CRSS 12, gamacum 1, rotation 3, later spin 3
-
-struct FieldPtrs {
-  char* sig; char* strain; char* epsp; char* edot; char* rot; char* crss; char* gam; char* wspin;
-};
-template <typename T>
-FieldPtrs field_ptrs_of(Fields<T>& f) {
-  return FieldPtrs{(char*)f.sig, (char*)f.strain, (char*)f.epsp, (char*)f.edot,
-                   (char*)f.rot, (char*)f.crss, (char*)f.gamacum, (char*)f.wspin};
-}
-
-struct AdjRun {
-  size_t esz = 0;
-  long long P = 0;
-  std::vector<void*> mem;
-  char* ckpt = nullptr;
-  char* snap = nullptr;
-  double* st = nullptr;
-  double* sigbar = nullptr;
-  char* ct = nullptr;
-  char* rhs = nullptr;
-  char* spec9 = nullptr;
-  char* mu = nullptr;
-  char* r = nullptr;
-  char* p = nullptr;
-  char* ap = nullptr;
-  char* tmp = nullptr;
-  std::vector<HostCkpt> hck;
-  ~AdjRun() {
-    for (void* m : mem) cudaFree(m);
-  }
-  cudaError_t alloc(void** out, size_t bytes) {
-    cudaError_t e = cudaMalloc(out, bytes ? bytes : 16);
-    if (e == cudaSuccess) mem.push_back(*out);
-    return e;
-  }
-};
-}  // namespace
-
-static FieldPtrs field_ptrs(mth_ctx* c) { return c->mixed ? field_ptrs_of(c->ff) : field_ptrs_of(c->fd); }
-
-// state before step slot*K (device planes and host macro state)
-static mth_status adj_save(mth_ctx* c, AdjRun& run, int slot) {
-  const FieldPtrs f = field_ptrs(c);
-  const size_t pl = run.esz * (size_t)run.P;
-  char* d = run.ckpt + (size_t)slot * CKPT_PLANES * pl;
-  CK(cudaMemcpyAsync(d, f.sig, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(d + 6 * pl, f.strain, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(d + 12 * pl, f.epsp, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(d + 18 * pl, f.edot, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(d + 24 * pl, f.rot, 9 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(d + 33 * pl, f.crss, 12 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(d + 45 * pl, f.gam, pl, cudaMemcpyDeviceToDevice, c->st));
-  HostCkpt& h = run.hck[slot];
-  memcpy(h.disgrad_avg, c->disgrad_avg, sizeof(t33));
-  memcpy(h.disgrad_avg_t, c->disgrad_avg_t, sizeof(t33));
-  memcpy(h.sig_avg, c->sig_avg, sizeof(t33));
-  memcpy(h.sig_avg1, c->sig_avg1, sizeof(t33));
-  h.e_vm = c->e_vm; h.d_vm = c->d_vm; h.s_vm = c->s_vm; h.s_vm1 = c->s_vm1;
-  h.err_e = c->err_e; h.err_s = c->err_s; h.time_tot = c->time_tot; h.istep = c->istep;
-  return MTH_OK;
-}
-
-static mth_status adj_restore(mth_ctx* c, AdjRun& run, int slot) {
-  const FieldPtrs f = field_ptrs(c);
-  const size_t pl = run.esz * (size_t)run.P;
-  const char* d = run.ckpt + (size_t)slot * CKPT_PLANES * pl;
-  CK(cudaMemcpyAsync(f.sig, d, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(f.strain, d + 6 * pl, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(f.epsp, d + 12 * pl, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(f.edot, d + 18 * pl, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(f.rot, d + 24 * pl, 9 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(f.crss, d + 33 * pl, 12 * pl, cudaMemcpyDeviceToDevice, c->st));
-  CK(cudaMemcpyAsync(f.gam, d + 45 * pl, pl, cudaMemcpyDeviceToDevice, c->st));
-  const HostCkpt& h = run.hck[slot];
-  memcpy(c->disgrad_avg, h.disgrad_avg, sizeof(t33));
-  memcpy(c->disgrad_avg_t, h.disgrad_avg_t, sizeof(t33));
-  memcpy(c->sig_avg, h.sig_avg, sizeof(t33));
-  memcpy(c->sig_avg1, h.sig_avg1, sizeof(t33));
-  c->e_vm = h.e_vm; c->d_vm = h.d_vm; c->s_vm = h.s_vm; c->s_vm1 = h.s_vm1;
-  c->err_e = h.err_e; c->err_s = h.err_s; c->time_tot = h.time_tot; c->istep = h.istep;
-  return MTH_OK;
-}
-
-// one forward step with its snapshot in slot; records <sigma_33> and the step data
-static mth_status adj_forward_step(mth_ctx* c, AdjRun& run, int slot, double* s33, AdjStepArgs* a) {
-  const FieldPtrs f = field_ptrs(c);
-  const size_t pl = run.esz * (size_t)run.P;
-  char* d = run.snap + (size_t)slot * SNAP_PLANES * pl;
-  const int istep = c->istep;
-  if (slot >= 0) {
-    CK(cudaMemcpyAsync(d, f.rot, 9 * pl, cudaMemcpyDeviceToDevice, c->st));
-    CK(cudaMemcpyAsync(d + 9 * pl, f.crss, 12 * pl, cudaMemcpyDeviceToDevice, c->st));
-    CK(cudaMemcpyAsync(d + 21 * pl, f.gam, pl, cudaMemcpyDeviceToDevice, c->st));
-  }
-  mth_step_report rep;
-  mth_status s = mth_step(c, &rep);
-  if (s) return s;
-  if (slot >= 0) {
-    CK(cudaMemcpyAsync(d + 22 * pl, f.sig, 6 * pl, cudaMemcpyDeviceToDevice, c->st));
-    CK(cudaMemcpyAsync(d + 28 * pl, f.wspin, 3 * pl, cudaMemcpyDeviceToDevice, c->st));
-  }
-  *s33 = rep.sig_avg[2][2];
-  for (int i = 0; i < 3; i++) a->au[i] = c->last_au[i];
-  a->flow_off = c->nc.flow_off;
-  a->do_orient = (c->p.update_flag == 1 && istep > 1) ? 1 : 0;
-  a->do_harden = (c->p.hard_flag == 1) ? 1 : 0;
-  a->seed = 0.0;
-  return MTH_OK;
-}
-
-// out = Q(in) (nin = 6) or Q(in[0..5]) + W^T(in[6..8]) (nin = 9): the
-// forward's z and y passes around the projection x pass
-template <typename T>
-static cudaError_t adj_project_launch(mth_ctx* c, AdjRun& run, const AdjProj& pj, const T* in, int nin, T* out) {
-  const FftGeom& g = c->geom;
-  c2<T>* sp = reinterpret_cast<c2<T>*>(run.spec9);
-  auto tw = [&](int a, int d) { return static_cast<const c2<T>*>(c->tw[a][d]); };
-  const IterIn none{nullptr, nullptr};
-  cudaError_t e = launch_fft_z_r2c<T>(g, in, sp, nin, tw(2, 0), none, c->st);
-  if (e == cudaSuccess) e = launch_fft_strided<T>(g, sp, nin, 1, -1, tw(1, 0), none, c->st);
-  if (e == cudaSuccess) e = launch_adj_x_proj<T>(g, pj, sp, nin, tw(0, 0), tw(0, 1), c->st);
-  if (e == cudaSuccess) e = launch_fft_strided<T>(g, sp, 6, 1, +1, tw(1, 1), none, c->st);
-  if (e == cudaSuccess) e = launch_fft_z_c2r<T>(g, sp, out, 6, tw(2, 1), (T)(1.0 / (double)c->nv), none, 0, c->st);
-  return e;
-}
-template <typename T>
-static mth_status adj_project(mth_ctx* c, AdjRun& run, const AdjProj& pj, const T* in, int nin, T* out) {
-  const FftGeom& g = c->geom;
-  const double w = sizeof(T), rp = w * (double)c->nv, kp = 2.0 * w * (double)g.n0 * g.n1 * g.kz;
-  LAUNCHN(K_ADJ_CG, 5, (nin + 6) * (rp + 2 * kp) + 2 * nin * kp, adj_project_launch<T>(c, run, pj, in, nin, out));
-  return MTH_OK;
-}
-
-template <typename T>
-static AdjViews<T> adj_views(mth_ctx* c, AdjRun& run, int slot) {
-  const size_t P = (size_t)run.P;
-  const T* d = reinterpret_cast<const T*>(run.snap) + (size_t)slot * SNAP_PLANES * P;
-  AdjViews<T> v;
-  v.nv = run.P;
-  v.s_rot = d;
-  v.s_crss = d + 9 * P;
-  v.s_gam = d + 21 * P;
-  v.s_sig = d + 22 * P;
-  v.s_wspin = d + 28 * P;
-  v.ep = run.st;
-  v.tau = run.st + 6 * P;
-  v.gam = run.st + 18 * P;
-  v.phi = run.st + 19 * P;
-  v.wnext = run.st + 22 * P;
-  v.sigbar = run.sigbar;
-  v.ct = reinterpret_cast<T*>(run.ct);
-  v.rhs = reinterpret_cast<T*>(run.rhs);
-  v.mu = reinterpret_cast<const T*>(run.mu);
-  (void)c;
-  return v;
-}
-
-template <typename T>
-static mth_status adj_reverse_step(mth_ctx* c, AdjRun& run, int step, int slot, const AdjStepArgs& a,
-                                   const AdjProj& pj, double tol, int itmax, double th[4], int* iters) {
-  const long long P = run.P;
-  const AdjViews<T> v = adj_views<T>(c, run, slot);
-  const double w = sizeof(T);
-  double red[4];
-  LAUNCH(K_ADJ_LOCAL, (double)P * (31 * w + 25 * 8 * 2 + 6 * 8 + 16 * w + 9 * w + 8 * ETAB_W / 64.0),
-         launch_adj_pre<T>(c->nc, a, v, c->eclass_d, c->etab_d, c->partials, c->st));
-  mth_status s = reduce_to_host(c, 4, red);
-  if (s) return s;
-  for (int i = 0; i < 4; i++) {
-    if (!std::isfinite(red[i]))
-      return set_err(MTH_ERR_NAN, "adjoint: tangent stiffness not positive definite or non-finite value (step %d)",
-                     step);
-    th[i] += red[i];
-  }
-  T* mu = reinterpret_cast<T*>(run.mu);
-  T* r = reinterpret_cast<T*>(run.r);
-  T* p = reinterpret_cast<T*>(run.p);
-  T* ap = reinterpret_cast<T*>(run.ap);
-  T* tmp = reinterpret_cast<T*>(run.tmp);
-  const T* ct = reinterpret_cast<const T*>(run.ct);
-  const size_t b6 = sizeof(T) * 6 * (size_t)P;
-  s = adj_project<T>(c, run, pj, reinterpret_cast<const T*>(run.rhs), 9, r);
-  if (s) return s;
-  CK(cudaMemsetAsync(mu, 0, b6, c->st));
-  LAUNCH(K_ADJ_CG, 12.0 * w * P, launch_adj_dot<T>(r, r, P, c->partials, c->st));
-  double rr0;
-  s = reduce_to_host(c, 1, &rr0);
-  if (s) return s;
-  int it = 0;
-  if (rr0 > 0.0) {
-    CK(cudaMemcpyAsync(p, r, b6, cudaMemcpyDeviceToDevice, c->st));
-    double rr = rr0, beta = 0.0;
-    const double stop = tol * tol * rr0;
-    for (; it < itmax;) {
-      LAUNCH(K_ADJ_CG, (it ? 18.0 : 12.0) * w * P + 16.0 * w * P,
-             launch_adj_ct_apply<T>(ct, p, r, beta, it > 0, tmp, P, c->st));
-      s = adj_project<T>(c, run, pj, tmp, 6, ap);
-      if (s) return s;
-      LAUNCH(K_ADJ_CG, 12.0 * w * P, launch_adj_dot<T>(p, ap, P, c->partials, c->st));
-      double pap;
-      s = reduce_to_host(c, 1, &pap);
-      if (s) return s;
-      if (!(pap > 0.0))
-        return set_err(MTH_ERR_NAN, "adjoint: projected tangent operator not positive (step %d, p.Ap=%g)", step, pap);
-      const double alpha = rr / pap;
-      LAUNCH(K_ADJ_CG, 36.0 * w * P, launch_adj_cg_update<T>(mu, r, p, ap, alpha, P, c->partials, c->st));
-      double rn;
-      s = reduce_to_host(c, 1, &rn);
-      if (s) return s;
-      it++;
-      if (!std::isfinite(rn)) return set_err(MTH_ERR_NAN, "adjoint: non-finite CG residual");
-      if (rn <= stop) break;
-      beta = rn / rr;
-      rr = rn;
-    }
-    if (it >= itmax)
-      return set_err(MTH_ERR_NOT_CONVERGED, "adjoint: CG did not reach %g in %d iterations (step %d)", tol, itmax, step);
-  }
-  *iters = it;
-  LAUNCH(K_ADJ_LOCAL, (double)P * (31 * w + 22 * 8 * 2 + 6 * 8 + 22 * w),
-         launch_adj_post<T>(c->nc, a, v, c->partials, c->st));
-  s = reduce_to_host(c, 4, red);
-  if (s) return s;
-  for (int i = 0; i < 4; i++) {
-    if (!std::isfinite(red[i])) return set_err(MTH_ERR_NAN, "adjoint: non-finite parameter adjoint");
-    th[i] += red[i];
-  }
-  return MTH_OK;
-}
-
-extern "C" mth_status mth_adjoint(mth_ctx* c, const mth_adjoint_opts* o, double* s33_out, mth_adjoint_result* res) {
-  if (!c || !o || !res) return set_err(MTH_ERR_ARG, "null argument");
-  if (!c->uploaded) return set_err(MTH_ERR_STATE, "mth_adjoint before mth_upload_microstructure");
-  if (c->istep != 0) return set_err(MTH_ERR_STATE, "mth_adjoint needs a context at step 0 (it runs the forward solve)");
-  if (c->in_batch) return set_err(MTH_ERR_STATE, "context belongs to a batch");
-  if (o->n_steps < 1 || !o->target) return set_err(MTH_ERR_ARG, "n_steps >= 1 and a target curve are required");
-  if (c->drx) return set_err(MTH_ERR_UNSUPPORTED, "adjoint with phase-field DRX");
-  if (c->dd) return set_err(MTH_ERR_UNSUPPORTED, "adjoint of the dislocation-density law");
-  if (!c->adj_solid) return set_err(MTH_ERR_UNSUPPORTED, "adjoint needs every voxel of phase 1 and crystalline");
-  if (c->p.elast_bc != 1) return set_err(MTH_ERR_UNSUPPORTED, "adjoint needs ElastBC = 1");
-  for (int a = 0; a < 6; a++) {
-    if (c->vbc[a] + c->sbc[a] != 1)
-      return set_err(MTH_ERR_UNSUPPORTED, "adjoint needs Stress_BC_Flag = 1 - VelGrad_BC_Flag (component %d)", a);
-    if (c->vbc[a] == 0 && a >= 3)
-      return set_err(MTH_ERR_UNSUPPORTED, "adjoint: stress-controlled shear component %d", a);
-  }
-  SETDEV(c);
-  const int N = o->n_steps;
-  const int K = o->checkpoint_every > 0 ? std::min(o->checkpoint_every, N) : std::min(10, N);
-  const int nseg = (N + K - 1) / K;
-  const int last0 = (nseg - 1) * K;
-  const double tol = o->cg_tol > 0 ? o->cg_tol : (c->mixed ? 1e-5 : 1e-7);
-  const int itmax = o->cg_itmax > 0 ? o->cg_itmax : 2000;
-  AdjRun run;
-  run.esz = c->mixed ? sizeof(float) : sizeof(double);
-  run.P = c->nv;
-  const size_t P = (size_t)c->nv, pl = run.esz * P;
-  void* m;
-  CK(run.alloc(&m, (size_t)(nseg + 1) * CKPT_PLANES * pl)); run.ckpt = (char*)m;
-  CK(run.alloc(&m, (size_t)K * SNAP_PLANES * pl)); run.snap = (char*)m;
-  CK(run.alloc(&m, sizeof(double) * ADJ_STATE_PLANES * P)); run.st = (double*)m;
-  CK(run.alloc(&m, sizeof(double) * 6 * P)); run.sigbar = (double*)m;
-  CK(run.alloc(&m, 16 * pl)); run.ct = (char*)m;
-  CK(run.alloc(&m, 9 * pl)); run.rhs = (char*)m;
-  CK(run.alloc(&m, 9 * 2 * run.esz * (size_t)c->geom.kplane)); run.spec9 = (char*)m;
-  CK(run.alloc(&m, 6 * pl)); run.mu = (char*)m;
-  CK(run.alloc(&m, 6 * pl)); run.r = (char*)m;
-  CK(run.alloc(&m, 6 * pl)); run.p = (char*)m;
-  CK(run.alloc(&m, 6 * pl)); run.ap = (char*)m;
-  CK(run.alloc(&m, 6 * pl)); run.tmp = (char*)m;
-  run.hck.resize(nseg + 1);
-  // k = 0 block of the projection: stress-controlled diagonal components
-  AdjProj pj;
-  memset(&pj, 0, sizeof(pj));
-  for (int a = 0; a < 3; a++) {
-    if (c->vbc[a] != 0) continue;
-    double e[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    e[a][a] = 1.0;
-    double v6[6];
-    cart_to_lt<double>(e, v6);
-    for (int i = 0; i < 6; i++)
-      for (int j = 0; j < 6; j++) pj.ps[i * 6 + j] += v6[i] * v6[j];
-  }
-  std::vector<double> s33(N);
-  std::vector<AdjStepArgs> args(N);
-  auto now = []() { return std::chrono::steady_clock::now(); };
-  auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
-    return std::chrono::duration<double, std::milli>(b - a).count();
-  };
-  CK(cudaStreamSynchronize(c->st));
-  const auto t0 = now();
-  for (int n = 0; n < N; n++) {
-    if (n % K == 0) {
-      mth_status s = adj_save(c, run, n / K);
-      if (s) return s;
-    }
-    mth_status s = adj_forward_step(c, run, n >= last0 ? n - last0 : -1, &s33[n], &args[n]);
-    if (s) return s;
-  }
-  {
-    mth_status s = adj_save(c, run, nseg);   // final state, put back at the end
-    if (s) return s;
-  }
-  CK(cudaStreamSynchronize(c->st));
-  const auto t1 = now();
-  double J = 0;
-  for (int n = 0; n < N; n++) J += (s33[n] - o->target[n]) * (s33[n] - o->target[n]);
-  CK(cudaMemsetAsync(run.st, 0, sizeof(double) * ADJ_STATE_PLANES * P, c->st));
-  double th[4] = {0, 0, 0, 0};
-  long long cg_total = 0;
-  int cg_max = 0, recomputed = 0;
-  for (int seg = nseg - 1; seg >= 0; seg--) {
-    const int n0 = seg * K, n1 = std::min(N, n0 + K);
-    if (seg != nseg - 1) {
-      mth_status s = adj_restore(c, run, seg);
-      if (s) return s;
-      for (int n = n0; n < n1; n++) {
-        double s33r;
-        AdjStepArgs ar;
-        s = adj_forward_step(c, run, n - n0, &s33r, &ar);
-        if (s) return s;
-        recomputed++;
-      }
-    }
-    for (int n = n1 - 1; n >= n0; n--) {
-      AdjStepArgs a = args[n];
-      a.seed = 2.0 * (s33[n] - o->target[n]) / (double)c->nv;
-      int it = 0;
-      mth_status s = c->mixed ? adj_reverse_step<float>(c, run, n, n - n0, a, pj, tol, itmax, th, &it)
-                              : adj_reverse_step<double>(c, run, n, n - n0, a, pj, tol, itmax, th, &it);
-      if (s) return s;
-      cg_total += it;
-      cg_max = std::max(cg_max, it);
-    }
-  }
-  double gt;
-  LAUNCH(K_ADJ_LOCAL, 8.0 * 12 * P, launch_adj_sum_tau(run.st + 6 * P, c->nc.ph[0].nsys, c->nv, c->partials, c->st));
-  {
-    mth_status s = reduce_to_host(c, 1, &gt);
-    if (s) return s;
-    s = adj_restore(c, run, nseg);
-    if (s) return s;
-  }
-  CK(cudaStreamSynchronize(c->st));
-  const auto t2 = now();
-  memset(res, 0, sizeof(*res));
-  res->misfit = J;
-  res->grad[0] = gt;
-  res->grad[1] = th[0];
-  res->grad[2] = th[1];
-  res->grad[3] = th[2];
-  res->grad[4] = th[3];
-  res->cg_iterations = cg_total;
-  res->cg_iterations_max = cg_max;
-  res->recomputed_steps = recomputed;
-  res->forward_ms = ms(t0, t1);
-  res->reverse_ms = ms(t1, t2);
-  if (s33_out) memcpy(s33_out, s33.data(), sizeof(double) * N);
   return MTH_OK;
 }

@@ -1,0 +1,301 @@
+// capi_batch.cu -- batches of independent RVEs (mth_batch_*).
+#include "capi_internal.h"
+
+// ------------------------------------------------------------ RVE batches
+// n independent volumes (own parameters, microstructure and grid size) on
+// one GPU.  Every member is an ordinary context whose stream, reduction
+// slot, error flag, strain-increment and live flag live in the batch.  One
+// Green iteration of the whole batch is one launch of a CUDA graph:
+//   H2D (strain increments and live flags of all members)
+//   -> per member, as parallel branches: its FFT passes, Newton, reduction
+//   -> D2H (reduced sums and error flags of all members).
+// A member that has converged keeps its branch but its live flag is 0, so
+// its kernels return at once.  The graph is captured again when the Newton
+// constants baked into its kernel parameters change (the first step runs
+// with the flow rule off).  For each distinct grid size and precision the
+// batch times the TMA and the shared-memory FFT passes once on a scratch
+// volume and keeps the faster (cached for the process).
+struct mth_batch {
+  int n = 0;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::vector<mth_ctx*> rve;
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr;
+  double* add_d = nullptr;
+  double* add_h = nullptr;
+  int* live_d = nullptr;
+  int* live_h = nullptr;
+  double* red_d = nullptr;
+  double* red_h = nullptr;
+  int* err_d = nullptr;
+  int* err_h = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<NewtonConst> cap_nc;
+};
+
+namespace {
+constexpr int BATCH_RED = 32;   // reduction slot of a member (doubles)
+
+void batch_free(mth_batch* b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (mth_ctx* c : b->rve) ctx_free(c);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (cudaStream_t s : b->branch) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  cudaFree(b->add_d);
+  cudaFree(b->live_d);
+  cudaFree(b->red_d);
+  cudaFree(b->err_d);
+  if (b->add_h) cudaFreeHost(b->add_h);
+  if (b->live_h) cudaFreeHost(b->live_h);
+  if (b->red_h) cudaFreeHost(b->red_h);
+  if (b->err_h) cudaFreeHost(b->err_h);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+// FFT pass choice per (grid, precision): 1 TMA, 0 shared memory
+std::map<std::vector<int>, int>& tuned_passes() {
+  static std::map<std::vector<int>, int> m;
+  return m;
+}
+
+// Time `its` Green iterations of a scratch volume with the parameters of p
+// (single grain, no pores) with the TMA and the shared-memory passes.
+mth_status tune_passes(const mth_params& p, int* use_tma) {
+  std::vector<int> key = {p.cell_dim[0], p.cell_dim[1], p.cell_dim[2], p.precision};
+  auto it = tuned_passes().find(key);
+  if (it != tuned_passes().end()) { *use_tma = it->second; return MTH_OK; }
+  mth_ctx* c = nullptr;
+  mth_status s = mth_create(&p, &c);
+  if (s) return s;
+  if (!tma_has(c->tma, 0) && !tma_has(c->tma, 1) && !tma_has(c->tma, 2)) {
+    ctx_free(c);
+    tuned_passes()[key] = 0;
+    *use_tma = 0;
+    return MTH_OK;
+  }
+  const size_t nv = (size_t)c->nv;
+  std::vector<int> grain(nv, 1), phase(nv, 1);
+  std::vector<double> eul(3 * nv, 0.0);
+  s = mth_upload_microstructure(c, grain.data(), phase.data(), eul.data(), nv);
+  if (s) { ctx_free(c); return s; }
+  c->add_h[0] = c->add_h[1] = c->add_h[2] = c->add_h[3] = c->add_h[4] = c->add_h[5] = 0.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float ms[2] = {0, 0};
+  for (int variant = 0; variant < 2; variant++) {
+    c->tma_off = variant == 1;
+    for (int rep = 0; rep < 2; rep++) {   // first pass warms up
+      if (cudaEventRecord(e0, c->st) != cudaSuccess) break;
+      for (int k = 0; k < 3; k++) {
+        s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+        if (s) break;
+      }
+      if (s) break;
+      cudaEventRecord(e1, c->st);
+      cudaStreamSynchronize(c->st);
+      cudaEventElapsedTime(&ms[variant], e0, e1);
+    }
+    if (s) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "pass tuning failed");
+  if (!s && *c->err_h) s = set_err(MTH_ERR_TIMEOUT, "pass tuning timed out");
+  ctx_free(c);
+  if (s) return s;
+  *use_tma = ms[0] <= ms[1] ? 1 : 0;
+  tuned_passes()[key] = *use_tma;
+  return MTH_OK;
+}
+
+// one Green iteration of every member as parallel graph branches
+mth_status batch_capture(mth_batch* b) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  const int n = b->n;
+  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  mth_status s = MTH_OK;
+  auto ck = [&](cudaError_t e) {
+    if (e != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  };
+  ck(cudaMemcpyAsync(b->add_d, b->add_h, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, b->st));
+  ck(cudaMemcpyAsync(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
+  ck(cudaEventRecord(b->fork, b->st));
+  for (int i = 0; i < n && !s; i++) {
+    mth_ctx* c = b->rve[i];
+    ck(cudaStreamWaitEvent(b->branch[i], b->fork, 0));
+    const int prof = c->prof_on;
+    c->prof_on = 0;
+    c->st = b->branch[i];
+    if (!s) s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+    if (!s) s = launch_reduce(c, NPART, true);
+    c->st = b->st;
+    c->prof_on = prof;
+    ck(cudaEventRecord(b->join[i], b->branch[i]));
+    ck(cudaStreamWaitEvent(b->st, b->join[i], 0));
+  }
+  ck(cudaMemcpyAsync(b->red_h, b->red_d, sizeof(double) * BATCH_RED * n, cudaMemcpyDeviceToHost, b->st));
+  ck(cudaMemcpyAsync(b->err_h, b->err_d, sizeof(int) * n, cudaMemcpyDeviceToHost, b->st));
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (!s && e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  if (!s) {
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+  }
+  if (g) cudaGraphDestroy(g);
+  if (s) return s;
+  b->cap_nc.resize(n);
+  for (int i = 0; i < n; i++) b->cap_nc[i] = b->rve[i]->nc;
+  return MTH_OK;
+}
+}  // namespace
+
+extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batch** out) {
+  if (!params || !out || n <= 0) return set_err(MTH_ERR_ARG, "batch needs params, out and n > 0");
+  *out = nullptr;
+  for (int i = 0; i < n; i++) {
+    if (params[i].device != params[0].device) return set_err(MTH_ERR_ARG, "batch members on different devices");
+    if (params[i].pf_substeps > 0) return set_err(MTH_ERR_UNSUPPORTED, "recrystallisation in a batch member");
+    if (params[i].flow_law != 0) return set_err(MTH_ERR_UNSUPPORTED, "dislocation-density law in a batch member");
+  }
+  mth_batch* b = new mth_batch();
+  b->n = n;
+  b->device = params[0].device;
+  mth_status s = MTH_OK;
+  auto ck = [&](cudaError_t e) {
+    if (e != cudaSuccess && !s)
+      s = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
+  };
+  for (int i = 0; i < n && !s; i++) {
+    mth_ctx* c = nullptr;
+    s = mth_create(&params[i], &c);
+    if (!s) b->rve.push_back(c);
+  }
+  if (!s) {
+    ck(cudaSetDevice(b->device));
+    ck(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    ck(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->branch.resize(n, nullptr);
+    b->join.resize(n, nullptr);
+    for (int i = 0; i < n; i++) {
+      ck(cudaStreamCreateWithFlags(&b->branch[i], cudaStreamNonBlocking));
+      ck(cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming));
+    }
+    ck(cudaMalloc(&b->add_d, sizeof(double) * 8 * n));
+    ck(cudaMalloc(&b->live_d, sizeof(int) * n));
+    ck(cudaMalloc(&b->red_d, sizeof(double) * BATCH_RED * n));
+    ck(cudaMalloc(&b->err_d, sizeof(int) * n));
+    ck(cudaMallocHost(&b->add_h, sizeof(double) * 8 * n));
+    ck(cudaMallocHost(&b->live_h, sizeof(int) * n));
+    ck(cudaMallocHost(&b->red_h, sizeof(double) * BATCH_RED * n));
+    ck(cudaMallocHost(&b->err_h, sizeof(int) * n));
+  }
+  if (!s) {
+    ck(cudaMemset(b->add_d, 0, sizeof(double) * 8 * n));
+    ck(cudaMemset(b->err_d, 0, sizeof(int) * n));
+    memset(b->add_h, 0, sizeof(double) * 8 * n);
+    memset(b->err_h, 0, sizeof(int) * n);
+    for (int i = 0; i < n; i++) b->live_h[i] = 1;
+    ck(cudaMemcpy(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice));
+  }
+  for (int i = 0; i < n && !s; i++) {
+    mth_ctx* c = b->rve[i];
+    int use_tma = 1;
+    s = tune_passes(params[i], &use_tma);
+    if (s) break;
+    c->tma_off = !use_tma;
+    ck(cudaStreamSynchronize(c->st));
+    cudaStreamDestroy(c->st);
+    cudaFree(c->red);
+    cudaFree(c->err_d);
+    cudaFree(c->add_d);
+    cudaFree(c->live_d);
+    c->st = b->st;
+    c->red = b->red_d + (size_t)BATCH_RED * i;
+    c->err_d = b->err_d + i;
+    c->add_d = b->add_d + (size_t)8 * i;
+    c->live_d = b->live_d + i;
+    c->in_batch = true;
+  }
+  if (s) {
+    batch_free(b);
+    return s;
+  }
+  *out = b;
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_batch_upload(mth_batch* b, int i, const int* grain, const int* phase, const double* euler_deg,
+                                       size_t n_voxels) {
+  if (!b || i < 0 || i >= b->n) return set_err(MTH_ERR_ARG, "batch member %d", i);
+  return mth_upload_microstructure(b->rve[i], grain, phase, euler_deg, n_voxels);
+}
+
+extern "C" mth_status mth_batch_step(mth_batch* b, mth_step_report* reports) {
+  if (!b) return set_err(MTH_ERR_ARG, "null batch");
+  CK(cudaSetDevice(b->device));
+  const int n = b->n;
+  for (int i = 0; i < n; i++)
+    if (!b->rve[i]->uploaded) return set_err(MTH_ERR_STATE, "batch member %d has no microstructure", i);
+  for (int i = 0; i < n; i++) {
+    mth_status s = step_begin(b->rve[i]);
+    if (s) return s;
+  }
+  bool recapture = !b->exec;
+  for (int i = 0; i < n && !recapture; i++)
+    recapture = memcmp(&b->cap_nc[i], &b->rve[i]->nc, sizeof(NewtonConst)) != 0;
+  if (recapture) {
+    mth_status s = batch_capture(b);
+    if (s) return s;
+  }
+  std::vector<char> active(n);
+  int nact = 0;
+  for (int i = 0; i < n; i++) nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
+  while (nact > 0) {
+    for (int i = 0; i < n; i++) {
+      b->live_h[i] = active[i];
+      if (active[i]) {
+        iter_add(b->rve[i]);
+        memcpy(b->add_h + (size_t)8 * i, b->rve[i]->add_h, sizeof(double) * 6);
+      }
+    }
+    CK(cudaGraphLaunch(b->exec, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    nact = 0;
+    for (int i = 0; i < n; i++) {
+      if (b->err_h[i]) return set_err(MTH_ERR_TIMEOUT, "batch member %d: a kernel timed out waiting for its tile copies", i);
+      if (!active[i]) continue;
+      mth_status s = iter_finish(b->rve[i], b->red_h + (size_t)BATCH_RED * i);
+      if (s) return s;
+      nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    mth_status s = step_end(b->rve[i], reports ? &reports[i] : nullptr);
+    if (s) return s;
+  }
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_batch_download_field(mth_batch* b, int i, int field, double* host, size_t n_values) {
+  if (!b || i < 0 || i >= b->n) return set_err(MTH_ERR_ARG, "batch member %d", i);
+  return mth_download_field(b->rve[i], field, host, n_values);
+}
+
+extern "C" mth_status mth_batch_destroy(mth_batch* b) {
+  if (!b) return set_err(MTH_ERR_ARG, "null batch");
+  cudaSetDevice(b->device);
+  batch_free(b);
+  return MTH_OK;
+}
+

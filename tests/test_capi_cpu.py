@@ -140,3 +140,13 @@ def test_namelist_dislocation_density_block(lib, tmp_path):
     assert list(par.dd_c) == list(ref.dd_c)
     assert list(par.dd_chi) == list(ref.dd_chi)
     assert ref.flow_law == 1 and par.flow_law == 0   # the law is chosen by the caller (forge --dd)
+
+
+def test_local_solve_rejects_dislocation_density_law(lib):
+    """The array-level local solve has no per-voxel density state: it runs the
+    power law and refuses flow_law = 1 before touching the device."""
+    par = capi.params_from_config(synth.Config(cell_dim=(8, 8, 8), n_grains=2, dd=synth.DD()))
+    a = np.zeros(64)
+    assert lib.mth_local_solve(C.byref(par), capi._dptr(a), 1, capi._dptr(a), capi._dptr(a), capi._dptr(a),
+                               capi._dptr(a), capi._dptr(a), capi._dptr(a), capi._dptr(a), None) == 10
+    assert b"power law" in lib.mth_last_error()
