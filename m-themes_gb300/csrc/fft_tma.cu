@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(NT) fft_s_tma_kernel(const __grid_constant__ C
 // added to the spin accumulator tile, inverse along x.  One block: fixed y,
 // KB consecutive kz.
 template <typename T, int L, int KB>
-__global__ void __launch_bounds__(NT) fft_xg_tma_kernel(const GreenConst gc, const __grid_constant__ CUtensorMap mspec,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) fft_xg_tma_kernel(const GreenConst gc, const __grid_constant__ CUtensorMap mspec,
                                                         const __grid_constant__ CUtensorMap manti, int n1, int n2,
                                                         int kz, const c2<T>* __restrict__ twf,
                                                         const c2<T>* __restrict__ twi, IterIn it, int* err) {

@@ -58,10 +58,13 @@ def test_fp64_matches_oracle_dd_16cube():
     s.close()
 
 
-def test_mixed_dd_within_tolerance():
+@pytest.mark.parametrize("precision", [capi.MTH_MIXED, capi.MTH_MIXED_FAST, capi.MTH_MIXED_ROOT64])
+def test_mixed_dd_within_tolerance(precision):
+    """Every mixed mode runs the dislocation-density law with the FP64
+    Jacobian solve at each Newton step."""
     cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=10, n_steps=5, seed=212, iter_max=40, dd=synth.DD())
     _, r64 = run_gpu(cfg, capi.MTH_FP64)
-    s, rm = run_gpu(cfg, capi.MTH_MIXED)
+    s, rm = run_gpu(cfg, precision)
     for k in range(cfg.n_steps):
         assert rel(rm[k]["sig_avg"], r64[k]["sig_avg"]) < 1e-4, k
         assert np.all(np.abs(rm[k]["dd_avg"] - r64[k]["dd_avg"]) <= 1e-3 * np.abs(r64[k]["dd_avg"]) + 1e-9), k
