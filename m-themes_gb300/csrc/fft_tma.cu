@@ -173,7 +173,7 @@ constexpr int NT = 256;   // threads per block of every TMA pass
 
 // Tile parameters, shared with the host launchers.
 template <typename T> __host__ __device__ constexpr int cw() { return (int)(sizeof(c2<T>) / 8); }   // 8-byte words per complex
-template <typename T> __host__ __device__ constexpr int kb_strided() { return sizeof(T) == 4 ? 8 : 4; }
+template <typename T> __host__ __device__ constexpr int kb_strided() { return sizeof(T) == 4 ? 16 : 4; }
 template <typename T> __host__ __device__ constexpr int kb_green() { return sizeof(T) == 4 ? 4 : 2; }
 template <typename T> __host__ __device__ constexpr int lb_z(int n) {
   int lb = 2048 / (n / 2);
