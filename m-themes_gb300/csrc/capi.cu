@@ -278,7 +278,7 @@ void ctx_free(mth_ctx* c) {
   cudaFree(c->rho_pf_d);
   cudaFree(c->rho_pf_t);
   cudaFree(c->gid_coarse_d);
-  cudaFree(c->ddc_d);
+  delete c->ddc;
   cudaFree(c->dd_mem);
   cudaFree(c->gb_d);
   delete c;
@@ -344,28 +344,44 @@ static mth_status make_twiddles(int n, int sign, void** out) {
 // otherwise; for the system order of the FCC .sx files this is the matrix of
 // InteractionStrengthMatrix, src/init.c:593-702) and the projections of
 // src/init.c:1107-1126.
+// The constants of the dislocation-density law for phase 1, folded in FP64
+// (the reference evaluates the same products and quotients per voxel and
+// system: StrainRate_Orowan src/constitutive.c:507-721, DislocationEvolution
+// src/constitutive.c:1346-1520), with an FP32 copy for the mixed modes.
 static void dd_constants(const mth_params& p, const PhaseConst& ph, DdConst& dc) {
   memset(&dc, 0, sizeof(dc));
   const mth_phase& in = p.phase[0];
+  DdCoef<double>& k = dc.d;
   dc.nsys = ph.nsys;
-  dc.b = p.dd_a0 / sqrt(2.0);
-  dc.G = 0.1 * (in.c11 - in.c12 + 3 * in.c44) +
-         (0.5) * (5 * (in.c11 - in.c12) * in.c44) / (4 * in.c44 + 3 * (in.c11 - in.c12));
-  dc.nu = p.dd_nu;
-  for (int k = 0; k < 8; k++) dc.c[k] = p.dd_c[k];
-  dc.T = p.dd_T;
-  dc.kT = p.dd_T * 1.380658e-23 * (1.0 / 1.60217733e-19);
-  dc.qslip = p.dd_q_slip * 0.62415063631 / dc.kT;
-  dc.qbulk = p.dd_q_bulk * 0.62415063631 / dc.kT;
-  dc.L0 = p.dd_L0;
-  dc.d0 = p.dd_d0;
+  const double* c = p.dd_c;
+  const double b = p.dd_a0 / sqrt(2.0);
+  const double G = 0.1 * (in.c11 - in.c12 + 3 * in.c44) +
+                   (0.5) * (5 * (in.c11 - in.c12) * in.c44) / (4 * in.c44 + 3 * (in.c11 - in.c12));
+  const double kT = p.dd_T * 1.380658e-23 * (1.0 / 1.60217733e-19);   // eV
+  const double j_in_ev = 0.62415063631;
+  const double qslip = p.dd_q_slip * j_in_ev / kT;
+  const double qbulk = p.dd_q_bulk * j_in_ev / kT;
+  k.rm = 2.0 * kT / c[0] / c[1] / c[2] / G / (b * b * b) * 160.2177;
+  k.tp = c[0] * G * b * 1.0e-3;
+  k.tcut = (kT / j_in_ev) / c[1] / c[2] / b / b * 0.1;
+  k.g0 = 1.0e-3 * 1.0e10 * c[1] * b * exp(-qslip);   // attempt frequency 1e10
+  k.dip = sqrt(3.0) * G * b / 16.0 / 3.14159265359 / (1 - p.dd_nu);
+  k.eps = 5.0e-3;
+  k.c4 = c[3];
+  k.c5 = c[4];
+  k.c6 = c[5];
+  k.ann = c[6] * 1.6 * 1E12 * 1E-9;
+  k.clb = 4 * 1E12 * (p.dd_d0 / b);
+  k.clb_h = b * b * b * 100 / (1.38 * p.dd_T);
+  k.clb_0 = -1.0 - qbulk;
+  k.gnd = 1.0 / b / p.dd_L0;
   const int ns = ph.nsys;
   for (int i = 0; i < ns; i++) {
-    for (int k = 0; k < 5; k++) dc.m_xt[i][k] = ph.m_xt[i][k];
-    for (int m = 0; m < 3; m++) dc.bb[i][m] = ph.bb[i][m];
-    dc.bp[i][0] = ph.bb[i][1] * ph.bn[i][2] - ph.bb[i][2] * ph.bn[i][1];
-    dc.bp[i][1] = ph.bb[i][2] * ph.bn[i][0] - ph.bb[i][0] * ph.bn[i][2];
-    dc.bp[i][2] = ph.bb[i][0] * ph.bn[i][1] - ph.bb[i][1] * ph.bn[i][0];
+    for (int m = 0; m < 5; m++) k.m[i][m] = ph.m_xt[i][m];
+    for (int m = 0; m < 3; m++) k.bb[i][m] = ph.bb[i][m];
+    k.bp[i][0] = ph.bb[i][1] * ph.bn[i][2] - ph.bb[i][2] * ph.bn[i][1];
+    k.bp[i][1] = ph.bb[i][2] * ph.bn[i][0] - ph.bb[i][0] * ph.bn[i][2];
+    k.bp[i][2] = ph.bb[i][0] * ph.bn[i][1] - ph.bb[i][1] * ph.bn[i][0];
   }
   auto dot3 = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
   for (int i = 0; i < ns; i++)
@@ -384,22 +400,20 @@ static void dd_constants(const mth_params& p, const PhaseConst& ph, DdConst& dc)
         const double q[3] = {bi[0] - sg * bj[0], bi[1] - sg * bj[1], bi[2] - sg * bj[2]};
         chi = (fabs(dot3(q, ni)) < 1e-6 || fabs(dot3(q, nj)) < 1e-6) ? p.dd_chi[3] : p.dd_chi[5];
       }
-      dc.chi[i][j] = chi;
+      k.chi[i][j] = chi;
       const double sv[3] = {nj[1] * bj[2] - nj[2] * bj[1], nj[2] * bj[0] - nj[0] * bj[2], nj[0] * bj[1] - nj[1] * bj[0]};
-      dc.cs[i][j] = fabs(dot3(ni, sv));
-      dc.ss[i][j] = fabs(sqrt(fabs(1.0 - dc.cs[i][j] * dc.cs[i][j])));
-      dc.cg1[i][j] = fabs(dot3(ni, bj));
-      dc.sg1[i][j] = fabs(sqrt(fabs(1.0 - dc.cg1[i][j] * dc.cg1[i][j])));
-      dc.cg3[i][j] = fabs(dot3(ni, nj));
-      dc.sg3[i][j] = fabs(sqrt(fabs(1.0 - dc.cg3[i][j] * dc.cg3[i][j])));
-      dc.chif[i][j] = (float)dc.chi[i][j];
-      dc.csf[i][j] = (float)dc.cs[i][j];
-      dc.ssf[i][j] = (float)dc.ss[i][j];
-      dc.cg1f[i][j] = (float)dc.cg1[i][j];
-      dc.sg1f[i][j] = (float)dc.sg1[i][j];
-      dc.cg3f[i][j] = (float)dc.cg3[i][j];
-      dc.sg3f[i][j] = (float)dc.sg3[i][j];
+      k.cs[i][j] = fabs(dot3(ni, sv));
+      k.ss[i][j] = fabs(sqrt(fabs(1.0 - k.cs[i][j] * k.cs[i][j])));
+      k.cg1[i][j] = fabs(dot3(ni, bj));
+      k.sg1[i][j] = fabs(sqrt(fabs(1.0 - k.cg1[i][j] * k.cg1[i][j])));
+      k.cg3[i][j] = fabs(dot3(ni, nj));
+      k.sg3[i][j] = fabs(sqrt(fabs(1.0 - k.cg3[i][j] * k.cg3[i][j])));
     }
+  // FP32 copy: every member is a double, in declaration order
+  static_assert(sizeof(DdCoef<double>) == 2 * sizeof(DdCoef<float>), "DdCoef holds only T members");
+  const double* src = reinterpret_cast<const double*>(&dc.d);
+  float* dst = reinterpret_cast<float*>(&dc.f);
+  for (size_t i = 0; i < sizeof(DdCoef<float>) / sizeof(float); i++) dst[i] = (float)src[i];
 }
 
 extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
@@ -576,10 +590,8 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   if (c->mixed) carve(static_cast<float*>(c->fieldmem), c->ff);
   else carve(static_cast<double*>(c->fieldmem), c->fd);
   if (c->dd) {
-    DdConst dc;
-    dd_constants(*p, c->nc.ph[0], dc);
-    CKC(cudaMalloc(&c->ddc_d, sizeof(DdConst)));
-    CKC(cudaMemcpy(c->ddc_d, &dc, sizeof(DdConst), cudaMemcpyHostToDevice));
+    c->ddc = new DdConst;
+    dd_constants(*p, c->nc.ph[0], *c->ddc);
     CKC(cudaMalloc(&c->dd_mem, esz * P * (7 * NSYS + 3 * NSYS)));
     CKC(cudaMalloc(&c->gb_d, P));
     auto carve_dd = [&](auto* base, auto& d, auto& f) {
@@ -1132,7 +1144,7 @@ mth_status step_begin(mth_ctx* c) {
     const void* dd = c->mixed ? (const void*)&c->ddf : (const void*)&c->ddd;
     const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
     const double w = c->mixed ? 4.0 : 8.0;
-    LAUNCH(K_DD, (double)c->nv * w * (4 * NSYS + 3 * NSYS), launch_dd_prep(c->mixed, c->ddc_d, dd, f, c->st));
+    LAUNCH(K_DD, (double)c->nv * w * (4 * NSYS + 3 * NSYS), launch_dd_prep(c->mixed, *c->ddc, dd, f, c->st));
   }
   memset(c->ddg, 0, sizeof(c->ddg));
   memset(c->ddg_acum, 0, sizeof(c->ddg_acum));
@@ -1224,10 +1236,10 @@ mth_status step_end(mth_ctx* c, mth_step_report* rep) {
     // before the lattice rotation of end_step
     const void* dd = c->mixed ? (const void*)&c->ddf : (const void*)&c->ddd;
     const double w = c->mixed ? 4.0 : 8.0, nv = (double)c->nv;
-    LAUNCH(K_DD, nv * w * (6 + 9 + 3 * NSYS + NSYS), launch_dd_gamdot(c->mixed, c->ddc_d, dd, f, c->nc.flow_off, c->st));
+    LAUNCH(K_DD, nv * w * (6 + 9 + 3 * NSYS + NSYS), launch_dd_gamdot(c->mixed, *c->ddc, dd, f, c->nc.flow_off, c->st));
     const int do_grad = (c->p.hard_flag == 1 && istep > 1) ? 1 : 0;
     LAUNCH(K_DD, nv * w * (6 + 9 + 7 * NSYS + 5 * NSYS) + nv,
-           launch_dd_evolve(c->mixed, c->ddc_d, dd, f, c->n, dt, do_grad, c->partials, c->st));
+           launch_dd_evolve(c->mixed, *c->ddc, dd, f, c->n, dt, do_grad, c->partials, c->st));
     double red[NPART_DD];
     mth_status s = reduce_to_host(c, NPART_DD, red);
     if (s) return s;

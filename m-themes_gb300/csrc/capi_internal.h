@@ -146,7 +146,7 @@ struct mth_ctx {
   double last_au[3];    // uniform spin increment of the last end of step
   // dislocation-density law
   int dd;
-  DdConst* ddc_d;       // device copy of the phase-1 constants
+  DdConst* ddc;         // phase-1 constants of the dislocation-density law (host; kernel parameters)
   void* dd_mem;         // 84 state planes + 36 per-step constant planes
   DdFields<float> ddf;
   DdFields<double> ddd;

@@ -12,8 +12,11 @@
 // differs from the current one only at the first evaluation of a step; the
 // converged stress is the same.)
 //
-// Arithmetic in FP64 except the forest/parallel sums, which run in the field
-// precision (FP32 in the mixed modes); the densities are stored in it too.
+// Arithmetic in the field precision T (FP32 in the mixed modes, where the
+// densities are stored in it too), with the material coefficients folded on
+// the host in FP64 (DdCoef) and passed as kernel parameters; the per-block
+// sums of the dd.out averages are FP64.  Loops over the slip systems are
+// unrolled over the NSYS slots so the per-system values stay in registers.
 #include <cstdio>
 #include "mth_common.cuh"
 #include "mth_internal.h"
@@ -21,12 +24,6 @@
 namespace mth {
 
 namespace {
-
-constexpr double DD_TAU0 = 1000.0;       // tau_0 of StrainRate_Orowan
-constexpr double DD_TRIAL_FREQ = 1.0e10; // TRIAL_FREQ_DRX
-constexpr double DD_MY_J_IN_EV = 0.62415063631;
-constexpr double DD_PI = 3.14159265359;
-constexpr double DD_EPS = 5.0e-3;        // EPSILON seen by DislocationEvolution
 
 template <int W>
 __device__ __forceinline__ void dd_block_sum(double (&v)[W], double* out) {
@@ -47,112 +44,125 @@ __device__ __forceinline__ void dd_block_sum(double (&v)[W], double* out) {
   }
 }
 
-// forest and parallel densities of every system of voxel v (from the
-// densities at the start of the step), summed in the field precision T
-// (the 12 x 12 sums are the bulk of the density kernels' arithmetic)
+// the densities of voxel v at the start of the step that the forest and
+// parallel sums read: rho_s and |rho_GND| (3 kinds) of every system
 template <typename T>
-__device__ __forceinline__ void forest_parallel(const DdConst& dc, const DdFields<T>& d, long long P, long long v,
-                                                double* rf, double* rp) {
+struct DdLocal {
   T s[NSYS], a1[NSYS], a2[NSYS], a3[NSYS];
+};
+template <typename T>
+__device__ __forceinline__ void load_local(int nsys, const DdFields<T>& d, long long P, long long v, DdLocal<T>& l) {
+#pragma unroll
   for (int j = 0; j < NSYS; j++) {
-    s[j] = d.rho_s[j * P + v];
-    a1[j] = fabs(d.g1[j * P + v]);
-    a2[j] = fabs(d.g2[j * P + v]);
-    a3[j] = fabs(d.g3[j * P + v]);
-  }
-  for (int i = 0; i < dc.nsys; i++) {
-    T f = 0, p = 0;
-    for (int j = 0; j < dc.nsys; j++) {
-      const T chi = cpick<T>(dc.chi[i][j], dc.chif[i][j]), cs = cpick<T>(dc.cs[i][j], dc.csf[i][j]);
-      const T ss = cpick<T>(dc.ss[i][j], dc.ssf[i][j]);
-      f += chi * (s[j] * cs + a1[j] * cpick<T>(dc.cg1[i][j], dc.cg1f[i][j]) + a2[j] * cs +
-                  a3[j] * cpick<T>(dc.cg3[i][j], dc.cg3f[i][j]));
-      p += chi * (s[j] * ss + a1[j] * cpick<T>(dc.sg1[i][j], dc.sg1f[i][j]) + a2[j] * ss +
-                  a3[j] * cpick<T>(dc.sg3[i][j], dc.sg3f[i][j]));
+    if (j < nsys) {
+      l.s[j] = d.rho_s[j * P + v];
+      l.a1[j] = fabs(d.g1[j * P + v]);
+      l.a2[j] = fabs(d.g2[j * P + v]);
+      l.a3[j] = fabs(d.g3[j * P + v]);
+    } else {
+      l.s[j] = l.a1[j] = l.a2[j] = l.a3[j] = (T)0;
     }
-    rf[i] = (double)f;
-    rp[i] = (double)p;
+  }
+}
+// forest (rf) and parallel (rp) density of system i
+template <typename T>
+__device__ __forceinline__ void forest_parallel(const DdCoef<T>& k, int i, const DdLocal<T>& l, T& rf, T& rp) {
+  T f = 0, p = 0;
+#pragma unroll
+  for (int j = 0; j < NSYS; j++) {
+    f += k.chi[i][j] * (l.s[j] * k.cs[i][j] + l.a1[j] * k.cg1[i][j] + l.a2[j] * k.cs[i][j] + l.a3[j] * k.cg3[i][j]);
+    p += k.chi[i][j] * (l.s[j] * k.ss[i][j] + l.a1[j] * k.sg1[i][j] + l.a2[j] * k.ss[i][j] + l.a3[j] * k.sg3[i][j]);
+  }
+  rf = f;
+  rp = p;
+}
+
+// deviatoric stress of voxel v in crystal axes
+template <typename T>
+__device__ __forceinline__ void crystal_stress(const Fields<T>& f, long long P, long long v, T (&x)[5]) {
+  T R[9], Q[25], s6[5];
+#pragma unroll
+  for (int i = 0; i < 9; i++) R[i] = f.rot[i * P + v];
+#pragma unroll
+  for (int i = 0; i < 5; i++) s6[i] = f.sig[i * P + v];
+  rot_to_q<T>(R, Q);
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    T a = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) a += Q[i * 5 + j] * s6[j];
+    x[i] = a;
   }
 }
 
-__device__ __forceinline__ double mobile_density(const DdConst& dc, double rf, double rp) {
-  const double b = dc.b;
-  return 2.0 * dc.kT / dc.c[0] / dc.c[1] / dc.c[2] / dc.G / (b * b * b) * sqrt(rp * rf) * 160.2177;
+template <typename T>
+__device__ __forceinline__ T resolved(const DdCoef<T>& k, int s, const T (&x)[5]) {
+  return k.m[s][0] * x[0] + k.m[s][1] * x[1] + k.m[s][2] * x[2] + k.m[s][3] * x[3] + k.m[s][4] * x[4];
 }
 
 // passing stress, tau_0 + cutting stress and reference rate per system
 template <typename T>
-__global__ void __launch_bounds__(256) dd_prep_kernel(const DdConst* __restrict__ dcp, DdFields<T> d, Fields<T> f) {
+__global__ void __launch_bounds__(256) dd_prep_kernel(const DdCoef<T> k, int nsys, DdFields<T> d, Fields<T> f) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   if (v >= P) return;
-  const DdConst& dc = *dcp;
   const bool crystal = f.phase[v] == 0;
-  double rf[NSYS], rp[NSYS];
-  if (crystal) forest_parallel(dc, d, P, v, rf, rp);
-  const double b = dc.b, c1 = dc.c[0], c2 = dc.c[1], c3 = dc.c[2];
+  DdLocal<T> l;
+  if (crystal) load_local(nsys, d, P, v, l);
+#pragma unroll
   for (int i = 0; i < NSYS; i++) {
-    double tp = 0.0, td = 1.0, g0 = 0.0;
-    if (crystal && i < dc.nsys) {
-      const double rm = mobile_density(dc, rf[i], rp[i]);
-      tp = c1 * dc.G * b * sqrt(fabs(rp[i] + rm)) * 1.0e-3;
-      const double tcut = (dc.kT / DD_MY_J_IN_EV) * sqrt(rf[i]) / c2 / c3 / b / b * 0.1;
-      td = DD_TAU0 + tcut;
-      g0 = 1.0e-3 * rm * DD_TRIAL_FREQ * c2 * b * exp(-1.0 * dc.qslip) / sqrt(rf[i]);
+    T tp = 0, td = 1, g0 = 0;
+    if (crystal && i < nsys) {
+      T rf, rp;
+      forest_parallel(k, i, l, rf, rp);
+      const T sf = sqrt(rf);
+      const T rm = k.rm * sqrt(rp * rf);
+      tp = k.tp * sqrt(fabs(rp + rm));
+      td = (T)1000 + k.tcut * sf;   // tau_0 + cutting stress
+      g0 = k.g0 * rm / sf;
     }
-    f.ddc[i * P + v] = (T)tp;
-    f.ddc[(NSYS + i) * P + v] = (T)td;
-    f.ddc[(2 * NSYS + i) * P + v] = (T)g0;
+    f.ddc[i * P + v] = tp;
+    f.ddc[(NSYS + i) * P + v] = td;
+    f.ddc[(2 * NSYS + i) * P + v] = g0;
   }
 }
 
 // shear rates at the converged stress (the last flow-rule evaluation of the
 // step); 0 in gas voxels
 template <typename T>
-__global__ void __launch_bounds__(256) dd_gamdot_kernel(const DdConst* __restrict__ dcp, DdFields<T> d, Fields<T> f,
+__global__ void __launch_bounds__(256) dd_gamdot_kernel(const DdCoef<T> k, int nsys, DdFields<T> d, Fields<T> f,
                                                         int flow_off) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   if (v >= P) return;
-  const DdConst& dc = *dcp;
-  double x[5] = {0, 0, 0, 0, 0};
+  T x[5] = {0, 0, 0, 0, 0};
   const bool active = f.phase[v] == 0 && !flow_off;
-  if (active) {
-    double R[9], Q[25], s6[5];
-    for (int i = 0; i < 9; i++) R[i] = (double)f.rot[i * P + v];
-    for (int i = 0; i < 5; i++) s6[i] = (double)f.sig[i * P + v];
-    rot_to_q<double>(R, Q);
-    for (int i = 0; i < 5; i++) {
-      double a = 0;
-      for (int j = 0; j < 5; j++) a += Q[i * 5 + j] * s6[j];
-      x[i] = a;
-    }
-  }
+  if (active) crystal_stress(f, P, v, x);
+#pragma unroll
   for (int s = 0; s < NSYS; s++) {
-    double g = 0.0;
-    if (active && s < dc.nsys) {
-      double rss = 0;
-      for (int i = 0; i < 5; i++) rss += dc.m_xt[s][i] * x[i];
-      const double tp = (double)f.ddc[s * P + v], td = (double)f.ddc[(NSYS + s) * P + v];
-      const double g0 = (double)f.ddc[(2 * NSYS + s) * P + v];
-      if (fabs(rss) > tp) g = g0 * sinh((fabs(rss) - tp) / td) * (rss > 0.0 ? 1.0 : -1.0);
+    T g = 0;
+    if (active && s < nsys) {
+      const T rss = resolved(k, s, x);
+      const T tp = f.ddc[s * P + v], td = f.ddc[(NSYS + s) * P + v];
+      const T g0 = f.ddc[(2 * NSYS + s) * P + v];
+      if (fabs(rss) > tp) g = g0 * sinh((fabs(rss) - tp) / td) * (rss > (T)0 ? (T)1 : (T)-1);
     }
-    d.gamdot[s * P + v] = (T)g;
+    d.gamdot[s * P + v] = g;
   }
 }
 
 // DislocationEvolution + the per-block sums of AvgDislocation: rho_F,
 // rho_P, rho_m (densities before the update, as the last flow evaluation
-// saw them), rho_s, |rho_GND|, rho_dipole, rho_forest (after it).
+// saw them), rho_s, |rho_GND|, rho_dipole, rho_forest (after it).  The
+// per-voxel sums over the systems are in T, the block sums in FP64.
 template <typename T>
-__global__ void __launch_bounds__(256) dd_evolve_kernel(const DdConst* __restrict__ dcp, DdFields<T> d, Fields<T> f,
-                                                        int n0, int n1, int n2, double dt, int do_grad,
+__global__ void __launch_bounds__(256) dd_evolve_kernel(const DdCoef<T> k, int nsys, DdFields<T> d, Fields<T> f,
+                                                        int n0, int n1, int n2, T dt, int do_grad,
                                                         double* __restrict__ partials) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   if (v < P && f.phase[v] == 0) {
-    const DdConst& dc = *dcp;
     const int z = (int)(v % n2), y = (int)((v / n2) % n1), x = (int)(v / ((long long)n1 * n2));
     // neighbours +x, -x, +y, -y, +z, -z (periodic)
     long long nb[6];
@@ -163,61 +173,64 @@ __global__ void __launch_bounds__(256) dd_evolve_kernel(const DdConst* __restric
     nb[4] = ((long long)x * n1 + y) * n2 + (z + 1) % n2;
     nb[5] = ((long long)x * n1 + y) * n2 + (z + n2 - 1) % n2;
     const unsigned gb = d.gb[v];
-    double rf[NSYS], rp[NSYS];
-    forest_parallel(dc, d, P, v, rf, rp);
-    double R[9], Q[25], s6[6], xs[5];
-    for (int i = 0; i < 9; i++) R[i] = (double)f.rot[i * P + v];
-    for (int i = 0; i < 6; i++) s6[i] = (double)f.sig[i * P + v];
-    rot_to_q<double>(R, Q);
-    for (int i = 0; i < 5; i++) {
-      double a = 0;
-      for (int j = 0; j < 5; j++) a += Q[i * 5 + j] * s6[j];
-      xs[i] = a;
-    }
-    const double hydro = (s6[0] + s6[1] + s6[2]) / 3.0;   // LT components 0..2, as DislocationEvolution
-    const double b = dc.b, c4 = dc.c[3], c5 = dc.c[4], c6 = dc.c[5], c7 = dc.c[6];
-    const double climb = exp((fabs(hydro) * b * b * b * 100 / (1.38 * dc.T)) - 1.0) * exp(-1.0 * dc.qbulk);
-    for (int i = 0; i < dc.nsys; i++) {
-      const double gd = (double)d.gamdot[i * P + v];
-      double grad[3] = {0.0, 0.0, 0.0};
-      if (do_grad) {
-        for (int a = 0; a < 3; a++) {
-          const int up = (gb >> (2 * a)) & 1, dn = (gb >> (2 * a + 1)) & 1;
-          const double gp = (double)d.gamdot[i * P + nb[2 * a]], gm = (double)d.gamdot[i * P + nb[2 * a + 1]];
-          if (!up && dn) grad[a] = gd - gm;
-          else if (up && !dn) grad[a] = gp - gd;
-          else if (up && dn) grad[a] = (gp - gm) / 2.0;
+    DdLocal<T> l;
+    load_local(nsys, d, P, v, l);
+    T xs[5];
+    crystal_stress(f, P, v, xs);
+    // LT components 0..2, as DislocationEvolution
+    const T hydro = (f.sig[v] + f.sig[P + v] + f.sig[2 * P + v]) / (T)3;
+    const T climb = exp(fabs(hydro) * k.clb_h + k.clb_0);
+    const T gdt = k.gnd * dt;
+    T sum[7] = {0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < NSYS; i++) {
+      if (i < nsys) {
+        const T gd = d.gamdot[i * P + v];
+        T grad[3] = {0, 0, 0};
+        if (do_grad) {
+#pragma unroll
+          for (int a = 0; a < 3; a++) {
+            const int up = (gb >> (2 * a)) & 1, dn = (gb >> (2 * a + 1)) & 1;
+            const T gp = d.gamdot[i * P + nb[2 * a]], gm = d.gamdot[i * P + nb[2 * a + 1]];
+            if (!up && dn) grad[a] = gd - gm;
+            else if (up && !dn) grad[a] = gp - gd;
+            else if (up && dn) grad[a] = (gp - gm) / (T)2;
+          }
         }
+        T rf, rp;
+        forest_parallel(k, i, l, rf, rp);
+        const T rss = resolved(k, i, xs);
+        const T sf = sqrt(rf);
+        const T rm = k.rm * sqrt(rp * rf);
+        const T d_dipole = k.dip / (fabs(rss) + k.eps);
+        const T ag = fabs(gd);
+        const T dip = d.dipole[i * P + v] + ag * (k.c6 * d_dipole * rm) * dt;
+        const T fst = d.forest[i * P + v] + ag * (k.c4 * sf) * dt;
+        const T rs = l.s[i];
+        const T dot_ssd = ag * (k.c4 * sf + k.c6 * d_dipole * rm - k.c5 * rs) - k.ann * rs * rs -
+                          k.clb * d_dipole * rs * rs * climb;
+        const T rs_n = rs + dot_ssd * dt;
+        const T g_screw = grad[0] * k.bp[i][0] + grad[1] * k.bp[i][1] + grad[2] * k.bp[i][2];
+        const T g_edge = grad[0] * k.bb[i][0] + grad[1] * k.bb[i][1] + grad[2] * k.bb[i][2];
+        const T g1 = d.g1[i * P + v] + g_screw * gdt;
+        const T g2 = d.g2[i * P + v] - g_edge * gdt;
+        const T g3 = d.g3[i * P + v];
+        d.dipole[i * P + v] = dip;
+        d.forest[i * P + v] = fst;
+        d.rho_s[i * P + v] = rs_n;
+        d.g1[i * P + v] = g1;
+        d.g2[i * P + v] = g2;
+        sum[0] += rf;
+        sum[1] += rp;
+        sum[2] += rs_n;
+        sum[3] += rm;
+        sum[4] += sqrt(g1 * g1 + g2 * g2 + g3 * g3);
+        sum[5] += dip;
+        sum[6] += fst;
       }
-      double rss = 0;
-      for (int k = 0; k < 5; k++) rss += dc.m_xt[i][k] * xs[k];
-      const double rm = mobile_density(dc, rf[i], rp[i]);
-      const double d_dipole = sqrt(3.0) * dc.G * b / 16.0 / DD_PI / (1 - dc.nu) / (fabs(rss) + DD_EPS);
-      const double ag = fabs(gd);
-      const double dip = (double)d.dipole[i * P + v] + ag * (c6 * d_dipole * rm) * dt;
-      const double fst = (double)d.forest[i * P + v] + ag * (c4 * sqrt(rf[i])) * dt;
-      const double rs = (double)d.rho_s[i * P + v];
-      const double dot_ssd = ag * (c4 * sqrt(rf[i]) + c6 * d_dipole * rm - c5 * rs) - c7 * 1.6 * 1E12 * 1E-9 * rs * rs -
-                             4 * 1E12 * d_dipole * (dc.d0 / b) * rs * rs * climb;
-      const double rs_n = rs + dot_ssd * dt;
-      const double g_screw = grad[0] * dc.bp[i][0] + grad[1] * dc.bp[i][1] + grad[2] * dc.bp[i][2];
-      const double g_edge = grad[0] * dc.bb[i][0] + grad[1] * dc.bb[i][1] + grad[2] * dc.bb[i][2];
-      const double g1 = (double)d.g1[i * P + v] + g_screw / b / dc.L0 * dt;
-      const double g2 = (double)d.g2[i * P + v] + (-1.0 * g_edge) / b / dc.L0 * dt;
-      const double g3 = (double)d.g3[i * P + v];
-      d.dipole[i * P + v] = (T)dip;
-      d.forest[i * P + v] = (T)fst;
-      d.rho_s[i * P + v] = (T)rs_n;
-      d.g1[i * P + v] = (T)g1;
-      d.g2[i * P + v] = (T)g2;
-      acc[0] += rf[i];
-      acc[1] += rp[i];
-      acc[2] += rs_n;
-      acc[3] += rm;
-      acc[4] += sqrt(g1 * g1 + g2 * g2 + g3 * g3);
-      acc[5] += dip;
-      acc[6] += fst;
     }
+#pragma unroll
+    for (int j = 0; j < 7; j++) acc[j] = (double)sum[j];
   }
   dd_block_sum<7>(acc, partials);
 }
@@ -248,40 +261,42 @@ cudaError_t launch_dd_init(int mixed, const void* dd, const uint8_t* phase, long
   return cudaGetLastError();
 }
 
-cudaError_t launch_dd_prep(int mixed, const DdConst* dc, const void* dd, const void* fields, cudaStream_t st) {
+cudaError_t launch_dd_prep(int mixed, const DdConst& dc, const void* dd, const void* fields, cudaStream_t st) {
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    dd_prep_kernel<float><<<blocks_of(f.nv), 256, 0, st>>>(dc, *static_cast<const DdFields<float>*>(dd), f);
+    dd_prep_kernel<float><<<blocks_of(f.nv), 256, 0, st>>>(dc.f, dc.nsys, *static_cast<const DdFields<float>*>(dd), f);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    dd_prep_kernel<double><<<blocks_of(f.nv), 256, 0, st>>>(dc, *static_cast<const DdFields<double>*>(dd), f);
+    dd_prep_kernel<double><<<blocks_of(f.nv), 256, 0, st>>>(dc.d, dc.nsys, *static_cast<const DdFields<double>*>(dd), f);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_dd_gamdot(int mixed, const DdConst* dc, const void* dd, const void* fields, int flow_off,
+cudaError_t launch_dd_gamdot(int mixed, const DdConst& dc, const void* dd, const void* fields, int flow_off,
                              cudaStream_t st) {
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    dd_gamdot_kernel<float><<<blocks_of(f.nv), 256, 0, st>>>(dc, *static_cast<const DdFields<float>*>(dd), f, flow_off);
+    dd_gamdot_kernel<float><<<blocks_of(f.nv), 256, 0, st>>>(dc.f, dc.nsys, *static_cast<const DdFields<float>*>(dd),
+                                                             f, flow_off);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    dd_gamdot_kernel<double><<<blocks_of(f.nv), 256, 0, st>>>(dc, *static_cast<const DdFields<double>*>(dd), f,
-                                                              flow_off);
+    dd_gamdot_kernel<double><<<blocks_of(f.nv), 256, 0, st>>>(dc.d, dc.nsys, *static_cast<const DdFields<double>*>(dd),
+                                                              f, flow_off);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_dd_evolve(int mixed, const DdConst* dc, const void* dd, const void* fields, const int dims[3],
+cudaError_t launch_dd_evolve(int mixed, const DdConst& dc, const void* dd, const void* fields, const int dims[3],
                              double dt, int do_grad, double* partials, cudaStream_t st) {
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    dd_evolve_kernel<float><<<blocks_of(f.nv), 256, 0, st>>>(dc, *static_cast<const DdFields<float>*>(dd), f, dims[0],
-                                                             dims[1], dims[2], dt, do_grad, partials);
+    dd_evolve_kernel<float><<<blocks_of(f.nv), 256, 0, st>>>(dc.f, dc.nsys, *static_cast<const DdFields<float>*>(dd),
+                                                             f, dims[0], dims[1], dims[2], (float)dt, do_grad,
+                                                             partials);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    dd_evolve_kernel<double><<<blocks_of(f.nv), 256, 0, st>>>(dc, *static_cast<const DdFields<double>*>(dd), f,
-                                                              dims[0], dims[1], dims[2], dt, do_grad, partials);
+    dd_evolve_kernel<double><<<blocks_of(f.nv), 256, 0, st>>>(dc.d, dc.nsys, *static_cast<const DdFields<double>*>(dd),
+                                                              f, dims[0], dims[1], dims[2], dt, do_grad, partials);
   }
   return cudaGetLastError();
 }

@@ -199,15 +199,32 @@ cudaError_t launch_gather_rot(int mixed, const void* rot, long long nv, const lo
 // energies, L0, D_0, T; junction strengths and the projection cosines/sines
 // of the forest and parallel densities (src/init.c:1096-1126); crystal-axes
 // Schmid vectors, screw sense vectors b x n and slip directions.
+// Constants of the dislocation-density law in precision T: the material
+// coefficients of StrainRate_Orowan and DislocationEvolution folded on the
+// host in FP64, the slip-system geometry and the 12 x 12 projection tables.
+// The density kernels take them by value, so they are read from the
+// kernel-parameter constant bank.
+template <typename T>
+struct DdCoef {
+  T rm;      // rho_m = rm sqrt(rho_P rho_F)
+  T tp;      // tau_pass = tp sqrt(|rho_P + rho_m|)
+  T tcut;    // tau_cut = tcut sqrt(rho_F)
+  T g0;      // gdot_0 = g0 rho_m / sqrt(rho_F)
+  T dip;     // d_dipole = dip / (|rss| + eps)
+  T eps;
+  T c4, c5, c6;
+  T ann;     // thermal annihilation: ann rho_s^2
+  T clb;     // climb: clb d_dipole rho_s^2 exp(clb_h |p| + clb_0), p the hydrostatic stress
+  T clb_h, clb_0;
+  T gnd;     // GND rate per shear-rate gradient: 1 / (b L0)
+  T m[NSYS][5], bp[NSYS][3], bb[NSYS][3];
+  T chi[NSYS][NSYS], cs[NSYS][NSYS], ss[NSYS][NSYS], cg1[NSYS][NSYS], sg1[NSYS][NSYS], cg3[NSYS][NSYS],
+      sg3[NSYS][NSYS];
+};
 struct DdConst {
   int nsys;
-  double b, G, nu, c[8], kT, qslip, qbulk, L0, d0, T;
-  double chi[NSYS][NSYS], cs[NSYS][NSYS], ss[NSYS][NSYS], cg1[NSYS][NSYS], sg1[NSYS][NSYS], cg3[NSYS][NSYS],
-      sg3[NSYS][NSYS];
-  double m_xt[NSYS][5], bp[NSYS][3], bb[NSYS][3];
-  // float copies of the projection tables for the FP32 forest/parallel sums
-  float chif[NSYS][NSYS], csf[NSYS][NSYS], ssf[NSYS][NSYS], cg1f[NSYS][NSYS], sg1f[NSYS][NSYS], cg3f[NSYS][NSYS],
-      sg3f[NSYS][NSYS];
+  DdCoef<double> d;
+  DdCoef<float> f;
 };
 // Per-voxel state, 12 planes each (voxel index fastest).
 template <typename T>
@@ -222,10 +239,10 @@ struct DdFields {
   const uint8_t* gb;   // per voxel: bit 2a / 2a+1 = neighbour +/- along axis a in the same grain
 };
 cudaError_t launch_dd_init(int mixed, const void* dd, const uint8_t* phase, long long P, double rho0, cudaStream_t st);
-cudaError_t launch_dd_prep(int mixed, const DdConst* dc, const void* dd, const void* fields, cudaStream_t st);
-cudaError_t launch_dd_gamdot(int mixed, const DdConst* dc, const void* dd, const void* fields, int flow_off,
+cudaError_t launch_dd_prep(int mixed, const DdConst& dc, const void* dd, const void* fields, cudaStream_t st);
+cudaError_t launch_dd_gamdot(int mixed, const DdConst& dc, const void* dd, const void* fields, int flow_off,
                              cudaStream_t st);
-cudaError_t launch_dd_evolve(int mixed, const DdConst* dc, const void* dd, const void* fields, const int dims[3],
+cudaError_t launch_dd_evolve(int mixed, const DdConst& dc, const void* dd, const void* fields, const int dims[3],
                              double dt, int do_grad, double* partials, cudaStream_t st);
 constexpr int NPART_DD = 7;
 
