@@ -109,4 +109,44 @@ __host__ __device__ __forceinline__ float cpick<float>(double, float f) { return
 template <>
 __host__ __device__ __forceinline__ double cpick<double>(double d, float) { return d; }
 
+#ifdef __CUDACC__
+// FP32 <-> FP64 conversions by integer operations on the two words of the
+// double: GB300 executes F2F conversions on its FP64 pipe (1/64 of the FP32
+// rate), these run on the integer pipes.  f32_to_f64 is exact for normal
+// numbers, zeros, infinities and NaNs and flushes FP32 subnormals to signed
+// zero.  f64_to_f32 rounds to nearest even, as the hardware conversion does,
+// for results in the FP32 normal range, flushes smaller magnitudes to signed
+// zero, and returns +-inf above the range and a quiet NaN for a NaN.
+__device__ __forceinline__ double f32_to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned sgn = u & 0x80000000u, mag = u & 0x7fffffffu;
+  // exponent bias 127 -> 1023: add (1023 - 127) << 20 to the high word
+  unsigned hi = sgn | ((mag >> 3) + (896u << 20));
+  unsigned lo = u << 29;
+  if (mag < 0x00800000u) {          // zero or subnormal
+    hi = sgn;
+    lo = 0u;
+  } else if (mag >= 0x7f800000u) {  // inf or NaN: all-ones exponent, same mantissa
+    hi |= 0x7ff00000u;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ float f64_to_f32(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sgn = hi & 0x80000000u, mhi = hi & 0x7fffffffu;
+  const int e = (int)(mhi >> 20) - 896;   // FP32 biased exponent
+  // exponent and the top 23 mantissa bits (meaningful for 0 < e < 255)
+  unsigned b = ((mhi - (896u << 20)) << 3) | (lo >> 29);
+  const unsigned r = lo & 0x1fffffffu;    // the 29 bits rounded off
+  // round to nearest even; a carry out of the mantissa steps the exponent
+  // (to inf from the largest binade)
+  b += (r > 0x10000000u || (r == 0x10000000u && (b & 1u))) ? 1u : 0u;
+  if (e <= 0) b = 0u;
+  else if (e >= 255) b = (mhi > 0x7ff00000u || (mhi == 0x7ff00000u && lo != 0u)) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float(sgn | b);
+}
+__device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
+__device__ __forceinline__ double to_f64(double x) { return x; }
+#endif
+
 }  // namespace mth

@@ -242,24 +242,32 @@ __device__ __forceinline__ T pivot_inv(T d) {
   else return (T)1 / d;
 }
 
+// dj > 0 for a pivot; for the FP64 solves of the mixed modes (NR) tested on
+// the high word with integer operations instead of an FP64 compare: a
+// positive finite double has a high word in [1, 0x7fefffff] (this also
+// rejects +inf and the subnormals below 2^-1042, which the reciprocal
+// estimate flushes).
+template <typename T, bool NR>
+__device__ __forceinline__ bool pivot_positive(T d) {
+  if constexpr (NR && sizeof(T) == 8) return (unsigned)__double2hiint(d) - 1u < 0x7fefffffu;
+  else return d > (T)0;
+}
+
 // LDL^T solve of the packed symmetric positive definite 5x5 matrix A:
 // x = A^-1 b.  Returns false when a pivot is not positive.  NR: pivot
 // reciprocals by pivot_rcp_nr (FP64 solves of the mixed modes).
 template <typename T, bool NR = false>
 __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
-  T L[5][5], d[5], id[5];
+  // U[i][k] = L[i][k] d[k], the column before its scaling by 1/d[k], kept so
+  // the updates need no products L d
+  T L[5][5], U[5][5], id[5];
 #pragma unroll
   for (int j = 0; j < 5; j++) {
-    T v[5];
     T dj = A[pk(j, j)];
 #pragma unroll
     for (int k = 0; k < 5; k++)
-      if (k < j) {
-        v[k] = L[j][k] * d[k];
-        dj -= L[j][k] * v[k];
-      }
-    if (!(dj > (T)0)) return false;
-    d[j] = dj;
+      if (k < j) dj -= U[j][k] * L[j][k];
+    if (!pivot_positive<T, NR>(dj)) return false;
     id[j] = pivot_inv<T, NR>(dj);
 #pragma unroll
     for (int i = 0; i < 5; i++)
@@ -267,7 +275,8 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
         T a = A[pk(i, j)];
 #pragma unroll
         for (int k = 0; k < 5; k++)
-          if (k < j) a -= L[i][k] * v[k];
+          if (k < j) a -= U[i][k] * L[j][k];
+        U[i][j] = a;
         L[i][j] = a * id[j];
       }
   }
@@ -291,23 +300,37 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
   return true;
 }
 
-// LDL^T solve of a TF system in precision TL.
+// LDL^T solve of a TF system in precision TL.  FP32 -> FP64 (and back):
+// the conversions by integer operations (f32_to_f64, f64_to_f32), as GB300
+// executes F2F conversions on its 1/64-rate FP64 pipe.
 template <typename TF, typename TL>
 __device__ __forceinline__ bool ldl_solve5_wide(const TF* H, const TF* b, TF* x) {
   TL Hl[15], bl[5], pl[5];
+  if constexpr (sizeof(TF) == 4 && sizeof(TL) == 8) {
 #pragma unroll
-  for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
+    for (int i = 0; i < 15; i++) Hl[i] = f32_to_f64(H[i]);
 #pragma unroll
-  for (int i = 0; i < 5; i++) bl[i] = (TL)b[i];
-  const bool ok = ldl_solve5<TL, true>(Hl, bl, pl);
+    for (int i = 0; i < 5; i++) bl[i] = f32_to_f64(b[i]);
+    const bool ok = ldl_solve5<TL, true>(Hl, bl, pl);
 #pragma unroll
-  for (int i = 0; i < 5; i++) x[i] = (TF)pl[i];
-  return ok;
+    for (int i = 0; i < 5; i++) x[i] = f64_to_f32(pl[i]);
+    return ok;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 15; i++) Hl[i] = (TL)H[i];
+#pragma unroll
+    for (int i = 0; i < 5; i++) bl[i] = (TL)b[i];
+    const bool ok = ldl_solve5<TL, true>(Hl, bl, pl);
+#pragma unroll
+    for (int i = 0; i < 5; i++) x[i] = (TF)pl[i];
+    return ok;
+  }
 }
 
 // Result of one voxel solve.
+template <typename TF>
 struct VoxelOut {
-  double conv_s, conv_e;
+  TF conv_s, conv_e;   // the voxel's error contributions, in the flow-rule precision
   int iters;
   int failed;
 };
@@ -331,9 +354,9 @@ struct VoxelOut {
 // with the first) for the back-transform and the error norms, so neither
 // the inputs nor the 5x5 frame rotation stay live across the Newton loop.
 template <typename TF, typename TL, bool ROOT_ONLY, typename Slip, typename Load>
-__device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const Slip& slip,
+__device__ VoxelOut<TF> solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const Slip& slip,
                                 const Load& load, TF* sig6, TF* ed6) {
-  VoxelOut o = {0.0, 0.0, 0, 0};
+  VoxelOut<TF> o = {(TF)0, (TF)0, 0, 0};
   const TF dt = cpick<TF>(nc.dt, nc.dtf);
   TF x[5], c[5], K[15];
   TF h, ref2, dh;
@@ -552,8 +575,8 @@ __device__ VoxelOut solve_voxel(const NewtonConst& nc, const PhaseConst& ph, con
     const TF de = ep6[5] + shh * h - eps6[5];
     ce += de * de;
   }
-  o.conv_s = (double)sqrt(cs);
-  o.conv_e = (double)sqrt(ce);
+  o.conv_s = sqrt(cs);
+  o.conv_e = sqrt(ce);
 #pragma unroll
   for (int j = 0; j < 5; j++) {
     sig6[j] = ss[j];
@@ -643,7 +666,7 @@ __device__ __forceinline__ void newton_block_reduce(const TV (&v)[NPART], double
     } else if (!ph1_only || comp < 8) {
       double a = 0.0;
 #pragma unroll
-      for (int k = 0; k < NT / 16; k++) a += (double)sv[comp][k * 16 + chunk];
+      for (int k = 0; k < NT / 16; k++) a += to_f64(sv[comp][k * 16 + chunk]);
       sp[comp][chunk] = a;
     }
   }
@@ -700,14 +723,14 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
       };
       TF s6[6], e6[6];
       const TF* et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
-      VoxelOut o = solve_voxel<TF, TS, ROOT_ONLY>(nc, ph, et, slip, load, s6, e6);
+      VoxelOut<TF> o = solve_voxel<TF, TS, ROOT_ONLY>(nc, ph, et, slip, load, s6, e6);
 #pragma unroll
       for (int i = 0; i < 6; i++) {
         f.sig[i * P + v] = (TSt)s6[i];
         f.edot[i * P + v] = (TSt)e6[i];
       }
-      acc[0] = (TF)o.conv_s;   // exact: computed in TF
-      acc[1] = (TF)o.conv_e;
+      acc[0] = o.conv_s;
+      acc[1] = o.conv_e;
 #pragma unroll
       for (int i = 0; i < 6; i++) {
         acc[2 + i] = s6[i];
@@ -1080,7 +1103,7 @@ __global__ void __launch_bounds__(256) local_solve_kernel(const NewtonConst nc, 
   PlSlip<double> pl;
   for (int k = 0; k < NSYS; k++) pl.tauf[k] = tauf[k];
   pl.tau_off = ph.tau_back_minus_fwd;
-  VoxelOut o = solve_voxel<double, double, false>(nc, ph, etab + (size_t)v * ETAB_W, pl, load, s6, e6);
+  VoxelOut<double> o = solve_voxel<double, double, false>(nc, ph, etab + (size_t)v * ETAB_W, pl, load, s6, e6);
   for (int i = 0; i < 6; i++) {
     sig[6 * v + i] = s6[i];
     edot[6 * v + i] = e6[i];
@@ -1173,7 +1196,7 @@ __global__ void __launch_bounds__(256) local_solve_noalloc_kernel(const NewtonCo
     PlSlip<double> pl;
     for (int k = 0; k < NSYS; k++) pl.tauf[k] = tauf[k];
     pl.tau_off = ph.tau_back_minus_fwd;
-    VoxelOut o = solve_voxel<double, double, false>(nc, ph, et, pl, load, s6, e6);
+    VoxelOut<double> o = solve_voxel<double, double, false>(nc, ph, et, pl, load, s6, e6);
     for (int i = 0; i < 6; i++) {
       sig[6 * v + i] = s6[i];
       edot[6 * v + i] = e6[i];
