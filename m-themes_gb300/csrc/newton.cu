@@ -223,18 +223,29 @@ __device__ __forceinline__ void symv5(const T* K, const T* x, T* y) {
   }
 }
 
-// 1/d for a positive normal FP64 pivot: the hardware estimate
-// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps
-// r <- r + r (1 - d r), each of which doubles the number of correct bits,
-// so the result is within a few ulp of 1/d without the special-case
-// handling of a correctly rounded divide.
+// 1/d for a positive normal FP64 pivot, without FP64-pipe work besides
+// three DFMA: the FP32 hardware reciprocal (rcp.approx.ftz.f32, within 1 ulp)
+// of d's mantissa m in [1, 2), truncated to 24 bits, gives 1/m to within
+// 2^-22; its exponent is shifted by d's with integer operations; one
+// cubically convergent Newton step x <- x (1 + e + e^2), e = 1 - d x,
+// takes the relative error from 2^-22 to below 2^-64, so the result is
+// within an ulp or two of 1/d without the special-case handling of a
+// correctly rounded divide.
 __device__ __forceinline__ double pivot_rcp_nr(double d) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
-  return fma(r, e, r);
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const int E = (int)((hi >> 20) & 0x7ffu);   // biased exponent of d (1..2046)
+  const float m = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29));
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(m));
+  const unsigned ru = __float_as_uint(r);     // 1/m in (0.5, 1]
+  // 1/d = (1/m) 2^(1023 - (E - 1023)): biased FP64 exponent Er - 127 + 2046 - E
+  const int eo = (int)((ru >> 23) & 0xffu) + 1919 - E;
+  unsigned xhi = ((unsigned)eo << 20) | ((ru >> 3) & 0xfffffu);
+  unsigned xlo = ru << 29;
+  if (eo <= 0) xhi = xlo = 0u;                // 1/d below the normal range
+  const double x = __hiloint2double((int)xhi, (int)xlo);
+  const double e = fma(-d, x, 1.0);
+  return fma(x, fma(e, e, e), x);
 }
 template <typename T, bool NR>
 __device__ __forceinline__ T pivot_inv(T d) {
