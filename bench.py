@@ -119,6 +119,38 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def fp64_peak_tflops(dev):
+    """FP64 throughput of this GPU, measured here: cuBLAS DGEMM
+    (torch.matmul in float64, 4096^3, best of 5 after 2 warm-up calls, CUDA
+    events on the current stream), in TFLOP/s."""
+    import torch
+    n = 4096
+    g = torch.Generator(device=dev).manual_seed(0)
+    a = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    for _ in range(2):
+        torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1)
+        best = t if best is None else min(best, t)
+    del a, b
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
+
+
+# FP64 flops of the mixed mode's Jacobian solve per local Newton step, counted
+# algorithmically (a fused multiply-add is two flops, a reciprocal one): the
+# LDL^T factorisation of the 5x5 Hessian (20 + 20 from the two update sums, 10
+# scalings, 5 pivot reciprocals) and the two triangular solves (20 + 25)
+SOLVE_FP64_FLOPS = 100
+
+
 def traffic_per_launch(kernel):
     """DRAM bytes per launch of a kernel from the committed ncu summary,
     scaled to the 128^3 workload (profiles/traffic.json), or None."""
@@ -253,6 +285,17 @@ def run_gpu(args):
                        "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_s * 1e3,
                        "note": "the local Newton is ALU-bound (FP64 solve, FP32 flow rule); its HBM fraction is low "
                                "by construction"}
+    if prec == capi.MTH_MIXED and dname == "newton":
+        # the local Newton is bound by GB300's FP64 pipe: its FP64 solve flops
+        # against the FP64 throughput measured in this run
+        p64 = fp64_peak_tflops("cuda:%d" % dev_index)
+        steps = float(sum(r["newton_iters"] for r in reps))
+        a64 = SOLVE_FP64_FLOPS * steps / (d["ms"] / 1e3) / 1e12
+        out["roofline"]["fp64"] = {"achieved": a64, "peak": p64, "unit": "TFLOP/s", "frac": a64 / p64,
+                                   "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                                   "flops_per_newton_step": SOLVE_FP64_FLOPS, "newton_steps": steps,
+                                   "note": "algorithmic FP64 flops of the Jacobian solves; the kernel also "
+                                           "runs the FP32 flow rule, residual and Hessian assembly"}
     tot_ms = sum(v["ms"] for v in prof.values())
     out["kernels"] = {k: {"ms": round(v["ms"], 3), "share": round(v["ms"] / tot_ms, 4) if tot_ms else None,
                           "launches": v["launches"],

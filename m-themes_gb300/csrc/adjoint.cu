@@ -27,20 +27,33 @@ namespace mth {
 // FP64 block sum of W values for 256-thread blocks, one partial per block.
 template <int W>
 __device__ __forceinline__ void adj_block_sum(double (&v)[W], double* out) {
-  __shared__ double sm[W][8];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // 256-thread blocks, fixed order: the values are staged in shared memory,
+  // 16 threads per component each sum 16 of them, one thread per component
+  // sums the 16 partials (one DADD per value instead of a shuffle tree in
+  // every thread: GB300's FP64 pipe runs at 1/64 of the FP32 rate)
+  constexpr int NT = 256;
+  static_assert(W <= 16, "at most 16 components");
+  __shared__ double sv[W][NT];
+  __shared__ double sp[W][16];
+  const int t = threadIdx.x;
 #pragma unroll
-  for (int i = 0; i < W; i++) {
-    double a = v[i];
+  for (int i = 0; i < W; i++) sv[i][t] = v[i];
+  __syncthreads();
+  {
+    const int comp = t >> 4, chunk = t & 15;
+    if (comp < W) {
+      double a = 0.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-    if (lane == 0) sm[i][wid] = a;
+      for (int k = 0; k < NT / 16; k++) a += sv[comp][k * 16 + chunk];
+      sp[comp][chunk] = a;
+    }
   }
   __syncthreads();
-  if (threadIdx.x < W) {
-    double a = 0;
-    for (int w = 0; w < 8; w++) a += sm[threadIdx.x][w];
-    out[(size_t)blockIdx.x * W + threadIdx.x] = a;
+  if (t < W) {
+    double a = 0.0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) a += sp[t][k];
+    out[(size_t)blockIdx.x * W + t] = a;
   }
 }
 
@@ -180,7 +193,7 @@ __global__ void __launch_bounds__(256) adj_dot_kernel(const T* __restrict__ a, c
   double s[1] = {0.0};
   if (v < P)
 #pragma unroll
-    for (int i = 0; i < 6; i++) s[0] += (double)a[i * P + v] * (double)b[i * P + v];
+    for (int i = 0; i < 6; i++) s[0] += to_f64(a[i * P + v]) * to_f64(b[i * P + v]);   // exact products
   adj_block_sum<1>(s, partials);
 }
 
@@ -198,7 +211,7 @@ __global__ void __launch_bounds__(256) adj_cg_update_kernel(T* __restrict__ x, T
       x[o] += alpha * p[o];
       const T rv = r[o] - alpha * ap[o];
       r[o] = rv;
-      s[0] += (double)rv * (double)rv;
+      s[0] += to_f64(rv) * to_f64(rv);
     }
   adj_block_sum<1>(s, partials);
 }

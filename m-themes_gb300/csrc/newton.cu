@@ -1133,28 +1133,44 @@ cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, 
 }
 
 // --------------------------------------------------- deterministic reduction
-// out[w] = sum over blocks (fixed order) of partials[b*width + w].
-__global__ void reduce_partials_kernel(const double* __restrict__ partials, int nblocks, int width,
-                                       double* __restrict__ out, IterIn it) {
+// out[w] = sum over blocks (fixed order) of partials[b*width + w].  One
+// 1024-thread block per component; each thread keeps four independent
+// partial sums so four L2 loads are in flight instead of a chain of
+// dependent ones.
+constexpr int RED_NT = 1024;   // 32 warps: the second shuffle stage sums one value per warp
+__global__ void __launch_bounds__(RED_NT) reduce_partials_kernel(const double* __restrict__ partials, int nblocks,
+                                                                 int width, double* __restrict__ out, IterIn it) {
   if (!is_live(it)) return;
-  __shared__ double sm[256];
+  __shared__ double sm[RED_NT / 32];
   for (int w = blockIdx.x; w < width; w += gridDim.x) {
-    double a = 0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a += partials[(size_t)b * width + w];
-    sm[threadIdx.x] = a;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
-      __syncthreads();
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int b = threadIdx.x;
+    for (; b + 3 * RED_NT < nblocks; b += 4 * RED_NT) {
+      a0 += partials[(size_t)b * width + w];
+      a1 += partials[(size_t)(b + RED_NT) * width + w];
+      a2 += partials[(size_t)(b + 2 * RED_NT) * width + w];
+      a3 += partials[(size_t)(b + 3 * RED_NT) * width + w];
     }
-    if (threadIdx.x == 0) out[w] = sm[0];
+    for (; b < nblocks; b += RED_NT) a0 += partials[(size_t)b * width + w];
+    // warp sums by shuffles, then the 32 warp sums by warp 0
+    double a = (a0 + a1) + (a2 + a3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      a = sm[threadIdx.x];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (threadIdx.x == 0) out[w] = a;
+    }
     __syncthreads();
   }
 }
 
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
                                    cudaStream_t st) {
-  reduce_partials_kernel<<<width, 256, 0, st>>>(partials, nblocks, width, out, it);
+  reduce_partials_kernel<<<width, RED_NT, 0, st>>>(partials, nblocks, width, out, it);
   return cudaGetLastError();
 }
 
