@@ -753,6 +753,8 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
     const PhaseConst& pc = c->nc.ph[phase[v] - 1];
     if (pc.type != 0) continue;
     const double* e = euler_deg + 3 * v;
+    if (!std::isfinite(e[0]) || !std::isfinite(e[1]) || !std::isfinite(e[2]))
+      return set_err(MTH_ERR_ARG, "voxel %zu has a non-finite Euler angle", v);
     // consecutive voxels mostly lie in one grain: reuse the previous class
     if (last_k >= 0 && phase[v] == last_key[0] && e[0] == last_e[0] && e[1] == last_e[1] && e[2] == last_e[2]) {
       counts[last_k]++;

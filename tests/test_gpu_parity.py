@@ -176,6 +176,10 @@ def test_status_codes():
     bad[3] = 5
     assert lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(bad), capi._dptr(e), g.size) == 1
     assert lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(ph), capi._dptr(e), g.size - 1) == 1
+    nan_e = e.copy()
+    nan_e[5, 1] = np.nan                                      # a non-finite Euler angle is refused
+    assert lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(ph), capi._dptr(nan_e), g.size) == 1
+    assert "non-finite" in lib.mth_last_error().decode()
     capi.check(lib, lib.mth_upload_microstructure(ctx, capi._iptr(g), capi._iptr(ph), capi._dptr(e), g.size))
     out = np.zeros(10)
     assert lib.mth_download_field(ctx, 0, capi._dptr(out), 10) == 1
