@@ -288,6 +288,7 @@ void ctx_free(mth_ctx* c) {
 static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain", "newton",
                                         "reduce", "end_step", "spin_fft", "setup", "drx",
                                         "pf_relax", "adj_local", "adj_cg", "dislocation_density"};
+const char* prof_class_name(int cls) { return cls >= 0 && cls < K_NCLASS ? k_names[cls] : "?"; }
 
 void prof_begin(mth_ctx* c) {
   if (!c->prof_on) return;

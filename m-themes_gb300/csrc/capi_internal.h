@@ -164,13 +164,16 @@ enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE,
 void prof_begin(mth_ctx* c);
 void prof_end(mth_ctx* c, int cls, int kernels, double bytes);
 void prof_resolve(mth_ctx* c);   // after the stream has been synchronised
+const char* prof_class_name(int cls);
 
 #define LAUNCHN(cls, kernels, bytes, call)         \
   do {                                             \
     prof_begin(c);                                 \
     cudaError_t e__ = (call);                      \
     prof_end(c, cls, (kernels), (double)(bytes));  \
-    if (e__ != cudaSuccess) CK(e__);               \
+    if (e__ != cudaSuccess)                        \
+      return set_err(MTH_ERR_CUDA, "launch of the %s kernels failed: %s (%s:%d)", prof_class_name(cls), \
+                     cudaGetErrorString(e__), __FILE__, __LINE__);                                   \
   } while (0)
 #define LAUNCH(cls, bytes, call) LAUNCHN(cls, 1, bytes, call)
 
