@@ -519,11 +519,22 @@ def run_batch(args):
     mechanical steps after W warm-up steps, plus the single-Solver-per-RVE
     baseline on the same steps."""
     import torch
-    from mth import Batch, Solver, capi, synth
-    cfgs = synth.batch_workload(args.workload)
+    from mth import Batch, Solver, capi, replicas, synth
+    ws, rank, lrank = dist_init()
+    if ws > 1:
+        # the members are partitioned over the ranks; no data-path collective
+        import torch.distributed as dist
+        torch.cuda.set_device(lrank)
+        dist.init_process_group("nccl")
+    dev_index = lrank if ws > 1 else 0
+    cfgs_all = synth.batch_workload(args.workload)
+    mine = replicas.batch_share([int(np.prod(c.cell_dim)) for c in cfgs_all], rank, ws)
+    cfgs = [cfgs_all[i] for i in mine]
     prec = {"mixed": capi.MTH_MIXED, "fp64": capi.MTH_FP64, "mixed_fast": capi.MTH_MIXED_FAST,
             "mixed_root64": capi.MTH_MIXED_ROOT64}[args.precision]
     params = [capi.params_from_config(c, precision=prec) for c in cfgs]
+    for p in params:
+        p.device = dev_index
     micro = [synth.microstructure(c) for c in cfgs]
     nvs = [int(np.prod(c.cell_dim)) for c in cfgs]
     t0 = time.perf_counter()
@@ -531,9 +542,11 @@ def run_batch(args):
     t_create = time.perf_counter() - t0
     for _ in range(args.warmup):
         b.step()
-    cs = ClockSampler(0)
+    cs = ClockSampler(dev_index)
     cs.start()
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     vox_it = 0
     for _ in range(args.steps):
@@ -541,21 +554,28 @@ def run_batch(args):
         vox_it += sum(n * r["iterations"] for n, r in zip(nvs, reps))
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    if ws > 1:
+        torch.distributed.barrier()
     clk = cs.stop()
     b.close()
-    out = {"metric": "voxel-iterations/s, 64 batched RVEs (24x32^3, 24x48^3, 16x64^3)", "value": vox_it / dt,
-           "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+    vox_it, dt, value = replicas.aggregate(float(vox_it), dt, device="cuda:%d" % dev_index)
+    if rank != 0:
+        return
+    out = {"metric": "voxel-iterations/s, 64 batched RVEs (24x32^3, 24x48^3, 16x64^3)", "value": value,
+           "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": {capi.MTH_MIXED: "f32 fields + f64 Newton solve", capi.MTH_FP64: "f64",
                      capi.MTH_MIXED_FAST: "f32", capi.MTH_MIXED_ROOT64: "f32 fields + f64 Newton solve near the root"}[prec],
            "data": "synthetic: per-RVE seeded periodic Voronoi, grains ~U[32,256], uniform SO(3), "
                    "tau0 ~U[12,20] MPa, n in {8,10,15,20}",
-           "config": {"workload": "%d RVEs, uniaxial tension, dt=1e-3" % len(cfgs), "rves": len(cfgs),
-                      "voxels": sum(nvs), "batch_create_s": t_create,
+           "config": {"workload": "%d RVEs, uniaxial tension, dt=1e-3" % len(cfgs_all), "rves": len(cfgs_all),
+                      "voxels": int(sum(np.prod(c.cell_dim) for c in cfgs_all)), "batch_create_s": t_create,
+                      "parallelism": ("members dealt over %d ranks by voxel count, one batch per rank, no "
+                                      "data-path collective" % ws) if ws > 1 else "single GPU",
                       "timing": "host wall clock around whole batch steps (graph launches + host convergence "
                                 "logic), device synchronised on both sides"},
            "clocks": clk}
-    if not args.no_fp64:
+    if not args.no_fp64 and ws == 1:
         # one Solver per RVE, stepped one after the other: the unbatched baseline
         sols = [Solver(p, *m) for p, m in zip(params, micro)]
         for _ in range(args.warmup):
