@@ -99,3 +99,16 @@ def test_batch_partition_two_ranks():
     assert r0[1] == r1[1] == 100.0 * sum(sizes)
     assert r0[2] == r1[2] == 1.5
     assert abs(r0[3] - 100.0 * sum(sizes) / 1.5) < 1e-6
+
+
+def test_batch_share_edges():
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "m-themes_gb300"))
+    from mth import replicas
+    sizes = [27, 8, 64, 8, 27]
+    assert replicas.batch_share(sizes, 0, 1) == [0, 1, 2, 3, 4]
+    shares = [replicas.batch_share(sizes, r, 3) for r in range(3)]
+    assert shares == [[2], [0, 1], [3, 4]]                 # 64 | 27+8 | 27+8
+    assert [replicas.batch_share([5], r, 3) for r in range(3)] == [[0], [], []]
+    with pytest.raises(ValueError):
+        replicas.batch_share(sizes, 3, 3)
