@@ -56,8 +56,8 @@ def test_adjoint_forward_is_the_plain_forward(fp64_case):
 
 
 def test_adjoint_matches_central_differences(fp64_case):
-    """Spec bar: each gradient entry within 1e-3 relative of central
-    differences with a relative step of 1e-4."""
+    """Each gradient entry within 1e-3 relative of central differences with
+    a relative step of 1e-4 (FP64)."""
     base, tgt, J, grad, s33, info = fp64_case
     vals = synth.calibration_values(base)
     for k in range(5):
