@@ -203,9 +203,48 @@ void class_row(const PhaseConst& ph, const double R[9], double* row) {
   row[ET_CGR_HH] = ph.c_xt[5];
   row[ET_SEL_HH] = ph.s_xt[5];
 }
+// Smallest eigenvalue of a symmetric 5x5 matrix (cyclic Jacobi rotations
+// until the off-diagonal part is negligible).
+static double sym5_min_eig(double a[5][5]) {
+  for (int sweep = 0; sweep < 50; sweep++) {
+    double off = 0, diag = 0;
+    for (int i = 0; i < 5; i++) {
+      diag += a[i][i] * a[i][i];
+      for (int j = i + 1; j < 5; j++) off += a[i][j] * a[i][j];
+    }
+    if (off <= 1e-30 * diag) break;
+    for (int p = 0; p < 4; p++)
+      for (int q = p + 1; q < 5; q++) {
+        if (a[p][q] == 0.0) continue;
+        const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < 5; k++) {   // columns p, q
+          const double akp = a[k][p], akq = a[k][q];
+          a[k][p] = cs * akp - sn * akq;
+          a[k][q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < 5; k++) {   // rows p, q
+          const double apk = a[p][k], aqk = a[q][k];
+          a[p][k] = cs * apk - sn * aqk;
+          a[q][k] = sn * apk + cs * aqk;
+        }
+      }
+  }
+  double m = a[0][0];
+  for (int i = 1; i < 5; i++) m = std::min(m, a[i][i]);
+  return m;
+}
 void class_row_add_s0(double* row, const double s066[6][6]) {
+  double a[5][5];
   for (int i = 0; i < 5; i++)
-    for (int j = i; j < 5; j++) row[ET_STOT + pkh(i, j)] = s066[i][j] + row[ET_SEL + pkh(i, j)];
+    for (int j = i; j < 5; j++) {
+      row[ET_STOT + pkh(i, j)] = s066[i][j] + row[ET_SEL + pkh(i, j)];
+      a[i][j] = a[j][i] = row[ET_STOT + pkh(i, j)];
+    }
+  // the Hessian base of the local solve is Q (this block) Q^T with Q
+  // orthogonal, so its smallest eigenvalue is this block's; kept 1e-6 low
+  row[ET_STOT_MIN] = sym5_min_eig(a) * (1.0 - 1e-6);
 }
 }  // namespace capi_host
 
@@ -466,6 +505,7 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   }
   c->nc.dt = p->time_step;
   c->nc.ph1_only = (p->n_phases == 1 || c->nc.ph[1].type != 0) ? 1 : 0;
+  c->nc.bound_stop = c->mixed ? 1 : 0;
   c->nc.tol = p->newton_tol > 0 ? p->newton_tol : (c->mixed ? 1e-6 : 1e-10);
   c->nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
   // boundary conditions (src/init.c:861-900)

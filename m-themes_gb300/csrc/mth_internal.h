@@ -55,6 +55,8 @@ struct NewtonConst {
   int flow_off;         // 1: Schmid tensors zero (Update_Flag=0 at istep 0)
   int ph1_only;         // 1: no crystal phase but phase 1 (sigma is 0 elsewhere), so the
                         // phase-1 stress sums equal the total ones
+  int bound_stop;       // 1: also end a local solve when the next Newton step is bounded
+                        // below the tolerance (ET_STOT_MIN; the FP32 flow-rule modes)
   // float copies (fill_float_consts)
   float s0devf[25];
   float s0hhf, dtf, tolf;
@@ -131,6 +133,7 @@ constexpr int ET_SEL = 15;    // S_gr dev (15)
 constexpr int ET_SEL_HH = 30; // S_gr hydrostatic
 constexpr int ET_CGR = 31;    // C_gr dev (15)
 constexpr int ET_CGR_HH = 46; // C_gr hydrostatic
+constexpr int ET_STOT_MIN = 47; // smallest eigenvalue of the S066_dev + S_gr block (a lower bound)
 
 // Partial sums written per block by the Newton kernel.
 constexpr int NPART = 16;   // err_s, err_e, sig[6], sig_ph1[6], newton_iters, newton_failed

@@ -507,6 +507,20 @@ __device__ VoxelOut<TF> solve_voxel(const NewtonConst& nc, const PhaseConst& ph,
     TF g[5];
 #pragma unroll
     for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * edf[i];
+    if (sizeof(TF) == 4 && nc.bound_stop) {
+      // The next step p = -H^-1 g has |p| <= |g| / lambda_min(H) <=
+      // |g| / lambda_min(K), as H = K + dt D with D = sum w m m^T positive
+      // semidefinite; when that bound is within the tolerance the step the
+      // reference would take next is too, and x is the answer to within it.
+      TF den2 = ref2;
+      if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
+      const TF mu = et[ET_STOT_MIN];
+      const TF gn2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + g[3] * g[3] + g[4] * g[4];
+      if (gn2 <= tol2 * den2 * mu * mu) {
+        done = true;
+        break;
+      }
+    }
     {
       TF H[15], mg[5];
 #pragma unroll
