@@ -612,6 +612,266 @@ __device__ VoxelOut<TF> solve_voxel(const NewtonConst& nc, const PhaseConst& ph,
   return o;
 }
 
+// ----------------------------------------- block-cooperative local solve
+// The local solve of solve_voxel in pieces, for newton_coop_kernel: nw_init
+// (set-up), nw_pass_a (one flow-rule evaluation and what it decides; when
+// the next Newton direction is needed it returns the system H p = -g) and
+// nw_pass_b (the move the direction gives), with the Jacobian solves of all
+// the block's threads done between them by as few threads as there are
+// systems.  Same arithmetic and order as solve_voxel.
+template <typename TF>
+struct NewtonState {
+  TF x[5], c[5], K[15];        // iterate, linear term and Hessian base of Phi (crystal axes)
+  TF h, ref2, dh, hstep2, tol2, ls_thr2;
+  TF xt[5];                    // point evaluated next
+  TF p[5], pn2, slope, phi0, alpha;
+  TF edf[5], psif;             // rates and psi at the last evaluated point
+  int it, ls, pass;
+  bool done, near_root, trial, failed;
+};
+
+template <typename TF, typename Load>
+__device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonConst& nc, const TF* __restrict__ et,
+                                        const Load& load) {
+  const TF shh = et[ET_SEL_HH];
+  TF lam6[6], eps6[6], ep6[6], Q[25];
+  {
+    TF R[9];
+    load(lam6, eps6, ep6, R, false);
+    rot_to_q<TF>(R, Q);
+  }
+  TF s0s[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    TF a = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) a += cpick<TF>(nc.s0dev[i * 5 + j], nc.s0devf[i * 5 + j]) * lam6[j];
+    s0s[i] = a;
+  }
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    TF a = 0, b = 0, e = 0, d = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+      a += Q[i * 5 + j] * lam6[j];
+      b += Q[i * 5 + j] * eps6[j];
+      e += Q[i * 5 + j] * ep6[j];
+      d += Q[i * 5 + j] * s0s[j];
+    }
+    s.x[i] = a;
+    s.c[i] = -d + e - b;
+  }
+  {
+    TF St[25], t[25];
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = 0; j < 5; j++) St[i * 5 + j] = et[ET_STOT + pk(i, j)];
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = 0; j < 5; j++) {
+        TF a = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) a += Q[i * 5 + k] * St[k * 5 + j];
+        t[i * 5 + j] = a;
+      }
+#pragma unroll
+    for (int i = 0; i < 5; i++)
+#pragma unroll
+      for (int j = i; j < 5; j++) {
+        TF a = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) a += t[i * 5 + k] * Q[j * 5 + k];
+        s.K[pk(i, j)] = a;
+      }
+  }
+  const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf);
+  s.h = (s0hh * lam6[5] + eps6[5] - ep6[5]) / (s0hh + shh);
+  TF ref2 = 0;
+#pragma unroll
+  for (int i = 0; i < 6; i++) ref2 += lam6[i] * lam6[i];
+  s.ref2 = ref2;
+  s.dh = s.h - lam6[5];
+  const TF tol = cpick<TF>(nc.tol, nc.tolf);
+  s.tol2 = tol * tol;
+  s.ls_thr2 = (TF)1e-6 * ref2;
+  s.hstep2 = s.dh * s.dh;
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    s.xt[i] = s.x[i];
+    s.p[i] = 0;
+  }
+  s.pn2 = s.slope = s.phi0 = 0;
+  s.alpha = 1;
+  s.it = s.ls = s.pass = 0;
+  s.done = s.near_root = s.trial = s.failed = false;
+}
+
+template <typename TF>
+__device__ __forceinline__ void nw_accept(NewtonState<TF>& s) {
+#pragma unroll
+  for (int i = 0; i < 5; i++) s.x[i] += s.alpha * s.p[i];
+  const TF step2 = s.alpha * s.alpha * s.pn2 + s.hstep2;
+  s.hstep2 = 0;
+  s.near_root = step2 <= s.ls_thr2;
+  TF den2 = s.ref2;
+  if (!(den2 > (TF)0))
+    den2 = s.x[0] * s.x[0] + s.x[1] * s.x[1] + s.x[2] * s.x[2] + s.x[3] * s.x[3] + s.x[4] * s.x[4] + s.h * s.h;
+  if (!(den2 > (TF)0) || step2 <= s.tol2 * den2) s.done = true;
+  s.it++;
+}
+
+// 0: pass done, no solve; 1: the Newton direction is needed (H, mg filled);
+// 2: the solve has ended
+template <typename TF, typename Slip>
+__device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonConst& nc, const PhaseConst& ph,
+                                         const Slip& slip, const TF* __restrict__ et, TF H[15], TF mg[5]) {
+  if (s.pass >= 41 * (nc.itmax + 1)) return 2;
+  s.pass++;
+  const TF dt = cpick<TF>(nc.dt, nc.dtf);
+  TF Df[15];
+  if (nc.flow_off) {
+#pragma unroll
+    for (int i = 0; i < 5; i++) s.edf[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 15; i++) Df[i] = 0;
+    s.psif = 0;
+  } else {
+    slip.template flow<true>(ph, s.xt, s.edf, Df, s.psif, nullptr);
+  }
+  TF Kx[5];
+  symv5<TF>(s.K, s.xt, Kx);
+  if (s.trial) {
+    TF phi = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) phi += s.xt[i] * ((TF)0.5 * Kx[i] + s.c[i]);
+    phi += dt * s.psif;
+    if (!(phi <= s.phi0 + (TF)1e-4 * s.alpha * s.slope)) {
+      TF den = (TF)2 * (phi - s.phi0 - s.slope * s.alpha);
+      TF an = den > (TF)0 ? -s.slope * s.alpha * s.alpha / den : (TF)0.5 * s.alpha;
+      an = fmin(an, (TF)0.5 * s.alpha);
+      s.alpha = fmax(an, (TF)0.1 * s.alpha);
+      s.ls++;
+#pragma unroll
+      for (int i = 0; i < 5; i++) s.xt[i] = s.x[i] + s.alpha * s.p[i];
+      if (!(s.alpha * s.alpha * s.pn2 <= (TF)1e-28 * (s.ref2 + (TF)1)) && s.ls < 40) return 0;
+      nw_accept(s);
+      s.trial = false;
+      return 0;
+    }
+    nw_accept(s);
+    s.trial = false;
+  }
+  if (s.done || s.it >= nc.itmax) return 2;
+  TF g[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) g[i] = Kx[i] + s.c[i] + dt * s.edf[i];
+  if (sizeof(TF) == 4 && nc.bound_stop) {
+    TF den2 = s.ref2;
+    if (!(den2 > (TF)0))
+      den2 = s.x[0] * s.x[0] + s.x[1] * s.x[1] + s.x[2] * s.x[2] + s.x[3] * s.x[3] + s.x[4] * s.x[4] + s.h * s.h;
+    const TF mu = et[ET_STOT_MIN];
+    const TF gn2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + g[3] * g[3] + g[4] * g[4];
+    if (gn2 <= s.tol2 * den2 * mu * mu) {
+      s.done = true;
+      return 2;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 15; i++) H[i] = s.K[i] + dt * Df[i];
+#pragma unroll
+  for (int i = 0; i < 5; i++) mg[i] = -g[i];
+  // Phi at x (= xt here), for a line search along the coming direction
+  TF phi0 = 0;
+#pragma unroll
+  for (int i = 0; i < 5; i++) phi0 += s.x[i] * ((TF)0.5 * Kx[i] + s.c[i]);
+  s.phi0 = phi0 + dt * s.psif;
+  return 1;
+}
+
+// the move along the solved direction p of -g (mg); false: the solve failed
+template <typename TF>
+__device__ __forceinline__ bool nw_pass_b(NewtonState<TF>& s, const NewtonConst& nc, const TF p[5], bool ok,
+                                          const TF mg[5]) {
+  if (!ok) {
+    s.failed = true;
+    return false;
+  }
+  s.pn2 = 0;
+  s.slope = 0;
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    s.p[i] = p[i];
+    s.pn2 += p[i] * p[i];
+    s.slope -= mg[i] * p[i];
+  }
+  s.alpha = 1;
+  if (s.pn2 > s.ls_thr2 && !nc.flow_off) {
+    s.ls = 0;
+    s.trial = true;
+#pragma unroll
+    for (int i = 0; i < 5; i++) s.xt[i] = s.x[i] + s.alpha * s.p[i];
+    return true;
+  }
+  nw_accept(s);
+#pragma unroll
+  for (int i = 0; i < 5; i++) s.xt[i] = s.x[i];
+  return true;
+}
+
+template <typename TF, typename Load>
+__device__ __forceinline__ VoxelOut<TF> nw_finish(const NewtonState<TF>& s, const NewtonConst& nc,
+                                                  const TF* __restrict__ et, const Load& load, TF* sig6, TF* ed6) {
+  VoxelOut<TF> o;
+  o.iters = s.it;
+  o.failed = (s.failed || !s.done) ? 1 : 0;
+  const TF dt = cpick<TF>(nc.dt, nc.dtf);
+  const TF shh = et[ET_SEL_HH];
+  TF lam6[6], eps6[6], ep6[6], Q[25];
+  {
+    TF R[9];
+    load(lam6, eps6, ep6, R, true);
+    rot_to_q<TF>(R, Q);
+  }
+  TF ss[5], es[5];
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    TF a = 0, b = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      a += Q[i * 5 + j] * s.x[i];
+      b += Q[i * 5 + j] * s.edf[i];
+    }
+    ss[j] = a;
+    es[j] = b;
+  }
+  TF cs = s.dh * s.dh, ce = 0;
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    const TF ds = ss[i] - lam6[i];
+    cs += ds * ds;
+    TF de = ep6[i] + dt * es[i] - eps6[i];
+#pragma unroll
+    for (int j = 0; j < 5; j++) de += et[ET_SEL + pk(i, j)] * ss[j];
+    ce += de * de;
+  }
+  {
+    const TF de = ep6[5] + shh * s.h - eps6[5];
+    ce += de * de;
+  }
+  o.conv_s = sqrt(cs);
+  o.conv_e = sqrt(ce);
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    sig6[j] = ss[j];
+    ed6[j] = es[j];
+  }
+  sig6[5] = s.h;
+  ed6[5] = 0;
+  return o;
+}
+
 // ------------------------------------------------------------ reductions
 template <int W>
 __device__ __forceinline__ void block_reduce_store(double (&v)[W], double* out) {
@@ -774,6 +1034,128 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
   newton_block_reduce<TF>(acc, partials, nc.ph1_only != 0);
 }
 
+// Newton kernel of the mixed modes with the FP64 Jacobian solve at every
+// step.  A warp runs its Newton passes until its slowest thread has ended,
+// so with the solves done by each thread about a third of the lanes of every
+// FP64 instruction idled.  Here the block's threads step their solves in
+// lock-step passes (a block-wide vote ends the loop): in each pass the
+// threads that need a Newton direction put their 5x5 systems in shared
+// memory, in thread order, the first n threads of the block solve the n
+// systems in FP64, and each thread reads its direction back.  Every voxel's
+// iterates and result are those of solve_voxel.
+template <typename TSt, typename TF, typename TL, int MINB, int LAW = 0>
+__global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonConst nc, Fields<TSt> f,
+                                                                double* __restrict__ partials, IterIn it) {
+  if (!is_live(it)) return;
+  __shared__ TF sH[15][256];
+  __shared__ TF sB[5][256];    // -g in, the direction out
+  __shared__ int sOk[256];
+  __shared__ int sWarp[8];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const long long v = (long long)blockIdx.x * blockDim.x + t;
+  const long long P = f.nv;
+  TF acc[NPART];
+#pragma unroll
+  for (int i = 0; i < NPART; i++) acc[i] = (TF)0;
+  int jph = 0;
+  bool active = false;
+  const TF* et = nullptr;
+  typename SlipOf<LAW, TF, TSt>::type slip;
+  NewtonState<TF> s;
+  auto load = [&](TF* lam6, TF* eps6, TF* ep6, TF* R, bool again) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      lam6[i] = (TF)ld_sel(f.sig + i * P + v, again);
+      eps6[i] = (TF)ld_sel(f.strain + i * P + v, again);
+      ep6[i] = (TF)ld_sel(f.epsp + i * P + v, again);
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) R[i] = (TF)ld_sel(f.rot + i * P + v, again);
+  };
+  if (v < P) {
+    jph = f.phase[v];
+    const PhaseConst& ph = nc.ph[jph];
+    if (ph.type == 0) {
+      SlipOf<LAW, TF, TSt>::load(ph, f, v, slip);
+      et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
+      nw_init(s, nc, et, load);
+      active = true;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 6; i++) {
+        f.sig[i * P + v] = (TSt)0;
+        f.edot[i * P + v] = (TSt)0;
+      }
+    }
+  }
+  const bool crystal = active;
+  // every thread of the block takes part in every barrier of this loop
+  while (__syncthreads_or(active)) {
+    TF H[15], mg[5];
+    int need = 0;
+    if (active) {
+      const int r = nw_pass_a(s, nc, nc.ph[jph], slip, et, H, mg);
+      if (r == 2) active = false;
+      need = r == 1;
+    }
+    // slots of the systems, in thread order
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (lane == 0) sWarp[w] = __popc(m);
+    __syncthreads();
+    int base = 0, n = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      base += k < w ? sWarp[k] : 0;
+      n += sWarp[k];
+    }
+    const int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (need) {
+#pragma unroll
+      for (int i = 0; i < 15; i++) sH[i][slot] = H[i];
+#pragma unroll
+      for (int i = 0; i < 5; i++) sB[i][slot] = mg[i];
+    }
+    __syncthreads();
+    if (t < n) {
+      TF Hs[15], bs[5], ps[5];
+#pragma unroll
+      for (int i = 0; i < 15; i++) Hs[i] = sH[i][t];
+#pragma unroll
+      for (int i = 0; i < 5; i++) bs[i] = sB[i][t];
+      const bool ok = ldl_solve5_wide<TF, TL>(Hs, bs, ps);
+#pragma unroll
+      for (int i = 0; i < 5; i++) sB[i][t] = ps[i];
+      sOk[t] = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (need) {
+      TF pd[5];
+#pragma unroll
+      for (int i = 0; i < 5; i++) pd[i] = sB[i][slot];
+      if (!nw_pass_b(s, nc, pd, sOk[slot] != 0, mg)) active = false;
+    }
+  }
+  if (crystal) {
+    TF s6[6], e6[6];
+    const VoxelOut<TF> o = nw_finish(s, nc, et, load, s6, e6);
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      f.sig[i * P + v] = (TSt)s6[i];
+      f.edot[i * P + v] = (TSt)e6[i];
+    }
+    acc[0] = o.conv_s;
+    acc[1] = o.conv_e;
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      acc[2 + i] = s6[i];
+      acc[8 + i] = jph == 0 ? s6[i] : (TF)0;
+    }
+    acc[14] = (TF)o.iters;
+    acc[15] = (TF)o.failed;
+  }
+  newton_block_reduce<TF>(acc, partials, nc.ph1_only != 0);
+}
+
 void fill_float_consts(NewtonConst& nc) {
   for (int k = 0; k < 2; k++) {
     PhaseConst& ph = nc.ph[k];
@@ -823,7 +1205,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     newton_kernel<float, float, double, 3, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    newton_coop_kernel<float, float, double, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
     newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
