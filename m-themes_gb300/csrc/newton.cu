@@ -619,9 +619,20 @@ __device__ VoxelOut<TF> solve_voxel(const NewtonConst& nc, const PhaseConst& ph,
 // nw_pass_b (the move the direction gives), with the Jacobian solves of all
 // the block's threads done between them by as few threads as there are
 // systems.  Same arithmetic and order as solve_voxel.
+// The linear term c and the Hessian base K of Phi, constant during a solve,
+// live in shared memory (component-major, one column per thread), so the
+// registers hold only what changes.
+template <typename TF>
+struct NewtonShared {
+  TF (*K)[256];   // [15][256]
+  TF (*c)[256];   // [5][256]
+  int t;
+  __device__ __forceinline__ TF k(int i) const { return K[i][t]; }
+  __device__ __forceinline__ TF cc(int i) const { return c[i][t]; }
+};
 template <typename TF>
 struct NewtonState {
-  TF x[5], c[5], K[15];        // iterate, linear term and Hessian base of Phi (crystal axes)
+  TF x[5];                     // iterate (crystal axes)
   TF h, ref2, dh, hstep2, tol2, ls_thr2;
   TF xt[5];                    // point evaluated next
   TF p[5], pn2, slope, phi0, alpha;
@@ -631,8 +642,8 @@ struct NewtonState {
 };
 
 template <typename TF, typename Load>
-__device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonConst& nc, const TF* __restrict__ et,
-                                        const Load& load) {
+__device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonShared<TF>& sh, const NewtonConst& nc,
+                                        const TF* __restrict__ et, const Load& load) {
   const TF shh = et[ET_SEL_HH];
   TF lam6[6], eps6[6], ep6[6], Q[25];
   {
@@ -659,7 +670,7 @@ __device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonConst& n
       d += Q[i * 5 + j] * s0s[j];
     }
     s.x[i] = a;
-    s.c[i] = -d + e - b;
+    sh.c[i][sh.t] = -d + e - b;
   }
   {
     TF St[25], t[25];
@@ -683,7 +694,7 @@ __device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonConst& n
         TF a = 0;
 #pragma unroll
         for (int k = 0; k < 5; k++) a += t[i * 5 + k] * Q[j * 5 + k];
-        s.K[pk(i, j)] = a;
+        sh.K[pk(i, j)][sh.t] = a;
       }
   }
   const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf);
@@ -725,8 +736,9 @@ __device__ __forceinline__ void nw_accept(NewtonState<TF>& s) {
 // 0: pass done, no solve; 1: the Newton direction is needed (H, mg filled);
 // 2: the solve has ended
 template <typename TF, typename Slip>
-__device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonConst& nc, const PhaseConst& ph,
-                                         const Slip& slip, const TF* __restrict__ et, TF H[15], TF mg[5]) {
+__device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonShared<TF>& sh, const NewtonConst& nc,
+                                         const PhaseConst& ph, const Slip& slip, const TF* __restrict__ et, TF H[15],
+                                         TF mg[5]) {
   if (s.pass >= 41 * (nc.itmax + 1)) return 2;
   s.pass++;
   const TF dt = cpick<TF>(nc.dt, nc.dtf);
@@ -741,11 +753,17 @@ __device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonConst& 
     slip.template flow<true>(ph, s.xt, s.edf, Df, s.psif, nullptr);
   }
   TF Kx[5];
-  symv5<TF>(s.K, s.xt, Kx);
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    TF a = 0;
+#pragma unroll
+    for (int j = 0; j < 5; j++) a += sh.k(pk(i, j)) * s.xt[j];
+    Kx[i] = a;
+  }
   if (s.trial) {
     TF phi = 0;
 #pragma unroll
-    for (int i = 0; i < 5; i++) phi += s.xt[i] * ((TF)0.5 * Kx[i] + s.c[i]);
+    for (int i = 0; i < 5; i++) phi += s.xt[i] * ((TF)0.5 * Kx[i] + sh.cc(i));
     phi += dt * s.psif;
     if (!(phi <= s.phi0 + (TF)1e-4 * s.alpha * s.slope)) {
       TF den = (TF)2 * (phi - s.phi0 - s.slope * s.alpha);
@@ -766,7 +784,7 @@ __device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonConst& 
   if (s.done || s.it >= nc.itmax) return 2;
   TF g[5];
 #pragma unroll
-  for (int i = 0; i < 5; i++) g[i] = Kx[i] + s.c[i] + dt * s.edf[i];
+  for (int i = 0; i < 5; i++) g[i] = Kx[i] + sh.cc(i) + dt * s.edf[i];
   if (sizeof(TF) == 4 && nc.bound_stop) {
     TF den2 = s.ref2;
     if (!(den2 > (TF)0))
@@ -779,13 +797,13 @@ __device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonConst& 
     }
   }
 #pragma unroll
-  for (int i = 0; i < 15; i++) H[i] = s.K[i] + dt * Df[i];
+  for (int i = 0; i < 15; i++) H[i] = sh.k(i) + dt * Df[i];
 #pragma unroll
   for (int i = 0; i < 5; i++) mg[i] = -g[i];
   // Phi at x (= xt here), for a line search along the coming direction
   TF phi0 = 0;
 #pragma unroll
-  for (int i = 0; i < 5; i++) phi0 += s.x[i] * ((TF)0.5 * Kx[i] + s.c[i]);
+  for (int i = 0; i < 5; i++) phi0 += s.x[i] * ((TF)0.5 * Kx[i] + sh.cc(i));
   s.phi0 = phi0 + dt * s.psif;
   return 1;
 }
@@ -1049,6 +1067,7 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
   if (!is_live(it)) return;
   __shared__ TF sH[15][256];
   __shared__ TF sB[5][256];    // -g in, the direction out
+  extern __shared__ __align__(16) unsigned char coop_dyn[];   // K [15][256] and c [5][256] of each thread's solve
   __shared__ int sOk[256];
   __shared__ int sWarp[8];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -1062,6 +1081,8 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
   const TF* et = nullptr;
   typename SlipOf<LAW, TF, TSt>::type slip;
   NewtonState<TF> s;
+  const NewtonShared<TF> sh{reinterpret_cast<TF(*)[256]>(coop_dyn),
+                            reinterpret_cast<TF(*)[256]>(coop_dyn + 15 * 256 * sizeof(TF)), t};
   auto load = [&](TF* lam6, TF* eps6, TF* ep6, TF* R, bool again) {
 #pragma unroll
     for (int i = 0; i < 6; i++) {
@@ -1078,7 +1099,7 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
     if (ph.type == 0) {
       SlipOf<LAW, TF, TSt>::load(ph, f, v, slip);
       et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
-      nw_init(s, nc, et, load);
+      nw_init(s, sh, nc, et, load);
       active = true;
     } else {
 #pragma unroll
@@ -1094,7 +1115,7 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
     TF H[15], mg[5];
     int need = 0;
     if (active) {
-      const int r = nw_pass_a(s, nc, nc.ph[jph], slip, et, H, mg);
+      const int r = nw_pass_a(s, sh, nc, nc.ph[jph], slip, et, H, mg);
       if (r == 2) active = false;
       need = r == 1;
     }
@@ -1205,7 +1226,19 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     newton_kernel<float, float, double, 3, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_coop_kernel<float, float, double, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    constexpr size_t dyn = 20 * 256 * sizeof(float);
+    auto k = newton_coop_kernel<float, float, double, 3>;
+    // the opt-in above 48 KB of shared memory per block, once per device
+    static bool attr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+      if (e != cudaSuccess) return e;
+      if (dev >= 0 && dev < 64) attr[dev] = true;
+    }
+    k<<<nblocks, 256, dyn, st>>>(nc, f, partials, it);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
     newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
