@@ -1177,6 +1177,27 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
   newton_block_reduce<TF>(acc, partials, nc.ph1_only != 0);
 }
 
+// newton_coop_kernel for the FP32 fields with the FP64 solve, with its 20 KB
+// of dynamic shared memory (K and c of each thread's solve)
+template <int MINB, int LAW>
+static cudaError_t launch_coop(const NewtonConst& nc, const Fields<float>& f, double* partials, int nblocks,
+                               const IterIn& it, cudaStream_t st) {
+  constexpr size_t dyn = 20 * 256 * sizeof(float);
+  auto k = newton_coop_kernel<float, float, double, MINB, LAW>;
+  // the opt-in above 48 KB of shared memory per block, once per device
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || !attr[dev]) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) attr[dev] = true;
+  }
+  k<<<nblocks, 256, dyn, st>>>(nc, f, partials, it);
+  return cudaGetLastError();
+}
+
 void fill_float_consts(NewtonConst& nc) {
   for (int k = 0; k < 2; k++) {
     PhaseConst& ph = nc.ph[k];
@@ -1226,19 +1247,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     newton_kernel<float, float, double, 3, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    constexpr size_t dyn = 20 * 256 * sizeof(float);
-    auto k = newton_coop_kernel<float, float, double, 3>;
-    // the opt-in above 48 KB of shared memory per block, once per device
-    static bool attr[64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64 || !attr[dev]) {
-      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-      if (e != cudaSuccess) return e;
-      if (dev >= 0 && dev < 64) attr[dev] = true;
-    }
-    k<<<nblocks, 256, dyn, st>>>(nc, f, partials, it);
+    return launch_coop<3, 0>(nc, f, partials, nblocks, it, st);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
     newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
