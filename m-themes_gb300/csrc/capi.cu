@@ -584,6 +584,7 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     }                                                                                              \
   } while (0)
   CKC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  CKC(prepare_newton_kernels());
   const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
   const long long P = c->nv;
   const int nplanes = 6 + 6 + 6 + 6 + 9 + 12 + 1 + 3;

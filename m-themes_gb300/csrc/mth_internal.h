@@ -144,6 +144,8 @@ constexpr int NPART_END = 12;  // epsp[6], edot[6]
 // Fields::ddc, harden off)
 cudaError_t launch_newton(int mixed, const NewtonConst& nc, const void* fields, double* partials, int nblocks,
                           const IterIn& it, cudaStream_t st, int law = 0);
+// kernel attributes the Newton launches need, set on the current device
+cudaError_t prepare_newton_kernels();
 cudaError_t launch_end_step(int mixed, const NewtonConst& nc, const void* fields, const double anti_uniform[3],
                             int do_orient, int do_harden, double* partials, int nblocks, cudaStream_t st, int law = 0);
 cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, const double* euler,

@@ -1179,24 +1179,34 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
 
 // newton_coop_kernel for the FP32 fields with the FP64 solve, with its 20 KB
 // of dynamic shared memory (K and c of each thread's solve)
+constexpr size_t COOP_DYN = 20 * 256 * sizeof(float);
+
+// the opt-in above 48 KB of shared memory per block, once per device (also
+// done by prepare_newton_kernels when a context is created, so that no
+// attribute call falls inside a stream capture)
 template <int MINB, int LAW>
-static cudaError_t launch_coop(const NewtonConst& nc, const Fields<float>& f, double* partials, int nblocks,
-                               const IterIn& it, cudaStream_t st) {
-  constexpr size_t dyn = 20 * 256 * sizeof(float);
-  auto k = newton_coop_kernel<float, float, double, MINB, LAW>;
-  // the opt-in above 48 KB of shared memory per block, once per device
+static cudaError_t coop_attr() {
   static bool attr[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64 || !attr[dev]) {
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    if (e != cudaSuccess) return e;
-    if (dev >= 0 && dev < 64) attr[dev] = true;
-  }
-  k<<<nblocks, 256, dyn, st>>>(nc, f, partials, it);
+  if (dev >= 0 && dev < 64 && attr[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(newton_coop_kernel<float, float, double, MINB, LAW>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COOP_DYN);
+  if (e == cudaSuccess && dev >= 0 && dev < 64) attr[dev] = true;
+  return e;
+}
+
+template <int MINB, int LAW>
+static cudaError_t launch_coop(const NewtonConst& nc, const Fields<float>& f, double* partials, int nblocks,
+                               const IterIn& it, cudaStream_t st) {
+  cudaError_t e = coop_attr<MINB, LAW>();
+  if (e != cudaSuccess) return e;
+  newton_coop_kernel<float, float, double, MINB, LAW><<<nblocks, 256, COOP_DYN, st>>>(nc, f, partials, it);
   return cudaGetLastError();
 }
+
+cudaError_t prepare_newton_kernels() { return coop_attr<3, 0>(); }
 
 void fill_float_consts(NewtonConst& nc) {
   for (int k = 0; k < 2; k++) {
