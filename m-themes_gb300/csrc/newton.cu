@@ -346,282 +346,17 @@ struct VoxelOut {
   int failed;
 };
 
-// Local solve of one crystal voxel.  lam6/eps6/ep6: LT sample-frame inputs
-// (lambda = current stress, total strain, plastic strain); Q: sample->crystal
-// 5x5 of the current lattice orientation; et: elastic-class row (initial
-// orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
-// (plastic strain rate, sample frame).
-// TF: flow rule, residual, Hessian assembly, line search and frame
-// transforms; TL: precision of the Jacobian (Hessian) solve.  FP64 mode:
-// both double.  Mixed mode: TF = float, TL = double: the FP32-assembled 5x5
-// system is factored and solved in FP64 at every Newton step.  Mixed
-// root-FP64 mode (ROOT_ONLY): the FP64 solve only for the steps within
-// 1e-3 |lambda| of the root, which set the converged answer, and the FP32
-// factorisation for the large early steps, whose direction only has to be a
-// descent direction (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
-// mode: all float.
-// load(lam6, eps6, ep6, R, again) fills the voxel's inputs; it is called
-// at the start and again (again = true: loads the compiler may not merge
-// with the first) for the back-transform and the error norms, so neither
-// the inputs nor the 5x5 frame rotation stay live across the Newton loop.
-template <typename TF, typename TL, bool ROOT_ONLY, typename Slip, typename Load>
-__device__ VoxelOut<TF> solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const Slip& slip,
-                                const Load& load, TF* sig6, TF* ed6) {
-  VoxelOut<TF> o = {(TF)0, (TF)0, 0, 0};
-  const TF dt = cpick<TF>(nc.dt, nc.dtf);
-  TF x[5], c[5], K[15];
-  TF h, ref2, dh;
-  const TF shh = et[ET_SEL_HH];
-  {
-  TF lam6[6], eps6[6], ep6[6], Q[25];
-  {
-    TF R[9];
-    load(lam6, eps6, ep6, R, false);
-    rot_to_q<TF>(R, Q);
-  }
-  // crystal-frame inputs
-  TF lamx[5], epsx[5], epx[5], s0s[5];
-#pragma unroll
-  for (int i = 0; i < 5; i++) {
-    TF a = 0;
-#pragma unroll
-    for (int j = 0; j < 5; j++) a += cpick<TF>(nc.s0dev[i * 5 + j], nc.s0devf[i * 5 + j]) * lam6[j];
-    s0s[i] = a;   // S0 lambda, sample axes
-  }
-#pragma unroll
-  for (int i = 0; i < 5; i++) {
-    TF a = 0, b = 0, e = 0, d = 0;
-#pragma unroll
-    for (int j = 0; j < 5; j++) {
-      a += Q[i * 5 + j] * lam6[j];
-      b += Q[i * 5 + j] * eps6[j];
-      e += Q[i * 5 + j] * ep6[j];
-      d += Q[i * 5 + j] * s0s[j];
-    }
-    lamx[i] = a; epsx[i] = b; epx[i] = e;
-    c[i] = -d + e - b;   // gradient of Phi = K x + c + dt edot
-  }
-  // Hessian base K = Q (S0 + S_gr) Q^T in crystal axes of the current lattice
-  {
-    TF St[25], t[25];
-#pragma unroll
-    for (int i = 0; i < 5; i++)
-#pragma unroll
-      for (int j = 0; j < 5; j++) St[i * 5 + j] = et[ET_STOT + pk(i, j)];
-#pragma unroll
-    for (int i = 0; i < 5; i++)
-#pragma unroll
-      for (int j = 0; j < 5; j++) {
-        TF a = 0;
-#pragma unroll
-        for (int k = 0; k < 5; k++) a += Q[i * 5 + k] * St[k * 5 + j];
-        t[i * 5 + j] = a;
-      }
-#pragma unroll
-    for (int i = 0; i < 5; i++)
-#pragma unroll
-      for (int j = i; j < 5; j++) {
-        TF a = 0;
-#pragma unroll
-        for (int k = 0; k < 5; k++) a += t[i * 5 + k] * Q[j * 5 + k];
-        K[pk(i, j)] = a;
-      }
-  }
-  // hydrostatic part in closed form
-  const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf);
-  h = (s0hh * lam6[5] + eps6[5] - ep6[5]) / (s0hh + shh);
-  ref2 = 0;
-#pragma unroll
-  for (int i = 0; i < 6; i++) ref2 += lam6[i] * lam6[i];
-  dh = h - lam6[5];
-#pragma unroll
-  for (int i = 0; i < 5; i++) x[i] = lamx[i];
-  }
-  const TF tol2 = cpick<TF>(nc.tol, nc.tolf) * cpick<TF>(nc.tol, nc.tolf);
-  const TF ls_thr2 = (TF)1e-6 * ref2;   // line search only for steps > 1e-3 |lambda|
-  // Newton with a backtracking line search on Phi for large steps.  One
-  // flow-rule evaluation site: every evaluation (with its Hessian) is at the
-  // point the loop moves to next, so an accepted line-search trial supplies
-  // the next Newton step and the last accepted iterate supplies the final
-  // rates, without evaluating any point twice.
-  int it = 0;
-  bool done = false;
-  bool near_root = false;   // previous step within 1e-3 |lambda|
-  TF hstep2 = dh * dh;      // the first step includes the hydrostatic correction
-  TF xt[5];                 // point evaluated next
-#pragma unroll
-  for (int i = 0; i < 5; i++) xt[i] = x[i];
-  bool trial = false;       // xt is a line-search trial x + alpha p
-  int ls = 0;
-  TF p[5], pn2 = 0, slope = 0, phi0 = 0, alpha = 1;
-  TF edf[5], psif;          // rates and psi at the last evaluated point
-  auto accept_step = [&]() {
-#pragma unroll
-    for (int i = 0; i < 5; i++) x[i] += alpha * p[i];
-    const TF step2 = alpha * alpha * pn2 + hstep2;
-    hstep2 = 0;
-    near_root = step2 <= ls_thr2;
-    TF den2 = ref2;
-    if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
-    if (!(den2 > (TF)0) || step2 <= tol2 * den2) done = true;
-    it++;
-  };
-  const int max_pass = 41 * (nc.itmax + 1);   // each Newton step: at most 40 trials + 1
-  for (int pass = 0; pass < max_pass; pass++) {
-    TF Df[15];
-    if (nc.flow_off) {
-#pragma unroll
-      for (int i = 0; i < 5; i++) edf[i] = 0;
-#pragma unroll
-      for (int i = 0; i < 15; i++) Df[i] = 0;
-      psif = 0;
-    } else {
-      slip.template flow<true>(ph, xt, edf, Df, psif, nullptr);
-    }
-    TF Kx[5];
-    symv5<TF>(K, xt, Kx);
-    if (trial) {
-      TF phi = 0;
-#pragma unroll
-      for (int i = 0; i < 5; i++) phi += xt[i] * ((TF)0.5 * Kx[i] + c[i]);
-      phi += dt * psif;
-      if (!(phi <= phi0 + (TF)1e-4 * alpha * slope)) {
-        TF den = (TF)2 * (phi - phi0 - slope * alpha);
-        TF an = den > (TF)0 ? -slope * alpha * alpha / den : (TF)0.5 * alpha;
-        an = fmin(an, (TF)0.5 * alpha);
-        alpha = fmax(an, (TF)0.1 * alpha);
-        ls++;
-#pragma unroll
-        for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
-        if (!(alpha * alpha * pn2 <= (TF)1e-28 * (ref2 + (TF)1)) && ls < 40) continue;
-        // step too small or trials exhausted: take it and evaluate there
-        accept_step();
-        trial = false;
-        continue;
-      }
-      accept_step();   // x + alpha p, the point just evaluated
-      trial = false;
-    }
-    // rates, Hessian and psi of the current iterate x are at hand
-    if (done || it >= nc.itmax) break;
-    TF g[5];
-#pragma unroll
-    for (int i = 0; i < 5; i++) g[i] = Kx[i] + c[i] + dt * edf[i];
-    if (sizeof(TF) == 4 && nc.bound_stop) {
-      // The next step p = -H^-1 g has |p| <= |g| / lambda_min(H) <=
-      // |g| / lambda_min(K), as H = K + dt D with D = sum w m m^T positive
-      // semidefinite; when that bound is within the tolerance the step the
-      // reference would take next is too, and x is the answer to within it.
-      TF den2 = ref2;
-      if (!(den2 > (TF)0)) den2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + h * h;
-      const TF mu = et[ET_STOT_MIN];
-      const TF gn2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + g[3] * g[3] + g[4] * g[4];
-      if (gn2 <= tol2 * den2 * mu * mu) {
-        done = true;
-        break;
-      }
-    }
-    {
-      TF H[15], mg[5];
-#pragma unroll
-      for (int i = 0; i < 15; i++) H[i] = K[i] + dt * Df[i];
-#pragma unroll
-      for (int i = 0; i < 5; i++) mg[i] = -g[i];
-      bool ok;
-      if (sizeof(TL) > sizeof(TF) && (!ROOT_ONLY || near_root)) {
-        // Jacobian solve in TL (FP64) of the TF-assembled system: at every
-        // step, or (ROOT_ONLY) for the steps within 1e-3 |lambda| of the
-        // root, which set the converged answer
-        ok = ldl_solve5_wide<TF, TL>(H, mg, p);
-      } else {
-        ok = ldl_solve5<TF>(H, mg, p);
-      }
-      if (!ok) { o.failed = 1; break; }
-    }
-    pn2 = 0;
-    slope = 0;
-#pragma unroll
-    for (int i = 0; i < 5; i++) { pn2 += p[i] * p[i]; slope += g[i] * p[i]; }
-    alpha = 1;
-    if (pn2 > ls_thr2 && !nc.flow_off) {
-      // line search on Phi for large steps; near the root the full step
-      phi0 = 0;
-#pragma unroll
-      for (int i = 0; i < 5; i++) phi0 += x[i] * ((TF)0.5 * Kx[i] + c[i]);
-      phi0 += dt * psif;
-      ls = 0;
-      trial = true;
-#pragma unroll
-      for (int i = 0; i < 5; i++) xt[i] = x[i] + alpha * p[i];
-      continue;
-    }
-    accept_step();
-#pragma unroll
-    for (int i = 0; i < 5; i++) xt[i] = x[i];
-  }
-  o.iters = it;
-  if (!done) o.failed = 1;
-  // final rates at the solution: the last evaluation was at x
-  TF edx[5];
-#pragma unroll
-  for (int i = 0; i < 5; i++) edx[i] = edf[i];
-  TF lam6[6], eps6[6], ep6[6], Q[25];
-  {
-    TF R[9];
-    load(lam6, eps6, ep6, R, true);
-    rot_to_q<TF>(R, Q);
-  }
-  // back to sample axes: s = Q^T x, edot = Q^T edot_x
-  TF ss[5], es[5];
-#pragma unroll
-  for (int j = 0; j < 5; j++) {
-    TF a = 0, b = 0;
-#pragma unroll
-    for (int i = 0; i < 5; i++) {
-      a += Q[i * 5 + j] * x[i];
-      b += Q[i * 5 + j] * edx[i];
-    }
-    ss[j] = a;
-    es[j] = b;
-  }
-  // error contributions (src/evolution.c:264-299): |sig - lambda| and
-  // |S_gr sig + e_p + edot dt - e|, in sample axes; summed over voxels in FP64
-  TF cs = dh * dh, ce = 0;
-#pragma unroll
-  for (int i = 0; i < 5; i++) {
-    const TF ds = ss[i] - lam6[i];
-    cs += ds * ds;
-    TF de = ep6[i] + dt * es[i] - eps6[i];
-#pragma unroll
-    for (int j = 0; j < 5; j++) de += et[ET_SEL + pk(i, j)] * ss[j];
-    ce += de * de;
-  }
-  {
-    const TF de = ep6[5] + shh * h - eps6[5];
-    ce += de * de;
-  }
-  o.conv_s = sqrt(cs);
-  o.conv_e = sqrt(ce);
-#pragma unroll
-  for (int j = 0; j < 5; j++) {
-    sig6[j] = ss[j];
-    ed6[j] = es[j];
-  }
-  sig6[5] = h;
-  ed6[5] = 0;
-  return o;
-}
-
-// ----------------------------------------- block-cooperative local solve
-// The local solve of solve_voxel in pieces, for newton_coop_kernel: nw_init
-// (set-up), nw_pass_a (one flow-rule evaluation and what it decides; when
-// the next Newton direction is needed it returns the system H p = -g) and
-// nw_pass_b (the move the direction gives), with the Jacobian solves of all
-// the block's threads done between them by as few threads as there are
-// systems.  Same arithmetic and order as solve_voxel.
-// The linear term c and the Hessian base K of Phi, constant during a solve,
-// live in shared memory (component-major, one column per thread), so the
-// registers hold only what changes.
+// ------------------------------------------------- the local solve, in pieces
+// nw_init (set-up), nw_pass_a (one flow-rule evaluation and what it decides;
+// when the next Newton direction is needed it returns the system H p = -g),
+// nw_pass_b (the move the direction gives) and nw_finish (back to sample
+// axes, error contributions).  solve_voxel runs them with its own Jacobian
+// solve in between; newton_coop_kernel runs the Jacobian solves of all the
+// threads of a block between them, done by as few threads as there are
+// systems.  The linear term c and the Hessian base K of Phi, constant during
+// a solve, are in registers (NewtonRegs) or in shared memory (NewtonShared:
+// component-major, one column per thread, so the registers hold only what
+// changes).
 template <typename TF>
 struct NewtonShared {
   TF (*K)[256];   // [15][256]
@@ -629,6 +364,17 @@ struct NewtonShared {
   int t;
   __device__ __forceinline__ TF k(int i) const { return K[i][t]; }
   __device__ __forceinline__ TF cc(int i) const { return c[i][t]; }
+  __device__ __forceinline__ void set_k(int i, TF v) const { K[i][t] = v; }
+  __device__ __forceinline__ void set_c(int i, TF v) const { c[i][t] = v; }
+};
+// the same in registers (one solve per thread)
+template <typename TF>
+struct NewtonRegs {
+  TF K[15], c[5];
+  __device__ __forceinline__ TF k(int i) const { return K[i]; }
+  __device__ __forceinline__ TF cc(int i) const { return c[i]; }
+  __device__ __forceinline__ void set_k(int i, TF v) { K[i] = v; }
+  __device__ __forceinline__ void set_c(int i, TF v) { c[i] = v; }
 };
 template <typename TF>
 struct NewtonState {
@@ -641,8 +387,8 @@ struct NewtonState {
   bool done, near_root, trial, failed;
 };
 
-template <typename TF, typename Load>
-__device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonShared<TF>& sh, const NewtonConst& nc,
+template <typename TF, typename Store, typename Load>
+__device__ __forceinline__ void nw_init(NewtonState<TF>& s, Store& sh, const NewtonConst& nc,
                                         const TF* __restrict__ et, const Load& load) {
   const TF shh = et[ET_SEL_HH];
   TF lam6[6], eps6[6], ep6[6], Q[25];
@@ -670,7 +416,7 @@ __device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonShared<T
       d += Q[i * 5 + j] * s0s[j];
     }
     s.x[i] = a;
-    sh.c[i][sh.t] = -d + e - b;
+    sh.set_c(i, -d + e - b);
   }
   {
     TF St[25], t[25];
@@ -694,7 +440,7 @@ __device__ __forceinline__ void nw_init(NewtonState<TF>& s, const NewtonShared<T
         TF a = 0;
 #pragma unroll
         for (int k = 0; k < 5; k++) a += t[i * 5 + k] * Q[j * 5 + k];
-        sh.K[pk(i, j)][sh.t] = a;
+        sh.set_k(pk(i, j), a);
       }
   }
   const TF s0hh = cpick<TF>(nc.s0hh, nc.s0hhf);
@@ -733,10 +479,16 @@ __device__ __forceinline__ void nw_accept(NewtonState<TF>& s) {
   s.it++;
 }
 
-// 0: pass done, no solve; 1: the Newton direction is needed (H, mg filled);
-// 2: the solve has ended
-template <typename TF, typename Slip>
-__device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const NewtonShared<TF>& sh, const NewtonConst& nc,
+// Newton with a backtracking line search on Phi for large steps.  One
+// flow-rule evaluation site: every evaluation (with its Hessian) is at the
+// point the solve moves to next, so an accepted line-search trial supplies
+// the next Newton step and the last accepted iterate supplies the final
+// rates, without evaluating any point twice.  At most 41 (itmax + 1)
+// passes: each Newton step takes at most 40 trials + 1.
+// Returns 0: pass done, no solve; 1: the Newton direction is needed (H, mg
+// filled); 2: the solve has ended.
+template <typename TF, typename Store, typename Slip>
+__device__ __forceinline__ int nw_pass_a(NewtonState<TF>& s, const Store& sh, const NewtonConst& nc,
                                          const PhaseConst& ph, const Slip& slip, const TF* __restrict__ et, TF H[15],
                                          TF mg[5]) {
   if (s.pass >= 41 * (nc.itmax + 1)) return 2;
@@ -888,6 +640,50 @@ __device__ __forceinline__ VoxelOut<TF> nw_finish(const NewtonState<TF>& s, cons
   sig6[5] = s.h;
   ed6[5] = 0;
   return o;
+}
+
+// Local solve of one crystal voxel.  lam6/eps6/ep6: LT sample-frame inputs
+// (lambda = current stress, total strain, plastic strain); Q: sample->crystal
+// 5x5 of the current lattice orientation; et: elastic-class row (initial
+// orientation); tauf: forward CRSS.  Outputs sig6 (sample frame) and ed6
+// (plastic strain rate, sample frame).
+// TF: flow rule, residual, Hessian assembly, line search and frame
+// transforms; TL: precision of the Jacobian (Hessian) solve.  FP64 mode:
+// both double.  Mixed mode: TF = float, TL = double: the FP32-assembled 5x5
+// system is factored and solved in FP64 at every Newton step.  Mixed
+// root-FP64 mode (ROOT_ONLY): the FP64 solve only for the steps within
+// 1e-3 |lambda| of the root, which set the converged answer, and the FP32
+// factorisation for the large early steps, whose direction only has to be a
+// descent direction (GB300 issues FP64 at 1/64 of the FP32 rate).  Fast
+// mode: all float.
+// load(lam6, eps6, ep6, R, again) fills the voxel's inputs; it is called
+// at the start and again (again = true: loads the compiler may not merge
+// with the first) for the back-transform and the error norms, so neither
+// the inputs nor the 5x5 frame rotation stay live across the Newton loop.
+template <typename TF, typename TL, bool ROOT_ONLY, typename Slip, typename Load>
+__device__ VoxelOut<TF> solve_voxel(const NewtonConst& nc, const PhaseConst& ph, const TF* __restrict__ et, const Slip& slip,
+                                    const Load& load, TF* sig6, TF* ed6) {
+  NewtonState<TF> s;
+  NewtonRegs<TF> r;
+  nw_init(s, r, nc, et, load);
+  for (;;) {
+    TF H[15], mg[5];
+    const int k = nw_pass_a(s, r, nc, ph, slip, et, H, mg);
+    if (k == 2) break;
+    if (k == 0) continue;
+    TF p[5];
+    bool ok;
+    if (sizeof(TL) > sizeof(TF) && (!ROOT_ONLY || s.near_root)) {
+      // Jacobian solve in TL (FP64) of the TF-assembled system: at every
+      // step, or (ROOT_ONLY) for the steps within 1e-3 |lambda| of the
+      // root, which set the converged answer
+      ok = ldl_solve5_wide<TF, TL>(H, mg, p);
+    } else {
+      ok = ldl_solve5<TF>(H, mg, p);
+    }
+    if (!nw_pass_b(s, nc, p, ok, mg)) break;
+  }
+  return nw_finish(s, nc, et, load, sig6, ed6);
 }
 
 // ------------------------------------------------------------ reductions
