@@ -82,7 +82,10 @@ typedef struct {
   int    hard_flag;          /* Hard_Flag: Voce hardening */
   int    precision;          /* mth_precision */
   double newton_tol;         /* local Newton tolerance; <=0 selects the default
-                                (1e-10 FP64 as in src/evolution.c:104, 1e-6 mixed) */
+                                (1e-10 FP64 as in src/evolution.c:104, 1e-6 mixed).  A solve
+                                ends when its last step is within it; in the mixed modes also
+                                when the next step is bounded within it (|gradient| over the
+                                smallest eigenvalue of the elastic Hessian base) */
   int    newton_itmax;       /* <=0 selects 500 (src/evolution.c:105) */
   /* Phase-field / DRX block (src/io.c:71-90) */
   double pf_length_scale;    /* dx [m] */
