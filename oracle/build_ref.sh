@@ -1,14 +1,14 @@
 #!/bin/bash
 # Builds the reference M-THEMES `forge` from its sources where they lie
-# (MTH_REFERENCE, default /root/reference) into oracle/_ref/ only, for
-# pinning the oracle.  It compiles the reference's own 8 translation units
+# (the directory named by MTH_REFERENCE, required) into oracle/_ref/ only,
+# for pinning the oracle.  It compiles the reference's own 8 translation units
 # (src/Makefile:11) with single-rank MPI/FFTW-MPI/GSL stand-ins
 # (oracle/refshim) and serial FFTW 2.1.5 built from the vendored tarball.
 # The reference's build system and MPICH are not used.  x86 or Arm host; no
 # GPU needed.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${MTH_REFERENCE:-/root/reference}"
+REF="${MTH_REFERENCE:?set MTH_REFERENCE to the reference checkout}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then echo "reference sources not found at $REF" >&2; exit 2; fi
 mkdir -p "$OUT/obj"
@@ -38,10 +38,18 @@ $CXX -x c++ "${COMMON[@]}" -DAvgDislocation=mth_ref_dd_after_step -DVonMises=mth
 # and with DD_CU as src/evpFlags.h ships it (fixed Cu elastic constants,
 # src/init.c:821-825), for runs on the unmodified test_run/ inputs
 $CXX -x c++ "${COMMON[@]}" -DDD_CU -c "$REF/src/init.c" -o "$OUT/obj/init_ddcu.o" &
+# the DRX harness: PF_XRX with the per-substep grid hook of mth_ref_prelude.h,
+# and evp.c without its main() for the global definitions
+$CXX -x c++ "${COMMON[@]}" -DMTH_PF_HOOK -c "$REF/src/pf_xrx.c" -o "$OUT/obj/pf_xrx_hook.o" &
+$CXX -x c++ "${COMMON[@]}" ${EXTRA[evp.c]} -Dmain=mth_ref_evp_main -c "$REF/src/evp.c" -o "$OUT/obj/evp_nomain.o" &
+$CXX "${COMMON[@]}" -DMTH_PF_HOOK -c "$HERE/refshim/drx_harness.cc" -o "$OUT/obj/drx_harness.o" &
 wait
 $CXX -o "$OUT/forge_ref" "${OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
 DD_OBJS=("${OBJS[@]/evolution.o/evolution_dd.o}")
 $CXX -o "$OUT/forge_ref_dd" "${DD_OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
 DDCU_OBJS=("${DD_OBJS[@]/init.o/init_ddcu.o}")
 $CXX -o "$OUT/forge_ref_dd_cu" "${DDCU_OBJS[@]}" "$OUT/obj/refshim.o" -L"$OUT/fftw/lib" -lfftw -lm
-echo "built $OUT/forge_ref $OUT/forge_ref_dd $OUT/forge_ref_dd_cu"
+H_OBJS=("${OBJS[@]/evp.o/evp_nomain.o}")
+H_OBJS=("${H_OBJS[@]/pf_xrx.o/pf_xrx_hook.o}")
+$CXX -o "$OUT/drx_ref" "${H_OBJS[@]}" "$OUT/obj/refshim.o" "$OUT/obj/drx_harness.o" -L"$OUT/fftw/lib" -lfftw -lm
+echo "built $OUT/forge_ref $OUT/forge_ref_dd $OUT/forge_ref_dd_cu $OUT/drx_ref"

@@ -5,33 +5,26 @@
  * CPU restatement, in FP64, of the dynamic-recrystallisation step of
  * M-THEMES: grain-boundary indicator (Gradient_ExchangeGrainID,
  * src/constitutive.c:724-873 and src/evolution.c:816-829), nucleation
- * (NucleationCheckDRX, src/integrated.c:161-494) and the sparse
+ * (NucleationCheckDRX, src/integrated.c:161-494), the sparse
  * order-parameter Allen-Cahn relaxation (PF_XRX / Update_grid / Update_gID,
- * src/pf_xrx.c:6-66,895-1311,1469-1698), in the deterministic form this
- * build defines (the reference's sparse lists are mutated during the sweep
- * and share a global rho_avg table, so its result depends on sweep order):
+ * src/pf_xrx.c:6-66,895-1311,1469-1698), restated statement by statement
+ * (section "phase field" below), and the grid transfer of InterpolateGrid
+ * (src/integrated.c:496-760).
  *
- *  - at most K order parameters per voxel, stored sorted by grain id;
- *  - the neighbourhood id set N(v) = ids with eta > 5e-3 in the 3x3x3 block
- *    (src/pf_xrx.c:937-973, EPSILON of src/PFgrid.h:49);
- *  - the stored-energy average of grain j at v is the mean of rho over the
- *    7x7x7 window voxels whose current grain id is j (src/pf_xrx.c:1052-1086),
- *    computed for every j in N(v) and every id held at v;
- *  - the explicit update of src/pf_xrx.c:1184-1233 for every j in N(v) when
- *    |N(v)| > 1, values <= 1e-4 dropped (src/pf_xrx.c:1207,1221); a copy when
- *    |N(v)| == 1; the K largest values kept;
- *  - grain id = argmax eta, ties to the smaller id (Update_gID,
- *    src/pf_xrx.c:11-66).
- * Nucleation: a grain-boundary voxel of a crystal phase whose total
- * dislocation density exceeds rho_nucleation nucleates with probability
- * nucleation_prob per step, drawn from a counter-based generator of
- * (seed, step, voxel); nuclei are numbered in voxel order and paint a
- * periodic disc |d|^2 <= r^2 (src/integrated.c:400), later nuclei over
- * earlier ones.
+ * Nucleation: a grain-boundary voxel (the reference's indicator, which skips
+ * the -z face) of a crystal phase whose dislocation density exceeds
+ * rho_nucleation nucleates with probability nucleation_prob per step, drawn
+ * from a counter-based generator of (seed, step, voxel) (the reference's
+ * static branch is the case nucleation_prob = 1 with a uniform threshold);
+ * nuclei are numbered in voxel order and paint every voxel within squared
+ * distance nucleus_radius, without periodic images (src/integrated.c:400),
+ * later nuclei over earlier ones.
  *
- * Compiled with -ffp-contract=off: every floating-point operation is a
- * separately rounded IEEE operation in a fixed order, which the CUDA kernels
- * reproduce (-fmad=false) so FP64 grain maps can be compared bit for bit.
+ * Pinned against the reference's own functions, run on crafted inputs by
+ * oracle/refshim/drx_harness.cc (tests/golden/pf_*.npz, nucl_*.npz,
+ * interp_*.npz).  Compiled with -ffp-contract=off: every floating-point
+ * operation is a separately rounded IEEE operation in the reference's order,
+ * which the CUDA kernels reproduce (-fmad=false).
  */
 #include <math.h>
 #include <stdint.h>
@@ -72,7 +65,12 @@ static inline long long vidx(const int* n, int x, int y, int z) {
   return ((long long)x * n[1] + y) * n[2] + z;
 }
 
-/* 1 where a face neighbour (periodic) belongs to another grain. */
+/* Grain-boundary indicator of src/evolution.c:816-829 from the checks of
+ * Gradient_ExchangeGrainID (src/constitutive.c:724-873), periodic: 1 where
+ * the +x, -x, +y, -y or +z neighbour belongs to another grain.  The
+ * reference's "-z" check compares with the -y neighbour
+ * (src/constitutive.c:808,831,853), so a difference across the -z face alone
+ * does not mark a voxel. */
 void orc_gb_indicator(const int* n, const int* grain, unsigned char* gb) {
   for (int x = 0; x < n[0]; x++)
     for (int y = 0; y < n[1]; y++)
@@ -81,7 +79,7 @@ void orc_gb_indicator(const int* n, const int* grain, unsigned char* gb) {
         int g = grain[v];
         int b = (grain[vidx(n, x + 1, y, z)] != g) | (grain[vidx(n, x - 1, y, z)] != g) |
                 (grain[vidx(n, x, y + 1, z)] != g) | (grain[vidx(n, x, y - 1, z)] != g) |
-                (grain[vidx(n, x, y, z + 1)] != g) | (grain[vidx(n, x, y, z - 1)] != g);
+                (grain[vidx(n, x, y, z + 1)] != g);
         gb[v] = (unsigned char)b;
       }
 }
@@ -106,190 +104,266 @@ long long orc_nucleation_sites(const int* n, const int* grain, const int* phase_
   return k;
 }
 
-void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, int first_id, int radius) {
-  const int r2 = radius * radius;
+void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, int first_id, int radius2) {
+  /* src/integrated.c:397-402: every voxel whose squared distance to the
+   * nucleus is <= nucleus_radius, without periodic images */
+  int r = 0;
+  while ((r + 1) * (r + 1) <= radius2) r++;
   for (int k = 0; k < nn; k++) {
     long long v = sites[k];
     int x0 = (int)(v / ((long long)n[1] * n[2])), y0 = (int)((v / n[2]) % n[1]), z0 = (int)(v % n[2]);
-    for (int dx = -radius; dx <= radius; dx++)
-      for (int dy = -radius; dy <= radius; dy++)
-        for (int dz = -radius; dz <= radius; dz++)
-          if (dx * dx + dy * dy + dz * dz <= r2) grain[vidx(n, x0 + dx, y0 + dy, z0 + dz)] = first_id + k;
-  }
-}
-
-/* eta of grain id at voxel w (0 when absent) */
-static inline double eta_of(const int* ids, const double* phi, const int* cnt, int K, long long w, int id) {
-  for (int s = 0; s < cnt[w]; s++)
-    if (ids[w * K + s] == id) return phi[w * K + s];
-  return 0.0;
-}
-
-static void sorted_insert(int* list, int* nl, int id) {
-  int i = 0;
-  while (i < *nl && list[i] < id) i++;
-  if (i < *nl && list[i] == id) return;
-  if (*nl >= MAXIDS) return;
-  for (int j = *nl; j > i; j--) list[j] = list[j - 1];
-  list[i] = id;
-  (*nl)++;
-}
-
-/* one explicit substep: (ids,phi,cnt) -> (ids2,phi2,cnt2); gid/rho: current
-   grain ids and stored energy used by the window averages */
-static void pf_substep(const int* n, int K, const int* ids, const double* phi, const int* cnt, int* ids2,
-                       double* phi2, int* cnt2, const int* gid, const double* rho, double mcoef, double kappa,
-                       double mwell, double edisl) {
-  const long long nv = (long long)n[0] * n[1] * n[2];
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long v = 0; v < nv; v++) {
-    const int x = (int)(v / ((long long)n[1] * n[2])), y = (int)((v / n[2]) % n[1]), z = (int)(v % n[2]);
-    int nid[MAXIDS], nn = 0;
-    for (int dx = -1; dx <= 1; dx++)
-      for (int dy = -1; dy <= 1; dy++)
-        for (int dz = -1; dz <= 1; dz++) {
-          long long w = vidx(n, x + dx, y + dy, z + dz);
-          for (int s = 0; s < cnt[w]; s++)
-            if (phi[w * K + s] > PF_EPS) sorted_insert(nid, &nn, ids[w * K + s]);
+    for (int dx = -r; dx <= r; dx++)
+      for (int dy = -r; dy <= r; dy++)
+        for (int dz = -r; dz <= r; dz++) {
+          const int x = x0 + dx, y = y0 + dy, z = z0 + dz;
+          if (x < 0 || x >= n[0] || y < 0 || y >= n[1] || z < 0 || z >= n[2]) continue;
+          if (dx * dx + dy * dy + dz * dz <= radius2) grain[vidx(n, x, y, z)] = first_id + k;
         }
-    if (nn <= 1) {
-      cnt2[v] = cnt[v];
-      for (int s = 0; s < K; s++) {
-        ids2[v * K + s] = s < cnt[v] ? ids[v * K + s] : 0;
-        phi2[v * K + s] = s < cnt[v] ? phi[v * K + s] : 0.0;
+  }
+}
+
+/* ------------------------------------------------------------ phase field
+ * Literal restatement of PF_XRX / Update_grid / Update_gID
+ * (src/pf_xrx.c:6-66,895-1311,1469-1698) for one rank, statement by
+ * statement where the result depends on it:
+ *  - the grid carries three halo layers per side (l = L + 6), refilled from
+ *    the periodic interior after every sweep (boundary_conditions,
+ *    src/pf_xrx.c:253-679): halo lists are copies, so reads of a halo do not
+ *    change the interior voxel it mirrors;
+ *  - each voxel holds an ordered list of (id, eta); lookups follow
+ *    PFdata::operator[] (src/PFgrid.h:70-90): a missing id takes over the
+ *    last entry when that entry is below EPSILON, else a (id, 0) entry is
+ *    appended -- reads of neighbours and of the voxel itself do this too,
+ *    during the sweep, on the grid being read;
+ *  - the sweep runs x, y, z over the interior; a voxel holding more than one
+ *    entry when the sweep reaches it is updated, one holding a single entry
+ *    copies its values of the ids in N(v) (src/pf_xrx.c:1276-1283); N(v) =
+ *    ids with eta > EPSILON over the 3x3x3 block in scan order
+ *    (src/pf_xrx.c:937-973);
+ *  - stored-energy averages over the 7x7x7 window use the grain map of the
+ *    start of the call (GID of PF_XRX: only its halos are refreshed,
+ *    src/pf_xrx.c:683-893) and the energy buffer, summed in window order per
+ *    held entry (src/pf_xrx.c:1052-1086) and written to the caller's rho_avg
+ *    table, from which ids not held at v read what earlier voxels left
+ *    (src/pf_xrx.c:1089-1095,1184-1233);
+ *  - a recrystallised id (> init_gid) that passes 0.5 at a voxel sets that
+ *    voxel's stored energy to 100 for the rest of the call (src/pf_xrx.c:
+ *    1217-1219); the Laplacian adds its twelve edge terms in the order its
+ *    parameters are bound at the call (src/pf_xrx.c:6-9 against :1193-1198);
+ *  - grain id = first maximum of the list, 0 when every eta <= 0
+ *    (src/pf_xrx.c:11-66).
+ * The GPU computes the same sweep in parallel passes (drx.cu); tests require
+ * both to agree bit for bit in FP64. */
+#define PF_OCAP 24
+
+typedef struct {
+  int n;
+  int id[PF_OCAP];
+  double v[PF_OCAP];
+} pf_list;
+
+/* PFdata::operator[]: slot of id j, taking over a weak last entry or
+ * appending; -1 (and *over set) when the list is full */
+static int pf_slot(pf_list* l, int j, int* over) {
+  for (int k = 0; k < l->n; k++)
+    if (l->id[k] == j) return k;
+  if (l->n > 0 && l->v[l->n - 1] < PF_EPS) {
+    l->id[l->n - 1] = j;
+    return l->n - 1;
+  }
+  if (l->n == PF_OCAP) { *over = 1; return -1; }
+  l->id[l->n] = j;
+  l->v[l->n] = 0.0;
+  return l->n++;
+}
+static double pf_rd(pf_list* l, int j, int* over) {
+  int k = pf_slot(l, j, over);
+  return k < 0 ? 0.0 : l->v[k];
+}
+static void pf_wr(pf_list* l, int j, double val, int* over) {
+  int k = pf_slot(l, j, over);
+  if (k >= 0) l->v[k] = val;
+}
+
+typedef struct {
+  int L[3], l[3];
+  size_t np;
+} pf_geom;
+static inline size_t pf_at(const pf_geom* g, int x, int y, int z) {
+  return ((size_t)x * g->l[1] + y) * g->l[2] + z;
+}
+static inline int pf_src(int x, int L) { return ((x - 3) % L + L) % L + 3; }
+static inline int pf_interior(const pf_geom* g, int x, int y, int z) {
+  return x >= 3 && x < g->l[0] - 3 && y >= 3 && y < g->l[1] - 3 && z >= 3 && z < g->l[2] - 3;
+}
+/* halo lists := copies of their periodic interior sources */
+static void pf_fill_halos(const pf_geom* g, pf_list* gd, int* over) {
+  for (int x = 0; x < g->l[0]; x++)
+    for (int y = 0; y < g->l[1]; y++)
+      for (int z = 0; z < g->l[2]; z++) {
+        if (pf_interior(g, x, y, z)) continue;
+        pf_list* d = &gd[pf_at(g, x, y, z)];
+        const pf_list* s = &gd[pf_at(g, pf_src(x, g->L[0]), pf_src(y, g->L[1]), pf_src(z, g->L[2]))];
+        d->n = 0;
+        for (int k = 0; k < s->n; k++) pf_wr(d, s->id[k], s->v[k], over);
       }
-      continue;
-    }
-    /* ids whose window average is needed: N(v) and the ids held at v */
-    int uid[MAXIDS], nu = 0;
-    for (int i = 0; i < nn; i++) sorted_insert(uid, &nu, nid[i]);
-    for (int s = 0; s < cnt[v]; s++) sorted_insert(uid, &nu, ids[v * K + s]);
-    /* window sums per id, in a fixed association: the 7x7 (y,z) patch of
-       each x plane summed in (y,z) order, then the seven planes in x order */
-    double wsum[MAXIDS];
-    int wcnt[MAXIDS];
-    for (int i = 0; i < nu; i++) { wsum[i] = 0.0; wcnt[i] = 0; }
-    for (int dx = -3; dx <= 3; dx++) {
-      double psum[MAXIDS];
-      int pcnt[MAXIDS];
-      for (int i = 0; i < nu; i++) { psum[i] = 0.0; pcnt[i] = 0; }
-      for (int dy = -3; dy <= 3; dy++)
-        for (int dz = -3; dz <= 3; dz++) {
-          long long w = vidx(n, x + dx, y + dy, z + dz);
-          const int g = gid[w];
-          for (int i = 0; i < nu; i++)
-            if (uid[i] == g) { psum[i] = psum[i] + rho[w]; pcnt[i]++; }
+}
+/* mesh_extend: halos of the energy and grain-id buffers from the interior */
+static void pf_fill_halo_scalars(const pf_geom* g, double* e, int* gid) {
+  for (int x = 0; x < g->l[0]; x++)
+    for (int y = 0; y < g->l[1]; y++)
+      for (int z = 0; z < g->l[2]; z++) {
+        if (pf_interior(g, x, y, z)) continue;
+        const size_t s = pf_at(g, pf_src(x, g->L[0]), pf_src(y, g->L[1]), pf_src(z, g->L[2]));
+        e[pf_at(g, x, y, z)] = e[s];
+        gid[pf_at(g, x, y, z)] = gid[s];
+      }
+}
+
+/* one sweep of Update_grid over gd into tmp */
+static int pf_sweep(const pf_geom* g, pf_list* gd, pf_list* tmp, const int* GID, double* E, double* table,
+                    int table_len, int init_gid, double mcoef, double kappa, double mwell, double edisl, int* over) {
+  const int l0 = g->l[0], l1 = g->l[1], l2 = g->l[2];
+  for (size_t i = 0; i < g->np; i++) tmp[i].n = 0;
+  for (int x = 3; x < l0 - 3; x++)
+    for (int y = 3; y < l1 - 3; y++)
+      for (int z = 3; z < l2 - 3; z++) {
+        const size_t me_at = pf_at(g, x, y, z);
+        int nid[MAXIDS], nn = 0;
+        for (int i = x - 1; i <= x + 1; i++)
+          for (int j = y - 1; j <= y + 1; j++)
+            for (int m = z - 1; m <= z + 1; m++) {
+              const pf_list* d = &gd[pf_at(g, i, j, m)];
+              for (int k = 0; k < d->n; k++)
+                if (d->v[k] > PF_EPS) {
+                  int a = 0;
+                  while (a < nn && nid[a] != d->id[k]) a++;
+                  if (a == nn) {
+                    if (nn == MAXIDS) { *over = 1; continue; }
+                    nid[nn++] = d->id[k];
+                  }
+                }
+            }
+        pf_list* me = &gd[me_at];
+        pf_list* out = &tmp[me_at];
+        const int NN = me->n;
+        if (NN > 1) {
+          double avg[PF_OCAP];
+          int cnt[PF_OCAP];
+          for (int k = 0; k < NN; k++) { avg[k] = 0.0; cnt[k] = 0; }
+          for (int i = x - 3; i <= x + 3; i++)
+            for (int j = y - 3; j <= y + 3; j++)
+              for (int m = z - 3; m <= z + 3; m++) {
+                const size_t p = pf_at(g, i, j, m);
+                for (int k = 0; k < NN; k++)
+                  if (GID[p] == me->id[k]) { avg[k] = avg[k] + E[p]; cnt[k]++; }
+              }
+          for (int k = 0; k < NN; k++) {
+            const int ix = me->id[k] - 1;
+            if (ix < 0 || ix >= table_len) return MTH_ERR_ARG;
+            table[ix] = 0.0;
+            if (cnt[k] > 0) table[ix] = avg[k] / (double)cnt[k];
+          }
+          double sum_rex = 0.0, sum1 = 0.0, hdef = 0.0;
+          for (int k = 0; k < NN; k++)
+            if (cnt[k] > 0 && avg[k] > 0.0) {
+              const double e = me->v[k];
+              sum_rex = sum_rex + e * e;
+              sum1 = sum1 + e * e * e * (10.0 - 15.0 * e + 6.0 * e * e);
+              hdef = hdef + (e * e * e * (10.0 - 15.0 * e + 6.0 * e * e)) * (avg[k] / (double)cnt[k]);
+            }
+          for (int a = 0; a < nn; a++) {
+            const int id = nid[a];
+            const double c = pf_rd(me, id, over);
+            const double h = c * c * c * (10.0 - 15.0 * c + 6.0 * c * c);
+            const double dh = c * c * (30.0 - 60.0 * c + 30.0 * c * c);
+#define NB(a_, b_, c_) pf_rd(&gd[pf_at(g, x + (a_), y + (b_), z + (c_))], id, over)
+            const double right = NB(1, 0, 0), left = NB(-1, 0, 0), front = NB(0, 1, 0), back = NB(0, -1, 0);
+            const double up = NB(0, 0, 1), down = NB(0, 0, -1);
+            const double lu = NB(-1, 0, 1), ld = NB(-1, 0, -1), lf = NB(-1, -1, 0), lb = NB(-1, 1, 0);
+            const double cuf = NB(0, -1, 1), cub = NB(0, 1, 1), cdf = NB(0, -1, -1), cdb = NB(0, 1, -1);
+            const double ru = NB(1, 0, 1), rdn = NB(1, 0, -1), rf = NB(1, -1, 0), rb = NB(1, 1, 0);
+#undef NB
+            const double lap = 0.5 * (right + left + front + back + up + down) +
+                               0.125 * (cuf + cdf + cub + cdb + ld + lu + lf + lb + ru + rb + rdn + rf) - 4.5 * c;
+            const int ix = id - 1;
+            if (ix < 0 || ix >= table_len) return MTH_ERR_ARG;
+            const double ra = table[ix];
+            if (ra > 0.0) {
+              const double val = c - mcoef * (mwell * (c * c * c - c + 3.0 * c * (sum_rex - c * c)) - kappa * lap +
+                                              edisl * dh * ((sum1 - h) * ra - (hdef - h * ra)) / (sum1 * sum1));
+              if (id > init_gid && c < 0.5 && val > 0.5) E[me_at] = 100.0;
+              if (val > PF_KEEP) pf_wr(out, id, val, over);
+            }
+          }
+        } else if (NN == 1) {
+          for (int a = 0; a < nn; a++) {
+            const double val = pf_rd(me, nid[a], over);
+            pf_wr(out, nid[a], val, over);
+          }
         }
-      for (int i = 0; i < nu; i++) { wsum[i] = wsum[i] + psum[i]; wcnt[i] += pcnt[i]; }
-    }
-    double rbar[MAXIDS];
-    for (int i = 0; i < nu; i++) rbar[i] = wcnt[i] > 0 ? wsum[i] / (double)wcnt[i] : 0.0;
-    /* sums over the order parameters held at v (src/pf_xrx.c:1096-1104) */
-    double sum_rex = 0.0, sum1 = 0.0, hdef = 0.0;
-    for (int s = 0; s < cnt[v]; s++) {
-      const int id = ids[v * K + s];
-      int i = 0;
-      while (i < nu && uid[i] != id) i++;
-      if (i < nu && wcnt[i] > 0 && rbar[i] > 0.0) {
-        const double e = phi[v * K + s];
-        const double h = e * e * e * (10.0 - 15.0 * e + 6.0 * e * e);
-        sum_rex = sum_rex + e * e;
-        sum1 = sum1 + h;
-        hdef = hdef + h * rbar[i];
       }
-    }
-    int kid[MAXIDS], nk = 0;
-    double kval[MAXIDS];
-    for (int a = 0; a < nn; a++) {
-      const int id = nid[a];
-      int i = 0;
-      while (i < nu && uid[i] != id) i++;
-      if (i == nu || !(rbar[i] > 0.0)) continue;
-      const double c = eta_of(ids, phi, cnt, K, v, id);
-      const double f_r = eta_of(ids, phi, cnt, K, vidx(n, x + 1, y, z), id);
-      const double f_l = eta_of(ids, phi, cnt, K, vidx(n, x - 1, y, z), id);
-      const double f_f = eta_of(ids, phi, cnt, K, vidx(n, x, y + 1, z), id);
-      const double f_b = eta_of(ids, phi, cnt, K, vidx(n, x, y - 1, z), id);
-      const double f_u = eta_of(ids, phi, cnt, K, vidx(n, x, y, z + 1), id);
-      const double f_d = eta_of(ids, phi, cnt, K, vidx(n, x, y, z - 1), id);
-      const double e_lu = eta_of(ids, phi, cnt, K, vidx(n, x - 1, y, z + 1), id);
-      const double e_lf = eta_of(ids, phi, cnt, K, vidx(n, x - 1, y - 1, z), id);
-      const double e_ld = eta_of(ids, phi, cnt, K, vidx(n, x - 1, y, z - 1), id);
-      const double e_lb = eta_of(ids, phi, cnt, K, vidx(n, x - 1, y + 1, z), id);
-      const double e_rd = eta_of(ids, phi, cnt, K, vidx(n, x + 1, y, z - 1), id);
-      const double e_ru = eta_of(ids, phi, cnt, K, vidx(n, x + 1, y, z + 1), id);
-      const double e_rf = eta_of(ids, phi, cnt, K, vidx(n, x + 1, y - 1, z), id);
-      const double e_rb = eta_of(ids, phi, cnt, K, vidx(n, x + 1, y + 1, z), id);
-      const double e_cuf = eta_of(ids, phi, cnt, K, vidx(n, x, y - 1, z + 1), id);
-      const double e_cdb = eta_of(ids, phi, cnt, K, vidx(n, x, y + 1, z - 1), id);
-      const double e_cub = eta_of(ids, phi, cnt, K, vidx(n, x, y + 1, z + 1), id);
-      const double e_cdf = eta_of(ids, phi, cnt, K, vidx(n, x, y - 1, z - 1), id);
-      /* laplacian(), src/pf_xrx.c:6-9: faces 0.5, edges 0.125, centre -4.5 */
-      const double lap = 0.5 * (f_r + f_l + f_f + f_b + f_u + f_d) +
-                         0.125 * (e_lu + e_lf + e_ld + e_lb + e_rd + e_ru + e_rf + e_rb + e_cuf + e_cdb + e_cub + e_cdf) -
-                         4.5 * c;
-      const double h = c * c * c * (10.0 - 15.0 * c + 6.0 * c * c);
-      const double dh = c * c * (30.0 - 60.0 * c + 30.0 * c * c);
-      const double drive = sum1 > 0.0 ? edisl * dh * ((sum1 - h) * rbar[i] - (hdef - h * rbar[i])) / (sum1 * sum1) : 0.0;
-      const double val = c - mcoef * (mwell * (c * c * c - c + 3.0 * c * (sum_rex - c * c)) - kappa * lap + drive);
-      if (val > PF_KEEP) { kid[nk] = id; kval[nk] = val; nk++; }
-    }
-    /* keep the K largest (ties to the smaller id), stored sorted by id */
-    while (nk > K) {
-      int m = 0;
-      for (int a = 1; a < nk; a++)
-        if (kval[a] < kval[m] || (kval[a] == kval[m] && kid[a] > kid[m])) m = a;
-      for (int a = m; a < nk - 1; a++) { kid[a] = kid[a + 1]; kval[a] = kval[a + 1]; }
-      nk--;
-    }
-    cnt2[v] = nk;
-    for (int s = 0; s < K; s++) {
-      ids2[v * K + s] = s < nk ? kid[s] : 0;
-      phi2[v * K + s] = s < nk ? kval[s] : 0.0;
-    }
-  }
+  pf_fill_halos(g, tmp, over);
+  return MTH_OK;
 }
 
-/* grain id = argmax eta, ties to the smaller id; a voxel that lost every
-   order parameter keeps its id */
-static void pf_argmax(long long nv, int K, const int* ids, const double* phi, const int* cnt, int* gid) {
-  for (long long v = 0; v < nv; v++) {
-    double best = 0.0;
-    int g = gid[v];
-    for (int s = 0; s < cnt[v]; s++)
-      if (phi[v * K + s] > best) { best = phi[v * K + s]; g = ids[v * K + s]; }
-    gid[v] = g;
-  }
-}
-
-int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps, int K,
-                 int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
-  const long long nv = (long long)n[0] * n[1] * n[2];
+int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps, int init_gid,
+                 double* table, int table_len, int* grain_out, int* cnt_out, int* ids_out, double* phi_out,
+                 int kmax) {
+  pf_geom g;
+  for (int i = 0; i < 3; i++) { g.L[i] = n[i]; g.l[i] = n[i] + 6; }
+  g.np = (size_t)g.l[0] * g.l[1] * g.l[2];
   double mcoef, kappa, mwell, edisl;
   orc_pf_coefficients(p, &mcoef, &kappa, &mwell, &edisl);
-  int *ids = (int*)calloc((size_t)nv * K, sizeof(int)), *ids2 = (int*)calloc((size_t)nv * K, sizeof(int));
-  double *phi = (double*)calloc((size_t)nv * K, sizeof(double)), *phi2 = (double*)calloc((size_t)nv * K, sizeof(double));
-  int *cnt = (int*)calloc(nv, sizeof(int)), *cnt2 = (int*)calloc(nv, sizeof(int));
-  if (!ids || !ids2 || !phi || !phi2 || !cnt || !cnt2) return MTH_ERR_NOMEM;
-  /* initial state: one order parameter per voxel (src/pf_xrx.c:1533-1578) */
-  for (long long v = 0; v < nv; v++) {
-    ids[v * K] = grain[v];
-    phi[v * K] = 1.0;
-    cnt[v] = 1;
-    grain_out[v] = grain[v];
+  pf_list* gd = (pf_list*)calloc(g.np, sizeof(pf_list));
+  pf_list* tmp = (pf_list*)calloc(g.np, sizeof(pf_list));
+  int* GID = (int*)calloc(g.np, sizeof(int));
+  double* E = (double*)calloc(g.np, sizeof(double));
+  if (!gd || !tmp || !GID || !E) { free(gd); free(tmp); free(GID); free(E); return MTH_ERR_NOMEM; }
+  int over = 0, st = MTH_OK;
+  for (int x = 0; x < n[0]; x++)
+    for (int y = 0; y < n[1]; y++)
+      for (int z = 0; z < n[2]; z++) {
+        const size_t v = ((size_t)x * n[1] + y) * n[2] + z, q = pf_at(&g, x + 3, y + 3, z + 3);
+        pf_wr(&gd[q], grain[v], 1.0, &over);
+        GID[q] = grain[v];
+        E[q] = rho[v];
+        grain_out[v] = grain[v];
+      }
+  pf_fill_halos(&g, gd, &over);
+  pf_fill_halo_scalars(&g, E, GID);
+  for (int s = 0; s < substeps && st == MTH_OK; s++) {
+    st = pf_sweep(&g, gd, tmp, GID, E, table, table_len, init_gid, mcoef, kappa, mwell, edisl, &over);
+    pf_list* t = gd; gd = tmp; tmp = t;
+    for (int x = 0; x < n[0]; x++)
+      for (int y = 0; y < n[1]; y++)
+        for (int z = 0; z < n[2]; z++) {
+          const pf_list* d = &gd[pf_at(&g, x + 3, y + 3, z + 3)];
+          double best = 0.0;
+          int id = 0;
+          for (int k = 0; k < d->n; k++)
+            if (best < d->v[k]) { best = d->v[k]; id = d->id[k]; }
+          grain_out[((size_t)x * n[1] + y) * n[2] + z] = id;
+        }
+    pf_fill_halo_scalars(&g, E, GID);
   }
-  for (int s = 0; s < substeps; s++) {
-    pf_substep(n, K, ids, phi, cnt, ids2, phi2, cnt2, grain_out, rho, mcoef, kappa, mwell, edisl);
-    int* ti = ids; ids = ids2; ids2 = ti;
-    double* tp = phi; phi = phi2; phi2 = tp;
-    int* tc = cnt; cnt = cnt2; cnt2 = tc;
-    pf_argmax(nv, K, ids, phi, cnt, grain_out);
+  if (st == MTH_OK && over) st = MTH_ERR_UNSUPPORTED;
+  if (st == MTH_OK && cnt_out) {
+    for (int x = 0; x < n[0]; x++)
+      for (int y = 0; y < n[1]; y++)
+        for (int z = 0; z < n[2]; z++) {
+          const size_t v = ((size_t)x * n[1] + y) * n[2] + z;
+          const pf_list* d = &gd[pf_at(&g, x + 3, y + 3, z + 3)];
+          cnt_out[v] = d->n;
+          for (int k = 0; k < kmax; k++) {
+            if (ids_out) ids_out[v * kmax + k] = k < d->n ? d->id[k] : 0;
+            if (phi_out) phi_out[v * kmax + k] = k < d->n ? d->v[k] : 0.0;
+          }
+          if (d->n > kmax) st = MTH_ERR_UNSUPPORTED;
+        }
   }
-  if (ids_out) memcpy(ids_out, ids, sizeof(int) * (size_t)nv * K);
-  if (phi_out) memcpy(phi_out, phi, sizeof(double) * (size_t)nv * K);
-  if (cnt_out) memcpy(cnt_out, cnt, sizeof(int) * (size_t)nv);
-  free(ids); free(ids2); free(phi); free(phi2); free(cnt); free(cnt2);
-  return MTH_OK;
+  free(gd); free(tmp); free(GID); free(E);
+  return st;
 }
 
 /* ------------------------------------------------ PF <-> FFT grid transfer

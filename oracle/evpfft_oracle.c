@@ -697,6 +697,8 @@ struct orc_ctx {
   mth_params par;
   int first_drx_id, next_grain_id, n_drx;
   double* drx_rot;           /* 9 per recrystallised grain */
+  double* rho_avg_tab;       /* PF_XRX's rho_avg table, kept across steps */
+  int rho_avg_len;
   t33 udot, udot_s, udot_a, scauchy;
   int vbc[6], sbc[6], creep, elast_bc, update_flag, hard_flag;
   double dt, err_tol, time_tot, e_vm, d_vm, s_vm, s_vm1, err_e, err_s;
@@ -928,7 +930,7 @@ void orc_destroy(orc_ctx* c) {
   free(c->velgrad); free(c->tranmat); free(c->sg66); free(c->schm); free(c->crss); free(c->gamdot);
   free(c->gamacum); free(c->kbuf); free(c->nvec); free(c->conv_s); free(c->conv_e);
   free(c->newton_it); free(c->newton_bad);
-  free(c->cgr); free(c->drx_rot);
+  free(c->cgr); free(c->drx_rot); free(c->rho_avg_tab);
   free(c->rho_s); free(c->rho_g1); free(c->rho_g2); free(c->rho_g3); free(c->rho_m); free(c->rho_F);
   free(c->rho_P); free(c->rho_dipole); free(c->rho_forest); free(c->gam_acum); free(c->trial_gam_acum);
   free(c->gadot_grad); free(c->gbchk);
@@ -1229,6 +1231,12 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
   }
   *n_new = nn;
   int st = MTH_OK;
+  if (c->next_grain_id > c->rho_avg_len) {   /* the table covers every grain id */
+    const int len = c->next_grain_id + 1024;
+    c->rho_avg_tab = (double*)realloc(c->rho_avg_tab, sizeof(double) * (size_t)len);
+    for (int i = c->rho_avg_len; i < len; i++) c->rho_avg_tab[i] = 0.0;
+    c->rho_avg_len = len;
+  }
   if (c->n_drx > 0) {
     /* phase field on its own grid when CellDim_pf differs (InterpolateGrid,
      * src/integrated.c:674-760; coarse-graining src/integrated.c:821-860) */
@@ -1242,11 +1250,13 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
       double* rpf = (double*)malloc(sizeof(double) * q);
       orc_resample_nearest(c->n, c->grain, npf, gpf);
       orc_resample_trilinear(c->n, rho, npf, rpf);
-      st = orc_pf_relax(p, npf, gpf, rpf, p->pf_substeps, 8, gnpf, NULL, NULL, NULL);
+      st = orc_pf_relax(p, npf, gpf, rpf, p->pf_substeps, c->first_drx_id - 1, c->rho_avg_tab, c->rho_avg_len,
+                        gnpf, NULL, NULL, NULL, 0);
       orc_resample_nearest(npf, gnpf, c->n, gnew);
       free(gpf); free(gnpf); free(rpf);
     } else {
-      st = orc_pf_relax(p, c->n, c->grain, rho, p->pf_substeps, 8, gnew, NULL, NULL, NULL);
+      st = orc_pf_relax(p, c->n, c->grain, rho, p->pf_substeps, c->first_drx_id - 1, c->rho_avg_tab,
+                        c->rho_avg_len, gnew, NULL, NULL, NULL, 0);
     }
     for (size_t v = 0; v < nv && st == MTH_OK; v++) {
       const int g = gnew[v];

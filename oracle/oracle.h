@@ -49,9 +49,16 @@ void orc_gb_indicator(const int* n, const int* grain, unsigned char* gb);
 long long orc_nucleation_sites(const int* n, const int* grain, const int* phase_crystal, const double* rho,
                                double rho_nuc, double prob, uint64_t seed, long long step, long long* sites,
                                long long cap);
-void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, int first_id, int radius);
-int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps, int K,
-                 int* grain_out, int* ids_out, double* phi_out, int* cnt_out);
+void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, int first_id, int radius2);
+/* PF_XRX on one rank: substeps sweeps from (grain, 1) per voxel; table is
+ * the caller's rho_avg table (table_len entries, grain id g at g-1), read and
+ * written as the reference does; init_gid: ids above it are recrystallised.
+ * Outputs the grain map after the last substep and, when cnt_out is given,
+ * every voxel's list in stored order (up to kmax entries, slot-major per
+ * voxel: ids_out[v*kmax+k]). */
+int orc_pf_relax(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps, int init_gid,
+                 double* table, int table_len, int* grain_out, int* cnt_out, int* ids_out, double* phi_out,
+                 int kmax);
 
 /* Transfer between the mechanical grid and a phase-field grid of another
  * size (InterpolateGrid, src/integrated.c:496-760): nearest-corner for

@@ -65,8 +65,9 @@ def load():
         lib.orc_paint_nuclei.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.c_int,
                                          C.c_int, C.c_int]
         lib.orc_pf_relax.argtypes = [C.POINTER(capi.MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                     C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                     C.POINTER(C.c_double), C.POINTER(C.c_int)]
+                                     C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double), C.c_int]
         lib.orc_resample_nearest.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                              C.POINTER(C.c_int)]
         lib.orc_resample_trilinear.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
@@ -151,22 +152,28 @@ def fft3d(data, sign):
     return a
 
 
-def pf_relax(params, dims, grain, rho, substeps, K=8):
-    """Oracle phase-field relaxation: (grain_out, ids[N,K], phi[N,K], cnt[N])."""
+def pf_relax(params, dims, grain, rho, substeps, init_gid=None, table=None, kmax=24):
+    """Oracle PF_XRX: (grain_out, ids[N,kmax], phi[N,kmax], cnt[N], table).
+    init_gid defaults to the largest id of grain (no recrystallised ids);
+    table is the rho_avg table (zeros of max id + 1 entries by default),
+    returned as left by the call."""
     lib = load()
     nv = int(np.prod(dims))
     d = (C.c_int * 3)(*dims)
     g = np.ascontiguousarray(grain, dtype=np.int32)
     r = np.ascontiguousarray(rho, dtype=np.float64)
+    if init_gid is None:
+        init_gid = int(g.max())
+    t = np.zeros(int(g.max()) + 1) if table is None else np.array(table, dtype=np.float64)
     go = np.zeros(nv, np.int32)
-    ids = np.zeros(nv * K, np.int32)
-    phi = np.zeros(nv * K)
+    ids = np.zeros(nv * kmax, np.int32)
+    phi = np.zeros(nv * kmax)
     cnt = np.zeros(nv, np.int32)
-    st = lib.orc_pf_relax(C.byref(params), d, capi._iptr(g), capi._dptr(r), substeps, K, capi._iptr(go),
-                          capi._iptr(ids), capi._dptr(phi), capi._iptr(cnt))
+    st = lib.orc_pf_relax(C.byref(params), d, capi._iptr(g), capi._dptr(r), substeps, init_gid, capi._dptr(t), len(t),
+                          capi._iptr(go), capi._iptr(cnt), capi._iptr(ids), capi._dptr(phi), kmax)
     if st != 0:
-        raise RuntimeError("orc_pf_relax failed")
-    return go, ids.reshape(nv, K), phi.reshape(nv, K), cnt
+        raise RuntimeError(f"orc_pf_relax failed: {capi.STATUS.get(st, st)}")
+    return go, ids.reshape(nv, kmax), phi.reshape(nv, kmax), cnt, t
 
 
 def nucleate(params, dims, grain, crystal, rho, step, first_id, cap=65536):

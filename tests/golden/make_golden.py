@@ -8,7 +8,7 @@ the configuration, the per-step trace (Green iterations, <sigma>,
 <grad u>, <eps_p>, <edot_p>, s_vm, s_vm1, e_vm, d_vm, Err_s, Err_e) and the
 final fields.
 
-Needs the reference sources (MTH_REFERENCE, default /root/reference) and a
+Needs the reference sources (the directory named by MTH_REFERENCE) and a
 C++ compiler; it is not run by the tests.
 
     python tests/golden/make_golden.py
@@ -125,7 +125,7 @@ def main_test_run():
     import ctypes as C
     import shutil
     from mth import capi
-    src = os.path.join(os.environ.get("MTH_REFERENCE", "/root/reference"), "test_run")
+    src = os.path.join(os.environ["MTH_REFERENCE"], "test_run")
     d = "/tmp/mth_golden_test_run"
     shutil.rmtree(d, ignore_errors=True)
     shutil.copytree(src, d)
@@ -152,7 +152,159 @@ def main_test_run():
     print("test_run step 0: iterations", int(trace[0, 1]), "->", os.path.relpath(out, REPO))
 
 
+# ------------------------------------------------------------------ DRX
+# The reference's own PF_XRX, NucleationCheckDRX (with Gradient_ExchangeGrainID
+# and the GB indicator of src/evolution.c:816-829) and InterpolateGrid, run on
+# crafted inputs through oracle/refshim/drx_harness.cc (oracle/_ref/drx_ref),
+# one case per process.  File layouts are those documented in the harness.
+
+DRX_REF = os.path.join(REPO, "oracle", "_ref", "drx_ref")
+# test_run/input.in's PF constants; stored-energy scale 0.5 and a 500x one
+# (a driving force that moves boundaries within a few substeps)
+PF_COEF = dict(E_gb=0.625, M_gb=1e-10, mu=48.0, bb=0.256, alpha=0.5, dx=2.5e-6, dt=0.004)
+PF_COEF_STRONG = dict(PF_COEF, alpha=1000.0)
+
+
+def _run_drx_ref(mode, blob, d):
+    fi, fo = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+    with open(fi, "wb") as f:
+        f.write(blob)
+    subprocess.run(["bash", "-c", f"ulimit -s unlimited; {DRX_REF} {mode} in.bin out.bin > ref.log 2>&1"], cwd=d,
+                   check=True)
+    return open(fo, "rb").read()
+
+
+def ref_pf(d, dims, gid, rho, steps, coef, init_gid, table):
+    """PF_XRX: per-substep (cnt, ids, vals), gID_new, rho_avg table."""
+    n = int(np.prod(dims))
+    blob = (np.array([*dims, steps, init_gid, len(table), 1], np.int32).tobytes() +
+            np.array([coef[k] for k in ("E_gb", "M_gb", "mu", "bb", "alpha", "dx", "dt")], np.float64).tobytes() +
+            np.asarray(gid, np.int32).tobytes() + np.asarray(rho, np.float64).tobytes() +
+            np.asarray(table, np.float64).tobytes())
+    b = _run_drx_ref("pf", blob, d)
+    off, subs = 0, []
+    for _ in range(steps):
+        cnt = np.frombuffer(b, np.int32, n, off); off += 4 * n
+        tot = int(np.frombuffer(b, np.int32, 1, off)[0]); off += 4
+        ids = np.frombuffer(b, np.int32, tot, off); off += 4 * tot
+        val = np.frombuffer(b, np.float64, tot, off); off += 8 * tot
+        subs.append((cnt.copy(), ids.copy(), val.copy()))
+    gnew = np.frombuffer(b, np.int32, n, off).copy(); off += 4 * n
+    tab = np.frombuffer(b, np.float64, len(table), off).copy(); off += 8 * len(table)
+    assert off == len(b)
+    return subs, gnew, tab
+
+
+def voronoi(dims, ng, rng):
+    pts = rng.uniform(0, 1, size=(ng, 3)) * np.array(dims)
+    pos = np.indices(dims).reshape(3, -1).T + 0.5
+    best = np.full(pos.shape[0], np.inf)
+    g = np.zeros(pos.shape[0], np.int32)
+    for k, c in enumerate(pts):
+        dd = pos - c
+        dd -= np.round(dd / np.array(dims)) * np.array(dims)
+        r = (dd ** 2).sum(1)
+        m = r < best
+        best[m] = r[m]
+        g[m] = k + 1
+    return g
+
+
+def pf_cases():
+    rng = np.random.default_rng(2024)
+    dims = (10, 10, 10)
+    ix = np.indices(dims)
+    cases = {}
+    for ax, nm in ((0, "x"), (2, "z")):
+        g = np.where(ix[ax] < 5, 1, 2).astype(np.int32).ravel()
+        cases[f"pf_bicrystal_{nm}"] = (dims, g, np.where(g == 1, 100.0, 600.0), 8, PF_COEF, 2)
+    r2 = ((ix - 5) ** 2).sum(0).ravel()
+    g = np.where(r2 <= 9, 2, 1).astype(np.int32)
+    cases["pf_nucleus"] = (dims, g, np.where(g == 1, 600.0, 1.0), 8, PF_COEF, 1)
+    cases["pf_nucleus_growing"] = (dims, g, np.where(g == 1, 600.0, 1.0), 10, PF_COEF_STRONG, 1)
+    g = np.ones(dims, np.int32)
+    g[ix[0] >= 5] = 2
+    g[(ix[0] < 5) & (ix[1] >= 5)] = 3
+    g = g.ravel()
+    cases["pf_triple"] = (dims, g, np.array([0.0, 100.0, 300.0, 600.0])[g], 8, PF_COEF, 3)
+    d2 = (12, 10, 8)
+    g = voronoi(d2, 9, rng)
+    cases["pf_voronoi"] = (d2, g, rng.uniform(50.0, 600.0, g.size), 10, PF_COEF_STRONG, 5)
+    return cases
+
+
+def main_drx():
+    subprocess.check_call([os.path.join(REPO, "oracle", "build_ref.sh")])
+    d = "/tmp/mth_golden_drx"
+    os.makedirs(d, exist_ok=True)
+    for name, (dims, g, rho, steps, coef, init_gid) in pf_cases().items():
+        table = np.zeros(int(g.max()) + 1)
+        subs, gnew, tab = ref_pf(d, dims, g, rho, steps, coef, init_gid, table)
+        extra = {}
+        if name == "pf_voronoi":   # a second call on the relaxed map, with the table the first one left
+            rho2 = np.where(gnew > init_gid, 1.0, rho)
+            subs2, gnew2, tab2 = ref_pf(d, dims, gnew, rho2, 4, coef, init_gid, tab)
+            extra = dict(rho2=rho2, gnew2=gnew2, table2=tab2, cnt2=subs2[-1][0], ids2=subs2[-1][1], val2=subs2[-1][2])
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out, dims=np.array(dims), grain=g, rho=rho, steps=steps, init_gid=init_gid,
+                            coef=json.dumps(coef), gnew=gnew, table=tab,
+                            cnt=np.concatenate([s[0] for s in subs]), ntot=np.array([len(s[1]) for s in subs]),
+                            ids=np.concatenate([s[1] for s in subs]), val=np.concatenate([s[2] for s in subs]),
+                            **extra)
+        print(name, "substeps", steps, "entries", [len(s[1]) for s in subs], "->", os.path.relpath(out, REPO))
+    # nucleation: static branch (threshold kappa_drx), nucleus_radius compared with |d|^2
+    rng = np.random.default_rng(77)
+    for name, dims, ng, kap, rad in (("nucl_voronoi", (10, 9, 8), 7, 47.0, 4), ("nucl_edges", (8, 8, 8), 5, 48.0, 2)):
+        n = int(np.prod(dims))
+        g = voronoi(dims, ng, rng)
+        phase = np.ones(n, np.int32)
+        phase[rng.uniform(size=n) < 0.05] = 2
+        rs = rng.uniform(0.0, 600.0, n)
+        kappa = np.full(n, kap)
+        rot = np.stack([_rand_rot(rng) for _ in range(ng)])[g - 1].reshape(n, 9)
+        blob = (np.array([*dims, ng, rad, 3], np.int32).tobytes() + g.tobytes() + phase.tobytes() + rs.tobytes() +
+                kappa.tobytes() + rot.tobytes())
+        b = _run_drx_ref("nucl", blob, d)
+        nn = int(np.frombuffer(b, np.int32, 1, 0)[0])
+        off = 4
+        gout = np.frombuffer(b, np.int32, n, off).copy(); off += 4 * n
+        gb = np.frombuffer(b, np.int32, n, off).copy(); off += 4 * n
+        diff = np.frombuffer(b, np.float64, n, off).copy(); off += 8 * n
+        rec = np.frombuffer(b, np.dtype([("id", "<i4"), ("t1", "<f8"), ("Phi", "<f8"), ("t2", "<f8")]), nn, off)
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out, dims=np.array(dims), grain=g, phase=phase, rho_s0=rs, kappa=kap, radius=rad,
+                            n_grains=ng, rot=rot, n_new=nn, grain_out=gout, gb=gb, diff_rho=diff,
+                            new_id=rec["id"].copy(), new_euler_deg=np.stack([rec["t1"], rec["Phi"], rec["t2"]], 1))
+        print(name, "nuclei", nn, "->", os.path.relpath(out, REPO))
+    # grid transfer, integer refinement in x (InterpolateGrid's slab rule)
+    for name, ns, nd in (("interp_refine", (8, 8, 8), (16, 12, 10)), ("interp_mixed", (6, 9, 12), (18, 6, 8))):
+        n, npf = int(np.prod(ns)), int(np.prod(nd))
+        g = rng.integers(1, 40, n).astype(np.int32)
+        rt = rng.uniform(0.0, 700.0, n)
+        b = _run_drx_ref("interp", np.array([*ns, *nd], np.int32).tobytes() + g.tobytes() + rt.tobytes(), d)
+        gpf = np.frombuffer(b, np.int32, npf, 0).copy()
+        rpf = np.frombuffer(b, np.float64, npf, 4 * npf).copy()
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out, ns=np.array(ns), nd=np.array(nd), grain=g, rho=rt, grain_pf=gpf, rho_pf=rpf)
+        print(name, ns, "->", nd, "->", os.path.relpath(out, REPO))
+
+
+def _rand_rot(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
 if __name__ == "__main__":
-    main()
-    main_dd()
-    main_test_run()
+    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx"]
+    if "evp" in which:
+        main()
+    if "dd" in which:
+        main_dd()
+    if "test_run" in which:
+        main_test_run()
+    if "drx" in which:
+        main_drx()

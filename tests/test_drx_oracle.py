@@ -1,10 +1,144 @@
-"""The DRX restatement (oracle/drx_oracle.c) on its own: invariants of the
-sparse order parameters and the physics the reference's phase-field step
-encodes (stored-energy-driven growth of a recrystallised nucleus)."""
+"""The DRX restatement (oracle/drx_oracle.c) against the reference's own
+functions: PF_XRX (src/pf_xrx.c:1469-1698), NucleationCheckDRX with the
+grain-boundary indicator (src/integrated.c:161-494, src/evolution.c:816-829,
+src/constitutive.c:724-873) and InterpolateGrid (src/integrated.c:674-760),
+run on crafted inputs by oracle/refshim/drx_harness.cc
+(tests/golden/make_golden.py main_drx); plus invariants of the sparse order
+parameters."""
+import json
+import os
+
 import numpy as np
+import pytest
 
 import pyoracle
 from mth import capi, synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+PF_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("pf_"))
+NUCL_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("nucl_"))
+INTERP_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("interp_"))
+
+
+def coef_params(coef, width=3.0):
+    """mth_params carrying the harness's PF constants; L_gb = 3 dx as
+    src/pf_xrx.c:1493 hard-codes it."""
+    p = capi.MthParams()
+    p.precision = capi.MTH_FP64
+    p.pf_length_scale, p.pf_time_step = coef["dx"], coef["dt"]
+    p.e_gb, p.m_gb, p.pf_width_cells = coef["E_gb"], coef["M_gb"], width
+    p.stored_energy_scale, p.shear_modulus, p.burgers = coef["alpha"], coef["mu"], coef["bb"]
+    return p
+
+
+def golden_lists(z, s):
+    """Per-voxel (ids, vals) after substep s (1-based) of a pf_* fixture."""
+    nv = int(np.prod(z["dims"]))
+    ntot = z["ntot"]
+    cnt = z["cnt"][(s - 1) * nv:s * nv]
+    off = int(ntot[:s - 1].sum())
+    return cnt, z["ids"][off:off + ntot[s - 1]], z["val"][off:off + ntot[s - 1]]
+
+
+def oracle_flat(cnt, ids, phi):
+    k = np.arange(ids.shape[1])[None, :] < cnt[:, None]
+    return ids[k], phi[k]
+
+
+@pytest.mark.parametrize("name", PF_CASES)
+def test_pf_matches_reference(name):
+    """Every substep's (id, eta) lists, in the reference's stored order, the
+    grain map and the rho_avg table: bit for bit."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    dims = tuple(int(d) for d in z["dims"])
+    p = coef_params(json.loads(str(z["coef"])))
+    steps, init_gid = int(z["steps"]), int(z["init_gid"])
+    table0 = np.zeros(int(z["grain"].max()) + 1)
+    for s in range(1, steps + 1):
+        go, ids, phi, cnt, tab = pyoracle.pf_relax(p, dims, z["grain"], z["rho"], s, init_gid, table0)
+        gc, gi, gv = golden_lists(z, s)
+        assert np.array_equal(cnt, gc), f"substep {s}: list lengths differ at {np.count_nonzero(cnt != gc)} voxels"
+        oi, ov = oracle_flat(cnt, ids, phi)
+        assert np.array_equal(oi, gi), f"substep {s}: ids or their order differ"
+        assert np.max(np.abs(ov - gv), initial=0.0) <= 1e-12, f"substep {s}: eta differs"
+        assert np.array_equal(ov, gv), f"substep {s}: eta not bit-identical"
+    assert np.array_equal(go, z["gnew"])
+    assert np.array_equal(tab, z["table"])
+    if "gnew2" in z.files:   # a second call that starts from the table the first one left
+        go2, ids2, phi2, cnt2, tab2 = pyoracle.pf_relax(p, dims, z["gnew"], z["rho2"], 4, init_gid, z["table"])
+        assert np.array_equal(go2, z["gnew2"]) and np.array_equal(tab2, z["table2"])
+        assert np.array_equal(cnt2, z["cnt2"])
+        oi, ov = oracle_flat(cnt2, ids2, phi2)
+        assert np.array_equal(oi, z["ids2"]) and np.array_equal(ov, z["val2"])
+
+
+def test_pf_cases_exercise_the_reference_rules():
+    """The fixtures reach the rules that make the sweep order matter: a
+    recrystallised id passing 0.5 (stored energy reset mid-sweep), voxels
+    holding three or more ids, and weak last entries."""
+    z = np.load(os.path.join(GOLDEN, "pf_nucleus_growing.npz"))
+    nv = int(np.prod(z["dims"]))
+    steps = int(z["steps"])
+    g0 = z["grain"]
+    assert (z["gnew"] == 2).sum() > (g0 == 2).sum()     # the nucleus grew: id 2 > init_gid crossed 0.5
+    zv = np.load(os.path.join(GOLDEN, "pf_voronoi.npz"))
+    cnt, ids, val = golden_lists(zv, int(zv["steps"]))
+    assert cnt.max() >= 3
+    ends = np.cumsum(cnt) - 1
+    assert np.any((val[ends] < 5e-3) & (cnt > 1))
+    # the tail rule: only the last entry of a list may be below EPSILON
+    first = np.ones(val.size, bool)
+    first[ends] = False
+    assert np.all(val[first] >= 5e-3)
+    del nv, steps
+
+
+@pytest.mark.parametrize("name", NUCL_CASES)
+def test_nucleation_matches_reference(name):
+    """Static-threshold nucleation of the reference (diff_rho > kappa_drx at
+    grain-boundary voxels, ids numbered in voxel order after the grain list,
+    |d|^2 <= nucleus_radius without periodic images) is the oracle's rule with
+    nucleation_prob = 1."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    dims = tuple(int(d) for d in z["dims"])
+    gb = np.zeros(int(np.prod(dims)), np.uint8)
+    lib = pyoracle.load()
+    import ctypes as C
+    lib.orc_gb_indicator.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_ubyte)]
+    g = np.ascontiguousarray(z["grain"], np.int32)
+    lib.orc_gb_indicator((C.c_int * 3)(*dims), capi._iptr(g), gb.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    assert np.array_equal(gb.astype(np.int32), z["gb"])
+    # the -z face is not checked by the reference: some voxels differ only there
+    p = capi.MthParams()
+    p.rho_nucleation = float(z["kappa"])
+    p.nucleation_prob = 1.0
+    p.nucleus_radius = int(z["radius"])
+    p.seed = 1
+    cry = (z["phase"] == 1).astype(np.int32)
+    ng = int(z["n_grains"])
+    gout, sites = pyoracle.nucleate(p, dims, g, cry, z["diff_rho"], step=3, first_id=ng + 1)
+    assert sites.size == int(z["n_new"])
+    assert np.array_equal(z["new_id"], np.arange(ng + 1, ng + 1 + sites.size))
+    assert np.array_equal(gout, z["grain_out"])
+    # orientation of each nucleus: the parent's (the reference passes it through Bunge angles)
+    rot = z["rot"].reshape(-1, 3, 3)
+    for k, v in enumerate(sites):
+        t1, ph, t2 = np.radians(z["new_euler_deg"][k])
+        c1, s1, cp, sp, c2, s2 = np.cos(t1), np.sin(t1), np.cos(ph), np.sin(ph), np.cos(t2), np.sin(t2)
+        a = np.array([[c1 * c2 - s1 * s2 * cp, s1 * c2 + c1 * s2 * cp, s2 * sp],
+                      [-c1 * s2 - s1 * c2 * cp, -s1 * s2 + c1 * c2 * cp, c2 * sp],
+                      [s1 * sp, -c1 * sp, cp]])
+        sa2xt = rot[v].T
+        if abs(sa2xt[2, 2]) <= 0.9999:   # the reference's angle extraction sets phi2 = 0 above this
+            assert np.abs(a - sa2xt).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", INTERP_CASES)
+def test_grid_transfer_matches_reference(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ns, nd = tuple(int(v) for v in z["ns"]), tuple(int(v) for v in z["nd"])
+    assert np.array_equal(pyoracle.resample(z["grain"], ns, nd), z["grain_pf"])
+    assert np.array_equal(pyoracle.resample(z["rho"], ns, nd), z["rho_pf"])
 
 
 def pf_params(**kw):
@@ -22,25 +156,24 @@ def test_single_grain_is_stationary():
     dims = (12, 12, 12)
     g = np.full(int(np.prod(dims)), 3, np.int32)
     rho = np.full(g.size, 200.0)
-    go, ids, phi, cnt = pyoracle.pf_relax(pf_params(), dims, g, rho, 5)
+    go, ids, phi, cnt, _ = pyoracle.pf_relax(pf_params(), dims, g, rho, 5)
     assert np.array_equal(go, g)
     assert np.all(cnt == 1) and np.all(ids[:, 0] == 3) and np.all(phi[:, 0] == 1.0)
 
 
 def test_nucleus_grows_into_deformed_grain():
-    """A dislocation-free nucleus (rho=1) in a grain at rho=500 expands: the
-    stored-energy driving force of src/pf_xrx.c:1184-1233."""
-    dims = (24, 24, 24)
+    """A dislocation-free recrystallised nucleus (rho=1) in a grain at
+    rho=500 expands under the stored-energy driving force of
+    src/pf_xrx.c:1184-1233; with equal energies it does not."""
+    dims = (20, 20, 20)
     nv = int(np.prod(dims))
     g = np.full(nv, 1, np.int32)
-    nuc = sphere(dims, (12, 12, 12), 3)
+    nuc = sphere(dims, (10, 10, 10), 3)
     g[nuc] = 2
-    rho = np.where(nuc, 1.0, 500.0)
-    p = pf_params()
-    go, ids, phi, cnt = pyoracle.pf_relax(p, dims, g, rho, 30)
+    p = pf_params(stored_energy_scale=250.0)
+    go, *_ = pyoracle.pf_relax(p, dims, g, np.where(nuc, 1.0, 500.0), 12, init_gid=1)
     assert (go == 2).sum() > nuc.sum()
-    # without the stored-energy difference the nucleus does not grow
-    go2, *_ = pyoracle.pf_relax(p, dims, g, np.full(nv, 500.0), 30)
+    go2, *_ = pyoracle.pf_relax(p, dims, g, np.full(nv, 500.0), 12, init_gid=1)
     assert (go2 == 2).sum() <= nuc.sum()
 
 
@@ -50,13 +183,14 @@ def test_sparse_invariants():
     g, _, _ = synth.microstructure(cfg)
     rng = np.random.default_rng(0)
     rho = 50.0 + 400.0 * rng.random(g.size)
-    go, ids, phi, cnt = pyoracle.pf_relax(pf_params(), dims, g, rho, 8)
-    assert cnt.min() >= 1 and cnt.max() <= 8
+    go, ids, phi, cnt, _ = pyoracle.pf_relax(pf_params(), dims, g, rho, 8)
+    assert cnt.min() >= 1
     for v in range(0, g.size, 7):
         k = cnt[v]
-        assert np.all(np.diff(ids[v, :k]) > 0)          # sorted, unique
-        assert np.all(phi[v, :k] > 1e-4)                 # kept values
-        assert go[v] == ids[v, np.argmax(phi[v, :k])]    # argmax, ties to the smaller id
+        assert len(set(ids[v, :k])) == k                    # unique ids
+        assert np.all(phi[v, :k - 1] >= 5e-3)               # only the last entry may be weak
+        best = np.argmax(phi[v, :k]) if phi[v, :k].max() > 0 else None
+        assert go[v] == (ids[v, best] if best is not None else 0)   # first maximum
 
 
 def test_nucleation_counter_rng():
@@ -75,14 +209,12 @@ def test_nucleation_counter_rng():
     # below the threshold nothing nucleates
     g4, s4 = pyoracle.nucleate(p, dims, g, cry, np.full(g.size, 5.0), step=3, first_id=100)
     assert s4.size == 0 and np.array_equal(g4, g)
-    # every site is a grain-boundary voxel, painted with consecutive ids
     assert set(np.unique(g1[g1 >= 100])) <= set(range(100, 100 + s1.size))
 
 
 def test_grid_transfer_properties():
     """Phase-field grid transfer (InterpolateGrid): identity on equal grids,
     up-then-down recovers integer maps, trilinear is exact on affine fields."""
-    import pyoracle
     rng = np.random.default_rng(7)
     ns = (8, 6, 10)
     g = rng.integers(1, 20, size=int(np.prod(ns))).astype(np.int32)
