@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration measurement")
     ap.add_argument("--no-dd", action="store_true", help="skip the dislocation-density law measurement")
+    ap.add_argument("--no-drx", action="store_true", help="skip the coupled recrystallisation measurement")
     return ap.parse_args()
 
 
@@ -370,6 +371,8 @@ def run_gpu(args):
         out["adjoint"] = adjoint_measure(dev_index)
     if not args.no_dd and args.workload == "c1":
         out["dislocation_density"] = dd_measure(dev_index, args)
+    if not args.no_drx and args.workload == "c1":
+        out["drx"] = drx_measure(dev_index, args)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -406,6 +409,48 @@ def dd_measure(dev_index, args):
                         "SSD + first-order GND evolution), tension eps33_dot=1/s, dt=0.001, IterMax=100, mixed",
             "value": nv * its / dt, "unit": UNIT, "ms_per_step": dt * 1e3 / len(reps), "green_iterations": its,
             "dd_avg_last_step": [float(x) for x in reps[-1]["dd_avg"]]}
+
+
+# ------------------------------------------- coupled recrystallisation (c2)
+def drx_measure(dev_index, args):
+    """The coupled EVPFFT + sparse phase-field workload at 128^3 (1000 grains,
+    compression, 10 PF substeps per mechanical step, nucleation every step
+    from the second on), mixed precision: timed mechanical steps with the
+    whole DRX step (density, nucleation, phase field, grain adoption, new
+    reference medium) inside the timed region, after two warm-up steps."""
+    import torch
+    from mth import Solver, capi, synth
+    cfg = synth.workload("c2f")
+    par = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
+    par.device = dev_index
+    nv = int(np.prod(cfg.cell_dim))
+    nsteps = 3
+    with Solver(par, *synth.microstructure(cfg)) as s:
+        for _ in range(2):
+            s.step()
+        s.profile(enable=True, reset=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = [s.step() for _ in range(nsteps)]
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        prof, launches = s.profile(reset=True)
+        grains = s.field("grain")
+    its = sum(r["iterations"] for r in reps)
+    pf = prof.get("pf_relax", {"ms": 0.0, "bytes": 0.0, "launches": 0})
+    sub = nsteps * cfg.drx.pf_substeps
+    peak, _ = measured_peaks()
+    pf_gbs = pf["bytes"] / (pf["ms"] / 1e3) / 1e9 if pf["ms"] > 0 else None
+    return {"workload": "128x128x128 RVE, 1000 grains, compression eps33_dot=-1/s, dt=0.001, IterMax=100, "
+                        "coupled DRX: 10 PF substeps per step, nucleation every step, mixed precision",
+            "value": nv * its / dt, "unit": UNIT, "ms_per_step": dt * 1e3 / nsteps, "green_iterations": its,
+            "nuclei_per_step": [r["n_new_grains"] for r in reps], "recrystallised_voxels": int((grains > 1000).sum()),
+            "pf_ms_per_mechanical_step": pf["ms"] / nsteps, "pf_substeps_per_s": sub / (pf["ms"] / 1e3) if pf["ms"] else None,
+            "pf_voxel_substeps_per_s": nv * sub / (pf["ms"] / 1e3) if pf["ms"] else None,
+            "pf_bytes_per_voxel_substep": pf["bytes"] / (nv * sub) if sub else None,
+            "pf_gbs": pf_gbs, "pf_hbm_frac": pf_gbs / peak if pf_gbs else None, "pf_launches": pf["launches"],
+            "kernels": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in prof.items() if v["launches"]},
+            "gpu_launches": launches}
 
 
 # ------------------------------------------------------ calibration adjoint

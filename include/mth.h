@@ -96,7 +96,7 @@ typedef struct {
   double stored_energy_scale;/* Scale_Fdeform (alpha in PF_XRX) */
   double shear_modulus;      /* mu in the stored energy alpha*mu*b^2 [GPa] */
   double burgers;            /* b [nm] */
-  int    nucleus_radius;     /* cells */
+  int    nucleus_radius;     /* bound on the squared distance [cells^2] a nucleus paints (key nucleus_radius) */
   double rho_nucleation;     /* nucleation threshold on rho_tot [1e12/m^2] */
   double rho0;               /* initial dislocation density [1e12/m^2] */
   double rho_k;              /* rho = rho0 + rho_k * accumulated slip [1e12/m^2] */
@@ -200,27 +200,40 @@ mth_status mth_local_solve(const mth_params* params, const double c066[36], size
                            const double* rot, const double* crss, double* edot,
                            double* err, long long* newton_iters);
 
-/* Sparse phase-field relaxation on arrays: PF_XRX (src/pf_xrx.c:1469-1698)
- * for `substeps` explicit substeps from sharp interfaces (one order
- * parameter per voxel), with rho the stored-energy density [1e12/m^2] of
- * each voxel.  Outputs the relaxed grain ids (argmax) and, when the pointers
- * are not NULL, the MTH_PF_K order parameters of every voxel (ids sorted
- * ascending, values, count).  FP64 when params->precision is MTH_FP64,
- * FP32 otherwise.  Coefficients from params (pf_length_scale,
- * pf_time_step, e_gb, m_gb, pf_width_cells, stored_energy_scale,
- * shear_modulus, burgers). */
-#define MTH_PF_K 8
+/* Sparse phase-field relaxation on arrays: PF_XRX (src/pf_xrx.c:1469-1698,
+ * whose argument list this follows) on one grid: `substeps` explicit
+ * substeps from sharp interfaces (one order parameter per voxel), with the
+ * result the reference's sequential sweep gives.  rho: stored-energy density
+ * of each voxel [1e12/m^2]; init_gid: grain ids above it are recrystallised
+ * (a voxel they pass 0.5 at loses its stored energy, src/pf_xrx.c:1217-1219);
+ * rho_avg: the caller's table of per-grain window averages (grain id g at
+ * g-1, rho_avg_len entries), read and updated as the reference does -- pass
+ * the same table to consecutive calls.  Outputs the relaxed grain ids (first
+ * maximum of each list) and, when the pointers are not NULL, every voxel's
+ * list in stored order, up to MTH_PF_K entries (ids, values, count).  FP64
+ * when params->precision is MTH_FP64, FP32 otherwise.  Coefficients from
+ * params (pf_length_scale, pf_time_step, e_gb, m_gb, pf_width_cells,
+ * stored_energy_scale, shear_modulus, burgers).  A list over MTH_PF_K
+ * entries, over 32 ids in a 3x3x3 neighbourhood or a grain id outside the
+ * table returns MTH_ERR_UNSUPPORTED.  A voxel left without a positive eta
+ * gets grain id 0, as Update_gID gives it (the reference then stops on the
+ * assert of GetStatistics that every voxel's etas sum above 0.5, src/pf_xrx.c:1383-1386). */
+#define MTH_PF_K 16
 mth_status mth_pf_relax(const mth_params* params, const int cell_dim[3], const int* grain, const double* rho,
-                        int substeps, int* grain_out, int* ids_out, double* phi_out, int* cnt_out);
+                        int substeps, int init_gid, double* rho_avg, int rho_avg_len, int* grain_out,
+                        int* ids_out, double* phi_out, int* cnt_out);
 
 /* DRX nucleation on arrays: NucleationCheckDRX (src/integrated.c:161-494)
- * with a counter-based generator.  A voxel nucleates when it has a face
- * neighbour in another grain, its phase (1-based) is a crystal phase of
+ * with a counter-based generator.  A voxel nucleates when it is a
+ * grain-boundary voxel as the reference marks it (its +x, -x, +y, -y or +z
+ * neighbour in another grain, src/evolution.c:816-829 with
+ * src/constitutive.c:724-873), its phase (1-based) is a crystal phase of
  * params, rho > params->rho_nucleation and u(params->seed, step*N + voxel) <
  * params->nucleation_prob.  Nuclei are numbered first_id, first_id+1, ... in
- * voxel order and paint grain ids on a periodic disc |d|^2 <= r^2
- * (r = params->nucleus_radius), later nuclei over earlier ones.  sites
- * receives up to cap nucleus voxels; *n_new the number of nuclei. */
+ * voxel order and paint every voxel within squared distance
+ * params->nucleus_radius (the reference's key, compared with |d|^2), without
+ * periodic images, later nuclei over earlier ones (src/integrated.c:397-402).
+ * sites receives up to cap nucleus voxels; *n_new the number of nuclei. */
 mth_status mth_nucleate(const mth_params* params, const int cell_dim[3], int* grain, const int* phase,
                         const double* rho, long long step, int first_id, long long* sites, long long cap,
                         int* n_new);
@@ -238,11 +251,14 @@ mth_status mth_nucleate(const mth_params* params, const int cell_dim[3], int* gr
  * device image, held by every GPU that loads the library until the process
  * exits; n may not exceed MTH_NOALLOC_MAX_VOXELS (MTH_ERR_ARG otherwise).
  * The first call on each device looks up that array's device address, so
- * make it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU (different streams or threads) race, so serialise them.
- * stream: a cudaStream_t passed as void* (NULL = the default stream); the
- * call returns after the stream has finished the solve.  The device is
- * params->device. */
+ * make it before any stream capture; a cudaDeviceReset by the caller
+ * invalidates the address the library keeps.  All calls share the array:
+ * calls that overlap on the GPU (different streams or threads) race, so
+ * serialise them.  stream: a cudaStream_t passed as void* (NULL = the
+ * default stream); the call synchronises the stream and returns after it has
+ * finished the solve (newton_iters is read back from the device).  The
+ * solve runs on params->device; the caller's current device is the same
+ * after the call as before it. */
 #define MTH_NOALLOC_MAX_VOXELS (1LL << 20)
 mth_status mth_local_solve_noalloc(const mth_params* params, const double c066[36], size_t n,
                                    double* d_sig, const double* d_eps_p, const double* d_strain,

@@ -295,14 +295,8 @@ void ctx_free(mth_ctx* c) {
   delete c->drx_class_h;
   cudaFree(c->drx_rot_d);
   cudaFree(c->drx_class_d);
-  for (int i = 0; i < 2; i++) {
-    cudaFree(c->pff.ids[i]); cudaFree(c->pff.phi[i]); cudaFree(c->pff.cnt[i]);
-    cudaFree(c->pfd.ids[i]); cudaFree(c->pfd.phi[i]); cudaFree(c->pfd.cnt[i]);
-  }
-  cudaFree(c->pff.gid);
-  cudaFree(c->pfd.gid);
-  cudaFree(c->pff.pl_id); cudaFree(c->pff.pl_sum); cudaFree(c->pff.pl_cnt); cudaFree(c->pff.pl_n);
-  cudaFree(c->pfd.pl_id); cudaFree(c->pfd.pl_sum); cudaFree(c->pfd.pl_cnt); cudaFree(c->pfd.pl_n);
+  pf_free(c->pff);
+  pf_free(c->pfd);
   cudaFree(c->rho_d);
   cudaFree(c->rho_t);
   cudaFree(c->grain_prev_d);
@@ -585,6 +579,13 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   } while (0)
   CKC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   CKC(prepare_newton_kernels());
+  // failure-path test hook: MTH_TEST_FAIL_TILE_WAIT=1 makes the tile passes'
+  // first waits report a time-out (steps return MTH_ERR_TIMEOUT); every
+  // context creation sets the device's hook from the environment
+  {
+    const char* probe = getenv("MTH_TEST_FAIL_TILE_WAIT");
+    CKC(tma_set_wait_probe(probe && probe[0] == '1' ? 1 : 0));
+  }
   const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
   const long long P = c->nv;
   const int nplanes = 6 + 6 + 6 + 6 + 9 + 12 + 1 + 3;
@@ -662,7 +663,7 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   c->drx = p->pf_substeps > 0;
   if (c->drx) {
     if (!(p->pf_length_scale > 0) || !(p->pf_time_step > 0) || !(p->pf_width_cells > 0) || !(p->m_gb >= 0) ||
-        p->nucleus_radius < 0 || p->nucleus_radius > 16) {
+        p->nucleus_radius < 0 || p->nucleus_radius > 256) {
       ctx_free(c);
       return set_err(MTH_ERR_ARG, "phase-field parameters");
     }
@@ -682,16 +683,8 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     c->pf_resample = c->npf[0] != c->n[0] || c->npf[1] != c->n[1] || c->npf[2] != c->n[2];
     c->nvpf = (long long)c->npf[0] * c->npf[1] * c->npf[2];
     const long long Q = c->nvpf;
-    for (int i = 0; i < 2; i++) {
-      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.ids[i] : (void*&)c->pfd.ids[i]), sizeof(int) * PF_K * Q));
-      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.phi[i] : (void*&)c->pfd.phi[i]), esz * PF_K * Q));
-      CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.cnt[i] : (void*&)c->pfd.cnt[i]), Q));
-    }
-    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.gid : (void*&)c->pfd.gid), sizeof(int) * Q));
-    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_id : (void*&)c->pfd.pl_id), sizeof(int) * PF_PATCH * Q));
-    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_sum : (void*&)c->pfd.pl_sum), esz * PF_PATCH * Q));
-    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_cnt : (void*&)c->pfd.pl_cnt), (size_t)PF_PATCH * Q));
-    CKC(cudaMalloc(&(c->mixed ? (void*&)c->pff.pl_n : (void*&)c->pfd.pl_n), (size_t)Q));
+    // the rho_avg table grows with the grain ids (drx_step)
+    CKC(c->mixed ? pf_alloc(c->pff, c->npf, 0) : pf_alloc(c->pfd, c->npf, 0));
     if (c->pf_resample) {
       CKC(cudaMalloc(&c->grain_pf_d, sizeof(int) * Q));
       CKC(cudaMalloc(&c->rho_pf_d, sizeof(double) * Q));
@@ -1057,17 +1050,21 @@ static mth_status refresh_reference_medium(mth_ctx* c) {
 }
 
 // Algorithmic HBM bytes of one phase-field relaxation of nv voxels with
-// field element size ts: each pass reads and/or writes the sparse state
-// (PF_K ids and order parameters and a count per voxel) once, the patch pass
-// reads the grain ids and rho and writes the patch lists (about two ids per
-// patch); neighbour reads are served from cache.
+// field element size ts: per substep the sparse state (PF_K ids and order
+// parameters and a count per voxel) is read and written once, with the
+// stored energy and the grain id of the voxel; neighbour and window reads are
+// served from cache.
 static double pf_relax_bytes(long long nv, size_t ts, int substeps) {
   const double state = PF_K * (4.0 + (double)ts) + 1.0;
-  const double init = 4.0 + state + 4.0;                   // grain in; state, grain id out
-  const double sub = 2.0 * state + (double)ts + 4.0;       // state in and out, rho, grain id
-  const double amax = state + 4.0;                         // state in, grain id out
-  const double patch = 4.0 + (double)ts + 2.0 * (5.0 + (double)ts) + 1.0;   // gid, rho in; ~2 patch entries out
-  return (double)nv * (init + substeps * (sub + amax + patch));
+  return (double)nv * (4.0 + state + (double)ts + substeps * (2.0 * state + (double)ts + 4.0));
+}
+
+mth_status pf_bad_status(unsigned bad) {
+  return set_err(MTH_ERR_UNSUPPORTED,
+                 "phase field beyond this build's capacities:%s%s%s%s", (bad & PF_BAD_LIST) ? " a voxel list over 16 entries;" : "",
+                 (bad & PF_BAD_NEIGH) ? " over 32 ids in a 3x3x3 neighbourhood;" : "",
+                 (bad & PF_BAD_ROW) ? " over 32 ids written by one row of voxels;" : "",
+                 (bad & PF_BAD_TABLE) ? " a grain id outside the rho_avg table;" : "");
 }
 
 // Dynamic recrystallisation at the start of a mechanical step, the order of
@@ -1149,16 +1146,26 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
     pf_grain = c->grain_pf_d;
     pf_rho = c->rho_pf_t;
   }
+  // PF_XRX's rho_avg table persists across mechanical steps (a global of the
+  // reference); ids above the initial grains' are recrystallised (init_gid)
   int* gid_new;
+  int pf_launches = 0;
+  unsigned pf_bad = 0;
+  const int init_gid = c->first_drx_id - 1;
   if (c->mixed) {
-    LAUNCHN(K_PF, 1 + 3 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(float), p.pf_substeps),
-            launch_pf_relax<float>(c->npf, pf_grain, (const float*)pf_rho, p.pf_substeps, c->pfc, c->pff, c->st));
+    CK(pf_table_reserve(c->pff, c->next_grain_id, c->st));
+    LAUNCHN(K_PF, pf_launches, pf_relax_bytes(c->nvpf, sizeof(float), p.pf_substeps),
+            launch_pf_relax<float>(c->npf, pf_grain, (const float*)pf_rho, p.pf_substeps, init_gid, c->pfc, c->pff,
+                                   c->st, &pf_launches, &pf_bad));
     gid_new = c->pff.gid;
   } else {
-    LAUNCHN(K_PF, 1 + 3 * p.pf_substeps, pf_relax_bytes(c->nvpf, sizeof(double), p.pf_substeps),
-            launch_pf_relax<double>(c->npf, pf_grain, (const double*)pf_rho, p.pf_substeps, c->pfc, c->pfd, c->st));
+    CK(pf_table_reserve(c->pfd, c->next_grain_id, c->st));
+    LAUNCHN(K_PF, pf_launches, pf_relax_bytes(c->nvpf, sizeof(double), p.pf_substeps),
+            launch_pf_relax<double>(c->npf, pf_grain, (const double*)pf_rho, p.pf_substeps, init_gid, c->pfc, c->pfd,
+                                    c->st, &pf_launches, &pf_bad));
     gid_new = c->pfd.gid;
   }
+  if (pf_bad) return pf_bad_status(pf_bad);
   if (c->pf_resample) {   // relaxed ids back to the mechanical grid (src/integrated.c:821-860)
     LAUNCH(K_DRX, (double)c->nvpf * 4 + (double)c->nv * 4,
            launch_resample_nearest(c->npf, gid_new, c->n, c->gid_coarse_d, c->st));

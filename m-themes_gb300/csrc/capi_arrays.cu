@@ -6,7 +6,8 @@
 // ------------------------------------------------------ array-level DRX
 template <typename T>
 static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* grain, const double* rho, int substeps,
-                                  int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
+                                  int init_gid, double* rho_avg, int rho_avg_len, int* grain_out, int* ids_out,
+                                  double* phi_out, int* cnt_out) {
   const long long nv = (long long)n[0] * n[1] * n[2];
   PfCoef co;
   const double lgb = p->pf_width_cells * p->pf_length_scale;
@@ -15,58 +16,63 @@ static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* 
   co.mwell = 6 * p->e_gb / lgb;
   co.edisl = p->stored_energy_scale * p->shear_modulus * p->burgers * p->burgers;
   PfBuffers<T> b;
-  memset(&b, 0, sizeof(b));
   int* g_d = nullptr;
   T* r_d = nullptr;
-  std::vector<T> rt(nv);
+  std::vector<T> rt(nv), tab(rho_avg_len);
   for (long long v = 0; v < nv; v++) rt[v] = (T)rho[v];
+  for (int i = 0; i < rho_avg_len; i++) tab[i] = (T)rho_avg[i];
   mth_status st = MTH_OK;
   cudaStream_t s = nullptr;
-  auto fail = [&](cudaError_t e, const char* what) {
-    st = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-  };
+  int launches = 0;
+  unsigned bad = 0;
   cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
-    e = cudaMalloc(&b.ids[i], sizeof(int) * PF_K * nv);
-    if (e == cudaSuccess) e = cudaMalloc(&b.phi[i], sizeof(T) * PF_K * nv);
-    if (e == cudaSuccess) e = cudaMalloc(&b.cnt[i], nv);
-  }
-  if (e == cudaSuccess) e = cudaMalloc(&b.gid, sizeof(int) * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_id, sizeof(int) * PF_PATCH * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_sum, sizeof(T) * PF_PATCH * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_cnt, (size_t)PF_PATCH * nv);
-  if (e == cudaSuccess) e = cudaMalloc(&b.pl_n, (size_t)nv);
+  if (e == cudaSuccess) e = pf_alloc(b, n, rho_avg_len);
   if (e == cudaSuccess) e = cudaMalloc(&g_d, sizeof(int) * nv);
   if (e == cudaSuccess) e = cudaMalloc(&r_d, sizeof(T) * nv);
   if (e == cudaSuccess) e = cudaMemcpyAsync(g_d, grain, sizeof(int) * nv, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(r_d, rt.data(), sizeof(T) * nv, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = launch_pf_relax<T>(n, g_d, r_d, substeps, co, b, s);
+  if (e == cudaSuccess && rho_avg_len > 0)
+    e = cudaMemcpyAsync(b.table, tab.data(), sizeof(T) * rho_avg_len, cudaMemcpyHostToDevice, s);
+  // the table as the caller sized it: ids beyond rho_avg_len are flagged
+  b.table_len = rho_avg_len;
+  if (e == cudaSuccess) e = launch_pf_relax<T>(n, g_d, r_d, substeps, init_gid, co, b, s, &launches, &bad);
   if (e == cudaSuccess) e = cudaMemcpyAsync(grain_out, b.gid, sizeof(int) * nv, cudaMemcpyDeviceToHost, s);
   std::vector<T> ph;
+  std::vector<int> id;
   std::vector<uint8_t> cn;
-  if (e == cudaSuccess && ids_out) e = cudaMemcpyAsync(ids_out, b.ids[b.cur], sizeof(int) * PF_K * nv, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && rho_avg_len > 0)
+    e = cudaMemcpyAsync(tab.data(), b.table, sizeof(T) * rho_avg_len, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && ids_out) {
+    id.resize((size_t)PF_K * nv);
+    e = cudaMemcpyAsync(id.data(), b.ids[b.cur], sizeof(int) * PF_K * nv, cudaMemcpyDeviceToHost, s);
+  }
   if (e == cudaSuccess && phi_out) {
     ph.resize((size_t)PF_K * nv);
     e = cudaMemcpyAsync(ph.data(), b.phi[b.cur], sizeof(T) * PF_K * nv, cudaMemcpyDeviceToHost, s);
   }
-  if (e == cudaSuccess && cnt_out) {
+  if (e == cudaSuccess) {
     cn.resize(nv);
     e = cudaMemcpyAsync(cn.data(), b.cnt[b.cur], nv, cudaMemcpyDeviceToHost, s);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) fail(e, "phase-field relaxation");
-  else {
-    if (phi_out)
-      for (size_t i = 0; i < ph.size(); i++) phi_out[i] = (double)ph[i];
-    if (cnt_out)
-      for (long long v = 0; v < nv; v++) cnt_out[v] = cn[v];
+  if (e != cudaSuccess) {
+    st = set_err(e == cudaErrorMemoryAllocation ? MTH_ERR_NOMEM : MTH_ERR_CUDA, "phase-field relaxation: %s",
+                 cudaGetErrorString(e));
+  } else if (bad) {
+    st = pf_bad_status(bad);
+  } else {
+    for (int i = 0; i < rho_avg_len; i++) rho_avg[i] = (double)tab[i];
+    // lists voxel-major in stored order (the device keeps them slot-major)
+    for (long long v = 0; v < nv; v++) {
+      if (cnt_out) cnt_out[v] = cn[v];
+      for (int k = 0; k < PF_K; k++) {
+        const bool in = k < cn[v];
+        if (ids_out) ids_out[v * PF_K + k] = in ? id[(size_t)k * nv + v] : 0;
+        if (phi_out) phi_out[v * PF_K + k] = in ? (double)ph[(size_t)k * nv + v] : 0.0;
+      }
+    }
   }
-  for (int i = 0; i < 2; i++) { cudaFree(b.ids[i]); cudaFree(b.phi[i]); cudaFree(b.cnt[i]); }
-  cudaFree(b.gid);
-  cudaFree(b.pl_id);
-  cudaFree(b.pl_sum);
-  cudaFree(b.pl_cnt);
-  cudaFree(b.pl_n);
+  pf_free(b);
   cudaFree(g_d);
   cudaFree(r_d);
   if (s) cudaStreamDestroy(s);
@@ -74,15 +80,20 @@ static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* 
 }
 
 extern "C" mth_status mth_pf_relax(const mth_params* p, const int cell_dim[3], const int* grain, const double* rho,
-                                   int substeps, int* grain_out, int* ids_out, double* phi_out, int* cnt_out) {
-  if (!p || !cell_dim || !grain || !rho || !grain_out) return set_err(MTH_ERR_ARG, "null argument");
+                                   int substeps, int init_gid, double* rho_avg, int rho_avg_len, int* grain_out,
+                                   int* ids_out, double* phi_out, int* cnt_out) {
+  if (!p || !cell_dim || !grain || !rho || !grain_out || (rho_avg_len > 0 && !rho_avg))
+    return set_err(MTH_ERR_ARG, "null argument");
   for (int i = 0; i < 3; i++)
     if (cell_dim[i] < 1) return set_err(MTH_ERR_ARG, "cell_dim");
-  if (substeps < 0) return set_err(MTH_ERR_ARG, "substeps");
+  if (substeps < 0 || rho_avg_len < 0) return set_err(MTH_ERR_ARG, "substeps or rho_avg_len");
   if (!(p->pf_length_scale > 0) || !(p->pf_width_cells > 0)) return set_err(MTH_ERR_ARG, "phase-field parameters");
   CK(cudaSetDevice(p->device));
-  return p->precision == MTH_FP64 ? pf_relax_arrays<double>(p, cell_dim, grain, rho, substeps, grain_out, ids_out, phi_out, cnt_out)
-                                  : pf_relax_arrays<float>(p, cell_dim, grain, rho, substeps, grain_out, ids_out, phi_out, cnt_out);
+  return p->precision == MTH_FP64
+             ? pf_relax_arrays<double>(p, cell_dim, grain, rho, substeps, init_gid, rho_avg, rho_avg_len, grain_out,
+                                       ids_out, phi_out, cnt_out)
+             : pf_relax_arrays<float>(p, cell_dim, grain, rho, substeps, init_gid, rho_avg, rho_avg_len, grain_out,
+                                      ids_out, phi_out, cnt_out);
 }
 
 extern "C" mth_status mth_nucleate(const mth_params* p, const int cell_dim[3], int* grain, const int* phase,
@@ -145,7 +156,7 @@ extern "C" mth_status mth_local_solve_noalloc(const mth_params* p, const double 
   if (!p || !c066 || !d_sig || !d_eps_p || !d_strain || !d_rot || !d_crss || !d_edot || !d_err)
     return set_err(MTH_ERR_ARG, "null argument");
   if (p->flow_law != 0) return set_err(MTH_ERR_UNSUPPORTED, "the array-level local solve runs the power law only");
-  if ((long long)n > noalloc_max_voxels())
+  if (n > (size_t)noalloc_max_voxels())
     return set_err(MTH_ERR_ARG, "n=%zu exceeds the allocation-free limit of %lld voxels", n, noalloc_max_voxels());
   if (n == 0) {
     if (newton_iters) *newton_iters = 0;
@@ -166,9 +177,17 @@ extern "C" mth_status mth_local_solve_noalloc(const mth_params* p, const double 
   nc.dt = p->time_step;
   nc.tol = p->newton_tol > 0 ? p->newton_tol : 1e-10;
   nc.itmax = p->newton_itmax > 0 ? p->newton_itmax : 500;
-  CK(cudaSetDevice(p->device));
-  CK(launch_local_solve_noalloc(nc, (long long)n, d_sig, d_eps_p, d_strain, d_rot, d_crss, d_edot, d_err,
-                                newton_iters, static_cast<cudaStream_t>(stream)));
+  // the solve runs with params->device current; the caller's current device
+  // is restored on return
+  int caller_dev = 0;
+  CK(cudaGetDevice(&caller_dev));
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e == cudaSuccess)
+    e = launch_local_solve_noalloc(nc, (long long)n, d_sig, d_eps_p, d_strain, d_rot, d_crss, d_edot, d_err,
+                                   newton_iters, static_cast<cudaStream_t>(stream));
+  const cudaError_t e2 = cudaSetDevice(caller_dev);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return set_err(MTH_ERR_CUDA, "allocation-free local solve: %s", cudaGetErrorString(e));
   return MTH_OK;
 }
 

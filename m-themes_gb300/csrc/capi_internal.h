@@ -164,6 +164,7 @@ enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE,
 void prof_begin(mth_ctx* c);
 void prof_end(mth_ctx* c, int cls, int kernels, double bytes);
 void prof_resolve(mth_ctx* c);   // after the stream has been synchronised
+mth_status pf_bad_status(unsigned bad);   // MTH_ERR_UNSUPPORTED naming the exceeded capacities
 const char* prof_class_name(int cls);
 
 #define LAUNCHN(cls, kernels, bytes, call)         \

@@ -1,14 +1,11 @@
 // drx.cu -- dynamic recrystallisation on the GPU: grain-boundary nucleation
 // with a counter-based generator (NucleationCheckDRX, src/integrated.c:161-494)
 // and the sparse order-parameter Allen-Cahn relaxation (PF_XRX / Update_grid /
-// Update_gID, src/pf_xrx.c:6-66,895-1311,1469-1698) in the deterministic form
-// documented in oracle/drx_oracle.c's restatement: at most PF_K order
-// parameters per voxel, sorted by grain id; neighbourhood id set over the
-// 3x3x3 block; stored-energy averages over the 7x7x7 window per grain id;
-// explicit update with the 18-point Laplacian; argmax with ties to the
-// smaller id.  One thread per voxel.  This translation unit is compiled
-// without FMA contraction so that FP64 results are the separately rounded
-// operations of the restatement, bit for bit.
+// Update_gID, src/pf_xrx.c:6-66,895-1311,1469-1698), the reference's
+// sequential sweep computed in parallel passes (section "phase field").
+// This translation unit is compiled without FMA contraction so that FP64
+// results are the separately rounded operations of the reference, bit for
+// bit.
 #include <cstdint>
 #include "mth_common.cuh"
 #include "mth_internal.h"
@@ -17,7 +14,6 @@ namespace mth {
 
 #define PF_EPS 5.0e-3
 #define PF_KEEP 1.0e-4
-constexpr int MAXIDS = 64;
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   x += 0x9E3779B97F4A7C15ULL;
@@ -42,9 +38,12 @@ struct Dims {
 };
 
 // -------------------------------------------------------------- nucleation
-// Candidate: face neighbour in another grain (GB indicator,
-// src/evolution.c:816-829), crystal phase, rho > rho_nuc, u(seed, counter) <
-// prob.  Candidates are appended in arbitrary order; the host sorts them.
+// Candidate: grain-boundary voxel as the reference marks it
+// (src/evolution.c:816-829 from Gradient_ExchangeGrainID,
+// src/constitutive.c:724-873: the +x, -x, +y, -y or +z neighbour in another
+// grain -- its "-z" check compares with the -y neighbour), crystal phase,
+// rho > rho_nuc, u(seed, counter) < prob.  Candidates are appended in
+// arbitrary order; the host sorts them.
 __global__ void nucleation_candidates_kernel(Dims d, const int* __restrict__ grain, const uint8_t* __restrict__ crystal,
                                              const double* __restrict__ rho, double rho_nuc, double prob,
                                              uint64_t seed, uint64_t counter0, long long* __restrict__ out,
@@ -57,7 +56,7 @@ __global__ void nucleation_candidates_kernel(Dims d, const int* __restrict__ gra
   const int g = grain[v];
   const bool gb = (grain[d.idx(x + 1, y, z)] != g) | (grain[d.idx(x - 1, y, z)] != g) |
                   (grain[d.idx(x, y + 1, z)] != g) | (grain[d.idx(x, y - 1, z)] != g) |
-                  (grain[d.idx(x, y, z + 1)] != g) | (grain[d.idx(x, y, z - 1)] != g);
+                  (grain[d.idx(x, y, z + 1)] != g);
   if (!gb || !(rho[v] > rho_nuc)) return;
   const double u = uniform01(seed, counter0 + (uint64_t)v);
   if (u < prob) {
@@ -66,21 +65,24 @@ __global__ void nucleation_candidates_kernel(Dims d, const int* __restrict__ gra
   }
 }
 
-// Disc painting: winner[v] = max nucleus index whose disc |d|^2 <= r^2
-// (periodic) covers v; later nuclei win, as the sequential overwrite.
-__global__ void paint_mark_kernel(Dims d, const long long* __restrict__ sites, int nn, int radius,
+// Disc painting (src/integrated.c:397-402): winner[v] = max nucleus index
+// whose squared distance to v is <= radius2 (the reference's nucleus_radius,
+// compared with |d|^2), without periodic images; later nuclei win, as the
+// sequential overwrite.
+__global__ void paint_mark_kernel(Dims d, const long long* __restrict__ sites, int nn, int r, int radius2,
                                   int* __restrict__ winner) {
-  const int side = 2 * radius + 1;
+  const int side = 2 * r + 1;
   const int per = side * side * side;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)nn * per) return;
   const int k = (int)(t / per);
   const int o = (int)(t % per);
-  const int dx = o / (side * side) - radius, dy = (o / side) % side - radius, dz = o % side - radius;
-  if (dx * dx + dy * dy + dz * dz > radius * radius) return;
+  const int dx = o / (side * side) - r, dy = (o / side) % side - r, dz = o % side - r;
+  if (dx * dx + dy * dy + dz * dz > radius2) return;
   const long long v = sites[k];
-  const int x = (int)(v / ((long long)d.n1 * d.n2)), y = (int)((v / d.n2) % d.n1), z = (int)(v % d.n2);
-  atomicMax(&winner[d.idx(x + dx, y + dy, z + dz)], k);
+  const int x = (int)(v / ((long long)d.n1 * d.n2)) + dx, y = (int)((v / d.n2) % d.n1) + dy, z = (int)(v % d.n2) + dz;
+  if (x < 0 || x >= d.n0 || y < 0 || y >= d.n1 || z < 0 || z >= d.n2) return;
+  atomicMax(&winner[((long long)x * d.n1 + y) * d.n2 + z], k);
 }
 
 __global__ void paint_apply_kernel(long long nv, int first_id, int* __restrict__ winner, int* __restrict__ grain) {
@@ -94,243 +96,431 @@ __global__ void paint_apply_kernel(long long nv, int first_id, int* __restrict__
 }
 
 // ------------------------------------------------------------ phase field
+// PF_XRX / Update_grid / Update_gID (src/pf_xrx.c:6-66,895-1311,1469-1698)
+// as the reference's sequential sweep computes it, in parallel passes.
+//
+// The reference sweeps x, y, z over the voxels and, while it does, changes
+// the grid it reads: looking up an id a voxel does not hold takes over that
+// voxel's last entry when the entry is below EPSILON (relabelling it) or
+// appends (id, 0) (PFdata::operator[], src/PFgrid.h:70-90); it writes a
+// global rho_avg table that later voxels read for ids they do not hold; and
+// it resets the stored energy of a voxel a recrystallised id crosses
+// (src/pf_xrx.c:1217-1219), which later voxels' window averages see.  Every
+// one of these effects reaches a voxel only from voxels earlier in the sweep,
+// and reads return the same value whatever the relabelling (a missing id
+// reads the weak last entry's value, or 0), so each voxel's outcome is a
+// function of the previous substep and of decisions of earlier voxels.  The
+// passes compute those decisions to their fixed point (iterating until no
+// voxel's decision changes, which happens after at most the length of the
+// longest chain of dependent voxels, in practice two to four iterations):
+//   nlist   N(v): ids with eta > EPSILON over the 3x3x3 block, scan order;
+//   upd     whether the voxel holds more than one entry when the sweep
+//           reaches it: it does if it held several, or if it held one strong
+//           entry and one of its nine preceding stencil neighbours that
+//           updates has an id it lacks in N (that neighbour's Laplacian
+//           lookup appends it) -- fixed point;
+//   tail    the id its last entry carries by then: the last such lookup, from
+//           the latest preceding updating neighbour;
+//   window  per held entry, the mean stored energy over the 7x7x7 window of
+//           voxels whose initial grain id matches, with the resets of
+//           earlier voxels in this substep;
+//   rows    per row of voxels, the last value each id wrote to the table;
+//   update  the new lists, with rho_avg of ids not held read from the latest
+//           earlier writer (same row, then earlier rows, then the table) and
+//           the energy resets this substep causes -- window/rows/update are
+//           iterated to the fixed point of the resets;
+//   table   each id's last writer's value into the table; finish: resets
+//           applied, grain id = first maximum.
+// Summation orders and the Laplacian's term order are the reference's, and
+// this file is compiled without FMA contraction, so FP64 results equal the
+// reference's sweep bit for bit (the oracle restates that sweep literally).
+
+struct PfView {
+  Dims d;
+  long long nv;
+  int rows;
+};
+
+// PFdata lookup by value: the entry's eta, else the weak last entry's, else 0
 template <typename T>
-__global__ void pf_init_kernel(long long nv, const int* __restrict__ grain, int* __restrict__ ids, T* __restrict__ phi,
-                               uint8_t* __restrict__ cnt, int* __restrict__ gid) {
-  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
-  ids[v * PF_K] = grain[v];
-  phi[v * PF_K] = (T)1;
-  for (int s = 1; s < PF_K; s++) {
-    ids[v * PF_K + s] = 0;
-    phi[v * PF_K + s] = (T)0;
+__device__ __forceinline__ T pf_read_local(const int* id, const T* ph, int n, int j) {
+  for (int k = 0; k < n; k++)
+    if (id[k] == j) return ph[k];
+  if (n > 0 && ph[n - 1] < (T)PF_EPS) return ph[n - 1];
+  return (T)0;
+}
+template <typename T>
+__device__ __forceinline__ T pf_read_g(const int* __restrict__ ids, const T* __restrict__ phi,
+                                       const uint8_t* __restrict__ cnt, long long nv, long long w, int j) {
+  const int n = cnt[w];
+  for (int k = 0; k < n; k++)
+    if (ids[(long long)k * nv + w] == j) return phi[(long long)k * nv + w];
+  if (n > 0) {
+    const T t = phi[(long long)(n - 1) * nv + w];
+    if (t < (T)PF_EPS) return t;
   }
+  return (T)0;
+}
+// PFdata lookup for assignment into a list under construction
+template <typename T>
+__device__ __forceinline__ void pf_write_local(int* id, T* ph, int& n, int j, T val, unsigned* bad) {
+  for (int k = 0; k < n; k++)
+    if (id[k] == j) { ph[k] = val; return; }
+  if (n > 0 && ph[n - 1] < (T)PF_EPS) { id[n - 1] = j; ph[n - 1] = val; return; }
+  if (n == PF_K) { *bad |= PF_BAD_LIST; return; }
+  id[n] = j;
+  ph[n] = val;
+  n++;
+}
+// the list a voxel holds when the sweep reaches it: its stored list with the
+// last entry relabelled or (tail, 0) appended
+template <typename T>
+__device__ __forceinline__ int pf_held(const PfView& g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                       const uint8_t* __restrict__ cnt, const int* __restrict__ tail,
+                                       const uint8_t* __restrict__ tmode, long long v, int* hid, T* hph) {
+  int n = cnt[v];
+  for (int k = 0; k < n; k++) {
+    hid[k] = ids[(long long)k * g.nv + v];
+    hph[k] = phi[(long long)k * g.nv + v];
+  }
+  const int m = tmode[v];
+  if (m == 1) hid[n - 1] = tail[v];
+  else if (m == 2) { hid[n] = tail[v]; hph[n] = (T)0; n++; }
+  return n;
+}
+// the nine stencil neighbours that precede v in the sweep, latest first
+__constant__ int8_t c_pred[9][3] = {{0, 0, -1}, {0, -1, 1}, {0, -1, 0}, {0, -1, -1}, {-1, 1, 0},
+                                    {-1, 0, 1}, {-1, 0, 0}, {-1, 0, -1}, {-1, -1, 0}};
+
+template <typename T>
+__global__ void pf_init_kernel(PfView g, const int* __restrict__ grain, const T* __restrict__ rho, int* __restrict__ ids,
+                               T* __restrict__ phi, uint8_t* __restrict__ cnt, T* __restrict__ energy,
+                               int* __restrict__ gid) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.nv) return;
+  ids[v] = grain[v];
+  phi[v] = (T)1;
   cnt[v] = 1;
+  energy[v] = rho[v];
   gid[v] = grain[v];
 }
 
 template <typename T>
-__device__ __forceinline__ T eta_of(const int* ids, const T* phi, const uint8_t* cnt, long long w, int id) {
-  const int c = cnt[w];
-  for (int s = 0; s < c; s++)
-    if (ids[w * PF_K + s] == id) return phi[w * PF_K + s];
-  return (T)0;
-}
-
-__device__ __forceinline__ void sorted_insert(int* list, int& nl, int id) {
-  int i = 0;
-  while (i < nl && list[i] < id) i++;
-  if (i < nl && list[i] == id) return;
-  if (nl >= MAXIDS) return;
-  for (int j = nl; j > i; j--) list[j] = list[j - 1];
-  list[i] = id;
-  nl++;
-}
-
-// Per voxel (x,y,z): for each grain id in the 7x7 patch of the x plane
-// (y-3..y+3, z-3..z+3) the sum of rho in (y,z) order and the voxel count;
-// up to PF_PATCH ids, else the patch is marked (n = 255) and the substep
-// scans it directly.
-template <typename T>
-__global__ void __launch_bounds__(256) pf_patch_kernel(Dims d, const int* __restrict__ gid, const T* __restrict__ rho,
-                                                       int* __restrict__ pl_id, T* __restrict__ pl_sum,
-                                                       uint8_t* __restrict__ pl_cnt, uint8_t* __restrict__ pl_n) {
-  const long long nv = (long long)d.n0 * d.n1 * d.n2;
+__global__ void __launch_bounds__(256) pf_nlist_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                                       const uint8_t* __restrict__ cnt, int* __restrict__ nid,
+                                                       uint8_t* __restrict__ ncnt, unsigned* __restrict__ word) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
-  const int x = (int)(v / ((long long)d.n1 * d.n2)), y = (int)((v / d.n2) % d.n1), z = (int)(v % d.n2);
-  int id[PF_PATCH];
-  T sm[PF_PATCH];
-  int ct[PF_PATCH];
+  if (v >= g.nv) return;
+  const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+  int L[PF_NM];
   int n = 0;
-  bool over = false;
-  for (int dy = -3; dy <= 3 && !over; dy++)
-    for (int dz = -3; dz <= 3; dz++) {
-      const long long w = d.idx(x, y + dy, z + dz);
-      const int g = gid[w];
-      int i = 0;
-      while (i < n && id[i] != g) i++;
-      if (i == n) {
-        if (n == PF_PATCH) { over = true; break; }
-        id[n] = g;
-        sm[n] = (T)0;
-        ct[n] = 0;
-        n++;
-      }
-      sm[i] = sm[i] + rho[w];
-      ct[i]++;
-    }
-  pl_n[v] = over ? (uint8_t)255 : (uint8_t)n;
-  if (over) return;
-  for (int i = 0; i < n; i++) {
-    pl_id[(long long)i * nv + v] = id[i];
-    pl_sum[(long long)i * nv + v] = sm[i];
-    pl_cnt[(long long)i * nv + v] = (uint8_t)ct[i];
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(128) pf_substep_kernel(Dims d, const int* __restrict__ ids, const T* __restrict__ phi,
-                                                         const uint8_t* __restrict__ cnt, int* __restrict__ ids2,
-                                                         T* __restrict__ phi2, uint8_t* __restrict__ cnt2,
-                                                         const int* __restrict__ gid, const T* __restrict__ rho,
-                                                         T mcoef, T kappa, T mwell, T edisl,
-                                                         const int* __restrict__ pl_id, const T* __restrict__ pl_sum,
-                                                         const uint8_t* __restrict__ pl_cnt,
-                                                         const uint8_t* __restrict__ pl_n) {
-  const long long nv = (long long)d.n0 * d.n1 * d.n2;
-  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
-  const int x = (int)(v / ((long long)d.n1 * d.n2)), y = (int)((v / d.n2) % d.n1), z = (int)(v % d.n2);
-  int nid[MAXIDS];
-  int nn = 0;
+  unsigned bad = 0;
   for (int dx = -1; dx <= 1; dx++)
     for (int dy = -1; dy <= 1; dy++)
       for (int dz = -1; dz <= 1; dz++) {
-        const long long w = d.idx(x + dx, y + dy, z + dz);
+        const long long w = g.d.idx(x + dx, y + dy, z + dz);
         const int c = cnt[w];
-        for (int s = 0; s < c; s++)
-          if (phi[w * PF_K + s] > (T)PF_EPS) sorted_insert(nid, nn, ids[w * PF_K + s]);
-      }
-  const int cv = cnt[v];
-  if (nn <= 1) {
-    cnt2[v] = (uint8_t)cv;
-    for (int s = 0; s < PF_K; s++) {
-      ids2[v * PF_K + s] = s < cv ? ids[v * PF_K + s] : 0;
-      phi2[v * PF_K + s] = s < cv ? phi[v * PF_K + s] : (T)0;
-    }
-    return;
-  }
-  int uid[MAXIDS];
-  int nu = 0;
-  for (int i = 0; i < nn; i++) sorted_insert(uid, nu, nid[i]);
-  for (int s = 0; s < cv; s++) sorted_insert(uid, nu, ids[v * PF_K + s]);
-  T wsum[MAXIDS];
-  int wcnt[MAXIDS];
-  for (int i = 0; i < nu; i++) {
-    wsum[i] = (T)0;
-    wcnt[i] = 0;
-  }
-  // window sums: the seven x planes' patch sums added in x order
-  for (int dx = -3; dx <= 3; dx++) {
-    const long long u = d.idx(x + dx, y, z);
-    const int pn = pl_n[u];
-    if (pn != 255) {
-      for (int i = 0; i < nu; i++) {
-        T ps = (T)0;
-        int pc = 0;
-        for (int j = 0; j < pn; j++)
-          if (pl_id[(long long)j * nv + u] == uid[i]) {
-            ps = pl_sum[(long long)j * nv + u];
-            pc = pl_cnt[(long long)j * nv + u];
-            break;
-          }
-        wsum[i] = wsum[i] + ps;
-        wcnt[i] += pc;
-      }
-    } else {   // more ids in that patch than the list holds: scan it here
-      for (int i = 0; i < nu; i++) {
-        T ps = (T)0;
-        int pc = 0;
-        for (int dy = -3; dy <= 3; dy++)
-          for (int dz = -3; dz <= 3; dz++) {
-            const long long w = d.idx(x + dx, y + dy, z + dz);
-            if (gid[w] == uid[i]) {
-              ps = ps + rho[w];
-              pc++;
-            }
-          }
-        wsum[i] = wsum[i] + ps;
-        wcnt[i] += pc;
-      }
-    }
-  }
-  T rbar[MAXIDS];
-  for (int i = 0; i < nu; i++) rbar[i] = wcnt[i] > 0 ? wsum[i] / (T)wcnt[i] : (T)0;
-  T sum_rex = 0, sum1 = 0, hdef = 0;
-  for (int s = 0; s < cv; s++) {
-    const int id = ids[v * PF_K + s];
-    int i = 0;
-    while (i < nu && uid[i] != id) i++;
-    if (i < nu && wcnt[i] > 0 && rbar[i] > (T)0) {
-      const T e = phi[v * PF_K + s];
-      const T h = e * e * e * ((T)10.0 - (T)15.0 * e + (T)6.0 * e * e);
-      sum_rex = sum_rex + e * e;
-      sum1 = sum1 + h;
-      hdef = hdef + h * rbar[i];
-    }
-  }
-  int kid[PF_K + 1];
-  T kval[PF_K + 1];
-  int nk = 0;
-  for (int a = 0; a < nn; a++) {
-    const int id = nid[a];
-    int i = 0;
-    while (i < nu && uid[i] != id) i++;
-    if (i == nu || !(rbar[i] > (T)0)) continue;
-    const T c = eta_of<T>(ids, phi, cnt, v, id);
-    const T f_r = eta_of<T>(ids, phi, cnt, d.idx(x + 1, y, z), id);
-    const T f_l = eta_of<T>(ids, phi, cnt, d.idx(x - 1, y, z), id);
-    const T f_f = eta_of<T>(ids, phi, cnt, d.idx(x, y + 1, z), id);
-    const T f_b = eta_of<T>(ids, phi, cnt, d.idx(x, y - 1, z), id);
-    const T f_u = eta_of<T>(ids, phi, cnt, d.idx(x, y, z + 1), id);
-    const T f_d = eta_of<T>(ids, phi, cnt, d.idx(x, y, z - 1), id);
-    const T e_lu = eta_of<T>(ids, phi, cnt, d.idx(x - 1, y, z + 1), id);
-    const T e_lf = eta_of<T>(ids, phi, cnt, d.idx(x - 1, y - 1, z), id);
-    const T e_ld = eta_of<T>(ids, phi, cnt, d.idx(x - 1, y, z - 1), id);
-    const T e_lb = eta_of<T>(ids, phi, cnt, d.idx(x - 1, y + 1, z), id);
-    const T e_rd = eta_of<T>(ids, phi, cnt, d.idx(x + 1, y, z - 1), id);
-    const T e_ru = eta_of<T>(ids, phi, cnt, d.idx(x + 1, y, z + 1), id);
-    const T e_rf = eta_of<T>(ids, phi, cnt, d.idx(x + 1, y - 1, z), id);
-    const T e_rb = eta_of<T>(ids, phi, cnt, d.idx(x + 1, y + 1, z), id);
-    const T e_cuf = eta_of<T>(ids, phi, cnt, d.idx(x, y - 1, z + 1), id);
-    const T e_cdb = eta_of<T>(ids, phi, cnt, d.idx(x, y + 1, z - 1), id);
-    const T e_cub = eta_of<T>(ids, phi, cnt, d.idx(x, y + 1, z + 1), id);
-    const T e_cdf = eta_of<T>(ids, phi, cnt, d.idx(x, y - 1, z - 1), id);
-    const T lap = (T)0.5 * (f_r + f_l + f_f + f_b + f_u + f_d) +
-                  (T)0.125 * (e_lu + e_lf + e_ld + e_lb + e_rd + e_ru + e_rf + e_rb + e_cuf + e_cdb + e_cub + e_cdf) -
-                  (T)4.5 * c;
-    const T h = c * c * c * ((T)10.0 - (T)15.0 * c + (T)6.0 * c * c);
-    const T dh = c * c * ((T)30.0 - (T)60.0 * c + (T)30.0 * c * c);
-    const T drive = sum1 > (T)0 ? edisl * dh * ((sum1 - h) * rbar[i] - (hdef - h * rbar[i])) / (sum1 * sum1) : (T)0;
-    const T val = c - mcoef * (mwell * (c * c * c - c + (T)3.0 * c * (sum_rex - c * c)) - kappa * lap + drive);
-    if (val > (T)PF_KEEP) {
-      kid[nk] = id;
-      kval[nk] = val;
-      nk++;
-      if (nk > PF_K) {   // drop the smallest (ties: the larger id), keep id order
-        int m = 0;
-        for (int b = 1; b < nk; b++)
-          if (kval[b] < kval[m] || (kval[b] == kval[m] && kid[b] > kid[m])) m = b;
-        for (int b = m; b < nk - 1; b++) {
-          kid[b] = kid[b + 1];
-          kval[b] = kval[b + 1];
+        for (int k = 0; k < c; k++) {
+          if (!(phi[(long long)k * g.nv + w] > (T)PF_EPS)) continue;
+          const int j = ids[(long long)k * g.nv + w];
+          bool seen = false;
+          for (int a = 0; a < n; a++) seen |= (L[a] == j);
+          if (seen) continue;
+          if (n == PF_NM) { bad |= PF_BAD_NEIGH; continue; }
+          L[n++] = j;
         }
-        nk--;
       }
-    }
-  }
-  cnt2[v] = (uint8_t)nk;
-  for (int s = 0; s < PF_K; s++) {
-    ids2[v * PF_K + s] = s < nk ? kid[s] : 0;
-    phi2[v * PF_K + s] = s < nk ? kval[s] : (T)0;
-  }
+  ncnt[v] = (uint8_t)n;
+  for (int a = 0; a < n; a++) nid[(long long)a * g.nv + v] = L[a];
+  if (bad) atomicOr(&word[1], bad);
 }
 
 template <typename T>
-__global__ void pf_argmax_kernel(long long nv, const int* __restrict__ ids, const T* __restrict__ phi,
-                                 const uint8_t* __restrict__ cnt, int* __restrict__ gid) {
+__global__ void __launch_bounds__(256) pf_upd_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                                     const uint8_t* __restrict__ cnt, const int* __restrict__ nid,
+                                                     const uint8_t* __restrict__ ncnt, const uint8_t* __restrict__ upd_in,
+                                                     uint8_t* __restrict__ upd_out, unsigned* __restrict__ word) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
-  T best = (T)0;
-  int g = gid[v];
+  if (v >= g.nv) return;
   const int c = cnt[v];
-  for (int s = 0; s < c; s++)
-    if (phi[v * PF_K + s] > best) {
-      best = phi[v * PF_K + s];
-      g = ids[v * PF_K + s];
+  bool u = c > 1;
+  if (c == 1 && phi[v] >= (T)PF_EPS) {
+    const int X = ids[v];
+    const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+    for (int o = 0; o < 9 && !u; o++) {
+      const int qx = x + c_pred[o][0], qy = y + c_pred[o][1], qz = z + c_pred[o][2];
+      if (qx < 0 || qy < 0 || qy >= g.d.n1 || qz < 0 || qz >= g.d.n2) continue;
+      const long long q = ((long long)qx * g.d.n1 + qy) * g.d.n2 + qz;
+      if (!upd_in[q]) continue;
+      const int nq = ncnt[q];
+      u = nq >= 2 || (nq == 1 && nid[q] != X);
     }
-  gid[v] = g;
+  }
+  upd_out[v] = (uint8_t)u;
+  if ((uint8_t)u != upd_in[v]) atomicAdd(&word[0], 1u);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) pf_tail_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                                      const uint8_t* __restrict__ cnt, const int* __restrict__ nid,
+                                                      const uint8_t* __restrict__ ncnt, const uint8_t* __restrict__ upd,
+                                                      int* __restrict__ tail, uint8_t* __restrict__ tmode,
+                                                      unsigned* __restrict__ word) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.nv) return;
+  const int c = cnt[v];
+  const bool weak = c > 0 && phi[(long long)(c - 1) * g.nv + v] < (T)PF_EPS;
+  const int ns = weak ? c - 1 : c;
+  int sid[PF_K];
+  for (int k = 0; k < ns; k++) sid[k] = ids[(long long)k * g.nv + v];
+  const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+  int t = -1;
+  for (int o = 0; o < 9 && t < 0; o++) {
+    const int qx = x + c_pred[o][0], qy = y + c_pred[o][1], qz = z + c_pred[o][2];
+    if (qx < 0 || qy < 0 || qy >= g.d.n1 || qz < 0 || qz >= g.d.n2) continue;
+    const long long q = ((long long)qx * g.d.n1 + qy) * g.d.n2 + qz;
+    if (!upd[q]) continue;
+    for (int a = ncnt[q] - 1; a >= 0; a--) {
+      const int j = nid[(long long)a * g.nv + q];
+      bool strong = false;
+      for (int k = 0; k < ns; k++) strong |= (sid[k] == j);
+      if (!strong) { t = j; break; }
+    }
+  }
+  uint8_t m = 0;
+  if (t >= 0) {
+    if (weak) m = 1;
+    else if (c < PF_K) m = 2;
+    else atomicOr(&word[1], (unsigned)PF_BAD_LIST);
+  }
+  tail[v] = t;
+  tmode[v] = m;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) pf_window_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                                        const uint8_t* __restrict__ cnt, const int* __restrict__ tail,
+                                                        const uint8_t* __restrict__ tmode, const int* __restrict__ gid0,
+                                                        const T* __restrict__ energy, const uint8_t* __restrict__ ow,
+                                                        T* __restrict__ wavg) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.nv) return;
+  int hid[PF_K + 1];
+  T hph[PF_K + 1];
+  const int n = pf_held<T>(g, ids, phi, cnt, tail, tmode, v, hid, hph);
+  if (n <= 1) return;
+  const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+  T A[PF_K + 1];
+  int C[PF_K + 1];
+  for (int k = 0; k < n; k++) { A[k] = (T)0; C[k] = 0; }
+  for (int i = x - 3; i <= x + 3; i++) {
+    const bool ix = i >= 0 && i < g.d.n0;
+    const int xi = (i % g.d.n0 + g.d.n0) % g.d.n0;
+    for (int j = y - 3; j <= y + 3; j++) {
+      const bool iy = ix && j >= 0 && j < g.d.n1;
+      const int yj = (j % g.d.n1 + g.d.n1) % g.d.n1;
+      for (int m = z - 3; m <= z + 3; m++) {
+        const bool in = iy && m >= 0 && m < g.d.n2;
+        const int zm = (m % g.d.n2 + g.d.n2) % g.d.n2;
+        const long long p = ((long long)xi * g.d.n1 + yj) * g.d.n2 + zm;
+        const int gp = gid0[p];
+        T e = energy[p];
+        if (in && p < v && ow[p]) e = (T)100;
+        for (int k = 0; k < n; k++)
+          if (gp == hid[k]) { A[k] = A[k] + e; C[k]++; }
+      }
+    }
+  }
+  for (int k = 0; k < n; k++) wavg[(long long)k * g.nv + v] = C[k] > 0 ? A[k] / (T)C[k] : (T)0;
+}
+
+template <typename T>
+__global__ void pf_rows_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                               const uint8_t* __restrict__ cnt, const int* __restrict__ tail,
+                               const uint8_t* __restrict__ tmode, const T* __restrict__ wavg, int* __restrict__ rw_id,
+                               T* __restrict__ rw_val, uint8_t* __restrict__ rw_n, unsigned* __restrict__ word) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.rows) return;
+  int rn = 0;
+  for (int z = 0; z < g.d.n2; z++) {
+    const long long v = (long long)r * g.d.n2 + z;
+    int hid[PF_K + 1];
+    T hph[PF_K + 1];
+    const int n = pf_held<T>(g, ids, phi, cnt, tail, tmode, v, hid, hph);
+    if (n <= 1) continue;
+    for (int k = 0; k < n; k++) {
+      const T val = wavg[(long long)k * g.nv + v];
+      int e = 0;
+      while (e < rn && rw_id[(long long)e * g.rows + r] != hid[k]) e++;
+      if (e == rn) {
+        if (rn == PF_RW) { atomicOr(&word[1], (unsigned)PF_BAD_ROW); continue; }
+        rw_id[(long long)e * g.rows + r] = hid[k];
+        rn++;
+      }
+      rw_val[(long long)e * g.rows + r] = val;
+    }
+  }
+  rw_n[r] = (uint8_t)rn;
+}
+
+// rho_avg of id j as the sweep leaves it just before voxel v: the latest
+// earlier writer in v's row, else in an earlier row, else the table
+template <typename T>
+__device__ T pf_stale(const PfView& g, long long v, int j, const int* __restrict__ ids, const T* __restrict__ phi,
+                      const uint8_t* __restrict__ cnt, const int* __restrict__ tail, const uint8_t* __restrict__ tmode,
+                      const T* __restrict__ wavg, const int* __restrict__ rw_id, const T* __restrict__ rw_val,
+                      const uint8_t* __restrict__ rw_n, const T* __restrict__ table, int table_len, unsigned* bad) {
+  const int r = (int)(v / g.d.n2);
+  for (long long w = v - 1; w >= (long long)r * g.d.n2; w--) {
+    const int c = cnt[w], m = tmode[w];
+    const int n = c + (m == 2 ? 1 : 0);
+    if (n <= 1) continue;
+    for (int k = 0; k < n; k++) {
+      int id;
+      if (k == c) id = tail[w];
+      else if (m == 1 && k == c - 1) id = tail[w];
+      else id = ids[(long long)k * g.nv + w];
+      if (id == j) return wavg[(long long)k * g.nv + w];
+    }
+  }
+  for (int q = r - 1; q >= 0; q--) {
+    const int rn = rw_n[q];
+    for (int e = 0; e < rn; e++)
+      if (rw_id[(long long)e * g.rows + q] == j) return rw_val[(long long)e * g.rows + q];
+  }
+  if (j < 1 || j > table_len) { *bad |= PF_BAD_TABLE; return (T)0; }
+  return table[j - 1];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) pf_update_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                                        const uint8_t* __restrict__ cnt, const int* __restrict__ nid,
+                                                        const uint8_t* __restrict__ ncnt, const int* __restrict__ tail,
+                                                        const uint8_t* __restrict__ tmode, const T* __restrict__ wavg,
+                                                        const int* __restrict__ rw_id, const T* __restrict__ rw_val,
+                                                        const uint8_t* __restrict__ rw_n, const T* __restrict__ table,
+                                                        int table_len, int init_gid, T mcoef, T kappa, T mwell, T edisl,
+                                                        const uint8_t* __restrict__ ow_in, uint8_t* __restrict__ ow_out,
+                                                        int* __restrict__ ids2, T* __restrict__ phi2,
+                                                        uint8_t* __restrict__ cnt2, unsigned* __restrict__ word) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.nv) return;
+  const long long nv = g.nv;
+  int hid[PF_K + 1];
+  T hph[PF_K + 1];
+  const int n = pf_held<T>(g, ids, phi, cnt, tail, tmode, v, hid, hph);
+  int oid[PF_K];
+  T oph[PF_K];
+  int on = 0;
+  unsigned bad = 0;
+  bool reset = false;
+  const int nn = ncnt[v];
+  if (n > 1) {
+    const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+    T sum_rex = 0, sum1 = 0, hdef = 0;
+    for (int k = 0; k < n; k++) {
+      const T a = wavg[(long long)k * nv + v];
+      if (a > (T)0) {
+        const T e = hph[k];
+        sum_rex = sum_rex + e * e;
+        sum1 = sum1 + e * e * e * ((T)10.0 - (T)15.0 * e + (T)6.0 * e * e);
+        hdef = hdef + (e * e * e * ((T)10.0 - (T)15.0 * e + (T)6.0 * e * e)) * a;
+      }
+    }
+    for (int a = 0; a < nn; a++) {
+      const int j = nid[(long long)a * nv + v];
+      const T c = pf_read_local<T>(hid, hph, n, j);
+      const T h = c * c * c * ((T)10.0 - (T)15.0 * c + (T)6.0 * c * c);
+      const T dh = c * c * ((T)30.0 - (T)60.0 * c + (T)30.0 * c * c);
+#define NB(a_, b_, c_) pf_read_g<T>(ids, phi, cnt, nv, g.d.idx(x + (a_), y + (b_), z + (c_)), j)
+      const T right = NB(1, 0, 0), left = NB(-1, 0, 0), front = NB(0, 1, 0), back = NB(0, -1, 0);
+      const T up = NB(0, 0, 1), down = NB(0, 0, -1);
+      const T lu = NB(-1, 0, 1), ld = NB(-1, 0, -1), lf = NB(-1, -1, 0), lb = NB(-1, 1, 0);
+      const T cuf = NB(0, -1, 1), cub = NB(0, 1, 1), cdf = NB(0, -1, -1), cdb = NB(0, 1, -1);
+      const T ru = NB(1, 0, 1), rdn = NB(1, 0, -1), rf = NB(1, -1, 0), rb = NB(1, 1, 0);
+#undef NB
+      // laplacian() receives left_up.. as its right_up.. parameters
+      // (src/pf_xrx.c:6-9 against the call at :1193-1198)
+      const T lap = (T)0.5 * (right + left + front + back + up + down) +
+                    (T)0.125 * (cuf + cdf + cub + cdb + ld + lu + lf + lb + ru + rb + rdn + rf) - (T)4.5 * c;
+      T ra;
+      int k = 0;
+      while (k < n && hid[k] != j) k++;
+      if (k < n) ra = wavg[(long long)k * nv + v];
+      else ra = pf_stale<T>(g, v, j, ids, phi, cnt, tail, tmode, wavg, rw_id, rw_val, rw_n, table, table_len, &bad);
+      if (ra > (T)0) {
+        const T val = c - mcoef * (mwell * (c * c * c - c + (T)3.0 * c * (sum_rex - c * c)) - kappa * lap +
+                                   edisl * dh * ((sum1 - h) * ra - (hdef - h * ra)) / (sum1 * sum1));
+        if (j > init_gid && c < (T)0.5 && val > (T)0.5) reset = true;
+        if (val > (T)PF_KEEP) pf_write_local<T>(oid, oph, on, j, val, &bad);
+      }
+    }
+  } else if (n == 1) {
+    for (int a = 0; a < nn; a++) {
+      const int j = nid[(long long)a * nv + v];
+      pf_write_local<T>(oid, oph, on, j, pf_read_local<T>(hid, hph, n, j), &bad);
+    }
+  }
+  cnt2[v] = (uint8_t)on;
+  for (int k = 0; k < on; k++) {
+    ids2[(long long)k * nv + v] = oid[k];
+    phi2[(long long)k * nv + v] = oph[k];
+  }
+  ow_out[v] = (uint8_t)reset;
+  if ((uint8_t)reset != ow_in[v]) atomicAdd(&word[0], 1u);
+  if (bad) atomicOr(&word[1], bad);
+}
+
+// the table after the sweep: each id's last writer (the last row writing it)
+template <typename T>
+__global__ void pf_table_mark_kernel(PfView g, const int* __restrict__ rw_id, const uint8_t* __restrict__ rw_n,
+                                     int* __restrict__ last_row, int table_len, unsigned* __restrict__ word) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.rows) return;
+  for (int e = 0; e < rw_n[r]; e++) {
+    const int j = rw_id[(long long)e * g.rows + r];
+    if (j < 1 || j > table_len) { atomicOr(&word[1], (unsigned)PF_BAD_TABLE); continue; }
+    atomicMax(&last_row[j - 1], r);
+  }
+}
+template <typename T>
+__global__ void pf_table_write_kernel(PfView g, const int* __restrict__ rw_id, const T* __restrict__ rw_val,
+                                      const uint8_t* __restrict__ rw_n, const int* __restrict__ last_row,
+                                      T* __restrict__ table, int table_len) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.rows) return;
+  for (int e = 0; e < rw_n[r]; e++) {
+    const int j = rw_id[(long long)e * g.rows + r];
+    if (j >= 1 && j <= table_len && last_row[j - 1] == r) table[j - 1] = rw_val[(long long)e * g.rows + r];
+  }
+}
+__global__ void pf_table_clear_kernel(PfView g, const int* __restrict__ rw_id, const uint8_t* __restrict__ rw_n,
+                                      int* __restrict__ last_row, int table_len) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= g.rows) return;
+  for (int e = 0; e < rw_n[r]; e++) {
+    const int j = rw_id[(long long)e * g.rows + r];
+    if (j >= 1 && j <= table_len) last_row[j - 1] = -1;
+  }
+}
+
+// resets applied to the energy; grain id = first maximum, 0 when no eta > 0
+// (Update_gID, src/pf_xrx.c:11-66)
+template <typename T>
+__global__ void pf_finish_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+                                 const uint8_t* __restrict__ cnt, const uint8_t* __restrict__ ow, T* __restrict__ energy,
+                                 int* __restrict__ gid) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.nv) return;
+  if (ow[v]) energy[v] = (T)100;
+  T best = (T)0;
+  int id = 0;
+  const int c = cnt[v];
+  for (int k = 0; k < c; k++) {
+    const T e = phi[(long long)k * g.nv + v];
+    if (best < e) { best = e; id = ids[(long long)k * g.nv + v]; }
+  }
+  gid[v] = id;
 }
 
 // ------------------------------------------------------------- launchers
@@ -346,13 +536,15 @@ cudaError_t launch_nucleation_candidates(const int dims[3], const int* grain, co
   return cudaGetLastError();
 }
 
-cudaError_t launch_paint_nuclei(const int dims[3], const long long* sites, int nn, int radius, int first_id,
+cudaError_t launch_paint_nuclei(const int dims[3], const long long* sites, int nn, int radius2, int first_id,
                                 int* winner, int* grain, cudaStream_t st) {
   Dims d{dims[0], dims[1], dims[2]};
   const long long nv = (long long)dims[0] * dims[1] * dims[2];
-  const int side = 2 * radius + 1;
+  int r = 0;
+  while ((r + 1) * (r + 1) <= radius2) r++;
+  const int side = 2 * r + 1;
   const long long work = (long long)nn * side * side * side;
-  if (work > 0) paint_mark_kernel<<<nb(work, 256), 256, 0, st>>>(d, sites, nn, radius, winner);
+  if (work > 0 && radius2 >= 0) paint_mark_kernel<<<nb(work, 256), 256, 0, st>>>(d, sites, nn, r, radius2, winner);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   paint_apply_kernel<<<nb(nv, 256), 256, 0, st>>>(nv, first_id, winner, grain);
@@ -360,37 +552,171 @@ cudaError_t launch_paint_nuclei(const int dims[3], const long long* sites, int n
 }
 
 template <typename T>
-cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, int substeps, const PfCoef& co,
-                            PfBuffers<T>& b, cudaStream_t st) {
-  Dims d{dims[0], dims[1], dims[2]};
+cudaError_t pf_alloc(PfBuffers<T>& b, const int dims[3], int table_len) {
+  memset(&b, 0, sizeof(b));
   const long long nv = (long long)dims[0] * dims[1] * dims[2];
-  pf_init_kernel<T><<<nb(nv, 256), 256, 0, st>>>(nv, grain, b.ids[0], b.phi[0], b.cnt[0], b.gid);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  int cur = 0;
-  for (int s = 0; s < substeps; s++) {
-    pf_patch_kernel<T><<<nb(nv, 256), 256, 0, st>>>(d, b.gid, rho, b.pl_id, b.pl_sum, b.pl_cnt, b.pl_n);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    pf_substep_kernel<T><<<nb(nv, 128), 128, 0, st>>>(d, b.ids[cur], b.phi[cur], b.cnt[cur], b.ids[1 - cur],
-                                                      b.phi[1 - cur], b.cnt[1 - cur], b.gid, rho, (T)co.mcoef,
-                                                      (T)co.kappa, (T)co.mwell, (T)co.edisl, b.pl_id, b.pl_sum,
-                                                      b.pl_cnt, b.pl_n);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    cur = 1 - cur;
-    pf_argmax_kernel<T><<<nb(nv, 256), 256, 0, st>>>(nv, b.ids[cur], b.phi[cur], b.cnt[cur], b.gid);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+  b.rows = dims[0] * dims[1];
+  cudaError_t e = cudaSuccess;
+  auto get = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  for (int i = 0; i < 2; i++) {
+    get((void**)&b.ids[i], sizeof(int) * PF_K * nv);
+    get((void**)&b.phi[i], sizeof(T) * PF_K * nv);
+    get((void**)&b.cnt[i], (size_t)nv);
+    get((void**)&b.upd[i], (size_t)nv);
+    get((void**)&b.ow[i], (size_t)nv);
   }
-  b.cur = cur;
+  get((void**)&b.gid, sizeof(int) * nv);
+  get((void**)&b.energy, sizeof(T) * nv);
+  get((void**)&b.nid, sizeof(int) * PF_NM * nv);
+  get((void**)&b.ncnt, (size_t)nv);
+  get((void**)&b.tail, sizeof(int) * nv);
+  get((void**)&b.tmode, (size_t)nv);
+  get((void**)&b.wavg, sizeof(T) * (PF_K + 1) * nv);
+  get((void**)&b.rw_id, sizeof(int) * PF_RW * (size_t)b.rows);
+  get((void**)&b.rw_val, sizeof(T) * PF_RW * (size_t)b.rows);
+  get((void**)&b.rw_n, (size_t)b.rows);
+  get((void**)&b.word, sizeof(unsigned) * 2);
+  if (e == cudaSuccess) e = pf_table_reserve(b, table_len, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return e;
+}
+
+template <typename T>
+void pf_free(PfBuffers<T>& b) {
+  for (int i = 0; i < 2; i++) {
+    cudaFree(b.ids[i]); cudaFree(b.phi[i]); cudaFree(b.cnt[i]); cudaFree(b.upd[i]); cudaFree(b.ow[i]);
+  }
+  cudaFree(b.gid); cudaFree(b.energy); cudaFree(b.nid); cudaFree(b.ncnt); cudaFree(b.tail); cudaFree(b.tmode);
+  cudaFree(b.wavg); cudaFree(b.rw_id); cudaFree(b.rw_val); cudaFree(b.rw_n); cudaFree(b.last_row);
+  cudaFree(b.table); cudaFree(b.word);
+  memset(&b, 0, sizeof(b));
+}
+
+template <typename T>
+cudaError_t pf_table_reserve(PfBuffers<T>& b, int len, cudaStream_t st) {
+  if (len <= b.table_len) return cudaSuccess;
+  const int cap = len + 1024;
+  T* t = nullptr;
+  int* lr = nullptr;
+  cudaError_t e = cudaMalloc(&t, sizeof(T) * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&lr, sizeof(int) * cap);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t, 0, sizeof(T) * cap, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lr, 0xff, sizeof(int) * cap, st);
+  if (e == cudaSuccess && b.table_len > 0)
+    e = cudaMemcpyAsync(t, b.table, sizeof(T) * b.table_len, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaFree(t);
+    cudaFree(lr);
+    return e;
+  }
+  cudaFree(b.table);
+  cudaFree(b.last_row);
+  b.table = t;
+  b.last_row = lr;
+  b.table_len = cap;
   return cudaSuccess;
 }
 
-template cudaError_t launch_pf_relax<float>(const int*, const int*, const float*, int, const PfCoef&, PfBuffers<float>&,
-                                            cudaStream_t);
-template cudaError_t launch_pf_relax<double>(const int*, const int*, const double*, int, const PfCoef&,
-                                             PfBuffers<double>&, cudaStream_t);
+// fixed-point driver: the host reads the change counter after each iterate
+static cudaError_t pf_read_counter(unsigned* word_d, unsigned* out, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(out, word_d, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
+}
+
+template <typename T>
+cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, int substeps, int init_gid,
+                            const PfCoef& co, PfBuffers<T>& b, cudaStream_t st, int* launches, unsigned* bad) {
+  PfView g{Dims{dims[0], dims[1], dims[2]}, (long long)dims[0] * dims[1] * dims[2], dims[0] * dims[1]};
+  const long long nv = g.nv;
+  int nl = 0;
+  *bad = 0;
+#define PF_CK(call)                        \
+  do {                                     \
+    cudaError_t e__ = (call);              \
+    if (e__ != cudaSuccess) {              \
+      *launches = nl;                      \
+      return e__;                          \
+    }                                      \
+  } while (0)
+#define PF_K_LAUNCH(...)          \
+  do {                            \
+    __VA_ARGS__;                  \
+    nl++;                         \
+    PF_CK(cudaGetLastError());    \
+  } while (0)
+  PF_CK(cudaMemsetAsync(b.word, 0, sizeof(unsigned) * 2, st));
+  PF_K_LAUNCH(pf_init_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, grain, rho, b.ids[0], b.phi[0], b.cnt[0], b.energy, b.gid));
+  int cur = 0;
+  unsigned changed = 0;
+  for (int s = 0; s < substeps; s++) {
+    const int* ids = b.ids[cur];
+    const T* phi = b.phi[cur];
+    const uint8_t* cnt = b.cnt[cur];
+    PF_K_LAUNCH(pf_nlist_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.word));
+    // update flags to their fixed point
+    PF_CK(cudaMemsetAsync(b.upd[0], 0, (size_t)nv, st));
+    int a = 0;
+    for (long long it = 0; it <= nv; it++) {
+      PF_CK(cudaMemsetAsync(b.word, 0, sizeof(unsigned), st));
+      PF_K_LAUNCH(pf_upd_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.upd[a],
+                                                                 b.upd[1 - a], b.word));
+      a = 1 - a;
+      PF_CK(pf_read_counter(b.word, &changed, st));
+      if (changed == 0) break;
+    }
+    PF_K_LAUNCH(pf_tail_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.upd[a], b.tail,
+                                                                b.tmode, b.word));
+    // values, with the stored-energy resets to their fixed point
+    PF_CK(cudaMemsetAsync(b.ow[0], 0, (size_t)nv, st));
+    int o = 0;
+    for (long long it = 0; it <= nv; it++) {
+      PF_CK(cudaMemsetAsync(b.word, 0, sizeof(unsigned), st));
+      PF_K_LAUNCH(pf_window_kernel<T><<<nb(nv, 128), 128, 0, st>>>(g, ids, phi, cnt, b.tail, b.tmode, grain, b.energy,
+                                                                    b.ow[o], b.wavg));
+      PF_K_LAUNCH(pf_rows_kernel<T><<<nb(g.rows, 128), 128, 0, st>>>(g, ids, phi, cnt, b.tail, b.tmode, b.wavg,
+                                                                      b.rw_id, b.rw_val, b.rw_n, b.word));
+      PF_K_LAUNCH(pf_update_kernel<T><<<nb(nv, 128), 128, 0, st>>>(
+          g, ids, phi, cnt, b.nid, b.ncnt, b.tail, b.tmode, b.wavg, b.rw_id, b.rw_val, b.rw_n, b.table, b.table_len,
+          init_gid, (T)co.mcoef, (T)co.kappa, (T)co.mwell, (T)co.edisl, b.ow[o], b.ow[1 - o], b.ids[1 - cur],
+          b.phi[1 - cur], b.cnt[1 - cur], b.word));
+      o = 1 - o;
+      PF_CK(pf_read_counter(b.word, &changed, st));
+      if (changed == 0) break;
+    }
+    PF_K_LAUNCH(pf_table_mark_kernel<T><<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_n, b.last_row, b.table_len,
+                                                                          b.word));
+    PF_K_LAUNCH(pf_table_write_kernel<T><<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_val, b.rw_n, b.last_row,
+                                                                           b.table, b.table_len));
+    PF_K_LAUNCH(pf_table_clear_kernel<<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_n, b.last_row, b.table_len));
+    cur = 1 - cur;
+    PF_K_LAUNCH(pf_finish_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, b.ids[cur], b.phi[cur], b.cnt[cur], b.ow[o],
+                                                                  b.energy, b.gid));
+  }
+  b.cur = cur;
+  unsigned w[2] = {0, 0};
+  PF_CK(cudaMemcpyAsync(w, b.word, sizeof(w), cudaMemcpyDeviceToHost, st));
+  PF_CK(cudaStreamSynchronize(st));
+  *bad = w[1];
+  *launches = nl;
+#undef PF_K_LAUNCH
+#undef PF_CK
+  return cudaSuccess;
+}
+
+template cudaError_t pf_alloc<float>(PfBuffers<float>&, const int*, int);
+template cudaError_t pf_alloc<double>(PfBuffers<double>&, const int*, int);
+template void pf_free<float>(PfBuffers<float>&);
+template void pf_free<double>(PfBuffers<double>&);
+template cudaError_t pf_table_reserve<float>(PfBuffers<float>&, int, cudaStream_t);
+template cudaError_t pf_table_reserve<double>(PfBuffers<double>&, int, cudaStream_t);
+template cudaError_t launch_pf_relax<float>(const int*, const int*, const float*, int, int, const PfCoef&,
+                                            PfBuffers<float>&, cudaStream_t, int*, unsigned*);
+template cudaError_t launch_pf_relax<double>(const int*, const int*, const double*, int, int, const PfCoef&,
+                                             PfBuffers<double>&, cudaStream_t, int*, unsigned*);
 
 }  // namespace mth
 
@@ -423,7 +749,10 @@ __global__ void drx_update_kernel(Fields<TSt> f, int* __restrict__ grain, const 
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   if (v >= P) return;
-  const int gn = gid_new[v];
+  // a voxel the phase field left without a positive eta (grain id 0, where
+  // the reference stops on GetStatistics' assert, src/pf_xrx.c:1383-1386)
+  // keeps the grain it had
+  const int gn = gid_new[v] != 0 ? gid_new[v] : grain[v];
   grain[v] = gn;
   if (gn == grain_prev[v] || f.phase[v] != 0) return;
   const int k = gn - first_drx_id;

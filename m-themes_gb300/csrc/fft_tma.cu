@@ -98,12 +98,17 @@ __device__ __forceinline__ void tma_store_commit_wait() {
 // generic-proxy writes to shared memory visible to the following TMA store
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Failure-path test hook (tma_set_wait_probe): when set, every block's first
+// wait reports a time-out at once; the drain wait below still waits for the
+// real copies, so nothing is left in flight and the kernels return normally.
+__device__ int g_tile_wait_probe = 0;
+
 // Thread 0 has issued the loads that complete on bar; all threads learn
 // whether they arrived.  On time-out the error flag is raised, the copies
 // still in flight get a second bounded wait, and false is returned.
 __device__ __forceinline__ bool block_wait_loads(uint64_t* bar, int* ok_s, int* err) {
   if (threadIdx.x == 0) {
-    bool ok = mbar_wait(bar, 0);
+    bool ok = g_tile_wait_probe ? false : mbar_wait(bar, 0);
     if (!ok) {
       atomicOr(err, 1);
       mbar_wait(bar, 0);
@@ -435,6 +440,8 @@ TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, 
   }
   return t;
 }
+
+cudaError_t tma_set_wait_probe(int on) { return cudaMemcpyToSymbol(g_tile_wait_probe, &on, sizeof(int)); }
 
 void tma_destroy(TmaMaps* t) { delete t; }
 bool tma_has(const TmaMaps* t, int pass) { return t && (pass == 0 ? t->z : pass == 1 ? t->s : t->g); }

@@ -75,6 +75,9 @@ struct TmaMaps;
 template <typename T>
 TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti);
 void tma_destroy(TmaMaps* t);
+// failure-path test hook of the tile passes: 1 makes each block's first
+// tile wait report a time-out (the copies are still drained); device-wide
+cudaError_t tma_set_wait_probe(int on);
 bool tma_has(const TmaMaps* t, int pass);
 template <typename T>
 cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, const IterIn& it, int* err,
@@ -154,34 +157,63 @@ cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, 
                                const double* strain, const double* rot, const double* crss, const double* etab,
                                double* edot, double* err, long long* iters, cudaStream_t st);
 // ------------------------------------------------------------ DRX / phase field
-constexpr int PF_K = 8;   // order parameters kept per voxel
+constexpr int PF_K = 16;   // (id, eta) entries a voxel's list holds
+constexpr int PF_NM = 32;  // ids of a voxel's 3x3x3 neighbourhood N(v)
+constexpr int PF_RW = 32;  // ids one row (x, y) of voxels writes to the rho_avg table per substep
 
 struct PfCoef { double mcoef, kappa, mwell, edisl; };
 
+// Overflow bits of a phase-field run (launch_pf_relax's *bad): a capacity
+// above was exceeded or a grain id fell outside the rho_avg table.
+enum { PF_BAD_LIST = 1, PF_BAD_NEIGH = 2, PF_BAD_ROW = 4, PF_BAD_TABLE = 8 };
+
+// Device state of the phase field (drx.cu).  Every per-voxel array is
+// slot-major ([slot][voxel]) so a warp's loads of one slot coalesce.
 template <typename T>
 struct PfBuffers {
-  int* ids[2];        // PF_K per voxel, voxel-major, sorted by id
+  int* ids[2];        // lists, in stored order: ids, etas, lengths
   T* phi[2];
   uint8_t* cnt[2];
-  int* gid;           // current argmax grain id
-  int cur;            // buffer holding the result
-  // per voxel: stored energy summed per grain id over its 7x7 (y,z) patch
-  // (PF_PATCH entries, component-major; count 255 = more ids than entries)
-  int* pl_id;
-  T* pl_sum;
-  uint8_t* pl_cnt;
-  uint8_t* pl_n;
+  int* gid;           // first-maximum grain id after the last substep
+  T* energy;          // stored energy of the call (DefEng_buf), reset to 100 where a recrystallised id passed 0.5
+  int* nid;           // N(v) in scan order [PF_NM][nv], and its length
+  uint8_t* ncnt;
+  uint8_t* upd[2];    // update flags, fixed-point iterates
+  int* tail;          // id the list's last entry carries when the sweep reaches the voxel
+  uint8_t* tmode;     // 0 unchanged, 1 weak last entry relabelled, 2 (tail, 0) appended
+  T* wavg;            // window averages of the held entries [PF_K + 1][nv]
+  uint8_t* ow[2];     // stored-energy resets of this substep, fixed-point iterates
+  int* rw_id;         // per row: the ids it writes to the table and the last value [PF_RW][rows]
+  T* rw_val;
+  uint8_t* rw_n;
+  int* last_row;      // per table entry: last row writing it (-1 between substeps)
+  T* table;           // rho_avg table: grain id g at g - 1
+  int table_len;
+  unsigned int* word; // [0] fixed-point change counter, [1] overflow bits
+  int cur;            // list buffer holding the result
+  int rows;
 };
-constexpr int PF_PATCH = 8;
+
+template <typename T>
+cudaError_t pf_alloc(PfBuffers<T>& b, const int dims[3], int table_len);
+template <typename T>
+void pf_free(PfBuffers<T>& b);
+// grow the table to at least len entries, keeping its contents (new entries 0)
+template <typename T>
+cudaError_t pf_table_reserve(PfBuffers<T>& b, int len, cudaStream_t st);
 
 cudaError_t launch_nucleation_candidates(const int dims[3], const int* grain, const uint8_t* crystal, const double* rho,
                                          double rho_nuc, double prob, uint64_t seed, uint64_t counter0,
                                          long long* out, unsigned long long* count, long long cap, cudaStream_t st);
-cudaError_t launch_paint_nuclei(const int dims[3], const long long* sites, int nn, int radius, int first_id,
+cudaError_t launch_paint_nuclei(const int dims[3], const long long* sites, int nn, int radius2, int first_id,
                                 int* winner, int* grain, cudaStream_t st);
+// PF_XRX on the device: substeps sweeps from (grain, 1) per voxel with the
+// table in b; ids above init_gid are recrystallised.  Synchronises the
+// stream once per fixed-point iteration; *launches counts the kernels,
+// *bad the overflow bits.
 template <typename T>
-cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, int substeps, const PfCoef& co,
-                            PfBuffers<T>& b, cudaStream_t st);
+cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, int substeps, int init_gid,
+                            const PfCoef& co, PfBuffers<T>& b, cudaStream_t st, int* launches, unsigned* bad);
 // DRX microstructure update on the fields: rho from accumulated slip,
 // adoption of the relaxed grain ids and the reset of recrystallised voxels.
 cudaError_t launch_drx_rho(int mixed, const void* fields, double rho0, double rho_k, double* rho_d, void* rho_t,

@@ -24,6 +24,7 @@
 // reference's erral (src/evolution.c:264-270).
 #include <cstdio>
 #include <cmath>
+#include <atomic>
 #include "mth_common.cuh"
 #include "mth_internal.h"
 
@@ -1494,9 +1495,11 @@ __global__ void noalloc_total_kernel(double* scratch, int nblocks) {
 
 // Device address of g_noalloc_scratch, looked up once per device with that
 // device current (the host-side name is only a stand-in, not a device
-// address).
+// address).  Atomic slots: host threads that make their first calls on the
+// same device at the same time both look the address up and store the same
+// value.
 constexpr int NOALLOC_MAX_DEVICES = 64;
-double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+std::atomic<double*> g_noalloc_ptr[NOALLOC_MAX_DEVICES];
 }  // namespace
 
 long long noalloc_max_voxels() { return NOALLOC_MAX_VOXELS; }
@@ -1508,13 +1511,12 @@ cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, doubl
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-  if (!g_noalloc_ptr[dev]) {
-    double* p = nullptr;
-    e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+  double* scratch = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    e = cudaGetSymbolAddress((void**)&scratch, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    g_noalloc_ptr[dev] = p;
+    g_noalloc_ptr[dev].store(scratch, std::memory_order_release);
   }
-  double* scratch = g_noalloc_ptr[dev];
   const int nb = (int)((n + 255) / 256);
   // the total slot is the only one read without being written first
   e = cudaMemsetAsync(scratch + NOALLOC_MAX_BLOCKS, 0, sizeof(double), st);

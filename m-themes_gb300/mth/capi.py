@@ -60,6 +60,7 @@ class MthParams(C.Structure):
 
 
 T33 = (C.c_double * 3) * 3
+PF_K = 16   # MTH_PF_K: list entries per voxel mth_pf_relax returns
 
 
 class MthStepReport(C.Structure):
@@ -221,8 +222,8 @@ def load(path: str | None = None):
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong), C.c_void_p]
     lib.mth_pf_relax.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
-                                 C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
-                                 C.POINTER(C.c_int)]
+                                 C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int)]
     lib.mth_nucleate.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                  C.POINTER(C.c_double), C.c_longlong, C.c_int, C.POINTER(C.c_longlong), C.c_longlong,
                                  C.POINTER(C.c_int)]

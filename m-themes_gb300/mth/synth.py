@@ -48,7 +48,9 @@ class Drx:
     """Dynamic-recrystallisation parameters.  Defaults follow the reference's
     test_run/input.in (pf_length_scale, pf_time_step, E_gb, Scale_Fdeform)
     and the coupled DRX workload (mobility 1e-10 m^4/(J s), interface width 4
-    cells, 10 substeps, nucleus radius 2, nucleation at 5e14 m^-2).  rho is
+    cells, 10 substeps, nucleus radius 2 cells -- nucleus_radius = 4, as the
+    reference compares the key with the squared distance -- nucleation at
+    5e14 m^-2).  rho is
     rho0 + rho_k * accumulated slip in units of 1e12 m^-2."""
     pf_substeps: int = 10
     pf_time_step: float = 0.004
@@ -62,7 +64,7 @@ class Drx:
     rho_k: float = 600.0
     rho_nucleation: float = 500.0
     nucleation_prob: float = 2e-5
-    nucleus_radius: int = 2
+    nucleus_radius: int = 4     # bound on |d|^2 (the reference's key): radius 2 cells
     seed: int = 12345
     pf_cell_dim: tuple = None   # CellDim_pf; None: the mechanical grid
 
@@ -274,7 +276,7 @@ GlissileJunction {x[3]!r} 0.0
 HirthLock {x[4]!r} 0.0
 LomerCottrellLock {x[5]!r} 0.0
 D_0 {dd.d0!r}
-nucleus_radius 2
+nucleus_radius {cfg.drx.nucleus_radius if cfg.drx is not None else 4}
 CellDim_pf {pfd[0]} {pfd[1]} {pfd[2]}
 RandSeed 123
 E_gb 0.625

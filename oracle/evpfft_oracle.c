@@ -1259,7 +1259,9 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
                         c->rho_avg_len, gnew, NULL, NULL, NULL, 0);
     }
     for (size_t v = 0; v < nv && st == MTH_OK; v++) {
-      const int g = gnew[v];
+      /* a voxel left without a positive eta (grain id 0: the reference stops
+         there on GetStatistics' assert, src/pf_xrx.c:1383-1386) keeps its grain */
+      const int g = gnew[v] != 0 ? gnew[v] : c->grain[v];
       c->grain[v] = g;
       const int k = g - c->first_drx_id;
       if (g == prev[v] || !cry[v] || k < 0 || k >= c->n_drx) continue;

@@ -6,7 +6,7 @@
  * infrastructure: nothing in the product uses it.
  *
  * Hooks (installed by -D renames on the reference translation units, see
- * build_ref.sh):
+ * build_ref.sh; FFTW's own fftw_malloc_hook pads the FFT buffers):
  *   evp.c:       SetupJob  -> mth_ref_SetupJob  (adds the power-law CRSS
  *                state that the DD build does not allocate: crss, trial_tau,
  *                xkin, gamacum, as src/init.c:1148-1174 does without DD)
@@ -178,7 +178,21 @@ static int g_vm_calls = 0;
 static ten2nd g_disgrad_actual;
 static long long g_inv_at_last_step = 0;
 
+/* fftw_malloc with slack.  The displacement block of Evolution assigns
+ * fft_data[pIDX] after its local_loop has finished (src/evolution.c:1598-1599),
+ * when px, py and pz are one past their ranges: about one x-plane past the end
+ * of the array.  Nothing reads that element; the slack takes the write, which
+ * otherwise corrupts the heap and crashes some runs (the second step of
+ * test_run/, 32^3 with 64 grains). */
+static void* mth_ref_fftw_malloc(size_t n) {
+  const size_t pad = n / 4 + 65536;
+  void* p = malloc(n + pad);
+  if (p) memset(p, 0, n + pad);
+  return p;
+}
+
 void mth_ref_SetupJob(void) {
+  fftw_malloc_hook = mth_ref_fftw_malloc;
   SetupJob();
   /* power-law CRSS state of the non-DD build (src/init.c:1148-1174) */
   AllocMem(gamacum, lsize, real);

@@ -152,6 +152,35 @@ def main_test_run():
     print("test_run step 0: iterations", int(trace[0, 1]), "->", os.path.relpath(out, REPO))
 
 
+# The configs[0] workload at its stated size: 32^3, 64 seeded Voronoi grains,
+# Cu power law + Voce, uniaxial tension, 10 steps, IterMax 100, Err 1e-5.
+# The input declares two phases (the second unused): with N_phases 1 the
+# reference reads nSYS[1] past its one-element allocation in SetupJob
+# (src/init.c:806-807 against the NPHMAX loop at :1104-1108), which crashes
+# this 64-grain case; with no voxel of phase 2 the traces are identical (checked
+# on an 8^3 case).  Trace plus a summary of the final stress field.
+SAMPLE_VOXELS = np.arange(0, 32 ** 3, 32 ** 3 // 64)
+
+
+def main_configs():
+    ref = os.path.join(REPO, "oracle", "_ref", "forge_ref")
+    cfg = synth.workload("c0")
+    d = "/tmp/mth_golden_cfg0"
+    synth.write_case(d, cfg)
+    inp = os.path.join(d, "input.in")
+    txt = open(inp).read().replace("N_phases\t1\n", "N_phases\t2\n")
+    open(inp, "w").write(txt)
+    env = dict(os.environ, MTH_REF_TRACE=os.path.join(d, "trace.txt"), MTH_REF_DUMP=d, MTH_REF_SEED="1")
+    subprocess.run(["bash", "-c", f"ulimit -s unlimited; {ref} input.in > ref.log 2>&1"], cwd=d, env=env, check=True)
+    trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))
+    nv = int(np.prod(cfg.cell_dim))
+    sig = np.fromfile(os.path.join(d, "sig.bin")).reshape(nv, 9)
+    out = os.path.join(HERE, "cfg0_c0.npz")
+    np.savez_compressed(out, config=cfg_to_json(cfg), trace=trace, sig_norm=np.linalg.norm(sig, axis=0),
+                        sample_voxels=SAMPLE_VOXELS, sig_sample=sig[SAMPLE_VOXELS])
+    print("cfg0_c0", trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
+
+
 # ------------------------------------------------------------------ DRX
 # The reference's own PF_XRX, NucleationCheckDRX (with Gradient_ExchangeGrainID
 # and the GB indicator of src/evolution.c:816-829) and InterpolateGrid, run on
@@ -299,7 +328,7 @@ def _rand_rot(rng):
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx"]
+    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "configs"]
     if "evp" in which:
         main()
     if "dd" in which:
@@ -308,3 +337,5 @@ if __name__ == "__main__":
         main_test_run()
     if "drx" in which:
         main_drx()
+    if "configs" in which:
+        main_configs()

@@ -1,10 +1,12 @@
-"""GPU dynamic recrystallisation against the DRX restatement in the oracle.
+"""GPU dynamic recrystallisation against the oracle and the reference.
 
-FP64: the phase-field relaxation and the nucleation are the same separately
-rounded IEEE operations in the same order (oracle built with
--ffp-contract=off, kernels with -fmad=false), so order parameters, grain maps
-and nucleation sites must be bit-identical.  Mixed precision (FP32 order
-parameters) must agree on at least 99% of the grain map."""
+The oracle restates the reference's phase-field sweep literally and matches
+the reference's own PF_XRX bit for bit (tests/test_drx_oracle.py); the GPU
+computes the same sweep in parallel passes.  FP64: order parameters (in
+stored order), grain maps, the rho_avg table and nucleation sites must be
+bit-identical to the oracle's, and to the reference fixtures directly.  Mixed
+precision (FP32 order parameters) must agree on at least 99% of the grain
+map."""
 import ctypes as C
 
 import numpy as np
@@ -28,7 +30,7 @@ def lib():
 
 
 def pf_case(dims=(24, 24, 24), seed=3):
-    cfg = synth.Config(cell_dim=dims, n_grains=8, seed=seed, drx=synth.Drx())
+    cfg = synth.Config(cell_dim=dims, n_grains=8, seed=seed, drx=synth.Drx(stored_energy_scale=50.0))
     g, _, _ = synth.microstructure(cfg)
     rng = np.random.default_rng(seed)
     base = 100.0 + 400.0 * rng.random(9)
@@ -43,36 +45,72 @@ def pf_case(dims=(24, 24, 24), seed=3):
     return cfg, g.astype(np.int32), rho
 
 
-def gpu_pf(lib, par, dims, g, rho, substeps):
+def gpu_pf(lib, par, dims, g, rho, substeps, init_gid, table):
     nv = g.size
     d = (C.c_int * 3)(*dims)
     go = np.zeros(nv, np.int32)
-    ids = np.zeros(nv * 8, np.int32)
-    phi = np.zeros(nv * 8)
+    K = capi.PF_K
+    ids = np.zeros(nv * K, np.int32)
+    phi = np.zeros(nv * K)
     cnt = np.zeros(nv, np.int32)
-    capi.check(lib, lib.mth_pf_relax(C.byref(par), d, capi._iptr(g), capi._dptr(rho), substeps, capi._iptr(go),
-                                     capi._iptr(ids), capi._dptr(phi), capi._iptr(cnt)))
-    return go, ids.reshape(nv, 8), phi.reshape(nv, 8), cnt
+    t = np.array(table, dtype=np.float64)
+    capi.check(lib, lib.mth_pf_relax(C.byref(par), d, capi._iptr(np.ascontiguousarray(g, np.int32)),
+                                     capi._dptr(np.ascontiguousarray(rho, np.float64)), substeps, init_gid,
+                                     capi._dptr(t), len(t), capi._iptr(go), capi._iptr(ids), capi._dptr(phi),
+                                     capi._iptr(cnt)))
+    return go, ids.reshape(nv, K), phi.reshape(nv, K), cnt, t
 
 
 def test_pf_relax_fp64_bit_exact(lib):
     cfg, g, rho = pf_case()
     par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
-    o = pyoracle.pf_relax(par, cfg.cell_dim, g, rho, 8)
-    r = gpu_pf(lib, par, cfg.cell_dim, g, rho, 8)
-    assert np.array_equal(r[0], o[0])                 # grain map
-    assert np.array_equal(r[3], o[3])                 # counts
-    assert np.array_equal(r[1], o[1])                 # ids
-    assert np.array_equal(r[2].view(np.int64), o[2].view(np.int64))   # values, bit for bit
+    table = np.zeros(12)
+    for steps in (1, 2, 8):
+        o = pyoracle.pf_relax(par, cfg.cell_dim, g, rho, steps, 8, table, kmax=capi.PF_K)
+        r = gpu_pf(lib, par, cfg.cell_dim, g, rho, steps, 8, table)
+        assert np.array_equal(r[0], o[0]), steps                 # grain map
+        assert np.array_equal(r[3], o[3]), steps                 # counts
+        assert np.array_equal(r[1], o[1]), steps                 # ids, in stored order
+        assert np.array_equal(r[2].view(np.int64), o[2].view(np.int64)), steps   # values, bit for bit
+        assert np.array_equal(r[4], o[4]), steps                 # rho_avg table
     assert (r[0] >= 9).sum() > 0
+    # a second call continues from the table the first one left
+    g2 = np.where(r[0] == 0, g, r[0]).astype(np.int32)
+    o2 = pyoracle.pf_relax(par, cfg.cell_dim, g2, rho, 4, 8, r[4], kmax=capi.PF_K)
+    r2 = gpu_pf(lib, par, cfg.cell_dim, g2, rho, 4, 8, r[4])
+    assert np.array_equal(r2[0], o2[0]) and np.array_equal(r2[4], o2[4])
+    assert np.array_equal(r2[2].view(np.int64), o2[2].view(np.int64))
+
+
+GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("name", sorted(f[:-4] for f in __import__("os").listdir(GOLDEN) if f.startswith("pf_")))
+def test_pf_relax_matches_reference_fixtures(lib, name):
+    """The GPU against the reference's own PF_XRX run on the same inputs."""
+    import json
+    from test_drx_oracle import coef_params, golden_lists
+    z = np.load(__import__("os").path.join(GOLDEN, name + ".npz"))
+    dims = tuple(int(d) for d in z["dims"])
+    par = coef_params(json.loads(str(z["coef"])))
+    steps, init_gid = int(z["steps"]), int(z["init_gid"])
+    table0 = np.zeros(int(z["grain"].max()) + 1)
+    for s in (1, 2, steps):
+        go, ids, phi, cnt, tab = gpu_pf(lib, par, dims, z["grain"], z["rho"], s, init_gid, table0)
+        gc, gi, gv = golden_lists(z, s)
+        assert np.array_equal(cnt, gc), s
+        k = np.arange(capi.PF_K)[None, :] < cnt[:, None]
+        assert np.array_equal(ids[k], gi), s
+        assert np.array_equal(phi[k], gv), s
+    assert np.array_equal(go, z["gnew"]) and np.array_equal(tab, z["table"])
 
 
 def test_pf_relax_mixed_close(lib):
     cfg, g, rho = pf_case(seed=5)
     par64 = capi.params_from_config(cfg, precision=capi.MTH_FP64)
     par32 = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
-    o = pyoracle.pf_relax(par64, cfg.cell_dim, g, rho, 8)
-    r = gpu_pf(lib, par32, cfg.cell_dim, g, rho, 8)
+    o = pyoracle.pf_relax(par64, cfg.cell_dim, g, rho, 8, 8, np.zeros(12))
+    r = gpu_pf(lib, par32, cfg.cell_dim, g, rho, 8, 8, np.zeros(12))
     assert (r[0] == o[0]).mean() >= 0.99
 
 
@@ -95,9 +133,33 @@ def test_nucleation_bit_exact(lib):
     assert np.array_equal(gg, og)
 
 
+@pytest.mark.parametrize("name", ["nucl_voronoi", "nucl_edges"])
+def test_nucleation_matches_reference_fixtures(lib, name):
+    """NucleationCheckDRX of the reference (static threshold) is mth_nucleate
+    with nucleation_prob = 1: same sites, ids and painted map."""
+    z = np.load(__import__("os").path.join(GOLDEN, name + ".npz"))
+    dims = tuple(int(d) for d in z["dims"])
+    par = capi.params_from_config(synth.Config(cell_dim=dims, drx=synth.Drx()))
+    par.rho_nucleation = float(z["kappa"])
+    par.nucleation_prob = 1.0
+    par.nucleus_radius = int(z["radius"])
+    par.n_phases = 2
+    par.phase[1].type = 1
+    gg = np.ascontiguousarray(z["grain"], np.int32).copy()
+    ph = np.ascontiguousarray(z["phase"], np.int32)
+    sites = np.zeros(4096, np.int64)
+    n = C.c_int(0)
+    ng = int(z["n_grains"])
+    capi.check(lib, lib.mth_nucleate(C.byref(par), (C.c_int * 3)(*dims), capi._iptr(gg), capi._iptr(ph),
+                                     capi._dptr(np.ascontiguousarray(z["diff_rho"])), 3, ng + 1,
+                                     sites.ctypes.data_as(C.POINTER(C.c_longlong)), 4096, C.byref(n)))
+    assert n.value == int(z["n_new"])
+    assert np.array_equal(gg, z["grain_out"])
+
+
 def test_coupled_drx_matches_oracle():
     cfg = synth.Config(cell_dim=(16, 16, 16), n_grains=6, n_steps=6, seed=5, iter_max=8,
-                       drx=synth.Drx(rho_k=4000.0, rho_nucleation=30.0, nucleation_prob=0.02))
+                       drx=synth.Drx(rho_k=4000.0, rho_nucleation=30.0, nucleation_prob=0.005))
     g, p, e = synth.microstructure(cfg)
     par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
     from mth import Solver

@@ -6,8 +6,10 @@ pool and may fail on a GPU the pool has filled, or synchronise the device).
 For them the local solve takes device pointers for every input and output and
 keeps its only scratch in a fixed array in the library's device image.  This
 test allocates the buffers itself, as such a caller would, and checks the
-result against the allocating entry point mth_local_solve on the same inputs,
-on two calls in a row (the scratch keeps the previous call's contents).
+result against the allocating entry point mth_local_solve and against the
+oracle's restatement of the reference's UpdateStress on the same inputs, on
+two calls in a row (the scratch keeps the previous call's contents), and that
+repeated calls leave the device's free memory unchanged.
 """
 import ctypes as C
 import os
@@ -77,6 +79,7 @@ def rel(a, b):
 
 
 def test_noalloc_matches_allocating_entry_point(lib):
+    import pyoracle
     from mth import local_solve
     cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=4)
     par = capi.params_from_config(cfg)
@@ -91,6 +94,37 @@ def test_noalloc_matches_allocating_entry_point(lib):
         assert rel(e, e_ref) < 1e-6
         assert rel(err[:, 0], err_ref[:, 0]) < 1e-6
         assert it > 0 and abs(it - it_ref) <= max(1, it_ref // 100)
+        # and the reference's own algorithm (Newton with line search on |R|^2)
+        s_orc, e_orc, _, _ = pyoracle.local_solve(par, c066, *st)
+        assert rel(s, s_orc) < 1e-8
+        assert rel(e, e_orc) < 1e-6
+
+
+def test_noalloc_leaves_device_memory_and_current_device_alone(lib):
+    import torch
+    cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=4)
+    par = capi.params_from_config(cfg)
+    c066 = np.ascontiguousarray(c066_of(cfg))
+    n = 1 << 20
+    st = states(n, 5)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in st]
+    d_edot = torch.zeros((n, 6), dtype=torch.float64, device="cuda")
+    d_err = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+    it = C.c_longlong(0)
+
+    def call():
+        capi.check(lib, lib.mth_local_solve_noalloc(C.byref(par), capi._dptr(c066), n, dev[0].data_ptr(),
+                                                    dev[1].data_ptr(), dev[2].data_ptr(), dev[3].data_ptr(),
+                                                    dev[4].data_ptr(), d_edot.data_ptr(), d_err.data_ptr(),
+                                                    C.byref(it), None))
+    call()                       # loads the module and looks up the scratch address
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.current_device() == par.device
 
 
 def test_noalloc_rejects_oversize(lib):
