@@ -1063,7 +1063,7 @@ mth_status pf_bad_status(unsigned bad) {
   return set_err(MTH_ERR_UNSUPPORTED,
                  "phase field beyond this build's capacities:%s%s%s%s", (bad & PF_BAD_LIST) ? " a voxel list over 16 entries;" : "",
                  (bad & PF_BAD_NEIGH) ? " over 32 ids in a 3x3x3 neighbourhood;" : "",
-                 (bad & PF_BAD_ROW) ? " over 32 ids written by one row of voxels;" : "",
+                 (bad & PF_BAD_ROW) ? " over 128 ids written by one row of voxels;" : "",
                  (bad & PF_BAD_TABLE) ? " a grain id outside the rho_avg table;" : "");
 }
 

@@ -159,7 +159,7 @@ cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, 
 // ------------------------------------------------------------ DRX / phase field
 constexpr int PF_K = 16;   // (id, eta) entries a voxel's list holds
 constexpr int PF_NM = 32;  // ids of a voxel's 3x3x3 neighbourhood N(v)
-constexpr int PF_RW = 32;  // ids one row (x, y) of voxels writes to the rho_avg table per substep
+constexpr int PF_RW = 128; // ids one row (x, y) of voxels writes to the rho_avg table per substep
 
 struct PfCoef { double mcoef, kappa, mwell, edisl; };
 

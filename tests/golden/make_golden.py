@@ -118,10 +118,10 @@ DD_CU_ELASTIC = (241.1674 * 1000, 89.1989 * 1000, 151.9685 * 1000)
 
 def main_test_run():
     """The reference's own test_run/ inputs, unmodified, through the build with
-    the shipped flags (DD law, DD_CU).  That build stops with a segmentation
-    fault during the second mechanical step of this input; the first step's
-    trace is kept, with the parameters and microstructure as this project's
-    readers parse them."""
+    the shipped flags (DD law, DD_CU): both mechanical steps' trace, with the
+    parameters and microstructure as this project's readers parse them.  (The
+    FFT buffers carry slack for the reference's out-of-range write at
+    src/evolution.c:1598-1599, which otherwise crashes the second step.)"""
     import ctypes as C
     import shutil
     from mth import capi
@@ -134,7 +134,7 @@ def main_test_run():
     ref = os.path.join(REPO, "oracle", "_ref", "forge_ref_dd_cu")
     env = dict(os.environ, MTH_REF_TRACE=os.path.join(d, "trace.txt"), MTH_REF_SEED="1")
     subprocess.run(["bash", "-c", f"ulimit -s unlimited; {ref} input.in > ref.log 2>&1"], cwd=d, env=env)
-    trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))[:1]
+    trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))
     lib = capi.load()
     par = capi.MthParams()
     s1, s2, ms = C.create_string_buffer(256), C.create_string_buffer(256), C.create_string_buffer(256)
@@ -146,10 +146,10 @@ def main_test_run():
     e = np.zeros(3 * nv)
     capi.check(lib, lib.mth_read_microstructure(os.path.join(d, ms.value.decode()).encode(), par.cell_dim,
                                                 capi._iptr(g), capi._iptr(ph), capi._dptr(e)))
-    out = os.path.join(HERE, "tr_dd_step0.npz")
+    out = os.path.join(HERE, "tr_dd_test_run.npz")
     np.savez_compressed(out, params=np.frombuffer(bytes(par), dtype=np.uint8), dd_cu=np.array(DD_CU_ELASTIC),
                         grain=g, phase=ph, euler=e.reshape(nv, 3), trace=trace)
-    print("test_run step 0: iterations", int(trace[0, 1]), "->", os.path.relpath(out, REPO))
+    print("test_run: iterations", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
 
 
 # The configs[0] workload at its stated size: 32^3, 64 seeded Voronoi grains,
@@ -179,6 +179,32 @@ def main_configs():
     np.savez_compressed(out, config=cfg_to_json(cfg), trace=trace, sig_norm=np.linalg.norm(sig, axis=0),
                         sample_voxels=SAMPLE_VOXELS, sig_sample=sig[SAMPLE_VOXELS])
     print("cfg0_c0", trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
+
+
+# The reference's own field files: with PrintControl 1 it writes, at the end
+# of step 0, the elastic strain and the stress (WriteElsMPI "els",
+# WriteSigMPI "sig_afterDRX", src/evolution.c:1632-1652, src/io.c:322-437)
+# through MPI-IO (here the single-rank shim: the same bytes at offset 0).
+def main_iout():
+    ref = os.path.join(REPO, "oracle", "_ref", "forge_ref")
+    cfg = CASES["g8_poly"]
+    cfg = dataclasses.replace(cfg, n_steps=1)
+    d = "/tmp/mth_golden_iout"
+    import shutil
+    shutil.rmtree(d, ignore_errors=True)
+    synth.write_case(d, cfg)
+    inp = os.path.join(d, "input.in")
+    txt = open(inp).read()
+    assert "PrintControl 0 2000" in txt
+    open(inp, "w").write(txt.replace("PrintControl 0 2000", "PrintControl 1 2000"))
+    env = dict(os.environ, MTH_REF_TRACE=os.path.join(d, "trace.txt"), MTH_REF_SEED="1")
+    subprocess.run(["bash", "-c", f"ulimit -s unlimited; {ref} input.in > ref.log 2>&1"], cwd=d, env=env, check=True)
+    names = sorted(f for f in os.listdir(d) if f.endswith(".iout"))
+    assert len(names) == 12, names
+    files = {n: np.frombuffer(open(os.path.join(d, n), "rb").read(), dtype=np.uint8) for n in names}
+    out = os.path.join(HERE, "iout_g8.npz")
+    np.savez_compressed(out, config=cfg_to_json(cfg), names=np.array(names), **{"f%02d" % i: files[n] for i, n in enumerate(names)})
+    print("iout_g8", names, "->", os.path.relpath(out, REPO))
 
 
 # ------------------------------------------------------------------ DRX
@@ -328,7 +354,7 @@ def _rand_rot(rng):
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "configs"]
+    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "configs", "iout"]
     if "evp" in which:
         main()
     if "dd" in which:
@@ -339,3 +365,5 @@ if __name__ == "__main__":
         main_drx()
     if "configs" in which:
         main_configs()
+    if "iout" in which:
+        main_iout()

@@ -66,3 +66,33 @@ def test_batch_workload_small():
                 assert np.all(np.isfinite(r["sig_avg"]))
                 assert abs(r["disgrad_avg"][2, 2] - (k + 1) * c.time_step) < 1e-12
                 assert 1 <= r["iterations"] <= c.iter_max
+
+
+def test_batch_members_match_the_oracle():
+    """One member of each grid size of the 64-RVE workload (32^3, 48^3, 64^3),
+    with their own grain counts, tau0 and n, stepped together in FP64, against
+    the oracle (the reference's algorithm restated) run on each alone."""
+    import os
+    import pyoracle
+    cfgs = synth.batch_workload("c3")
+    pick = {}
+    for c in cfgs:
+        pick.setdefault(c.cell_dim, c)
+    members = [pick[d] for d in sorted(pick)]
+    assert sorted(m.cell_dim[0] for m in members) == [32, 48, 64]
+    import dataclasses
+    members = [dataclasses.replace(m, n_steps=2, iter_max=8) for m in members]
+    params = [capi.params_from_config(c, precision=capi.MTH_FP64) for c in members]
+    micro = [synth.microstructure(c) for c in members]
+    with Batch(params, micro) as b:
+        reps = [b.step() for _ in range(2)]
+        sig = [b.field(i, "sig") for i in range(len(members))]
+    for i, (p, m) in enumerate(zip(params, micro)):
+        o = pyoracle.Oracle(p, *m, nthreads=os.cpu_count())
+        orep = [o.step() for _ in range(2)]
+        for k in range(2):
+            assert reps[k][i]["iterations"] == orep[k]["iterations"], (i, k)
+            assert rel(reps[k][i]["sig_avg"], orep[k]["sig_avg"]) < 1e-6, (i, k)
+            assert rel(reps[k][i]["disgrad_avg"], orep[k]["disgrad_avg"]) < 1e-6, (i, k)
+        assert rel(sig[i], o.field("sig")) < 1e-5
+        o.close()

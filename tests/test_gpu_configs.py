@@ -1,0 +1,86 @@
+"""GPU parity at the configurations' stated sizes, not only on small cases.
+
+* configs[0] exactly (32^3, 64 grains, 10 steps, IterMax 100, Err 1e-5)
+  against the trace the reference itself wrote (tests/golden/cfg0_c0.npz):
+  FP64 within 1e-6 relative on <sigma>, <grad u> and s_vm at every step with
+  the same Green-iteration counts; mixed precision within 1e-4 on <sigma>.
+* 64^3 (256 grains), 5 steps, FP64 against the oracle on all host cores.
+* 128^3 configs[1] (512 grains, 40 pores), 2 steps of 5 Green iterations:
+  FP64 within 1e-6 and mixed within 1e-4 of the oracle's FP64.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, T_DG, T_ITER, T_SIG, T_SVM, rel, rel_l2, run_gpu, run_oracle
+from mth import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def cfg0():
+    z = np.load(os.path.join(GOLDEN, "cfg0_c0.npz"))
+    d = json.loads(str(z["config"]))
+    d["material"] = synth.Material(**d["material"])
+    for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
+        d[k] = tuple(d[k])
+    return synth.Config(**d), z
+
+
+def test_configs0_fp64_matches_reference():
+    cfg, z = cfg0()
+    assert cfg.cell_dim == (32, 32, 32) and cfg.n_grains == 64 and cfg.n_steps == 10 and cfg.iter_max == 100
+    s, reps = run_gpu(cfg, capi.MTH_FP64)
+    for k, r in enumerate(reps):
+        row = z["trace"][k]
+        assert r["iterations"] == int(row[T_ITER]), k
+        assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-6, k
+        assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-6, k
+        assert abs(r["s_vm"] - row[T_SVM]) < 1e-6 * row[T_SVM], k
+        assert r["newton_failed"] == 0
+    sig = s.field("sig")
+    assert rel(np.linalg.norm(sig, axis=0), z["sig_norm"]) < 1e-6
+    assert rel(sig[z["sample_voxels"]], z["sig_sample"]) < 1e-5
+    s.close()
+
+
+def test_configs0_mixed_within_1e4_of_reference():
+    cfg, z = cfg0()
+    s, reps = run_gpu(cfg, capi.MTH_MIXED)
+    for k, r in enumerate(reps):
+        assert rel(r["sig_avg"], z["trace"][k][T_SIG].reshape(3, 3)) < 1e-4, k
+    s.close()
+
+
+def test_64cube_fp64_matches_oracle():
+    cfg = synth.Config(cell_dim=(64, 64, 64), n_grains=256, n_steps=5, seed=20240107, iter_max=10)
+    o, oreps = run_oracle(cfg, nthreads=os.cpu_count())
+    s, reps = run_gpu(cfg, capi.MTH_FP64)
+    for k, (a, b) in enumerate(zip(reps, oreps)):
+        assert a["iterations"] == b["iterations"], k
+        assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
+        assert rel(a["disgrad_avg"], b["disgrad_avg"]) < 1e-6, k
+    assert rel_l2(s.field("sig"), o.field("sig")) < 1e-6
+    assert rel_l2(s.field("strain"), o.field("strain")) < 1e-6
+    s.close()
+    o.close()
+
+
+def test_128cube_configs1_matches_oracle():
+    cfg = synth.workload("c1")
+    cfg.n_steps, cfg.iter_max = 2, 5
+    o, oreps = run_oracle(cfg, nthreads=os.cpu_count())
+    sig_o = o.field("sig")
+    o.close()
+    s, reps = run_gpu(cfg, capi.MTH_FP64)
+    for k, (a, b) in enumerate(zip(reps, oreps)):
+        assert a["iterations"] == b["iterations"] == 5, k
+        assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
+    assert rel_l2(s.field("sig"), sig_o) < 1e-6
+    s.close()
+    s, reps = run_gpu(cfg, capi.MTH_MIXED)
+    for k, (a, b) in enumerate(zip(reps, oreps)):
+        assert rel(a["sig_avg"], b["sig_avg"]) < 1e-4, k
+    s.close()

@@ -99,3 +99,37 @@ def test_iout_errors(tmp_path):
     with pytest.raises(capi.MthError):
         s.wait_iout()
     s.close()
+
+
+def test_iout_against_the_reference_writers(tmp_path):
+    """The files the reference itself wrote at the end of step 0 (WriteElsMPI
+    "els" and WriteSigMPI "sig_afterDRX", src/io.c:322-437, with PrintControl
+    1) against mth_write_iout after the same step in FP64: the same file
+    names and sizes, values within the FP64 parity tolerance."""
+    import json
+    from helpers import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "iout_g8.npz"))
+    d = json.loads(str(z["config"]))
+    d["material"] = synth.Material(**d["material"])
+    for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
+        d[k] = tuple(d[k])
+    d.pop("dd", None)
+    d.pop("drx", None)
+    cfg = synth.Config(**d)
+    s, _ = run_gpu(cfg, capi.MTH_FP64)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        s.write_iout("els", "els", 0)
+        s.write_iout("sig", "sig_afterDRX", 0)
+        s.wait_iout()
+        names = sorted(f for f in os.listdir(tmp_path) if f.endswith(".iout"))
+        assert names == [str(n) for n in z["names"]]
+        for i, n in enumerate(names):
+            ref = z["f%02d" % i].view("<f8")
+            got = np.fromfile(n, dtype="<f8")
+            assert got.nbytes == z["f%02d" % i].size
+            assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max(), n
+    finally:
+        os.chdir(cwd)
+        s.close()

@@ -59,3 +59,31 @@ def test_oracle_matches_reference_dd_trace(name):
     assert rel(o.field("rho_ssd"), fields["rho_ssd"]) < 1e-11
     if np.abs(fields["rho_gnd"]).max() > 0:
         assert rel(o.field("rho_gnd"), fields["rho_gnd"]) < 1e-10
+
+
+def test_oracle_matches_reference_at_configs0_size():
+    """configs[0] as stated: 32^3, 64 grains, 10 steps, IterMax 100, Err 1e-5
+    (every step runs its 100 Green iterations); per-step trace and a summary
+    of the final stress field (component norms and 64 sampled voxels)."""
+    import json
+    import os
+    from helpers import GOLDEN
+    from mth import synth
+    z = np.load(os.path.join(GOLDEN, "cfg0_c0.npz"))
+    d = json.loads(str(z["config"]))
+    d["material"] = synth.Material(**d["material"])
+    for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
+        d[k] = tuple(d[k])
+    cfg = synth.Config(**d)
+    o, reps = run_oracle(cfg, nthreads=os.cpu_count() or 4)
+    trace = z["trace"]
+    for s, r in enumerate(reps):
+        row = trace[s]
+        assert r["iterations"] == int(row[T_ITER]) == 100
+        assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-10
+        assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-10
+        assert abs(r["s_vm"] - row[T_SVM]) <= 1e-10 * abs(row[T_SVM])
+        assert abs(r["err_s"] - row[T_ERRS]) <= 1e-6 * abs(row[T_ERRS])
+    sig = o.field("sig")
+    assert rel(np.linalg.norm(sig, axis=0), z["sig_norm"]) < 1e-10
+    assert rel(sig[z["sample_voxels"]], z["sig_sample"]) < 1e-9
