@@ -34,7 +34,7 @@ static mth_status pf_relax_arrays(const mth_params* p, const int* n, const int* 
   if (e == cudaSuccess && rho_avg_len > 0)
     e = cudaMemcpyAsync(b.table, tab.data(), sizeof(T) * rho_avg_len, cudaMemcpyHostToDevice, s);
   // the table as the caller sized it: ids beyond rho_avg_len are flagged
-  b.table_len = rho_avg_len;
+  b.table_len = rho_avg_len < b.table_cap ? rho_avg_len : b.table_cap;
   if (e == cudaSuccess) e = launch_pf_relax<T>(n, g_d, r_d, substeps, init_gid, co, b, s, &launches, &bad);
   if (e == cudaSuccess) e = cudaMemcpyAsync(grain_out, b.gid, sizeof(int) * nv, cudaMemcpyDeviceToHost, s);
   std::vector<T> ph;

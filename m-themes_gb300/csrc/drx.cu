@@ -297,98 +297,186 @@ __global__ void __launch_bounds__(256) pf_tail_kernel(PfView g, const int* __res
   tmode[v] = m;
 }
 
+// Window averages, one 8x8x8 tile of voxels per block: the tile and its
+// 3-voxel halo (periodic) of initial grain ids, energies and this substep's
+// resets are staged in shared memory once, and every voxel of the tile that
+// updates sums its 7x7x7 window from there, in window order, one pass per
+// held entry.  The window positions before the centre in that order are
+// exactly the voxels earlier in the sweep (the first 171), so a reset applies
+// there when the position lies inside the volume (a periodic image is a halo
+// copy, refreshed only after the sweep).
+constexpr int PF_WT = 8;
+constexpr int PF_WH = PF_WT + 6;
 template <typename T>
-__global__ void __launch_bounds__(128) pf_window_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
+__global__ void __launch_bounds__(256) pf_window_kernel(PfView g, const int* __restrict__ ids,
                                                         const uint8_t* __restrict__ cnt, const int* __restrict__ tail,
                                                         const uint8_t* __restrict__ tmode, const int* __restrict__ gid0,
                                                         const T* __restrict__ energy, const uint8_t* __restrict__ ow,
-                                                        T* __restrict__ wavg) {
-  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= g.nv) return;
-  int hid[PF_K + 1];
-  T hph[PF_K + 1];
-  const int n = pf_held<T>(g, ids, phi, cnt, tail, tmode, v, hid, hph);
-  if (n <= 1) return;
-  const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
-  T A[PF_K + 1];
-  int C[PF_K + 1];
-  for (int k = 0; k < n; k++) { A[k] = (T)0; C[k] = 0; }
-  for (int i = x - 3; i <= x + 3; i++) {
-    const bool ix = i >= 0 && i < g.d.n0;
-    const int xi = (i % g.d.n0 + g.d.n0) % g.d.n0;
-    for (int j = y - 3; j <= y + 3; j++) {
-      const bool iy = ix && j >= 0 && j < g.d.n1;
-      const int yj = (j % g.d.n1 + g.d.n1) % g.d.n1;
-      for (int m = z - 3; m <= z + 3; m++) {
-        const bool in = iy && m >= 0 && m < g.d.n2;
-        const int zm = (m % g.d.n2 + g.d.n2) % g.d.n2;
-        const long long p = ((long long)xi * g.d.n1 + yj) * g.d.n2 + zm;
-        const int gp = gid0[p];
-        T e = energy[p];
-        if (in && p < v && ow[p]) e = (T)100;
-        for (int k = 0; k < n; k++)
-          if (gp == hid[k]) { A[k] = A[k] + e; C[k]++; }
-      }
-    }
+                                                        T* __restrict__ wavg, int tiles_y, int tiles_z) {
+  __shared__ int s_gid[PF_WH * PF_WH * PF_WH];
+  __shared__ T s_e[PF_WH * PF_WH * PF_WH];
+  __shared__ uint8_t s_reset[PF_WH * PF_WH * PF_WH];
+  const int tz = blockIdx.x % tiles_z, ty = (blockIdx.x / tiles_z) % tiles_y, tx = blockIdx.x / (tiles_z * tiles_y);
+  const int x0 = tx * PF_WT, y0 = ty * PF_WT, z0 = tz * PF_WT;
+  for (int i = threadIdx.x; i < PF_WH * PF_WH * PF_WH; i += blockDim.x) {
+    const int hz = i % PF_WH, hy = (i / PF_WH) % PF_WH, hx = i / (PF_WH * PF_WH);
+    const int gx = x0 - 3 + hx, gy = y0 - 3 + hy, gz = z0 - 3 + hz;
+    const bool in = gx >= 0 && gx < g.d.n0 && gy >= 0 && gy < g.d.n1 && gz >= 0 && gz < g.d.n2;
+    const long long p = g.d.idx(gx, gy, gz);
+    s_gid[i] = gid0[p];
+    s_e[i] = energy[p];
+    s_reset[i] = (uint8_t)(in && ow[p]);
   }
-  for (int k = 0; k < n; k++) wavg[(long long)k * g.nv + v] = C[k] > 0 ? A[k] / (T)C[k] : (T)0;
-}
-
-template <typename T>
-__global__ void pf_rows_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
-                               const uint8_t* __restrict__ cnt, const int* __restrict__ tail,
-                               const uint8_t* __restrict__ tmode, const T* __restrict__ wavg, int* __restrict__ rw_id,
-                               T* __restrict__ rw_val, uint8_t* __restrict__ rw_n, unsigned* __restrict__ word) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= g.rows) return;
-  int rn = 0;
-  for (int z = 0; z < g.d.n2; z++) {
-    const long long v = (long long)r * g.d.n2 + z;
-    int hid[PF_K + 1];
-    T hph[PF_K + 1];
-    const int n = pf_held<T>(g, ids, phi, cnt, tail, tmode, v, hid, hph);
+  __syncthreads();
+  const int lz = threadIdx.x % PF_WT, ly = (threadIdx.x / PF_WT) % PF_WT;
+  for (int half = 0; half < 2; half++) {
+    const int lx = threadIdx.x / (PF_WT * PF_WT) + 4 * half;
+    const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+    if (x >= g.d.n0 || y >= g.d.n1 || z >= g.d.n2) continue;
+    const long long v = ((long long)x * g.d.n1 + y) * g.d.n2 + z;
+    const int c = cnt[v], mode = tmode[v];
+    const int n = c + (mode == 2 ? 1 : 0);
     if (n <= 1) continue;
     for (int k = 0; k < n; k++) {
-      const T val = wavg[(long long)k * g.nv + v];
-      int e = 0;
-      while (e < rn && rw_id[(long long)e * g.rows + r] != hid[k]) e++;
-      if (e == rn) {
-        if (rn == PF_RW) { atomicOr(&word[1], (unsigned)PF_BAD_ROW); continue; }
-        rw_id[(long long)e * g.rows + r] = hid[k];
-        rn++;
-      }
-      rw_val[(long long)e * g.rows + r] = val;
+      const int id = (k == c || (mode == 1 && k == c - 1)) ? tail[v] : ids[(long long)k * g.nv + v];
+      T A = (T)0;
+      int C = 0;
+      int q = 0;
+      for (int i = 0; i < 7; i++)
+        for (int j = 0; j < 7; j++) {
+          const int base = ((lx + i) * PF_WH + (ly + j)) * PF_WH + lz;
+          for (int m = 0; m < 7; m++, q++) {
+            const int w = base + m;
+            if (s_gid[w] == id) {
+              A = A + ((q < 171 && s_reset[w]) ? (T)100 : s_e[w]);
+              C++;
+            }
+          }
+        }
+      wavg[(long long)k * g.nv + v] = C > 0 ? A / (T)C : (T)0;
     }
   }
-  rw_n[r] = (uint8_t)rn;
+}
+
+// Row summaries, one block per row of voxels (x, y): every id the row's
+// updating voxels hold, with the first and last z holding it and the value
+// the last one writes.  Ids go through a shared-memory hash (open addressing,
+// 2 PF_RW slots); the order of the entries is immaterial (lookups are by id).
+constexpr int PF_RHASH = 2 * PF_RW;
+template <typename T>
+__global__ void __launch_bounds__(128) pf_rows_kernel(PfView g, const int* __restrict__ ids,
+                                                      const uint8_t* __restrict__ cnt, const int* __restrict__ tail,
+                                                      const uint8_t* __restrict__ tmode, const T* __restrict__ wavg,
+                                                      int* __restrict__ rw_id, T* __restrict__ rw_val,
+                                                      int* __restrict__ rw_zf, int* __restrict__ rw_zl,
+                                                      uint8_t* __restrict__ rw_n, unsigned* __restrict__ word) {
+  __shared__ int h_id[PF_RHASH], h_zf[PF_RHASH], h_zl[PF_RHASH];
+  __shared__ int h_n;
+  const int r = blockIdx.x;
+  for (int i = threadIdx.x; i < PF_RHASH; i += blockDim.x) {
+    h_id[i] = 0;   // grain ids are >= 1 in a table-writing list; 0 marks a free slot
+    h_zf[i] = INT_MAX;
+    h_zl[i] = -1;
+  }
+  if (threadIdx.x == 0) h_n = 0;
+  __syncthreads();
+  unsigned bad = 0;
+  // pass 1: slots, first and last z per id
+  for (int z = threadIdx.x; z < g.d.n2; z += blockDim.x) {
+    const long long v = (long long)r * g.d.n2 + z;
+    const int c = cnt[v], mode = tmode[v];
+    const int n = c + (mode == 2 ? 1 : 0);
+    if (n <= 1) continue;
+    for (int k = 0; k < n; k++) {
+      const int id = (k == c || (mode == 1 && k == c - 1)) ? tail[v] : ids[(long long)k * g.nv + v];
+      if (id < 1) { bad |= PF_BAD_TABLE; continue; }
+      int slot = (int)(((unsigned)id * 2654435761u) % PF_RHASH), tries = 0;
+      for (; tries < PF_RHASH; tries++, slot = (slot + 1) % PF_RHASH) {
+        const int prev = atomicCAS(&h_id[slot], 0, id);
+        if (prev == 0) { atomicAdd(&h_n, 1); break; }
+        if (prev == id) break;
+      }
+      if (tries == PF_RHASH) { bad |= PF_BAD_ROW; continue; }
+      atomicMin(&h_zf[slot], z);
+      atomicMax(&h_zl[slot], z);
+    }
+  }
+  __syncthreads();
+  if (h_n > PF_RW) bad |= PF_BAD_ROW;
+  // pass 2: the last writer's value, compacted into the summary
+  __shared__ int h_pos[PF_RHASH];
+  if (threadIdx.x == 0) {
+    int e = 0;
+    for (int i = 0; i < PF_RHASH; i++) h_pos[i] = (h_id[i] != 0 && e < PF_RW) ? e++ : -1;
+    rw_n[r] = (uint8_t)e;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < PF_RHASH; i += blockDim.x) {
+    const int e = h_pos[i];
+    if (e < 0) continue;
+    rw_id[(long long)e * g.rows + r] = h_id[i];
+    rw_zf[(long long)e * g.rows + r] = h_zf[i];
+    rw_zl[(long long)e * g.rows + r] = h_zl[i];
+  }
+  for (int z = threadIdx.x; z < g.d.n2; z += blockDim.x) {
+    const long long v = (long long)r * g.d.n2 + z;
+    const int c = cnt[v], mode = tmode[v];
+    const int n = c + (mode == 2 ? 1 : 0);
+    if (n <= 1) continue;
+    for (int k = 0; k < n; k++) {
+      const int id = (k == c || (mode == 1 && k == c - 1)) ? tail[v] : ids[(long long)k * g.nv + v];
+      if (id < 1) continue;
+      int slot = (int)(((unsigned)id * 2654435761u) % PF_RHASH);
+      for (int tries = 0; tries < PF_RHASH && h_id[slot] != id; tries++) slot = (slot + 1) % PF_RHASH;
+      if (h_id[slot] != id || h_pos[slot] < 0 || h_zl[slot] != z) continue;
+      rw_val[(long long)h_pos[slot] * g.rows + r] = wavg[(long long)k * g.nv + v];
+    }
+  }
+  if (bad) atomicOr(&word[1], bad);
 }
 
 // rho_avg of id j as the sweep leaves it just before voxel v: the latest
-// earlier writer in v's row, else in an earlier row, else the table
+// earlier writer in v's row, else in the earlier rows of v's block of PF_RB
+// rows, else the last writer up to the previous block (prefix table), else
+// the table as the previous substep left it
 template <typename T>
-__device__ T pf_stale(const PfView& g, long long v, int j, const int* __restrict__ ids, const T* __restrict__ phi,
-                      const uint8_t* __restrict__ cnt, const int* __restrict__ tail, const uint8_t* __restrict__ tmode,
-                      const T* __restrict__ wavg, const int* __restrict__ rw_id, const T* __restrict__ rw_val,
-                      const uint8_t* __restrict__ rw_n, const T* __restrict__ table, int table_len, unsigned* bad) {
-  const int r = (int)(v / g.d.n2);
-  for (long long w = v - 1; w >= (long long)r * g.d.n2; w--) {
-    const int c = cnt[w], m = tmode[w];
-    const int n = c + (m == 2 ? 1 : 0);
-    if (n <= 1) continue;
-    for (int k = 0; k < n; k++) {
-      int id;
-      if (k == c) id = tail[w];
-      else if (m == 1 && k == c - 1) id = tail[w];
-      else id = ids[(long long)k * g.nv + w];
-      if (id == j) return wavg[(long long)k * g.nv + w];
+__device__ T pf_stale(const PfView& g, long long v, int j, const int* __restrict__ ids, const uint8_t* __restrict__ cnt,
+                      const int* __restrict__ tail, const uint8_t* __restrict__ tmode, const T* __restrict__ wavg,
+                      const int* __restrict__ rw_id, const T* __restrict__ rw_val, const int* __restrict__ rw_zf,
+                      const int* __restrict__ rw_zl, const uint8_t* __restrict__ rw_n,
+                      const int* __restrict__ blk_row, const T* __restrict__ blk_val, int table_cap,
+                      const T* __restrict__ table, int table_len, unsigned* bad) {
+  const int r = (int)(v / g.d.n2), z = (int)(v % g.d.n2);
+  // v's row: the summary gives the first and last z holding j
+  const int rn = rw_n[r];
+  for (int e = 0; e < rn; e++) {
+    if (rw_id[(long long)e * g.rows + r] != j) continue;
+    const int zf = rw_zf[(long long)e * g.rows + r], zl = rw_zl[(long long)e * g.rows + r];
+    if (zl < z) return rw_val[(long long)e * g.rows + r];
+    if (zf < z) {   // the latest writer before v lies in [zf, z)
+      for (long long w = v - 1; w >= (long long)r * g.d.n2 + zf; w--) {
+        const int c = cnt[w], m = tmode[w];
+        const int n = c + (m == 2 ? 1 : 0);
+        if (n <= 1) continue;
+        for (int k = 0; k < n; k++) {
+          const int id = (k == c || (m == 1 && k == c - 1)) ? tail[w] : ids[(long long)k * g.nv + w];
+          if (id == j) return wavg[(long long)k * g.nv + w];
+        }
+      }
     }
+    break;
   }
-  for (int q = r - 1; q >= 0; q--) {
+  if (j < 1 || j > table_len) { *bad |= PF_BAD_TABLE; return (T)0; }
+  const int blk = r / PF_RB;
+  for (int q = r - 1; q >= blk * PF_RB; q--) {
     const int rn = rw_n[q];
     for (int e = 0; e < rn; e++)
       if (rw_id[(long long)e * g.rows + q] == j) return rw_val[(long long)e * g.rows + q];
   }
-  if (j < 1 || j > table_len) { *bad |= PF_BAD_TABLE; return (T)0; }
+  if (blk > 0) {
+    const long long at = (long long)(blk - 1) * table_cap + (j - 1);
+    if (blk_row[at] >= 0) return blk_val[at];
+  }
   return table[j - 1];
 }
 
@@ -398,8 +486,11 @@ __global__ void __launch_bounds__(128) pf_update_kernel(PfView g, const int* __r
                                                         const uint8_t* __restrict__ ncnt, const int* __restrict__ tail,
                                                         const uint8_t* __restrict__ tmode, const T* __restrict__ wavg,
                                                         const int* __restrict__ rw_id, const T* __restrict__ rw_val,
-                                                        const uint8_t* __restrict__ rw_n, const T* __restrict__ table,
-                                                        int table_len, int init_gid, T mcoef, T kappa, T mwell, T edisl,
+                                                        const int* __restrict__ rw_zf, const int* __restrict__ rw_zl,
+                                                        const uint8_t* __restrict__ rw_n, const int* __restrict__ blk_row,
+                                                        const T* __restrict__ blk_val, int table_cap,
+                                                        const T* __restrict__ table, int table_len, int init_gid, T mcoef,
+                                                        T kappa, T mwell, T edisl,
                                                         const uint8_t* __restrict__ ow_in, uint8_t* __restrict__ ow_out,
                                                         int* __restrict__ ids2, T* __restrict__ phi2,
                                                         uint8_t* __restrict__ cnt2, unsigned* __restrict__ word) {
@@ -447,7 +538,9 @@ __global__ void __launch_bounds__(128) pf_update_kernel(PfView g, const int* __r
       int k = 0;
       while (k < n && hid[k] != j) k++;
       if (k < n) ra = wavg[(long long)k * nv + v];
-      else ra = pf_stale<T>(g, v, j, ids, phi, cnt, tail, tmode, wavg, rw_id, rw_val, rw_n, table, table_len, &bad);
+      else
+        ra = pf_stale<T>(g, v, j, ids, cnt, tail, tmode, wavg, rw_id, rw_val, rw_zf, rw_zl, rw_n, blk_row, blk_val,
+                         table_cap, table, table_len, &bad);
       if (ra > (T)0) {
         const T val = c - mcoef * (mwell * (c * c * c - c + (T)3.0 * c * (sum_rex - c * c)) - kappa * lap +
                                    edisl * dh * ((sum1 - h) * ra - (hdef - h * ra)) / (sum1 * sum1));
@@ -471,37 +564,69 @@ __global__ void __launch_bounds__(128) pf_update_kernel(PfView g, const int* __r
   if (bad) atomicOr(&word[1], bad);
 }
 
-// the table after the sweep: each id's last writer (the last row writing it)
-template <typename T>
-__global__ void pf_table_mark_kernel(PfView g, const int* __restrict__ rw_id, const uint8_t* __restrict__ rw_n,
-                                     int* __restrict__ last_row, int table_len, unsigned* __restrict__ word) {
+// Prefix of the table writers: per block of PF_RB rows and id, the last row
+// writing the id in that block and its value (mark, write), then carried
+// forward over the blocks (prefix), so that entry [b][j] is the last writer
+// of j up to block b.  After the sweep, the last block's entries update the
+// table (final).
+__global__ void pf_blk_mark_kernel(PfView g, const int* __restrict__ rw_id, const uint8_t* __restrict__ rw_n,
+                                   int* __restrict__ blk_row, int table_cap, int table_len,
+                                   unsigned* __restrict__ word) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= g.rows) return;
+  const long long base = (long long)(r / PF_RB) * table_cap;
   for (int e = 0; e < rw_n[r]; e++) {
     const int j = rw_id[(long long)e * g.rows + r];
     if (j < 1 || j > table_len) { atomicOr(&word[1], (unsigned)PF_BAD_TABLE); continue; }
-    atomicMax(&last_row[j - 1], r);
+    atomicMax(&blk_row[base + j - 1], r);
   }
 }
 template <typename T>
-__global__ void pf_table_write_kernel(PfView g, const int* __restrict__ rw_id, const T* __restrict__ rw_val,
-                                      const uint8_t* __restrict__ rw_n, const int* __restrict__ last_row,
-                                      T* __restrict__ table, int table_len) {
+__global__ void pf_blk_write_kernel(PfView g, const int* __restrict__ rw_id, const T* __restrict__ rw_val,
+                                    const uint8_t* __restrict__ rw_n, const int* __restrict__ blk_row,
+                                    T* __restrict__ blk_val, int table_cap, int table_len) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= g.rows) return;
+  const long long base = (long long)(r / PF_RB) * table_cap;
   for (int e = 0; e < rw_n[r]; e++) {
     const int j = rw_id[(long long)e * g.rows + r];
-    if (j >= 1 && j <= table_len && last_row[j - 1] == r) table[j - 1] = rw_val[(long long)e * g.rows + r];
+    if (j >= 1 && j <= table_len && blk_row[base + j - 1] == r) blk_val[base + j - 1] = rw_val[(long long)e * g.rows + r];
   }
 }
-__global__ void pf_table_clear_kernel(PfView g, const int* __restrict__ rw_id, const uint8_t* __restrict__ rw_n,
-                                      int* __restrict__ last_row, int table_len) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= g.rows) return;
-  for (int e = 0; e < rw_n[r]; e++) {
-    const int j = rw_id[(long long)e * g.rows + r];
-    if (j >= 1 && j <= table_len) last_row[j - 1] = -1;
+template <typename T>
+__global__ void pf_blk_prefix_kernel(int nblk, int* __restrict__ blk_row, T* __restrict__ blk_val, int table_cap,
+                                     int table_len) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= table_len) return;
+  int cr = blk_row[j];
+  T cv = cr >= 0 ? blk_val[j] : (T)0;
+  // eight blocks' rows loaded before any is written (each address is read
+  // before it is written), then carried forward in order
+  for (int b0 = 1; b0 < nblk; b0 += 8) {
+    int rr[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) rr[u] = b0 + u < nblk ? blk_row[(long long)(b0 + u) * table_cap + j] : 0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (b0 + u >= nblk) break;
+      const long long at = (long long)(b0 + u) * table_cap + j;
+      if (rr[u] >= 0) {
+        cr = rr[u];
+        cv = blk_val[at];
+      } else if (cr >= 0) {
+        blk_row[at] = cr;
+        blk_val[at] = cv;
+      }
+    }
   }
+}
+template <typename T>
+__global__ void pf_table_final_kernel(int nblk, const int* __restrict__ blk_row, const T* __restrict__ blk_val,
+                                      int table_cap, int table_len, T* __restrict__ table) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= table_len) return;
+  const long long at = (long long)(nblk - 1) * table_cap + j;
+  if (blk_row[at] >= 0) table[j] = blk_val[at];
 }
 
 // resets applied to the energy; grain id = first maximum, 0 when no eta > 0
@@ -556,6 +681,7 @@ cudaError_t pf_alloc(PfBuffers<T>& b, const int dims[3], int table_len) {
   memset(&b, 0, sizeof(b));
   const long long nv = (long long)dims[0] * dims[1] * dims[2];
   b.rows = dims[0] * dims[1];
+  b.nblk = (b.rows + PF_RB - 1) / PF_RB;
   cudaError_t e = cudaSuccess;
   auto get = [&](void** p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMalloc(p, bytes);
@@ -576,6 +702,8 @@ cudaError_t pf_alloc(PfBuffers<T>& b, const int dims[3], int table_len) {
   get((void**)&b.wavg, sizeof(T) * (PF_K + 1) * nv);
   get((void**)&b.rw_id, sizeof(int) * PF_RW * (size_t)b.rows);
   get((void**)&b.rw_val, sizeof(T) * PF_RW * (size_t)b.rows);
+  get((void**)&b.rw_zf, sizeof(int) * PF_RW * (size_t)b.rows);
+  get((void**)&b.rw_zl, sizeof(int) * PF_RW * (size_t)b.rows);
   get((void**)&b.rw_n, (size_t)b.rows);
   get((void**)&b.word, sizeof(unsigned) * 2);
   if (e == cudaSuccess) e = pf_table_reserve(b, table_len, nullptr);
@@ -589,34 +717,43 @@ void pf_free(PfBuffers<T>& b) {
     cudaFree(b.ids[i]); cudaFree(b.phi[i]); cudaFree(b.cnt[i]); cudaFree(b.upd[i]); cudaFree(b.ow[i]);
   }
   cudaFree(b.gid); cudaFree(b.energy); cudaFree(b.nid); cudaFree(b.ncnt); cudaFree(b.tail); cudaFree(b.tmode);
-  cudaFree(b.wavg); cudaFree(b.rw_id); cudaFree(b.rw_val); cudaFree(b.rw_n); cudaFree(b.last_row);
+  cudaFree(b.wavg); cudaFree(b.rw_id); cudaFree(b.rw_val); cudaFree(b.rw_zf); cudaFree(b.rw_zl); cudaFree(b.rw_n); cudaFree(b.blk_row);
+  cudaFree(b.blk_val);
   cudaFree(b.table); cudaFree(b.word);
   memset(&b, 0, sizeof(b));
 }
 
 template <typename T>
 cudaError_t pf_table_reserve(PfBuffers<T>& b, int len, cudaStream_t st) {
-  if (len <= b.table_len) return cudaSuccess;
+  if (len <= b.table_cap) {
+    b.table_len = b.table_cap;
+    return cudaSuccess;
+  }
   const int cap = len + 1024;
   T* t = nullptr;
-  int* lr = nullptr;
+  int* br = nullptr;
+  T* bv = nullptr;
+  const size_t nb_entries = (size_t)b.nblk * cap;
   cudaError_t e = cudaMalloc(&t, sizeof(T) * cap);
-  if (e == cudaSuccess) e = cudaMalloc(&lr, sizeof(int) * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&br, sizeof(int) * nb_entries);
+  if (e == cudaSuccess) e = cudaMalloc(&bv, sizeof(T) * nb_entries);
   if (e == cudaSuccess) e = cudaMemsetAsync(t, 0, sizeof(T) * cap, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(lr, 0xff, sizeof(int) * cap, st);
-  if (e == cudaSuccess && b.table_len > 0)
-    e = cudaMemcpyAsync(t, b.table, sizeof(T) * b.table_len, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && b.table_cap > 0)
+    e = cudaMemcpyAsync(t, b.table, sizeof(T) * b.table_cap, cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaFree(t);
-    cudaFree(lr);
+    cudaFree(br);
+    cudaFree(bv);
     return e;
   }
   cudaFree(b.table);
-  cudaFree(b.last_row);
+  cudaFree(b.blk_row);
+  cudaFree(b.blk_val);
   b.table = t;
-  b.last_row = lr;
-  b.table_len = cap;
+  b.blk_row = br;
+  b.blk_val = bv;
+  b.table_cap = b.table_len = cap;
   return cudaSuccess;
 }
 
@@ -652,6 +789,8 @@ cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, i
   PF_K_LAUNCH(pf_init_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, grain, rho, b.ids[0], b.phi[0], b.cnt[0], b.energy, b.gid));
   int cur = 0;
   unsigned changed = 0;
+  const int wtx = (dims[0] + PF_WT - 1) / PF_WT, wty = (dims[1] + PF_WT - 1) / PF_WT, wtz = (dims[2] + PF_WT - 1) / PF_WT;
+  const int wtiles = wtx * wty * wtz;
   for (int s = 0; s < substeps; s++) {
     const int* ids = b.ids[cur];
     const T* phi = b.phi[cur];
@@ -675,23 +814,33 @@ cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, i
     int o = 0;
     for (long long it = 0; it <= nv; it++) {
       PF_CK(cudaMemsetAsync(b.word, 0, sizeof(unsigned), st));
-      PF_K_LAUNCH(pf_window_kernel<T><<<nb(nv, 128), 128, 0, st>>>(g, ids, phi, cnt, b.tail, b.tmode, grain, b.energy,
-                                                                    b.ow[o], b.wavg));
-      PF_K_LAUNCH(pf_rows_kernel<T><<<nb(g.rows, 128), 128, 0, st>>>(g, ids, phi, cnt, b.tail, b.tmode, b.wavg,
-                                                                      b.rw_id, b.rw_val, b.rw_n, b.word));
+      PF_K_LAUNCH(pf_window_kernel<T><<<wtiles, 256, 0, st>>>(g, ids, cnt, b.tail, b.tmode, grain, b.energy, b.ow[o],
+                                                               b.wavg, wty, wtz));
+      PF_K_LAUNCH(pf_rows_kernel<T><<<g.rows, 128, 0, st>>>(g, ids, cnt, b.tail, b.tmode, b.wavg, b.rw_id, b.rw_val,
+                                                              b.rw_zf, b.rw_zl, b.rw_n, b.word));
+      // prefix of the table writers (their values change over the iterates)
+      PF_CK(cudaMemsetAsync(b.blk_row, 0xff, sizeof(int) * (size_t)b.nblk * b.table_cap, st));
+      if (b.table_len > 0) {
+        PF_K_LAUNCH(pf_blk_mark_kernel<<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_n, b.blk_row, b.table_cap,
+                                                                         b.table_len, b.word));
+        PF_K_LAUNCH(pf_blk_write_kernel<T><<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_val, b.rw_n, b.blk_row,
+                                                                             b.blk_val, b.table_cap, b.table_len));
+        PF_K_LAUNCH(pf_blk_prefix_kernel<T><<<nb(b.table_len, 128), 128, 0, st>>>(b.nblk, b.blk_row, b.blk_val,
+                                                                                   b.table_cap, b.table_len));
+      }
       PF_K_LAUNCH(pf_update_kernel<T><<<nb(nv, 128), 128, 0, st>>>(
-          g, ids, phi, cnt, b.nid, b.ncnt, b.tail, b.tmode, b.wavg, b.rw_id, b.rw_val, b.rw_n, b.table, b.table_len,
+          g, ids, phi, cnt, b.nid, b.ncnt, b.tail, b.tmode, b.wavg, b.rw_id, b.rw_val, b.rw_zf, b.rw_zl, b.rw_n,
+          b.blk_row, b.blk_val,
+          b.table_cap, b.table, b.table_len,
           init_gid, (T)co.mcoef, (T)co.kappa, (T)co.mwell, (T)co.edisl, b.ow[o], b.ow[1 - o], b.ids[1 - cur],
           b.phi[1 - cur], b.cnt[1 - cur], b.word));
       o = 1 - o;
       PF_CK(pf_read_counter(b.word, &changed, st));
       if (changed == 0) break;
     }
-    PF_K_LAUNCH(pf_table_mark_kernel<T><<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_n, b.last_row, b.table_len,
-                                                                          b.word));
-    PF_K_LAUNCH(pf_table_write_kernel<T><<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_val, b.rw_n, b.last_row,
-                                                                           b.table, b.table_len));
-    PF_K_LAUNCH(pf_table_clear_kernel<<<nb(g.rows, 256), 256, 0, st>>>(g, b.rw_id, b.rw_n, b.last_row, b.table_len));
+    if (b.table_len > 0)
+      PF_K_LAUNCH(pf_table_final_kernel<T><<<nb(b.table_len, 256), 256, 0, st>>>(b.nblk, b.blk_row, b.blk_val,
+                                                                                   b.table_cap, b.table_len, b.table));
     cur = 1 - cur;
     PF_K_LAUNCH(pf_finish_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, b.ids[cur], b.phi[cur], b.cnt[cur], b.ow[o],
                                                                   b.energy, b.gid));

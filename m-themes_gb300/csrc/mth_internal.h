@@ -160,6 +160,7 @@ cudaError_t launch_local_solve(const NewtonConst& nc, long long n, double* sig, 
 constexpr int PF_K = 16;   // (id, eta) entries a voxel's list holds
 constexpr int PF_NM = 32;  // ids of a voxel's 3x3x3 neighbourhood N(v)
 constexpr int PF_RW = 128; // ids one row (x, y) of voxels writes to the rho_avg table per substep
+constexpr int PF_RB = 16;  // rows per block of the table-writer prefix
 
 struct PfCoef { double mcoef, kappa, mwell, edisl; };
 
@@ -183,12 +184,17 @@ struct PfBuffers {
   uint8_t* tmode;     // 0 unchanged, 1 weak last entry relabelled, 2 (tail, 0) appended
   T* wavg;            // window averages of the held entries [PF_K + 1][nv]
   uint8_t* ow[2];     // stored-energy resets of this substep, fixed-point iterates
-  int* rw_id;         // per row: the ids it writes to the table and the last value [PF_RW][rows]
-  T* rw_val;
+  int* rw_id;         // per row: the ids it writes to the table, the last value, and the
+  T* rw_val;          // first and last z of a writer [PF_RW][rows]
+  int* rw_zf;
+  int* rw_zl;
   uint8_t* rw_n;
-  int* last_row;      // per table entry: last row writing it (-1 between substeps)
+  int* blk_row;       // per block of PF_RB rows and table entry: the last row up to that block
+  T* blk_val;         // writing the id, and the value it wrote ([nblk][table_cap]; row -1: none)
   T* table;           // rho_avg table: grain id g at g - 1
-  int table_len;
+  int table_len;      // entries the kernels may use (<= table_cap)
+  int table_cap;      // entries allocated
+  int nblk;
   unsigned int* word; // [0] fixed-point change counter, [1] overflow bits
   int cur;            // list buffer holding the result
   int rows;

@@ -100,22 +100,23 @@ def test_dd_rejected_setups():
 
 def test_reference_test_run_unmodified():
     """The reference's own test_run/ inputs (32^3 single crystal with a pore,
-    the shipped DD parameters, DD_CU elastic constants, Err 5e-5), parsed by
-    this project's readers, against the reference's first step."""
-    import ctypes as C
+    the shipped DD parameters, DD_CU elastic constants, Err 5e-5, two steps),
+    parsed by this project's readers, against both steps of the reference's
+    run."""
     from helpers import GOLDEN
-    z = np.load(os.path.join(GOLDEN, "tr_dd_step0.npz"))
+    z = np.load(os.path.join(GOLDEN, "tr_dd_test_run.npz"))
     par = capi.MthParams.from_buffer_copy(z["params"].tobytes())
     par.phase[0].c11, par.phase[0].c12, par.phase[0].c44 = (float(x) for x in z["dd_cu"])
     par.flow_law = 1
     par.precision = capi.MTH_FP64
     par.device = 0
-    row = z["trace"][0]
+    assert z["trace"].shape[0] == 2
     with Solver(par, z["grain"], z["phase"], z["euler"]) as s:
-        r = s.step()
-    assert abs(r["iterations"] - int(row[T_ITER])) <= 2, (r["iterations"], row[T_ITER])
-    assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-6
-    assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-6
-    ref = row[T_DD]
-    for j in range(7):
-        assert abs(r["dd_avg"][j] - ref[j]) <= 1e-6 * abs(ref[j]), (j, r["dd_avg"], ref)
+        for k, row in enumerate(z["trace"]):
+            r = s.step()
+            assert abs(r["iterations"] - int(row[T_ITER])) <= 2, (k, r["iterations"], row[T_ITER])
+            assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-6, k
+            assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-6, k
+            ref = row[T_DD]
+            for j in range(7):
+                assert abs(r["dd_avg"][j] - ref[j]) <= 1e-6 * abs(ref[j]), (k, j, r["dd_avg"], ref)
