@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--precision", choices=["mixed", "fp64", "mixed_fast", "mixed_root64"], default="mixed")
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--iter-max", type=int, default=0, help="override IterMax (default: the workload's 100)")
+    ap.add_argument("--err", type=float, default=0.0, help="override Err (c4fd only; default: the workload's 1e-5)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -502,6 +503,61 @@ def adjoint_measure(dev_index, name="c4"):
             "kernels_during_gradient": classes, "gpu_launches_during_gradient": launches}
 
 
+def adjoint_fd_check(dev_index, err=None, iter_max=None):
+    """The calibration gradient of configs[4] (64^3, 256 grains, 50 steps)
+    against central finite differences with relative step 1e-4 of the FP64
+    forward, for all five parameters: the FP64 adjoint and the mixed one.
+    err / iter_max override the workload's Err 1e-5 / IterMax 100 (the
+    adjoint is that of the converged fixed point; the finite differences see
+    the forward as it stops)."""
+    import dataclasses
+    from mth import Solver, capi, synth
+    cfg = synth.workload("c4")
+    if err is not None:
+        cfg = dataclasses.replace(cfg, err=err)
+    if iter_max is not None:
+        cfg = dataclasses.replace(cfg, iter_max=iter_max)
+    micro = synth.microstructure(cfg)
+
+    def params(c, prec):
+        p = capi.params_from_config(c, precision=prec)
+        p.device = dev_index
+        return p
+
+    def forward(c, prec):
+        with Solver(params(c, prec), *micro) as s:
+            reps = [s.step() for _ in range(c.n_steps)]
+        return np.array([r["sig_avg"][2][2] for r in reps]), sum(r["iterations"] for r in reps)
+
+    t0 = time.perf_counter()
+    target, _ = forward(dataclasses.replace(cfg, material=synth.calibration_target_material()), capi.MTH_FP64)
+    base = cfg.material
+    out = {"workload": "64x64x64 RVE, 256 grains, tension, 50 steps of 1e-3, Err %g, IterMax %d" % (cfg.err, cfg.iter_max),
+           "params": list(capi.ADJOINT_PARAMS)}
+    grads = {}
+    for name, prec in (("fp64", capi.MTH_FP64), ("mixed", capi.MTH_MIXED)):
+        with Solver(params(cfg, prec), *micro) as s:
+            J, g, s33, info = s.adjoint(target, checkpoint_every=10)
+        grads[name] = np.asarray(g)
+        out["adjoint_" + name] = {"misfit": J, "grad": [float(x) for x in g]}
+    vals = synth.calibration_values(base)
+    fd, its = [], 0
+    for k in range(5):
+        h = 1e-4 * vals[k]
+        sp, ip = forward(dataclasses.replace(cfg, material=synth.perturb_material(base, k, h)), capi.MTH_FP64)
+        sm, im = forward(dataclasses.replace(cfg, material=synth.perturb_material(base, k, -h)), capi.MTH_FP64)
+        its += ip + im
+        fd.append((np.sum((sp - target) ** 2) - np.sum((sm - target) ** 2)) / (2 * h))
+    fd = np.array(fd)
+    out["central_fd_fp64"] = [float(x) for x in fd]
+    out["rel_err_fp64_adjoint_vs_fd"] = [float(abs(a - b) / abs(b)) for a, b in zip(grads["fp64"], fd)]
+    out["rel_err_mixed_adjoint_vs_fd"] = [float(abs(a - b) / abs(b)) for a, b in zip(grads["mixed"], fd)]
+    out["rel_err_mixed_vs_fp64_adjoint"] = [float(abs(a - b) / abs(b)) for a, b in zip(grads["mixed"], grads["fp64"])]
+    out["fd_green_iterations_per_forward"] = its / 10
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 # ------------------------------------------------------------ CPU (oracle)
 def cpu_sample(cfg, iterations=1):
     """Oracle (C port of the reference algorithm, OpenMP over all host cores)
@@ -650,6 +706,10 @@ def main():
     elif args.workload == "c4":
         # the calibration gradient alone (the adjoint block of the default line)
         print(json.dumps({"workload": "c4", "adjoint": adjoint_measure(0)}), flush=True)
+    elif args.workload == "c4fd":
+        # the calibration gradient against central finite differences (configs[4], all five parameters)
+        print(json.dumps({"workload": "c4fd", "adjoint_fd": adjoint_fd_check(0, err=args.err or None,
+                                                                          iter_max=args.iter_max or None)}), flush=True)
     elif args.workload == "c1dd":
         # the dislocation-density law alone (the dislocation_density block of the default line)
         print(json.dumps({"workload": "c1dd", "dislocation_density": dd_measure(0, args)}), flush=True)
