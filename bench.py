@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--iter-max", type=int, default=0, help="override IterMax (default: the workload's 100)")
     ap.add_argument("--err", type=float, default=0.0, help="override Err (c4fd only; default: the workload's 1e-5)")
+    ap.add_argument("--fd-steps", type=int, default=0, help="override the mechanical steps (c4fd only; default 50)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -191,7 +192,8 @@ def describe(cfg):
     wl = "%s RVE, %d grains%s, FCC Cu power law n=%g + Voce, %s, dt=%g, IterMax=%d" % (
         g, cfg.n_grains, pores, m.nrs, load, cfg.time_step, cfg.iter_max)
     if cfg.drx is not None:
-        wl += ", coupled DRX (%d PF substeps, K=8)" % cfg.drx.pf_substeps
+        from mth import capi
+        wl += ", coupled DRX (%d PF substeps, K=%d)" % (cfg.drx.pf_substeps, capi.PF_K)
     return data, wl
 
 
@@ -503,7 +505,7 @@ def adjoint_measure(dev_index, name="c4"):
             "kernels_during_gradient": classes, "gpu_launches_during_gradient": launches}
 
 
-def adjoint_fd_check(dev_index, err=None, iter_max=None):
+def adjoint_fd_check(dev_index, err=None, iter_max=None, n_steps=None):
     """The calibration gradient of configs[4] (64^3, 256 grains, 50 steps)
     against central finite differences with relative step 1e-4 of the FP64
     forward, for all five parameters: the FP64 adjoint and the mixed one.
@@ -517,6 +519,8 @@ def adjoint_fd_check(dev_index, err=None, iter_max=None):
         cfg = dataclasses.replace(cfg, err=err)
     if iter_max is not None:
         cfg = dataclasses.replace(cfg, iter_max=iter_max)
+    if n_steps is not None:
+        cfg = dataclasses.replace(cfg, n_steps=n_steps)
     micro = synth.microstructure(cfg)
 
     def params(c, prec):
@@ -532,7 +536,8 @@ def adjoint_fd_check(dev_index, err=None, iter_max=None):
     t0 = time.perf_counter()
     target, _ = forward(dataclasses.replace(cfg, material=synth.calibration_target_material()), capi.MTH_FP64)
     base = cfg.material
-    out = {"workload": "64x64x64 RVE, 256 grains, tension, 50 steps of 1e-3, Err %g, IterMax %d" % (cfg.err, cfg.iter_max),
+    out = {"workload": "64x64x64 RVE, 256 grains, tension, %d steps of 1e-3, Err %g, IterMax %d" % (
+               cfg.n_steps, cfg.err, cfg.iter_max),
            "params": list(capi.ADJOINT_PARAMS)}
     grads = {}
     for name, prec in (("fp64", capi.MTH_FP64), ("mixed", capi.MTH_MIXED)):
@@ -658,6 +663,9 @@ def run_batch(args):
     if ws > 1:
         torch.distributed.barrier()
     clk = cs.stop()
+    passes = {}
+    for i, c in enumerate(cfgs):
+        passes.setdefault("x".join(str(n) for n in c.cell_dim), b.passes(i))
     b.close()
     vox_it, dt, value = replicas.aggregate(float(vox_it), dt, device="cuda:%d" % dev_index)
     if rank != 0:
@@ -674,7 +682,8 @@ def run_batch(args):
                       "parallelism": ("members dealt over %d ranks by voxel count, one batch per rank, no "
                                       "data-path collective" % ws) if ws > 1 else "single GPU",
                       "timing": "host wall clock around whole batch steps (graph launches + host convergence "
-                                "logic), device synchronised on both sides"},
+                                "logic), device synchronised on both sides",
+                      "fft_passes": passes},
            "clocks": clk}
     if not args.no_fp64 and ws == 1:
         # one Solver per RVE, stepped one after the other: the unbatched baseline
@@ -708,8 +717,8 @@ def main():
         print(json.dumps({"workload": "c4", "adjoint": adjoint_measure(0)}), flush=True)
     elif args.workload == "c4fd":
         # the calibration gradient against central finite differences (configs[4], all five parameters)
-        print(json.dumps({"workload": "c4fd", "adjoint_fd": adjoint_fd_check(0, err=args.err or None,
-                                                                          iter_max=args.iter_max or None)}), flush=True)
+        print(json.dumps({"workload": "c4fd", "adjoint_fd": adjoint_fd_check(
+            0, err=args.err or None, iter_max=args.iter_max or None, n_steps=args.fd_steps or None)}), flush=True)
     elif args.workload == "c1dd":
         # the dislocation-density law alone (the dislocation_density block of the default line)
         print(json.dumps({"workload": "c1dd", "dislocation_density": dd_measure(0, args)}), flush=True)

@@ -308,6 +308,13 @@ mth_status mth_batch_upload(mth_batch* batch, int member, const int* grain, cons
 mth_status mth_batch_step(mth_batch* batch, mth_step_report* reports);
 mth_status mth_batch_download_field(mth_batch* batch, int member, int field, double* host, size_t n_values);
 mth_status mth_batch_destroy(mth_batch* batch);
+/* The FFT passes mth_batch_create chose for a member by timing Green
+ * iterations of a scratch volume of its grid and precision (once per grid and
+ * precision in the process): *tma 1 for the tensor-map (TMA) tile passes, 0
+ * for the shared-memory passes; *kz_strided and *kz_green the kz columns per
+ * tile block of the strided (y, x) and the Green passes (0 when *tma is 0).
+ * No reference counterpart. */
+mth_status mth_batch_passes(const mth_batch* batch, int member, int* tma, int* kz_strided, int* kz_green);
 
 /* Per-kernel device timing.  When enabled, every kernel launch of the context
  * is bracketed by CUDA events on the context's stream; times are summed per

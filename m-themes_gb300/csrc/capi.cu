@@ -260,6 +260,18 @@ bool mth::make_plan(int n, FftPlan* p) {
 
 // ---------------------------------------------------------------- context
 
+// (Re)builds the context's tensor maps with ks / kg kz columns per tile of the
+// strided / Green passes; 0 or a width the passes are not compiled for takes
+// the default.
+void ctx_set_tiles(mth_ctx* c, int ks, int kg) {
+  tma_destroy(c->tma);
+  const FftGeom& g = c->geom;
+  c->tma = c->mixed ? tma_create<float>(g, c->ff.sig, c->ff.strain, c->ff.wspin, static_cast<c2<float>*>(c->spec),
+                                        static_cast<c2<float>*>(c->anti), ks, kg)
+                    : tma_create<double>(g, c->fd.sig, c->fd.strain, c->fd.wspin, static_cast<c2<double>*>(c->spec),
+                                         static_cast<c2<double>*>(c->anti), ks, kg);
+}
+
 void ctx_free(mth_ctx* c) {
   if (!c) return;
   iout_free(c->iout);
@@ -652,10 +664,14 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     if (c->mixed) carve_dd(static_cast<float*>(c->dd_mem), c->ddf, c->ff);
     else carve_dd(static_cast<double*>(c->dd_mem), c->ddd, c->fd);
   }
-  c->tma = c->mixed ? tma_create<float>(g, c->ff.sig, c->ff.strain, c->ff.wspin, static_cast<c2<float>*>(c->spec),
-                                        static_cast<c2<float>*>(c->anti))
-                    : tma_create<double>(g, c->fd.sig, c->fd.strain, c->fd.wspin, static_cast<c2<double>*>(c->spec),
-                                         static_cast<c2<double>*>(c->anti));
+  {
+    // MTH_FFT_TILES="ks,kg" picks the TMA passes' tile widths (tests cover
+    // every compiled width); unset or unknown widths take the defaults
+    int ks = 0, kg = 0;
+    const char* tiles = getenv("MTH_FFT_TILES");
+    if (tiles && sscanf(tiles, "%d,%d", &ks, &kg) != 2) ks = kg = 0;
+    ctx_set_tiles(c, ks, kg);
+  }
   CKC(cudaMalloc(&c->crystal_d, P));
   c->etab_h = new std::vector<double>();
   c->drx_rot_h = new std::vector<double>();

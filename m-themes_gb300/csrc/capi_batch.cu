@@ -1,4 +1,5 @@
 // capi_batch.cu -- batches of independent RVEs (mth_batch_*).
+#include <algorithm>
 #include "capi_internal.h"
 
 // ------------------------------------------------------------ RVE batches
@@ -58,25 +59,35 @@ void batch_free(mth_batch* b) {
   delete b;
 }
 
-// FFT pass choice per (grid, precision): 1 TMA, 0 shared memory
-std::map<std::vector<int>, int>& tuned_passes() {
-  static std::map<std::vector<int>, int> m;
+// FFT pass choice per (grid, precision): TMA or shared-memory passes, and
+// the TMA passes' tile widths (kz columns per block of the strided and the
+// Green pass)
+struct PassChoice {
+  int tma, ks, kg;
+};
+std::map<std::vector<int>, PassChoice>& tuned_passes() {
+  static std::map<std::vector<int>, PassChoice> m;
   return m;
 }
 
-// Time `its` Green iterations of a scratch volume with the parameters of p
-// (single grain, no pores) with the TMA and the shared-memory passes.
-mth_status tune_passes(const mth_params& p, int* use_tma) {
+// Times Green iterations of a scratch volume with the parameters of p
+// (single grain, no pores; at least 3 iterations and about 2^21
+// voxel-iterations, at most 64 iterations) for each candidate: the
+// shared-memory passes, the strided pass's three compiled tile widths, then
+// the Green pass's three with the best strided width (the passes are
+// separate kernels, so their times add).  The best of two timed runs after a
+// warm-up run counts.
+mth_status tune_passes(const mth_params& p, PassChoice* out) {
   std::vector<int> key = {p.cell_dim[0], p.cell_dim[1], p.cell_dim[2], p.precision};
   auto it = tuned_passes().find(key);
-  if (it != tuned_passes().end()) { *use_tma = it->second; return MTH_OK; }
+  if (it != tuned_passes().end()) { *out = it->second; return MTH_OK; }
   mth_ctx* c = nullptr;
   mth_status s = mth_create(&p, &c);
   if (s) return s;
+  *out = {0, 0, 0};
   if (!tma_has(c->tma, 0) && !tma_has(c->tma, 1) && !tma_has(c->tma, 2)) {
     ctx_free(c);
-    tuned_passes()[key] = 0;
-    *use_tma = 0;
+    tuned_passes()[key] = *out;
     return MTH_OK;
   }
   const size_t nv = (size_t)c->nv;
@@ -88,30 +99,44 @@ mth_status tune_passes(const mth_params& p, int* use_tma) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  float ms[2] = {0, 0};
-  for (int variant = 0; variant < 2; variant++) {
-    c->tma_off = variant == 1;
-    for (int rep = 0; rep < 2; rep++) {   // first pass warms up
-      if (cudaEventRecord(e0, c->st) != cudaSuccess) break;
-      for (int k = 0; k < 3; k++) {
-        s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
-        if (s) break;
-      }
+  const int its = (int)std::min<long long>(64, std::max<long long>(3, (1LL << 21) / std::max<long long>(1, c->nv)));
+  auto time = [&](float* best) {
+    *best = 3.4e38f;
+    for (int rep = 0; rep < 3 && !s; rep++) {   // the first run warms up
+      if (cudaEventRecord(e0, c->st) != cudaSuccess) { s = set_err(MTH_ERR_CUDA, "pass tuning"); break; }
+      for (int k = 0; k < its && !s; k++) s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
       if (s) break;
       cudaEventRecord(e1, c->st);
       cudaStreamSynchronize(c->st);
-      cudaEventElapsedTime(&ms[variant], e0, e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep && ms < *best) *best = ms;
     }
-    if (s) break;
-  }
+  };
+  float t_smem = 0, t_best = 3.4e38f;
+  c->tma_off = true;
+  time(&t_smem);
+  c->tma_off = false;
+  int ks_def = 0, kg_def = 0;
+  tma_tiles(c->tma, &ks_def, &kg_def);
+  PassChoice best = {1, ks_def, kg_def};
+  for (int pass = 1; pass <= 2 && !s; pass++)
+    for (int i = 0; i < 3 && !s; i++) {
+      const int w = tma_tile_choice(c->mixed, pass, i);
+      PassChoice cand = pass == 1 ? PassChoice{1, w, kg_def} : PassChoice{1, best.ks, w};
+      ctx_set_tiles(c, cand.ks, cand.kg);
+      float t = 0;
+      time(&t);
+      if (!s && t < t_best) { t_best = t; best = cand; }
+    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (cudaStreamSynchronize(c->st) != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "pass tuning failed");
   if (!s && *c->err_h) s = set_err(MTH_ERR_TIMEOUT, "pass tuning timed out");
   ctx_free(c);
   if (s) return s;
-  *use_tma = ms[0] <= ms[1] ? 1 : 0;
-  tuned_passes()[key] = *use_tma;
+  *out = t_smem < t_best ? PassChoice{0, 0, 0} : best;
+  tuned_passes()[key] = *out;
   return MTH_OK;
 }
 
@@ -210,10 +235,11 @@ extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batc
   }
   for (int i = 0; i < n && !s; i++) {
     mth_ctx* c = b->rve[i];
-    int use_tma = 1;
-    s = tune_passes(params[i], &use_tma);
+    PassChoice pc;
+    s = tune_passes(params[i], &pc);
     if (s) break;
-    c->tma_off = !use_tma;
+    c->tma_off = !pc.tma;
+    if (pc.tma) ctx_set_tiles(c, pc.ks, pc.kg);
     ck(cudaStreamSynchronize(c->st));
     cudaStreamDestroy(c->st);
     cudaFree(c->red);
@@ -232,6 +258,15 @@ extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batc
     return s;
   }
   *out = b;
+  return MTH_OK;
+}
+
+extern "C" mth_status mth_batch_passes(const mth_batch* b, int i, int* tma, int* kz_strided, int* kz_green) {
+  if (!b || i < 0 || i >= b->n || !tma || !kz_strided || !kz_green) return set_err(MTH_ERR_ARG, "batch member %d", i);
+  const mth_ctx* c = b->rve[i];
+  *tma = c->tma_off ? 0 : (tma_has(c->tma, 0) || tma_has(c->tma, 1) || tma_has(c->tma, 2)) ? 1 : 0;
+  *kz_strided = *kz_green = 0;
+  if (*tma) tma_tiles(c->tma, kz_strided, kz_green);
   return MTH_OK;
 }
 

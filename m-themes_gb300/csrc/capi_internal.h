@@ -157,6 +157,7 @@ struct mth_ctx {
 struct IoutWriter;
 void iout_free(IoutWriter* w);
 void ctx_free(mth_ctx* c);
+void ctx_set_tiles(mth_ctx* c, int ks, int kg);   // tensor maps with these tile widths
 
 // ------------------------------------------------------------- profiling
 enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_DRX,

@@ -127,10 +127,15 @@ __device__ __forceinline__ bool block_wait_loads(uint64_t* bar, int* ok_s, int* 
 // (j/Ns)*Ns*R + k + r*Ns (Stockham autosort); inputs go through registers so
 // the stage is done in place.  Twiddles W_N^i = tw[i*TWM] (table of N*TWM
 // points, the sign of the transform).
-template <typename T, int N, int QN, int ES, int GS, int NG, int TWM, int SG, int NT, int S = 0, int NS = 1>
+// RMAX: the largest radix of a stage.  Measured at 128^3 (FP32, 200
+// launches of each pass): the y pass 11.0 / 9.9 / 9.0 ms and the x + Green
+// pass 12.2 / 11.8 / 11.1 ms with RMAX 4 / 8 / 16; the z passes 7.1 / 7.1 /
+// 8.1 ms (r2c) and 8.1 / 8.2 / 9.0 ms (c2r), where a 16-point stage leaves
+// half of the threads without a butterfly.
+template <typename T, int N, int QN, int ES, int GS, int NG, int TWM, int SG, int NT, int RMAX, int S = 0, int NS = 1>
 __device__ __forceinline__ void tile_fft(c2<T>* d, const c2<T>* __restrict__ tw) {
-  if constexpr (S < ct_nst(N)) {
-    constexpr int R = ct_radix(N, S);
+  if constexpr (S < tl_nst(N, RMAX)) {
+    constexpr int R = tl_radix(N, S, RMAX);
     constexpr int NB = N / R;
     constexpr int TWS = N / (NS * R);
     constexpr int TOTAL = NG * NB * QN;
@@ -168,11 +173,13 @@ __device__ __forceinline__ void tile_fft(c2<T>* d, const c2<T>* __restrict__ tw)
       }
     }
     __syncthreads();
-    tile_fft<T, N, QN, ES, GS, NG, TWM, SG, NT, S + 1, NS * R>(d, tw);
+    tile_fft<T, N, QN, ES, GS, NG, TWM, SG, NT, RMAX, S + 1, NS * R>(d, tw);
   }
 }
 
 constexpr int NT = 256;   // threads per block of every TMA pass
+constexpr int RMAX_Z = 8;     // largest radix: z passes
+constexpr int RMAX_S = 16;    // strided (y, x) and Green passes
 
 }  // namespace
 
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(NT) fft_zr_tma_kernel(const __grid_constant__ 
     tma_load3(A, &mreal, 0, line0, comp, &bar);
   }
   if (!block_wait_loads(&bar, &ok_s, err)) return;
-  tile_fft<T, M, 1, 1, M, LB, 2, -1, NT>(A, tw);
+  tile_fft<T, M, 1, 1, M, LB, 2, -1, NT, RMAX_Z>(A, tw);
   // split step: X_k = (Z_k + conj Z_{M-k})/2 - i W_N^k (Z_k - conj Z_{M-k})/2
   for (int idx = threadIdx.x; idx < LB * KZS; idx += NT) {
     const int l = idx / KZS, k = idx - l * KZS;
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(NT) fft_zc_tma_kernel(const __grid_constant__ 
     A[l * M + k] = mk<T>(e.x - o.y, e.y + o.x);   // e + i o
   }
   __syncthreads();
-  tile_fft<T, M, 1, 1, M, LB, 2, +1, NT>(A, tw);
+  tile_fft<T, M, 1, 1, M, LB, 2, +1, NT, RMAX_Z>(A, tw);
   const T ad = it.add ? (T)it.add[comp] : (T)0;
   for (int idx = threadIdx.x; idx < LB * N; idx += NT) {
     const int l = idx / N, z = idx - l * N;
@@ -298,7 +305,7 @@ __global__ void __launch_bounds__(NT) fft_s_tma_kernel(const __grid_constant__ C
     tma_load4(D, &m, x0, c1, c2i, comp, &bar);
   }
   if (!block_wait_loads(&bar, &ok_s, err)) return;
-  tile_fft<T, L, KB, KB, 0, 1, 1, SG, NT>(D, tw);
+  tile_fft<T, L, KB, KB, 0, 1, 1, SG, NT, RMAX_S>(D, tw);
   fence_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -311,8 +318,16 @@ __global__ void __launch_bounds__(NT) fft_s_tma_kernel(const __grid_constant__ C
 // Gamma0 : sigma-hat at every wave vector of the tile, antisymmetric part
 // added to the spin accumulator tile, inverse along x.  One block: fixed y,
 // KB consecutive kz.
+// resident blocks per SM the Green pass asks registers for: up to 4 in FP32,
+// no more than its shared-memory tile lets fit (228 KB per SM)
 template <typename T, int L, int KB>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) fft_xg_tma_kernel(const GreenConst gc, const __grid_constant__ CUtensorMap mspec,
+constexpr int xg_min_blocks() {
+  constexpr long fit = 228L * 1024 / (9L * L * KB * (long)sizeof(c2<T>) + 2048);
+  return sizeof(T) == 8 || fit < 1 ? 1 : fit > 4 ? 4 : (int)fit;
+}
+
+template <typename T, int L, int KB>
+__global__ void __launch_bounds__(NT, xg_min_blocks<T, L, KB>()) fft_xg_tma_kernel(const GreenConst gc, const __grid_constant__ CUtensorMap mspec,
                                                         const __grid_constant__ CUtensorMap manti, int n1, int n2,
                                                         int kz, const c2<T>* __restrict__ twf,
                                                         const c2<T>* __restrict__ twi, IterIn it, int* err) {
@@ -334,7 +349,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) fft_xg_tma_kernel(
     for (int c = 0; c < 3; c++) tma_load4(Aq + c * SLAB, &manti, x0, y, 0, c, &bar);
   }
   if (!block_wait_loads(&bar, &ok_s, err)) return;
-  tile_fft<T, L, KB, KB, SLAB, 6, 1, -1, NT>(D, twf);
+  tile_fft<T, L, KB, KB, SLAB, 6, 1, -1, NT, RMAX_S>(D, twf);
   for (int idx = threadIdx.x; idx < SLAB; idx += NT) {
     const int kk = idx % KB, kx = idx / KB;
     if (k0 + kk >= kz) continue;
@@ -348,7 +363,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 1) fft_xg_tma_kernel(
     for (int c = 0; c < 3; c++) Aq[c * SLAB + idx] = cadd<T>(Aq[c * SLAB + idx], a[c]);
   }
   __syncthreads();
-  tile_fft<T, L, KB, KB, SLAB, 6, 1, +1, NT>(D, twi);
+  tile_fft<T, L, KB, KB, SLAB, 6, 1, +1, NT, RMAX_S>(D, twi);
   fence_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -398,12 +413,26 @@ struct TmaMaps {
   CUtensorMap spec_y, anti_y, anti_x;              // strided passes
   CUtensorMap spec_g, anti_g;                      // Green x pass
   bool z, s, g;                                    // passes with maps
+  int ks, kg;                                      // kz columns per tile: strided passes, Green pass
 };
 
+// Tile widths (kz columns per block) the strided and Green passes are
+// compiled for; tma_create falls back to the default for any other value.
 template <typename T>
-TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti) {
+bool tile_ok_strided(int k) {
+  return sizeof(T) == 4 ? (k == 8 || k == 16 || k == 32) : (k == 2 || k == 4 || k == 8);
+}
+template <typename T>
+bool tile_ok_green(int k) {
+  return sizeof(T) == 4 ? (k == 2 || k == 4 || k == 8) : (k == 1 || k == 2 || k == 4);
+}
+
+template <typename T>
+TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti, int ks, int kg) {
   TmaMaps* t = new TmaMaps();
   memset(t, 0, sizeof(*t));
+  t->ks = tile_ok_strided<T>(ks) ? ks : kb_strided<T>();
+  t->kg = tile_ok_green<T>(kg) ? kg : kb_green<T>();
   if (!ct_size(g.n0) || !ct_size(g.n1) || !ct_size(g.n2) || !encode_fn()) return t;
   const CUtensorMapDataType rt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
   const CUtensorMapDataType wt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;   // spectra in 8-byte words
@@ -429,7 +458,7 @@ TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, 
     cuuint64_t k6[4] = {(cuuint64_t)g.kzs * C, (cuuint64_t)g.n1, (cuuint64_t)g.n0, 6};
     cuuint64_t k3[4] = {(cuuint64_t)g.kzs * C, (cuuint64_t)g.n1, (cuuint64_t)g.n0, 3};
     cuuint64_t st[3] = {(cuuint64_t)g.kzs * cb, (cuuint64_t)g.n1 * g.kzs * cb, (cuuint64_t)g.kplane * cb};
-    const cuuint32_t ks = (cuuint32_t)(kb_strided<T>() * C), kg = (cuuint32_t)(kb_green<T>() * C);
+    const cuuint32_t ks = (cuuint32_t)(t->ks * C), kg = (cuuint32_t)(t->kg * C);
     cuuint32_t by[4] = {ks, (cuuint32_t)g.n1, 1, 1}, bxs[4] = {ks, 1, (cuuint32_t)g.n0, 1};
     cuuint32_t bg[4] = {kg, 1, (cuuint32_t)g.n0, 1};
     bool s_ok = encode(&t->spec_y, wt, 4, spec, k6, st, by) && encode(&t->anti_y, wt, 4, anti, k3, st, by) &&
@@ -445,6 +474,14 @@ cudaError_t tma_set_wait_probe(int on) { return cudaMemcpyToSymbol(g_tile_wait_p
 
 void tma_destroy(TmaMaps* t) { delete t; }
 bool tma_has(const TmaMaps* t, int pass) { return t && (pass == 0 ? t->z : pass == 1 ? t->s : t->g); }
+int tma_tile_choice(bool fp32, int pass, int i) {
+  static const int w[2][2][3] = {{{2, 4, 8}, {1, 2, 4}}, {{8, 16, 32}, {2, 4, 8}}};
+  return w[fp32 ? 1 : 0][pass == 1 ? 0 : 1][i];
+}
+void tma_tiles(const TmaMaps* t, int* ks, int* kg) {
+  *ks = t ? t->ks : 0;
+  *kg = t ? t->kg : 0;
+}
 
 static size_t zr_smem(int n, int lb, size_t cb) {
   const int M = n / 2, KZS = (M + 2) & ~1;
@@ -485,10 +522,9 @@ static cudaError_t zc_launch(const CUtensorMap& ms, const CUtensorMap& mr, int n
   return cudaGetLastError();
 }
 
-template <typename T, int L>
+template <typename T, int L, int KB>
 static cudaError_t s_launch(const CUtensorMap& m, int axis, int ncomp, int nouter, int kzs, int sign,
                             const c2<T>* tw, const IterIn& it, int* err, cudaStream_t st) {
-  constexpr int KB = kb_strided<T>();
   const size_t sm = (size_t)L * KB * sizeof(c2<T>);
   dim3 grid((kzs + KB - 1) / KB, nouter, ncomp);
   if (sign < 0) {
@@ -503,16 +539,36 @@ static cudaError_t s_launch(const CUtensorMap& m, int axis, int ncomp, int noute
   return cudaGetLastError();
 }
 
-template <typename T, int L>
+template <typename T, int L, int KB>
 static cudaError_t g_launch(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
                             const c2<T>* twi, const IterIn& it, int* err, cudaStream_t st) {
-  constexpr int KB = kb_green<T>();
   const size_t sm = (size_t)9 * L * KB * sizeof(c2<T>);
   auto k = fft_xg_tma_kernel<T, L, KB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kzs + KB - 1) / KB, g.n1);
   k<<<grid, NT, sm, st>>>(gc, t->spec_g, t->anti_g, g.n1, g.n2, g.kz, twf, twi, it, err);
   return cudaGetLastError();
+}
+
+// the compiled tile widths: FP32 strided 8/16/32, Green 2/4/8; FP64 strided
+// 2/4/8, Green 1/2/4 (index 0/1/2 of each list)
+template <typename T, int L>
+static cudaError_t s_dispatch(const TmaMaps* t, const CUtensorMap& m, int axis, int ncomp, int nouter, int kzs, int sign,
+                              const c2<T>* tw, const IterIn& it, int* err, cudaStream_t st) {
+  constexpr int A = sizeof(T) == 4 ? 8 : 2;
+  if (t->ks == A) return s_launch<T, L, A>(m, axis, ncomp, nouter, kzs, sign, tw, it, err, st);
+  if (t->ks == 2 * A) return s_launch<T, L, 2 * A>(m, axis, ncomp, nouter, kzs, sign, tw, it, err, st);
+  if (t->ks == 4 * A) return s_launch<T, L, 4 * A>(m, axis, ncomp, nouter, kzs, sign, tw, it, err, st);
+  return cudaErrorInvalidValue;
+}
+template <typename T, int L>
+static cudaError_t g_dispatch(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
+                              const c2<T>* twi, const IterIn& it, int* err, cudaStream_t st) {
+  constexpr int A = sizeof(T) == 4 ? 2 : 1;
+  if (t->kg == A) return g_launch<T, L, A>(t, g, gc, twf, twi, it, err, st);
+  if (t->kg == 2 * A) return g_launch<T, L, 2 * A>(t, g, gc, twf, twi, it, err, st);
+  if (t->kg == 4 * A) return g_launch<T, L, 4 * A>(t, g, gc, twf, twi, it, err, st);
+  return cudaErrorInvalidValue;
 }
 
 #define MTH_TMA_SIZES(X) X(16) X(32) X(48) X(64) X(96) X(128) X(256)
@@ -556,7 +612,7 @@ cudaError_t tma_fft_strided(const TmaMaps* t, const FftGeom& g, int which, int s
   const int L = axis == 1 ? g.n1 : g.n0, nouter = axis == 1 ? g.n0 : g.n1;
   const int ncomp = which == 0 ? 6 : 3;
   switch (L) {
-#define MTH_CASE(N) case N: return s_launch<T, N>(m, axis, ncomp, nouter, g.kzs, sign, tw, it, err, st);
+#define MTH_CASE(N) case N: return s_dispatch<T, N>(t, m, axis, ncomp, nouter, g.kzs, sign, tw, it, err, st);
     MTH_TMA_SIZES(MTH_CASE)
 #undef MTH_CASE
     default: return cudaErrorInvalidValue;
@@ -567,7 +623,7 @@ template <typename T>
 cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst& gc, const c2<T>* twf,
                             const c2<T>* twi, const IterIn& it, int* err, cudaStream_t st) {
   switch (g.n0) {
-#define MTH_CASE(N) case N: return g_launch<T, N>(t, g, gc, twf, twi, it, err, st);
+#define MTH_CASE(N) case N: return g_dispatch<T, N>(t, g, gc, twf, twi, it, err, st);
     MTH_TMA_SIZES(MTH_CASE)
 #undef MTH_CASE
     default: return cudaErrorInvalidValue;
@@ -575,7 +631,7 @@ cudaError_t tma_fft_x_green(const TmaMaps* t, const FftGeom& g, const GreenConst
 }
 
 #define INST(T)                                                                                                    \
-  template TmaMaps* tma_create<T>(const FftGeom&, T*, T*, T*, c2<T>*, c2<T>*);                                     \
+  template TmaMaps* tma_create<T>(const FftGeom&, T*, T*, T*, c2<T>*, c2<T>*, int, int);                       \
   template cudaError_t tma_fft_z_r2c<T>(const TmaMaps*, const FftGeom&, const c2<T>*, const IterIn&, int*,        \
                                         cudaStream_t);                                                             \
   template cudaError_t tma_fft_z_c2r<T>(const TmaMaps*, const FftGeom&, int, const c2<T>*, T, const IterIn&, int*, \

@@ -73,12 +73,15 @@ bool make_plan(int n, FftPlan* p);
 // 2 (x + Green) has them.  err: device flag raised by a timed-out wait.
 struct TmaMaps;
 template <typename T>
-TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti);
+TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, c2<T>* anti, int ks = 0,
+                    int kg = 0);   // ks, kg: kz columns per tile of the strided / Green passes (0: default)
 void tma_destroy(TmaMaps* t);
 // failure-path test hook of the tile passes: 1 makes each block's first
 // tile wait report a time-out (the copies are still drained); device-wide
 cudaError_t tma_set_wait_probe(int on);
 bool tma_has(const TmaMaps* t, int pass);
+void tma_tiles(const TmaMaps* t, int* ks, int* kg);   // the tile widths in use
+int tma_tile_choice(bool fp32, int pass, int i);      // compiled width i (0..2) of pass 1 (strided) / 2 (Green)
 template <typename T>
 cudaError_t tma_fft_z_r2c(const TmaMaps* t, const FftGeom& g, const c2<T>* tw, const IterIn& it, int* err,
                           cudaStream_t st);

@@ -232,6 +232,7 @@ __device__ __forceinline__ void symv5(const T* K, const T* x, T* y) {
 // takes the relative error from 2^-22 to below 2^-64, so the result is
 // within an ulp or two of 1/d without the special-case handling of a
 // correctly rounded divide.
+template <bool QUAD = false>
 __device__ __forceinline__ double pivot_rcp_nr(double d) {
   const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
   const int E = (int)((hi >> 20) & 0x7ffu);   // biased exponent of d (1..2046)
@@ -246,11 +247,15 @@ __device__ __forceinline__ double pivot_rcp_nr(double d) {
   if (eo <= 0) xhi = xlo = 0u;                // 1/d below the normal range
   const double x = __hiloint2double((int)xhi, (int)xlo);
   const double e = fma(-d, x, 1.0);
+  if constexpr (QUAD) return fma(x, e, x);   // quadratic step: within 2^-43 of 1/d
   return fma(x, fma(e, e, e), x);
 }
-template <typename T, bool NR>
+// QUAD: the quadratic step, for solves whose result is rounded to FP32 (a
+// pivot reciprocal off by 2^-43 is a backward error of that size in D,
+// far below the FP32 rounding of the assembled Hessian and of the step)
+template <typename T, bool NR, bool QUAD = false>
 __device__ __forceinline__ T pivot_inv(T d) {
-  if constexpr (NR && sizeof(T) == 8) return pivot_rcp_nr(d);
+  if constexpr (NR && sizeof(T) == 8) return pivot_rcp_nr<QUAD>(d);
   else return (T)1 / d;
 }
 
@@ -268,7 +273,7 @@ __device__ __forceinline__ bool pivot_positive(T d) {
 // LDL^T solve of the packed symmetric positive definite 5x5 matrix A:
 // x = A^-1 b.  Returns false when a pivot is not positive.  NR: pivot
 // reciprocals by pivot_rcp_nr (FP64 solves of the mixed modes).
-template <typename T, bool NR = false>
+template <typename T, bool NR = false, bool QUAD = false>
 __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
   // U[i][k] = L[i][k] d[k], the column before its scaling by 1/d[k], kept so
   // the updates need no products L d
@@ -280,7 +285,7 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
     for (int k = 0; k < 5; k++)
       if (k < j) dj -= U[j][k] * L[j][k];
     if (!pivot_positive<T, NR>(dj)) return false;
-    id[j] = pivot_inv<T, NR>(dj);
+    id[j] = pivot_inv<T, NR, QUAD>(dj);
 #pragma unroll
     for (int i = 0; i < 5; i++)
       if (i > j) {
@@ -312,6 +317,9 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
   return true;
 }
 
+#ifndef MTH_PIVOT_QUAD
+#define MTH_PIVOT_QUAD false   // quadratic pivot-reciprocal step in the FP64 solves of FP32 systems
+#endif
 // LDL^T solve of a TF system in precision TL.  FP32 -> FP64 (and back):
 // the conversions by integer operations (f32_to_f64, f64_to_f32), as GB300
 // executes F2F conversions on its 1/64-rate FP64 pipe.
@@ -323,7 +331,7 @@ __device__ __forceinline__ bool ldl_solve5_wide(const TF* H, const TF* b, TF* x)
     for (int i = 0; i < 15; i++) Hl[i] = f32_to_f64(H[i]);
 #pragma unroll
     for (int i = 0; i < 5; i++) bl[i] = f32_to_f64(b[i]);
-    const bool ok = ldl_solve5<TL, true>(Hl, bl, pl);
+    const bool ok = ldl_solve5<TL, true, MTH_PIVOT_QUAD>(Hl, bl, pl);
 #pragma unroll
     for (int i = 0; i < 5; i++) x[i] = f64_to_f32(pl[i]);
     return ok;

@@ -242,6 +242,7 @@ def load(path: str | None = None):
     lib.mth_batch_step.argtypes = [C.c_void_p, C.POINTER(MthStepReport)]
     lib.mth_batch_download_field.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_size_t]
     lib.mth_batch_destroy.argtypes = [C.c_void_p]
+    lib.mth_batch_passes.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.mth_adjoint.argtypes = [C.c_void_p, C.POINTER(MthAdjointOpts), C.POINTER(C.c_double),
                                 C.POINTER(MthAdjointResult)]
     if path is None:

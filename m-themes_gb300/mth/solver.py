@@ -136,6 +136,13 @@ class Batch:
         capi.check(self.lib, self.lib.mth_batch_step(self.b, reps))
         return [r.to_dict() for r in reps]
 
+    def passes(self, i: int) -> dict:
+        """The FFT passes chosen for member i: {"tma": 0/1, "kz_strided": w,
+        "kz_green": w} (tile widths in kz columns; 0 without TMA)."""
+        t, ks, kg = C.c_int(), C.c_int(), C.c_int()
+        capi.check(self.lib, self.lib.mth_batch_passes(self.b, i, C.byref(t), C.byref(ks), C.byref(kg)))
+        return {"tma": t.value, "kz_strided": ks.value, "kz_green": kg.value}
+
     def field(self, i: int, name: str) -> np.ndarray:
         f = capi.FIELD[name]
         out = np.zeros(self.nv[i] * capi.FIELD_NCOMP[f])

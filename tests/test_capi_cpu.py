@@ -117,6 +117,8 @@ def test_batch_argument_checks(lib):
     assert lib.mth_batch_step(None, None) == 1
     assert lib.mth_batch_destroy(None) == 1
     assert lib.mth_batch_upload(None, 0, None, None, None, 0) == 1
+    t = C.c_int()
+    assert lib.mth_batch_passes(None, 0, C.byref(t), C.byref(t), C.byref(t)) == 1
 
 
 def test_iout_argument_checks(lib):

@@ -22,7 +22,7 @@ def _cfg(mat, precision, steps=4, **kw):
     if precision == capi.MTH_FP64:
         base.update(err=1e-10, iter_max=2500)   # converged far below the finite-difference step
     else:
-        base.update(err=1e-6, iter_max=400)
+        base.update(err=1e-7, iter_max=1000)
     base.update(kw)
     return synth.Config(**base)
 
@@ -69,15 +69,18 @@ def test_adjoint_matches_central_differences(fp64_case):
 
 
 def test_mixed_adjoint_matches_fp64(fp64_case):
-    """The mixed forward stops at Err = 1e-6 with FP32 fields, so its curve
-    (and the misfit built from it) differs from the FP64 one by ~1e-4
-    relative per point; the gradient follows within a few 1e-3."""
+    """The mixed forward stops at Err = 1e-7 with FP32 fields: its curve
+    differs from the FP64 one by 2.2e-5 of the peak stress, the misfit by
+    3.5e-4 and the gradient entries by at most 5.3e-4 relative (tau1 2.5e-4,
+    nrs 5.3e-4).  Stopping at Err = 1e-6 instead leaves 8e-5 on the curve
+    and up to 2.2e-3 on the nrs entry: the forward's stopping error, not the
+    adjoint, sets the floor."""
     base, tgt, J64, g64, s64, _ = fp64_case
     J, g, s33, info = _adjoint(_cfg(base, capi.MTH_MIXED), capi.MTH_MIXED, tgt)
-    assert np.abs(s33 - s64).max() <= 2e-4 * np.abs(s64).max()
-    assert abs(J - J64) <= 5e-3 * J64
+    assert np.abs(s33 - s64).max() <= 5e-5 * np.abs(s64).max()
+    assert abs(J - J64) <= 1e-3 * J64
     for k in range(5):
-        assert abs(g[k] - g64[k]) <= 2e-2 * abs(g64[k]), (capi.ADJOINT_PARAMS[k], g.tolist(), g64.tolist())
+        assert abs(g[k] - g64[k]) <= 1e-3 * abs(g64[k]), (capi.ADJOINT_PARAMS[k], g.tolist(), g64.tolist())
 
 
 def test_checkpoint_spacing_does_not_change_the_gradient():

@@ -1,7 +1,10 @@
 """Batched RVEs (mth_batch_*) against one Solver per member: uneven grid
 sizes, per-member material and precision, members converging at different
-Green iterations."""
+Green iterations; the FFT tile widths the batch tunes per grid, each checked
+against the default widths."""
 from __future__ import annotations
+
+import os
 
 import numpy as np
 import pytest
@@ -41,6 +44,12 @@ def test_batch_matches_single_solvers(precision, tol):
     with Batch(params, micro) as b:
         reps = [b.step() for _ in range(3)]
         sig = [b.field(i, "sig") for i in range(len(cfgs))]
+        chosen = [b.passes(i) for i in range(len(cfgs))]
+    wide = {capi.MTH_FP64: ((2, 4, 8), (1, 2, 4)), capi.MTH_MIXED: ((8, 16, 32), (2, 4, 8))}[precision]
+    for c in chosen:
+        assert c["tma"] in (0, 1)
+        if c["tma"]:
+            assert c["kz_strided"] in wide[0] and c["kz_green"] in wide[1], c
     its = set()
     for i in range(len(cfgs)):
         for k in range(3):
@@ -96,3 +105,35 @@ def test_batch_members_match_the_oracle():
             assert rel(reps[k][i]["disgrad_avg"], orep[k]["disgrad_avg"]) < 1e-6, (i, k)
         assert rel(sig[i], o.field("sig")) < 1e-5
         o.close()
+
+
+@pytest.mark.parametrize("precision", [capi.MTH_FP64, capi.MTH_MIXED])
+def test_every_tile_width_gives_the_default_result(precision):
+    """Each compiled tile width of the strided and the Green TMA passes (kz
+    columns per block; the batch picks among them by timing) against the
+    default widths, on a 32x48x64 grid whose 34 kz columns leave a partial
+    last tile for every width above 2."""
+    cfg = synth.Config(cell_dim=(32, 48, 64), n_grains=7, n_steps=2, seed=311, iter_max=6)
+    par = capi.params_from_config(cfg, precision=precision)
+    micro = synth.microstructure(cfg)
+
+    def run(tiles):
+        if tiles:
+            os.environ["MTH_FFT_TILES"] = tiles
+        try:
+            with Solver(par, *micro) as s:
+                reps = [s.step() for _ in range(2)]
+                return reps, s.field("sig")
+        finally:
+            os.environ.pop("MTH_FFT_TILES", None)
+
+    ref, sig0 = run(None)
+    tol = 1e-12 if precision == capi.MTH_FP64 else 1e-5
+    ks_list, kg_list = {capi.MTH_FP64: ((2, 4, 8), (1, 2, 4)), capi.MTH_MIXED: ((8, 16, 32), (2, 4, 8))}[precision]
+    for ks in ks_list:
+        for kg in kg_list:
+            reps, sig = run(f"{ks},{kg}")
+            for a, r in zip(reps, ref):
+                assert a["iterations"] == r["iterations"], (ks, kg)
+                assert rel(a["sig_avg"], r["sig_avg"]) < tol, (ks, kg)
+            assert rel(sig, sig0) < 10 * tol, (ks, kg)
