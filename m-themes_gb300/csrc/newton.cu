@@ -317,12 +317,12 @@ __device__ __forceinline__ bool ldl_solve5(const T* A, const T* b, T* x) {
   return true;
 }
 
-#ifndef MTH_PIVOT_QUAD
-#define MTH_PIVOT_QUAD false   // quadratic pivot-reciprocal step in the FP64 solves of FP32 systems
-#endif
 // LDL^T solve of a TF system in precision TL.  FP32 -> FP64 (and back):
 // the conversions by integer operations (f32_to_f64, f64_to_f32), as GB300
-// executes F2F conversions on its 1/64-rate FP64 pipe.
+// executes F2F conversions on its 1/64-rate FP64 pipe; the pivot
+// reciprocals with the quadratic step (the FP64 solve of an FP32 system is
+// rounded to FP32; 5 DFMA fewer per solve, the 400 Newton launches of the
+// 128^3 benchmark 2.3 % faster).
 template <typename TF, typename TL>
 __device__ __forceinline__ bool ldl_solve5_wide(const TF* H, const TF* b, TF* x) {
   TL Hl[15], bl[5], pl[5];
@@ -331,7 +331,7 @@ __device__ __forceinline__ bool ldl_solve5_wide(const TF* H, const TF* b, TF* x)
     for (int i = 0; i < 15; i++) Hl[i] = f32_to_f64(H[i]);
 #pragma unroll
     for (int i = 0; i < 5; i++) bl[i] = f32_to_f64(b[i]);
-    const bool ok = ldl_solve5<TL, true, MTH_PIVOT_QUAD>(Hl, bl, pl);
+    const bool ok = ldl_solve5<TL, true, true>(Hl, bl, pl);
 #pragma unroll
     for (int i = 0; i < 5; i++) x[i] = f64_to_f32(pl[i]);
     return ok;
