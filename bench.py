@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration measurement")
     ap.add_argument("--no-dd", action="store_true", help="skip the dislocation-density law measurement")
     ap.add_argument("--no-drx", action="store_true", help="skip the coupled recrystallisation measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-RVE batch measurement")
     return ap.parse_args()
 
 
@@ -376,6 +377,8 @@ def run_gpu(args):
         out["dislocation_density"] = dd_measure(dev_index, args)
     if not args.no_drx and args.workload == "c1":
         out["drx"] = drx_measure(dev_index, args)
+    if not args.no_batch and args.workload == "c1" and ws == 1:
+        out["batch"] = batch_measure(dev_index)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -617,6 +620,46 @@ def run_reference(args):
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def batch_measure(dev_index, steps=2, warmup=3):
+    """The 64-RVE batch (the c3 workload) on this GPU, mixed precision:
+    whole-batch voxel-iterations/s over `steps` mechanical steps after
+    `warmup`, the tile widths the batch chose per grid, and one Solver per
+    RVE stepped in turn on the same steps."""
+    import torch
+    from mth import Batch, Solver, capi, synth
+    cfgs = synth.batch_workload("c3")
+    params = [capi.params_from_config(c, precision=capi.MTH_MIXED) for c in cfgs]
+    for p in params:
+        p.device = dev_index
+    micro = [synth.microstructure(c) for c in cfgs]
+    nvs = [int(np.prod(c.cell_dim)) for c in cfgs]
+
+    def timed(step_all):
+        for _ in range(warmup):
+            step_all()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vi = sum(step_all() for _ in range(steps))
+        torch.cuda.synchronize()
+        return vi / (time.perf_counter() - t0)
+
+    with Batch(params, micro) as b:
+        batched = timed(lambda: sum(n * r["iterations"] for n, r in zip(nvs, b.step())))
+        passes = {}
+        for i, c in enumerate(cfgs):
+            passes.setdefault("x".join(str(n) for n in c.cell_dim), b.passes(i))
+    sols = [Solver(p, *m) for p, m in zip(params, micro)]
+    try:
+        single = timed(lambda: sum(n * s.step()["iterations"] for n, s in zip(nvs, sols)))
+    finally:
+        for s in sols:
+            s.close()
+    return {"workload": "64 RVEs (24x32^3, 24x48^3, 16x64^3), per-RVE seed, grains ~U[32,256], tau0 ~U[12,20] "
+                        "MPa, n in {8,10,15,20}, tension, dt=1e-3, mixed",
+            "value": batched, "unit": UNIT, "steps": steps, "warmup": warmup, "fft_passes": passes,
+            "one_solver_per_rve": single, "batched_over_one_solver_per_rve": batched / single}
 
 
 def run_batch(args):

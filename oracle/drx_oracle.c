@@ -137,7 +137,7 @@ void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, 
  *    during the sweep, on the grid being read;
  *  - the sweep runs x, y, z over the interior; a voxel holding more than one
  *    entry when the sweep reaches it is updated, one holding a single entry
- *    copies its values of the ids in N(v) (src/pf_xrx.c:1276-1283); N(v) =
+ *    copies its values of the ids in N(v) (src/pf_xrx.c:1235-1240); N(v) =
  *    ids with eta > EPSILON over the 3x3x3 block in scan order
  *    (src/pf_xrx.c:937-973);
  *  - stored-energy averages over the 7x7x7 window use the grain map of the
@@ -145,7 +145,7 @@ void orc_paint_nuclei(const int* n, int* grain, const long long* sites, int nn, 
  *    src/pf_xrx.c:683-893) and the energy buffer, summed in window order per
  *    held entry (src/pf_xrx.c:1052-1086) and written to the caller's rho_avg
  *    table, from which ids not held at v read what earlier voxels left
- *    (src/pf_xrx.c:1089-1095,1184-1233);
+ *    (written at src/pf_xrx.c:1079-1086, read at :1202-1214);
  *  - a recrystallised id (> init_gid) that passes 0.5 at a voxel sets that
  *    voxel's stored energy to 100 for the rest of the call (src/pf_xrx.c:
  *    1217-1219); the Laplacian adds its twelve edge terms in the order its
