@@ -22,6 +22,7 @@
 // for cubic crystals (edot_p has no trace, src/constitutive.c:50) and is
 // solved in closed form.  Convergence: |step| <= tol |lambda|, as the
 // reference's erral (src/evolution.c:264-270).
+#include <type_traits>
 #include <cstdio>
 #include <cmath>
 #include <atomic>
@@ -178,6 +179,20 @@ struct DdSlip {
   __device__ __forceinline__ void flow(const PhaseConst& ph, const TF x[5], TF ed[5], TF D[15], TF& psi,
                                        TF* gam) const {
     flow_rule_dd<TF, WANT_D>(ph, x, tp, td, g0, ed, D, psi, gam);
+  }
+};
+// The power law's state with the CRSS in shared memory (the cooperative
+// kernel, whose registers bound how many blocks share an SM): tauf points
+// at this thread's NSYS values, rows of NSYS + 1 so that a warp's threads
+// read distinct banks.
+template <typename TF>
+struct PlSlipSh {
+  const TF* tauf;
+  TF tau_off;
+  template <bool WANT_D>
+  __device__ __forceinline__ void flow(const PhaseConst& ph, const TF x[5], TF ed[5], TF D[15], TF& psi,
+                                       TF* gam) const {
+    flow_rule<TF, WANT_D>(ph, x, tauf, tau_off, ed, D, psi, gam);
   }
 };
 // slip-law state of voxel v from the fields (LAW 0: power law, 1: dislocation density)
@@ -754,11 +769,22 @@ __device__ __forceinline__ void block_reduce_smem(const TV (&v)[W], double* out)
 // 8..13) are the total ones (2..7), added once and written twice; the
 // Newton-iteration and failure counts (14, 15: small integers) are summed in
 // the staging precision, exact below 2^24.
+constexpr int NRED_LD = 256 + 16;   // row stride of the staged values
+template <typename TV>
+__device__ __forceinline__ void newton_block_reduce_in(const TV (&v)[NPART], double* out, bool ph1_only,
+                                                       TV (*sv)[NRED_LD], double (*sp)[16]);
 template <typename TV>
 __device__ __forceinline__ void newton_block_reduce(const TV (&v)[NPART], double* out, bool ph1_only) {
-  constexpr int NT = 256, LD = NT + 16;
-  __shared__ TV sv[NPART][LD];
+  __shared__ TV sv[NPART][NRED_LD];
   __shared__ double sp[NPART][16];
+  newton_block_reduce_in<TV>(v, out, ph1_only, sv, sp);
+}
+// the same with the staging buffers given (the cooperative kernel lays them
+// over its system buffers, free once its pass loop has ended)
+template <typename TV>
+__device__ __forceinline__ void newton_block_reduce_in(const TV (&v)[NPART], double* out, bool ph1_only,
+                                                       TV (*sv)[NRED_LD], double (*sp)[16]) {
+  constexpr int NT = 256;
   const int t = threadIdx.x;
 #pragma unroll
   for (int i = 0; i < NPART; i++)
@@ -866,13 +892,20 @@ __global__ void __launch_bounds__(256, MINB) newton_kernel(const NewtonConst nc,
 // memory, in thread order, the first n threads of the block solve the n
 // systems in FP64, and each thread reads its direction back.  Every voxel's
 // iterates and result are those of solve_voxel.
+#ifndef MTH_COOP_TAU_SMEM
+#define MTH_COOP_TAU_SMEM 1   // power-law CRSS of the cooperative kernel in shared memory
+#endif
 template <typename TSt, typename TF, typename TL, int MINB, int LAW = 0>
 __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonConst nc, Fields<TSt> f,
                                                                 double* __restrict__ partials, IterIn it) {
   if (!is_live(it)) return;
-  __shared__ TF sH[15][256];
-  __shared__ TF sB[5][256];    // -g in, the direction out
-  extern __shared__ __align__(16) unsigned char coop_dyn[];   // K [15][256] and c [5][256] of each thread's solve
+  // the systems of a pass (H, -g in / direction out), and after the pass
+  // loop the block sums' staging buffers, in one static buffer
+  constexpr size_t SYS_B = sizeof(TF) * 20 * 256, RED_B = sizeof(TF) * NPART * NRED_LD + sizeof(double) * NPART * 16;
+  __shared__ __align__(16) unsigned char sbuf[SYS_B > RED_B ? SYS_B : RED_B];
+  TF(*sH)[256] = reinterpret_cast<TF(*)[256]>(sbuf);
+  TF(*sB)[256] = reinterpret_cast<TF(*)[256]>(sbuf + sizeof(TF) * 15 * 256);
+  extern __shared__ __align__(16) unsigned char coop_dyn[];   // K [15][256], c [5][256], CRSS [256][NSYS + 1]
   __shared__ int sOk[256];
   __shared__ int sWarp[8];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -884,7 +917,9 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
   int jph = 0;
   bool active = false;
   const TF* et = nullptr;
-  typename SlipOf<LAW, TF, TSt>::type slip;
+  // power law: the CRSS in shared memory, after K and c
+  using SlipT = std::conditional_t<LAW == 0 && MTH_COOP_TAU_SMEM, PlSlipSh<TF>, typename SlipOf<LAW, TF, TSt>::type>;
+  SlipT slip;
   NewtonState<TF> s;
   const NewtonShared<TF> sh{reinterpret_cast<TF(*)[256]>(coop_dyn),
                             reinterpret_cast<TF(*)[256]>(coop_dyn + 15 * 256 * sizeof(TF)), t};
@@ -902,7 +937,15 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
     jph = f.phase[v];
     const PhaseConst& ph = nc.ph[jph];
     if (ph.type == 0) {
-      SlipOf<LAW, TF, TSt>::load(ph, f, v, slip);
+      if constexpr (LAW == 0 && MTH_COOP_TAU_SMEM) {
+        TF* tau = reinterpret_cast<TF*>(coop_dyn + 20 * 256 * sizeof(TF)) + t * (NSYS + 1);
+#pragma unroll
+        for (int q = 0; q < NSYS; q++) tau[q] = q < ph.nsys ? (TF)f.crss[q * P + v] : (TF)1;
+        slip.tauf = tau;
+        slip.tau_off = cpick<TF>(ph.tau_back_minus_fwd, ph.tau_offf);
+      } else {
+        SlipOf<LAW, TF, TSt>::load(ph, f, v, slip);
+      }
       et = cpick_ptr<TF>(f.etab, f.etabf) + (size_t)f.eclass[v] * ETAB_W;
       nw_init(s, sh, nc, et, load);
       active = true;
@@ -979,12 +1022,13 @@ __global__ void __launch_bounds__(256, MINB) newton_coop_kernel(const NewtonCons
     acc[14] = (TF)o.iters;
     acc[15] = (TF)o.failed;
   }
-  newton_block_reduce<TF>(acc, partials, nc.ph1_only != 0);
+  newton_block_reduce_in<TF>(acc, partials, nc.ph1_only != 0, reinterpret_cast<TF(*)[NRED_LD]>(sbuf),
+                             reinterpret_cast<double(*)[16]>(sbuf + sizeof(TF) * NPART * NRED_LD));
 }
 
-// newton_coop_kernel for the FP32 fields with the FP64 solve, with its 20 KB
-// of dynamic shared memory (K and c of each thread's solve)
-constexpr size_t COOP_DYN = 20 * 256 * sizeof(float);
+// newton_coop_kernel for the FP32 fields with the FP64 solve, with its 33 KB
+// of dynamic shared memory (K and c of each thread's solve, its CRSS)
+constexpr size_t COOP_DYN = (20 + (MTH_COOP_TAU_SMEM ? NSYS + 1 : 0)) * 256 * sizeof(float);
 
 // the opt-in above 48 KB of shared memory per block, once per device (also
 // done by prepare_newton_kernels when a context is created, so that no
@@ -1011,7 +1055,16 @@ static cudaError_t launch_coop(const NewtonConst& nc, const Fields<float>& f, do
   return cudaGetLastError();
 }
 
-cudaError_t prepare_newton_kernels() { return coop_attr<3, 0>(); }
+// blocks per SM the cooperative kernel is compiled for: 4 (64 registers,
+// 54.5 KB of shared memory per block with the block sums' buffers laid over
+// the system buffers and the CRSS in shared memory) against 3 (80
+// registers): 301.2 against 319.7 ms for the 300 Newton launches of three
+// 128^3 steps (307.2 ms with the CRSS in registers; 5 blocks at 48
+// registers, 352.8 ms)
+#ifndef MTH_COOP_MINB
+#define MTH_COOP_MINB 4
+#endif
+cudaError_t prepare_newton_kernels() { return coop_attr<MTH_COOP_MINB, 0>(); }
 
 void fill_float_consts(NewtonConst& nc) {
   for (int k = 0; k < 2; k++) {
@@ -1062,7 +1115,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     newton_kernel<float, float, double, 3, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    return launch_coop<3, 0>(nc, f, partials, nblocks, it, st);
+    return launch_coop<MTH_COOP_MINB, 0>(nc, f, partials, nblocks, it, st);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
     newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
