@@ -1091,6 +1091,18 @@ void fill_float_consts(NewtonConst& nc) {
   nc.tolf = (float)nc.tol;
 }
 
+// blocks per SM of the one-solve-per-thread kernels: the
+// dislocation-density law in the mixed modes, and the FP32-solve and
+// near-root FP64 modes of the power law.  Measured at 128^3: the
+// dislocation-density law 2.31e9 voxel-iterations/s with 2 blocks against
+// 2.09e9 (3) and 2.12e9 (4); FP32 solves 2.55e9 with 3 against 2.52e9 (4);
+// near-root FP64 solves the same with 3 and 4
+#ifndef MTH_DD_MINB
+#define MTH_DD_MINB 2
+#endif
+#ifndef MTH_FAST_MINB
+#define MTH_FAST_MINB 3
+#endif
 cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* fields, double* partials, int nblocks,
                           const IterIn& it, cudaStream_t st, int law) {
   NewtonConst nc = nc_in;
@@ -1100,7 +1112,7 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     // mixed modes (no FP32-solve variants)
     if (mixed) {
       const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-      newton_kernel<float, float, double, 2, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+      newton_kernel<float, float, double, MTH_DD_MINB, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
     } else {
       const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
       newton_kernel<double, double, double, 1, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
@@ -1109,10 +1121,10 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
   }
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, float, 3><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    newton_kernel<float, float, float, MTH_FAST_MINB><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed == 3) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double, 3, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    newton_kernel<float, float, double, MTH_FAST_MINB, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     return launch_coop<MTH_COOP_MINB, 0>(nc, f, partials, nblocks, it, st);
