@@ -23,10 +23,10 @@ LIB = os.path.join(HERE, "lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + os.path.join(REPO, "include")]
-CU_SOURCES = ["fft_green.cu", "fft_tma.cu", "newton.cu", "drx.cu", "dd.cu", "adjoint.cu", "capi.cu", "capi_iout.cu",
+CU_SOURCES = ["fft_green.cu", "fft_tma.cu", "newton.cu", "drx.cu", "dd.cu", "adjoint.cu", "book.cu", "capi.cu", "capi_iout.cu",
               "capi_arrays.cu", "capi_batch.cu", "capi_adjoint.cu"]
 # sources compiled without FMA contraction (bit-exact FP64 restatement)
-NO_FMAD = {"drx.cu"}
+NO_FMAD = {"drx.cu", "book.cu"}
 # sources whose host code is compiled without FMA contraction: the FP64 host
 # bookkeeping gives the same doubles on x86 and Arm (gcc contracts by default
 # on aarch64), and host-side tensor conversions match the device's rounded,

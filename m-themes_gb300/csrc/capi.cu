@@ -8,6 +8,7 @@
 // updates (src/evolution.c:1471-1535,1691-1693) run on the host in FP64 on
 // the reduced sums that the kernels produce; everything per voxel or per
 // wave vector runs on the GPU.
+#include <algorithm>
 #include "capi_internal.h"
 
 static thread_local char g_err[512] = "";
@@ -294,6 +295,8 @@ void ctx_free(mth_ctx* c) {
   cudaFree(c->etabf_d);
   cudaFree(c->partials);
   if (c->red_h) cudaFreeHost(c->red_h);
+  cudaFree(c->bk_d);
+  if (c->book_h) cudaFreeHost(c->book_h);
   for (int a = 0; a < 3; a++)
     for (int d = 0; d < 2; d++) cudaFree(c->tw[a][d]);
   if (c->st && !c->in_batch) cudaStreamDestroy(c->st);
@@ -332,7 +335,7 @@ void ctx_free(mth_ctx* c) {
 // ------------------------------------------------------------- profiling
 static const char* k_names[K_NCLASS] = {"fft_z_r2c", "fft_y", "fft_x_green", "fft_z_c2r_strain", "newton",
                                         "reduce", "end_step", "spin_fft", "setup", "drx",
-                                        "pf_relax", "adj_local", "adj_cg", "dislocation_density"};
+                                        "pf_relax", "adj_local", "adj_cg", "dislocation_density", "iter_book"};
 const char* prof_class_name(int cls) { return cls >= 0 && cls < K_NCLASS ? k_names[cls] : "?"; }
 
 void prof_begin(mth_ctx* c) {
@@ -613,6 +616,9 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
   CKC(cudaMalloc(&c->partials, sizeof(double) * 21 * c->nblocks));
   CKC(cudaMalloc(&c->red, sizeof(double) * 32));
   CKC(cudaMallocHost(&c->red_h, sizeof(double) * 32));
+  CKC(cudaMalloc(&c->bk_d, sizeof(IterBook)));
+  CKC(cudaMallocHost(&c->book_h, sizeof(int) * 4));
+  c->book_h[3] = 1;   // source of the live flag's reset
   CKC(cudaMalloc(&c->err_d, sizeof(int)));
   CKC(cudaMemset(c->err_d, 0, sizeof(int)));
   CKC(cudaMallocHost(&c->err_h, sizeof(int)));
@@ -663,6 +669,12 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     };
     if (c->mixed) carve_dd(static_cast<float*>(c->dd_mem), c->ddf, c->ff);
     else carve_dd(static_cast<double*>(c->dd_mem), c->ddd, c->fd);
+  }
+  // MTH_HOST_BOOK=1: mth_step keeps the per-iteration bookkeeping on the
+  // host (tests compare it with the device's, bit for bit)
+  {
+    const char* hb = getenv("MTH_HOST_BOOK");
+    c->host_book = hb && hb[0] == '1';
   }
   {
     // MTH_FFT_TILES="ks,kg" picks the TMA passes' tile widths (tests cover
@@ -917,53 +929,6 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   return MTH_OK;
 }
 
-// get_smacro (src/evolution.c:473-547) on the reduced sums.  The von Mises
-// stress keeps the reference's formula, whose out-of-bounds word
-// SigDevAvg[3][3] (src/evolution.c:531) holds SigAvg1[0][0] in the reference
-// as built with g++ (SigAvg1 is laid out right after SigDevAvg's padding).
-static void get_smacro(mth_ctx* c, const double* red) {
-  static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
-  double s6[6], s16[6];
-  for (int i = 0; i < 6; i++) {
-    s6[i] = red[2 + i] * c->wgt;
-    s16[i] = red[8 + i] * (c->wgt / c->wgt_ph1);
-  }
-  v2t(s6, c->sig_avg, 6);
-  v2t(s16, c->sig_avg1, 6);
-  for (int a = 0; a < 6; a++) {
-    int ii = IJV[0][a], jj = IJV[1][a];
-    c->ddg[ii][jj] = 0.0;
-    if (c->vbc[a] == 0)
-      for (int b = 0; b < 6; b++) {
-        int kk = IJV[0][b], ll = IJV[1][b];
-        c->ddg[ii][jj] += c->s0_4[((ii * 3 + jj) * 3 + kk) * 3 + ll] * c->sbc[b] * (c->scauchy[kk][ll] - c->sig_avg[kk][ll]);
-      }
-  }
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) c->ddg_acum[i][j] += c->ddg[i][j];
-  t33 dev;
-  double v6[6];
-  t2v(c->sig_avg, v6, 6);
-  v2t(v6, dev, 5);
-  const double oob = c->sig_avg1[0][0];
-  double svm = 0;
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) {
-      if (i != j) svm += dev[i][j] * dev[i][j];
-      else {
-        double d = dev[i][j] - (dev[1][1] + dev[2][2] + oob) / 3.0;
-        svm += d * d;
-      }
-    }
-  c->s_vm = sqrt(3. / 2. * svm);
-  t2v(c->sig_avg1, v6, 6);
-  v2t(v6, dev, 5);
-  double svm1 = 0;
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) svm1 += dev[i][j] * dev[i][j];
-  c->s_vm1 = sqrt(3. / 2. * svm1);
-}
-
 template <typename T>
 mth_status green_iteration(mth_ctx* c) {
   const IterIn it = iter_in(c);
@@ -1213,50 +1178,43 @@ mth_status step_begin(mth_ctx* c) {
     const double w = c->mixed ? 4.0 : 8.0;
     LAUNCH(K_DD, (double)c->nv * w * (4 * NSYS + 3 * NSYS), launch_dd_prep(c->mixed, *c->ddc, dd, f, c->st));
   }
-  memset(c->ddg, 0, sizeof(c->ddg));
-  memset(c->ddg_acum, 0, sizeof(c->ddg_acum));
-  memset(c->ddg_applied, 0, sizeof(c->ddg_applied));
+  // the step's bookkeeping: constants, then the state of a step's start
+  IterBook& b = c->bk;
+  memcpy(b.udot, c->udot, sizeof(t33));
+  memcpy(b.scauchy, c->scauchy, sizeof(t33));
+  memcpy(b.s0_4, c->s0_4, sizeof(b.s0_4));
+  memcpy(b.vbc, c->vbc, sizeof(b.vbc));
+  memcpy(b.sbc, c->sbc, sizeof(b.sbc));
+  b.wgt = c->wgt;
+  b.wgt_ph1 = c->wgt_ph1;
+  b.dt = c->p.time_step;
+  b.err = c->p.err;
+  b.e_vm = c->e_vm;
+  b.iter_max = c->p.iter_max;
+  b.nan = 0;
+  memset(b.ddg, 0, sizeof(b.ddg));
+  memset(b.ddg_acum, 0, sizeof(b.ddg_acum));
+  memset(b.ddg_applied, 0, sizeof(b.ddg_applied));
   const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
   CK(cudaMemsetAsync(c->anti, 0, 2 * esz * c->geom.kplane * 3, c->st));
-  c->it_iter = 0;
-  c->it_nit = 0;
-  c->it_nbad = 0;
-  c->err_e = 2. * c->p.err;
-  c->err_s = 2. * c->p.err;
+  c->bk.it_iter = 0;
+  c->bk.it_nit = 0;
+  c->bk.it_nbad = 0;
+  c->bk.err_e = 2. * c->p.err;
+  c->bk.err_s = 2. * c->p.err;
   return MTH_OK;
 }
 
-bool iter_more(const mth_ctx* c) {
-  return c->it_iter < c->p.iter_max && fmax(fabs(c->err_s), fabs(c->err_e)) > c->p.err;
-}
+bool iter_more(const mth_ctx* c) { return book_more(c->bk); }
 
 // uniform strain added this iteration: dDisGradAvg of the previous
 // get_smacro, plus Udot dt on the first one (src/evolution.c:1319-1332)
-void iter_add(mth_ctx* c) {
-  c->it_iter++;
-  const double dt = c->p.time_step;
-  t33 u;
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) {
-      u[i][j] = c->ddg[i][j] + (c->it_iter == 1 ? c->udot[i][j] * dt : 0.0);
-      c->ddg_applied[i][j] += c->ddg[i][j];
-    }
-  t2v(u, c->add_h, 6);
-}
+void iter_add(mth_ctx* c) { book_add(c->bk, c->add_h); }
 
 mth_status iter_finish(mth_ctx* c, const double* red) {
-  for (int i = 0; i < NPART; i++)
-    if (!std::isfinite(red[i]))
-      return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", c->istep,
-                     c->it_iter);
-  c->it_nit += (long long)red[14];
-  c->it_nbad += (long long)red[15];
-  c->err_s = red[0] * c->wgt;
-  c->err_e = red[1] * c->wgt;
-  get_smacro(c, red);
-  if (fabs(c->e_vm) < 1E-5) c->err_e = 0.0;
-  else c->err_e /= c->e_vm;
-  c->err_s /= c->s_vm;
+  if (!book_finish(c->bk, red, NPART))
+    return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", c->istep,
+                   c->bk.it_iter);
   return MTH_OK;
 }
 
@@ -1267,7 +1225,7 @@ mth_status step_end(mth_ctx* c, mth_step_report* rep) {
   t33 actual, vg;
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) {
-      actual[i][j] = c->disgrad_avg[i][j] + c->ddg_acum[i][j];
+      actual[i][j] = c->disgrad_avg[i][j] + c->bk.ddg_acum[i][j];
       vg[i][j] = (actual[i][j] - c->disgrad_avg_t[i][j]) / dt;
     }
   c->e_vm = von_mises(actual);
@@ -1289,7 +1247,7 @@ mth_status step_end(mth_ctx* c, mth_step_report* rep) {
     t33 a;
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++)
-        a[i][j] = 2.0 * c->udot_a[i][j] * dt + 0.5 * (c->ddg_applied[i][j] - c->ddg_applied[j][i]);
+        a[i][j] = 2.0 * c->udot_a[i][j] * dt + 0.5 * (c->bk.ddg_applied[i][j] - c->bk.ddg_applied[j][i]);
     au[0] = a[2][1];
     au[1] = a[0][2];
     au[2] = a[1][0];
@@ -1334,18 +1292,18 @@ mth_status step_end(mth_ctx* c, mth_step_report* rep) {
   if (rep) {
     memset(rep, 0, sizeof(*rep));
     rep->step = istep;
-    rep->iterations = c->it_iter;
+    rep->iterations = c->bk.it_iter;
     rep->time = c->time_tot;
-    memcpy(rep->sig_avg, c->sig_avg, sizeof(t33));
-    memcpy(rep->sig_avg_ph1, c->sig_avg1, sizeof(t33));
+    memcpy(rep->sig_avg, c->bk.sig_avg, sizeof(t33));
+    memcpy(rep->sig_avg_ph1, c->bk.sig_avg1, sizeof(t33));
     memcpy(rep->disgrad_avg, actual, sizeof(t33));
     memcpy(rep->eps_avg, ea, sizeof(t33));
     memcpy(rep->edot_avg, da, sizeof(t33));
     rep->e_vm = c->e_vm; rep->evmp = evmp; rep->d_vm = c->d_vm; rep->dvmp = dvmp;
-    rep->s_vm = c->s_vm; rep->s_vm1 = c->s_vm1;
-    rep->err_s = c->err_s; rep->err_e = c->err_e;
-    rep->newton_iters = c->it_nit;
-    rep->newton_failed = c->it_nbad;
+    rep->s_vm = c->bk.s_vm; rep->s_vm1 = c->bk.s_vm1;
+    rep->err_s = c->bk.err_s; rep->err_e = c->bk.err_e;
+    rep->newton_iters = c->bk.it_nit;
+    rep->newton_failed = c->bk.it_nbad;
     rep->n_new_grains = c->it_nnew;
     if (c->dd) memcpy(rep->dd_avg, c->dd_avg, sizeof(c->dd_avg));
   }
@@ -1362,17 +1320,57 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
   SETDEV(c);
   mth_status s = step_begin(c);
   if (s) return s;
-  while (iter_more(c)) {
-    iter_add(c);
-    CK(cudaMemcpyAsync(c->add_d, c->add_h, sizeof(double) * 6, cudaMemcpyHostToDevice, c->st));
-    s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
-    if (s) return s;
-    double red[NPART];
-    s = reduce_to_host(c, NPART, red);
-    if (s) return s;
-    s = iter_finish(c, red);
-    if (s) return s;
+  // The iterations run with their bookkeeping on the device (book.cu): each
+  // iteration's kernels, its reduction and the one-thread bookkeeping
+  // kernel, which computes the next iteration's strain increment or drops
+  // the live flag; the host queues groups of iterations and reads the flag
+  // once per group, so the iterations follow one another without a host
+  // round trip.  Iterations queued after the last one return at once.
+  IterBook& b = c->bk;
+  if (c->host_book) {
+    // the same bookkeeping on the host after every iteration (test hook)
+    while (iter_more(c)) {
+      iter_add(c);
+      CK(cudaMemcpyAsync(c->add_d, c->add_h, sizeof(double) * 6, cudaMemcpyHostToDevice, c->st));
+      s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+      if (s) return s;
+      double red[NPART];
+      s = reduce_to_host(c, NPART, red);
+      if (s) return s;
+      s = iter_finish(c, red);
+      if (s) return s;
+    }
+    return step_end(c, rep);
   }
+  CK(cudaMemcpyAsync(c->bk_d, &b, sizeof(IterBook), cudaMemcpyHostToDevice, c->st));
+  LAUNCH(K_BOOK, 0, launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 1, c->st));
+  int queued = 0, group = 2;
+  for (;;) {
+    const int n = std::min(group, b.iter_max - queued);
+    for (int k = 0; k < n; k++) {
+      s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+      if (s) return s;
+      s = launch_reduce(c, NPART, true);
+      if (s) return s;
+      LAUNCH(K_BOOK, 0, launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 0, c->st));
+    }
+    queued += n;
+    CK(cudaMemcpyAsync(&c->book_h[0], c->live_d, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&c->book_h[1], &c->bk_d->nan, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&c->book_h[2], &c->bk_d->it_iter, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(c->err_h, c->err_d, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    prof_resolve(c);
+    if (*c->err_h) return set_err(MTH_ERR_TIMEOUT, "a kernel timed out waiting for its tile copies");
+    if (c->book_h[1])
+      return set_err(MTH_ERR_NAN, "non-finite value in the Green iteration (step %d, iteration %d)", c->istep,
+                     c->book_h[2]);
+    if (!c->book_h[0] || queued >= b.iter_max) break;
+    group = std::min(2 * group, 16);
+  }
+  CK(cudaMemcpyAsync(&b, c->bk_d, sizeof(IterBook), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->live_d, &c->book_h[3], sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return step_end(c, rep);
 }
 

@@ -72,10 +72,10 @@ static mth_status adj_save(mth_ctx* c, AdjRun& run, int slot) {
   HostCkpt& h = run.hck[slot];
   memcpy(h.disgrad_avg, c->disgrad_avg, sizeof(t33));
   memcpy(h.disgrad_avg_t, c->disgrad_avg_t, sizeof(t33));
-  memcpy(h.sig_avg, c->sig_avg, sizeof(t33));
-  memcpy(h.sig_avg1, c->sig_avg1, sizeof(t33));
-  h.e_vm = c->e_vm; h.d_vm = c->d_vm; h.s_vm = c->s_vm; h.s_vm1 = c->s_vm1;
-  h.err_e = c->err_e; h.err_s = c->err_s; h.time_tot = c->time_tot; h.istep = c->istep;
+  memcpy(h.sig_avg, c->bk.sig_avg, sizeof(t33));
+  memcpy(h.sig_avg1, c->bk.sig_avg1, sizeof(t33));
+  h.e_vm = c->e_vm; h.d_vm = c->d_vm; h.s_vm = c->bk.s_vm; h.s_vm1 = c->bk.s_vm1;
+  h.err_e = c->bk.err_e; h.err_s = c->bk.err_s; h.time_tot = c->time_tot; h.istep = c->istep;
   return MTH_OK;
 }
 
@@ -93,10 +93,10 @@ static mth_status adj_restore(mth_ctx* c, AdjRun& run, int slot) {
   const HostCkpt& h = run.hck[slot];
   memcpy(c->disgrad_avg, h.disgrad_avg, sizeof(t33));
   memcpy(c->disgrad_avg_t, h.disgrad_avg_t, sizeof(t33));
-  memcpy(c->sig_avg, h.sig_avg, sizeof(t33));
-  memcpy(c->sig_avg1, h.sig_avg1, sizeof(t33));
-  c->e_vm = h.e_vm; c->d_vm = h.d_vm; c->s_vm = h.s_vm; c->s_vm1 = h.s_vm1;
-  c->err_e = h.err_e; c->err_s = h.err_s; c->time_tot = h.time_tot; c->istep = h.istep;
+  memcpy(c->bk.sig_avg, h.sig_avg, sizeof(t33));
+  memcpy(c->bk.sig_avg1, h.sig_avg1, sizeof(t33));
+  c->e_vm = h.e_vm; c->d_vm = h.d_vm; c->bk.s_vm = h.s_vm; c->bk.s_vm1 = h.s_vm1;
+  c->bk.err_e = h.err_e; c->bk.err_s = h.err_s; c->time_tot = h.time_tot; c->istep = h.istep;
   return MTH_OK;
 }
 

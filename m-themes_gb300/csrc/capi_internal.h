@@ -17,6 +17,7 @@
 #include "../../include/mth.h"
 #include "mth_common.cuh"
 #include "mth_internal.h"
+#include "book.cuh"
 #include "adjoint.h"
 
 using namespace mth;
@@ -83,8 +84,7 @@ struct mth_ctx {
   double* dl_d;       // download staging in the host layout
   size_t dl_cap;      // doubles
   // state of the mechanical step in progress (mth_step and the batch driver)
-  int it_iter, it_nnew;
-  long long it_nit, it_nbad;
+  int it_nnew;
   uint8_t* phase_d;
   int* grain_d;
   int* eclass_d;
@@ -105,9 +105,13 @@ struct mth_ctx {
   // macro state (FP64, host)
   t33 udot, udot_s, udot_a, scauchy;
   int vbc[6], sbc[6], creep;
-  t33 disgrad_avg, disgrad_avg_t, ddg, ddg_acum, ddg_applied, sig_avg, sig_avg1;
+  t33 disgrad_avg, disgrad_avg_t;
   double c066[6][6], s066[6][6], s0_4[81];
-  double wgt, wgt_ph1, e_vm, d_vm, s_vm, s_vm1, err_e, err_s, time_tot;
+  double wgt, wgt_ph1, e_vm, d_vm, time_tot;
+  IterBook bk;        // the step's per-iteration bookkeeping (host copy)
+  IterBook* bk_d;     // its device copy (mth_step's device-side bookkeeping)
+  int* book_h;        // pinned: live flag, iteration, non-finite flag read after a group of iterations
+  bool host_book;     // bookkeeping on the host after every iteration instead (test hook)
   int istep;
   int uploaded;
   // dynamic recrystallisation
@@ -161,7 +165,7 @@ void ctx_set_tiles(mth_ctx* c, int ks, int kg);   // tensor maps with these tile
 
 // ------------------------------------------------------------- profiling
 enum { K_FFT_Z_R2C = 0, K_FFT_Y, K_FFT_X_GREEN, K_FFT_Z_C2R, K_NEWTON, K_REDUCE, K_END_STEP, K_SPIN, K_SETUP, K_DRX,
-       K_PF, K_ADJ_LOCAL, K_ADJ_CG, K_DD, K_NCLASS };
+       K_PF, K_ADJ_LOCAL, K_ADJ_CG, K_DD, K_BOOK, K_NCLASS };
 void prof_begin(mth_ctx* c);
 void prof_end(mth_ctx* c, int cls, int kernels, double bytes);
 void prof_resolve(mth_ctx* c);   // after the stream has been synchronised

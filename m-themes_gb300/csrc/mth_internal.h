@@ -302,4 +302,8 @@ cudaError_t launch_to_host_layout(int mixed, const void* src, long long P, int n
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
                                    cudaStream_t st);
 
+// the per-iteration bookkeeping on the device (book.cu, book.cuh)
+struct IterBook;
+cudaError_t launch_iter_book(IterBook* b, const double* red, double* add, int* live, int first, cudaStream_t st);
+
 }  // namespace mth
