@@ -37,6 +37,24 @@ struct Dims {
   }
 };
 
+// The periodic 3x3x3 neighbourhood of voxel (x, y, z) without divisions:
+// the wrapped coordinates of the three planes, rows and columns once, a
+// neighbour's index by multiply-adds.
+struct Nbhd {
+  long long px[3];   // plane offsets of x-1, x, x+1 (times n1 n2)
+  int py[3], pz[3];  // row offsets of y-1, y, y+1 (times n2); columns z-1, z, z+1
+  __device__ __forceinline__ Nbhd(const Dims& d, int x, int y, int z) {
+    const int xm = x == 0 ? d.n0 - 1 : x - 1, xp = x == d.n0 - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? d.n1 - 1 : y - 1, yp = y == d.n1 - 1 ? 0 : y + 1;
+    const long long pl = (long long)d.n1 * d.n2;
+    px[0] = xm * pl; px[1] = x * pl; px[2] = xp * pl;
+    py[0] = ym * d.n2; py[1] = y * d.n2; py[2] = yp * d.n2;
+    pz[0] = z == 0 ? d.n2 - 1 : z - 1; pz[1] = z; pz[2] = z == d.n2 - 1 ? 0 : z + 1;
+  }
+  // neighbour at offset (a, b, c), each in -1..1
+  __device__ __forceinline__ long long at(int a, int b, int c) const { return px[a + 1] + py[b + 1] + pz[c + 1]; }
+};
+
 // -------------------------------------------------------------- nucleation
 // Candidate: grain-boundary voxel as the reference marks it
 // (src/evolution.c:816-829 from Gradient_ExchangeGrainID,
@@ -215,10 +233,11 @@ __global__ void __launch_bounds__(256) pf_nlist_kernel(PfView g, const int* __re
   int L[PF_NM];
   int n = 0;
   unsigned bad = 0;
+  const Nbhd nb(g.d, x, y, z);
   for (int dx = -1; dx <= 1; dx++)
     for (int dy = -1; dy <= 1; dy++)
       for (int dz = -1; dz <= 1; dz++) {
-        const long long w = g.d.idx(x + dx, y + dy, z + dz);
+        const long long w = nb.at(dx, dy, dz);
         const int c = cnt[w];
         for (int k = 0; k < c; k++) {
           if (!(phi[(long long)k * g.nv + w] > (T)PF_EPS)) continue;
@@ -235,29 +254,62 @@ __global__ void __launch_bounds__(256) pf_nlist_kernel(PfView g, const int* __re
   if (bad) atomicOr(&word[1], bad);
 }
 
+// One pass of the update flags' fixed point, in place.  The flags only turn
+// on as the passes proceed (a flag is an OR over earlier voxels' flags), so
+// reading some neighbours' flags of this pass and some of the last one still
+// ends at the same fixed point, and a pass that changes nothing is at it.
+// Within a warp (consecutive z of one row) the chain through the (0,0,-1)
+// neighbour is resolved in the pass itself: u(z) = G(z) | (P(z) & u(z-1)),
+// G the voxel's own and its other eight neighbours' part, P whether the
+// z-1 neighbour's flag would carry over, solved for the warp's 32 lanes by
+// a prefix over ballot masks.
 template <typename T>
 __global__ void __launch_bounds__(256) pf_upd_kernel(PfView g, const int* __restrict__ ids, const T* __restrict__ phi,
                                                      const uint8_t* __restrict__ cnt, const int* __restrict__ nid,
-                                                     const uint8_t* __restrict__ ncnt, const uint8_t* __restrict__ upd_in,
-                                                     uint8_t* __restrict__ upd_out, unsigned* __restrict__ word) {
+                                                     const uint8_t* __restrict__ ncnt, uint8_t* __restrict__ upd,
+                                                     unsigned* __restrict__ word) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= g.nv) return;
-  const int c = cnt[v];
-  bool u = c > 1;
-  if (c == 1 && phi[v] >= (T)PF_EPS) {
-    const int X = ids[v];
-    const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
-    for (int o = 0; o < 9 && !u; o++) {
-      const int qx = x + c_pred[o][0], qy = y + c_pred[o][1], qz = z + c_pred[o][2];
-      if (qx < 0 || qy < 0 || qy >= g.d.n1 || qz < 0 || qz >= g.d.n2) continue;
-      const long long q = ((long long)qx * g.d.n1 + qy) * g.d.n2 + qz;
-      if (!upd_in[q]) continue;
-      const int nq = ncnt[q];
-      u = nq >= 2 || (nq == 1 && nid[q] != X);
+  const bool in = v < g.nv;
+  const int lane = threadIdx.x & 31;
+  bool gen = false, prop = false, zin = false;
+  uint8_t old = 0;
+  if (in) {
+    old = upd[v];
+    const int c = cnt[v];
+    gen = c > 1;
+    if (c == 1 && phi[v] >= (T)PF_EPS) {
+      const int X = ids[v];
+      const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+      for (int o = 0; o < 9; o++) {
+        const int qx = x + c_pred[o][0], qy = y + c_pred[o][1], qz = z + c_pred[o][2];
+        if (qx < 0 || qy < 0 || qy >= g.d.n1 || qz < 0 || qz >= g.d.n2) continue;
+        const long long q = ((long long)qx * g.d.n1 + qy) * g.d.n2 + qz;
+        const int nq = ncnt[q];
+        const bool carries = nq >= 2 || (nq == 1 && nid[q] != X);
+        if (o == 0) {   // (0,0,-1): the previous voxel of the row
+          prop = carries;
+          zin = upd[q] != 0;
+        } else if (carries && upd[q]) {
+          gen = true;
+        }
+      }
     }
   }
-  upd_out[v] = (uint8_t)u;
-  if ((uint8_t)u != upd_in[v]) atomicAdd(&word[0], 1u);
+  // u = G | (P & u(z-1)) over the warp; lane 0 takes u(z-1) from the buffer
+  const unsigned am = __activemask();
+  unsigned gm = __ballot_sync(am, gen || (lane == 0 && prop && zin)), pm = __ballot_sync(am, prop);
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    gm |= pm & (gm << s);
+    pm &= pm << s;
+  }
+  if (in) {
+    const uint8_t u = (uint8_t)((gm >> lane) & 1u);
+    if (u != old) {
+      upd[v] = u;
+      atomicAdd(&word[0], 1u);
+    }
+  }
 }
 
 template <typename T>
@@ -508,6 +560,7 @@ __global__ void __launch_bounds__(128) pf_update_kernel(PfView g, const int* __r
   const int nn = ncnt[v];
   if (n > 1) {
     const int x = (int)(v / ((long long)g.d.n1 * g.d.n2)), y = (int)((v / g.d.n2) % g.d.n1), z = (int)(v % g.d.n2);
+    const Nbhd nbh(g.d, x, y, z);
     T sum_rex = 0, sum1 = 0, hdef = 0;
     for (int k = 0; k < n; k++) {
       const T a = wavg[(long long)k * nv + v];
@@ -523,7 +576,7 @@ __global__ void __launch_bounds__(128) pf_update_kernel(PfView g, const int* __r
       const T c = pf_read_local<T>(hid, hph, n, j);
       const T h = c * c * c * ((T)10.0 - (T)15.0 * c + (T)6.0 * c * c);
       const T dh = c * c * ((T)30.0 - (T)60.0 * c + (T)30.0 * c * c);
-#define NB(a_, b_, c_) pf_read_g<T>(ids, phi, cnt, nv, g.d.idx(x + (a_), y + (b_), z + (c_)), j)
+#define NB(a_, b_, c_) pf_read_g<T>(ids, phi, cnt, nv, nbh.at(a_, b_, c_), j)
       const T right = NB(1, 0, 0), left = NB(-1, 0, 0), front = NB(0, 1, 0), back = NB(0, -1, 0);
       const T up = NB(0, 0, 1), down = NB(0, 0, -1);
       const T lu = NB(-1, 0, 1), ld = NB(-1, 0, -1), lf = NB(-1, -1, 0), lb = NB(-1, 1, 0);
@@ -796,14 +849,12 @@ cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, i
     const T* phi = b.phi[cur];
     const uint8_t* cnt = b.cnt[cur];
     PF_K_LAUNCH(pf_nlist_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.word));
-    // update flags to their fixed point
+    // update flags to their fixed point (in place)
     PF_CK(cudaMemsetAsync(b.upd[0], 0, (size_t)nv, st));
-    int a = 0;
+    const int a = 0;
     for (long long it = 0; it <= nv; it++) {
       PF_CK(cudaMemsetAsync(b.word, 0, sizeof(unsigned), st));
-      PF_K_LAUNCH(pf_upd_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.upd[a],
-                                                                 b.upd[1 - a], b.word));
-      a = 1 - a;
+      PF_K_LAUNCH(pf_upd_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.upd[a], b.word));
       PF_CK(pf_read_counter(b.word, &changed, st));
       if (changed == 0) break;
     }
