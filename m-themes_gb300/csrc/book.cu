@@ -19,6 +19,7 @@ namespace mth {
 // iteration kernels queued after that return at once.  One warp.
 __global__ void __launch_bounds__(32) iter_book_kernel(IterBook* __restrict__ b, const double* __restrict__ red,
                                                        double* __restrict__ add, int* __restrict__ live, int first) {
+  chain_wait();
   const int lane = threadIdx.x;
   __shared__ double s6[6], s16[6], sg[9], sg1[9], v6[6], v61[6], dv[9], dv1[9], u[9];
   __shared__ int more;
@@ -139,9 +140,9 @@ __global__ void __launch_bounds__(32) iter_book_kernel(IterBook* __restrict__ b,
   }
 }
 
-cudaError_t launch_iter_book(IterBook* b, const double* red, double* add, int* live, int first, cudaStream_t st) {
-  iter_book_kernel<<<1, 32, 0, st>>>(b, red, add, live, first);
-  return cudaGetLastError();
+cudaError_t launch_iter_book(IterBook* b, const double* red, double* add, int* live, int first, cudaStream_t st,
+                             int pdl) {
+  return launch_chain(iter_book_kernel, dim3(1), dim3(32), 0, st, pdl, b, red, add, live, first);
 }
 
 }  // namespace mth

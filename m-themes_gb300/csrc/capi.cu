@@ -670,6 +670,12 @@ extern "C" mth_status mth_create(const mth_params* p, mth_ctx** out) {
     if (c->mixed) carve_dd(static_cast<float*>(c->dd_mem), c->ddf, c->ff);
     else carve_dd(static_cast<double*>(c->dd_mem), c->ddd, c->fd);
   }
+  // MTH_PDL=0: the iteration's kernels launched one after the other without
+  // programmatic dependencies (for comparisons)
+  {
+    const char* pd = getenv("MTH_PDL");
+    c->pdl = pd && pd[0] == '0' ? 0 : 1;
+  }
   // MTH_HOST_BOOK=1: mth_step keeps the per-iteration bookkeeping on the
   // host (tests compare it with the device's, bit for bit)
   {
@@ -750,7 +756,9 @@ extern "C" mth_status mth_destroy(mth_ctx* c) {
   return MTH_OK;
 }
 
-IterIn iter_in(const mth_ctx* c) { return IterIn{c->add_d, c->live_d}; }
+// programmatic dependent launches along the iteration's kernels, outside a
+// batch (whose graph keeps ordinary edges)
+IterIn iter_in(const mth_ctx* c) { return IterIn{c->add_d, c->live_d, c->in_batch ? 0 : c->pdl}; }
 
 // gated: the kernel follows the live flag (inside a batch graph)
 mth_status launch_reduce(mth_ctx* c, int width, bool gated) {
@@ -1343,7 +1351,7 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
     return step_end(c, rep);
   }
   CK(cudaMemcpyAsync(c->bk_d, &b, sizeof(IterBook), cudaMemcpyHostToDevice, c->st));
-  LAUNCH(K_BOOK, 0, launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 1, c->st));
+  LAUNCH(K_BOOK, 0, launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 1, c->st, 0));
   int queued = 0, group = 2;
   for (;;) {
     const int n = std::min(group, b.iter_max - queued);
@@ -1352,7 +1360,7 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
       if (s) return s;
       s = launch_reduce(c, NPART, true);
       if (s) return s;
-      LAUNCH(K_BOOK, 0, launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 0, c->st));
+      LAUNCH(K_BOOK, 0, launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 0, c->st, c->pdl));
     }
     queued += n;
     CK(cudaMemcpyAsync(&c->book_h[0], c->live_d, sizeof(int), cudaMemcpyDeviceToHost, c->st));

@@ -112,6 +112,7 @@ struct mth_ctx {
   IterBook* bk_d;     // its device copy (mth_step's device-side bookkeeping)
   int* book_h;        // pinned: live flag, iteration, non-finite flag read after a group of iterations
   bool host_book;     // bookkeeping on the host after every iteration instead (test hook)
+  int pdl;            // programmatic dependent launches along the iteration's kernels
   int istep;
   int uploaded;
   // dynamic recrystallisation

@@ -525,8 +525,7 @@ static cudaError_t zr_launch(const TmaMaps* t, int ncomp, long long lines, const
   auto k = fft_zr_tma_kernel<T, N, LB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((unsigned)((lines + LB - 1) / LB), ncomp);
-  k<<<grid, NT, sm, st>>>(t->real_sig, t->spec_z, tw, it, err);
-  return cudaGetLastError();
+  return launch_chain(k, grid, dim3(NT), sm, st, it.pdl, t->real_sig, t->spec_z, tw, it, err);
 }
 
 template <typename T, int N>
@@ -538,13 +537,12 @@ static cudaError_t zc_launch(const CUtensorMap& ms, const CUtensorMap& mr, int n
   if (mode) {
     auto k = fft_zc_tma_kernel<T, N, LB, 1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, it, err);
+    return launch_chain(k, grid, dim3(NT), sm, st, it.pdl, ms, mr, tw, scale, it, err);
   } else {
     auto k = fft_zc_tma_kernel<T, N, LB, 0>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(ms, mr, tw, scale, it, err);
+    return launch_chain(k, grid, dim3(NT), sm, st, it.pdl, ms, mr, tw, scale, it, err);
   }
-  return cudaGetLastError();
 }
 
 template <typename T, int L, int KB>
@@ -555,13 +553,11 @@ static cudaError_t s_launch(const CUtensorMap& m, int axis, int ncomp, int noute
   if (sign < 0) {
     auto k = fft_s_tma_kernel<T, L, KB, -1>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(m, axis, tw, it, err);
-  } else {
-    auto k = fft_s_tma_kernel<T, L, KB, +1>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<grid, NT, sm, st>>>(m, axis, tw, it, err);
+    return launch_chain(k, grid, dim3(NT), sm, st, it.pdl, m, axis, tw, it, err);
   }
-  return cudaGetLastError();
+  auto k = fft_s_tma_kernel<T, L, KB, +1>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  return launch_chain(k, grid, dim3(NT), sm, st, it.pdl, m, axis, tw, it, err);
 }
 
 template <typename T, int L, int KB>
@@ -571,8 +567,8 @@ static cudaError_t g_launch(const TmaMaps* t, const FftGeom& g, const GreenConst
   auto k = fft_xg_tma_kernel<T, L, KB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   dim3 grid((g.kzs + KB - 1) / KB, g.n1);
-  k<<<grid, NT, sm, st>>>(gc, t->spec_g, t->anti_g, g.n1, g.n2, g.kz, twf, twi, it, err);
-  return cudaGetLastError();
+  return launch_chain(k, grid, dim3(NT), sm, st, it.pdl, gc, t->spec_g, t->anti_g, g.n1, g.n2, g.kz, twf, twi, it,
+                      err);
 }
 
 // the compiled tile widths: FP32 strided 8/16/32, Green 2/4/8; FP64 strided

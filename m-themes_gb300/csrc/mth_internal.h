@@ -32,8 +32,42 @@ struct AddVec { double v[6]; };
 struct IterIn {
   const double* add;
   const int* live;
+  int pdl;   // host side: launch the pass as a programmatic dependent of the kernel before it
 };
-__device__ __forceinline__ bool is_live(const IterIn& in) { return !in.live || *in.live; }
+// The kernels of the Green iteration's chain start with is_live.  Launched
+// as programmatic dependents (launch_chain) they may begin while the kernel
+// before them drains, so they first wait there for that grid and its memory
+// (griddepcontrol.wait; it returns at once after an ordinary launch), then
+// read the live flag.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ bool is_live(const IterIn& in) {
+  chain_wait();
+  return !in.live || *in.live;
+}
+#ifdef __CUDACC__
+// Launch of a chain kernel: with pdl, as a programmatic dependent of the
+// previous kernel in the stream (its launch and prologue overlap that
+// kernel's last blocks); the kernel must begin with chain_wait.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_chain(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, int pdl,
+                                Args... args) {
+  if (!pdl) {
+    k<<<grid, block, smem, st>>>(args...);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+#endif
 
 // Green-operator constants, passed by value (kernel parameter space).
 struct GreenConst {
@@ -304,6 +338,7 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, int widt
 
 // the per-iteration bookkeeping on the device (book.cu, book.cuh)
 struct IterBook;
-cudaError_t launch_iter_book(IterBook* b, const double* red, double* add, int* live, int first, cudaStream_t st);
+cudaError_t launch_iter_book(IterBook* b, const double* red, double* add, int* live, int first, cudaStream_t st,
+                             int pdl);
 
 }  // namespace mth

@@ -1051,8 +1051,8 @@ static cudaError_t launch_coop(const NewtonConst& nc, const Fields<float>& f, do
                                const IterIn& it, cudaStream_t st) {
   cudaError_t e = coop_attr<MINB, LAW>();
   if (e != cudaSuccess) return e;
-  newton_coop_kernel<float, float, double, MINB, LAW><<<nblocks, 256, COOP_DYN, st>>>(nc, f, partials, it);
-  return cudaGetLastError();
+  return launch_chain(newton_coop_kernel<float, float, double, MINB, LAW>, dim3(nblocks), dim3(256), COOP_DYN, st,
+                      it.pdl, nc, f, partials, it);
 }
 
 // blocks per SM the cooperative kernel is compiled for: 4 (64 registers,
@@ -1112,25 +1112,30 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     // mixed modes (no FP32-solve variants)
     if (mixed) {
       const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-      newton_kernel<float, float, double, MTH_DD_MINB, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+      return launch_chain(newton_kernel<float, float, double, MTH_DD_MINB, false, 1>, dim3(nblocks), dim3(256), 0, st,
+                          it.pdl, nc, f, partials, it);
     } else {
       const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-      newton_kernel<double, double, double, 1, false, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+      return launch_chain(newton_kernel<double, double, double, 1, false, 1>, dim3(nblocks), dim3(256), 0, st, it.pdl,
+                          nc, f, partials, it);
     }
     return cudaGetLastError();
   }
   if (mixed == 2) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, float, MTH_FAST_MINB><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    return launch_chain(newton_kernel<float, float, float, MTH_FAST_MINB>, dim3(nblocks), dim3(256), 0, st, it.pdl, nc,
+                        f, partials, it);
   } else if (mixed == 3) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
-    newton_kernel<float, float, double, MTH_FAST_MINB, true><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    return launch_chain(newton_kernel<float, float, double, MTH_FAST_MINB, true>, dim3(nblocks), dim3(256), 0, st,
+                        it.pdl, nc, f, partials, it);
   } else if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
     return launch_coop<MTH_COOP_MINB, 0>(nc, f, partials, nblocks, it, st);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    newton_kernel<double, double, double, 1><<<nblocks, 256, 0, st>>>(nc, f, partials, it);
+    return launch_chain(newton_kernel<double, double, double, 1>, dim3(nblocks), dim3(256), 0, st, it.pdl, nc, f,
+                        partials, it);
   }
   return cudaGetLastError();
 }
@@ -1488,8 +1493,8 @@ __global__ void __launch_bounds__(RED_NT) reduce_partials_kernel(const double* _
 
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
                                    cudaStream_t st) {
-  reduce_partials_kernel<<<width, RED_NT, 0, st>>>(partials, nblocks, width, out, it);
-  return cudaGetLastError();
+  return launch_chain(reduce_partials_kernel, dim3(width), dim3(RED_NT), 0, st, it.pdl, partials, nblocks, width, out,
+                      it);
 }
 
 
