@@ -343,12 +343,17 @@ __global__ void __launch_bounds__(NT) fft_s_tma_kernel(const __grid_constant__ C
 // Gamma0 : sigma-hat at every wave vector of the tile, antisymmetric part
 // added to the spin accumulator tile, inverse along x.  One block: fixed y,
 // KB consecutive kz.
-// resident blocks per SM the Green pass asks registers for: up to 4 in FP32,
-// no more than its shared-memory tile lets fit (228 KB per SM)
+// resident blocks per SM the Green pass asks registers for: up to
+// MTH_XG_CAP in FP32, no more than its shared-memory tile lets fit (228 KB
+// per SM).  128^3, 300 launches: 15.5 ms with 5 (48 registers), 16.1 ms
+// with 4 (64), 16.9 ms with 6 (40)
+#ifndef MTH_XG_CAP
+#define MTH_XG_CAP 5
+#endif
 template <typename T, int L, int KB>
 constexpr int xg_min_blocks() {
   constexpr long fit = 228L * 1024 / (9L * L * KB * (long)sizeof(c2<T>) + 2048);
-  return sizeof(T) == 8 || fit < 1 ? 1 : fit > 4 ? 4 : (int)fit;
+  return sizeof(T) == 8 || fit < 1 ? 1 : fit > MTH_XG_CAP ? MTH_XG_CAP : (int)fit;
 }
 
 template <typename T, int L, int KB>
