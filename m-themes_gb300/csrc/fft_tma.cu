@@ -212,8 +212,14 @@ template <typename T> __host__ __device__ constexpr int cw() { return (int)(size
 // 8.3 ms against 9.0 ms (16) and 10.8 ms (8) for 400 launches)
 template <typename T> __host__ __device__ constexpr int kb_strided() { return sizeof(T) == 4 ? 32 : 4; }
 template <typename T> __host__ __device__ constexpr int kb_green() { return sizeof(T) == 4 ? 4 : 2; }
-template <typename T> __host__ __device__ constexpr int lb_z(int n) {
-  int lb = 2048 / (n / 2);
+// lines per z-pass tile: about `elems` complex points (lines x N/2).  At
+// 128^3 (FP32, 300 launches): R2C 9.4 ms with 2048 (32 lines), 9.5 ms with
+// 1024, 10.6 ms with 4096; C2R + strain 9.9 ms with 1024 (16 lines), 11.1 ms
+// with 2048, 12.9 ms with 4096 (its tile holds the spectrum rows, the work
+// lines and the real field, so the smaller tile doubles the blocks per SM).
+constexpr int ZR_ELEMS = 2048, ZC_ELEMS = 1024;
+template <typename T> __host__ __device__ constexpr int lb_z(int n, int elems) {
+  int lb = elems / (n / 2);
   int p = 8;
   while (p * 2 <= lb && p < 64) p *= 2;
   if (sizeof(T) == 8 && p > 8) p /= 2;
@@ -439,7 +445,7 @@ static bool encode(CUtensorMap* m, CUtensorMapDataType dt, int rank, void* base,
 
 struct TmaMaps {
   CUtensorMap real_sig, real_strain, real_wspin;   // z passes, real fields
-  CUtensorMap spec_z, anti_z;                      // z passes, half spectra
+  CUtensorMap spec_z, spec_zc, anti_z;             // z passes, half spectra (R2C / C2R tiles)
   CUtensorMap spec_y, anti_y, anti_x;              // strided passes
   CUtensorMap spec_g, anti_g;                      // Green x pass
   bool z, s, g;                                    // passes with maps
@@ -468,19 +474,22 @@ TmaMaps* tma_create(const FftGeom& g, T* sig, T* strain, T* wspin, c2<T>* spec, 
   const CUtensorMapDataType wt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;   // spectra in 8-byte words
   const cuuint64_t C = (cuuint64_t)cw<T>(), cb = sizeof(c2<T>), ws = sizeof(T);
   const cuuint64_t lines = (cuuint64_t)g.n0 * g.n1;
-  const int lb = lb_z<T>(g.n2);
+  const int lbr = lb_z<T>(g.n2, ZR_ELEMS), lbc = lb_z<T>(g.n2, ZC_ELEMS);
   bool ok = true;
-  // z passes: real [c][line][z] and spectrum [c][line][kzs]
+  // z passes: real [c][line][z] and spectrum [c][line][kzs]; boxes of the
+  // R2C tile (stress in, spectrum out) and of the C2R tile (spectra in,
+  // strain and spin fields in and out)
   if ((cuuint64_t)g.kzs * C <= 256) {
     cuuint64_t d6[3] = {(cuuint64_t)g.n2, lines, 6}, d3[3] = {(cuuint64_t)g.n2, lines, 3};
     cuuint64_t st[2] = {g.n2 * ws, (cuuint64_t)g.plane * ws};
-    cuuint32_t bx[3] = {(cuuint32_t)g.n2, (cuuint32_t)lb, 1};
-    ok = ok && encode(&t->real_sig, rt, 3, sig, d6, st, bx) && encode(&t->real_strain, rt, 3, strain, d6, st, bx) &&
-         encode(&t->real_wspin, rt, 3, wspin, d3, st, bx);
+    cuuint32_t bxr[3] = {(cuuint32_t)g.n2, (cuuint32_t)lbr, 1}, bxc[3] = {(cuuint32_t)g.n2, (cuuint32_t)lbc, 1};
+    ok = ok && encode(&t->real_sig, rt, 3, sig, d6, st, bxr) && encode(&t->real_strain, rt, 3, strain, d6, st, bxc) &&
+         encode(&t->real_wspin, rt, 3, wspin, d3, st, bxc);
     cuuint64_t k6[3] = {(cuuint64_t)g.kzs * C, lines, 6}, k3[3] = {(cuuint64_t)g.kzs * C, lines, 3};
     cuuint64_t ks[2] = {(cuuint64_t)g.kzs * cb, (cuuint64_t)g.kplane * cb};
-    cuuint32_t kbx[3] = {(cuuint32_t)(g.kzs * C), (cuuint32_t)lb, 1};
-    ok = ok && encode(&t->spec_z, wt, 3, spec, k6, ks, kbx) && encode(&t->anti_z, wt, 3, anti, k3, ks, kbx);
+    cuuint32_t kbr[3] = {(cuuint32_t)(g.kzs * C), (cuuint32_t)lbr, 1}, kbc[3] = {(cuuint32_t)(g.kzs * C), (cuuint32_t)lbc, 1};
+    ok = ok && encode(&t->spec_z, wt, 3, spec, k6, ks, kbr) && encode(&t->spec_zc, wt, 3, spec, k6, ks, kbc) &&
+         encode(&t->anti_z, wt, 3, anti, k3, ks, kbc);
     t->z = ok;
   }
   // strided and Green passes: [c][x][y][kzs] as 4-D
@@ -525,7 +534,7 @@ static size_t zc_smem(int n, int lb, size_t cb) {
 template <typename T, int N>
 static cudaError_t zr_launch(const TmaMaps* t, int ncomp, long long lines, const c2<T>* tw, const IterIn& it,
                              int* err, cudaStream_t st) {
-  constexpr int LB = lb_z<T>(N);
+  constexpr int LB = lb_z<T>(N, ZR_ELEMS);
   const size_t sm = zr_smem(N, LB, sizeof(c2<T>));
   auto k = fft_zr_tma_kernel<T, N, LB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -536,7 +545,7 @@ static cudaError_t zr_launch(const TmaMaps* t, int ncomp, long long lines, const
 template <typename T, int N>
 static cudaError_t zc_launch(const CUtensorMap& ms, const CUtensorMap& mr, int ncomp, long long lines,
                              const c2<T>* tw, T scale, const IterIn& it, int mode, int* err, cudaStream_t st) {
-  constexpr int LB = lb_z<T>(N);
+  constexpr int LB = lb_z<T>(N, ZC_ELEMS);
   const size_t sm = zc_smem(N, LB, sizeof(c2<T>));
   dim3 grid((unsigned)((lines + LB - 1) / LB), ncomp);
   if (mode) {
@@ -617,7 +626,7 @@ template <typename T>
 cudaError_t tma_fft_z_c2r(const TmaMaps* t, const FftGeom& g, int which, const c2<T>* tw, T scale, const IterIn& it,
                           int* err, cudaStream_t st) {
   const long long lines = (long long)g.n0 * g.n1;
-  const CUtensorMap& ms = which ? t->anti_z : t->spec_z;
+  const CUtensorMap& ms = which ? t->anti_z : t->spec_zc;
   const CUtensorMap& mr = which ? t->real_wspin : t->real_strain;
   const int ncomp = which ? 3 : 6, mode = which ? 0 : 1;
   switch (g.n2) {
