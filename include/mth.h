@@ -167,7 +167,14 @@ typedef enum {
 const char* mth_version(void);
 const char* mth_last_error(void);   /* thread-local message of the last failure */
 
-/* Context lifecycle: replaces SetupJob/Evolution/DestroyJob (src/evp.c:23-26). */
+/* Context lifecycle: replaces SetupJob/Evolution/DestroyJob (src/evp.c:23-26).
+ * mth_step runs the Green iterations with their bookkeeping on the GPU and
+ * queues them in groups, reading a convergence flag once per group.
+ * Environment read by mth_create, for tests and comparisons only:
+ *   MTH_FFT_TILES="ks,kg"      tile widths of the strided / Green TMA passes
+ *   MTH_PDL=0                  no programmatic dependent launches
+ *   MTH_HOST_BOOK=1            per-iteration bookkeeping on the host
+ *   MTH_TEST_FAIL_TILE_WAIT=1  tile waits report a time-out (failure-path test) */
 typedef struct mth_ctx mth_ctx;
 mth_status mth_create(const mth_params* params, mth_ctx** out);
 /* Voxel microstructure in the reference's text order: z fastest, then y, then
