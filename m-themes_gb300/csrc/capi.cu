@@ -310,6 +310,7 @@ void ctx_free(mth_ctx* c) {
   delete c->drx_class_h;
   cudaFree(c->drx_rot_d);
   cudaFree(c->drx_class_d);
+  cudaFree(c->drx_cnt_d);
   pf_free(c->pff);
   pf_free(c->pfd);
   cudaFree(c->rho_d);
@@ -1117,9 +1118,11 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
   if ((size_t)n_drx > c->drx_cap) {
     cudaFree(c->drx_rot_d);
     cudaFree(c->drx_class_d);
+    cudaFree(c->drx_cnt_d);
     c->drx_cap = (size_t)n_drx * 2 + 64;
     CK(cudaMalloc(&c->drx_rot_d, sizeof(double) * 9 * c->drx_cap));
     CK(cudaMalloc(&c->drx_class_d, sizeof(int) * c->drx_cap));
+    CK(cudaMalloc(&c->drx_cnt_d, sizeof(int) * 2 * c->drx_cap));
   }
   CK(cudaMemcpyAsync(c->drx_rot_d, c->drx_rot_h->data(), sizeof(double) * 9 * n_drx, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->drx_class_d, c->drx_class_h->data(), sizeof(int) * n_drx, cudaMemcpyHostToDevice, c->st));
@@ -1160,8 +1163,9 @@ static mth_status drx_step(mth_ctx* c, int* n_new) {
            launch_resample_nearest(c->npf, gid_new, c->n, c->gid_coarse_d, c->st));
     gid_new = c->gid_coarse_d;
   }
-  LAUNCH(K_DRX, (double)c->nv * 12, launch_drx_update(c->mixed, f, c->grain_d, c->grain_prev_d, gid_new, c->first_drx_id, n_drx,
-                                       c->drx_rot_d, c->drx_class_d, c->tau0f, c->nsys, c->st));
+  LAUNCHN(K_DRX, 2, (double)c->nv * 24,
+          launch_drx_update(c->mixed, f, c->grain_d, c->grain_prev_d, gid_new, c->first_drx_id, n_drx, c->drx_rot_d,
+                            c->drx_class_d, c->tau0f, c->nsys, c->drx_cnt_d, c->st));
   return refresh_reference_medium(c);
 }
 

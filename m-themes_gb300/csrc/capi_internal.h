@@ -123,6 +123,7 @@ struct mth_ctx {
   std::vector<int>* drx_class_h;
   double* drx_rot_d;
   int* drx_class_d;
+  int* drx_cnt_d;     // per recrystallised grain: voxels, voxels that joined it this step
   size_t drx_cap;
   PfBuffers<float> pff;
   PfBuffers<double> pfd;

@@ -935,6 +935,22 @@ __global__ void drx_rho_kernel(Fields<TSt> f, double rho0, double rho_k, double*
   rho_t[v] = (TSt)r;
 }
 
+// Per recrystallised grain k: its voxels after the relaxation (cnt[k]) and
+// those of them that joined it in this step (cnt[n_drx + k]), for the
+// "< 1 % grew" rule of src/integrated.c:1537-1582.
+template <typename TSt>
+__global__ void drx_count_kernel(Fields<TSt> f, const int* __restrict__ grain, const int* __restrict__ grain_prev,
+                                 const int* __restrict__ gid_new, int first_drx_id, int n_drx,
+                                 int* __restrict__ cnt) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= f.nv) return;
+  const int gn = gid_new[v] != 0 ? gid_new[v] : grain[v];
+  const int k = gn - first_drx_id;
+  if (k < 0 || k >= n_drx) return;
+  atomicAdd(&cnt[k], 1);
+  if (gn != grain_prev[v] && f.phase[v] == 0) atomicAdd(&cnt[n_drx + k], 1);
+}
+
 // Voxels whose relaxed grain id differs from the id before this step's
 // nucleation and belongs to a recrystallised grain become part of it: the
 // treatment of growth==1 voxels after PF_XRX (src/evolution.c:1120-1200):
@@ -945,7 +961,7 @@ template <typename TSt>
 __global__ void drx_update_kernel(Fields<TSt> f, int* __restrict__ grain, const int* __restrict__ grain_prev,
                                   const int* __restrict__ gid_new, int first_drx_id, int n_drx,
                                   const double* __restrict__ drx_rot, const int* __restrict__ drx_class, double tau0f,
-                                  int nsys) {
+                                  int nsys, const int* __restrict__ cnt) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long P = f.nv;
   if (v >= P) return;
@@ -957,6 +973,9 @@ __global__ void drx_update_kernel(Fields<TSt> f, int* __restrict__ grain, const 
   if (gn == grain_prev[v] || f.phase[v] != 0) return;
   const int k = gn - first_drx_id;
   if (k < 0 || k >= n_drx) return;
+  // a grain whose joining voxels are under 1 % of it (integer percent 0,
+  // src/integrated.c:1562-1577) resets none of them: they take its id only
+  if ((long long)cnt[n_drx + k] * 100 / cnt[k] == 0) return;
   for (int i = 0; i < 6; i++) f.sig[i * P + v] = (TSt)0;
   f.gamacum[v] = (TSt)0;
   for (int s = 0; s < NSYS; s++) f.crss[s * P + v] = (TSt)(s < nsys ? tau0f : 0.0);
@@ -985,15 +1004,19 @@ cudaError_t launch_drx_rho(int mixed, const void* fields, double rho0, double rh
 
 cudaError_t launch_drx_update(int mixed, const void* fields, int* grain, const int* grain_prev, const int* gid_new,
                               int first_drx_id, int n_drx, const double* drx_rot, const int* drx_class, double tau0f,
-                              int nsys, cudaStream_t st) {
+                              int nsys, int* cnt, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int) * 2 * (size_t)n_drx, st);
+  if (e != cudaSuccess) return e;
   if (mixed) {
     const Fields<float>& f = *static_cast<const Fields<float>*>(fields);
+    drx_count_kernel<float><<<nb(f.nv, 256), 256, 0, st>>>(f, grain, grain_prev, gid_new, first_drx_id, n_drx, cnt);
     drx_update_kernel<float><<<nb(f.nv, 256), 256, 0, st>>>(f, grain, grain_prev, gid_new, first_drx_id, n_drx, drx_rot,
-                                                            drx_class, tau0f, nsys);
+                                                            drx_class, tau0f, nsys, cnt);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
+    drx_count_kernel<double><<<nb(f.nv, 256), 256, 0, st>>>(f, grain, grain_prev, gid_new, first_drx_id, n_drx, cnt);
     drx_update_kernel<double><<<nb(f.nv, 256), 256, 0, st>>>(f, grain, grain_prev, gid_new, first_drx_id, n_drx,
-                                                             drx_rot, drx_class, tau0f, nsys);
+                                                             drx_rot, drx_class, tau0f, nsys, cnt);
   }
   return cudaGetLastError();
 }

@@ -261,9 +261,11 @@ cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, i
 // adoption of the relaxed grain ids and the reset of recrystallised voxels.
 cudaError_t launch_drx_rho(int mixed, const void* fields, double rho0, double rho_k, double* rho_d, void* rho_t,
                            cudaStream_t st);
+// cnt: scratch of 2 n_drx ints (per recrystallised grain: its voxels, those
+// that joined it in this step)
 cudaError_t launch_drx_update(int mixed, const void* fields, int* grain, const int* grain_prev, const int* gid_new,
                               int first_drx_id, int n_drx, const double* drx_rot, const int* drx_class,
-                              double tau0f, int nsys, cudaStream_t st);
+                              double tau0f, int nsys, int* cnt, cudaStream_t st);
 cudaError_t launch_class_histogram(long long nv, const uint8_t* crystal, const int* eclass, unsigned long long* hist,
                                    cudaStream_t st);
 // grid transfer between the mechanical and the phase-field grid

@@ -1258,6 +1258,19 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
       st = orc_pf_relax(p, c->n, c->grain, rho, p->pf_substeps, c->first_drx_id - 1, c->rho_avg_tab,
                         c->rho_avg_len, gnew, NULL, NULL, NULL, 0);
     }
+    /* per recrystallised grain: its voxels after the relaxation and those
+       that joined it in this step; a grain whose joining voxels are under
+       1 % of it (integer percent 0) resets none of them, they take its id
+       only (the "growth" rollback, src/integrated.c:1537-1582) */
+    long long* gtot = (long long*)calloc((size_t)c->n_drx, sizeof(long long));
+    long long* gjoin = (long long*)calloc((size_t)c->n_drx, sizeof(long long));
+    for (size_t v = 0; v < nv; v++) {
+      const int g = gnew[v] != 0 ? gnew[v] : c->grain[v];
+      const int k = g - c->first_drx_id;
+      if (k < 0 || k >= c->n_drx) continue;
+      gtot[k]++;
+      if (g != prev[v] && cry[v]) gjoin[k]++;
+    }
     for (size_t v = 0; v < nv && st == MTH_OK; v++) {
       /* a voxel left without a positive eta (grain id 0: the reference stops
          there on GetStatistics' assert, src/pf_xrx.c:1383-1386) keeps its grain */
@@ -1265,6 +1278,7 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
       c->grain[v] = g;
       const int k = g - c->first_drx_id;
       if (g == prev[v] || !cry[v] || k < 0 || k >= c->n_drx) continue;
+      if (gjoin[k] * 100 / gtot[k] == 0) continue;
       memset(c->sig[v], 0, sizeof(t33));
       c->gamacum[v] = 0.0;
       for (int i = 0; i < ph0->nsys; i++) { c->crss[v][i][0] = ph0->tau[0]; c->crss[v][i][1] = ph0->tau[1]; }
@@ -1277,6 +1291,8 @@ static int orc_drx_step(orc_ctx* c, int* n_new) {
       memcpy(c->sg66[v], c->cgr[v], sizeof(m66));
       if (lu_inv66(c->sg66[v])) st = MTH_ERR_SINGULAR;
     }
+    free(gtot);
+    free(gjoin);
     if (st == MTH_OK) {
       m66 csum;
       memset(csum, 0, sizeof(csum));

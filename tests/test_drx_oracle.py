@@ -230,3 +230,59 @@ def test_grid_transfer_properties():
     Xd, Yd, Zd = np.meshgrid(*[np.arange(n) / (n - 1) for n in nd], indexing="ij")
     want = (1.5 + 2.0 * Xd - 0.5 * Yd + 3.0 * Zd).ravel()
     np.testing.assert_allclose(pyoracle.resample(f, ns, nd), want, rtol=0, atol=1e-12)
+
+
+def rollback_case(radius2):
+    """Coupled runs at 24^3.  With nuclei of radius 6 (|d|^2 <= 36) grown
+    recrystallised grains gain a voxel or two per step: under 1 % of their
+    voxels.  With radius 3 (|d|^2 <= 9) small grains grow by a few percent."""
+    return synth.Config(cell_dim=(24, 24, 24), n_grains=6, n_steps=6, seed=5, iter_max=8,
+                        drx=synth.Drx(rho_k=4000.0, rho_nucleation=30.0, nucleation_prob=0.001 if radius2 > 9 else 0.003,
+                                      nucleus_radius=radius2))
+
+
+def joined_fractions(prev, cur, first_drx_id):
+    """Per recrystallised grain present after a step: (id, voxels, voxels
+    that joined it in the step)."""
+    out = []
+    joined = (cur != prev) & (cur >= first_drx_id)
+    for i, c in zip(*np.unique(cur[cur >= first_drx_id], return_counts=True)):
+        out.append((int(i), int(c), int(np.sum(joined & (cur == i)))))
+    return out
+
+
+def test_slowly_growing_grains_reset_no_joining_voxel():
+    """src/integrated.c:1537-1582: a recrystallised grain whose joining voxels
+    are under 1 % of it (integer percent 0) clears their growth flags, so
+    they take its id without the reset of src/evolution.c:1120-1200 (stress,
+    accumulated slip, CRSS and the grain's orientation).  Joining voxels of
+    such grains keep their lattice orientation (it moves by one step's
+    rotation only); those of grains that grew by 1 % or more take the
+    grain's (that of the voxels it held)."""
+    kept = reset = 0
+    for radius2 in (36, 9):
+        cfg = rollback_case(radius2)
+        g, p, e = synth.microstructure(cfg)
+        par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
+        o = pyoracle.Oracle(par, g, p, e, nthreads=os.cpu_count())
+        first = int(g.max()) + 1
+        prev = o.field("grain").ravel().astype(int)
+        rot_prev = o.field("rot")
+        for _ in range(cfg.n_steps):
+            o.step()
+            cur = o.field("grain").ravel().astype(int)
+            rot = o.field("rot")
+            for gid, tot, joined in joined_fractions(prev, cur, first):
+                sel = (cur == gid) & (cur != prev)
+                held = np.flatnonzero((cur == gid) & (cur == prev))
+                if not joined or held.size == 0:
+                    continue
+                if joined * 100 // tot == 0:
+                    assert np.abs(rot[sel] - rot_prev[sel]).max() < 1e-2, gid
+                    kept += joined
+                else:
+                    assert np.abs(rot[sel] - rot[held[0]]).max() < 5e-2, gid
+                    reset += joined
+            prev, rot_prev = cur, rot
+        o.close()
+    assert kept > 0 and reset > 0

@@ -8,6 +8,7 @@ bit-identical to the oracle's, and to the reference fixtures directly.  Mixed
 precision (FP32 order parameters) must agree on at least 99% of the grain
 map."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -197,3 +198,28 @@ def test_coupled_drx_on_its_own_pf_grid(pf_dims):
         assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
     assert total_new > 0
     s.close()
+
+
+@pytest.mark.parametrize("radius2", [36, 9])
+def test_coupled_drx_growth_rule_matches_oracle(radius2):
+    """The "< 1 % grew" rule (src/integrated.c:1537-1582) on the GPU: runs in
+    which grown recrystallised grains gain under 1 % of their voxels in a
+    step (radius-6 nuclei) and some percent (radius-3 nuclei), FP64 grain
+    maps identical to the oracle's and its orientation, slip and stress
+    fields at every step."""
+    from test_drx_oracle import rollback_case
+    cfg = rollback_case(radius2)
+    g, p, e = synth.microstructure(cfg)
+    par = capi.params_from_config(cfg, precision=capi.MTH_FP64)
+    from mth import Solver
+    s = Solver(par, g, p, e)
+    o = pyoracle.Oracle(par, g, p, e, nthreads=os.cpu_count())
+    for k in range(cfg.n_steps):
+        a, b = s.step(), o.step()
+        assert a["n_new_grains"] == b["n_new_grains"], k
+        assert np.array_equal(s.field("grain"), o.field("grain")), k
+        assert rel(s.field("rot"), o.field("rot")) < 1e-8, k
+        assert rel(s.field("gamacum"), o.field("gamacum")) < 1e-6, k
+        assert rel(a["sig_avg"], b["sig_avg"]) < 1e-6, k
+    s.close()
+    o.close()
