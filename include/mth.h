@@ -301,9 +301,11 @@ mth_status mth_iout_wait(mth_ctx* ctx);
 /* Batches of independent volumes (RVEs) on one GPU.  Each member has its own
  * parameters (material, loading, precision), microstructure and grid size;
  * mth_batch_step advances every member by one mechanical step, with the same
- * results as mth_step on each member alone.  One Green iteration of all
- * members still iterating is one CUDA-graph launch (the members' kernels as
- * parallel branches); converged members are switched off on the device.
+ * results as mth_step on each member alone.  The step is one CUDA-graph
+ * launch: a device-side loop whose body is one Green iteration of all
+ * members (their kernels as parallel branches, each with its bookkeeping);
+ * converged members are switched off on the device and the loop ends when
+ * none is left.
  * The reference runs one volume per job (src/evp.c:7-32) and has no
  * counterpart.  Recrystallisation (pf_substeps > 0) is not supported in a
  * batch (MTH_ERR_UNSUPPORTED); all members must name the same device. */

@@ -32,6 +32,8 @@ struct mth_batch {
   double* red_h = nullptr;
   int* err_d = nullptr;
   int* err_h = nullptr;
+  int* ctl_d = nullptr;   // iterations the step's loop ran, and whether it hit its bound
+  int* ctl_h = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<NewtonConst> cap_nc;
 };
@@ -51,6 +53,8 @@ void batch_free(mth_batch* b) {
   cudaFree(b->live_d);
   cudaFree(b->red_d);
   cudaFree(b->err_d);
+  cudaFree(b->ctl_d);
+  if (b->ctl_h) cudaFreeHost(b->ctl_h);
   if (b->add_h) cudaFreeHost(b->add_h);
   if (b->live_h) cudaFreeHost(b->live_h);
   if (b->red_h) cudaFreeHost(b->red_h);
@@ -140,44 +144,79 @@ mth_status tune_passes(const mth_params& p, PassChoice* out) {
   return MTH_OK;
 }
 
-// one Green iteration of every member as parallel graph branches
+// The Green-iteration loop of a mechanical step of every member, as one
+// graph: a while node whose body is one iteration of all members (each
+// member's FFT passes, Newton, reduction and one-warp bookkeeping as a
+// parallel branch, gated by its live flag) followed by a one-thread kernel
+// that continues the loop while a member is live.  The bookkeeping kernels
+// (book.cu) drop a member's flag when it is done, so one graph launch runs
+// the step's iterations with no host round trip; the loop also ends on a
+// tile-wait time-out and after `bound` iterations (an error).
+__global__ void batch_more_kernel(cudaGraphConditionalHandle h, const int* __restrict__ live,
+                                  const int* __restrict__ err, int n, int* __restrict__ ctl, int bound) {
+  if (threadIdx.x != 0) return;
+  int any = 0, bad = 0;
+  for (int i = 0; i < n; i++) {
+    any |= live[i];
+    bad |= err[i];
+  }
+  const int it = ++ctl[0];
+  if (any && it >= bound) ctl[1] = 1;
+  cudaGraphSetConditional(h, (any && !bad && it < bound) ? 1u : 0u);
+}
+
 mth_status batch_capture(mth_batch* b) {
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
   }
   const int n = b->n;
-  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  int bound = 1;
+  for (mth_ctx* c : b->rve) bound = std::max(bound, c->p.iter_max + 1);
   mth_status s = MTH_OK;
   auto ck = [&](cudaError_t e) {
     if (e != cudaSuccess && !s) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
   };
-  ck(cudaMemcpyAsync(b->add_d, b->add_h, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, b->st));
-  ck(cudaMemcpyAsync(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
-  ck(cudaEventRecord(b->fork, b->st));
-  for (int i = 0; i < n && !s; i++) {
-    mth_ctx* c = b->rve[i];
-    ck(cudaStreamWaitEvent(b->branch[i], b->fork, 0));
-    const int prof = c->prof_on;
-    c->prof_on = 0;
-    c->st = b->branch[i];
-    if (!s) s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
-    if (!s) s = launch_reduce(c, NPART, true);
-    c->st = b->st;
-    c->prof_on = prof;
-    ck(cudaEventRecord(b->join[i], b->branch[i]));
-    ck(cudaStreamWaitEvent(b->st, b->join[i], 0));
-  }
-  ck(cudaMemcpyAsync(b->red_h, b->red_d, sizeof(double) * BATCH_RED * n, cudaMemcpyDeviceToHost, b->st));
-  ck(cudaMemcpyAsync(b->err_h, b->err_d, sizeof(int) * n, cudaMemcpyDeviceToHost, b->st));
   cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(b->st, &g);
-  if (!s && e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  ck(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t loop = nullptr;
+  if (!s) ck(cudaGraphAddNode(&loop, g, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = s ? nullptr : cp.conditional.phGraph_out[0];
+  if (!s) ck(cudaStreamBeginCaptureToGraph(b->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   if (!s) {
-    e = cudaGraphInstantiate(&b->exec, g, 0);
+    ck(cudaEventRecord(b->fork, b->st));
+    for (int i = 0; i < n && !s; i++) {
+      mth_ctx* c = b->rve[i];
+      ck(cudaStreamWaitEvent(b->branch[i], b->fork, 0));
+      const int prof = c->prof_on;
+      c->prof_on = 0;
+      c->st = b->branch[i];
+      if (!s) s = c->mixed ? green_iteration<float>(c) : green_iteration<double>(c);
+      if (!s) s = launch_reduce(c, NPART, true);
+      if (!s) ck(launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 0, c->st, 0));
+      c->st = b->st;
+      c->prof_on = prof;
+      ck(cudaEventRecord(b->join[i], b->branch[i]));
+      ck(cudaStreamWaitEvent(b->st, b->join[i], 0));
+    }
+    batch_more_kernel<<<1, 32, 0, b->st>>>(h, b->live_d, b->err_d, n, b->ctl_d, bound);
+    ck(cudaGetLastError());
+    cudaGraph_t out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->st, &out);
+    if (!s && e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+  }
+  if (!s) {
+    cudaError_t e = cudaGraphInstantiate(&b->exec, g, 0);
     if (e != cudaSuccess) s = set_err(MTH_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
   }
-  if (g) cudaGraphDestroy(g);
+  cudaGraphDestroy(g);
   if (s) return s;
   b->cap_nc.resize(n);
   for (int i = 0; i < n; i++) b->cap_nc[i] = b->rve[i]->nc;
@@ -220,6 +259,8 @@ extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batc
     ck(cudaMalloc(&b->live_d, sizeof(int) * n));
     ck(cudaMalloc(&b->red_d, sizeof(double) * BATCH_RED * n));
     ck(cudaMalloc(&b->err_d, sizeof(int) * n));
+    ck(cudaMalloc(&b->ctl_d, sizeof(int) * 2));
+    ck(cudaMallocHost(&b->ctl_h, sizeof(int) * 2));
     ck(cudaMallocHost(&b->add_h, sizeof(double) * 8 * n));
     ck(cudaMallocHost(&b->live_h, sizeof(int) * n));
     ck(cudaMallocHost(&b->red_h, sizeof(double) * BATCH_RED * n));
@@ -293,28 +334,31 @@ extern "C" mth_status mth_batch_step(mth_batch* b, mth_step_report* reports) {
     mth_status s = batch_capture(b);
     if (s) return s;
   }
-  std::vector<char> active(n);
-  int nact = 0;
-  for (int i = 0; i < n; i++) nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
-  while (nact > 0) {
-    for (int i = 0; i < n; i++) {
-      b->live_h[i] = active[i];
-      if (active[i]) {
-        iter_add(b->rve[i]);
-        memcpy(b->add_h + (size_t)8 * i, b->rve[i]->add_h, sizeof(double) * 6);
-      }
-    }
-    CK(cudaGraphLaunch(b->exec, b->st));
-    CK(cudaStreamSynchronize(b->st));
-    nact = 0;
-    for (int i = 0; i < n; i++) {
-      if (b->err_h[i]) return set_err(MTH_ERR_TIMEOUT, "batch member %d: a kernel timed out waiting for its tile copies", i);
-      if (!active[i]) continue;
-      mth_status s = iter_finish(b->rve[i], b->red_h + (size_t)BATCH_RED * i);
-      if (s) return s;
-      nact += (active[i] = iter_more(b->rve[i]) ? 1 : 0);
-    }
+  // each member's bookkeeping to the device and its first iteration's
+  // increment (live flags set), then the step's iterations in one launch
+  for (int i = 0; i < n; i++) {
+    mth_ctx* c = b->rve[i];
+    CK(cudaMemcpyAsync(c->bk_d, &c->bk, sizeof(IterBook), cudaMemcpyHostToDevice, b->st));
+    CK(launch_iter_book(c->bk_d, c->red, c->add_d, c->live_d, 1, b->st, 0));
   }
+  CK(cudaMemsetAsync(b->ctl_d, 0, sizeof(int) * 2, b->st));
+  CK(cudaGraphLaunch(b->exec, b->st));
+  CK(cudaMemcpyAsync(b->ctl_h, b->ctl_d, sizeof(int) * 2, cudaMemcpyDeviceToHost, b->st));
+  CK(cudaMemcpyAsync(b->err_h, b->err_d, sizeof(int) * n, cudaMemcpyDeviceToHost, b->st));
+  for (int i = 0; i < n; i++) {
+    mth_ctx* c = b->rve[i];
+    CK(cudaMemcpyAsync(&c->bk, c->bk_d, sizeof(IterBook), cudaMemcpyDeviceToHost, b->st));
+    b->live_h[i] = 1;
+  }
+  CK(cudaMemcpyAsync(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
+  CK(cudaStreamSynchronize(b->st));
+  for (int i = 0; i < n; i++)
+    if (b->err_h[i]) return set_err(MTH_ERR_TIMEOUT, "batch member %d: a kernel timed out waiting for its tile copies", i);
+  if (b->ctl_h[1]) return set_err(MTH_ERR_CUDA, "batch: the iteration loop reached its bound");
+  for (int i = 0; i < n; i++)
+    if (b->rve[i]->bk.nan)
+      return set_err(MTH_ERR_NAN, "batch member %d: non-finite value in the Green iteration (step %d, iteration %d)", i,
+                     b->rve[i]->istep, b->rve[i]->bk.it_iter);
   for (int i = 0; i < n; i++) {
     mth_status s = step_end(b->rve[i], reports ? &reports[i] : nullptr);
     if (s) return s;
