@@ -730,8 +730,8 @@ def run_batch(args):
                       "voxels": int(sum(np.prod(c.cell_dim) for c in cfgs_all)), "batch_create_s": t_create,
                       "parallelism": ("members dealt over %d ranks by voxel count, one batch per rank, no "
                                       "data-path collective" % ws) if ws > 1 else "single GPU",
-                      "timing": "host wall clock around whole batch steps (graph launches + host convergence "
-                                "logic), device synchronised on both sides",
+                      "timing": "host wall clock around whole batch steps (one graph launch per step + host "
+                                "bookkeeping), device synchronised on both sides",
                       "fft_passes": passes},
            "clocks": clk}
     if not args.no_fp64 and ws == 1:
