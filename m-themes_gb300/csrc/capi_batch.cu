@@ -25,11 +25,9 @@ struct mth_batch {
   std::vector<cudaEvent_t> join;
   cudaEvent_t fork = nullptr;
   double* add_d = nullptr;
-  double* add_h = nullptr;
   int* live_d = nullptr;
   int* live_h = nullptr;
   double* red_d = nullptr;
-  double* red_h = nullptr;
   int* err_d = nullptr;
   int* err_h = nullptr;
   int* ctl_d = nullptr;   // iterations the step's loop ran, and whether it hit its bound
@@ -55,9 +53,7 @@ void batch_free(mth_batch* b) {
   cudaFree(b->err_d);
   cudaFree(b->ctl_d);
   if (b->ctl_h) cudaFreeHost(b->ctl_h);
-  if (b->add_h) cudaFreeHost(b->add_h);
   if (b->live_h) cudaFreeHost(b->live_h);
-  if (b->red_h) cudaFreeHost(b->red_h);
   if (b->err_h) cudaFreeHost(b->err_h);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -261,15 +257,12 @@ extern "C" mth_status mth_batch_create(const mth_params* params, int n, mth_batc
     ck(cudaMalloc(&b->err_d, sizeof(int) * n));
     ck(cudaMalloc(&b->ctl_d, sizeof(int) * 2));
     ck(cudaMallocHost(&b->ctl_h, sizeof(int) * 2));
-    ck(cudaMallocHost(&b->add_h, sizeof(double) * 8 * n));
     ck(cudaMallocHost(&b->live_h, sizeof(int) * n));
-    ck(cudaMallocHost(&b->red_h, sizeof(double) * BATCH_RED * n));
     ck(cudaMallocHost(&b->err_h, sizeof(int) * n));
   }
   if (!s) {
     ck(cudaMemset(b->add_d, 0, sizeof(double) * 8 * n));
     ck(cudaMemset(b->err_d, 0, sizeof(int) * n));
-    memset(b->add_h, 0, sizeof(double) * 8 * n);
     memset(b->err_h, 0, sizeof(int) * n);
     for (int i = 0; i < n; i++) b->live_h[i] = 1;
     ck(cudaMemcpy(b->live_d, b->live_h, sizeof(int) * n, cudaMemcpyHostToDevice));
