@@ -1103,6 +1103,9 @@ void fill_float_consts(NewtonConst& nc) {
 #ifndef MTH_FAST_MINB
 #define MTH_FAST_MINB 3
 #endif
+#ifndef MTH_FP64_MINB
+#define MTH_FP64_MINB 1   // FP64 mode: 1.01e8 with 1 (255 registers) against 0.99e8 with 2 (128, 516 B of spills)
+#endif
 cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* fields, double* partials, int nblocks,
                           const IterIn& it, cudaStream_t st, int law) {
   NewtonConst nc = nc_in;
@@ -1134,8 +1137,8 @@ cudaError_t launch_newton(int mixed, const NewtonConst& nc_in, const void* field
     return launch_coop<MTH_COOP_MINB, 0>(nc, f, partials, nblocks, it, st);
   } else {
     const Fields<double>& f = *static_cast<const Fields<double>*>(fields);
-    return launch_chain(newton_kernel<double, double, double, 1>, dim3(nblocks), dim3(256), 0, st, it.pdl, nc, f,
-                        partials, it);
+    return launch_chain(newton_kernel<double, double, double, MTH_FP64_MINB>, dim3(nblocks), dim3(256), 0, st, it.pdl,
+                        nc, f, partials, it);
   }
   return cudaGetLastError();
 }
