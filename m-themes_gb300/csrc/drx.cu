@@ -849,10 +849,14 @@ cudaError_t launch_pf_relax(const int dims[3], const int* grain, const T* rho, i
     const T* phi = b.phi[cur];
     const uint8_t* cnt = b.cnt[cur];
     PF_K_LAUNCH(pf_nlist_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.word));
-    // update flags to their fixed point (in place)
+    // update flags to their fixed point (in place), two passes between
+    // reads of the change counter (a pass at the fixed point changes
+    // nothing, so a second one costs only its launch); the counter read is
+    // the second pass's
     PF_CK(cudaMemsetAsync(b.upd[0], 0, (size_t)nv, st));
     const int a = 0;
-    for (long long it = 0; it <= nv; it++) {
+    for (long long it = 0; it <= nv; it += 2) {
+      PF_K_LAUNCH(pf_upd_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.upd[a], b.word));
       PF_CK(cudaMemsetAsync(b.word, 0, sizeof(unsigned), st));
       PF_K_LAUNCH(pf_upd_kernel<T><<<nb(nv, 256), 256, 0, st>>>(g, ids, phi, cnt, b.nid, b.ncnt, b.upd[a], b.word));
       PF_CK(pf_read_counter(b.word, &changed, st));
