@@ -515,7 +515,7 @@ def adjoint_measure(dev_index, name="c4"):
 
 
 def adjoint_fd_check(dev_index, err=None, iter_max=None, n_steps=None):
-    """The calibration gradient of configs[4] (64^3, 256 grains, 50 steps)
+    """The calibration gradient of the 64^3 calibration workload (256 grains, 50 steps)
     against central finite differences with relative step 1e-4 of the FP64
     forward, for all five parameters: the FP64 adjoint and the mixed one.
     err / iter_max override the workload's Err 1e-5 / IterMax 100 (the
@@ -765,7 +765,7 @@ def main():
         # the calibration gradient alone (the adjoint block of the default line)
         print(json.dumps({"workload": "c4", "adjoint": adjoint_measure(0)}), flush=True)
     elif args.workload == "c4fd":
-        # the calibration gradient against central finite differences (configs[4], all five parameters)
+        # the calibration gradient against central finite differences (64^3 calibration workload, all five parameters)
         print(json.dumps({"workload": "c4fd", "adjoint_fd": adjoint_fd_check(
             0, err=args.err or None, iter_max=args.iter_max or None, n_steps=args.fd_steps or None)}), flush=True)
     elif args.workload == "c1dd":

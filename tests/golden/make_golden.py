@@ -152,7 +152,7 @@ def main_test_run():
     print("test_run: iterations", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
 
 
-# The configs[0] workload at its stated size: 32^3, 64 seeded Voronoi grains,
+# The 32^3 FP64 workload at its stated size: 64 seeded Voronoi grains,
 # Cu power law + Voce, uniaxial tension, 10 steps, IterMax 100, Err 1e-5.
 # The input declares two phases (the second unused): with N_phases 1 the
 # reference reads nSYS[1] past its one-element allocation in SetupJob
@@ -165,7 +165,7 @@ SAMPLE_VOXELS = np.arange(0, 32 ** 3, 32 ** 3 // 64)
 def main_configs():
     ref = os.path.join(REPO, "oracle", "_ref", "forge_ref")
     cfg = synth.workload("c0")
-    d = "/tmp/mth_golden_cfg0"
+    d = "/tmp/mth_golden_fp64_32cube"
     synth.write_case(d, cfg)
     inp = os.path.join(d, "input.in")
     txt = open(inp).read().replace("N_phases\t1\n", "N_phases\t2\n")
@@ -175,10 +175,10 @@ def main_configs():
     trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))
     nv = int(np.prod(cfg.cell_dim))
     sig = np.fromfile(os.path.join(d, "sig.bin")).reshape(nv, 9)
-    out = os.path.join(HERE, "cfg0_c0.npz")
+    out = os.path.join(HERE, "fp64_32cube_trace.npz")
     np.savez_compressed(out, config=cfg_to_json(cfg), trace=trace, sig_norm=np.linalg.norm(sig, axis=0),
                         sample_voxels=SAMPLE_VOXELS, sig_sample=sig[SAMPLE_VOXELS])
-    print("cfg0_c0", trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
+    print("fp64_32cube_trace", trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
 
 
 # The reference's own field files: with PrintControl 1 it writes, at the end

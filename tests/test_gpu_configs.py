@@ -1,11 +1,11 @@
-"""GPU parity at the configurations' stated sizes, not only on small cases.
+"""GPU parity at the workloads' stated sizes, not only on small cases.
 
-* configs[0] exactly (32^3, 64 grains, 10 steps, IterMax 100, Err 1e-5)
-  against the trace the reference itself wrote (tests/golden/cfg0_c0.npz):
+* the 32^3 FP64 workload exactly (64 grains, 10 steps, IterMax 100, Err 1e-5)
+  against the trace the reference itself wrote (tests/golden/fp64_32cube_trace.npz):
   FP64 within 1e-6 relative on <sigma>, <grad u> and s_vm at every step with
   the same Green-iteration counts; mixed precision within 1e-4 on <sigma>.
 * 64^3 (256 grains), 5 steps, FP64 against the oracle on all host cores.
-* 128^3 configs[1] (512 grains, 40 pores), 2 steps of 5 Green iterations:
+* the 128^3 benchmark workload (512 grains, 40 pores), 2 steps of 5 Green iterations:
   FP64 within 1e-6 and mixed within 1e-4 of the oracle's FP64.
 """
 import json
@@ -20,8 +20,8 @@ from mth import capi, synth
 pytestmark = pytest.mark.gpu
 
 
-def cfg0():
-    z = np.load(os.path.join(GOLDEN, "cfg0_c0.npz"))
+def fp64_32cube():
+    z = np.load(os.path.join(GOLDEN, "fp64_32cube_trace.npz"))
     d = json.loads(str(z["config"]))
     d["material"] = synth.Material(**d["material"])
     for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
@@ -29,8 +29,8 @@ def cfg0():
     return synth.Config(**d), z
 
 
-def test_configs0_fp64_matches_reference():
-    cfg, z = cfg0()
+def test_32cube_fp64_matches_reference():
+    cfg, z = fp64_32cube()
     assert cfg.cell_dim == (32, 32, 32) and cfg.n_grains == 64 and cfg.n_steps == 10 and cfg.iter_max == 100
     s, reps = run_gpu(cfg, capi.MTH_FP64)
     for k, r in enumerate(reps):
@@ -46,8 +46,8 @@ def test_configs0_fp64_matches_reference():
     s.close()
 
 
-def test_configs0_mixed_within_1e4_of_reference():
-    cfg, z = cfg0()
+def test_32cube_mixed_within_1e4_of_reference():
+    cfg, z = fp64_32cube()
     s, reps = run_gpu(cfg, capi.MTH_MIXED)
     for k, r in enumerate(reps):
         assert rel(r["sig_avg"], z["trace"][k][T_SIG].reshape(3, 3)) < 1e-4, k
@@ -68,7 +68,7 @@ def test_64cube_fp64_matches_oracle():
     o.close()
 
 
-def test_128cube_configs1_matches_oracle():
+def test_128cube_benchmark_matches_oracle():
     cfg = synth.workload("c1")
     cfg.n_steps, cfg.iter_max = 2, 5
     o, oreps = run_oracle(cfg, nthreads=os.cpu_count())

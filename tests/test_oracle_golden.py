@@ -61,15 +61,15 @@ def test_oracle_matches_reference_dd_trace(name):
         assert rel(o.field("rho_gnd"), fields["rho_gnd"]) < 1e-10
 
 
-def test_oracle_matches_reference_at_configs0_size():
-    """configs[0] as stated: 32^3, 64 grains, 10 steps, IterMax 100, Err 1e-5
+def test_oracle_matches_reference_at_32cube_size():
+    """The 32^3 FP64 workload as stated: 64 grains, 10 steps, IterMax 100, Err 1e-5
     (every step runs its 100 Green iterations); per-step trace and a summary
     of the final stress field (component norms and 64 sampled voxels)."""
     import json
     import os
     from helpers import GOLDEN
     from mth import synth
-    z = np.load(os.path.join(GOLDEN, "cfg0_c0.npz"))
+    z = np.load(os.path.join(GOLDEN, "fp64_32cube_trace.npz"))
     d = json.loads(str(z["config"]))
     d["material"] = synth.Material(**d["material"])
     for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
