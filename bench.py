@@ -46,10 +46,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--precision", choices=["mixed", "fp64", "mixed_fast", "mixed_root64"], default="mixed")
-    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--workload", default="rve128")
     ap.add_argument("--iter-max", type=int, default=0, help="override IterMax (default: the workload's 100)")
-    ap.add_argument("--err", type=float, default=0.0, help="override Err (c4fd only; default: the workload's 1e-5)")
-    ap.add_argument("--fd-steps", type=int, default=0, help="override the mechanical steps (c4fd only; default 50)")
+    ap.add_argument("--err", type=float, default=0.0, help="override Err (calib64_fd only; default: the workload's 1e-5)")
+    ap.add_argument("--fd-steps", type=int, default=0, help="override the mechanical steps (calib64_fd only; default 50)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -377,13 +377,13 @@ def run_gpu(args):
 
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_sample(cfg)
-    if not args.no_adjoint and args.workload == "c1":
+    if not args.no_adjoint and args.workload == "rve128":
         out["adjoint"] = adjoint_measure(dev_index)
-    if not args.no_dd and args.workload == "c1":
+    if not args.no_dd and args.workload == "rve128":
         out["dislocation_density"] = dd_measure(dev_index, args)
-    if not args.no_drx and args.workload == "c1":
+    if not args.no_drx and args.workload == "rve128":
         out["drx"] = drx_measure(dev_index, args)
-    if not args.no_batch and args.workload == "c1" and ws == 1:
+    if not args.no_batch and args.workload == "rve128" and ws == 1:
         out["batch"] = batch_measure(dev_index)
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -400,7 +400,7 @@ def dd_measure(dev_index, args):
     import dataclasses
     import torch
     from mth import Solver, capi, synth
-    cfg = dataclasses.replace(synth.workload("c1"), dd=synth.DD())
+    cfg = dataclasses.replace(synth.workload("rve128"), dd=synth.DD())
     par = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
     par.device = dev_index
     nv = int(np.prod(cfg.cell_dim))
@@ -423,7 +423,7 @@ def dd_measure(dev_index, args):
             "dd_avg_last_step": [float(x) for x in reps[-1]["dd_avg"]]}
 
 
-# ------------------------------------------- coupled recrystallisation (c2)
+# ------------------------------------------- coupled recrystallisation (drx128)
 def drx_measure(dev_index, args):
     """The coupled EVPFFT + sparse phase-field workload at 128^3 (1000 grains,
     compression, 10 PF substeps per mechanical step, nucleation every step
@@ -432,7 +432,7 @@ def drx_measure(dev_index, args):
     reference medium) inside the timed region, after two warm-up steps."""
     import torch
     from mth import Solver, capi, synth
-    cfg = synth.workload("c2f")
+    cfg = synth.workload("drx128_each")
     par = capi.params_from_config(cfg, precision=capi.MTH_MIXED)
     par.device = dev_index
     nv = int(np.prod(cfg.cell_dim))
@@ -466,7 +466,7 @@ def drx_measure(dev_index, args):
 
 
 # ------------------------------------------------------ calibration adjoint
-def adjoint_measure(dev_index, name="c4"):
+def adjoint_measure(dev_index, name="calib64"):
     """Cost of the calibration gradient (mth_adjoint: forward sweep with
     stored states every 10 steps, recomputation, reverse sweep) against a
     plain forward run of the same 64^3 / 256-grain, 50-step tension, mixed
@@ -523,7 +523,7 @@ def adjoint_fd_check(dev_index, err=None, iter_max=None, n_steps=None):
     the forward as it stops)."""
     import dataclasses
     from mth import Solver, capi, synth
-    cfg = synth.workload("c4")
+    cfg = synth.workload("calib64")
     if err is not None:
         cfg = dataclasses.replace(cfg, err=err)
     if iter_max is not None:
@@ -629,13 +629,13 @@ def run_reference(args):
 
 
 def batch_measure(dev_index, steps=2, warmup=3):
-    """The 64-RVE batch (the c3 workload) on this GPU, mixed precision:
+    """The 64-RVE batch (the batch64 workload) on this GPU, mixed precision:
     whole-batch voxel-iterations/s over `steps` mechanical steps after
     `warmup`, the tile widths the batch chose per grid, and one Solver per
     RVE stepped in turn on the same steps."""
     import torch
     from mth import Batch, Solver, capi, synth
-    cfgs = synth.batch_workload("c3")
+    cfgs = synth.batch_workload("batch64")
     params = [capi.params_from_config(c, precision=capi.MTH_MIXED) for c in cfgs]
     for p in params:
         p.device = dev_index
@@ -759,18 +759,18 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload in ("c3", "c3s"):
+    elif args.workload in ("batch64", "batch6"):
         run_batch(args)
-    elif args.workload == "c4":
+    elif args.workload == "calib64":
         # the calibration gradient alone (the adjoint block of the default line)
-        print(json.dumps({"workload": "c4", "adjoint": adjoint_measure(0)}), flush=True)
-    elif args.workload == "c4fd":
+        print(json.dumps({"workload": "calib64", "adjoint": adjoint_measure(0)}), flush=True)
+    elif args.workload == "calib64_fd":
         # the calibration gradient against central finite differences (64^3 calibration workload, all five parameters)
-        print(json.dumps({"workload": "c4fd", "adjoint_fd": adjoint_fd_check(
+        print(json.dumps({"workload": "calib64_fd", "adjoint_fd": adjoint_fd_check(
             0, err=args.err or None, iter_max=args.iter_max or None, n_steps=args.fd_steps or None)}), flush=True)
-    elif args.workload == "c1dd":
+    elif args.workload == "dd128":
         # the dislocation-density law alone (the dislocation_density block of the default line)
-        print(json.dumps({"workload": "c1dd", "dislocation_density": dd_measure(0, args)}), flush=True)
+        print(json.dumps({"workload": "dd128", "dislocation_density": dd_measure(0, args)}), flush=True)
     else:
         run_gpu(args)
 

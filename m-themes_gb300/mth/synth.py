@@ -313,44 +313,44 @@ def write_case(directory, cfg: Config):
 
 # ------------------------------------------------------ named workloads
 def workload(name: str) -> Config:
-    """Benchmark workloads: 'c0' = 32^3 / 64 grains FP64 plain EVPFFT, 10 steps;
-    'c1' = 128^3 / 512 grains + 40 radius-3 pores, 100 steps; 'c1m' = the same at 96^3
+    """Benchmark workloads: 'fp64_32cube' = 32^3 / 64 grains FP64 plain EVPFFT, 10 steps;
+    'rve128' = 128^3 / 512 grains + 40 radius-3 pores, 100 steps; 'rve96' = the same at 96^3
     (216 grains, 17 pores) for profiler captures."""
-    if name == "c0":
+    if name == "fp64_32cube":
         return Config(cell_dim=(32, 32, 32), n_grains=64, n_steps=10, seed=20240101)
-    if name == "c1":
+    if name == "rve128":
         return Config(cell_dim=(128, 128, 128), n_grains=512, n_pores=40, pore_radius=3,
                       n_steps=100, seed=20240102)
-    if name == "c2":    # coupled EVPFFT + sparse phase-field DRX, compression to true strain 0.5
+    if name == "drx128":    # coupled EVPFFT + sparse phase-field DRX, compression to true strain 0.5
         return Config(cell_dim=(128, 128, 128), n_grains=1000, n_steps=500, seed=20240104,
                       velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0), drx=Drx())
-    if name == "c2s":   # 64^3 profiling case of c2: nucleation from the second step on
+    if name == "drx64":   # 64^3 profiling case of drx128: nucleation from the second step on
         return Config(cell_dim=(64, 64, 64), n_grains=125, n_steps=10, seed=20240105, iter_max=10,
                       velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0),
                       drx=Drx(rho_k=40000.0, nucleation_prob=2e-3))
-    if name == "c2f":   # c2 with nucleation from the second step on: the DRX step at 128^3 every step
+    if name == "drx128_each":   # drx128 with nucleation from the second step on: the DRX step at 128^3 every step
         return Config(cell_dim=(128, 128, 128), n_grains=1000, n_steps=500, seed=20240104,
                       velgrad_bc=(0.5, 0.5, -1.0, 0.0, 0.0, 0.0), drx=Drx(rho_k=40000.0, nucleation_prob=2e-4))
-    if name == "c4":    # adjoint calibration: 64^3, 256 grains, tension for 50 steps of 1e-3
+    if name == "calib64":    # adjoint calibration: 64^3, 256 grains, tension for 50 steps of 1e-3
         return Config(cell_dim=(64, 64, 64), n_grains=256, n_steps=50, seed=20240107)
-    if name == "c4s":   # small case of c4 for tests: 16^3, 8 grains, 5 steps
+    if name == "calib16":   # small case of calib64 for tests: 16^3, 8 grains, 5 steps
         return Config(cell_dim=(16, 16, 16), n_grains=8, n_steps=5, seed=777)
-    if name == "c1m":   # 96^3 profiling case of c1: fields still larger than L2
+    if name == "rve96":   # 96^3 profiling case of rve128: fields still larger than L2
         return Config(cell_dim=(96, 96, 96), n_grains=216, n_pores=17, pore_radius=3,
                       n_steps=100, seed=20240103)
     raise KeyError(name)
 
 
-def batch_workload(name: str = "c3", master_seed: int = 20240106) -> list:
-    """Batched-RVE workloads.  'c3': 64 independent RVEs, 24 x 32^3, 24 x 48^3
+def batch_workload(name: str = "batch64", master_seed: int = 20240106) -> list:
+    """Batched-RVE workloads.  'batch64': 64 independent RVEs, 24 x 32^3, 24 x 48^3
     and 16 x 64^3; RVE i has seed master + i, a grain count drawn uniformly
     from [32, 256], uniform orientations, tau0 ~ U[12, 20] MPa (forward and
     backward CRSS) and n drawn from {8, 10, 15, 20}; uniaxial tension for 50
-    steps of 1e-3.  'c3s': the first 2 RVEs of each size (6), for tests."""
+    steps of 1e-3.  'batch6': the first 2 RVEs of each size (6), for tests."""
     sizes = [32] * 24 + [48] * 24 + [64] * 16
-    if name == "c3s":
+    if name == "batch6":
         sizes = [32, 32, 48, 48, 64, 64]
-    elif name != "c3":
+    elif name != "batch64":
         raise KeyError(name)
     out = []
     for i, n in enumerate(sizes):

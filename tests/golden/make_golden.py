@@ -164,7 +164,7 @@ SAMPLE_VOXELS = np.arange(0, 32 ** 3, 32 ** 3 // 64)
 
 def main_configs():
     ref = os.path.join(REPO, "oracle", "_ref", "forge_ref")
-    cfg = synth.workload("c0")
+    cfg = synth.workload("fp64_32cube")
     d = "/tmp/mth_golden_fp64_32cube"
     synth.write_case(d, cfg)
     inp = os.path.join(d, "input.in")

@@ -65,7 +65,7 @@ def test_batch_matches_single_solvers(precision, tol):
 def test_batch_workload_small():
     """The 6-member slice of the 64-RVE workload: steps run, reports finite,
     the imposed strain rate reached by every member."""
-    cfgs = synth.batch_workload("c3s")
+    cfgs = synth.batch_workload("batch6")
     params = [capi.params_from_config(c, precision=capi.MTH_MIXED) for c in cfgs]
     micro = [synth.microstructure(c) for c in cfgs]
     with Batch(params, micro) as b:
@@ -83,7 +83,7 @@ def test_batch_members_match_the_oracle():
     the oracle (the reference's algorithm restated) run on each alone."""
     import os
     import pyoracle
-    cfgs = synth.batch_workload("c3")
+    cfgs = synth.batch_workload("batch64")
     pick = {}
     for c in cfgs:
         pick.setdefault(c.cell_dim, c)

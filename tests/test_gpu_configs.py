@@ -69,7 +69,7 @@ def test_64cube_fp64_matches_oracle():
 
 
 def test_128cube_benchmark_matches_oracle():
-    cfg = synth.workload("c1")
+    cfg = synth.workload("rve128")
     cfg.n_steps, cfg.iter_max = 2, 5
     o, oreps = run_oracle(cfg, nthreads=os.cpu_count())
     sig_o = o.field("sig")

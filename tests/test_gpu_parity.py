@@ -142,7 +142,7 @@ def test_deterministic(precision):
 def test_fullsize_mixed_properties():
     """128^3, 512 grains, 40 pores: the benchmark workload for 2 steps of 6
     Green iterations; size-independent checks."""
-    cfg = synth.workload("c1")
+    cfg = synth.workload("rve128")
     cfg.n_steps = 2
     cfg.iter_max = 6
     g, p, e = synth.microstructure(cfg)

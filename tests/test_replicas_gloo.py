@@ -65,7 +65,7 @@ def _batch_worker(rank, world, port, out):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    sizes = [int(np.prod(c.cell_dim)) for c in synth.batch_workload("c3")]
+    sizes = [int(np.prod(c.cell_dim)) for c in synth.batch_workload("batch64")]
     mine = replicas.batch_share(sizes, rank, world)
     vox_it = float(sum(sizes[i] for i in mine) * 100)   # 100 Green iterations per member
     tot, mx, val = replicas.aggregate(vox_it, 1.0 + 0.5 * rank)
@@ -82,7 +82,7 @@ def test_batch_partition_two_ranks():
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "m-themes_gb300"))
     from mth import synth
-    sizes = [int(np.prod(c.cell_dim)) for c in synth.batch_workload("c3")]
+    sizes = [int(np.prod(c.cell_dim)) for c in synth.batch_workload("batch64")]
     ctx = mp.get_context("spawn")
     with ctx.Manager() as m:
         out = m.dict()
