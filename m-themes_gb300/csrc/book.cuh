@@ -4,12 +4,13 @@
 // the error norms (src/evolution.c:1430-1455) and get_smacro
 // (src/evolution.c:473-547: volume-averaged stress, the mixed-boundary
 // strain correction, von Mises measures).  The host runs it in the batch
-// and the adjoint; mth_step runs it in a one-thread kernel after each
+// and the adjoint; mth_step runs it in a one-warp kernel after each
 // iteration, so iterations follow one another on the device without a host
 // round trip.  Both builds compile it without FMA contraction; the basic
 // operations and sqrt are correctly rounded on both, so the two give the
 // same doubles.
 #pragma once
+#include <cmath>
 #include "mth_common.cuh"
 
 #ifdef __CUDACC__
@@ -60,6 +61,14 @@ MTH_HD inline void book_v2t(const double* v, double t[3][3], int nv) {
       for (int i = 0; i < nv; i++) s += v[i] * book_basis(i, m, n);
       t[m][n] = s;
     }
+}
+
+MTH_HD inline bool book_finite(double x) {
+#ifdef __CUDA_ARCH__
+  return isfinite(x);
+#else
+  return std::isfinite(x);
+#endif
 }
 
 // another iteration: IterMax not reached and Err not met
@@ -130,7 +139,7 @@ MTH_HD inline void book_smacro(IterBook& b, const double* red) {
 // the end of an iteration; false (and nan set) on a non-finite sum
 MTH_HD inline bool book_finish(IterBook& b, const double* red, int npart) {
   for (int i = 0; i < npart; i++)
-    if (!isfinite(red[i])) {
+    if (!book_finite(red[i])) {
       b.nan = 1;
       return false;
     }

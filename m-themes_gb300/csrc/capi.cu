@@ -1333,7 +1333,7 @@ extern "C" mth_status mth_step(mth_ctx* c, mth_step_report* rep) {
   mth_status s = step_begin(c);
   if (s) return s;
   // The iterations run with their bookkeeping on the device (book.cu): each
-  // iteration's kernels, its reduction and the one-thread bookkeeping
+  // iteration's kernels, its reduction and the one-warp bookkeeping
   // kernel, which computes the next iteration's strain increment or drops
   // the live flag; the host queues groups of iterations and reads the flag
   // once per group, so the iterations follow one another without a host

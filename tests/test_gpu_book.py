@@ -1,7 +1,7 @@
 """The per-iteration bookkeeping of the Green iteration (book.cuh: error
 norms, get_smacro's volume averages and mixed-boundary strain correction,
 the next iteration's strain increment, the convergence test) runs in a
-one-thread kernel in mth_step, so that iterations follow one another
+one-warp kernel in mth_step, so that iterations follow one another
 without a host round trip.  With MTH_HOST_BOOK=1 the same code runs on the
 host after every iteration.  Both must give the same doubles: equal
 reports and bit-identical fields, in FP64 and mixed precision, for steps
