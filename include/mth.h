@@ -160,7 +160,8 @@ typedef enum {
   MTH_FIELD_GRAIN = 7,    /* 1: grain id (as double) */
   MTH_FIELD_RHO = 8,      /* 1: total dislocation density */
   MTH_FIELD_RHO_SSD = 9,  /* 12: statistically stored density per system (dislocation-density law) */
-  MTH_FIELD_RHO_GND = 10  /* 36: GND densities per system: screw (12), edge I (12), edge II (12) */
+  MTH_FIELD_RHO_GND = 10, /* 36: GND densities per system: screw (12), edge I (12), edge II (12) */
+  MTH_FIELD_DISGRAD = 11  /* 9: displacement gradient grad u (DisGrad, 3x3 row-major); needs mth_track_disgrad */
 } mth_field;
 
 /* Library */
@@ -188,6 +189,16 @@ mth_status mth_upload_microstructure(mth_ctx* ctx, const int* grain, const int* 
 mth_status mth_step(mth_ctx* ctx, mth_step_report* report);
 /* Copy a field to host memory as doubles (count = voxels * components). */
 mth_status mth_download_field(mth_ctx* ctx, int field, double* host, size_t count);
+/* Keep the full displacement gradient DisGrad (src/evolution.c:1319-1405),
+ * for MTH_FIELD_DISGRAD and MTH_IOUT_DISGRAD.  The strain field holds its
+ * symmetric part; with tracking on, each step also accumulates the
+ * antisymmetric part (3 planes per voxel: the step's uniform rotation
+ * increment and the local one from the Green operator's antisymmetric
+ * part), at the cost of one inverse transform of 3 components per step.
+ * Switch it on after mth_upload_microstructure and before the first
+ * mth_step (MTH_ERR_STATE otherwise); on = 0 switches it off and frees the
+ * planes.  mth_adjoint refuses a context that tracks it. */
+mth_status mth_track_disgrad(mth_ctx* ctx, int on);
 mth_status mth_destroy(mth_ctx* ctx);
 
 /* Batch local solve: the per-voxel Newton of UpdateStress
@@ -257,13 +268,14 @@ mth_status mth_nucleate(const mth_params* params, const int cell_dim[3], int* gr
  * Its only scratch (per-block partial sums) is a fixed array in the library's
  * device image, held by every GPU that loads the library until the process
  * exits; n may not exceed MTH_NOALLOC_MAX_VOXELS (MTH_ERR_ARG otherwise).
- * The first call on each device looks up that array's device address, so
- * make it before any stream capture; a cudaDeviceReset by the caller
- * invalidates the address the library keeps.  All calls share the array:
- * calls that overlap on the GPU (different streams or threads) race, so
- * serialise them.  stream: a cudaStream_t passed as void* (NULL = the
- * default stream); the call synchronises the stream and returns after it has
- * finished the solve (newton_iters is read back from the device).  The
+ * The first call on each device looks up that array's device address; a
+ * cudaDeviceReset by the caller invalidates the address the library keeps.
+ * All calls share the array: calls that overlap on the GPU (different
+ * streams or threads) race, so serialise them.  stream: a cudaStream_t
+ * passed as void* (NULL = the default stream); the call synchronises the
+ * stream and returns after it has finished the solve (newton_iters is read
+ * back from the device), so it cannot be made while the stream (or, for
+ * NULL, any stream) is being captured into a graph.  The
  * solve runs on params->device; the caller's current device is the same
  * after the call as before it. */
 #define MTH_NOALLOC_MAX_VOXELS (1LL << 20)
@@ -277,6 +289,9 @@ mth_status mth_local_solve_noalloc(const mth_params* params, const double c066[3
  *   MTH_IOUT_SIG, _EPS (plastic strain), _EDOT, _ELS (elastic strain
  *   sym(grad u) - eps_p, WriteElsMPI): six files "<prefix>_<c>_S<step>.iout"
  *   of doubles, c = 1..6 for the components 11, 22, 33, 23, 13, 12;
+ *   MTH_IOUT_DISGRAD: six files as above of the displacement gradient's
+ *   entries 11, 22, 33, 23, 13, 12 (WriteDisgradMPI, src/io.c:283-320;
+ *   needs mth_track_disgrad);
  *   MTH_IOUT_GRAIN: "<prefix>_S<step>.iout", int32 grain ids (WriteGrainMPI);
  *   MTH_IOUT_TEXTURE: "<prefix>_S<step>.iout", 48-byte records {double
  *   Bunge angles in degrees [3]; int 1-based coordinates [3]; int grain;
@@ -293,7 +308,8 @@ typedef enum {
   MTH_IOUT_EDOT = 2,
   MTH_IOUT_ELS = 3,
   MTH_IOUT_GRAIN = 4,
-  MTH_IOUT_TEXTURE = 5
+  MTH_IOUT_TEXTURE = 5,
+  MTH_IOUT_DISGRAD = 6
 } mth_iout_kind;
 mth_status mth_write_iout(mth_ctx* ctx, int kind, const char* prefix, int step);
 mth_status mth_iout_wait(mth_ctx* ctx);

@@ -279,6 +279,7 @@ void ctx_free(mth_ctx* c) {
   cudaFree(c->fieldmem);
   cudaFree(c->spec);
   cudaFree(c->anti);
+  cudaFree(c->skew_d);
   tma_destroy(c->tma);
   if (!c->in_batch) {
     cudaFree(c->err_d);
@@ -933,6 +934,11 @@ extern "C" mth_status mth_upload_microstructure(mth_ctx* c, const int* grain, co
   CK(cudaStreamSynchronize(c->st));
   prof_resolve(c);
   cudaFree(eul_d);
+  if (c->skew_d) {
+    const size_t esz = c->mixed ? sizeof(float) : sizeof(double);
+    CK(cudaMemsetAsync(c->skew_d, 0, 3 * esz * c->nv, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
   c->uploaded = 1;
   c->istep = 0;
   return MTH_OK;
@@ -1246,7 +1252,7 @@ mth_status step_end(mth_ctx* c, mth_step_report* rep) {
   memcpy(c->disgrad_avg_t, actual, sizeof(t33));
   const int do_orient = (c->p.update_flag == 1 && istep > 1);
   const int do_harden = (c->p.hard_flag == 1);
-  if (do_orient) {
+  if (do_orient || c->skew_d) {
     mth_status s = c->mixed ? spin_field<float>(c) : spin_field<double>(c);
     if (s) return s;
   }
@@ -1266,6 +1272,19 @@ mth_status step_end(mth_ctx* c, mth_step_report* rep) {
   }
   for (int i = 0; i < 3; i++) c->last_au[i] = au[i];
   const void* f = c->mixed ? (const void*)&c->ff : (const void*)&c->fd;
+  if (c->skew_d) {
+    // DisGrad's antisymmetric part: the step's uniform increment, the
+    // antisymmetric part of Udot dt plus that of the applied corrections,
+    // and the local part in wspin
+    t33 w;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        w[i][j] = c->udot_a[i][j] * dt + 0.5 * (c->bk.ddg_applied[i][j] - c->bk.ddg_applied[j][i]);
+    const double u[3] = {w[2][1], w[0][2], w[1][0]};
+    const double rp = (double)(c->mixed ? sizeof(float) : sizeof(double)) * (double)c->nv;
+    const void* wspin = c->mixed ? (const void*)c->ff.wspin : (const void*)c->fd.wspin;
+    LAUNCH(K_SPIN, 9 * rp, launch_disgrad_skew(c->mixed, wspin, c->skew_d, c->nv, u, c->st));
+  }
   if (c->dd) {
     // shear rates at the converged stress, then DislocationEvolution (with
     // the shear-rate gradients from the third step on when Hard_Flag = 1,
@@ -1397,7 +1416,8 @@ static mth_status download(mth_ctx* c, int field, double* host) {
     case MTH_FIELD_SIG: src = f.sig; nc = 6; break;
     case MTH_FIELD_EPS: src = f.epsp; nc = 6; break;
     case MTH_FIELD_EDOT: src = f.edot; nc = 6; break;
-    case MTH_FIELD_STRAIN: src = f.strain; nc = 6; break;
+    case MTH_FIELD_STRAIN:
+    case MTH_FIELD_DISGRAD: src = f.strain; nc = 6; break;
     case MTH_FIELD_ROT: src = f.rot; nc = 9; break;
     case MTH_FIELD_CRSS: src = f.crss; nc = 12; break;
     case MTH_FIELD_GAMACUM: src = f.gamacum; nc = 1; break;
@@ -1422,7 +1442,8 @@ static mth_status download(mth_ctx* c, int field, double* host) {
     CK(cudaMalloc(&c->dl_d, sizeof(double) * out));
     c->dl_cap = out;
   }
-  CK(launch_to_host_layout(c->mixed, src, P, nc, nc == 6 ? 1 : 0, c->dl_d, c->st));
+  if (field == MTH_FIELD_DISGRAD) CK(launch_disgrad_to_host(c->mixed, src, c->skew_d, P, c->dl_d, c->st));
+  else CK(launch_to_host_layout(c->mixed, src, P, nc, nc == 6 ? 1 : 0, c->dl_d, c->st));
   CK(cudaMemcpyAsync(host, c->dl_d, sizeof(double) * out, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   return MTH_OK;
@@ -1449,12 +1470,39 @@ extern "C" mth_status mth_download_field(mth_ctx* c, int field, double* host, si
     for (long long v = 0; v < c->nv; v++) host[v] = h[v];
     return MTH_OK;
   }
+  if (field == MTH_FIELD_DISGRAD && !c->skew_d)
+    return set_err(MTH_ERR_STATE, "DisGrad is kept only after mth_track_disgrad (before the first step)");
   const int ncomp = (field == MTH_FIELD_CRSS || field == MTH_FIELD_RHO_SSD) ? 12
                     : (field == MTH_FIELD_RHO_GND)                          ? 36
                     : (field == MTH_FIELD_GAMACUM || field == MTH_FIELD_RHO) ? 1
                                                                              : 9;
   if (count != (size_t)ncomp * c->nv) return set_err(MTH_ERR_ARG, "count=%zu, expected %lld", count, ncomp * c->nv);
   return c->mixed ? download<float>(c, field, host) : download<double>(c, field, host);
+}
+
+// The reference keeps the full displacement gradient DisGrad per voxel
+// (src/evolution.c:1319-1405); here the strain planes hold its symmetric
+// part, and the antisymmetric part (3 planes) is kept only on request.
+extern "C" mth_status mth_track_disgrad(mth_ctx* c, int on) {
+  if (!c) return set_err(MTH_ERR_ARG, "null context");
+  if (c->in_batch) return set_err(MTH_ERR_STATE, "context belongs to a batch");
+  SETDEV(c);
+  if (!on) {
+    if (c->skew_d) {
+      CK(cudaStreamSynchronize(c->st));
+      cudaFree(c->skew_d);
+      c->skew_d = nullptr;
+    }
+    return MTH_OK;
+  }
+  if (!c->uploaded || c->istep != 0)
+    return set_err(MTH_ERR_STATE, "mth_track_disgrad after mth_upload_microstructure and before the first step");
+  if (c->skew_d) return MTH_OK;
+  const size_t bytes = 3 * (c->mixed ? sizeof(float) : sizeof(double)) * (size_t)c->nv;
+  CK(cudaMalloc(&c->skew_d, bytes));
+  CK(cudaMemsetAsync(c->skew_d, 0, bytes, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return MTH_OK;
 }
 
 // ------------------------------------------------------------- profiling

@@ -252,6 +252,7 @@ extern "C" mth_status mth_adjoint(mth_ctx* c, const mth_adjoint_opts* o, double*
   if (!c->uploaded) return set_err(MTH_ERR_STATE, "mth_adjoint before mth_upload_microstructure");
   if (c->istep != 0) return set_err(MTH_ERR_STATE, "mth_adjoint needs a context at step 0 (it runs the forward solve)");
   if (c->in_batch) return set_err(MTH_ERR_STATE, "context belongs to a batch");
+  if (c->skew_d) return set_err(MTH_ERR_STATE, "mth_adjoint on a context that tracks DisGrad (its replays would add to it)");
   if (o->n_steps < 1 || !o->target) return set_err(MTH_ERR_ARG, "n_steps >= 1 and a target curve are required");
   if (c->drx) return set_err(MTH_ERR_UNSUPPORTED, "adjoint with phase-field DRX");
   if (c->dd) return set_err(MTH_ERR_UNSUPPORTED, "adjoint of the dislocation-density law");

@@ -150,6 +150,7 @@ struct mth_ctx {
   int nsys;
   int adj_solid;        // every voxel is of phase 1 and crystalline (adjoint precondition)
   double last_au[3];    // uniform spin increment of the last end of step
+  void* skew_d;         // DisGrad's antisymmetric part, planes (W21, W02, W10), while tracked (mth_track_disgrad)
   // dislocation-density law
   int dd;
   DdConst* ddc;         // phase-1 constants of the dislocation-density law (host; kernel parameters)

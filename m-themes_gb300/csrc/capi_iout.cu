@@ -114,9 +114,12 @@ static void iout_work(IoutWriter* w, int kind, std::string prefix, int step, lon
     if (!write_file(prefix + "_" + sfx, rec.data(), sizeof(TexRecord) * P, w->msg)) w->status = MTH_ERR_IO;
     return;
   }
-  // symmetric tensors: components 11, 22, 33, 23, 13, 12 (src/io.c:404-418)
+  // components 11, 22, 33, 23, 13, 12 (src/io.c:292-305, 404-418) of a
+  // symmetric tensor, or of DisGrad: the strain's plus the antisymmetric
+  // planes (W21, W02, W10), W23 = -W21, W13 = W02, W12 = -W10
   const T* a = static_cast<const T*>(w->stage_h);
   const T* b = kind == MTH_IOUT_ELS ? a + 6 * P : nullptr;   // ELS: strain - plastic strain
+  const T* sk = kind == MTH_IOUT_DISGRAD ? a + 6 * P : nullptr;
   static const int ci[6][2] = {{0, 0}, {1, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
   std::vector<double> comp((size_t)6 * P);
   for (long long v = 0; v < P; v++) {
@@ -125,6 +128,11 @@ static void iout_work(IoutWriter* w, int kind, std::string prefix, int step, lon
     for (int i = 0; i < 6; i++) s6[i] = (double)a[i * P + v] - (b ? (double)b[i * P + v] : 0.0);
     v2t(s6, t, 6);
     for (int c = 0; c < 6; c++) comp[c * P + v] = t[ci[c][0]][ci[c][1]];
+    if (sk) {
+      comp[3 * P + v] -= (double)sk[v];
+      comp[4 * P + v] += (double)sk[P + v];
+      comp[5 * P + v] -= (double)sk[2 * P + v];
+    }
   }
   for (int c = 0; c < 6; c++) {
     if (!write_file(prefix + "_" + std::to_string(c + 1) + "_" + sfx, comp.data() + c * P, sizeof(double) * P,
@@ -144,6 +152,7 @@ static mth_status iout_start(mth_ctx* c, int kind, const char* prefix, int step)
   switch (kind) {
     case MTH_IOUT_SIG: case MTH_IOUT_EPS: case MTH_IOUT_EDOT: bytes = 6 * P * w; break;
     case MTH_IOUT_ELS: bytes = 12 * P * w; break;
+    case MTH_IOUT_DISGRAD: bytes = 9 * P * w; break;
     case MTH_IOUT_GRAIN: bytes = sizeof(int) * P; break;
     case MTH_IOUT_TEXTURE: bytes = 9 * P * w + sizeof(int) * P + P; break;
     default: return set_err(MTH_ERR_ARG, "iout kind %d", kind);
@@ -181,6 +190,7 @@ static mth_status iout_start(mth_ctx* c, int kind, const char* prefix, int step)
     case MTH_IOUT_EPS: CK(snap(f.epsp, 6 * P * w)); break;
     case MTH_IOUT_EDOT: CK(snap(f.edot, 6 * P * w)); break;
     case MTH_IOUT_ELS: CK(snap(f.strain, 6 * P * w)); CK(snap(f.epsp, 6 * P * w)); break;
+    case MTH_IOUT_DISGRAD: CK(snap(f.strain, 6 * P * w)); CK(snap(c->skew_d, 3 * P * w)); break;
     case MTH_IOUT_GRAIN: CK(snap(c->grain_d, sizeof(int) * P)); break;
     case MTH_IOUT_TEXTURE:
       CK(snap(f.rot, 9 * P * w));
@@ -196,7 +206,9 @@ static mth_status iout_start(mth_ctx* c, int kind, const char* prefix, int step)
 extern "C" mth_status mth_write_iout(mth_ctx* c, int kind, const char* prefix, int step) {
   if (!c || !prefix) return set_err(MTH_ERR_ARG, "null argument");
   if (!c->uploaded) return set_err(MTH_ERR_STATE, "no microstructure uploaded");
-  if (kind < MTH_IOUT_SIG || kind > MTH_IOUT_TEXTURE) return set_err(MTH_ERR_ARG, "iout kind %d", kind);
+  if (kind < MTH_IOUT_SIG || kind > MTH_IOUT_DISGRAD) return set_err(MTH_ERR_ARG, "iout kind %d", kind);
+  if (kind == MTH_IOUT_DISGRAD && !c->skew_d)
+    return set_err(MTH_ERR_STATE, "DisGrad is kept only after mth_track_disgrad (before the first step)");
   SETDEV(c);
   if (c->iout) {   // report a failure of the previous write before starting the next
     iout_join(c->iout);

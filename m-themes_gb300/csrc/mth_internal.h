@@ -335,6 +335,12 @@ cudaError_t launch_local_solve_noalloc(const NewtonConst& nc, long long n, doubl
 // field planes (6 LT planes when sym, else nc planes) -> voxel-major doubles
 cudaError_t launch_to_host_layout(int mixed, const void* src, long long P, int nc, int sym, double* dst,
                                   cudaStream_t st);
+// DisGrad = strain planes (6 LT) + antisymmetric planes (W21, W02, W10) -> voxel-major 3x3 doubles
+cudaError_t launch_disgrad_to_host(int mixed, const void* strain, const void* skew, long long P, double* dst,
+                                   cudaStream_t st);
+// skew += u + wspin per voxel, (W21, W02, W10) planes
+cudaError_t launch_disgrad_skew(int mixed, const void* wspin, void* skew, long long P, const double u[3],
+                                cudaStream_t st);
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, int width, double* out, const IterIn& it,
                                    cudaStream_t st);
 

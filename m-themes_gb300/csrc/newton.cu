@@ -1381,27 +1381,89 @@ cudaError_t launch_setup(int mixed, const NewtonConst& nc, const void* fields, c
 // (the products and left-to-right sums of the host conversion, with
 // rounded, uncontracted operations, so both give the same doubles); other
 // fields are interleaved per voxel.
+// the symmetric tensor of voxel v's 6 LT planes, row-major into o[9]
+template <typename TSt>
+__device__ __forceinline__ void sym_to_host(const TSt* __restrict__ src, long long P, long long v, double* o) {
+  double a[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) a[i] = (double)src[i * P + v];
+  const double r2 = RSQ2, r3 = RSQ3, r6 = RSQ6;
+  const double t00 = __dadd_rn(__dadd_rn(__dmul_rn(a[0], -r2), __dmul_rn(a[1], -r6)), __dmul_rn(a[5], r3));
+  const double t11 = __dadd_rn(__dadd_rn(__dmul_rn(a[0], r2), __dmul_rn(a[1], -r6)), __dmul_rn(a[5], r3));
+  const double t22 = __dadd_rn(__dmul_rn(a[1], 2. * r6), __dmul_rn(a[5], r3));
+  const double t12 = __dmul_rn(a[2], r2), t02 = __dmul_rn(a[3], r2), t01 = __dmul_rn(a[4], r2);
+  o[0] = t00; o[1] = t01; o[2] = t02;
+  o[3] = t01; o[4] = t11; o[5] = t12;
+  o[6] = t02; o[7] = t12; o[8] = t22;
+}
+
 template <typename TSt>
 __global__ void to_host_layout_kernel(const TSt* __restrict__ src, long long P, int nc, int sym,
                                       double* __restrict__ dst) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= P) return;
   if (sym) {
-    double a[6];
-#pragma unroll
-    for (int i = 0; i < 6; i++) a[i] = (double)src[i * P + v];
-    const double r2 = RSQ2, r3 = RSQ3, r6 = RSQ6;
-    const double t00 = __dadd_rn(__dadd_rn(__dmul_rn(a[0], -r2), __dmul_rn(a[1], -r6)), __dmul_rn(a[5], r3));
-    const double t11 = __dadd_rn(__dadd_rn(__dmul_rn(a[0], r2), __dmul_rn(a[1], -r6)), __dmul_rn(a[5], r3));
-    const double t22 = __dadd_rn(__dmul_rn(a[1], 2. * r6), __dmul_rn(a[5], r3));
-    const double t12 = __dmul_rn(a[2], r2), t02 = __dmul_rn(a[3], r2), t01 = __dmul_rn(a[4], r2);
-    double* o = dst + 9 * v;
-    o[0] = t00; o[1] = t01; o[2] = t02;
-    o[3] = t01; o[4] = t11; o[5] = t12;
-    o[6] = t02; o[7] = t12; o[8] = t22;
+    sym_to_host(src, P, v, dst + 9 * v);
   } else {
     for (int i = 0; i < nc; i++) dst[nc * v + i] = (double)src[i * P + v];
   }
+}
+
+// DisGrad for the host: the symmetric part from the strain planes plus the
+// antisymmetric part W, held as the planes (W21, W02, W10)
+template <typename TSt>
+__global__ void disgrad_to_host_kernel(const TSt* __restrict__ strain, const TSt* __restrict__ skew, long long P,
+                                       double* __restrict__ dst) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= P) return;
+  double* o = dst + 9 * v;
+  sym_to_host(strain, P, v, o);
+  const double w21 = (double)skew[v], w02 = (double)skew[P + v], w10 = (double)skew[2 * P + v];
+  o[1] = __dsub_rn(o[1], w10);
+  o[3] = __dadd_rn(o[3], w10);
+  o[2] = __dadd_rn(o[2], w02);
+  o[6] = __dsub_rn(o[6], w02);
+  o[5] = __dsub_rn(o[5], w21);
+  o[7] = __dadd_rn(o[7], w21);
+}
+
+cudaError_t launch_disgrad_to_host(int mixed, const void* strain, const void* skew, long long P, double* dst,
+                                   cudaStream_t st) {
+  const int nb = (int)((P + 255) / 256);
+  if (mixed)
+    disgrad_to_host_kernel<float><<<nb, 256, 0, st>>>(static_cast<const float*>(strain),
+                                                       static_cast<const float*>(skew), P, dst);
+  else
+    disgrad_to_host_kernel<double><<<nb, 256, 0, st>>>(static_cast<const double*>(strain),
+                                                        static_cast<const double*>(skew), P, dst);
+  return cudaGetLastError();
+}
+
+// The antisymmetric part of DisGrad grows each step by that of its uniform
+// increments (Udot dt at the step's start, the dDisGradAvg corrections
+// before each iteration), u, and by that of the Gamma : sigma-hat terms added
+// at src/evolution.c:1401, which the Green passes accumulate and the spin
+// transform brings to wspin.  skew += u + wspin, all as (W21, W02, W10).
+template <typename TSt>
+__global__ void disgrad_skew_kernel(const TSt* __restrict__ wspin, TSt* __restrict__ skew, long long P, double u0,
+                                    double u1, double u2) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= P) return;
+  const double u[3] = {u0, u1, u2};
+#pragma unroll
+  for (int c = 0; c < 3; c++) skew[c * P + v] = (TSt)((double)skew[c * P + v] + (u[c] + (double)wspin[c * P + v]));
+}
+
+cudaError_t launch_disgrad_skew(int mixed, const void* wspin, void* skew, long long P, const double u[3],
+                                cudaStream_t st) {
+  const int nb = (int)((P + 255) / 256);
+  if (mixed)
+    disgrad_skew_kernel<float><<<nb, 256, 0, st>>>(static_cast<const float*>(wspin), static_cast<float*>(skew), P,
+                                                    u[0], u[1], u[2]);
+  else
+    disgrad_skew_kernel<double><<<nb, 256, 0, st>>>(static_cast<const double*>(wspin), static_cast<double*>(skew),
+                                                     P, u[0], u[1], u[2]);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_to_host_layout(int mixed, const void* src, long long P, int nc, int sym, double* dst,

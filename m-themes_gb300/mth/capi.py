@@ -24,8 +24,8 @@ MTH_MIXED_FAST = 2
 MTH_MIXED_ROOT64 = 3
 
 FIELD = {"sig": 0, "eps": 1, "edot": 2, "strain": 3, "rot": 4, "crss": 5, "gamacum": 6, "grain": 7, "rho": 8,
-         "rho_ssd": 9, "rho_gnd": 10}
-FIELD_NCOMP = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 1, 7: 1, 8: 1, 9: 12, 10: 36}
+         "rho_ssd": 9, "rho_gnd": 10, "disgrad": 11}
+FIELD_NCOMP = {0: 9, 1: 9, 2: 9, 3: 9, 4: 9, 5: 12, 6: 1, 7: 1, 8: 1, 9: 12, 10: 36, 11: 9}
 
 STATUS = {0: "MTH_OK", 1: "MTH_ERR_ARG", 2: "MTH_ERR_CUDA", 3: "MTH_ERR_NOMEM", 4: "MTH_ERR_SINGULAR",
           5: "MTH_ERR_NOT_CONVERGED", 6: "MTH_ERR_IO", 7: "MTH_ERR_STATE", 8: "MTH_ERR_TIMEOUT",
@@ -187,7 +187,7 @@ def _iptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
-IOUT = {"sig": 0, "eps": 1, "edot": 2, "els": 3, "grain": 4, "texture": 5}
+IOUT = {"sig": 0, "eps": 1, "edot": 2, "els": 3, "grain": 4, "texture": 5, "disgrad": 6}
 
 
 class MthError(RuntimeError):
@@ -213,6 +213,7 @@ def load(path: str | None = None):
                                               C.POINTER(C.c_double), C.c_size_t]
     lib.mth_step.argtypes = [C.c_void_p, C.POINTER(MthStepReport)]
     lib.mth_download_field.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t]
+    lib.mth_track_disgrad.argtypes = [C.c_void_p, C.c_int]
     lib.mth_destroy.argtypes = [C.c_void_p]
     lib.mth_local_solve.argtypes = [C.POINTER(MthParams), C.POINTER(C.c_double), C.c_size_t,
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),

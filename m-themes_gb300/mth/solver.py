@@ -40,6 +40,11 @@ class Solver:
         capi.check(self.lib, self.lib.mth_download_field(self.ctx, f, capi._dptr(out), out.size))
         return out.reshape(self.nv, -1)
 
+    def track_disgrad(self, on: bool = True):
+        """Keep the full displacement gradient (field "disgrad", iout kind
+        "disgrad"); before the first step (mth_track_disgrad)."""
+        capi.check(self.lib, self.lib.mth_track_disgrad(self.ctx, 1 if on else 0))
+
     def write_iout(self, kind: str, prefix: str, step: int):
         """Start writing a field in the reference's .iout format (mth_write_iout);
         the files are complete after wait_iout()."""

@@ -1502,6 +1502,7 @@ int orc_get_field(orc_ctx* c, int field, double* out) {
           out[9 * v + 3 * i + j] = (c->disgrad[v][i][j] + c->disgrad[v][j][i]) / 2.0;
         break;
       case MTH_FIELD_ROT: memcpy(out + 9 * v, c->tranmat[v], sizeof(t33)); break;
+      case MTH_FIELD_DISGRAD: memcpy(out + 9 * v, c->disgrad[v], sizeof(t33)); break;   /* DisGrad as kept */
       case MTH_FIELD_CRSS:
         for (int i = 0; i < NS; i++) out[NS * v + i] = c->crss[v][i][0];
         break;

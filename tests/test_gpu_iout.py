@@ -74,6 +74,47 @@ def test_iout_files(tmp_path, precision):
     s.close()
 
 
+@pytest.mark.parametrize("precision", [capi.MTH_FP64, capi.MTH_MIXED])
+def test_iout_disgrad(tmp_path, precision):
+    """WriteDisgradMPI's files (src/io.c:283-320): entries 11, 22, 33, 23,
+    13, 12 of the full displacement gradient, whose off-diagonal pairs differ
+    by the local rotation, against the downloaded field."""
+    from mth import Solver
+    cfg = synth.Config(cell_dim=(16, 8, 12), n_grains=5, n_pores=1, pore_radius=2, n_steps=2, seed=61, iter_max=15)
+    s = Solver(capi.params_from_config(cfg, precision=precision), *synth.microstructure(cfg))
+    s.track_disgrad()
+    for _ in range(cfg.n_steps):
+        s.step()
+    nv = 16 * 8 * 12
+    pre = str(tmp_path / "disg")
+    s.write_iout("disgrad", pre, 2)
+    s.wait_iout()
+    dg = s.field("disgrad").reshape(nv, 3, 3)
+    got = _components(pre, 2, nv)
+    for c, (i, j) in enumerate(COMP):
+        np.testing.assert_allclose(got[:, c], dg[:, i, j], rtol=1e-12, atol=1e-15)
+    strain = s.field("strain").reshape(nv, 3, 3)
+    np.testing.assert_allclose(0.5 * (dg + dg.transpose(0, 2, 1)), strain, rtol=1e-12, atol=1e-15)
+    w = 0.5 * (dg - dg.transpose(0, 2, 1))
+    assert np.abs(w).max() > 1e-2 * np.abs(dg).max()
+    assert sorted(os.listdir(tmp_path)) == [f"disg_{c}_S000002.iout" for c in range(1, 7)]
+    s.close()
+
+
+def test_disgrad_needs_tracking(tmp_path):
+    """Without mth_track_disgrad the full gradient is not kept: its download
+    and its files are refused, and tracking cannot start after a step."""
+    cfg = synth.Config(cell_dim=(8, 8, 8), n_grains=2, n_steps=1, seed=63, iter_max=5)
+    s, _ = run_gpu(cfg)
+    with pytest.raises(capi.MthError):
+        s.field("disgrad")
+    with pytest.raises(capi.MthError):
+        s.write_iout("disgrad", str(tmp_path / "d"), 0)
+    with pytest.raises(capi.MthError):
+        s.track_disgrad()
+    s.close()
+
+
 def test_iout_overlaps_next_step(tmp_path):
     """The snapshot is taken at the call: files hold the state before the
     step that runs while they are written."""

@@ -55,6 +55,31 @@ def test_fp64_matches_reference(name):
     s.close()
 
 
+@pytest.mark.parametrize("name,precision", [("g8_poly", capi.MTH_FP64), ("g8_shear", capi.MTH_FP64),
+                                            ("g12_radix3", capi.MTH_FP64), ("g8_shear", capi.MTH_MIXED)])
+def test_disgrad_matches_reference(name, precision):
+    """The full displacement gradient DisGrad (mth_track_disgrad): the strain
+    planes' symmetric part plus the antisymmetric part accumulated step by
+    step, against the reference's own field, whose antisymmetric part (the
+    local rotation) varies from voxel to voxel; stress-controlled shear
+    (g8_shear) adds a uniform one through the dDisGradAvg corrections."""
+    from mth import Solver
+    cfg, _, fields = load_golden(name)
+    s = Solver(capi.params_from_config(cfg, precision=precision), *synth.microstructure(cfg))
+    s.track_disgrad()
+    for _ in range(cfg.n_steps):
+        s.step()
+    tol = FP64_FIELD if precision == capi.MTH_FP64 else 1e-4
+    ref = fields["disgrad"].reshape(-1, 3, 3)
+    got = s.field("disgrad").reshape(-1, 3, 3)
+    assert rel_l2(got, ref) < tol
+    w_ref = 0.5 * (ref - ref.transpose(0, 2, 1))
+    w_got = 0.5 * (got - got.transpose(0, 2, 1))
+    assert np.abs(w_ref - w_ref.mean(0)).max() > 0.1 * np.abs(w_ref).max()
+    assert rel_l2(w_got, w_ref) < 10 * tol
+    s.close()
+
+
 @pytest.mark.parametrize("precision", [capi.MTH_MIXED, capi.MTH_MIXED_FAST, capi.MTH_MIXED_ROOT64])
 @pytest.mark.parametrize("name", ["g8_poly", "g12_radix3", "g16_pores", "g8_shear"])
 def test_mixed_within_tolerance(name, precision):

@@ -35,6 +35,9 @@ def test_oracle_matches_reference_trace(name):
         dg = fields["disgrad"].reshape(-1, 3, 3)
         strain = 0.5 * (dg + dg.transpose(0, 2, 1))
         assert rel(o.field("strain"), strain.reshape(-1, 9)) < 1e-10
+        # the full displacement gradient, whose antisymmetric part (the local
+        # rotation) varies from voxel to voxel
+        assert rel(o.field("disgrad"), dg.reshape(-1, 9)) < 1e-10
     assert o.second_backtracks() == 0
 
 
