@@ -124,6 +124,7 @@ def test_batch_argument_checks(lib):
 def test_iout_argument_checks(lib):
     assert lib.mth_write_iout(None, 0, b"x", 0) == 1
     assert lib.mth_iout_wait(None) == 1
+    assert lib.mth_track_disgrad(None, 1) == 1
 
 
 def test_namelist_dislocation_density_block(lib, tmp_path):
