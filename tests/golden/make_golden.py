@@ -181,6 +181,29 @@ def main_configs():
     print("fp64_32cube_trace", trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
 
 
+# The 128^3 benchmark workload at its stated grid (512 grains, 40 radius-3
+# pores as the gas phase), 2 steps of 5 Green iterations: the trace plus a
+# summary of the final stress field (column norms, 64 sampled voxels).
+def main_rve128():
+    ref = os.path.join(REPO, "oracle", "_ref", "forge_ref")
+    cfg = synth.workload("rve128")
+    cfg = dataclasses.replace(cfg, n_steps=2, iter_max=5)
+    d = "/tmp/mth_golden_rve128"
+    import shutil
+    shutil.rmtree(d, ignore_errors=True)
+    synth.write_case(d, cfg)
+    env = dict(os.environ, MTH_REF_TRACE=os.path.join(d, "trace.txt"), MTH_REF_DUMP=d, MTH_REF_SEED="1")
+    subprocess.run(["bash", "-c", f"ulimit -s unlimited; {ref} input.in > ref.log 2>&1"], cwd=d, env=env, check=True)
+    trace = np.atleast_2d(np.loadtxt(os.path.join(d, "trace.txt")))
+    nv = int(np.prod(cfg.cell_dim))
+    sig = np.fromfile(os.path.join(d, "sig.bin")).reshape(nv, 9)
+    samples = np.arange(0, nv, nv // 64)
+    out = os.path.join(HERE, "rve128_2x5_trace.npz")
+    np.savez_compressed(out, config=cfg_to_json(cfg), trace=trace, sig_norm=np.linalg.norm(sig, axis=0),
+                        sample_voxels=samples, sig_sample=sig[samples])
+    print("rve128_2x5_trace", trace.shape, "iters", trace[:, 1].astype(int).tolist(), "->", os.path.relpath(out, REPO))
+
+
 # The reference's own field files: with PrintControl 1 it writes, at the end
 # of step 0, the elastic strain and the stress (WriteElsMPI "els",
 # WriteSigMPI "sig_afterDRX", src/evolution.c:1632-1652, src/io.c:322-437)
@@ -354,7 +377,7 @@ def _rand_rot(rng):
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "configs", "iout"]
+    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "configs", "rve128", "iout"]
     if "evp" in which:
         main()
     if "dd" in which:
@@ -365,5 +388,7 @@ if __name__ == "__main__":
         main_drx()
     if "configs" in which:
         main_configs()
+    if "rve128" in which:
+        main_rve128()
     if "iout" in which:
         main_iout()

@@ -90,3 +90,36 @@ def test_oracle_matches_reference_at_32cube_size():
     sig = o.field("sig")
     assert rel(np.linalg.norm(sig, axis=0), z["sig_norm"]) < 1e-10
     assert rel(sig[z["sample_voxels"]], z["sig_sample"]) < 1e-9
+
+
+def test_oracle_matches_reference_at_128cube_benchmark_grid():
+    """The 128^3 benchmark workload on its stated grid (512 grains, 40
+    radius-3 pores as the gas phase), 2 steps of 5 Green iterations, against
+    the reference's own run: per-step trace and a summary of the final stress
+    field.  tests/test_gpu_configs.py holds the GPU to the oracle on the same
+    case in FP64 and mixed precision."""
+    import json
+    import os
+    from helpers import GOLDEN
+    from mth import synth
+    z = np.load(os.path.join(GOLDEN, "rve128_2x5_trace.npz"))
+    d = json.loads(str(z["config"]))
+    d["material"] = synth.Material(**d["material"])
+    for k in ("cell_dim", "velgrad_bc_flag", "velgrad_bc", "stress_bc_flag", "stress_bc"):
+        d[k] = tuple(d[k])
+    cfg = synth.Config(**d)
+    ref = synth.workload("rve128")
+    assert (cfg.cell_dim, cfg.n_grains, cfg.n_pores, cfg.seed) == (ref.cell_dim, ref.n_grains, ref.n_pores, ref.seed)
+    o, reps = run_oracle(cfg, nthreads=os.cpu_count() or 4)
+    trace = z["trace"]
+    for s, r in enumerate(reps):
+        row = trace[s]
+        assert r["iterations"] == int(row[T_ITER]) == 5
+        assert rel(r["sig_avg"], row[T_SIG].reshape(3, 3)) < 1e-10
+        assert rel(r["disgrad_avg"], row[T_DG].reshape(3, 3)) < 1e-10
+        assert abs(r["s_vm"] - row[T_SVM]) <= 1e-10 * abs(row[T_SVM])
+        assert abs(r["err_s"] - row[T_ERRS]) <= 1e-6 * abs(row[T_ERRS])
+    sig = o.field("sig")
+    assert rel(np.linalg.norm(sig, axis=0), z["sig_norm"]) < 1e-10
+    assert rel(sig[z["sample_voxels"]], z["sig_sample"]) < 1e-9
+    o.close()
