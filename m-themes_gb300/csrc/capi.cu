@@ -1499,9 +1499,15 @@ extern "C" mth_status mth_track_disgrad(mth_ctx* c, int on) {
     return set_err(MTH_ERR_STATE, "mth_track_disgrad after mth_upload_microstructure and before the first step");
   if (c->skew_d) return MTH_OK;
   const size_t bytes = 3 * (c->mixed ? sizeof(float) : sizeof(double)) * (size_t)c->nv;
-  CK(cudaMalloc(&c->skew_d, bytes));
-  CK(cudaMemsetAsync(c->skew_d, 0, bytes, c->st));
-  CK(cudaStreamSynchronize(c->st));
+  void* planes = nullptr;
+  CK(cudaMalloc(&planes, bytes));
+  cudaError_t e = cudaMemsetAsync(planes, 0, bytes, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) {
+    cudaFree(planes);
+    return set_err(MTH_ERR_CUDA, "clearing the DisGrad planes failed: %s", cudaGetErrorString(e));
+  }
+  c->skew_d = planes;   // kept only once cleared
   return MTH_OK;
 }
 
