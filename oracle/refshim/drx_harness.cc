@@ -16,6 +16,12 @@
  *   drx_ref interp IN OUT   InterpolateGrid (src/integrated.c:674-760):
  *                           grain ids by TrilinearInterpolationINT, rho_tot
  *                           by TrilinearInterpolation onto CellDim_pf
+ *   drx_ref upd    IN OUT   Update_microstructure (src/integrated.c:801-1807)
+ *                           on the mechanical grid, over a sequence of
+ *                           relaxed grain maps: the grain map and the
+ *                           membership counters gID_rex and growth after
+ *                           each call (growth == 1 marks the voxels
+ *                           src/evolution.c:1132-1145 resets)
  *
  * IN/OUT are flat little-endian binaries whose layout is written next to
  * each mode below (tests/golden/make_golden.py writes and reads them).
@@ -187,9 +193,64 @@ static int run_interp(FILE* in) {
   return 0;
 }
 
+/* IN:  int32 dims[3], n_ids, n_calls; int32 ids[n_ids] (gID_list);
+ *      int32 grain[N], gid_rex[N], growth[N] (state before the first call);
+ *      n_calls x {int32 paint[N]; int32 gID_new[N]}: before each call the
+ *      voxels with paint != 0 take that id and gID_rex = 1, as the nuclei
+ *      NucleationCheckDRX paints (src/integrated.c:397-404)
+ * OUT: n_calls x {int32 grain[N]; int32 gid_rex[N]; int32 growth[N]} */
+static int run_upd(FILE* in) {
+  std::vector<int> h = rd<int>(in, 5);
+  CellDim[0] = h[0]; CellDim[1] = h[1]; CellDim[2] = h[2];
+  const int n_ids = h[3], n_calls = h[4];
+  const size_t n = (size_t)h[0] * h[1] * h[2];
+  Nxyz = (int)n; lnx = h[0]; lxs = 0; lsize = (int)n; mpirank = 0; NumPE = 1;
+  DRX_Interpolation_Flag = 0;
+  std::vector<int> ids = rd<int>(in, (size_t)n_ids);
+  std::vector<int> grain = rd<int>(in, n), rex = rd<int>(in, n), grow = rd<int>(in, n);
+  std::vector<int> gnew(n), gfn(n);
+  grain_f = grain.data();
+  gID_rex = rex.data();
+  growth = grow.data();
+  gID_new = gnew.data();
+  grain_f_new = gfn.data();
+  GB_type = (int*)calloc(n, sizeof(int));
+  int** chk[3];
+  for (int a = 0; a < 3; a++) {
+    AllocMem(chk[a], n, int*);
+    for (size_t v = 0; v < n; v++) chk[a][v] = (int*)calloc(2, sizeof(int));
+  }
+  GB_checkX = chk[0]; GB_checkY = chk[1]; GB_checkZ = chk[2];
+  const size_t plane = (size_t)h[1] * h[2];
+  local_pxpG_send = (int*)calloc(plane, sizeof(int));
+  local_pxmG_send = (int*)calloc(plane, sizeof(int));
+  local_pxpG_recv = (int*)calloc(plane, sizeof(int));
+  local_pxmG_recv = (int*)calloc(plane, sizeof(int));
+  gID_list.clear();
+  for (int k = 0; k < n_ids; k++) {
+    G_Info e = {ids[k], 0.0, 0.0, 0.0};
+    gID_list.push_back(e);
+  }
+  for (int call = 0; call < n_calls; call++) {
+    std::vector<int> paint = rd<int>(in, n);
+    for (size_t v = 0; v < n; v++)
+      if (paint[v] != 0) {
+        grain_f[v] = paint[v];
+        gID_rex[v] = 1;
+      }
+    std::vector<int> g = rd<int>(in, n);
+    memcpy(gID_new, g.data(), sizeof(int) * n);
+    Update_microstructure();
+    wr(grain_f, n);
+    wr(gID_rex, n);
+    wr(growth, n);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc != 4) {
-    fprintf(stderr, "usage: drx_ref pf|nucl|interp IN OUT\n");
+    fprintf(stderr, "usage: drx_ref pf|nucl|interp|upd IN OUT\n");
     return 2;
   }
   FILE* in = fopen(argv[2], "rb");
@@ -202,6 +263,7 @@ int main(int argc, char** argv) {
   if (!strcmp(argv[1], "pf")) rc = run_pf(in);
   else if (!strcmp(argv[1], "nucl")) rc = run_nucl(in);
   else if (!strcmp(argv[1], "interp")) rc = run_interp(in);
+  else if (!strcmp(argv[1], "upd")) rc = run_upd(in);
   fclose(in);
   fclose(g_out);
   return rc;

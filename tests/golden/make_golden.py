@@ -367,6 +367,69 @@ def main_drx():
         print(name, ns, "->", nd, "->", os.path.relpath(out, REPO))
 
 
+# Update_microstructure (src/integrated.c:801-1807) over crafted sequences of
+# relaxed grain maps on a 10^3 grid of three deformed x slabs (ids 1-3,
+# init_gid 3): the grain map and the membership counters after each call.
+# The reference resets the voxels whose counter `growth` is 1 after the call
+# (src/evolution.c:1132-1145).
+def upd_sequences():
+    dims = (10, 10, 10)
+    X, Y, Z = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    base = np.where(X < 4, 1, np.where(X < 7, 2, 3)).astype(np.int32).ravel()
+
+    def box(x0, x1, y0, y1, z0, z1):
+        return ((X >= x0) & (X < x1) & (Y >= y0) & (Y < y1) & (Z >= z0) & (Z < z1)).ravel()
+
+    zero = np.zeros(base.size, np.int32)
+    seq = {}
+    # one recrystallised grain: painted, grows, grows by 16 %, by one voxel
+    # (under 1 %: rolled back), then by 19 voxels
+    paint = np.where(box(2, 5, 4, 7, 4, 7), 4, 0).astype(np.int32)
+    g0 = np.where(box(1, 6, 3, 8, 3, 8), 4, base).astype(np.int32)
+    g1 = np.where(box(1, 6, 3, 8, 3, 9), 4, g0).astype(np.int32)
+    g2 = g1.copy()
+    g2[np.flatnonzero((g1 != 4) & box(6, 7, 3, 4, 3, 4))[:1]] = 4
+    g3 = np.where(box(6, 7, 3, 8, 3, 7), 4, g2).astype(np.int32)
+    seq["upd_growth_rollback"] = ([1, 2, 3, 4], [(paint, g0), (zero, g1), (zero, g2), (zero, g3)])
+    # two recrystallised grains: voxels of the older (4) go to the younger
+    # (5), voxels of the younger go to the older, and some go back to a
+    # deformed grain
+    p4 = np.where(box(1, 3, 1, 3, 1, 3), 4, 0)
+    p5 = np.where(box(6, 8, 6, 8, 6, 8), 5, 0)
+    paint = (p4 + p5).astype(np.int32)
+    h0 = np.where(box(0, 4, 0, 4, 0, 4), 4, np.where(box(5, 9, 5, 9, 5, 9), 5, base)).astype(np.int32)
+    h1 = h0.copy()
+    h1[box(3, 4, 0, 4, 0, 4)] = 5          # older -> younger
+    h1[box(5, 6, 5, 9, 5, 9)] = 4          # younger -> older
+    h1[box(0, 1, 0, 4, 0, 1)] = 1          # recrystallised -> deformed
+    h2 = np.where(box(0, 4, 4, 6, 0, 4), 4, h1).astype(np.int32)
+    seq["upd_two_grains"] = ([1, 2, 3, 4, 5], [(paint, h0), (zero, h1), (zero, h2)])
+    return dims, base, seq
+
+
+def main_upd():
+    exe = os.path.join(REPO, "oracle", "_ref", "drx_ref")
+    d = "/tmp/mth_golden_upd"
+    os.makedirs(d, exist_ok=True)
+    dims, base, seq = upd_sequences()
+    n = int(np.prod(dims))
+    for name, (ids, calls) in seq.items():
+        blob = np.array([*dims, len(ids), len(calls)], np.int32).tobytes() + np.array(ids, np.int32).tobytes()
+        blob += base.tobytes() + np.zeros(n, np.int32).tobytes() + np.zeros(n, np.int32).tobytes()
+        for paint, gnew in calls:
+            blob += paint.astype(np.int32).tobytes() + gnew.astype(np.int32).tobytes()
+        fin, fout = os.path.join(d, name + ".in"), os.path.join(d, name + ".out")
+        open(fin, "wb").write(blob)
+        subprocess.check_call([exe, "upd", fin, fout], stdout=subprocess.DEVNULL)
+        out = np.fromfile(fout, np.int32).reshape(len(calls), 3, n)
+        dst = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(dst, dims=np.array(dims), ids=np.array(ids), base=base,
+                            paint=np.stack([c[0] for c in calls]), gnew=np.stack([c[1] for c in calls]),
+                            grain=out[:, 0], gid_rex=out[:, 1], growth=out[:, 2])
+        print(name, "reset per call", [(out[k, 2] == 1).sum() for k in range(len(calls))], "->",
+              os.path.relpath(dst, REPO))
+
+
 def _rand_rot(rng):
     q = rng.normal(size=4)
     q /= np.linalg.norm(q)
@@ -377,7 +440,7 @@ def _rand_rot(rng):
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "configs", "rve128", "iout"]
+    which = sys.argv[1:] or ["evp", "dd", "test_run", "drx", "upd", "configs", "rve128", "iout"]
     if "evp" in which:
         main()
     if "dd" in which:
@@ -386,6 +449,8 @@ if __name__ == "__main__":
         main_test_run()
     if "drx" in which:
         main_drx()
+    if "upd" in which:
+        main_upd()
     if "configs" in which:
         main_configs()
     if "rve128" in which:

@@ -286,3 +286,50 @@ def test_slowly_growing_grains_reset_no_joining_voxel():
             prev, rot_prev = cur, rot
         o.close()
     assert kept > 0 and reset > 0
+
+
+def build_resets(prev, cur, first_drx_id):
+    """The voxels the coupled step resets (orc_drx_step in
+    oracle/evpfft_oracle.c, drx_count_kernel and drx_update_kernel in
+    drx.cu): those whose grain changed in the step to a recrystallised one,
+    unless that grain's joining voxels are under 1 % of its voxels."""
+    joined = (cur != prev) & (cur >= first_drx_id)
+    reset = np.zeros(cur.shape, bool)
+    for gid, tot, nj in joined_fractions(prev, cur, first_drx_id):
+        if nj * 100 // tot != 0:
+            reset |= joined & (cur == gid)
+    return reset
+
+
+@pytest.mark.parametrize("name", ["upd_growth_rollback", "upd_two_grains"])
+def test_reset_rule_against_update_microstructure(name):
+    """The reference's own Update_microstructure (src/integrated.c:801-1807),
+    run by the harness on crafted sequences of nuclei and relaxed grain
+    maps, marks with growth == 1 the voxels src/evolution.c:1132-1145 resets.
+    The build's rule gives the same voxels on every call but two, which
+    this test pins: after a rolled-back step the reference drops the grain
+    from its membership and resets none of its later joining voxels, where
+    the build resets them once they are 1 % of the grain; and voxels moving
+    from a recrystallised grain to a younger one keep their counter running
+    in the reference (no reset), where the build resets them."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    first = int(np.max(z["base"])) + 1
+    prev = z["base"]
+    for k in range(len(z["gnew"])):
+        cur = z["gnew"][k]
+        assert np.array_equal(z["grain"][k], cur)   # the relaxed map is adopted
+        ref = z["growth"][k] == 1
+        ours = build_resets(prev, cur, first)
+        if name == "upd_growth_rollback" and k == 2:
+            assert not ref.any() and not ours.any()   # one joining voxel of 151: rolled back in both
+        if name == "upd_growth_rollback" and k == 3:
+            assert not ref.any() and ours.sum() == 19
+            assert np.array_equal(np.flatnonzero(ours), np.flatnonzero((cur == 4) & (prev != 4)))
+        elif name == "upd_two_grains" and k == 1:
+            older_to_younger = (prev == 4) & (cur == 5)
+            assert older_to_younger.sum() == 16 and not (ref & older_to_younger).any()
+            assert np.array_equal(ours & ~older_to_younger, ref) and (ours & older_to_younger).sum() == 16
+            assert ref[(prev == 5) & (cur == 4)].all()   # younger to older: reset in both
+        else:
+            assert np.array_equal(ours, ref), (name, k)
+        prev = cur
